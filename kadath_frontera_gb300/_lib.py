@@ -1,0 +1,136 @@
+"""ctypes binding of ``libkadath_gb300.so`` (the C ABI in include/kadath_gb300.h).
+
+The shared library is the product: every numeric call goes through it to
+CUDA kernels.  If it cannot be loaded this module raises -- there is no
+Python or CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = _HERE / "libkadath_gb300.so"
+
+KD_OK, KD_ERR_ARG, KD_ERR_CUDA, KD_ERR_SINGULAR, KD_ERR_NOCONV, KD_ERR_TIMEOUT, KD_ERR_UNSUPPORTED, KD_ERR_STATE = range(8)
+
+STATUS_NAMES = {0: "KD_OK", 1: "KD_ERR_ARG", 2: "KD_ERR_CUDA", 3: "KD_ERR_SINGULAR", 4: "KD_ERR_NOCONV",
+                5: "KD_ERR_TIMEOUT", 6: "KD_ERR_UNSUPPORTED", 7: "KD_ERR_STATE"}
+
+
+class KadathError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+class TransformDesc(C.Structure):
+    _fields_ = [("nbr_points", C.c_int * 3), ("nbr_coefs", C.c_int * 3), ("base_r", C.POINTER(C.c_int)),
+                ("base_t", C.POINTER(C.c_int)), ("base_p", C.c_int), ("batch", C.c_int),
+                ("in_", C.c_void_p), ("out", C.c_void_p)]
+
+
+_lib = None
+
+
+def load(build_if_missing: bool = True) -> C.CDLL:
+    """Loads the library (building it in-tree first if it is absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        if not build_if_missing:
+            raise KadathError(KD_ERR_STATE, f"{LIB_PATH} missing; run kadath_frontera_gb300.build.build()")
+        from . import build as _build
+        _build.build()
+    lib = C.CDLL(str(LIB_PATH))
+    _declare(lib)
+    _lib = lib
+    return lib
+
+
+def _declare(lib: C.CDLL) -> None:
+    P, I, D, V = C.c_void_p, C.c_int, C.c_double, None
+    IP, DP = C.POINTER(C.c_int), C.POINTER(C.c_double)
+    sig = {
+        "kd_ctx_create": (I, [C.POINTER(P), I]),
+        "kd_ctx_destroy": (I, [P]),
+        "kd_last_error": (C.c_char_p, [P]),
+        "kd_ctx_synchronize": (I, [P]),
+        "kd_ctx_launch_count": (C.c_longlong, [P]),
+        "kd_coef_many": (I, [P, I, C.POINTER(TransformDesc)]),
+        "kd_coef_i_many": (I, [P, I, C.POINTER(TransformDesc)]),
+        "kd_coef_host": (I, [P, C.POINTER(TransformDesc)]),
+        "kd_coef_i_host": (I, [P, C.POINTER(TransformDesc)]),
+        "kd_ope_1d": (I, [P, I, I, C.POINTER(TransformDesc), IP, IP, IP]),
+        "kd_matrix_1d": (I, [P, I, I, I, I, DP, IP]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _declare_more(lib)
+
+
+def _declare_more(lib: C.CDLL) -> None:
+    """Signatures of the system/solver entry points (added as they exist)."""
+    for name, (res, args) in EXTRA_SIGNATURES.items():
+        if hasattr(lib, name):
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+
+
+EXTRA_SIGNATURES: dict = {}
+
+
+def check(status: int, ctx=None) -> None:
+    if status != KD_OK:
+        msg = load().kd_last_error(ctx).decode() if ctx is not None else ""
+        raise KadathError(status, msg)
+
+
+class Context:
+    """Owns one kd_ctx (one GPU, one CUDA stream)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = C.c_void_p()
+        st = self.lib.kd_ctx_create(C.byref(h), device)
+        self.h = h
+        if st != KD_OK:
+            msg = self.lib.kd_last_error(h).decode() if h else ""
+            raise KadathError(st, f"cannot create GPU context on device {device}: {msg}")
+
+    def check(self, st: int) -> None:
+        if st != KD_OK:
+            raise KadathError(st, self.lib.kd_last_error(self.h).decode())
+
+    def synchronize(self) -> None:
+        self.check(self.lib.kd_ctx_synchronize(self.h))
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.kd_ctx_launch_count(self.h))
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.kd_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(int(os.environ.get("KD_DEVICE", "0")))
+    return _default_ctx

@@ -1,0 +1,151 @@
+#include "kd_context.hpp"
+
+#include <cstring>
+#include <sstream>
+
+namespace kd {
+
+void cuda_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    std::ostringstream os;
+    os << what << ": " << cudaGetErrorName(e) << " (" << cudaGetErrorString(e) << ")";
+    throw KdError(KD_ERR_CUDA, os.str());
+  }
+}
+
+DeviceArena::~DeviceArena() {
+  for (auto& c : chunks_) cudaFree(c.ptr);
+}
+
+void* DeviceArena::alloc_bytes(size_t n) {
+  n = (n + 255) & ~size_t(255);
+  if (n == 0) n = 256;
+  while (true) {
+    if (cur_chunk_ < chunks_.size()) {
+      if (off_ + n <= chunks_[cur_chunk_].size) {
+        void* p = chunks_[cur_chunk_].ptr + off_;
+        off_ += n;
+        return p;
+      }
+      cur_chunk_++;
+      off_ = 0;
+      continue;
+    }
+    size_t sz = n > chunk_ ? n : chunk_;
+    void* p = nullptr;
+    cuda_check(cudaMalloc(&p, sz), "cudaMalloc(arena chunk)");
+    chunks_.push_back({static_cast<char*>(p), sz});
+  }
+}
+
+double* DeviceArena::alloc_doubles(size_t n) {
+  return static_cast<double*>(alloc_bytes(n * sizeof(double)));
+}
+
+void DeviceArena::reset() {
+  cur_chunk_ = 0;
+  off_ = 0;
+}
+
+size_t DeviceArena::used() const {
+  size_t u = 0;
+  for (size_t i = 0; i < cur_chunk_ && i < chunks_.size(); i++) u += chunks_[i].size;
+  return u + off_;
+}
+
+size_t DeviceArena::mark() const { return (cur_chunk_ << 40) | off_; }
+
+void DeviceArena::release_to(size_t m) {
+  cur_chunk_ = m >> 40;
+  off_ = m & ((size_t(1) << 40) - 1);
+}
+
+Context::Context(int device) : device_(device) {
+  cuda_check(cudaSetDevice(device), "cudaSetDevice");
+  cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+  pool_cap_ = size_t(4) << 20;  // 4 Mi doubles = 32 MB of operator matrices
+  cuda_check(cudaMalloc(&d_pool_, pool_cap_ * sizeof(double)), "cudaMalloc(matrix pool)");
+}
+
+Context::~Context() {
+  cudaStreamSynchronize(stream_);
+  for (auto& kv : itables_) cudaFree(kv.second);
+  for (auto& kv : dtables_) cudaFree(kv.second);
+  cudaFree(d_pool_);
+  cudaStreamDestroy(stream_);
+}
+
+const double* Context::pool() {
+  size_t n = bank_.pool_size();
+  if (n > pool_uploaded_) {
+    if (capturing) throw KdError(KD_ERR_STATE, "matrix pool grew during graph capture");
+    if (n > pool_cap_) throw KdError(KD_ERR_ARG, "matrix pool capacity exceeded");
+    cuda_check(cudaMemcpyAsync(d_pool_ + pool_uploaded_, bank_.pool().data() + pool_uploaded_,
+                               (n - pool_uploaded_) * sizeof(double), cudaMemcpyHostToDevice, stream_),
+               "upload matrix pool");
+    cuda_check(cudaStreamSynchronize(stream_), "sync after pool upload");
+    pool_uploaded_ = n;
+  }
+  return d_pool_;
+}
+
+const int* Context::table(const std::vector<int>& content) {
+  auto it = itables_.find(content);
+  if (it != itables_.end()) return it->second;
+  if (capturing) throw KdError(KD_ERR_STATE, "new device table during graph capture");
+  int* p = nullptr;
+  size_t n = content.empty() ? 1 : content.size();
+  cuda_check(cudaMalloc(&p, n * sizeof(int)), "cudaMalloc(table)");
+  if (!content.empty())
+    cuda_check(cudaMemcpy(p, content.data(), content.size() * sizeof(int), cudaMemcpyHostToDevice),
+               "upload table");
+  itables_[content] = p;
+  return p;
+}
+
+const double* Context::dtable(const std::vector<double>& content) {
+  auto it = dtables_.find(content);
+  if (it != dtables_.end()) return it->second;
+  if (capturing) throw KdError(KD_ERR_STATE, "new device table during graph capture");
+  double* p = nullptr;
+  size_t n = content.empty() ? 1 : content.size();
+  cuda_check(cudaMalloc(&p, n * sizeof(double)), "cudaMalloc(dtable)");
+  if (!content.empty())
+    cuda_check(cudaMemcpy(p, content.data(), content.size() * sizeof(double), cudaMemcpyHostToDevice),
+               "upload dtable");
+  dtables_[content] = p;
+  return p;
+}
+
+void Context::run_items(const std::vector<KdItem>& items, const std::vector<int>& batches) {
+  const double* dp = pool();
+  size_t i = 0;
+  while (i < items.size()) {
+    KdItemList list;
+    std::memset(&list, 0, sizeof(list));
+    int smem = 0;
+    list.prefix[0] = 0;
+    int n = 0;
+    while (i < items.size() && n < KD_MAX_ITEMS) {
+      const KdItem& it = items[i];
+      list.items[n] = it;
+      list.prefix[n + 1] = list.prefix[n] + batches[i];
+      int d0 = it.n0, d1 = it.n1, d2 = it.n2;
+      int m = d0 * d1 * d2;
+      for (int q = 0; q < it.npass; q++) {
+        if (it.pass[q].dim == 0) d0 = it.pass[q].n_out;
+        if (it.pass[q].dim == 1) d1 = it.pass[q].n_out;
+        if (it.pass[q].dim == 2) d2 = it.pass[q].n_out;
+        if (d0 * d1 * d2 > m) m = d0 * d1 * d2;
+      }
+      if (m > smem) smem = m;
+      n++;
+      i++;
+    }
+    list.nitems = n;
+    cuda_check(launch_line_passes(list, smem, dp, stream_), "line_passes kernel");
+    launches++;
+  }
+}
+
+}  // namespace kd

@@ -1,0 +1,99 @@
+// Per-thread solver context: CUDA stream, FP64 matrix pool, device tables,
+// bump arenas for field storage, and error state.  One context drives one
+// GPU; the C ABI hands it out as an opaque kd_ctx*.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "kadath_gb300.h"  // status codes
+#include "kd_bases.hpp"
+#include "kd_device.hpp"
+
+namespace kd {
+
+struct KdError : std::runtime_error {
+  int code;
+  KdError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+void cuda_check(cudaError_t e, const char* what);
+
+// Bump allocator over large device chunks; reset() recycles everything.
+// Allocation order is deterministic, so a replayed sequence of allocations
+// returns the same addresses (needed for CUDA-graph replays).
+class DeviceArena {
+ public:
+  explicit DeviceArena(size_t chunk_bytes = size_t(256) << 20) : chunk_(chunk_bytes) {}
+  ~DeviceArena();
+  double* alloc_doubles(size_t n);
+  void* alloc_bytes(size_t n);
+  void reset();
+  size_t used() const;
+  size_t mark() const;          // current position (for scoped reuse)
+  void release_to(size_t mark);
+
+ private:
+  struct Chunk {
+    char* ptr;
+    size_t size;
+  };
+  std::vector<Chunk> chunks_;
+  size_t cur_chunk_ = 0, off_ = 0, chunk_;
+};
+
+class Context {
+ public:
+  explicit Context(int device);
+  ~Context();
+
+  int device() const { return device_; }
+  cudaStream_t stream() const { return stream_; }
+
+  MatrixBank& bank() { return bank_; }
+  // Makes sure every matrix in the bank is present in the device pool.
+  const double* pool();
+  // Device copy of an int table, cached by content.
+  const int* table(const std::vector<int>& content);
+  // Device copy of a double table, cached by content.
+  const double* dtable(const std::vector<double>& content);
+
+  DeviceArena& scratch() { return scratch_; }
+  DeviceArena& persistent() { return persistent_; }
+
+  // While a CUDA graph is being captured no host->device upload may happen;
+  // the first (uncaptured) evaluation fills every cache.
+  bool capturing = false;
+
+  std::string last_error;
+
+  // Packs items into launches of at most KD_MAX_ITEMS and runs them.
+  void run_items(const std::vector<KdItem>& items, const std::vector<int>& batches);
+
+  // Statistic: number of kernels this context launched.
+  long long launches = 0;
+
+ private:
+  int device_;
+  cudaStream_t stream_ = nullptr;
+  MatrixBank bank_;
+  double* d_pool_ = nullptr;
+  size_t pool_cap_ = 0, pool_uploaded_ = 0;
+  std::map<std::vector<int>, int*> itables_;
+  std::map<std::vector<double>, double*> dtables_;
+  DeviceArena scratch_;
+  DeviceArena persistent_{size_t(64) << 20};
+};
+
+// Builds the pass description of a 1-D operator along `dim` for a field of
+// current dims `dims` whose per-line bases are given by the basis table of
+// that dim.  Used by transforms and by coefficient-space operators.
+struct LinePassSpec {
+  int dim, n_in, n_out, mat_ld;
+  std::vector<int> offsets;  // per line, -1 for zero lines
+};
+
+}  // namespace kd

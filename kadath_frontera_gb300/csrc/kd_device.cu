@@ -1,0 +1,257 @@
+// FP64 kernels for the spectral layer: fused separable transforms (one CTA
+// per field, the field staged whole in shared memory), elementwise algebra
+// on collocation values, and the sparse gathers used by the tau/Galerkin
+// export.  All arithmetic is FP64, as in the reference.
+#include <cuda_runtime.h>
+
+#include "kd_device.hpp"
+
+namespace kd {
+
+namespace {
+
+__device__ __forceinline__ int line_matrix(const KdPass& p, int c1, int c2) {
+  if (p.dim == 0) return p.mat[c1 * p.mat_ld + c2];
+  if (p.dim == 1) return p.mat[c2];
+  return p.mat[0];
+}
+
+// One pass: X has dims (d0,d1,d2); Y has the pass dim replaced by n_out.
+__device__ void run_pass(const KdPass& p, const double* __restrict__ X, double* __restrict__ Y,
+                         int d0, int d1, int d2, const double* __restrict__ pool, double scale) {
+  int o0 = d0, o1 = d1, o2 = d2;
+  if (p.dim == 0) o0 = p.n_out;
+  if (p.dim == 1) o1 = p.n_out;
+  if (p.dim == 2) o2 = p.n_out;
+  const int total = o0 * o1 * o2;
+  const int nin = p.n_in;
+  for (int e = threadIdx.x; e < total; e += blockDim.x) {
+    int c2 = e % o2;
+    int t = e / o2;
+    int c1 = t % o1;
+    int c0 = t / o1;
+    int row, off, base, stride;
+    if (p.dim == 0) {
+      row = c0;
+      off = line_matrix(p, c1, c2);
+      base = c1 * d2 + c2;
+      stride = d1 * d2;
+    } else if (p.dim == 1) {
+      row = c1;
+      off = line_matrix(p, c0, c2);
+      base = c0 * d1 * d2 + c2;
+      stride = d2;
+    } else {
+      row = c2;
+      off = line_matrix(p, c0, c1);
+      base = (c0 * d1 + c1) * d2;
+      stride = 1;
+    }
+    double acc = 0.0;
+    if (off >= 0) {
+      const double* M = pool + off + static_cast<long long>(row) * nin;
+#pragma unroll 4
+      for (int q = 0; q < nin; q++) acc = fma(__ldg(M + q), X[base + q * stride], acc);
+    }
+    Y[e] = acc * scale;
+  }
+}
+
+__global__ void line_passes_kernel(const __grid_constant__ KdItemList list, const double* __restrict__ pool) {
+  extern __shared__ double smem[];
+  const int total_fields = list.prefix[list.nitems];
+  // Grid-stride over fields so that any grid size covers the work.
+  for (int f = blockIdx.x; f < total_fields; f += gridDim.x) {
+    int item = 0;
+    while (item + 1 < list.nitems && list.prefix[item + 1] <= f) item++;
+    const KdItem& it = list.items[item];
+    const int field_in_item = f - list.prefix[item];
+    const int n_in_elems = it.n0 * it.n1 * it.n2;
+    // Buffer sizes: every stage fits in half of the dynamic shared memory.
+    int d0 = it.n0, d1 = it.n1, d2 = it.n2;
+    int maxe = n_in_elems;
+    {
+      int e0 = d0, e1 = d1, e2 = d2;
+      for (int q = 0; q < it.npass; q++) {
+        if (it.pass[q].dim == 0) e0 = it.pass[q].n_out;
+        if (it.pass[q].dim == 1) e1 = it.pass[q].n_out;
+        if (it.pass[q].dim == 2) e2 = it.pass[q].n_out;
+        int e = e0 * e1 * e2;
+        if (e > maxe) maxe = e;
+      }
+    }
+    double* bufA = smem;
+    double* bufB = smem + maxe;
+    const double* src = it.in + static_cast<long long>(field_in_item) * it.in_stride;
+    double* dst = it.out + static_cast<long long>(field_in_item) * it.out_stride;
+    for (int e = threadIdx.x; e < n_in_elems; e += blockDim.x) bufA[e] = src[e];
+    __syncthreads();
+    double* X = bufA;
+    double* Y = bufB;
+    for (int q = 0; q < it.npass; q++) {
+      const KdPass& p = it.pass[q];
+      bool last = (q == it.npass - 1);
+      int o0 = d0, o1 = d1, o2 = d2;
+      if (p.dim == 0) o0 = p.n_out;
+      if (p.dim == 1) o1 = p.n_out;
+      if (p.dim == 2) o2 = p.n_out;
+      // The last pass writes straight to global memory.
+      run_pass(p, X, last ? dst : Y, d0, d1, d2, pool, last ? it.scale : 1.0);
+      __syncthreads();
+      d0 = o0;
+      d1 = o1;
+      d2 = o2;
+      double* tmp = X;
+      X = Y;
+      Y = tmp;
+    }
+    if (it.npass == 0) {
+      for (int e = threadIdx.x; e < n_in_elems; e += blockDim.x) dst[e] = bufA[e] * it.scale;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void ew_kernel(int op, long long npts, long long total, int ba, const double* __restrict__ a,
+                          int bb, const double* __restrict__ b, double* __restrict__ out, double alpha,
+                          double beta) {
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < total;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    long long p = i % npts;
+    double x = (a != nullptr) ? a[ba == 1 ? p : i] : 0.0;
+    double y = (b != nullptr) ? b[bb == 1 ? p : i] : 0.0;
+    double r;
+    switch (op) {
+      case EW_ADD: r = x + y; break;
+      case EW_SUB: r = x - y; break;
+      case EW_MUL: r = x * y; break;
+      case EW_DIV: r = x / y; break;
+      case EW_AXPBY: r = alpha * x + beta * y; break;
+      case EW_SCALE: r = alpha * x; break;
+      case EW_ADDC: r = x + alpha; break;
+      case EW_CSUB: r = alpha - x; break;
+      case EW_CDIV: r = alpha / x; break;
+      case EW_POWD: r = pow(x, alpha); break;
+      case EW_EXP: r = exp(x); break;
+      case EW_LOG: r = log(x); break;
+      case EW_SQRT: r = sqrt(x); break;
+      case EW_SIN: r = sin(x); break;
+      case EW_COS: r = cos(x); break;
+      case EW_NEG: r = -x; break;
+      case EW_FILL: r = alpha; break;
+      case EW_COPY: r = x; break;
+      case EW_POWI: r = pow(x, alpha); break;
+      case EW_ATAN: r = atan(x); break;
+      case EW_MULC_ADD: r = x * y * alpha; break;
+      default: r = 0.0; break;
+    }
+    out[i] = r;
+  }
+}
+
+__global__ void gather_rows_kernel(const double* __restrict__ in, long long in_stride, int batch, int nrows,
+                                   const int* __restrict__ idx4, const double* __restrict__ w4,
+                                   double* __restrict__ out, long long osf, long long osr, double alpha,
+                                   int accumulate) {
+  long long total = static_cast<long long>(batch) * nrows;
+  for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < total;
+       t += static_cast<long long>(gridDim.x) * blockDim.x) {
+    int r = static_cast<int>(t % nrows);
+    int f = static_cast<int>(t / nrows);
+    const double* src = in + f * in_stride;
+    double acc = 0.0;
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      int ix = idx4[4 * r + e];
+      if (ix >= 0) acc += w4[4 * r + e] * src[ix];
+    }
+    double* dst = out + f * osf + r * osr;
+    if (accumulate) *dst += alpha * acc; else *dst = alpha * acc;
+  }
+}
+
+__global__ void scatter_seeds_kernel(double* out, long long stride, int nent, const int* seed, const int* pos,
+                                     const double* w) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nent; e += gridDim.x * blockDim.x)
+    out[seed[e] * stride + pos[e]] = w[e];
+}
+
+__global__ void absmax_kernel(const double* __restrict__ x, long long n, double* out) {
+  __shared__ double red[32];
+  double m = 0.0;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x)
+    m = fmax(m, fabs(x[i]));
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    m = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (threadIdx.x == 0) {
+      // Non-negative doubles order like their bit patterns.
+      atomicMax(reinterpret_cast<unsigned long long*>(out), __double_as_longlong(m));
+    }
+  }
+}
+
+int grid_for(long long n, int threads) {
+  long long g = (n + threads - 1) / threads;
+  if (g < 1) g = 1;
+  if (g > 152 * 16) g = 152 * 16;
+  return static_cast<int>(g);
+}
+
+}  // namespace
+
+cudaError_t launch_line_passes(const KdItemList& list, int smem_doubles, const double* d_pool,
+                               cudaStream_t s) {
+  const int total_fields = list.prefix[list.nitems];
+  if (total_fields <= 0) return cudaSuccess;
+  size_t smem = static_cast<size_t>(smem_doubles) * 2 * sizeof(double);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(line_passes_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+  }
+  int grid = total_fields < 152 * 8 ? total_fields : 152 * 8;
+  line_passes_kernel<<<grid, 128, smem, s>>>(list, d_pool);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ew(int op, long long npts, int ba, const double* a, int bb, const double* b, double* out,
+                      double alpha, double beta, cudaStream_t s) {
+  int nf = ba > bb ? ba : bb;
+  if (nf < 1) nf = 1;
+  long long total = npts * nf;
+  if (total <= 0) return cudaSuccess;
+  ew_kernel<<<grid_for(total, 256), 256, 0, s>>>(op, npts, total, ba, a, bb, b, out, alpha, beta);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather_rows(const double* in, long long in_stride, int batch, int nrows, const int* idx4,
+                               const double* w4, double* out, long long osf, long long osr, double alpha,
+                               int accumulate, cudaStream_t s) {
+  long long total = static_cast<long long>(batch) * nrows;
+  if (total <= 0) return cudaSuccess;
+  gather_rows_kernel<<<grid_for(total, 256), 256, 0, s>>>(in, in_stride, batch, nrows, idx4, w4, out, osf, osr,
+                                                         alpha, accumulate);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_seeds(double* out, long long stride, int nent, const int* seed, const int* pos,
+                                 const double* w, cudaStream_t s) {
+  if (nent <= 0) return cudaSuccess;
+  scatter_seeds_kernel<<<grid_for(nent, 256), 256, 0, s>>>(out, stride, nent, seed, pos, w);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_absmax(const double* x, long long n, double* out_scalar, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(out_scalar, 0, sizeof(double), s);
+  if (e != cudaSuccess) return e;
+  if (n <= 0) return cudaSuccess;
+  absmax_kernel<<<grid_for(n, 256), 256, 0, s>>>(x, n, out_scalar);
+  return cudaGetLastError();
+}
+
+}  // namespace kd

@@ -1,0 +1,94 @@
+// Device-side descriptors and kernel launchers (implemented in kd_device.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace kd {
+
+// One 1-D pass of a separable operator over a 3-D block (r, theta, phi),
+// phi fastest.  The matrix applied to a line is looked up per line:
+//   dim 0 (r):     mat[j * mat_ld + k]   (basis depends on theta/phi indices)
+//   dim 1 (theta): mat[k]                (basis depends on the phi index)
+//   dim 2 (phi):   mat[0]
+// An entry < 0 means "this line's output is zero".  Offsets are in doubles
+// into the shared matrix pool; the matrix is row-major n_out x n_in.
+struct KdPass {
+  int dim;
+  int n_in;
+  int n_out;
+  int mat_ld;
+  const int* mat;
+};
+
+// A run of `batch` fields of identical shape processed by the same pass list.
+struct KdItem {
+  const double* in;
+  double* out;
+  long long in_stride;   // elements between consecutive fields of the batch
+  long long out_stride;
+  int n0, n1, n2;        // input dims
+  int npass;
+  double scale;          // applied to the final result
+  KdPass pass[3];
+};
+
+// Up to KD_MAX_ITEMS runs packed in one launch (uneven domains together).
+// Passed by value as a kernel parameter so that launches can be captured in
+// a CUDA graph without staging descriptors through host memory.
+constexpr int KD_MAX_ITEMS = 12;
+struct KdItemList {
+  int nitems;
+  int prefix[KD_MAX_ITEMS + 1];  // prefix sums of batch sizes
+  KdItem items[KD_MAX_ITEMS];
+};
+
+// Runs the pass lists of all items; one CTA per field.
+cudaError_t launch_line_passes(const KdItemList& list, int smem_doubles, const double* d_pool,
+                               cudaStream_t s);
+
+// Elementwise ops on fields of npts values. a has ba fields, b has bb fields
+// (ba, bb in {1, B}); out has max(ba, bb) fields.
+enum EwOp : int {
+  EW_ADD = 0,    // a + b
+  EW_SUB = 1,    // a - b
+  EW_MUL = 2,    // a * b
+  EW_DIV = 3,    // a / b
+  EW_AXPBY = 4,  // alpha*a + beta*b
+  EW_SCALE = 5,  // alpha*a
+  EW_ADDC = 6,   // a + alpha
+  EW_CSUB = 7,   // alpha - a
+  EW_CDIV = 8,   // alpha / a
+  EW_POWD = 9,   // pow(a, alpha)
+  EW_EXP = 10,
+  EW_LOG = 11,
+  EW_SQRT = 12,
+  EW_SIN = 13,
+  EW_COS = 14,
+  EW_NEG = 15,
+  EW_FILL = 16,  // alpha
+  EW_COPY = 17,  // a
+  EW_POWI = 18,  // pow(a, (int)alpha) for alpha <= 0 (reference uses std::pow)
+  EW_ATAN = 19,
+  EW_MULC_ADD = 20,  // out = a*b*alpha (product with constant)
+};
+
+cudaError_t launch_ew(int op, long long npts, int ba, const double* a, int bb, const double* b,
+                      double* out, double alpha, double beta, cudaStream_t s);
+
+// out[f][r] = sum_e w[r][e] * in[f][idx[r][e]] for up to 4 terms per row
+// (Galerkin/tau export, boundary sums).  rows with idx < 0 terms skipped.
+cudaError_t launch_gather_rows(const double* in, long long in_stride, int batch, int nrows,
+                               const int* idx4, const double* w4, double* out,
+                               long long out_stride_field, long long out_stride_row,
+                               double alpha, int accumulate, cudaStream_t s);
+
+// out[f][idx[e]] += w[e] * coef for seeds: builds batched seed patterns.
+// pattern entries: (seed s, position p, weight w) -> out[s*stride + p] = w.
+cudaError_t launch_scatter_seeds(double* out, long long stride, int nent, const int* seed,
+                                 const int* pos, const double* w, cudaStream_t s);
+
+// Sum over the last axis reduction helpers used by residual norms.
+cudaError_t launch_absmax(const double* x, long long n, double* out_scalar, cudaStream_t s);
+
+}  // namespace kd

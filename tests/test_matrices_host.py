@@ -1,0 +1,83 @@
+"""The C++ restatement of every 1-D operator (host code inside the CUDA
+library, exported as kd_matrix_1d) against the numpy oracle.  Host-only
+calls: no GPU needed."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from kadath_frontera_gb300 import _lib
+from oracle import spectral as S
+
+THETA = [S.COS_EVEN, S.COS_ODD, S.SIN_EVEN, S.SIN_ODD]
+FULL = [S.COS, S.SIN]
+RADIAL = [S.CHEB, S.CHEB_EVEN, S.CHEB_ODD]
+
+CASES = []
+for n in (5, 7, 9, 11, 13, 17):
+    for b in RADIAL + THETA + FULL:
+        CASES.append((S.OP_COEF, b, n, n))
+        CASES.append((S.OP_COEF_I, b, n, n))
+        CASES.append((S.OP_DER, b, n, n))
+    for b in THETA + FULL:
+        CASES += [(S.OP_MULT_SIN, b, n, n), (S.OP_DIV_SIN, b, n, n), (S.OP_MULT_COS, b, n, n)]
+    for b in THETA:
+        CASES.append((S.OP_DIV_COS, b, n, n))
+    for b in RADIAL:
+        CASES += [(S.OP_MULT_X, b, n, n), (S.OP_DIV_1MX2, b, n, n)]
+    for b in (S.CHEB_EVEN, S.CHEB_ODD):
+        CASES.append((S.OP_DIV_X, b, n, n))
+    CASES += [(S.OP_MULT_XM1, S.CHEB, n, n), (S.OP_DIV_XM1, S.CHEB, n, n), (S.OP_DIV_XP1, S.CHEB, n, n)]
+for nphi in (1, 4, 6, 8, 12):
+    CASES.append((S.OP_COEF, S.COSSIN, nphi, nphi + 2))
+    CASES.append((S.OP_COEF_I, S.COSSIN, nphi + 2, nphi))
+    if nphi >= 4:
+        CASES += [(S.OP_DER, S.COSSIN, nphi + 2, nphi + 2), (S.OP_MULT_SIN, S.COSSIN, nphi + 2, nphi + 2),
+                  (S.OP_MULT_COS, S.COSSIN, nphi + 2, nphi + 2)]
+for nphi in (4, 8):
+    for b in (S.COSSIN_EVEN, S.COSSIN_ODD):
+        CASES.append((S.OP_COEF, b, nphi, nphi + 2))
+        CASES.append((S.OP_COEF_I, b, nphi + 2, nphi))
+        CASES.append((S.OP_DER, b, nphi + 2, nphi + 2))
+
+
+def product_matrix(op, base, n_in, n_out):
+    lib = _lib.load()
+    m = (C.c_double * (n_in * n_out))()
+    ob = C.c_int()
+    st = lib.kd_matrix_1d(None, op, base, n_in, n_out, m, C.byref(ob))
+    assert st == 0
+    return ob.value, np.frombuffer(m, dtype=np.float64).reshape(n_out, n_in).copy()
+
+
+@pytest.mark.parametrize("op,base,n_in,n_out", CASES)
+def test_product_matrix_matches_oracle(op, base, n_in, n_out):
+    ob, mp = product_matrix(op, base, n_in, n_out)
+    if op == S.OP_COEF and base in (S.COSSIN, S.COSSIN_EVEN, S.COSSIN_ODD):
+        # the oracle's forward line has nbr = n_out slots, of which the first n_in are values
+        mo = np.zeros((n_out, n_in))
+        for c in range(n_in):
+            t = np.zeros(n_out)
+            t[c] = 1.0
+            mo[:, c] = S.COEF_1D[base](t)[:n_out]
+        obo = base
+    elif op == S.OP_COEF_I and base in (S.COSSIN, S.COSSIN_EVEN, S.COSSIN_ODD):
+        mo = np.zeros((n_out, n_in))
+        for c in range(n_in):
+            t = np.zeros(n_in)
+            t[c] = 1.0
+            mo[:, c] = S.COEF_I_1D[base](t)[:n_out]
+        obo = base
+    else:
+        obo, mo = S.matrix_1d(op, base, n_in, n_out)
+    assert ob == obo
+    scale = max(1.0, np.abs(mo).max())
+    assert np.abs(mp - mo).max() <= 1e-13 * scale, np.abs(mp - mo).max()
+
+
+def test_unsupported_pair_reports_status():
+    lib = _lib.load()
+    m = (C.c_double * 25)()
+    ob = C.c_int()
+    # div_x is defined only for the parity Chebyshev bases
+    assert lib.kd_matrix_1d(None, S.OP_DIV_X, S.CHEB, 5, 5, m, C.byref(ob)) == _lib.KD_ERR_UNSUPPORTED
