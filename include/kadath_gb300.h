@@ -103,6 +103,105 @@ int kd_ope_1d(kd_ctx* ctx, int op, int dim, const kd_transform_desc* desc, int* 
  * (row-major n_out x n_in) and its output basis; host memory. */
 int kd_matrix_1d(kd_ctx* ctx, int op, int basis, int n_in, int n_out, double* mat, int* out_basis);
 
+/* ---- spaces and fields (API surface of Space / Scalar) ----------------- */
+typedef struct kd_space kd_space;
+typedef struct kd_field kd_field;
+typedef struct kd_system kd_system;
+
+/* Space_spheric(CHEB_TYPE, center, res, bounds, withzec)
+ * (src/Space/Spheric/space_spheric.cpp:25): nucleus, shells, and a
+ * compactified outer domain when withzec != 0. */
+int kd_space_spheric_create(kd_ctx* ctx, const double center[3], const int res[3], const double* bounds,
+                            int nbounds, int withzec, kd_space** out);
+int kd_space_destroy(kd_space* sp);
+int kd_space_nbr_domains(const kd_space* sp, int* n);
+/* type: 1 nucleus, 2 shell, 3 compact (Domain_nucleus/_shell/_compact). */
+int kd_space_domain_info(const kd_space* sp, int dom, int* type, int npts[3], int ncoefs[3], double* alpha,
+                         double* beta);
+/* Domain::get_radius() and get_cart(c) at the collocation points (host). */
+int kd_space_radius(const kd_space* sp, int dom, double* out);
+int kd_space_cart(const kd_space* sp, int dom, int c, double* out);
+/* Standard bases of a domain (Domain_*::set_cheb_base): r table nc1*nc2,
+ * theta table nc2, phi basis. */
+int kd_space_std_base(const kd_space* sp, int dom, int* base_r, int* base_t, int* base_p);
+
+/* Scalar(space): one Val_domain per domain (include/scalar.hpp:67). */
+int kd_field_create(kd_space* sp, kd_field** out);
+int kd_field_destroy(kd_field* f);
+int kd_field_set_value(kd_field* f, double v);                 /* Scalar = v */
+int kd_field_std_base(kd_field* f);                            /* Scalar::std_base */
+int kd_field_set_conf(kd_field* f, int dom, const double* v);  /* values at collocation points */
+int kd_field_get_conf(kd_field* f, int dom, double* out);      /* Val_domain::coef_i + copy */
+int kd_field_get_coef(kd_field* f, int dom, double* out);      /* Val_domain::coef + copy */
+int kd_field_get_base(const kd_field* f, int dom, int* base_r, int* base_t, int* base_p);
+
+/* ---- System_of_eqs (include/system_of_eqs.hpp:54) ----------------------- */
+int kd_system_create(kd_space* sp, int dom_min, int dom_max, kd_system** out);
+int kd_system_destroy(kd_system* s);
+int kd_system_add_var(kd_system* s, const char* name, kd_field* f);        /* add_var(name, Tensor&) */
+int kd_system_add_var_double(kd_system* s, const char* name, double v);    /* add_var(name, double&) */
+int kd_system_get_var_double(const kd_system* s, const char* name, double* v);
+int kd_system_add_cst(kd_system* s, const char* name, double v);           /* add_cst(name, double) */
+int kd_system_add_cst_field(kd_system* s, const char* name, kd_field* f);  /* add_cst(name, Tensor) */
+int kd_system_add_def(kd_system* s, int dom, const char* text);            /* add_def; dom < 0: all */
+int kd_system_add_eq_inside(kd_system* s, int dom, const char* eq);        /* add_eq_inside */
+int kd_system_add_eq_bc(kd_system* s, int dom, int bound, const char* eq); /* add_eq_bc */
+int kd_system_add_eq_matching(kd_system* s, int dom, int bound, const char* eq); /* add_eq_matching */
+int kd_system_sizes(kd_system* s, int* n_unknowns, int* n_conditions);
+int kd_system_n_equations(kd_system* s, int* neq);
+/* sec_member (src/System_of_eqs/solver.cpp:49): F(u) into host F. */
+int kd_system_residual(kd_system* s, double* F);
+/* check_equations (solver.cpp:24): per-equation max |F| into errors[neq]. */
+int kd_system_check_equations(kd_system* s, double* errors);
+/* All columns of do_col_J (solver.cpp:120) as one column-major N x N
+ * host matrix (ld = N). */
+int kd_system_jacobian(kd_system* s, double* J);
+/* Same, into a device buffer of leading dimension ld (device pointer). */
+int kd_system_jacobian_device(kd_system* s, double* dJ, long long ld);
+/* xx_to_vars + var = old - x (src_par/do_newton.cpp:397-414), host x. */
+int kd_system_update(kd_system* s, const double* x);
+
+/* LU modes for the dense solve. */
+#define KD_LU_FP64 0     /* blocked LU, FP64 trailing updates */
+#define KD_LU_TF32_IR 1  /* TF32 tensor-core trailing updates + FP64 GMRES-IR */
+#define KD_LU_FP32_IR 2  /* FP32 trailing updates + FP64 GMRES-IR */
+
+typedef struct kd_newton_opts {
+  double precision;  /* stop when max |F| < precision (do_newton's first argument) */
+  int lu_mode;       /* KD_LU_* */
+  double gmres_tol;  /* relative residual target of the refinement */
+  int max_refine;    /* GMRES iterations per restart */
+  int graph_capture; /* reserved */
+} kd_newton_opts;
+
+typedef struct kd_newton_report {
+  double error;      /* pre-step max |F| (do_newton's `error` output) */
+  int converged;     /* do_newton's return value */
+  int n;             /* N = number of unknowns */
+  double t_residual_ms, t_assembly_ms, t_factor_ms, t_solve_ms, t_update_ms;
+  int refine_iters;
+  double refine_rel_residual;
+  long long kernel_launches;
+} kd_newton_report;
+
+/* System_of_eqs::do_newton (src_par/do_newton.cpp:65; decl
+ * include/system_of_eqs.hpp:871).  Returns KD_OK and fills rep; the fields
+ * registered with add_var are updated in place on the device. */
+int kd_newton_step(kd_system* s, const kd_newton_opts* opts, kd_newton_report* rep);
+
+/* ---- dense LU (Matrice::set_lu / solve, src/Matrice/matrice.cpp:192-249) */
+typedef struct kd_lu kd_lu;
+int kd_lu_create(kd_ctx* ctx, kd_lu** out);
+int kd_lu_destroy(kd_lu* lu);
+/* Factors the device matrix dA (column-major, ld).  FP64 mode overwrites
+ * dA with its factors; mixed modes keep dA as the refinement operator. */
+int kd_lu_factor(kd_lu* lu, double* dA, long long ld, int n, int mode);
+/* Solves in place on the device vector db; trans = 1 solves A^T x = b
+ * with the same factors (FP64 mode). */
+int kd_lu_solve(kd_lu* lu, double* db, int trans);
+int kd_lu_stats(const kd_lu* lu, double* t_factor_ms, double* t_solve_ms, int* refine_iters,
+                double* rel_residual);
+
 #ifdef __cplusplus
 }
 #endif

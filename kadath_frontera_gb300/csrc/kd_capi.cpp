@@ -1,6 +1,8 @@
 // C ABI entry points (declared in include/kadath_gb300.h).  Each call turns
 // C++ exceptions into status codes and records the message on the context.
+#include <cmath>
 #include <cstring>
+#include <algorithm>
 #include <memory>
 #include <string>
 
@@ -178,6 +180,402 @@ int kd_matrix_1d(kd_ctx* ctx, int op, int basis, int n_in, int n_out, double* ma
     std::memcpy(mat, m.m.data(), m.m.size() * sizeof(double));
     if (out_basis) *out_basis = m.out_basis;
   });
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------------
+// Spaces, fields, systems, Newton, LU.
+#include "kd_newton.hpp"
+
+struct kd_space {
+  kd_ctx* ctx;
+  std::unique_ptr<kd::Space> sp;
+};
+struct kd_field {
+  kd_space* sp;
+  std::unique_ptr<kd::Field> f;
+};
+struct kd_system {
+  kd_space* sp;
+  std::unique_ptr<kd::System> sys;
+  std::unique_ptr<kd::Newton> newton;
+};
+struct kd_lu {
+  kd_ctx* ctx;
+  std::unique_ptr<kd::DenseLU> lu;
+};
+
+namespace {
+template <class F>
+int guarded_ctx(kd_ctx* ctx, F&& f) {
+  if (!ctx) return KD_ERR_ARG;
+  return guarded(ctx, std::forward<F>(f));
+}
+void check_dom(const kd::Space& sp, int dom) {
+  if (dom < 0 || dom >= sp.ndom()) throw kd::KdError(KD_ERR_ARG, "domain index out of range");
+}
+}  // namespace
+
+extern "C" {
+
+int kd_space_spheric_create(kd_ctx* ctx, const double center[3], const int res[3], const double* bounds, int nbounds,
+                            int withzec, kd_space** out) {
+  if (!ctx || !out) return KD_ERR_ARG;
+  return guarded(ctx, [&] {
+    if (!center || !res || !bounds || nbounds < 1) throw kd::KdError(KD_ERR_ARG, "bad space arguments");
+    for (int i = 0; i < 3; i++)
+      if (res[i] < 1) throw kd::KdError(KD_ERR_ARG, "resolution must be positive");
+    if (res[0] < 3 || res[1] < 2) throw kd::KdError(KD_ERR_ARG, "need nr >= 3 and ntheta >= 2");
+    std::vector<double> b(bounds, bounds + nbounds);
+    auto* s = new kd_space{ctx, std::make_unique<kd::Space>(center, res, b, withzec != 0)};
+    *out = s;
+  });
+}
+
+int kd_space_destroy(kd_space* sp) {
+  if (!sp) return KD_ERR_ARG;
+  delete sp;
+  return KD_OK;
+}
+
+int kd_space_nbr_domains(const kd_space* sp, int* n) {
+  if (!sp || !n) return KD_ERR_ARG;
+  *n = sp->sp->ndom();
+  return KD_OK;
+}
+
+int kd_space_domain_info(const kd_space* sp, int dom, int* type, int npts[3], int ncoefs[3], double* alpha,
+                         double* beta) {
+  if (!sp) return KD_ERR_ARG;
+  return guarded(sp->ctx, [&] {
+    check_dom(*sp->sp, dom);
+    const kd::Domain& d = sp->sp->dom(dom);
+    if (type) *type = d.type;
+    for (int i = 0; i < 3; i++) {
+      if (npts) npts[i] = d.np[i];
+      if (ncoefs) ncoefs[i] = d.nc[i];
+    }
+    if (alpha) *alpha = d.alpha;
+    if (beta) *beta = d.beta;
+  });
+}
+
+int kd_space_radius(const kd_space* sp, int dom, double* out) {
+  if (!sp || !out) return KD_ERR_ARG;
+  return guarded(sp->ctx, [&] {
+    check_dom(*sp->sp, dom);
+    auto r = sp->sp->dom(dom).radius_values();
+    std::memcpy(out, r.data(), r.size() * sizeof(double));
+  });
+}
+
+int kd_space_cart(const kd_space* sp, int dom, int c, double* out) {
+  if (!sp || !out || c < 0 || c > 2) return KD_ERR_ARG;
+  return guarded(sp->ctx, [&] {
+    check_dom(*sp->sp, dom);
+    auto r = sp->sp->dom(dom).cart_values(c);
+    std::memcpy(out, r.data(), r.size() * sizeof(double));
+  });
+}
+
+int kd_space_std_base(const kd_space* sp, int dom, int* base_r, int* base_t, int* base_p) {
+  if (!sp) return KD_ERR_ARG;
+  return guarded(sp->ctx, [&] {
+    check_dom(*sp->sp, dom);
+    kd::Base b = sp->sp->dom(dom).std_base();
+    if (base_r) std::memcpy(base_r, b.r.data(), b.r.size() * sizeof(int));
+    if (base_t) std::memcpy(base_t, b.t.data(), b.t.size() * sizeof(int));
+    if (base_p) *base_p = b.p;
+  });
+}
+
+int kd_field_create(kd_space* sp, kd_field** out) {
+  if (!sp || !out) return KD_ERR_ARG;
+  return guarded(sp->ctx, [&] {
+    *out = new kd_field{sp, std::make_unique<kd::Field>(sp->ctx->c.get(), sp->sp.get())};
+  });
+}
+
+int kd_field_destroy(kd_field* f) {
+  if (!f) return KD_ERR_ARG;
+  delete f;
+  return KD_OK;
+}
+
+int kd_field_set_value(kd_field* f, double v) {
+  if (!f) return KD_ERR_ARG;
+  return guarded(f->sp->ctx, [&] { f->f->set_value(v); });
+}
+
+int kd_field_std_base(kd_field* f) {
+  if (!f) return KD_ERR_ARG;
+  return guarded(f->sp->ctx, [&] { f->f->std_base(); });
+}
+
+int kd_field_set_conf(kd_field* f, int dom, const double* v) {
+  if (!f || !v) return KD_ERR_ARG;
+  return guarded(f->sp->ctx, [&] {
+    check_dom(*f->sp->sp, dom);
+    f->f->set_conf_host(dom, v);
+  });
+}
+
+int kd_field_get_conf(kd_field* f, int dom, double* out) {
+  if (!f || !out) return KD_ERR_ARG;
+  return guarded(f->sp->ctx, [&] {
+    check_dom(*f->sp->sp, dom);
+    f->f->get_conf_host(dom, out);
+  });
+}
+
+int kd_field_get_coef(kd_field* f, int dom, double* out) {
+  if (!f || !out) return KD_ERR_ARG;
+  return guarded(f->sp->ctx, [&] {
+    check_dom(*f->sp->sp, dom);
+    f->f->get_coef_host(dom, out);
+  });
+}
+
+int kd_field_get_base(const kd_field* f, int dom, int* base_r, int* base_t, int* base_p) {
+  if (!f) return KD_ERR_ARG;
+  return guarded(f->sp->ctx, [&] {
+    check_dom(*f->sp->sp, dom);
+    const kd::Base& b = f->f->d[dom].base;
+    if (!b.def) throw kd::KdError(KD_ERR_STATE, "basis not defined");
+    if (base_r) std::memcpy(base_r, b.r.data(), b.r.size() * sizeof(int));
+    if (base_t) std::memcpy(base_t, b.t.data(), b.t.size() * sizeof(int));
+    if (base_p) *base_p = b.p;
+  });
+}
+
+int kd_system_create(kd_space* sp, int dom_min, int dom_max, kd_system** out) {
+  if (!sp || !out) return KD_ERR_ARG;
+  return guarded(sp->ctx, [&] {
+    auto* s = new kd_system{sp, std::make_unique<kd::System>(sp->ctx->c.get(), sp->sp.get(), dom_min, dom_max), nullptr};
+    s->newton = std::make_unique<kd::Newton>(s->sys.get());
+    *out = s;
+  });
+}
+
+int kd_system_destroy(kd_system* s) {
+  if (!s) return KD_ERR_ARG;
+  delete s;
+  return KD_OK;
+}
+
+#define SYS_GUARD(s) \
+  if (!(s)) return KD_ERR_ARG; \
+  return guarded((s)->sp->ctx, [&]
+
+int kd_system_add_var(kd_system* s, const char* name, kd_field* f) {
+  SYS_GUARD(s) {
+    if (!name || !f) throw kd::KdError(KD_ERR_ARG, "null argument");
+    s->sys->add_var(name, f->f.get());
+  });
+}
+
+int kd_system_add_var_double(kd_system* s, const char* name, double v) {
+  SYS_GUARD(s) {
+    if (!name) throw kd::KdError(KD_ERR_ARG, "null name");
+    s->sys->add_var_double(name, v);
+  });
+}
+
+int kd_system_get_var_double(const kd_system* s, const char* name, double* v) {
+  if (!s || !name || !v) return KD_ERR_ARG;
+  return guarded(s->sp->ctx, [&] {
+    int w = s->sys->find_var_double(kd::trim_expr(name).substr(0, kd::trim_expr(name).size() - 1));
+    if (w < 0) throw kd::KdError(KD_ERR_ARG, "unknown double variable");
+    *v = s->sys->var_double(w);
+  });
+}
+
+int kd_system_add_cst(kd_system* s, const char* name, double v) {
+  SYS_GUARD(s) {
+    if (!name) throw kd::KdError(KD_ERR_ARG, "null name");
+    s->sys->add_cst(name, v);
+  });
+}
+
+int kd_system_add_cst_field(kd_system* s, const char* name, kd_field* f) {
+  SYS_GUARD(s) {
+    if (!name || !f) throw kd::KdError(KD_ERR_ARG, "null argument");
+    s->sys->add_cst_field(name, f->f.get());
+  });
+}
+
+int kd_system_add_def(kd_system* s, int dom, const char* text) {
+  SYS_GUARD(s) {
+    if (!text) throw kd::KdError(KD_ERR_ARG, "null text");
+    s->sys->add_def(dom, text);
+  });
+}
+
+int kd_system_add_eq_inside(kd_system* s, int dom, const char* eq) {
+  SYS_GUARD(s) {
+    if (!eq) throw kd::KdError(KD_ERR_ARG, "null equation");
+    s->sys->add_eq_inside(dom, eq);
+  });
+}
+
+int kd_system_add_eq_bc(kd_system* s, int dom, int bound, const char* eq) {
+  SYS_GUARD(s) {
+    if (!eq) throw kd::KdError(KD_ERR_ARG, "null equation");
+    s->sys->add_eq_bc(dom, bound, eq);
+  });
+}
+
+int kd_system_add_eq_matching(kd_system* s, int dom, int bound, const char* eq) {
+  SYS_GUARD(s) {
+    if (!eq) throw kd::KdError(KD_ERR_ARG, "null equation");
+    s->sys->add_eq_matching(dom, bound, eq);
+  });
+}
+
+int kd_system_sizes(kd_system* s, int* n_unknowns, int* n_conditions) {
+  SYS_GUARD(s) {
+    if (s->sys->nbr_conditions() < 0) s->sys->residual(nullptr);
+    if (n_unknowns) *n_unknowns = s->sys->nbr_unknowns();
+    if (n_conditions) *n_conditions = s->sys->nbr_conditions();
+  });
+}
+
+int kd_system_n_equations(kd_system* s, int* neq) {
+  SYS_GUARD(s) {
+    if (!neq) throw kd::KdError(KD_ERR_ARG, "null output");
+    *neq = s->sys->n_equations();
+  });
+}
+
+int kd_system_residual(kd_system* s, double* F) {
+  SYS_GUARD(s) {
+    if (!F) throw kd::KdError(KD_ERR_ARG, "null output");
+    kd::Context* c = s->sp->ctx->c.get();
+    if (s->sys->nbr_conditions() < 0) s->sys->residual(nullptr);
+    int n = s->sys->nbr_conditions();
+    s->newton->ensure(n > 0 ? n : 1);
+    s->sys->residual(s->newton->d_F);
+    kd::cuda_check(cudaMemcpyAsync(F, s->newton->d_F, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream()), "D2H");
+    kd::cuda_check(cudaStreamSynchronize(c->stream()), "sync");
+  });
+}
+
+int kd_system_check_equations(kd_system* s, double* errors) {
+  SYS_GUARD(s) {
+    if (!errors) throw kd::KdError(KD_ERR_ARG, "null output");
+    kd::Context* c = s->sp->ctx->c.get();
+    if (s->sys->nbr_conditions() < 0) s->sys->residual(nullptr);
+    int n = s->sys->nbr_conditions();
+    s->newton->ensure(n > 0 ? n : 1);
+    s->sys->residual(s->newton->d_F);
+    std::vector<double> F(n);
+    kd::cuda_check(cudaMemcpyAsync(F.data(), s->newton->d_F, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream()),
+                   "D2H");
+    kd::cuda_check(cudaStreamSynchronize(c->stream()), "sync");
+    for (int i = 0; i < s->sys->n_equations(); i++) {
+      const kd::Equation& e = s->sys->equation(i);
+      double m = 0;
+      for (int r = 0; r < e.n_cond; r++) m = std::max(m, std::fabs(F[e.row0 + r]));
+      errors[i] = m;
+    }
+  });
+}
+
+int kd_system_jacobian_device(kd_system* s, double* dJ, long long ld) {
+  SYS_GUARD(s) {
+    if (!dJ) throw kd::KdError(KD_ERR_ARG, "null output");
+    s->sys->jacobian(dJ, ld);
+    kd::cuda_check(cudaStreamSynchronize(s->sp->ctx->c->stream()), "sync");
+  });
+}
+
+int kd_system_jacobian(kd_system* s, double* J) {
+  SYS_GUARD(s) {
+    if (!J) throw kd::KdError(KD_ERR_ARG, "null output");
+    kd::Context* c = s->sp->ctx->c.get();
+    if (s->sys->nbr_conditions() < 0) s->sys->residual(nullptr);
+    int n = s->sys->nbr_unknowns();
+    s->newton->ensure(n);
+    s->sys->jacobian(s->newton->d_J, n);
+    kd::cuda_check(cudaMemcpyAsync(J, s->newton->d_J, sizeof(double) * n * n, cudaMemcpyDeviceToHost, c->stream()),
+                   "D2H");
+    kd::cuda_check(cudaStreamSynchronize(c->stream()), "sync");
+  });
+}
+
+int kd_system_update(kd_system* s, const double* x) {
+  SYS_GUARD(s) {
+    if (!x) throw kd::KdError(KD_ERR_ARG, "null input");
+    kd::Context* c = s->sp->ctx->c.get();
+    int n = s->sys->nbr_unknowns();
+    s->newton->ensure(n);
+    kd::cuda_check(cudaMemcpyAsync(s->newton->d_F, x, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream()), "H2D");
+    s->sys->update_from_x(s->newton->d_F);
+  });
+}
+
+int kd_newton_step(kd_system* s, const kd_newton_opts* opts, kd_newton_report* rep) {
+  SYS_GUARD(s) {
+    if (!opts || !rep) throw kd::KdError(KD_ERR_ARG, "null argument");
+    kd::NewtonOpts o;
+    o.precision = opts->precision;
+    o.lu_mode = opts->lu_mode;
+    o.gmres_tol = opts->gmres_tol > 0 ? opts->gmres_tol : 1e-14;
+    o.max_refine = opts->max_refine > 0 ? opts->max_refine : 50;
+    o.graph_capture = opts->graph_capture;
+    kd::NewtonReport r;
+    s->newton->step(o, r);
+    rep->error = r.error;
+    rep->converged = r.converged;
+    rep->n = r.n;
+    rep->t_residual_ms = r.t_residual_ms;
+    rep->t_assembly_ms = r.t_assembly_ms;
+    rep->t_factor_ms = r.t_factor_ms;
+    rep->t_solve_ms = r.t_solve_ms;
+    rep->t_update_ms = r.t_update_ms;
+    rep->refine_iters = r.refine_iters;
+    rep->refine_rel_residual = r.refine_rel_residual;
+    rep->kernel_launches = r.kernel_launches;
+  });
+}
+
+int kd_lu_create(kd_ctx* ctx, kd_lu** out) {
+  if (!ctx || !ctx->c || !out) return KD_ERR_ARG;
+  return guarded(ctx, [&] { *out = new kd_lu{ctx, std::make_unique<kd::DenseLU>(ctx->c.get())}; });
+}
+
+int kd_lu_destroy(kd_lu* lu) {
+  if (!lu) return KD_ERR_ARG;
+  delete lu;
+  return KD_OK;
+}
+
+int kd_lu_factor(kd_lu* lu, double* dA, long long ld, int n, int mode) {
+  if (!lu) return KD_ERR_ARG;
+  return guarded(lu->ctx, [&] {
+    if (!dA || n <= 0 || ld < n) throw kd::KdError(KD_ERR_ARG, "bad matrix");
+    if (mode < KD_LU_FP64 || mode > KD_LU_FP32_IR) throw kd::KdError(KD_ERR_ARG, "unknown LU mode");
+    lu->lu->factor(dA, ld, n, mode);
+  });
+}
+
+int kd_lu_solve(kd_lu* lu, double* db, int trans) {
+  if (!lu) return KD_ERR_ARG;
+  return guarded(lu->ctx, [&] {
+    if (!db) throw kd::KdError(KD_ERR_ARG, "null vector");
+    if (lu->lu->n() <= 0) throw kd::KdError(KD_ERR_STATE, "factor first");
+    lu->lu->solve(db, trans);
+  });
+}
+
+int kd_lu_stats(const kd_lu* lu, double* t_factor_ms, double* t_solve_ms, int* refine_iters, double* rel_residual) {
+  if (!lu) return KD_ERR_ARG;
+  if (t_factor_ms) *t_factor_ms = lu->lu->stats.t_factor_ms;
+  if (t_solve_ms) *t_solve_ms = lu->lu->stats.t_solve_ms;
+  if (refine_iters) *refine_iters = lu->lu->stats.refine_iters;
+  if (rel_residual) *rel_residual = lu->lu->stats.final_rel_residual;
+  return KD_OK;
 }
 
 }  // extern "C"

@@ -149,22 +149,18 @@ __global__ void ew_kernel(int op, long long npts, long long total, int ba, const
   }
 }
 
-__global__ void gather_rows_kernel(const double* __restrict__ in, long long in_stride, int batch, int nrows,
-                                   const int* __restrict__ idx4, const double* __restrict__ w4,
-                                   double* __restrict__ out, long long osf, long long osr, double alpha,
-                                   int accumulate) {
+__global__ void gather_csr_kernel(const double* __restrict__ in, long long in_stride, int batch, int nrows,
+                                  const int* __restrict__ rowptr, const int* __restrict__ idx,
+                                  const double* __restrict__ w, double* __restrict__ out, long long osf,
+                                  long long osr, double alpha, int accumulate) {
   long long total = static_cast<long long>(batch) * nrows;
   for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < total;
        t += static_cast<long long>(gridDim.x) * blockDim.x) {
     int r = static_cast<int>(t % nrows);
-    int f = static_cast<int>(t / nrows);
+    long long f = t / nrows;
     const double* src = in + f * in_stride;
     double acc = 0.0;
-#pragma unroll
-    for (int e = 0; e < 4; e++) {
-      int ix = idx4[4 * r + e];
-      if (ix >= 0) acc += w4[4 * r + e] * src[ix];
-    }
+    for (int e = rowptr[r]; e < rowptr[r + 1]; e++) acc = fma(w[e], src[idx[e]], acc);
     double* dst = out + f * osf + r * osr;
     if (accumulate) *dst += alpha * acc; else *dst = alpha * acc;
   }
@@ -229,13 +225,13 @@ cudaError_t launch_ew(int op, long long npts, int ba, const double* a, int bb, c
   return cudaGetLastError();
 }
 
-cudaError_t launch_gather_rows(const double* in, long long in_stride, int batch, int nrows, const int* idx4,
-                               const double* w4, double* out, long long osf, long long osr, double alpha,
-                               int accumulate, cudaStream_t s) {
+cudaError_t launch_gather_csr(const double* in, long long in_stride, int batch, int nrows, const int* rowptr,
+                              const int* idx, const double* w, double* out, long long osf, long long osr,
+                              double alpha, int accumulate, cudaStream_t s) {
   long long total = static_cast<long long>(batch) * nrows;
   if (total <= 0) return cudaSuccess;
-  gather_rows_kernel<<<grid_for(total, 256), 256, 0, s>>>(in, in_stride, batch, nrows, idx4, w4, out, osf, osr,
-                                                         alpha, accumulate);
+  gather_csr_kernel<<<grid_for(total, 256), 256, 0, s>>>(in, in_stride, batch, nrows, rowptr, idx, w, out, osf, osr,
+                                                        alpha, accumulate);
   return cudaGetLastError();
 }
 

@@ -76,17 +76,12 @@ enum EwOp : int {
 cudaError_t launch_ew(int op, long long npts, int ba, const double* a, int bb, const double* b,
                       double* out, double alpha, double beta, cudaStream_t s);
 
-// out[f][r] = sum_e w[r][e] * in[f][idx[r][e]] for up to 4 terms per row
-// (Galerkin/tau export, boundary sums).  rows with idx < 0 terms skipped.
-cudaError_t launch_gather_rows(const double* in, long long in_stride, int batch, int nrows,
-                               const int* idx4, const double* w4, double* out,
-                               long long out_stride_field, long long out_stride_row,
-                               double alpha, int accumulate, cudaStream_t s);
-
-// out[f][idx[e]] += w[e] * coef for seeds: builds batched seed patterns.
-// pattern entries: (seed s, position p, weight w) -> out[s*stride + p] = w.
-cudaError_t launch_scatter_seeds(double* out, long long stride, int nent, const int* seed,
-                                 const int* pos, const double* w, cudaStream_t s);
+// Sparse row gather (CSR): for each field f of the batch and row r,
+//   out[f*osf + r*osr] (+)= alpha * sum_{e in [rowptr[r], rowptr[r+1])} w[e] * in[f*in_stride + idx[e]]
+// in_stride = 0 broadcasts one input field to every output field.
+cudaError_t launch_gather_csr(const double* in, long long in_stride, int batch, int nrows, const int* rowptr,
+                              const int* idx, const double* w, double* out, long long osf, long long osr,
+                              double alpha, int accumulate, cudaStream_t s);
 
 // Sum over the last axis reduction helpers used by residual norms.
 cudaError_t launch_absmax(const double* x, long long n, double* out_scalar, cudaStream_t s);

@@ -1,0 +1,71 @@
+// Dense LU with partial pivoting on the GPU, replacing Matrice::set_lu /
+// Matrice::solve (src/Matrice/matrice.cpp:192-249, LAPACK dgetrf/dgetrs)
+// and the ScaLAPACK pdgesv of src_par/do_newton.cpp:317.
+//
+// Matrices are column-major with leading dimension ld.  Modes:
+//   KD_LU_FP64      blocked right-looking LU, FP64 trailing updates
+//   KD_LU_TF32_IR   FP32 working copy, trailing updates on tcgen05 tensor
+//                   cores in TF32 with FP32 accumulation, then FP64 GMRES
+//                   iterative refinement against the FP64 matrix
+#pragma once
+#include <cublas_v2.h>
+
+#include "kd_context.hpp"
+
+namespace kd {
+
+enum LuMode : int { LU_FP64 = 0, LU_TF32_IR = 1, LU_FP32_IR = 2 };
+
+struct LuStats {
+  double t_factor_ms = 0, t_solve_ms = 0;
+  int refine_iters = 0;
+  double final_rel_residual = 0;
+  long long flops = 0;
+};
+
+class DenseLU {
+ public:
+  explicit DenseLU(Context* ctx);
+  ~DenseLU();
+
+  // Factors the N x N matrix A (device, FP64, column-major, ld).  For the
+  // FP64 mode A is overwritten by its factors; for the mixed modes A is kept
+  // (it is the refinement operator) and an FP32 copy is factored.
+  void factor(double* A, long long ld, int N, int mode);
+  // Solves A x = b in place (b on the device).  Mixed modes run GMRES-IR.
+  void solve(double* b, int trans = 0);
+  // Transposed solve with the same factors (A^T x = b), FP64 mode only.
+  void solve_transposed(double* b) { solve(b, 1); }
+
+  int mode() const { return mode_; }
+  int n() const { return N_; }
+  LuStats stats;
+  double gmres_tol = 1e-14;
+  int gmres_max_iter = 50;
+  int nb = 128;
+
+ private:
+  Context* ctx_;
+  cublasHandle_t blas_ = nullptr;
+  int mode_ = 0, N_ = 0;
+  long long ld_ = 0;
+  double* A_ = nullptr;        // FP64 matrix (factors in FP64 mode, operator in mixed modes)
+  float* A32_ = nullptr;       // FP32 factors (mixed modes)
+  size_t a32_cap_ = 0;
+  int* ipiv_ = nullptr;        // device pivots
+  size_t ipiv_cap_ = 0;
+  int* d_info_ = nullptr;
+  double* work_ = nullptr;     // solver workspace
+  size_t work_cap_ = 0;
+  float* work32_ = nullptr;
+  size_t work32_cap_ = 0;
+
+  void ensure_work(size_t n);
+  void factor_fp64(double* A, long long ld, int N);
+  void factor_f32(float* A, long long ld, int N, bool tf32);
+  void solve_fp64(const double* LU, long long ld, int N, double* b, int trans);
+  void solve_f32(double* b);  // applies the FP32 factors to an FP64 vector
+  void gmres_ir(double* b);
+};
+
+}  // namespace kd

@@ -1,0 +1,49 @@
+// One Newton-Raphson step with the semantics of System_of_eqs::do_newton
+// (src_par/do_newton.cpp:65-430) and do_newton_seq (:519-572):
+//   F = sec_member(); error = max|F|; if error < precision -> true, no update
+//   else assemble J, solve J x = F, fields <- fields - x, return false.
+#pragma once
+#include <memory>
+
+#include "kd_lu.hpp"
+#include "kd_system.hpp"
+
+namespace kd {
+
+struct NewtonOpts {
+  double precision = 1e-10;
+  int lu_mode = LU_FP64;
+  double gmres_tol = 1e-14;
+  int max_refine = 50;
+  int graph_capture = 0;
+};
+
+struct NewtonReport {
+  double error = 0;
+  int converged = 0;
+  int n = 0;
+  double t_residual_ms = 0, t_assembly_ms = 0, t_factor_ms = 0, t_solve_ms = 0, t_update_ms = 0;
+  int refine_iters = 0;
+  double refine_rel_residual = 0;
+  long long kernel_launches = 0;
+};
+
+class Newton {
+ public:
+  explicit Newton(System* s);
+  ~Newton();
+  bool step(const NewtonOpts& o, NewtonReport& rep);
+  // Device buffers of the last step (valid until the next call).
+  double* d_F = nullptr;
+  double* d_J = nullptr;
+  long long ld = 0;
+  DenseLU& lu() { return *lu_; }
+  void ensure(int N);
+
+ private:
+  System* sys_;
+  std::unique_ptr<DenseLU> lu_;
+  size_t capF_ = 0, capJ_ = 0;
+};
+
+}  // namespace kd

@@ -1,0 +1,559 @@
+#include "kd_system.hpp"
+
+#include <cstring>
+#include <sstream>
+
+namespace kd {
+
+// ------------------------------------------------------------------ Field --
+Field::Field(Context* c, const Space* s) : ctx(c), sp(s), d(s->ndom()) {
+  for (int i = 0; i < s->ndom(); i++) {
+    cuda_check(cudaMalloc(&d[i].c, sizeof(double) * s->dom(i).npts()), "cudaMalloc(field conf)");
+    cuda_check(cudaMalloc(&d[i].cf, sizeof(double) * s->dom(i).ncoefs()), "cudaMalloc(field coef)");
+  }
+}
+
+Field::~Field() {
+  for (auto& p : d) {
+    cudaFree(p.c);
+    cudaFree(p.cf);
+  }
+}
+
+DVal Field::val(int dom) const {
+  const PerDom& p = d.at(dom);
+  const Domain* dm = &sp->dom(dom);
+  if (p.zero) {
+    DVal z = DVal::zeros(ctx, dm, 1);
+    z.base = p.base;
+    return z;
+  }
+  DVal v(ctx, dm, 1);
+  v.zero = false;
+  v.base = p.base;
+  if (p.in_conf) {
+    v.c = p.c;
+    v.in_conf = true;
+  }
+  if (p.in_coef) {
+    v.cf = p.cf;
+    v.in_coef = true;
+  }
+  return v;
+}
+
+void Field::assign(int dom, const DVal& v) {
+  PerDom& p = d.at(dom);
+  if (v.batch != 1) throw KdError(KD_ERR_ARG, "a field holds one value per domain");
+  p.base = v.base;
+  if (v.zero) {
+    p.zero = true;
+    p.in_conf = p.in_coef = false;
+    return;
+  }
+  p.zero = false;
+  p.in_conf = v.in_conf;
+  p.in_coef = v.in_coef;
+  const Domain& dm = sp->dom(dom);
+  if (v.in_conf && v.c != p.c)
+    cuda_check(cudaMemcpyAsync(p.c, v.c, sizeof(double) * dm.npts(), cudaMemcpyDeviceToDevice, ctx->stream()),
+               "field copy");
+  if (v.in_coef && v.cf != p.cf)
+    cuda_check(cudaMemcpyAsync(p.cf, v.cf, sizeof(double) * dm.ncoefs(), cudaMemcpyDeviceToDevice, ctx->stream()),
+               "field copy");
+}
+
+void Field::set_conf_host(int dom, const double* values) {
+  PerDom& p = d.at(dom);
+  const Domain& dm = sp->dom(dom);
+  cuda_check(cudaMemcpyAsync(p.c, values, sizeof(double) * dm.npts(), cudaMemcpyHostToDevice, ctx->stream()),
+             "field upload");
+  cuda_check(cudaStreamSynchronize(ctx->stream()), "sync");
+  p.zero = false;
+  p.in_conf = true;
+  p.in_coef = false;
+}
+
+void Field::set_value(double v) {
+  for (int i = 0; i < sp->ndom(); i++) {
+    PerDom& p = d[i];
+    if (v == 0.0) {
+      p.zero = true;
+      p.in_conf = p.in_coef = false;
+      continue;
+    }
+    cuda_check(launch_ew(EW_FILL, sp->dom(i).npts(), 1, nullptr, 1, nullptr, p.c, v, 0.0, ctx->stream()), "fill");
+    p.zero = false;
+    p.in_conf = true;
+    p.in_coef = false;
+  }
+}
+
+void Field::std_base() {
+  for (int i = 0; i < sp->ndom(); i++) d[i].base = sp->dom(i).std_base();
+}
+
+void Field::get_conf_host(int dom, double* out) {
+  const Domain& dm = sp->dom(dom);
+  if (d.at(dom).zero) {
+    std::memset(out, 0, sizeof(double) * dm.npts());
+    return;
+  }
+  size_t mark = ctx->scratch().mark();
+  DVal v = val(dom);
+  v.coef_i();
+  cuda_check(cudaMemcpyAsync(out, v.c, sizeof(double) * dm.npts(), cudaMemcpyDeviceToHost, ctx->stream()), "D2H");
+  cuda_check(cudaStreamSynchronize(ctx->stream()), "sync");
+  ctx->scratch().release_to(mark);
+}
+
+void Field::get_coef_host(int dom, double* out) {
+  const Domain& dm = sp->dom(dom);
+  if (d.at(dom).zero) {
+    std::memset(out, 0, sizeof(double) * dm.ncoefs());
+    return;
+  }
+  size_t mark = ctx->scratch().mark();
+  DVal v = val(dom);
+  v.coef();
+  cuda_check(cudaMemcpyAsync(out, v.cf, sizeof(double) * dm.ncoefs(), cudaMemcpyDeviceToHost, ctx->stream()), "D2H");
+  cuda_check(cudaStreamSynchronize(ctx->stream()), "sync");
+  ctx->scratch().release_to(mark);
+}
+
+// -------------------------------------------------------------- EvalState --
+Term EvalState::var_term(int which, int dom) {
+  Term t;
+  t.dom = dom;
+  t.valence = 0;
+  const auto& vi = sys->vars_.at(which);
+  t.vt.push_back(vi.f->val(dom));
+  if (with_der) {
+    t.has_dt = true;
+    if (which == seed_var && dom == seed_dom) t.dt.push_back(seed);
+    else t.dt.push_back(DVal::zeros(sys->ctx, &sys->sp->dom(dom), B));
+  }
+  return t;
+}
+
+Term EvalState::var_double_term(int which, int dom) {
+  Term t = Term::dbl(dom, sys->vdoubles_.at(which).value);
+  if (with_der) {
+    t.has_dd = true;
+    t.dd = (which == seed_var_double) ? 1.0 : 0.0;
+  }
+  return t;
+}
+
+Term EvalState::cst_term(int which, int dom) {
+  const auto& c = sys->csts_.at(which);
+  if (!c.is_field) {
+    Term t = Term::dbl(dom, c.value);
+    if (with_der) {
+      t.has_dd = true;
+      t.dd = 0.0;
+    }
+    return t;
+  }
+  Term t;
+  t.dom = dom;
+  t.vt.push_back(c.f->val(dom));
+  if (with_der) {
+    t.has_dt = true;
+    t.dt.push_back(DVal::zeros(sys->ctx, &sys->sp->dom(dom), B));
+  }
+  return t;
+}
+
+Term EvalState::def_term(int which, int dom) {
+  auto key = std::make_pair(which, dom);
+  auto it = def_cache.find(key);
+  if (it != def_cache.end()) return it->second;
+  const auto& df = sys->defs_.at(which);
+  Term t = df.ope->action(*this);
+  def_cache[key] = t;
+  return t;
+}
+
+// ----------------------------------------------------------------- System --
+System::System(Context* c, const Space* s, int dmin, int dmax) : ctx(c), sp(s), dom_min(dmin), dom_max(dmax) {
+  if (dmin < 0 || dmax >= s->ndom() || dmin > dmax) throw KdError(KD_ERR_ARG, "bad domain range for the system");
+}
+
+namespace {
+std::string bare(const std::string& s) {
+  std::string t = trim_expr(s);
+  while (!t.empty() && t.back() == ' ') t.pop_back();
+  return t;
+}
+
+// Splits "lhs = rhs" at the last '=' with balanced parentheses on both sides.
+bool split_eq(const std::string& s, std::string& l, std::string& r) {
+  for (int p = static_cast<int>(s.size()) - 1; p >= 0; p--)
+    if (s[p] == '=') {
+      l = s.substr(0, p);
+      r = s.substr(p + 1);
+      auto cnt = [](const std::string& x, char c) {
+        int n = 0;
+        for (char y : x) n += (y == c);
+        return n;
+      };
+      if (bare(l).empty() || bare(r).empty()) continue;
+      if (cnt(l, '(') == cnt(l, ')') && cnt(r, '(') == cnt(r, ')')) return true;
+    }
+  return false;
+}
+
+class OpeSubEq : public Ope {
+ public:
+  OpeSubEq(int dom, OpePtr a, OpePtr b) : Ope(dom), a(std::move(a)), b(std::move(b)) {}
+  Term action(EvalState& st) const override { return a->action(st) - b->action(st); }
+  OpePtr a, b;
+};
+}  // namespace
+
+int System::find_var(const std::string& n) const {
+  for (size_t i = 0; i < vars_.size(); i++)
+    if (vars_[i].name == n) return static_cast<int>(i);
+  return -1;
+}
+int System::find_var_double(const std::string& n) const {
+  for (size_t i = 0; i < vdoubles_.size(); i++)
+    if (vdoubles_[i].name == n) return static_cast<int>(i);
+  return -1;
+}
+int System::find_cst(const std::string& n) const {
+  for (size_t i = 0; i < csts_.size(); i++)
+    if (csts_[i].name == n) return static_cast<int>(i);
+  return -1;
+}
+int System::find_def(const std::string& n, int dom) const {
+  for (size_t i = 0; i < defs_.size(); i++)
+    if (defs_[i].name == n && defs_[i].dom == dom) return static_cast<int>(i);
+  return -1;
+}
+
+int System::add_var(const std::string& name, Field* f) {
+  if (name.find('_') != std::string::npos || name.find('^') != std::string::npos)
+    throw KdError(KD_ERR_ARG, "No indices allowed in names of variables");
+  for (int dd = dom_min; dd <= dom_max; dd++)
+    if (!f->d[dd].base.def) throw KdError(KD_ERR_STATE, "unknown field without a basis (call std_base)");
+  vars_.push_back({bare(name), f});
+  nbr_unknowns_ = -1;
+  return static_cast<int>(vars_.size()) - 1;
+}
+
+int System::add_var_double(const std::string& name, double value) {
+  vdoubles_.push_back({bare(name), value});
+  nbr_unknowns_ = -1;
+  return static_cast<int>(vdoubles_.size()) - 1;
+}
+
+int System::add_cst(const std::string& name, double value) {
+  csts_.push_back({bare(name), false, value, nullptr});
+  return static_cast<int>(csts_.size()) - 1;
+}
+
+int System::add_cst_field(const std::string& name, Field* f) {
+  csts_.push_back({bare(name), true, 0.0, f});
+  return static_cast<int>(csts_.size()) - 1;
+}
+
+void System::add_def(int dom, const std::string& text) {
+  std::string l, r;
+  if (!split_eq(text, l, r)) throw KdError(KD_ERR_ARG, "= needed for definitions");
+  if (dom < 0) {
+    for (int dd = dom_min; dd <= dom_max; dd++) add_def(dd, text);
+    return;
+  }
+  DefInfo df{bare(l), dom, parse_ope(*this, dom, r, -1)};
+  defs_.push_back(df);
+}
+
+void System::add_eq_inside(int dom, const std::string& text) {
+  std::string l, r;
+  if (!split_eq(text, l, r)) throw KdError(KD_ERR_ARG, "= needed for equations");
+  Equation eq;
+  eq.kind = Equation::INSIDE;
+  eq.dom = dom;
+  eq.order = 2;
+  eq.text = text;
+  eq.lhs = (bare(r) == "0") ? parse_ope(*this, dom, l, -1)
+                            : std::make_shared<OpeSubEq>(dom, parse_ope(*this, dom, l, -1), parse_ope(*this, dom, r, -1));
+  eqs_.push_back(eq);
+  nbr_conditions_ = -1;
+}
+
+void System::add_eq_bc(int dom, int bound, const std::string& text) {
+  std::string l, r;
+  if (!split_eq(text, l, r)) throw KdError(KD_ERR_ARG, "= needed for equations");
+  if (!sp->dom(dom).has_boundary(bound)) throw KdError(KD_ERR_ARG, "domain has no such boundary");
+  Equation eq;
+  eq.kind = Equation::BC;
+  eq.dom = dom;
+  eq.bound = bound;
+  eq.text = text;
+  eq.lhs = (bare(r) == "0") ? parse_ope(*this, dom, l, bound)
+                            : std::make_shared<OpeSubEq>(dom, parse_ope(*this, dom, l, bound),
+                                                         parse_ope(*this, dom, r, bound));
+  eqs_.push_back(eq);
+  nbr_conditions_ = -1;
+}
+
+void System::add_eq_matching(int dom, int bound, const std::string& text) {
+  Equation eq;
+  eq.kind = Equation::MATCHING;
+  eq.dom = dom;
+  eq.bound = bound;
+  eq.text = text;
+  sp->dom(dom).find_other_dom(dom, bound, eq.other_dom, eq.other_bound);
+  if (eq.other_dom < dom_min || eq.other_dom > dom_max) throw KdError(KD_ERR_ARG, "matching outside the system");
+  std::string l, r;
+  if (split_eq(text, l, r)) {
+    eq.lhs = parse_ope(*this, dom, l, bound);
+    eq.rhs = parse_ope(*this, eq.other_dom, r, eq.other_bound);
+  } else {
+    eq.lhs = parse_ope(*this, dom, text, bound);
+    eq.rhs = parse_ope(*this, eq.other_dom, text, eq.other_bound);
+  }
+  eqs_.push_back(eq);
+  nbr_conditions_ = -1;
+}
+
+CsrTable System::upload_rows(const std::vector<SparseRow>& rows) {
+  std::vector<int> rp(rows.size() + 1, 0), idx;
+  std::vector<double> w;
+  for (size_t r = 0; r < rows.size(); r++) {
+    for (auto& e : rows[r].e) {
+      idx.push_back(e.first);
+      w.push_back(e.second);
+    }
+    rp[r + 1] = static_cast<int>(idx.size());
+  }
+  CsrTable t;
+  t.rowptr = ctx->table(rp);
+  t.idx = ctx->table(idx);
+  t.w = ctx->dtable(w);
+  t.nrows = static_cast<int>(rows.size());
+  return t;
+}
+
+const CsrTable& System::export_table(const Domain& d, const Base& b, int kind, int arg) {
+  std::vector<int> key = {d.num, kind, arg, b.p};
+  key.insert(key.end(), b.t.begin(), b.t.end());
+  key.insert(key.end(), b.r.begin(), b.r.end());
+  auto it = tables_.find(key);
+  if (it != tables_.end()) return it->second;
+  std::vector<SparseRow> rows;
+  if (kind == 0) d.export_tau_rows(b, 0, arg, rows);
+  else d.export_tau_boundary_rows(b, 0, arg, rows);
+  tables_[key] = upload_rows(rows);
+  return tables_[key];
+}
+
+int System::count_rows(const Equation& eq, const Term& t) {
+  if (t.is_double) throw KdError(KD_ERR_UNSUPPORTED, "equation residual must be a field");
+  int n = 0;
+  const Domain& d = sp->dom(eq.dom);
+  for (auto& v : t.vt) {
+    if (!v.base.def) throw KdError(KD_ERR_STATE, "residual without a defined basis: " + eq.text);
+    const CsrTable& tab = (eq.kind == Equation::INSIDE) ? export_table(d, v.base, 0, eq.order)
+                                                        : export_table(d, v.base, 1, eq.bound);
+    n += tab.nrows;
+  }
+  return n;
+}
+
+// Writes the export rows of every component of t (value or tangent).
+void System::export_term(const Equation& eq, const Term& t, bool der, int side_dom, int side_bound, double* out,
+                         long long osf, long long osr, int batch, double alpha, bool accumulate) {
+  const Domain& d = sp->dom(side_dom);
+  const auto& comps = der ? t.dt : t.vt;
+  long long row = 0;
+  for (size_t c = 0; c < comps.size(); c++) {
+    const DVal& v = comps[c];
+    // rows of this component are fixed by the value's basis (n_cond)
+    const Base& bval = t.vt[c].base;
+    const CsrTable& tv = (eq.kind == Equation::INSIDE) ? export_table(d, bval, 0, eq.order)
+                                                       : export_table(d, bval, 1, side_bound);
+    if (!v.zero) {
+      if (!v.base.def) throw KdError(KD_ERR_STATE, "exported field without basis: " + eq.text);
+      v.coef();
+      const CsrTable& tab = (eq.kind == Equation::INSIDE) ? export_table(d, v.base, 0, eq.order)
+                                                          : export_table(d, v.base, 1, side_bound);
+      if (tab.nrows != tv.nrows) throw KdError(KD_ERR_STATE, "tangent basis changes the number of conditions");
+      long long in_stride = (v.batch == 1 && batch > 1) ? 0 : v.ncoefs();
+      cuda_check(launch_gather_csr(v.cf, in_stride, batch, tab.nrows, tab.rowptr, tab.idx, tab.w, out + row * osr,
+                                   osf, osr, alpha, accumulate ? 1 : 0, ctx->stream()),
+                 "export gather");
+      ctx->launches++;
+    }
+    row += tv.nrows;
+  }
+}
+
+void System::compute_unknowns() {
+  col0_.clear();
+  nunk_.clear();
+  int n = static_cast<int>(vdoubles_.size());
+  for (size_t v = 0; v < vars_.size(); v++)
+    for (int dd = dom_min; dd <= dom_max; dd++) {
+      std::vector<SparseRow> pats;
+      sp->dom(dd).unknown_patterns(vars_[v].f->d[dd].base, 0, pats);
+      col0_[{static_cast<int>(v), dd}] = n;
+      nunk_[{static_cast<int>(v), dd}] = static_cast<int>(pats.size());
+      n += static_cast<int>(pats.size());
+    }
+  nbr_unknowns_ = n;
+}
+
+int System::nbr_unknowns() {
+  if (nbr_unknowns_ < 0) compute_unknowns();
+  return nbr_unknowns_;
+}
+
+void System::residual(double* d_F) {
+  ctx->scratch().reset();
+  EvalState st;
+  st.sys = this;
+  st.with_der = false;
+  std::vector<Term> lhs(eqs_.size()), rhs(eqs_.size());
+  for (size_t i = 0; i < eqs_.size(); i++) {
+    lhs[i] = eqs_[i].lhs->action(st);
+    if (eqs_[i].kind == Equation::MATCHING) rhs[i] = eqs_[i].rhs->action(st);
+  }
+  if (nbr_conditions_ < 0) {
+    int row = 0;
+    for (size_t i = 0; i < eqs_.size(); i++) {
+      eqs_[i].n_cond = count_rows(eqs_[i], lhs[i]);
+      eqs_[i].row0 = row;
+      row += eqs_[i].n_cond;
+    }
+    nbr_conditions_ = row;
+  }
+  if (!d_F) return;
+  cuda_check(cudaMemsetAsync(d_F, 0, sizeof(double) * nbr_conditions_, ctx->stream()), "memset F");
+  for (size_t i = 0; i < eqs_.size(); i++) {
+    Equation& eq = eqs_[i];
+    double* out = d_F + eq.row0;
+    if (eq.kind == Equation::MATCHING) {
+      export_term(eq, lhs[i], false, eq.dom, eq.bound, out, 0, 1, 1, 1.0, false);
+      export_term(eq, rhs[i], false, eq.other_dom, eq.other_bound, out, 0, 1, 1, -1.0, true);
+    } else {
+      export_term(eq, lhs[i], false, eq.dom, eq.bound, out, 0, 1, 1, 1.0, false);
+    }
+  }
+}
+
+const double* System::seed_block(int var, int dom, int& B, Base& base) {
+  base = vars_[var].f->d[dom].base;
+  std::vector<SparseRow> pats;
+  const Domain& d = sp->dom(dom);
+  d.unknown_patterns(base, 0, pats);
+  B = static_cast<int>(pats.size());
+  auto key = std::make_pair(var, dom);
+  auto it = seeds_.find(key);
+  if (it != seeds_.end()) return it->second;
+  std::vector<double> block(static_cast<size_t>(B) * d.ncoefs(), 0.0);
+  for (int s = 0; s < B; s++)
+    for (auto& e : pats[s].e) block[static_cast<size_t>(s) * d.ncoefs() + e.first] = e.second;
+  const double* p = ctx->dtable(block);
+  seeds_[key] = p;
+  return p;
+}
+
+void System::jacobian(double* d_J, long long ld) {
+  int N = nbr_unknowns();
+  if (nbr_conditions_ < 0) residual(nullptr);
+  if (nbr_conditions_ != N) {
+    std::ostringstream os;
+    os << "Number of unknowns (" << N << ") is different from the number of equations (" << nbr_conditions_ << ")";
+    throw KdError(KD_ERR_STATE, os.str());
+  }
+  if (!vdoubles_.empty()) throw KdError(KD_ERR_UNSUPPORTED, "double unknowns are not supported yet");
+  cuda_check(cudaMemsetAsync(d_J, 0, sizeof(double) * ld * N, ctx->stream()), "memset J");
+  for (size_t v = 0; v < vars_.size(); v++)
+    for (int dd = dom_min; dd <= dom_max; dd++) {
+      int B;
+      Base base;
+      const double* seeds = seed_block(static_cast<int>(v), dd, B, base);
+      if (B == 0) continue;
+      ctx->scratch().reset();
+      EvalState st;
+      st.sys = this;
+      st.with_der = true;
+      st.B = B;
+      st.seed_var = static_cast<int>(v);
+      st.seed_dom = dd;
+      st.seed = DVal::from_coef(ctx, &sp->dom(dd), B, seeds, base);
+      int col0 = col0_[{static_cast<int>(v), dd}];
+      double* Jblock = d_J + static_cast<long long>(col0) * ld;
+      for (auto& eq : eqs_) {
+        if (!eq.take_into_account(dd)) continue;
+        if (eq.kind != Equation::MATCHING || dd == eq.dom) {
+          Term t = eq.lhs->action(st);
+          export_term(eq, t, true, eq.dom, eq.bound, Jblock + eq.row0, ld, 1, B, 1.0, true);
+        }
+        if (eq.kind == Equation::MATCHING && dd == eq.other_dom) {
+          Term t = eq.rhs->action(st);
+          export_term(eq, t, true, eq.other_dom, eq.other_bound, Jblock + eq.row0, ld, 1, B, -1.0, true);
+        }
+      }
+    }
+}
+
+void System::update_from_x(const double* d_x) {
+  int N = nbr_unknowns();
+  (void)N;
+  ctx->scratch().reset();
+  // doubles first
+  if (!vdoubles_.empty()) {
+    std::vector<double> hx(vdoubles_.size());
+    cuda_check(cudaMemcpyAsync(hx.data(), d_x, sizeof(double) * hx.size(), cudaMemcpyDeviceToHost, ctx->stream()),
+               "D2H x");
+    cuda_check(cudaStreamSynchronize(ctx->stream()), "sync");
+    for (size_t i = 0; i < vdoubles_.size(); i++) vdoubles_[i].value -= hx[i];
+  }
+  for (size_t v = 0; v < vars_.size(); v++) {
+    Field* f = vars_[v].f;
+    for (int dd = 0; dd < sp->ndom(); dd++) {
+      const Domain& d = sp->dom(dd);
+      DVal old = f->val(dd);
+      if (dd < dom_min || dd > dom_max) {
+        // old - old: the reference's update leaves exact zeros outside the system
+        if (!old.zero) {
+          DVal z = old - old;
+          f->assign(dd, z);
+        }
+        continue;
+      }
+      auto key = std::make_pair(static_cast<int>(v), dd);
+      auto it = xmaps_.find(key);
+      if (it == xmaps_.end()) {
+        std::vector<SparseRow> rows;
+        int used = d.affecte_tau_map(f->d[dd].base, 0, rows);
+        if (used != nunk_[key]) throw KdError(KD_ERR_STATE, "affecte_tau consumes a different number of unknowns");
+        xmaps_[key] = upload_rows(rows);
+        it = xmaps_.find(key);
+      }
+      double* cf = ctx->scratch().alloc_doubles(d.ncoefs());
+      const CsrTable& t = it->second;
+      cuda_check(launch_gather_csr(d_x + col0_[key], 0, 1, t.nrows, t.rowptr, t.idx, t.w, cf, 0, 1, 1.0, 0,
+                                   ctx->stream()),
+                 "affecte_tau gather");
+      ctx->launches++;
+      DVal nv = DVal::from_coef(ctx, &d, 1, cf, f->d[dd].base);
+      DVal res = old - nv;
+      f->assign(dd, res);
+    }
+  }
+  cuda_check(cudaStreamSynchronize(ctx->stream()), "sync after update");
+}
+
+void System::jx(const double* d_x, double* d_out) {
+  (void)d_x;
+  (void)d_out;
+  throw KdError(KD_ERR_UNSUPPORTED, "matrix-free J*x is served by the assembled Jacobian");
+}
+
+}  // namespace kd

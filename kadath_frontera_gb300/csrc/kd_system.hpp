@@ -1,0 +1,182 @@
+// System_of_eqs (include/system_of_eqs.hpp:54) on the GPU: registry of
+// unknowns, constants, definitions and equations; residual F(u)
+// (sec_member, src/System_of_eqs/solver.cpp:49); Jacobian assembly that
+// replaces the do_col_J column loop (solver.cpp:120) by one batched tangent
+// pass per (unknown field, domain); and the update x -> fields
+// (xx_to_vars, src/System_of_eqs/system_of_eqs.cpp:597).
+#pragma once
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "kd_term.hpp"
+
+namespace kd {
+
+// A user field (Kadath Scalar): one Val_domain per domain, kept in device
+// memory owned by the field.
+class Field {
+ public:
+  Field(Context* ctx, const Space* sp);
+  ~Field();
+  Field(const Field&) = delete;
+  Field& operator=(const Field&) = delete;
+
+  struct PerDom {
+    bool zero = true;
+    bool in_conf = false, in_coef = false;
+    double* c = nullptr;
+    double* cf = nullptr;
+    Base base;
+  };
+  Context* ctx;
+  const Space* sp;
+  std::vector<PerDom> d;
+
+  DVal val(int dom) const;
+  void assign(int dom, const DVal& v);       // copies v's representations
+  void set_conf_host(int dom, const double* values);
+  void set_value(double v);                   // Scalar = v (conf)
+  void std_base();
+  // Host read-back in the requested representation (computes it if needed).
+  void get_conf_host(int dom, double* out);
+  void get_coef_host(int dom, double* out);
+};
+
+struct CsrTable {
+  const int* rowptr = nullptr;
+  const int* idx = nullptr;
+  const double* w = nullptr;
+  int nrows = 0;
+};
+
+class System;
+
+// State of one evaluation pass (residual or one batched Jacobian block).
+struct EvalState {
+  System* sys = nullptr;
+  bool with_der = false;
+  int B = 1;               // number of tangent seeds
+  int seed_var = -1;       // field unknown being seeded (-1: a double unknown)
+  int seed_dom = -1;
+  int seed_var_double = -1;
+  DVal seed;               // batch-B coefficient patterns
+  std::map<std::pair<int, int>, Term> def_cache;
+
+  Term var_term(int which, int dom);
+  Term var_double_term(int which, int dom);
+  Term cst_term(int which, int dom);
+  Term def_term(int which, int dom);
+};
+
+struct Equation {
+  enum Kind { INSIDE, BC, MATCHING };
+  Kind kind;
+  int dom, bound = -1, other_dom = -1, other_bound = -1;
+  int order = 2;
+  std::string text;
+  OpePtr lhs, rhs;
+  int n_cond = -1;
+  int row0 = 0;
+  bool take_into_account(int d) const {
+    return d == dom || (kind == MATCHING && d == other_dom);
+  }
+};
+
+class System {
+ public:
+  System(Context* ctx, const Space* sp, int dom_min, int dom_max);
+
+  Context* ctx;
+  const Space* sp;
+  int dom_min, dom_max;
+  int ndom() const { return dom_max - dom_min + 1; }
+
+  // registry (system_of_eqs.cpp:284-440, add_eq.cpp)
+  int add_var(const std::string& name, Field* f);
+  int add_var_double(const std::string& name, double value);
+  int add_cst(const std::string& name, double value);
+  int add_cst_field(const std::string& name, Field* f);
+  void add_def(int dom, const std::string& text);
+  void add_eq_inside(int dom, const std::string& eq);
+  void add_eq_bc(int dom, int bound, const std::string& eq);
+  void add_eq_matching(int dom, int bound, const std::string& eq);
+
+  int find_var(const std::string& n) const;
+  int find_var_double(const std::string& n) const;
+  int find_cst(const std::string& n) const;
+  int find_def(const std::string& n, int dom) const;
+
+  double var_double(int i) const { return vdoubles_[i].value; }
+  void set_var_double(int i, double v) { vdoubles_[i].value = v; }
+
+  // Sizes (valid after the first residual evaluation).
+  int nbr_unknowns();
+  int nbr_conditions() const { return nbr_conditions_; }
+  int n_equations() const { return static_cast<int>(eqs_.size()); }
+  const Equation& equation(int i) const { return eqs_[i]; }
+
+  // F(u) into a device vector of nbr_conditions doubles.
+  void residual(double* d_F);
+  // Column-major dense Jacobian (ld >= nbr_conditions) on the device.
+  void jacobian(double* d_J, long long ld);
+  // J * x for a device vector x (System_of_eqs::do_JX, solver.cpp:87).
+  void jx(const double* d_x, double* d_out);
+  // var = old - (fields built from x)  (do_newton's update, src_par/do_newton.cpp:397-414)
+  void update_from_x(const double* d_x);
+
+  struct VarInfo {
+    std::string name;
+    Field* f;
+  };
+  struct VarDouble {
+    std::string name;
+    double value;
+  };
+  struct CstInfo {
+    std::string name;
+    bool is_field;
+    double value;
+    Field* f;
+  };
+  struct DefInfo {
+    std::string name;
+    int dom;
+    OpePtr ope;
+  };
+  const std::vector<VarInfo>& vars() const { return vars_; }
+
+  // Column offset of the unknowns of (var, dom); valid after nbr_unknowns().
+  int col_offset(int var, int dom) const { return col0_.at({var, dom}); }
+  int n_unknowns_of(int var, int dom) const { return nunk_.at({var, dom}); }
+
+  // Export table of a residual value (cached by domain, basis, kind).
+  const CsrTable& export_table(const Domain& d, const Base& b, int kind, int order_or_bound);
+
+  long long assembly_launches = 0;
+
+ private:
+  friend struct EvalState;
+  std::vector<VarInfo> vars_;
+  std::vector<VarDouble> vdoubles_;
+  std::vector<CstInfo> csts_;
+  std::vector<DefInfo> defs_;
+  std::vector<Equation> eqs_;
+  int nbr_conditions_ = -1;
+  int nbr_unknowns_ = -1;
+  std::map<std::pair<int, int>, int> col0_, nunk_;
+  std::map<std::pair<int, int>, const double*> seeds_;  // device seed blocks
+  std::map<std::pair<int, int>, CsrTable> xmaps_;      // affecte_tau maps
+  std::map<std::vector<int>, CsrTable> tables_;
+
+  void compute_unknowns();
+  void apply(Equation& eq, EvalState& st, Term& lhs, Term& rhs, bool do_lhs, bool do_rhs);
+  int count_rows(const Equation& eq, const Term& t);
+  void export_term(const Equation& eq, const Term& t, bool der, int side_dom, int side_bound, double* out,
+                   long long osf, long long osr, int batch, double alpha, bool accumulate);
+  CsrTable upload_rows(const std::vector<SparseRow>& rows);
+  const double* seed_block(int var, int dom, int& B, Base& base);
+};
+
+}  // namespace kd

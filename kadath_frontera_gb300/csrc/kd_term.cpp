@@ -1,0 +1,624 @@
+#include "kd_term.hpp"
+
+#include <cmath>
+#include <cstdlib>
+
+#include "kd_system.hpp"
+
+namespace kd {
+
+// ----------------------------------------------------------- Term algebra --
+// src/Term_eq/term_eq_math.cpp.  A tangent that is exactly zero (a double
+// constant's der_d = 0, or an untouched field) is skipped: adding or
+// multiplying it only produces exact zeros.
+
+namespace {
+
+bool dd_zero(const Term& t) { return !t.has_dd || t.dd == 0.0; }
+
+void check_dom(const Term& a, const Term& b) {
+  if (a.dom != b.dom) throw KdError(KD_ERR_ARG, "Term_eq operation across domains");
+}
+
+Term tensor_like(const Term& t) {
+  Term r;
+  r.dom = t.dom;
+  r.valence = t.valence;
+  return r;
+}
+
+int ncomp(const Term& t) { return static_cast<int>(t.vt.size()); }
+
+void check_valence(const Term& a, const Term& b) {
+  if (a.vt.size() != b.vt.size())
+    throw KdError(KD_ERR_UNSUPPORTED, "tensor operation between different valences");
+}
+
+}  // namespace
+
+Term operator+(const Term& a, const Term& b) {
+  check_dom(a, b);
+  bool do_der = a.has_der() && b.has_der();
+  if (a.is_double && b.is_double) {
+    Term r = Term::dbl(a.dom, a.vd + b.vd);
+    if (do_der) {
+      r.has_dd = true;
+      r.dd = a.dd + b.dd;
+    }
+    return r;
+  }
+  if (a.is_double || b.is_double) {
+    const Term& t = a.is_double ? b : a;
+    const Term& d = a.is_double ? a : b;
+    Term r = tensor_like(t);
+    for (auto& v : t.vt) r.vt.push_back(v + d.vd);
+    if (do_der) {
+      r.has_dt = true;
+      for (int i = 0; i < ncomp(t); i++) r.dt.push_back(d.dd == 0.0 ? t.dt[i] : t.dt[i] + d.dd);
+    }
+    return r;
+  }
+  check_valence(a, b);
+  Term r = tensor_like(a);
+  for (int i = 0; i < ncomp(a); i++) r.vt.push_back(a.vt[i] + b.vt[i]);
+  if (do_der) {
+    r.has_dt = true;
+    for (int i = 0; i < ncomp(a); i++) r.dt.push_back(a.dt[i] + b.dt[i]);
+  }
+  return r;
+}
+
+Term operator-(const Term& a, const Term& b) {
+  check_dom(a, b);
+  bool do_der = a.has_der() && b.has_der();
+  if (a.is_double && b.is_double) {
+    Term r = Term::dbl(a.dom, a.vd - b.vd);
+    if (do_der) {
+      r.has_dd = true;
+      r.dd = a.dd - b.dd;
+    }
+    return r;
+  }
+  if (b.is_double) {
+    Term r = tensor_like(a);
+    for (auto& v : a.vt) r.vt.push_back(v - b.vd);
+    if (do_der) {
+      r.has_dt = true;
+      for (int i = 0; i < ncomp(a); i++) r.dt.push_back(b.dd == 0.0 ? a.dt[i] : a.dt[i] - b.dd);
+    }
+    return r;
+  }
+  if (a.is_double) {
+    Term r = tensor_like(b);
+    for (auto& v : b.vt) r.vt.push_back(a.vd - v);
+    if (do_der) {
+      r.has_dt = true;
+      for (int i = 0; i < ncomp(b); i++) r.dt.push_back(a.dd == 0.0 ? -b.dt[i] : a.dd - b.dt[i]);
+    }
+    return r;
+  }
+  check_valence(a, b);
+  Term r = tensor_like(a);
+  for (int i = 0; i < ncomp(a); i++) r.vt.push_back(a.vt[i] - b.vt[i]);
+  if (do_der) {
+    r.has_dt = true;
+    for (int i = 0; i < ncomp(a); i++) r.dt.push_back(a.dt[i] - b.dt[i]);
+  }
+  return r;
+}
+
+Term operator-(const Term& a) {
+  // Term_eq operator-(aa) = -1. * aa
+  if (a.is_double) {
+    Term r = Term::dbl(a.dom, -a.vd);
+    if (a.has_dd) {
+      r.has_dd = true;
+      r.dd = -a.dd;
+    }
+    return r;
+  }
+  Term r = tensor_like(a);
+  for (auto& v : a.vt) r.vt.push_back(v * -1.0);
+  if (a.has_dt) {
+    r.has_dt = true;
+    for (auto& v : a.dt) r.dt.push_back(v * -1.0);
+  }
+  return r;
+}
+
+Term operator*(const Term& a, const Term& b) {
+  check_dom(a, b);
+  bool do_der = a.has_der() && b.has_der();
+  if (a.is_double && b.is_double) {
+    Term r = Term::dbl(a.dom, a.vd * b.vd);
+    if (do_der) {
+      r.has_dd = true;
+      r.dd = a.dd * b.vd + a.vd * b.dd;
+    }
+    return r;
+  }
+  if (a.is_double || b.is_double) {
+    const Term& t = a.is_double ? b : a;
+    const Term& d = a.is_double ? a : b;
+    Term r = tensor_like(t);
+    for (auto& v : t.vt) r.vt.push_back(v * d.vd);
+    if (do_der) {
+      r.has_dt = true;
+      for (int i = 0; i < ncomp(t); i++) {
+        DVal part = t.dt[i] * d.vd;
+        if (!dd_zero(d)) part = part + t.vt[i] * d.dd;
+        r.dt.push_back(part);
+      }
+    }
+    return r;
+  }
+  if (a.vt.size() != 1 && b.vt.size() != 1)
+    throw KdError(KD_ERR_UNSUPPORTED, "product of two non-scalar tensors: use scal()");
+  const Term& s = (a.vt.size() == 1) ? a : b;
+  const Term& t = (a.vt.size() == 1) ? b : a;
+  bool s_first = (&s == &a);
+  Term r = tensor_like(t);
+  for (int i = 0; i < ncomp(t); i++) r.vt.push_back(s_first ? s.vt[0] * t.vt[i] : t.vt[i] * s.vt[0]);
+  if (do_der) {
+    r.has_dt = true;
+    for (int i = 0; i < ncomp(t); i++) {
+      // der = a' b + a b'
+      const DVal& av = s_first ? s.vt[0] : t.vt[i];
+      const DVal& bv = s_first ? t.vt[i] : s.vt[0];
+      const DVal& ad = s_first ? s.dt[0] : t.dt[i];
+      const DVal& bd = s_first ? t.dt[i] : s.dt[0];
+      r.dt.push_back(ad * bv + av * bd);
+    }
+  }
+  return r;
+}
+
+Term operator/(const Term& a, const Term& b) {
+  check_dom(a, b);
+  bool do_der = a.has_der() && b.has_der();
+  if (a.is_double && b.is_double) {
+    Term r = Term::dbl(a.dom, a.vd / b.vd);
+    if (do_der) {
+      r.has_dd = true;
+      r.dd = (a.dd * b.vd - a.vd * b.dd) / (b.vd * b.vd);
+    }
+    return r;
+  }
+  if (b.is_double) {
+    Term r = tensor_like(a);
+    for (auto& v : a.vt) r.vt.push_back(v / b.vd);
+    if (do_der) {
+      r.has_dt = true;
+      for (int i = 0; i < ncomp(a); i++) {
+        DVal num = a.dt[i] * b.vd;
+        if (!dd_zero(b)) num = num - a.vt[i] * b.dd;
+        r.dt.push_back(num / (b.vd * b.vd));
+      }
+    }
+    return r;
+  }
+  if (b.vt.size() != 1) throw KdError(KD_ERR_UNSUPPORTED, "division by a non-scalar tensor");
+  if (a.is_double) {
+    Term r = tensor_like(b);
+    r.vt.push_back(a.vd / b.vt[0]);
+    if (do_der) {
+      r.has_dt = true;
+      DVal num = (dd_zero(a) ? DVal::zeros(b.vt[0].ctx, b.vt[0].dom, 1) : b.vt[0] * a.dd) - b.dt[0] * a.vd;
+      r.dt.push_back(num / (b.vt[0] * b.vt[0]));
+    }
+    return r;
+  }
+  Term r = tensor_like(a);
+  for (int i = 0; i < ncomp(a); i++) r.vt.push_back(a.vt[i] / b.vt[0]);
+  if (do_der) {
+    r.has_dt = true;
+    DVal bb = b.vt[0] * b.vt[0];
+    for (int i = 0; i < ncomp(a); i++) r.dt.push_back((a.dt[i] * b.vt[0] - a.vt[i] * b.dt[0]) / bb);
+  }
+  return r;
+}
+
+Term term_pow(const Term& a, int n) {
+  // pow(Term_eq, int), term_eq_math.cpp:547
+  if (n > 0) {
+    Term r = a;
+    for (int i = 1; i < n; i++) r = r * a;
+    return r;
+  }
+  if (a.is_double) {
+    Term one = Term::dbl_der(a.dom, 1.0, 0.0);
+    Term r = one;
+    for (int i = 0; i < -n; i++) r = r / a;
+    return r;
+  }
+  Term one = tensor_like(a);
+  DVal o = DVal::constant(a.vt[0].ctx, a.vt[0].dom, 1.0);
+  o.base = a.vt[0].dom->std_base();
+  one.vt.push_back(o);
+  one.has_dt = true;
+  one.dt.push_back(DVal::zeros(a.vt[0].ctx, a.vt[0].dom, 1));
+  Term r = one;
+  for (int i = 0; i < -n; i++) r = r / a;
+  return r;
+}
+
+// --------------------------------------------------------------- Ope tree --
+namespace {
+
+Term comp_by_comp(const Term& t, const std::function<DVal(const DVal&)>& f) {
+  if (t.is_double) throw KdError(KD_ERR_UNSUPPORTED, "operator only defined for tensor terms");
+  Term r = tensor_like(t);
+  for (auto& v : t.vt) r.vt.push_back(v.zero ? v : f(v));
+  if (t.has_dt) {
+    r.has_dt = true;
+    for (auto& v : t.dt) r.dt.push_back(v.zero ? v : f(v));
+  }
+  return r;
+}
+
+class OpeBin : public Ope {
+ public:
+  OpeBin(int dom, char op, OpePtr a, OpePtr b) : Ope(dom), op(op), a(std::move(a)), b(std::move(b)) {}
+  Term action(EvalState& st) const override {
+    Term x = a->action(st);
+    Term y = b->action(st);
+    switch (op) {
+      case '+': return x + y;
+      case '-': return x - y;
+      case '*': return x * y;
+      default: return x / y;
+    }
+  }
+  char op;
+  OpePtr a, b;
+};
+
+class OpeMinus : public Ope {
+ public:
+  OpeMinus(int dom, OpePtr a) : Ope(dom), a(std::move(a)) {}
+  Term action(EvalState& st) const override { return -a->action(st); }
+  OpePtr a;
+};
+
+class OpePow : public Ope {
+ public:
+  OpePow(int dom, int n, OpePtr a) : Ope(dom), n(n), a(std::move(a)) {}
+  Term action(EvalState& st) const override { return term_pow(a->action(st), n); }
+  int n;
+  OpePtr a;
+};
+
+// Unary operators acting component by component on value and tangent.
+class OpeUnary : public Ope {
+ public:
+  enum Kind { LAP, DN, DR, MULTR, DIVR, DIVSINT, MULTSINT, DIVCOST };
+  OpeUnary(int dom, Kind k, int bound, OpePtr a) : Ope(dom), kind(k), bound(bound), a(std::move(a)) {}
+  Term action(EvalState& st) const override {
+    Term t = a->action(st);
+    switch (kind) {
+      case LAP: return comp_by_comp(t, [](const DVal& v) { return laplacian(v); });
+      case DN: {
+        int b = bound;
+        return comp_by_comp(t, [b](const DVal& v) { return der_normal(v, b); });
+      }
+      case DR: return comp_by_comp(t, [](const DVal& v) { return der_r(v); });
+      case MULTR: return comp_by_comp(t, [](const DVal& v) { return mult_r(v); });
+      case DIVR: return comp_by_comp(t, [](const DVal& v) { return div_r(v); });
+      case DIVSINT: return comp_by_comp(t, [](const DVal& v) { return div_sin_theta(v); });
+      case MULTSINT: return comp_by_comp(t, [](const DVal& v) { return mult_sin_theta(v); });
+      default: return comp_by_comp(t, [](const DVal& v) { return div_cos_theta(v); });
+    }
+  }
+  Kind kind;
+  int bound;
+  OpePtr a;
+};
+
+// exp / sqrt / log of a scalar (src/Ope_eq/ope_exp.cpp, ope_sqrt.cpp, ope_log.cpp)
+class OpeFunc : public Ope {
+ public:
+  enum Kind { EXP, SQRT, LOG };
+  OpeFunc(int dom, Kind k, OpePtr a) : Ope(dom), kind(k), a(std::move(a)) {}
+  Term action(EvalState& st) const override {
+    Term t = a->action(st);
+    if (t.is_double) {
+      double v = kind == EXP ? std::exp(t.vd) : kind == SQRT ? std::sqrt(t.vd) : std::log(t.vd);
+      Term r = Term::dbl(t.dom, v);
+      if (t.has_dd) {
+        r.has_dd = true;
+        r.dd = kind == EXP ? t.dd * std::exp(t.vd) : kind == SQRT ? t.dd / 2. / std::sqrt(t.vd) : t.dd / t.vd;
+      }
+      return r;
+    }
+    if (t.vt.size() != 1) throw KdError(KD_ERR_UNSUPPORTED, "exp/sqrt/log only defined for a scalar");
+    Term r = tensor_like(t);
+    const DVal& v = t.vt[0];
+    if (kind == EXP) r.vt.push_back(vd_exp(v));
+    else if (kind == SQRT) r.vt.push_back(v.zero ? v : vd_sqrt(v));
+    else r.vt.push_back(vd_log(v));
+    if (t.has_dt) {
+      r.has_dt = true;
+      const DVal& d = t.dt[0];
+      if (kind == EXP) r.dt.push_back(d * vd_exp(v));
+      else if (kind == SQRT) r.dt.push_back(d.zero ? d : d / 2. / vd_sqrt(v));
+      else r.dt.push_back(d / v);
+    }
+    return r;
+  }
+  Kind kind;
+  OpePtr a;
+};
+
+// grad(scalar): Cartesian components der_abs(1..3) (Domain::grad_term_eq)
+class OpeGrad : public Ope {
+ public:
+  OpeGrad(int dom, OpePtr a) : Ope(dom), a(std::move(a)) {}
+  Term action(EvalState& st) const override {
+    Term t = a->action(st);
+    if (t.is_double || t.vt.size() != 1) throw KdError(KD_ERR_UNSUPPORTED, "grad only defined for scalars");
+    Term r;
+    r.dom = t.dom;
+    r.valence = 1;
+    for (int i = 1; i <= 3; i++) r.vt.push_back(t.vt[0].der_abs(i));
+    if (t.has_dt) {
+      r.has_dt = true;
+      for (int i = 1; i <= 3; i++) r.dt.push_back(t.dt[0].der_abs(i));
+    }
+    return r;
+  }
+  OpePtr a;
+};
+
+// scal(a, b): flat scalar product of two Cartesian vectors (Ope_scal)
+class OpeScal : public Ope {
+ public:
+  OpeScal(int dom, OpePtr a, OpePtr b) : Ope(dom), a(std::move(a)), b(std::move(b)) {}
+  Term action(EvalState& st) const override {
+    Term x = a->action(st);
+    Term y = b->action(st);
+    if (x.vt.size() != 3 || y.vt.size() != 3) throw KdError(KD_ERR_UNSUPPORTED, "scal needs two vectors");
+    Term r;
+    r.dom = x.dom;
+    r.valence = 0;
+    DVal v = x.vt[0] * y.vt[0];
+    for (int i = 1; i < 3; i++) v = v + x.vt[i] * y.vt[i];
+    r.vt.push_back(v);
+    if (x.has_dt && y.has_dt) {
+      r.has_dt = true;
+      DVal d = x.dt[0] * y.vt[0] + x.vt[0] * y.dt[0];
+      for (int i = 1; i < 3; i++) d = d + (x.dt[i] * y.vt[i] + x.vt[i] * y.dt[i]);
+      r.dt.push_back(d);
+    }
+    return r;
+  }
+  OpePtr a, b;
+};
+
+// partial_i (Cartesian derivative of each component), i = x, y, z
+class OpePartial : public Ope {
+ public:
+  OpePartial(int dom, int i, OpePtr a) : Ope(dom), i(i), a(std::move(a)) {}
+  Term action(EvalState& st) const override {
+    int ii = i;
+    return comp_by_comp(a->action(st), [ii](const DVal& v) { return v.der_abs(ii); });
+  }
+  int i;
+  OpePtr a;
+};
+
+class OpeLeaf : public Ope {
+ public:
+  enum Kind { VAR, VAR_DOUBLE, CST, HARD, DEF };
+  OpeLeaf(int dom, Kind k, int which, double v = 0.0) : Ope(dom), kind(k), which(which), val(v) {}
+  Term action(EvalState& st) const override;
+  Kind kind;
+  int which;
+  double val;
+};
+
+Term OpeLeaf::action(EvalState& st) const {
+  switch (kind) {
+    case VAR: return st.var_term(which, dom);
+    case VAR_DOUBLE: return st.var_double_term(which, dom);
+    case CST: return st.cst_term(which, dom);
+    case DEF: return st.def_term(which, dom);
+    default: {
+      Term t = Term::dbl(dom, val);
+      if (st.with_der) {
+        t.has_dd = true;
+        t.dd = 0.0;
+      }
+      return t;
+    }
+  }
+}
+
+// ----------------------------------------------------------------- parser --
+int count_char(const std::string& s, char c) {
+  int n = 0;
+  for (char x : s)
+    if (x == c) n++;
+  return n;
+}
+
+bool balanced(const std::string& s) { return count_char(s, '(') == count_char(s, ')'); }
+
+// get_parts (src/Utilities/name_tools.cpp:150): split at the place-th
+// occurrence of sep counted from the END of the string.
+bool get_parts(const std::string& in, std::string& first, std::string& second, char sep, int place) {
+  int nfound = -1;
+  int pos = static_cast<int>(in.size()) - 1;
+  bool fin = false;
+  while (!fin) {
+    if (pos < 0) break;
+    if (in[pos] == sep) nfound++;
+    pos--;
+    if (nfound == place) fin = true;
+    if (pos == -1) fin = true;
+  }
+  if (pos == -1 && nfound != place) {
+    first.clear();
+    second = "0";
+    return false;
+  }
+  if (pos == -1 && nfound == place && in[0] == sep) {
+    first.clear();
+    second = "0";
+    return false;
+  }
+  pos++;
+  first = trim_expr(in.substr(0, pos));
+  second = trim_expr(in.substr(pos + 1));
+  if (first == " ") first.clear();
+  if (second == " ") second.clear();
+  return true;
+}
+
+// is_ope_bin (give_ope.cpp:276)
+bool is_ope_bin(const std::string& name, std::string& p1, std::string& p2, char cible) {
+  int n = count_char(name, cible);
+  for (int conte = 0; conte < n; conte++) {
+    if (!get_parts(name, p1, p2, cible, conte)) continue;
+    if (!p1.empty() && !p2.empty() && balanced(p1) && balanced(p2)) return true;
+  }
+  return false;
+}
+
+// is_ope_uni (give_ope.cpp:314): "name(" ... ") "
+bool is_ope_uni(const std::string& name, std::string& inner, const std::string& ope) {
+  std::string head = ope + "(";
+  if (name.compare(0, head.size(), head) != 0) return false;
+  if (name.size() < head.size() + 2) return false;
+  if (name[name.size() - 2] != ')') return false;
+  inner = trim_expr(name.substr(head.size(), name.size() - head.size() - 2));
+  return balanced(inner);
+}
+
+bool is_ope_uni2(const std::string& name, std::string& p1, std::string& p2, const std::string& ope) {
+  std::string inner;
+  if (!is_ope_uni(name, inner, ope)) return false;
+  // split at the only top-level comma
+  int depth = 0, at = -1, ncomma = 0;
+  for (size_t i = 0; i < inner.size(); i++) {
+    if (inner[i] == '(') depth++;
+    if (inner[i] == ')') depth--;
+    if (inner[i] == ',' && depth == 0) {
+      at = static_cast<int>(i);
+      ncomma++;
+    }
+  }
+  if (ncomma != 1) return false;
+  p1 = trim_expr(inner.substr(0, at));
+  p2 = trim_expr(inner.substr(at + 1));
+  return true;
+}
+
+bool is_double_str(const std::string& name, double& v) {
+  std::string s = name;
+  while (!s.empty() && s.back() == ' ') s.pop_back();
+  if (s.empty()) return false;
+  char* end = nullptr;
+  v = std::strtod(s.c_str(), &end);
+  return end && *end == '\0';
+}
+
+}  // namespace
+
+std::string trim_expr(const std::string& s) {
+  // trim_spaces (src/Utilities/name_tools.cpp:26): collapse runs of spaces,
+  // drop leading spaces, keep one trailing space, strip redundant outer ().
+  std::string a;
+  bool inspace = !s.empty() && s[0] == ' ';
+  for (char c : s) {
+    bool sp = (c == ' ');
+    if (!sp || !inspace) a.push_back(c);
+    inspace = sp;
+  }
+  if (a.empty() || a.back() != ' ') a.push_back(' ');
+  int first = 0, last = static_cast<int>(a.size()) - 2;
+  while (true) {
+    if (last <= first) break;
+    bool need = (a[first] == '(') && (a[last] == ')');
+    if (need) {
+      int nin = 0;
+      for (int i = first; i < last; i++) {
+        if (a[i] == '(') nin++;
+        if (a[i] == ')') nin--;
+        if (a[i] == ')' && nin == 0) need = false;
+      }
+    }
+    if (!need) break;
+    first++;
+    last--;
+  }
+  std::string out = a.substr(first, static_cast<size_t>(last - first + 1));
+  // trailing single space convention
+  while (!out.empty() && out.back() == ' ') out.pop_back();
+  while (!out.empty() && out.front() == ' ') out.erase(out.begin());
+  return out + " ";
+}
+
+OpePtr parse_ope(const System& sys, int dd, const std::string& expr, int bound) {
+  std::string name = trim_expr(expr);
+  std::string p1, p2;
+  if (is_ope_bin(name, p1, p2, '+'))
+    return std::make_shared<OpeBin>(dd, '+', parse_ope(sys, dd, p1, bound), parse_ope(sys, dd, p2, bound));
+  if (is_ope_bin(name, p1, p2, '-'))
+    return std::make_shared<OpeBin>(dd, '-', parse_ope(sys, dd, p1, bound), parse_ope(sys, dd, p2, bound));
+  if (name[0] == '-') return std::make_shared<OpeMinus>(dd, parse_ope(sys, dd, name.substr(1), bound));
+  if (is_ope_bin(name, p1, p2, '*'))
+    return std::make_shared<OpeBin>(dd, '*', parse_ope(sys, dd, p1, bound), parse_ope(sys, dd, p2, bound));
+  if (is_ope_bin(name, p1, p2, '/'))
+    return std::make_shared<OpeBin>(dd, '/', parse_ope(sys, dd, p1, bound), parse_ope(sys, dd, p2, bound));
+  struct U {
+    const char* n;
+    OpeUnary::Kind k;
+  };
+  static const U unis[] = {{"Lap", OpeUnary::LAP},       {"lap", OpeUnary::LAP},        {"dn", OpeUnary::DN},
+                           {"multr", OpeUnary::MULTR},   {"dr", OpeUnary::DR},          {"divr", OpeUnary::DIVR},
+                           {"divsint", OpeUnary::DIVSINT}, {"multsint", OpeUnary::MULTSINT},
+                           {"divcost", OpeUnary::DIVCOST}};
+  for (const auto& u : unis)
+    if (is_ope_uni(name, p1, u.n)) {
+      if (u.k == OpeUnary::DN && bound < 0) throw KdError(KD_ERR_ARG, "dn() needs a boundary");
+      return std::make_shared<OpeUnary>(dd, u.k, bound, parse_ope(sys, dd, p1, bound));
+    }
+  if (is_ope_uni(name, p1, "grad")) return std::make_shared<OpeGrad>(dd, parse_ope(sys, dd, p1, bound));
+  if (is_ope_uni(name, p1, "sqrt"))
+    return std::make_shared<OpeFunc>(dd, OpeFunc::SQRT, parse_ope(sys, dd, p1, bound));
+  if (is_ope_uni(name, p1, "exp")) return std::make_shared<OpeFunc>(dd, OpeFunc::EXP, parse_ope(sys, dd, p1, bound));
+  if (is_ope_uni(name, p1, "log")) return std::make_shared<OpeFunc>(dd, OpeFunc::LOG, parse_ope(sys, dd, p1, bound));
+  if (is_ope_uni2(name, p1, p2, "scal"))
+    return std::make_shared<OpeScal>(dd, parse_ope(sys, dd, p1, bound), parse_ope(sys, dd, p2, bound));
+  // partial_x(f) etc.
+  for (int i = 0; i < 3; i++) {
+    std::string pn = std::string("partial_") + "xyz"[i];
+    if (is_ope_uni(name, p1, pn)) return std::make_shared<OpePartial>(dd, i + 1, parse_ope(sys, dd, p1, bound));
+  }
+  // integer power: split at the last '^' (is_ope_pow, give_ope.cpp:519)
+  if (count_char(name, '^') >= 1) {
+    if (get_parts(name, p1, p2, '^', 0)) {
+      std::string e = p2;
+      while (!e.empty() && e.back() == ' ') e.pop_back();
+      char* end = nullptr;
+      long n = std::strtol(e.c_str(), &end, 0);
+      if (!e.empty() && end && *end == '\0')
+        return std::make_shared<OpePow>(dd, static_cast<int>(n), parse_ope(sys, dd, p1, bound));
+    }
+  }
+  std::string bare = name;
+  while (!bare.empty() && bare.back() == ' ') bare.pop_back();
+  int which = sys.find_var_double(bare);
+  if (which >= 0) return std::make_shared<OpeLeaf>(dd, OpeLeaf::VAR_DOUBLE, which);
+  which = sys.find_var(bare);
+  if (which >= 0) return std::make_shared<OpeLeaf>(dd, OpeLeaf::VAR, which);
+  which = sys.find_cst(bare);
+  if (which >= 0) return std::make_shared<OpeLeaf>(dd, OpeLeaf::CST, which);
+  double v;
+  if (is_double_str(name, v)) return std::make_shared<OpeLeaf>(dd, OpeLeaf::HARD, -1, v);
+  which = sys.find_def(bare, dd);
+  if (which >= 0) return std::make_shared<OpeLeaf>(dd, OpeLeaf::DEF, which);
+  throw KdError(KD_ERR_ARG, "Unknown operator " + bare);
+}
+
+}  // namespace kd

@@ -1,0 +1,74 @@
+// Term_eq (include/term_eq.hpp:63) and Ope_eq trees (include/ope_eq.hpp:34)
+// for one domain, evaluated on the GPU.  A Term carries a value and,
+// during Jacobian assembly, a batched tangent ("der"): B forward-mode seeds
+// pushed through the same tree in one pass, instead of the reference's one
+// column per pass.
+#pragma once
+#include <functional>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "kd_field.hpp"
+
+namespace kd {
+
+struct Term {
+  int dom = -1;
+  bool is_double = false;
+  // double data
+  double vd = 0.0;
+  bool has_dd = false;
+  double dd = 0.0;  // tangent of a double (same for every seed)
+  // tensor data: valence 0 (one component) or 1 (three Cartesian components)
+  int valence = 0;
+  std::vector<DVal> vt;
+  bool has_dt = false;
+  std::vector<DVal> dt;
+
+  static Term dbl(int dom, double v) {
+    Term t;
+    t.dom = dom;
+    t.is_double = true;
+    t.vd = v;
+    return t;
+  }
+  static Term dbl_der(int dom, double v, double d) {
+    Term t = dbl(dom, v);
+    t.has_dd = true;
+    t.dd = d;
+    return t;
+  }
+  bool has_der() const { return is_double ? has_dd : has_dt; }
+};
+
+Term operator+(const Term& a, const Term& b);
+Term operator-(const Term& a, const Term& b);
+Term operator*(const Term& a, const Term& b);
+Term operator/(const Term& a, const Term& b);
+Term operator-(const Term& a);
+Term term_pow(const Term& a, int n);
+
+class System;
+struct EvalState;
+
+// Expression-tree node.
+class Ope {
+ public:
+  explicit Ope(int dom) : dom(dom) {}
+  virtual ~Ope() = default;
+  virtual Term action(EvalState& st) const = 0;
+  int dom;
+};
+using OpePtr = std::shared_ptr<Ope>;
+
+// Parses an expression for domain `dom` (System_of_eqs::give_ope,
+// src/System_of_eqs/give_ope.cpp:1127).  `bound` is the boundary used by
+// dn(); -1 inside the domain.
+OpePtr parse_ope(const System& sys, int dom, const std::string& expr, int bound);
+
+// Trims spaces the way Kadath's trim_spaces does (single spaces, one trailing).
+std::string trim_expr(const std::string& s);
+
+}  // namespace kd

@@ -1,0 +1,387 @@
+"""Python mirror of Kadath's user-facing classes, driving the GB300 library.
+
+Names, argument meaning and error behaviour follow the reference:
+
+* ``Space_spheric``  -- src/Space/Spheric/space_spheric.cpp:25 (plus the
+  add_eq / add_inner_bc / add_outer_bc / add_matching helpers of
+  src/Space/Spheric/spheric_add_eq.cpp)
+* ``Scalar``         -- include/scalar.hpp:67 (one Val_domain per domain)
+* ``System_of_eqs``  -- include/system_of_eqs.hpp:54 (add_var, add_cst,
+  add_def, add_eq_inside, add_eq_bc, add_eq_matching, sec_member,
+  check_equations, do_col_J, do_newton)
+
+Every numerical operation runs in the CUDA library through the C ABI.
+Where the reference aborts, these raise ``KadathError`` with the same message.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import KadathError, default_context
+
+CHEB_TYPE = 1
+OUTER_BC, INNER_BC = 0, 1
+NEWTON_RAPHSON = 0
+
+KD_LU_FP64, KD_LU_TF32_IR, KD_LU_FP32_IR = 0, 1, 2
+
+
+class NewtonOpts(C.Structure):
+    _fields_ = [("precision", C.c_double), ("lu_mode", C.c_int), ("gmres_tol", C.c_double), ("max_refine", C.c_int),
+                ("graph_capture", C.c_int)]
+
+
+class NewtonReport(C.Structure):
+    _fields_ = [("error", C.c_double), ("converged", C.c_int), ("n", C.c_int), ("t_residual_ms", C.c_double),
+                ("t_assembly_ms", C.c_double), ("t_factor_ms", C.c_double), ("t_solve_ms", C.c_double),
+                ("t_update_ms", C.c_double), ("refine_iters", C.c_int), ("refine_rel_residual", C.c_double),
+                ("kernel_launches", C.c_longlong)]
+
+    def as_dict(self):
+        return {f[0]: getattr(self, f[0]) for f in self._fields_}
+
+
+def _declare_system(lib):
+    P, I, D = C.c_void_p, C.c_int, C.c_double
+    IP, DP = C.POINTER(C.c_int), C.POINTER(C.c_double)
+    sig = {
+        "kd_space_spheric_create": (I, [P, DP, IP, DP, I, I, C.POINTER(P)]),
+        "kd_space_destroy": (I, [P]),
+        "kd_space_nbr_domains": (I, [P, IP]),
+        "kd_space_domain_info": (I, [P, I, IP, IP, IP, DP, DP]),
+        "kd_space_radius": (I, [P, I, DP]),
+        "kd_space_cart": (I, [P, I, I, DP]),
+        "kd_space_std_base": (I, [P, I, IP, IP, IP]),
+        "kd_field_create": (I, [P, C.POINTER(P)]),
+        "kd_field_destroy": (I, [P]),
+        "kd_field_set_value": (I, [P, D]),
+        "kd_field_std_base": (I, [P]),
+        "kd_field_set_conf": (I, [P, I, DP]),
+        "kd_field_get_conf": (I, [P, I, DP]),
+        "kd_field_get_coef": (I, [P, I, DP]),
+        "kd_field_get_base": (I, [P, I, IP, IP, IP]),
+        "kd_system_create": (I, [P, I, I, C.POINTER(P)]),
+        "kd_system_destroy": (I, [P]),
+        "kd_system_add_var": (I, [P, C.c_char_p, P]),
+        "kd_system_add_var_double": (I, [P, C.c_char_p, D]),
+        "kd_system_get_var_double": (I, [P, C.c_char_p, DP]),
+        "kd_system_add_cst": (I, [P, C.c_char_p, D]),
+        "kd_system_add_cst_field": (I, [P, C.c_char_p, P]),
+        "kd_system_add_def": (I, [P, I, C.c_char_p]),
+        "kd_system_add_eq_inside": (I, [P, I, C.c_char_p]),
+        "kd_system_add_eq_bc": (I, [P, I, I, C.c_char_p]),
+        "kd_system_add_eq_matching": (I, [P, I, I, C.c_char_p]),
+        "kd_system_sizes": (I, [P, IP, IP]),
+        "kd_system_n_equations": (I, [P, IP]),
+        "kd_system_residual": (I, [P, DP]),
+        "kd_system_check_equations": (I, [P, DP]),
+        "kd_system_jacobian": (I, [P, DP]),
+        "kd_system_jacobian_device": (I, [P, P, C.c_longlong]),
+        "kd_system_update": (I, [P, DP]),
+        "kd_newton_step": (I, [P, C.POINTER(NewtonOpts), C.POINTER(NewtonReport)]),
+        "kd_lu_create": (I, [P, C.POINTER(P)]),
+        "kd_lu_destroy": (I, [P]),
+        "kd_lu_factor": (I, [P, P, C.c_longlong, I, I]),
+        "kd_lu_solve": (I, [P, P, I]),
+        "kd_lu_stats": (I, [P, DP, DP, IP, DP]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+
+
+_declared = False
+
+
+def _L():
+    global _declared
+    lib = _lib.load()
+    if not _declared:
+        _declare_system(lib)
+        _declared = True
+    return lib
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+class Space_spheric:
+    """Space_spheric(type_coloc, center, res, bounds, withzec=True)."""
+
+    def __init__(self, type_coloc, center, res, bounds, withzec=True, ctx=None):
+        if type_coloc != CHEB_TYPE:
+            raise KadathError(_lib.KD_ERR_UNSUPPORTED, "only CHEB_TYPE collocation is supported")
+        self.ctx = ctx or default_context()
+        lib = _L()
+        c = np.asarray(center, dtype=np.float64)
+        r = np.asarray(res, dtype=np.int32)
+        b = np.asarray(bounds, dtype=np.float64)
+        h = C.c_void_p()
+        self.ctx.check(lib.kd_space_spheric_create(self.ctx.h, _dp(c), _ip(r), _dp(b), len(b), int(withzec), C.byref(h)))
+        self.h = h
+        self.res = tuple(int(v) for v in res)
+        self.bounds = tuple(float(v) for v in bounds)
+
+    def get_nbr_domains(self):
+        n = C.c_int()
+        _L().kd_space_nbr_domains(self.h, C.byref(n))
+        return n.value
+
+    def domain_info(self, dom):
+        t = C.c_int()
+        npts = np.zeros(3, np.int32)
+        nc = np.zeros(3, np.int32)
+        a, b = C.c_double(), C.c_double()
+        self.ctx.check(_L().kd_space_domain_info(self.h, dom, C.byref(t), _ip(npts), _ip(nc), C.byref(a), C.byref(b)))
+        return {"type": t.value, "nbr_points": tuple(npts), "nbr_coefs": tuple(nc), "alpha": a.value, "beta": b.value}
+
+    def get_radius(self, dom):
+        info = self.domain_info(dom)
+        out = np.zeros(info["nbr_points"])
+        self.ctx.check(_L().kd_space_radius(self.h, dom, _dp(out)))
+        return out
+
+    def get_cart(self, dom, c):
+        info = self.domain_info(dom)
+        out = np.zeros(info["nbr_points"])
+        self.ctx.check(_L().kd_space_cart(self.h, dom, c - 1, _dp(out)))
+        return out
+
+    # spheric_add_eq.cpp helpers
+    def add_inner_bc(self, syst, eq):
+        syst.add_eq_bc(syst.dom_min, INNER_BC, eq)
+
+    def add_outer_bc(self, syst, eq):
+        syst.add_eq_bc(syst.dom_max, OUTER_BC, eq)
+
+    def add_matching(self, syst, eq):
+        for dd in range(syst.dom_min, syst.dom_max):
+            syst.add_eq_matching(dd, OUTER_BC, eq)
+
+    def add_eq(self, syst, eq, rac=None, rac_der=None):
+        if rac is None:
+            for dd in range(syst.dom_min, syst.dom_max + 1):
+                syst.add_eq_inside(dd, eq)
+            return
+        for dd in range(syst.dom_min, syst.dom_max):
+            syst.add_eq_inside(dd, eq)
+            syst.add_eq_matching(dd, OUTER_BC, rac)
+            syst.add_eq_matching(dd, OUTER_BC, rac_der)
+        syst.add_eq_inside(syst.dom_max, eq)
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                _L().kd_space_destroy(self.h)
+        except Exception:
+            pass
+
+
+class Scalar:
+    """Scalar(space); ``field = v`` is ``set_value(v)``."""
+
+    def __init__(self, space: Space_spheric, value=None):
+        self.space = space
+        h = C.c_void_p()
+        space.ctx.check(_L().kd_field_create(space.h, C.byref(h)))
+        self.h = h
+        if value is not None:
+            self.set_value(value)
+
+    def set_value(self, v):
+        self.space.ctx.check(_L().kd_field_set_value(self.h, float(v)))
+        return self
+
+    def std_base(self):
+        self.space.ctx.check(_L().kd_field_std_base(self.h))
+        return self
+
+    def set_domain(self, dom, values):
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        info = self.space.domain_info(dom)
+        if v.shape != tuple(info["nbr_points"]):
+            raise KadathError(_lib.KD_ERR_ARG, f"expected shape {info['nbr_points']}")
+        self.space.ctx.check(_L().kd_field_set_conf(self.h, dom, _dp(v)))
+
+    def get_domain(self, dom):
+        """Values at the collocation points of domain dom."""
+        info = self.space.domain_info(dom)
+        out = np.zeros(info["nbr_points"])
+        self.space.ctx.check(_L().kd_field_get_conf(self.h, dom, _dp(out)))
+        return out
+
+    def get_coef(self, dom):
+        info = self.space.domain_info(dom)
+        out = np.zeros(info["nbr_coefs"])
+        self.space.ctx.check(_L().kd_field_get_coef(self.h, dom, _dp(out)))
+        return out
+
+    def get_base(self, dom):
+        info = self.space.domain_info(dom)
+        nc = info["nbr_coefs"]
+        r = np.zeros(nc[1] * nc[2], np.int32)
+        t = np.zeros(nc[2], np.int32)
+        p = C.c_int()
+        self.space.ctx.check(_L().kd_field_get_base(self.h, dom, _ip(r), _ip(t), C.byref(p)))
+        return r.reshape(nc[1], nc[2]), t, p.value
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                _L().kd_field_destroy(self.h)
+        except Exception:
+            pass
+
+
+class System_of_eqs:
+    """System_of_eqs(space, dom_min, dom_max)."""
+
+    def __init__(self, space: Space_spheric, dom_min=None, dom_max=None):
+        if dom_min is None:
+            dom_min, dom_max = 0, space.get_nbr_domains() - 1
+        elif dom_max is None:
+            dom_max = dom_min
+        self.space = space
+        self.ctx = space.ctx
+        self.dom_min, self.dom_max = dom_min, dom_max
+        h = C.c_void_p()
+        self.ctx.check(_L().kd_system_create(space.h, dom_min, dom_max, C.byref(h)))
+        self.h = h
+        self._keep = []
+        self.lu_mode = KD_LU_FP64
+        self.last_report = None
+        self._J = None
+
+    def get_dom_min(self):
+        return self.dom_min
+
+    def get_dom_max(self):
+        return self.dom_max
+
+    def add_var(self, name, field):
+        if isinstance(field, Scalar):
+            self._keep.append(field)
+            self.ctx.check(_L().kd_system_add_var(self.h, name.encode(), field.h))
+        else:
+            self.ctx.check(_L().kd_system_add_var_double(self.h, name.encode(), float(field)))
+
+    def get_var_double(self, name):
+        v = C.c_double()
+        self.ctx.check(_L().kd_system_get_var_double(self.h, name.encode(), C.byref(v)))
+        return v.value
+
+    def add_cst(self, name, value):
+        if isinstance(value, Scalar):
+            self._keep.append(value)
+            self.ctx.check(_L().kd_system_add_cst_field(self.h, name.encode(), value.h))
+        else:
+            self.ctx.check(_L().kd_system_add_cst(self.h, name.encode(), float(value)))
+
+    def add_def(self, *args):
+        dom, text = (-1, args[0]) if len(args) == 1 else args
+        self.ctx.check(_L().kd_system_add_def(self.h, int(dom), text.encode()))
+
+    def add_eq_inside(self, dom, eq):
+        self.ctx.check(_L().kd_system_add_eq_inside(self.h, dom, eq.encode()))
+
+    def add_eq_bc(self, dom, bound, eq):
+        self.ctx.check(_L().kd_system_add_eq_bc(self.h, dom, bound, eq.encode()))
+
+    def add_eq_matching(self, dom, bound, eq):
+        self.ctx.check(_L().kd_system_add_eq_matching(self.h, dom, bound, eq.encode()))
+
+    def sizes(self):
+        nu, nc = C.c_int(), C.c_int()
+        self.ctx.check(_L().kd_system_sizes(self.h, C.byref(nu), C.byref(nc)))
+        return nu.value, nc.value
+
+    def get_nbr_unknowns(self):
+        return self.sizes()[0]
+
+    def get_nbr_conditions(self):
+        return self.sizes()[1]
+
+    def sec_member(self):
+        n = self.get_nbr_conditions()
+        out = np.zeros(n)
+        self.ctx.check(_L().kd_system_residual(self.h, _dp(out)))
+        return out
+
+    def check_equations(self):
+        neq = C.c_int()
+        self.ctx.check(_L().kd_system_n_equations(self.h, C.byref(neq)))
+        out = np.zeros(neq.value)
+        self.ctx.check(_L().kd_system_check_equations(self.h, _dp(out)))
+        return out
+
+    def jacobian(self):
+        """All do_col_J columns at once: the dense N x N Jacobian."""
+        n = self.get_nbr_unknowns()
+        out = np.zeros((n, n), order="F")
+        self.ctx.check(_L().kd_system_jacobian(self.h, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return np.asfortranarray(out.reshape((n, n), order="F"))
+
+    def do_col_J(self, cc):
+        """One column of the Jacobian (System_of_eqs::do_col_J)."""
+        if self._J is None:
+            self._J = self.jacobian()
+        return self._J[:, cc].copy()
+
+    def xx_to_vars_update(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        self.ctx.check(_L().kd_system_update(self.h, _dp(x)))
+        self._J = None
+
+    def do_newton(self, precision, lu_mode=None, gmres_tol=1e-14, max_refine=50):
+        """System_of_eqs::do_newton: returns (converged, error)."""
+        opts = NewtonOpts(precision, self.lu_mode if lu_mode is None else lu_mode, gmres_tol, max_refine, 0)
+        rep = NewtonReport()
+        self.ctx.check(_L().kd_newton_step(self.h, C.byref(opts), C.byref(rep)))
+        self.last_report = rep.as_dict()
+        self._J = None
+        return bool(rep.converged), rep.error
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                _L().kd_system_destroy(self.h)
+        except Exception:
+            pass
+
+
+class DenseLU:
+    """GPU LU of a device matrix (torch tensor, float64, column-major view)."""
+
+    def __init__(self, ctx=None):
+        self.ctx = ctx or default_context()
+        h = C.c_void_p()
+        self.ctx.check(_L().kd_lu_create(self.ctx.h, C.byref(h)))
+        self.h = h
+
+    def factor(self, dA_ptr, ld, n, mode=KD_LU_FP64):
+        self.ctx.check(_L().kd_lu_factor(self.h, C.c_void_p(dA_ptr), ld, n, mode))
+
+    def solve(self, db_ptr, trans=0):
+        self.ctx.check(_L().kd_lu_solve(self.h, C.c_void_p(db_ptr), trans))
+
+    def stats(self):
+        a, b, r = C.c_double(), C.c_double(), C.c_double()
+        it = C.c_int()
+        _L().kd_lu_stats(self.h, C.byref(a), C.byref(b), C.byref(it), C.byref(r))
+        return {"t_factor_ms": a.value, "t_solve_ms": b.value, "refine_iters": it.value, "rel_residual": r.value}
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                _L().kd_lu_destroy(self.h)
+        except Exception:
+            pass

@@ -1,0 +1,970 @@
+"""CPU oracle for the Newton-Raphson path of Kadath (TEST INFRASTRUCTURE ONLY).
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` may import this module, and only as the checker or as the timed
+CPU baseline.  The product path never imports it.
+
+A numpy restatement of the reference's CPU solver for spherical spaces:
+
+* Val_domain with its lazy conf/coef state (src/Val_domain/val_domain.cpp,
+  val_domain_math.cpp), batched over Jacobian seeds;
+* Domain_{nucleus,shell,compact} geometry, basis product rules and operators
+  (src/Domain/Spheric/domain_*.cpp, domain_*_ope.cpp), Cartesian derivatives
+  by the chain rule (do_der_abs_from_der_var) and the flat Laplacian
+  (src/Domain/domain.cpp:155);
+* tau/Galerkin tables: export_tau (domain_*_export_tau.cpp), boundary export
+  (domain_*_export_tau_boundary.cpp + val_boundary, domain_*_systems.cpp),
+  unknown patterns (domain_*_affecte_tau_one_coef.cpp) and the x -> fields
+  map (domain_*_affecte_tau.cpp);
+* Term_eq forward-mode rules (src/Term_eq/term_eq_math.cpp);
+* the serial Newton step do_newton_seq (src_par/do_newton.cpp:519-572) with
+  the Jacobian built column by column as do_col_J (solver.cpp:120) would,
+  here vectorised over columns, and LAPACK getrf/getrs through scipy.
+
+Equations are given as Python callables on ``OTerm`` objects instead of
+strings (the string parser is product code under test).
+
+Pinning: the analytic solutions printed by tutorials/tuto5.cpp
+(F = 1 + a/r), codes/Seq_version/schwarz.cpp (conformal factor 1 + a/r,
+max error over 100 points) and tutorials/tuto6.cpp (P = log(1 + a/r)) are
+reproduced by this oracle in tests/test_oracle_newton.py.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import spectral as S
+
+NUCLEUS, SHELL, COMPACT = 1, 2, 3
+OUTER_BC, INNER_BC = 0, 1
+
+_MAT_CACHE: dict = {}
+
+
+def mat(op, base, n_in, n_out=None):
+    key = (op, int(base), n_in, n_out or n_in)
+    if key not in _MAT_CACHE:
+        _MAT_CACHE[key] = S.matrix_1d(op, int(base), n_in, n_out or n_in)
+    return _MAT_CACHE[key]
+
+
+class OBase:
+    def __init__(self, r=None, t=None, p=None):
+        self.r = None if r is None else np.array(r, dtype=int)
+        self.t = None if t is None else np.array(t, dtype=int)
+        self.p = p
+
+    @property
+    def defined(self):
+        return self.r is not None
+
+    def copy(self):
+        return OBase(None if self.r is None else self.r.copy(), None if self.t is None else self.t.copy(), self.p)
+
+    def key(self):
+        return (tuple(self.r.ravel()), tuple(self.t), self.p)
+
+
+def _apply_dim(x, dim, op, base_table, n_in, n_out):
+    """Applies per-line matrices along `dim` of a batch x[B, n0, n1, n2].
+
+    base_table: for dim 0 an (n1, n2) table, dim 1 an (n2,) table, dim 2 a
+    scalar.  Returns (result, output basis table)."""
+    B, n0, n1, n2 = x.shape
+    shape = [B, n0, n1, n2]
+    shape[dim + 1] = n_out
+    y = np.zeros(shape)
+    if dim == 2:
+        ob, m = mat(op, base_table, n_in, n_out)
+        y[:] = np.einsum("ok,bijk->bijo", m, x)
+        return y, ob
+    if dim == 1:
+        out_t = np.array(base_table).copy()
+        for k in range(n2):
+            ob, m = mat(op, base_table[k], n_in, n_out)
+            y[:, :, :, k] = np.einsum("oj,bij->bio", m, x[:, :, :, k])
+            out_t[k] = ob
+        return y, out_t
+    out_r = np.array(base_table).copy()
+    for j in range(n1):
+        for k in range(n2):
+            ob, m = mat(op, base_table[j][k], n_in, n_out)
+            y[:, :, j, k] = np.einsum("oi,bi->bo", m, x[:, :, j, k])
+            out_r[j][k] = ob
+    return y, out_r
+
+
+class ODomain:
+    """Domain_nucleus / Domain_shell / Domain_compact (CHEB_TYPE)."""
+
+    def __init__(self, num, dtype, res, alpha, beta):
+        self.num, self.type = num, dtype
+        self.np = tuple(res)
+        self.nc = (res[0], res[1], res[2] + 2)
+        self.alpha, self.beta = alpha, beta
+        n0, n1, n2 = res
+        if dtype == NUCLEUS:
+            self.x = np.array([math.sin(math.pi / 2. * i / (n0 - 1)) for i in range(n0)])
+        else:
+            self.x = np.array([-math.cos(math.pi * i / (n0 - 1)) for i in range(n0)])
+        self.theta = np.array([math.pi / 2. * j / (n1 - 1) for j in range(n1)])
+        self.phi = np.array([math.pi * 2. * k / n2 for k in range(n2)])
+
+    # geometry --------------------------------------------------------------
+    def radius_1d(self):
+        if self.type == NUCLEUS:
+            return self.alpha * self.x
+        if self.type == SHELL:
+            return self.alpha * self.x + self.beta
+        with np.errstate(divide="ignore"):
+            return 1. / self.alpha / (self.x - 1)
+
+    def radius(self):
+        r = self.radius_1d()
+        return np.broadcast_to(r[:, None, None], self.np).copy()
+
+    def cart(self, c):
+        r = self.radius()
+        th = self.theta[None, :, None]
+        ph = self.phi[None, None, :]
+        if c == 0:
+            return r * np.sin(th) * np.cos(ph)
+        if c == 1:
+            return r * np.sin(th) * np.sin(ph)
+        return r * np.cos(th) * np.ones_like(ph)
+
+    # bases -----------------------------------------------------------------
+    def std_base(self):
+        nc1, nc2 = self.nc[1], self.nc[2]
+        t = np.zeros(nc2, dtype=int)
+        r = np.zeros((nc1, nc2), dtype=int)
+        for k in range(nc2):
+            m = k // 2
+            t[k] = S.COS_EVEN if m % 2 == 0 else S.SIN_ODD
+            for j in range(nc1):
+                if self.type == NUCLEUS:
+                    l = 2 * j if m % 2 == 0 else 2 * j + 1
+                    r[j, k] = S.CHEB_EVEN if l % 2 == 0 else S.CHEB_ODD
+                else:
+                    r[j, k] = S.CHEB
+        return OBase(r, t, S.COSSIN)
+
+    def mult(self, a, b):
+        """Domain_*::mult: basis of a product."""
+        if not (a.defined and b.defined):
+            return OBase()
+        sig = {S.COS_EVEN: (1, 1), S.COS_ODD: (1, -1), S.SIN_EVEN: (-1, -1), S.SIN_ODD: (-1, 1)}
+        inv = {v: k for k, v in sig.items()}
+        t = np.zeros_like(a.t)
+        for k in range(len(a.t)):
+            s1a, s2a = sig[int(a.t[k])]
+            s1b, s2b = sig[int(b.t[k])]
+            flip = 1 if k % 4 < 2 else -1
+            t[k] = inv[(s1a * s1b * flip, s2a * s2b)]
+        r = np.zeros_like(a.r)
+        for j in range(a.r.shape[0]):
+            for k in range(a.r.shape[1]):
+                if self.type == NUCLEUS:
+                    pa = 1 if a.r[j, k] == S.CHEB_EVEN else -1
+                    pb = 1 if b.r[j, k] == S.CHEB_EVEN else -1
+                    flip = 1 if k % 4 < 2 else -1
+                    r[j, k] = S.CHEB_EVEN if pa * pb * flip > 0 else S.CHEB_ODD
+                else:
+                    r[j, k] = S.CHEB
+        return OBase(r, t, S.COSSIN)
+
+    # tau tables ------------------------------------------------------------
+    def cidx(self, i, j, k):
+        return (i * self.nc[1] + j) * self.nc[2] + k
+
+    def export_tau(self, base, order):
+        """export_tau_val_domain (mlim = 0): list of rows [(idx, w), ...]."""
+        nc0, nc1, nc2 = self.nc
+        kmin = 2
+        rows = []
+        ci = self.cidx
+        if self.type != NUCLEUS:
+            for k in range(nc2 - 1):
+                if k == 1:
+                    continue
+                bt = base.t[k]
+                for j in range(nc1):
+                    for i in range(nc0 - order):
+                        if bt == S.COS_EVEN:
+                            if k < kmin:
+                                rows.append([(ci(i, j, k), 1.0)])
+                            elif j != 0:
+                                rows.append([(ci(i, j, k), 1.0), (ci(i, 0, k), -2.0)])
+                        elif bt == S.COS_ODD:
+                            if j != nc1 - 1:
+                                if k < kmin:
+                                    rows.append([(ci(i, j, k), 1.0)])
+                                elif j != 0:
+                                    rows.append([(ci(i, j, k), 1.0), (ci(i, 0, k), -1.0)])
+                        elif bt == S.SIN_EVEN:
+                            if j != 0 and j != nc1 - 1:
+                                if k < kmin + 2:
+                                    rows.append([(ci(i, j, k), 1.0)])
+                                elif j != 1:
+                                    rows.append([(ci(i, j, k), 1.0), (ci(i, 1, k), -float(j))])
+                        elif bt == S.SIN_ODD:
+                            if j != nc1 - 1:
+                                if k < kmin + 2:
+                                    rows.append([(ci(i, j, k), 1.0)])
+                                elif j != 0:
+                                    rows.append([(ci(i, j, k), 1.0), (ci(i, 0, k), -float(2 * j + 1))])
+            return rows
+        rlim = 1 if order == 0 else 2
+        llim = 0
+        sg = lambda i: 1.0 if i % 2 == 0 else -1.0
+        for k in range(nc2 - 1):
+            if k == 1:
+                continue
+            bt = base.t[k]
+            for j in range(nc1):
+                for i in range(nc0):
+                    if bt == S.COS_EVEN:
+                        lq = 2 * j
+                        if k < kmin and lq <= llim:
+                            if i != nc0 - rlim + 1:
+                                rows.append([(ci(i, j, k), 1.0)])
+                        elif k < kmin:
+                            if i != 0 and i != nc0 - rlim + 1:
+                                rows.append([(ci(i, j, k), 1.0), (ci(0, j, k), -2 * sg(i))])
+                        elif j != 0 and i != 0 and i != nc0 - rlim + 1:
+                            rows.append([(ci(i, j, k), 1.0), (ci(0, j, k), -2 * sg(i)), (ci(i, 0, k), -2.0),
+                                         (ci(0, 0, k), 4 * sg(i))])
+                    elif bt == S.COS_ODD:
+                        lq = 2 * j + 1
+                        if j != nc1 - 1 and i != nc0 - rlim + 1 and i != nc0 - rlim:
+                            if k < kmin and lq <= llim + 1:
+                                rows.append([(ci(i, j, k), 1.0)])
+                            elif k < kmin and i != 0:
+                                rows.append([(ci(i, j, k), 1.0), (ci(0, j, k), -(2 * i + 1) * sg(i))])
+                            elif j != 0 and i != 0:
+                                rows.append([(ci(i, j, k), 1.0), (ci(0, j, k), -sg(i) * (2 * i + 1)),
+                                             (ci(i, 0, k), -1.0), (ci(0, 0, k), sg(i) * (2 * i + 1))])
+                    elif bt == S.SIN_EVEN:
+                        lq = 2 * j
+                        if j != 0 and j != nc1 - 1 and i != nc0 - rlim + 1:
+                            if k < kmin + 2 and lq <= llim:
+                                rows.append([(ci(i, j, k), 1.0)])
+                            elif k < kmin + 2 and i != 0:
+                                rows.append([(ci(i, j, k), 1.0), (ci(0, j, k), -2 * sg(i))])
+                            elif k >= kmin + 2 and j != 1 and i != 0:
+                                rows.append([(ci(i, j, k), 1.0), (ci(0, j, k), -sg(i)), (ci(i, 1, k), -float(j)),
+                                             (ci(0, 1, k), sg(i) * j)])
+                    elif bt == S.SIN_ODD:
+                        lq = 2 * j + 1
+                        if j != nc1 - 1 and i != nc0 - rlim + 1 and i != nc0 - rlim:
+                            if k < kmin + 2 and lq <= llim + 1:
+                                rows.append([(ci(i, j, k), 1.0)])
+                            elif k < kmin + 2 and i != 0:
+                                rows.append([(ci(i, j, k), 1.0), (ci(0, j, k), -(2 * i + 1) * sg(i))])
+                            elif j != 0 and i != 0:
+                                rows.append([(ci(i, j, k), 1.0), (ci(0, j, k), -sg(i) * (2 * i + 1)),
+                                             (ci(i, 0, k), -float(2 * j + 1)),
+                                             (ci(0, 0, k), sg(i) * (2 * i + 1) * (2 * j + 1))])
+        return rows
+
+    def val_boundary(self, bound, j, k, w):
+        """val_boundary as (idx, w) terms."""
+        out = []
+        for i in range(self.nc[0]):
+            s = (1.0 if i % 2 == 0 else -1.0) if bound == INNER_BC else 1.0
+            out.append((self.cidx(i, j, k), w * s))
+        return out
+
+    def export_tau_boundary(self, base, bound):
+        nc0, nc1, nc2 = self.nc
+        kmin = 2
+        rows = []
+        vb = self.val_boundary
+        for k in range(nc2 - 1):
+            if k == 1:
+                continue
+            bt = base.t[k]
+            for j in range(nc1):
+                if bt == S.COS_EVEN:
+                    if k < kmin:
+                        rows.append(vb(bound, j, k, 1.0))
+                    elif j != 0:
+                        rows.append(vb(bound, j, k, 1.0) + vb(bound, 0, k, -2.0))
+                elif bt == S.COS_ODD:
+                    if j != nc1 - 1:
+                        if k < kmin:
+                            rows.append(vb(bound, j, k, 1.0))
+                        elif j != 0:
+                            rows.append(vb(bound, j, k, 1.0) + vb(bound, 0, k, -1.0))
+                elif bt == S.SIN_EVEN:
+                    if j != 0 and j != nc1 - 1:
+                        if k < kmin + 2:
+                            rows.append(vb(bound, j, k, 1.0))
+                        elif j != 1:
+                            rows.append(vb(bound, j, k, 1.0) + vb(bound, 1, k, -float(j)))
+                elif bt == S.SIN_ODD:
+                    if j != nc1 - 1:
+                        if k < kmin + 2:
+                            rows.append(vb(bound, j, k, 1.0))
+                        elif j != 0:
+                            rows.append(vb(bound, j, k, 1.0) + vb(bound, 0, k, -float(2 * j + 1)))
+        return rows
+
+    def unknown_patterns(self, base):
+        """affecte_tau_one_coef_val_domain (mlim = llim = 0)."""
+        nc0, nc1, nc2 = self.nc
+        kmin = 2
+        pats = []
+        ci = self.cidx
+        if self.type != NUCLEUS:
+            for k in range(nc2 - 1):
+                if k == 1:
+                    continue
+                bt = base.t[k]
+                for j in range(nc1):
+                    if bt == S.COS_EVEN:
+                        true_t = not (j == 0 and k >= kmin)
+                    elif bt == S.COS_ODD:
+                        true_t = not (j == nc1 - 1 or (j == 0 and k >= kmin))
+                    elif bt == S.SIN_EVEN:
+                        true_t = not ((j == 1 and k >= kmin + 2) or j == 0 or j == nc1 - 1)
+                    else:
+                        true_t = not ((j == 0 and k >= kmin + 2) or j == nc1 - 1)
+                    if not true_t:
+                        continue
+                    for i in range(nc0):
+                        p = [(ci(i, j, k), 1.0)]
+                        if bt in (S.COS_EVEN, S.COS_ODD) and k >= kmin:
+                            p.append((ci(i, 0, k), -1.0))
+                        if bt == S.SIN_EVEN and k >= kmin + 2:
+                            p.append((ci(i, 1, k), -float(j)))
+                        if bt == S.SIN_ODD and k >= kmin + 2:
+                            p.append((ci(i, 0, k), -float(2 * j + 1)))
+                        pats.append(p)
+            return pats
+        llim = 0
+        sg = lambda i: 1.0 if i % 2 == 0 else -1.0
+        for k in range(nc2 - 1):
+            if k == 1:
+                continue
+            bt = base.t[k]
+            for j in range(nc1):
+                for i in range(nc0):
+                    p = None
+                    if bt == S.COS_EVEN:
+                        lq = 2 * j
+                        if k < kmin and lq <= llim:
+                            p = [(ci(i, j, k), 1.0)]
+                        elif k < kmin:
+                            if i != 0:
+                                p = [(ci(i, j, k), 1.0), (ci(0, j, k), -sg(i))]
+                        elif j != 0 and i != 0:
+                            p = [(ci(i, j, k), 1.0), (ci(0, j, k), -sg(i)), (ci(i, 0, k), -1.0), (ci(0, 0, k), sg(i))]
+                    elif bt == S.COS_ODD:
+                        lq = 2 * j + 1
+                        if j != nc1 - 1 and i != nc0 - 1:
+                            if k < kmin and lq <= llim + 1:
+                                p = [(ci(i, j, k), 1.0)]
+                            elif k < kmin and i != 0:
+                                p = [(ci(i, j, k), 1.0), (ci(0, j, k), -(2 * i + 1) * sg(i))]
+                            elif j != 0 and i != 0:
+                                p = [(ci(i, j, k), 1.0), (ci(0, j, k), -sg(i) * (2 * i + 1)), (ci(i, 0, k), -1.0),
+                                     (ci(0, 0, k), sg(i) * (2 * i + 1))]
+                    elif bt == S.SIN_EVEN:
+                        lq = 2 * j
+                        if j != 0 and j != nc1 - 1:
+                            if k < kmin + 2 and lq <= llim:
+                                p = [(ci(i, j, k), 1.0)]
+                            elif k < kmin + 2 and i != 0:
+                                p = [(ci(i, j, k), 1.0), (ci(0, j, k), -sg(i))]
+                            elif k >= kmin + 2 and j != 1 and i != 0:
+                                p = [(ci(i, j, k), 1.0), (ci(0, j, k), -sg(i)), (ci(i, 1, k), -float(j)),
+                                     (ci(0, 1, k), sg(i) * j)]
+                    elif bt == S.SIN_ODD:
+                        lq = 2 * j + 1
+                        if j != nc1 - 1 and i != nc0 - 1:
+                            if k < kmin + 2 and lq <= llim + 1:
+                                p = [(ci(i, j, k), 1.0)]
+                            elif k < kmin + 2 and i != 0:
+                                p = [(ci(i, j, k), 1.0), (ci(0, j, k), -(2 * i + 1) * sg(i))]
+                            elif j != 0 and i != 0:
+                                p = [(ci(i, j, k), 1.0), (ci(0, j, k), -sg(i) * (2 * i + 1)),
+                                     (ci(i, 0, k), -float(2 * j + 1)), (ci(0, 0, k), sg(i) * (2 * i + 1) * (2 * j + 1))]
+                    if p is not None:
+                        pats.append(p)
+        return pats
+
+    def affecte_tau_matrix(self, base):
+        """x -> coefficients (affecte_tau_val_domain) as a dense matrix."""
+        nc0, nc1, nc2 = self.nc
+        ncf = nc0 * nc1 * nc2
+        if self.type == NUCLEUS:
+            pats = self.unknown_patterns(base)
+            M = np.zeros((ncf, len(pats)))
+            for u, p in enumerate(pats):
+                for idx, w in p:
+                    M[idx, u] += w
+            return M
+        kmin = 2
+        cols = []
+        M = np.zeros((ncf, ncf))
+        conte = 0
+        ci = self.cidx
+        for k in range(nc2 - 1):
+            if k == 1:
+                continue
+            bt = base.t[k]
+            for j in range(nc1):
+                if bt == S.COS_EVEN:
+                    tt = not (j == 0 and k >= kmin)
+                elif bt == S.COS_ODD:
+                    tt = not (j == nc1 - 1 or (j == 0 and k >= kmin))
+                elif bt == S.SIN_EVEN:
+                    tt = not ((j == 1 and k >= kmin + 2) or j == 0 or j == nc1 - 1)
+                else:
+                    tt = not ((j == 0 and k > kmin + 2) or j == nc1 - 1)
+                if not tt:
+                    continue
+                for i in range(nc0):
+                    M[ci(i, j, k), conte] = 1.0
+                    conte += 1
+        for k in range(nc2 - 1):
+            bt = base.t[k]
+            for i in range(nc0):
+                if bt in (S.COS_EVEN, S.COS_ODD) and k >= kmin:
+                    M[ci(i, 0, k), :] = -sum(M[ci(i, j, k), :] for j in range(1, nc1))
+                elif bt == S.SIN_EVEN and k >= kmin + 2:
+                    M[ci(i, 1, k), :] = -sum(j * M[ci(i, j, k), :] for j in range(2, nc1))
+                elif bt == S.SIN_ODD and k >= kmin + 2:
+                    M[ci(i, 0, k), :] = -sum((2 * j + 1) * M[ci(i, j, k), :] for j in range(1, nc1))
+        return M[:, :conte]
+
+    def has_boundary(self, bound):
+        if self.type == NUCLEUS:
+            return bound == OUTER_BC
+        return True
+
+
+def space_spheric(res, bounds, withzec=True):
+    """Space_spheric (src/Space/Spheric/space_spheric.cpp:25)."""
+    doms = [ODomain(0, NUCLEUS, res, bounds[0], 0.0)]
+    nd = len(bounds) + 1 if withzec else len(bounds)
+    nshell = nd - 1 if withzec else nd
+    for i in range(1, nshell):
+        doms.append(ODomain(i, SHELL, res, (bounds[i] - bounds[i - 1]) / 2., (bounds[i] + bounds[i - 1]) / 2.))
+    if withzec:
+        doms.append(ODomain(nd - 1, COMPACT, res, -0.5 / bounds[nd - 2], 0.0))
+    return doms
+
+
+# ------------------------------------------------------------- Val_domain --
+class VD:
+    """Val_domain batch: c has shape (B,)+np, cf (B,)+nc."""
+
+    def __init__(self, dom, B=1, c=None, cf=None, base=None, zero=False):
+        self.dom, self.B = dom, B
+        self.c, self.cf = c, cf
+        self.base = base if base is not None else OBase()
+        self.zero = zero
+        self._dvar = None
+        self._dabs = None
+
+    @staticmethod
+    def zeros(dom, B=1):
+        return VD(dom, B, zero=True)
+
+    def coef(self):
+        if self.zero or self.cf is not None:
+            return
+        b = self.base
+        d = self.dom
+        x, _ = _apply_dim(self.c, 2, S.OP_COEF, b.p, d.np[2], d.nc[2])
+        x, _ = _apply_dim(x, 1, S.OP_COEF, b.t, d.np[1], d.nc[1])
+        x, _ = _apply_dim(x, 0, S.OP_COEF, b.r, d.np[0], d.nc[0])
+        self.cf = x
+
+    def coef_i(self):
+        if self.zero or self.c is not None:
+            return
+        b = self.base
+        d = self.dom
+        x, _ = _apply_dim(self.cf, 0, S.OP_COEF_I, b.r, d.nc[0], d.np[0])
+        x, _ = _apply_dim(x, 1, S.OP_COEF_I, b.t, d.nc[1], d.np[1])
+        x, _ = _apply_dim(x, 2, S.OP_COEF_I, b.p, d.nc[2], d.np[2])
+        self.c = x
+
+    def ope(self, op, dim):
+        self.coef()
+        b = self.base.copy()
+        d = self.dom
+        table = [b.r, b.t, b.p][dim]
+        y, ob = _apply_dim(self.cf, dim, op, table, d.nc[dim], d.nc[dim])
+        if dim == 0:
+            b.r = ob
+        elif dim == 1:
+            b.t = ob
+        else:
+            b.p = ob
+        return VD(d, self.B, cf=y, base=b)
+
+    def der_var(self, var):
+        if self.zero:
+            return self
+        if self._dvar is None:
+            self._dvar = [self.ope(S.OP_DER, v) for v in range(3)]
+        return self._dvar[var - 1]
+
+    def der_abs(self, var):
+        if self.zero:
+            return self
+        if self._dabs is None:
+            self._dabs = der_abs_from_der_var(self.dom, [self.der_var(v) for v in (1, 2, 3)])
+        return self._dabs[var - 1]
+
+    # algebra (val_domain_math.cpp) ------------------------------------------
+    def _bc(self, other):
+        return max(self.B, other.B)
+
+    def __add__(self, o):
+        if isinstance(o, (int, float)):
+            if self.zero:
+                return VD(self.dom, 1, c=np.full((1,) + self.dom.np, float(o)), base=self.dom.std_base())
+            self.coef_i()
+            return VD(self.dom, self.B, c=self.c + o, base=self.base)
+        if self.zero:
+            return o
+        if o.zero:
+            return self
+        if self.c is not None or o.c is not None:
+            self.coef_i(); o.coef_i()
+            res = VD(self.dom, self._bc(o), c=self.c + o.c)
+        else:
+            res = VD(self.dom, self._bc(o), cf=self.cf + o.cf)
+        if self.base.defined and o.base.defined:
+            res.base = self.base
+        return res
+
+    def __neg__(self):
+        if self.zero:
+            return self
+        return self.scale(-1.0)
+
+    def __sub__(self, o):
+        if isinstance(o, (int, float)):
+            return self + (-o)
+        if self.zero:
+            return -o
+        if o.zero:
+            return self
+        if self.c is not None or o.c is not None:
+            self.coef_i(); o.coef_i()
+            res = VD(self.dom, self._bc(o), c=self.c - o.c)
+        else:
+            res = VD(self.dom, self._bc(o), cf=self.cf - o.cf)
+        if self.base.defined and o.base.defined:
+            res.base = self.base
+        return res
+
+    def rsub(self, x):
+        """x - self (double minus Val_domain)."""
+        if self.zero:
+            return VD(self.dom, 1, c=np.full((1,) + self.dom.np, float(x)), base=self.dom.std_base())
+        self.coef_i()
+        return VD(self.dom, self.B, c=x - self.c, base=self.base)
+
+    def scale(self, x):
+        if self.zero:
+            return self
+        return VD(self.dom, self.B, c=None if self.c is None else self.c * x,
+                  cf=None if self.cf is None else self.cf * x, base=self.base)
+
+    def __mul__(self, o):
+        if isinstance(o, (int, float)):
+            return self.scale(float(o))
+        if self.zero:
+            return self
+        if o.zero:
+            return o
+        self.coef_i(); o.coef_i()
+        return VD(self.dom, self._bc(o), c=self.c * o.c, base=self.dom.mult(self.base, o.base))
+
+    def __truediv__(self, o):
+        if isinstance(o, (int, float)):
+            return self.scale(1.0 / o)
+        if self.zero:
+            return self
+        self.coef_i(); o.coef_i()
+        return VD(self.dom, self._bc(o), c=self.c / o.c, base=self.dom.mult(self.base, o.base))
+
+    def rdiv(self, x):
+        self.coef_i()
+        return VD(self.dom, self.B, c=x / self.c, base=self.dom.std_base())
+
+
+def radius_vd(dom):
+    return VD(dom, 1, c=dom.radius()[None])
+
+
+def _swap_t(b):
+    return {S.COS_EVEN: S.SIN_ODD, S.COS_ODD: S.SIN_EVEN, S.SIN_EVEN: S.COS_ODD, S.SIN_ODD: S.COS_EVEN}[int(b)]
+
+
+def mult_trig_phi(so, op):
+    if so.zero:
+        return so
+    so.coef()
+    nb = so.base.copy()
+    nb.t = np.array([_swap_t(b) for b in so.base.t])
+    if so.dom.type == NUCLEUS:
+        nb.r = np.where(so.base.r == S.CHEB_EVEN, S.CHEB_ODD, S.CHEB_EVEN)
+    y, ob = _apply_dim(so.cf, 2, op, so.base.p, so.dom.nc[2], so.dom.nc[2])
+    nb.p = ob
+    return VD(so.dom, so.B, cf=y, base=nb)
+
+
+def opc(so, op, dim):
+    return so if so.zero else so.ope(op, dim)
+
+
+def der_abs_from_der_var(dom, dv):
+    a = dom.alpha
+    if dom.type == SHELL:
+        sintdr = opc(dv[0], S.OP_MULT_SIN, 1) / a
+        rad = radius_vd(dom)
+        dtsr = dv[1] / rad
+        dtsr.base = dv[1].base
+        dpsr = dv[2] / rad
+        dpsr.base = dv[2].base
+        costdtsr = opc(dtsr, S.OP_MULT_COS, 1)
+        dpsrssint = opc(dpsr, S.OP_DIV_SIN, 1)
+        s = sintdr + costdtsr
+        dx = mult_trig_phi(s, S.OP_MULT_COS) - mult_trig_phi(dpsrssint, S.OP_MULT_SIN)
+        dy = mult_trig_phi(s, S.OP_MULT_SIN) + mult_trig_phi(dpsrssint, S.OP_MULT_COS)
+        dz = opc(dv[0], S.OP_MULT_COS, 1) / a - opc(dtsr, S.OP_MULT_SIN, 1)
+        return [dx, dy, dz]
+    if dom.type == NUCLEUS:
+        sintdr = opc(dv[0], S.OP_MULT_SIN, 1) / a
+        dtsr = opc(dv[1], S.OP_DIV_X, 0) / a
+        dpsr = opc(dv[2], S.OP_DIV_X, 0) / a
+        costdtsr = opc(dtsr, S.OP_MULT_COS, 1)
+        dpsrssint = opc(dpsr, S.OP_DIV_SIN, 1)
+        s = sintdr + costdtsr
+        dx = mult_trig_phi(s, S.OP_MULT_COS) - mult_trig_phi(dpsrssint, S.OP_MULT_SIN)
+        dy = mult_trig_phi(s, S.OP_MULT_SIN) + mult_trig_phi(dpsrssint, S.OP_MULT_COS)
+        dz = opc(dv[0], S.OP_MULT_COS, 1) / a - opc(dtsr, S.OP_MULT_SIN, 1)
+        return [dx, dy, dz]
+    dr = -opc(dv[0], S.OP_MULT_XM1, 0)
+    sintdr = opc(dr, S.OP_MULT_SIN, 1)
+    costdt = opc(dv[1], S.OP_MULT_COS, 1)
+    dpssint = opc(dv[2], S.OP_DIV_SIN, 1)
+    s = sintdr + costdt
+    ax = mult_trig_phi(s, S.OP_MULT_COS) - mult_trig_phi(dpssint, S.OP_MULT_SIN)
+    ay = mult_trig_phi(s, S.OP_MULT_SIN) + mult_trig_phi(dpssint, S.OP_MULT_COS)
+    az = opc(dr, S.OP_MULT_COS, 1) - opc(dv[1], S.OP_MULT_SIN, 1)
+    return [opc(ax, S.OP_MULT_XM1, 0) * a, opc(ay, S.OP_MULT_XM1, 0) * a, opc(az, S.OP_MULT_XM1, 0) * a]
+
+
+def laplacian(so):
+    res = so.der_abs(1).der_abs(1)
+    for j in (2, 3):
+        res = res + so.der_abs(j).der_abs(j)
+    return res
+
+
+def der_normal(so, bound):
+    d = so.dom
+    if d.type == COMPACT:
+        r = opc(opc(so.der_var(1), S.OP_MULT_XM1, 0), S.OP_MULT_XM1, 0)
+        return r * (-d.alpha)
+    return so.der_var(1) / d.alpha
+
+
+# ----------------------------------------------------------------- Term_eq --
+class OTerm:
+    """Scalar Term_eq: value (VD or float) and optional batched tangent."""
+
+    def __init__(self, dom, val, der=None):
+        self.dom, self.val, self.der = dom, val, der
+
+    @property
+    def is_double(self):
+        return isinstance(self.val, float)
+
+    def _coerce(self, o):
+        if isinstance(o, OTerm):
+            return o
+        return OTerm(self.dom, float(o), 0.0 if self.der is not None else None)
+
+    def __add__(self, o):
+        o = self._coerce(o)
+        do = self.der is not None and o.der is not None
+        if self.is_double and o.is_double:
+            return OTerm(self.dom, self.val + o.val, self.der + o.der if do else None)
+        if self.is_double or o.is_double:
+            t, dd = (o, self) if self.is_double else (self, o)
+            der = None
+            if do:
+                der = t.der if dd.der == 0.0 else t.der + dd.der
+            return OTerm(self.dom, t.val + dd.val, der)
+        return OTerm(self.dom, self.val + o.val, self.der + o.der if do else None)
+
+    __radd__ = __add__
+
+    def __sub__(self, o):
+        o = self._coerce(o)
+        do = self.der is not None and o.der is not None
+        if self.is_double and o.is_double:
+            return OTerm(self.dom, self.val - o.val, self.der - o.der if do else None)
+        if o.is_double:
+            return OTerm(self.dom, self.val - o.val, (self.der if o.der == 0.0 else self.der - o.der) if do else None)
+        if self.is_double:
+            der = None
+            if do:
+                der = -o.der if self.der == 0.0 else o.der.rsub(self.der)
+            return OTerm(self.dom, o.val.rsub(self.val), der)
+        return OTerm(self.dom, self.val - o.val, self.der - o.der if do else None)
+
+    def __rsub__(self, o):
+        return self._coerce(o) - self
+
+    def __neg__(self):
+        if self.is_double:
+            return OTerm(self.dom, -self.val, None if self.der is None else -self.der)
+        return OTerm(self.dom, self.val * -1.0, None if self.der is None else self.der * -1.0)
+
+    def __mul__(self, o):
+        o = self._coerce(o)
+        do = self.der is not None and o.der is not None
+        if self.is_double and o.is_double:
+            return OTerm(self.dom, self.val * o.val, self.der * o.val + self.val * o.der if do else None)
+        if self.is_double or o.is_double:
+            t, dd = (o, self) if self.is_double else (self, o)
+            der = None
+            if do:
+                der = t.der * dd.val
+                if dd.der != 0.0:
+                    der = der + t.val * dd.der
+            return OTerm(self.dom, t.val * dd.val, der)
+        return OTerm(self.dom, self.val * o.val, self.der * o.val + self.val * o.der if do else None)
+
+    __rmul__ = __mul__
+
+    def __truediv__(self, o):
+        o = self._coerce(o)
+        do = self.der is not None and o.der is not None
+        if o.is_double:
+            der = None
+            if do:
+                num = self.der * o.val
+                if o.der != 0.0:
+                    num = num - self.val * o.der
+                der = num / (o.val * o.val)
+            return OTerm(self.dom, self.val / o.val, der)
+        raise NotImplementedError("division by a field term")
+
+    def __pow__(self, n):
+        assert isinstance(n, int) and n > 0
+        r = self
+        for _ in range(1, n):
+            r = r * self
+        return r
+
+    def lap(self):
+        return OTerm(self.dom, laplacian(self.val), None if self.der is None else laplacian(self.der))
+
+    def dn(self, bound):
+        return OTerm(self.dom, der_normal(self.val, bound), None if self.der is None else
+                     (self.der if self.der.zero else der_normal(self.der, bound)))
+
+
+# -------------------------------------------------------------- the system --
+class OSystem:
+    """System_of_eqs restricted to scalar unknowns and the equation kinds
+    Eq_inside (order 2), Eq_bc and Eq_matching."""
+
+    def __init__(self, doms, dom_min, dom_max):
+        self.doms, self.dmin, self.dmax = doms, dom_min, dom_max
+        self.vars = []       # (name, dict dom -> VD with B=1)
+        self.eqs = []        # (kind, dom, bound, fn_lhs, other_dom, other_bound, fn_rhs)
+        self.nbr_conditions = None
+
+    def add_var(self, name, fields):
+        self.vars.append((name, fields))
+
+    def add_eq_inside(self, dom, fn):
+        self.eqs.append(("inside", dom, None, fn, None, None, None))
+
+    def add_eq_bc(self, dom, bound, fn):
+        self.eqs.append(("bc", dom, bound, fn, None, None, None))
+
+    def add_eq_matching(self, dom, bound, fn_lhs, fn_rhs=None):
+        other = dom + 1 if bound == OUTER_BC else dom - 1
+        other_bound = INNER_BC if bound == OUTER_BC else OUTER_BC
+        self.eqs.append(("matching", dom, bound, fn_lhs, other, other_bound, fn_rhs or fn_lhs))
+
+    def _terms(self, dom, seed=None):
+        out = {}
+        for vi, (name, f) in enumerate(self.vars):
+            val = f[dom]
+            der = None
+            if seed is not None:
+                sv, sd, sb = seed
+                der = sb if (vi == sv and dom == sd) else VD.zeros(self.doms[dom], sb.B)
+            out[name] = OTerm(dom, val, der)
+        return out
+
+    def _rows(self, kind, dom, base, bound):
+        d = self.doms[dom]
+        if kind == "inside":
+            return d.export_tau(base, 2)
+        return d.export_tau_boundary(base, bound)
+
+    def _export(self, kind, vd, dom, bound, nrows_expected=None):
+        d = self.doms[dom]
+        rows = self._rows(kind, dom, vd.base, bound)
+        if vd.zero:
+            return None, len(rows)
+        vd.coef()
+        cf = vd.cf.reshape(vd.B, -1)
+        M = np.zeros((len(rows), cf.shape[1]))
+        for r, row in enumerate(rows):
+            for idx, w in row:
+                M[r, idx] += w
+        return cf @ M.T, len(rows)
+
+    def residual(self):
+        F = []
+        for (kind, dom, bound, fn, odom, obound, fnr) in self.eqs:
+            t = fn(self._terms(dom), bound)
+            v, n = self._export(kind, t.val, dom, bound)
+            block = np.zeros(n) if v is None else v[0].copy()
+            if kind == "matching":
+                t2 = fnr(self._terms(odom), obound)
+                v2, _ = self._export(kind, t2.val, odom, obound)
+                if v2 is not None:
+                    block = block - v2[0]
+            F.append(block)
+        F = np.concatenate(F)
+        self.nbr_conditions = len(F)
+        return F
+
+    def unknown_layout(self):
+        layout = []
+        col = 0
+        for vi, (name, f) in enumerate(self.vars):
+            for dd in range(self.dmin, self.dmax + 1):
+                pats = self.doms[dd].unknown_patterns(f[dd].base)
+                layout.append((vi, dd, col, pats))
+                col += len(pats)
+        return layout, col
+
+    def jacobian(self):
+        F = self.residual()
+        layout, N = self.unknown_layout()
+        assert N == len(F), (N, len(F))
+        J = np.zeros((N, N))
+        row0 = []
+        r = 0
+        for eq in self.eqs:
+            kind, dom, bound, fn, odom, obound, fnr = eq
+            _, n = self._export(kind, fn(self._terms(dom), bound).val, dom, bound)
+            row0.append((r, n))
+            r += n
+        for vi, dd, col, pats in layout:
+            d = self.doms[dd]
+            B = len(pats)
+            seed = np.zeros((B, d.nc[0] * d.nc[1] * d.nc[2]))
+            for s, p in enumerate(pats):
+                for idx, w in p:
+                    seed[s, idx] = w
+            base = self.vars[vi][1][dd].base
+            sb = VD(d, B, cf=seed.reshape((B,) + d.nc), base=base)
+            for e, (kind, dom, bound, fn, odom, obound, fnr) in enumerate(self.eqs):
+                r0, n = row0[e]
+                if dom == dd:
+                    t = fn(self._terms(dom, (vi, dd, sb)), bound)
+                    v, _ = self._export(kind, t.der, dom, bound)
+                    if v is not None:
+                        J[r0:r0 + n, col:col + B] += v.T
+                if kind == "matching" and odom == dd:
+                    t = fnr(self._terms(odom, (vi, dd, sb)), obound)
+                    v, _ = self._export(kind, t.der, odom, obound)
+                    if v is not None:
+                        J[r0:r0 + n, col:col + B] -= v.T
+        return F, J
+
+    def update(self, x):
+        """xx_to_vars then var = old - new (do_newton_seq, src_par/do_newton.cpp:558-566)."""
+        layout, N = self.unknown_layout()
+        for vi, dd, col, pats in layout:
+            name, f = self.vars[vi]
+            d = self.doms[dd]
+            M = d.affecte_tau_matrix(f[dd].base)
+            cf = (M @ x[col:col + M.shape[1]]).reshape((1,) + d.nc)
+            new = VD(d, 1, cf=cf, base=f[dd].base)
+            f[dd] = f[dd] - new
+        for vi, (name, f) in enumerate(self.vars):
+            for dd in range(len(self.doms)):
+                if dd < self.dmin or dd > self.dmax:
+                    if not f[dd].zero:
+                        f[dd] = f[dd] - f[dd]
+
+    def newton_step(self, precision, solve=None):
+        import scipy.linalg as sla
+        F, J = self.jacobian()
+        err = float(np.max(np.abs(F)))
+        if err < precision:
+            return True, err, F, J
+        if solve is None:
+            x = sla.lu_solve(sla.lu_factor(J), F)
+        else:
+            x = solve(J, F)
+        self.update(x)
+        return False, err, F, J
+
+
+def scalar_field(doms, value_fn):
+    """A Scalar with std_base, values from value_fn(dom) -> (n0,n1,n2) array."""
+    out = {}
+    for d in doms:
+        out[d.num] = VD(d, 1, c=np.asarray(value_fn(d), dtype=float)[None].copy(), base=d.std_base())
+    return out
+
+
+def val_point(doms, field, point):
+    """Scalar::val_point: evaluate the spectral expansion at a Cartesian point."""
+    x, y, z = point
+    r = math.sqrt(x * x + y * y + z * z)
+    for d in doms:
+        rin = 0.0 if d.type == NUCLEUS else (d.beta - d.alpha if d.type == SHELL else -0.5 / d.alpha)
+        rout = d.alpha if d.type == NUCLEUS else (d.beta + d.alpha if d.type == SHELL else math.inf)
+        if rin - 1e-12 <= r <= rout + 1e-12:
+            break
+    if d.type == NUCLEUS:
+        xi = r / d.alpha
+    elif d.type == SHELL:
+        xi = (r - d.beta) / d.alpha
+    else:
+        xi = 1. + 1. / r / d.alpha
+    rho = math.sqrt(x * x + y * y)
+    if rho == 0:
+        th, ph = (0.0 if z >= 0 else math.pi), 0.0
+    else:
+        th = math.atan(rho / z) if z != 0 else math.pi / 2
+        ph = math.atan2(y, x)
+    if th < 0:
+        th += math.pi
+    v = field[d.num]
+    v.coef()
+    cf = v.cf[0]
+    b = v.base
+    nc0, nc1, nc2 = d.nc
+    # Base_spectral::summation: r first, then theta, then phi
+    lines = np.zeros((nc1, nc2))
+    for j in range(nc1):
+        for k in range(nc2):
+            lines[j, k] = S.summation_1d(int(b.r[j, k]), xi, cf[:, j, k])
+    tvals = np.array([S.summation_1d(int(b.t[k]), th, lines[:, k]) for k in range(nc2)])
+    return S.summation_1d(int(b.p), ph, tvals)

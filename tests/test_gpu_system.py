@@ -1,0 +1,170 @@
+"""GPU parity of the Newton-Raphson path against the oracle: residual
+(sec_member), dense Jacobian (all do_col_J columns), Newton updates and the
+converged fields, on the toy configuration and the reference's known-answer
+programs."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import configs, kadath as K
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-12     # residual / Jacobian, normwise relative (FP64 both sides)
+FIELD = 1e-10   # converged fields (the benchmark spec's bound)
+
+
+def build_toy(res=(13, 7, 4), bounds=(1.0, 2.0)):
+    from kadath_frontera_gb300.kadath import CHEB_TYPE, OUTER_BC, Scalar, Space_spheric, System_of_eqs
+    space = Space_spheric(CHEB_TYPE, (0, 0, 0), res, bounds)
+    nd = space.get_nbr_domains()
+    psi = Scalar(space, 1.0).std_base()
+    rho = Scalar(space)
+    doms = K.space_spheric(res, list(bounds))
+    for d in range(nd):
+        rho.set_domain(d, configs.toy_rho(doms[d]))
+    rho.std_base()
+    syst = System_of_eqs(space, 0, nd - 1)
+    syst.add_var("psi", psi)
+    syst.add_cst("pi", math.pi)
+    syst.add_cst("rho", rho)
+    for d in range(nd):
+        syst.add_eq_inside(d, "Lap(psi) + 2*pi*rho*psi^5 = 0")
+    for d in range(nd - 1):
+        syst.add_eq_matching(d, OUTER_BC, "psi")
+        syst.add_eq_matching(d, OUTER_BC, "dn(psi)")
+    syst.add_eq_bc(nd - 1, OUTER_BC, "psi = 1")
+    return space, syst, psi, rho
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def test_toy_residual_and_jacobian_match_oracle(ctx):
+    space, syst, psi, rho = build_toy()
+    doms, osys, opsi, orho = configs.toy()
+    F = syst.sec_member()
+    Fo = osys.residual()
+    assert F.shape == Fo.shape
+    assert rel(F, Fo) < REL
+    J = syst.jacobian()
+    Fo2, Jo = osys.jacobian()
+    assert J.shape == Jo.shape
+    assert rel(J, Jo) < REL
+    # do_col_J column access
+    assert rel(syst.do_col_J(5), Jo[:, 5]) < REL
+
+
+def test_toy_newton_iterates_match_oracle(ctx):
+    space, syst, psi, rho = build_toy()
+    doms, osys, opsi, orho = configs.toy()
+    for it in range(8):
+        done, err = syst.do_newton(1e-10)
+        odone, oerr, _, _ = osys.newton_step(1e-10)
+        assert done == odone
+        assert abs(err - oerr) <= 1e-10 * max(1.0, abs(oerr)) + 1e-13
+        for d in range(space.get_nbr_domains()):
+            g = psi.get_coef(d)
+            o = opsi[d]
+            o.coef()
+            assert rel(g, o.cf[0]) < FIELD
+        if done:
+            break
+    assert done
+
+
+def test_tuto5_known_answer_gpu(ctx):
+    from kadath_frontera_gb300.kadath import CHEB_TYPE, INNER_BC, OUTER_BC, Scalar, Space_spheric, System_of_eqs
+    space = Space_spheric(CHEB_TYPE, (0, 0, 0), (13, 5, 4), (1, 2, 4))
+    field = Scalar(space, 1.0).std_base()
+    syst = System_of_eqs(space, 1, 3)
+    syst.add_var("F", field)
+    syst.add_cst("a", 1.0)
+    for d in range(1, 4):
+        syst.add_eq_inside(d, "Lap(F)=0")
+    syst.add_eq_bc(1, INNER_BC, "dn(F) + 0.5*F/a = 0")
+    syst.add_eq_bc(3, OUTER_BC, "F=1")
+    for d in range(1, 3):
+        syst.add_eq_matching(d, OUTER_BC, "F")
+        syst.add_eq_matching(d, OUTER_BC, "dn(F)")
+    n = 0
+    while True:
+        done, err = syst.do_newton(1e-8)
+        if done:
+            break
+        n += 1
+        assert n < 5
+    assert n == 1
+    doms = K.space_spheric((13, 5, 4), [1.0, 2.0, 4.0])
+    of = {d.num: K.VD(d, 1, cf=field.get_coef(d.num)[None], base=d.std_base()) for d in doms}
+    num = K.val_point(doms, of, configs.TUTO_POINT)
+    rr = math.sqrt(sum(c * c for c in configs.TUTO_POINT))
+    assert abs(num - (1 + 1 / rr)) / num < 1e-8
+    # the nucleus (outside the system) is zeroed by the update, as in the reference
+    assert np.all(field.get_domain(0) == 0.0)
+
+
+def test_tuto6_grad_scal_definition(ctx):
+    """tutorials/tuto6.cpp: add_def with scal(grad(P), grad(P)); analytic log(1+a/r)."""
+    from kadath_frontera_gb300.kadath import CHEB_TYPE, INNER_BC, OUTER_BC, Scalar, Space_spheric, System_of_eqs
+    space = Space_spheric(CHEB_TYPE, (0, 0, 0), (13, 5, 4), (1, 2, 4))
+    field = Scalar(space, 1.0).std_base()
+    syst = System_of_eqs(space, 1, 3)
+    syst.add_var("P", field)
+    syst.add_def("dP2 = scal(grad(P), grad(P))")
+    syst.add_cst("a", 1.0)
+    for d in range(1, 4):
+        syst.add_eq_inside(d, "Lap(P) + dP2 = 0")
+    syst.add_eq_bc(1, INNER_BC, "dn(P) + 0.5/a = 0")
+    syst.add_eq_bc(3, OUTER_BC, "P=0")
+    for d in range(1, 3):
+        syst.add_eq_matching(d, OUTER_BC, "P")
+        syst.add_eq_matching(d, OUTER_BC, "dn(P)")
+    for it in range(20):
+        done, err = syst.do_newton(1e-8)
+        if done:
+            break
+    assert done
+    doms = K.space_spheric((13, 5, 4), [1.0, 2.0, 4.0])
+    of = {d.num: K.VD(d, 1, cf=field.get_coef(d.num)[None], base=d.std_base()) for d in doms}
+    num = K.val_point(doms, of, configs.TUTO_POINT)
+    rr = math.sqrt(sum(c * c for c in configs.TUTO_POINT))
+    ana = math.log(1 + 1 / rr)
+    assert abs(num - ana) / abs(num) < 1e-6
+
+
+def test_schwarz_matches_oracle_and_analytic(ctx):
+    from kadath_frontera_gb300.kadath import CHEB_TYPE, Scalar, Space_spheric, System_of_eqs
+    aa = 1.323
+    bounds = (aa, 1.7557 * aa, 2.9861 * aa)
+    space = Space_spheric(CHEB_TYPE, (0, 0, 0), (13, 5, 4), bounds)
+    conf = Scalar(space, 1.0).std_base()
+    syst = System_of_eqs(space, 1, 3)
+    syst.add_var("P", conf)
+    syst.add_cst("a", aa)
+    space.add_inner_bc(syst, "dn(P) + 0.5 / a * P = 0")
+    space.add_eq(syst, "Lap(P) = 0", "P", "dn(P)")
+    space.add_outer_bc(syst, "P=1")
+    doms, osys, oP = configs.schwarz(aa=aa)
+    while True:
+        done, err = syst.do_newton(1e-8)
+        odone, oerr, _, _ = osys.newton_step(1e-8)
+        assert done == odone
+        if done:
+            break
+    for d in range(1, 4):
+        oP[d].coef()
+        assert rel(conf.get_coef(d), oP[d].cf[0]) < FIELD
+
+
+def test_unknown_variable_is_an_error(ctx):
+    from kadath_frontera_gb300 import KadathError
+    from kadath_frontera_gb300.kadath import CHEB_TYPE, Scalar, Space_spheric, System_of_eqs
+    space = Space_spheric(CHEB_TYPE, (0, 0, 0), (9, 5, 4), (1, 2))
+    f = Scalar(space, 1.0).std_base()
+    syst = System_of_eqs(space, 0, 2)
+    syst.add_var("f", f)
+    with pytest.raises(KadathError, match="Unknown operator"):
+        syst.add_eq_inside(0, "Lap(g) = 0")
