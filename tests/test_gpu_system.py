@@ -48,10 +48,13 @@ def test_toy_residual_and_jacobian_match_oracle(ctx):
     F = syst.sec_member()
     Fo = osys.residual()
     assert F.shape == Fo.shape
-    assert rel(F, Fo) < REL
     J = syst.jacobian()
     Fo2, Jo = osys.jacobian()
     assert J.shape == Jo.shape
+    # F(u) at u = 1 is the roundoff of Lap(1) plus the source: compare on the
+    # scale of the operator (both sides amplify eps through the derivatives).
+    scale = np.abs(Jo).max()
+    assert np.abs(F - Fo).max() <= 1e-13 * scale
     assert rel(J, Jo) < REL
     # do_col_J column access
     assert rel(syst.do_col_J(5), Jo[:, 5]) < REL
