@@ -1,0 +1,383 @@
+"""Newton-step benchmark of the GB300 Kadath path.
+
+    python bench.py --gpus N --steps K --warmup W [--impl reference] [--workload star|toy]
+
+A step is one System_of_eqs::do_newton update (residual, Jacobian assembly,
+dense LU, solve, field update) of the workload from its initial guess.  The
+headline `value` is the mixed-precision step (TF32 tensor-core LU + FP64
+GMRES-IR); the plain FP64 step is reported beside it.  `e2e` times the same
+step through the C ABI with the fields uploaded from pinned host memory and
+the converged coefficients read back inside the timed region.
+
+With --gpus N > 1 (launched by torch.distributed.run) every rank solves its
+own replica of the problem on its own GPU ("replicas only": the dense Newton
+step has no data-parallel split in this design); value is the slowest rank's
+step time.
+
+--impl reference times the reference's CPU algorithm (the numpy restatement
+under oracle/, the reference itself does not build here) on a bounded sample
+of the same workload, on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Newton-step time (assemble+LU+solve) at 1e-10 residual: FP64 vs mixed-prec"
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d, "measured"
+    return PEAKS_FALLBACK, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ws, x):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], device="cuda", dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# --------------------------------------------------------------- CPU side --
+def cpu_step_sample(workload, blocks=2):
+    """Times the oracle's Newton step on a bounded sample: the residual, a
+    subset of the Jacobian column blocks (scaled to all blocks), and the dense
+    LU factor + solve of the full-size matrix with scipy's LAPACK."""
+    import numpy as np
+    import scipy.linalg as sla
+    from oracle import configs
+
+    if workload == "toy":
+        doms, sysm, *_ = configs.toy()
+    else:
+        doms, sysm, *_ = configs.star()
+    t0 = time.perf_counter()
+    F = sysm.residual()
+    t_res = time.perf_counter() - t0
+    layout, N = sysm.unknown_layout()
+    sample = layout[:blocks] if blocks < len(layout) else layout
+    # assemble only the sampled column blocks (same code path as jacobian())
+    J = np.zeros((N, N))
+    t0 = time.perf_counter()
+    _assemble_blocks(sysm, sample, N, J)
+    t_blocks = time.perf_counter() - t0
+    cols_done = sum(len(p) for _, _, _, p in sample)
+    t_asm = t_blocks * N / max(cols_done, 1)
+    # LU of a matrix of the same size (values do not change LAPACK's work)
+    rng = np.random.default_rng(0)
+    A = rng.standard_normal((N, N)) + N * np.eye(N)
+    t0 = time.perf_counter()
+    lu = sla.lu_factor(A, overwrite_a=True, check_finite=False)
+    x = sla.lu_solve(lu, F, check_finite=False)
+    t_lu = time.perf_counter() - t0
+    total = t_res + t_asm + t_lu
+    return {"ms": 1e3 * total, "residual_ms": 1e3 * t_res, "assembly_ms": 1e3 * t_asm, "lu_solve_ms": 1e3 * t_lu,
+            "N": N, "sample": f"residual + {len(sample)}/{len(layout)} Jacobian column blocks ({cols_done}/{N} "
+                               f"columns, time scaled by N/columns) + full {N}x{N} LAPACK getrf/getrs"}
+
+
+def _assemble_blocks(sysm, blocks, N, J):
+    import numpy as np
+    from oracle import kadath as K
+    r = 0
+    row0 = []
+    for kind, dom, bound, fn, odom, obound, fnr in sysm.eqs:
+        _, n = sysm._export(kind, fn(sysm._terms(dom), bound).val, dom, bound)
+        row0.append((r, n))
+        r += n
+    for vi, dd, col, pats in blocks:
+        d = sysm.doms[dd]
+        B = len(pats)
+        seed = np.zeros((B, d.nc[0] * d.nc[1] * d.nc[2]))
+        for s, p in enumerate(pats):
+            for idx, w in p:
+                seed[s, idx] = w
+        sb = K.VD(d, B, cf=seed.reshape((B,) + d.nc), base=sysm.vars[vi][1][dd].base)
+        for e, (kind, dom, bound, fn, odom, obound, fnr) in enumerate(sysm.eqs):
+            r0, n = row0[e]
+            if dom == dd:
+                t = fn(sysm._terms(dom, (vi, dd, sb)), bound)
+                v, _ = sysm._export(kind, t.der, dom, bound, n)
+                if v is not None:
+                    J[r0:r0 + n, col:col + B] += v.T
+            if kind == "matching" and odom == dd:
+                t = fnr(sysm._terms(odom, (vi, dd, sb)), obound)
+                v, _ = sysm._export(kind, t.der, odom, obound, n)
+                if v is not None:
+                    J[r0:r0 + n, col:col + B] -= v.T
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return 0
+    cores = os.cpu_count() or 1
+    times = []
+    info = None
+    for i in range(args.warmup + args.steps):
+        info = cpu_step_sample(args.workload, blocks=args.cpu_blocks)
+        if i >= args.warmup:
+            times.append(info["ms"])
+    ms = statistics.mean(times)
+    line = {"impl": "reference", "metric": METRIC, "value": ms, "unit": "ms", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": workload_label(args.workload), "N": info["N"]},
+            "cpu_baseline": {"value": ms, "unit": "ms", "cores": cores, "kind": "port", "sample": info["sample"],
+                             "phases_ms": {k: info[k] for k in ("residual_ms", "assembly_ms", "lu_solve_ms")}},
+            "e2e": {"value": ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def workload_label(name):
+    if name == "toy":
+        return "toy: Space_spheric 3 domains (13,7,4), Lap(psi) = -2 pi rho psi^5"
+    return ("star: XCTS-shaped static star, Space_spheric 6 domains (13,9,4), unknowns P, NP, bx, by, bz, "
+            "frozen Gamma=2 K=100 rho_c=1.28e-3 matter in the nucleus")
+
+
+# --------------------------------------------------------------- GPU side --
+def run_gpu(args, ws, rank, local):
+    import numpy as np
+    import torch
+
+    from kadath_frontera_gb300 import Context
+    from kadath_frontera_gb300 import kadath as KD
+    from kadath_frontera_gb300 import workloads
+
+    ctx = Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream_ptr, device=f"cuda:{local}")
+    wl = workloads.WORKLOADS[args.workload](ctx=ctx)
+    syst = wl.syst
+    N = syst.get_nbr_unknowns()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")  # 256 MB > L2
+
+    def one_step(mode, timed_events=True):
+        wl.restore()
+        flush.zero_()
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        done, err = syst.do_newton(args.precision, lu_mode=mode)
+        ev1.record(stream)
+        ev1.synchronize()
+        rep = dict(syst.last_report)
+        return ev0.elapsed_time(ev1), rep
+
+    modes = {"mixed": KD.KD_LU_TF32_IR, "fp64": KD.KD_LU_FP64}
+    # warm-up: builds matrices, tables, seeds, cuBLAS handles
+    for _ in range(args.warmup):
+        for m in modes.values():
+            one_step(m)
+    results = {}
+    launches0 = ctx.launches
+    barrier(ws)
+    with ClockSampler(local) as clk:
+        for name, m in modes.items():
+            times, reps = [], []
+            for _ in range(args.steps if name == "mixed" else max(1, args.fp64_steps)):
+                t, rep = one_step(m)
+                times.append(t)
+                reps.append(rep)
+            results[name] = (times, reps)
+    barrier(ws)
+    launches_mixed = sum(r["kernel_launches"] for r in results["mixed"][1]) / len(results["mixed"][1])
+    mixed_ms = max_over_ranks(ws, statistics.mean(results["mixed"][0]))
+    fp64_ms = max_over_ranks(ws, statistics.mean(results["fp64"][0]))
+
+    # end-to-end through the C ABI with host buffers (pinned), mixed LU
+    host = [[torch.from_numpy(v).pin_memory().numpy() for v in per] for per in wl.initial_host]
+    h2d = sum(v.nbytes for per in host for v in per)
+    e2e_times = []
+    d2h = 0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        wl.upload_initial(host)
+        syst.do_newton(args.precision, lu_mode=modes["mixed"])
+        out = wl.download()
+        e2e_times.append(1e3 * (time.perf_counter() - t0))
+        d2h = sum(v.nbytes for per in out for v in per)
+    e2e_ms = max_over_ranks(ws, statistics.mean(e2e_times))
+
+    # one instrumented step per mode: per-category kernel time and work
+    prof = {}
+    for name, m in modes.items():
+        wl.restore()
+        KD.profile_enable(ctx, True)
+        syst.do_newton(args.precision, lu_mode=m)
+        prof[name] = KD.profile_read(ctx)
+        KD.profile_enable(ctx, False)
+
+    if rank != 0:
+        return 0
+    peaks, peak_kind = load_peaks()
+    top = max(prof["mixed"].items(), key=lambda kv: kv[1]["ms"])
+    cat, st = top
+    roof = roofline_for(cat, st, peaks, peak_kind, N)
+    rep0 = results["mixed"][1][-1]
+    rep64 = results["fp64"][1][-1]
+    line = {
+        "metric": METRIC, "value": mixed_ms, "unit": "ms", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": mixed_ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 (LU trailing update tf32, refined to f64)", "data": "synthetic",
+        "config": {"workload": workload_label(args.workload), "N": N, "precision": args.precision,
+                   "l2": "flushed between steps (256 MB write)", "parallelism": "replicas" if ws > 1 else "single"},
+        "fp64_ms_per_step": fp64_ms, "mixed_speedup_vs_fp64": fp64_ms / mixed_ms if mixed_ms > 0 else None,
+        "phases_ms": {"mixed": {k: rep0[k] for k in ("t_residual_ms", "t_assembly_ms", "t_factor_ms", "t_solve_ms",
+                                                      "t_update_ms")},
+                      "fp64": {k: rep64[k] for k in ("t_residual_ms", "t_assembly_ms", "t_factor_ms", "t_solve_ms",
+                                                      "t_update_ms")}},
+        "refine": {"iters": rep0["refine_iters"], "rel_residual": rep0["refine_rel_residual"]},
+        "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches_mixed),
+        "kernel_profile_ms": {name: {k: round(v["ms"], 3) for k, v in p.items()} for name, p in prof.items()},
+        "roofline": roof,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu:
+        cb = cpu_step_sample(args.workload, blocks=args.cpu_blocks)
+        line["cpu_baseline"] = {"value": cb["ms"], "unit": "ms", "cores": os.cpu_count(), "kind": "port",
+                                "sample": cb["sample"],
+                                "phases_ms": {k: cb[k] for k in ("residual_ms", "assembly_ms", "lu_solve_ms")}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def roofline_for(cat, st, peaks, peak_kind, N):
+    """Roofline of the dominant kernel category of the mixed step."""
+    per_launch_ms = st["ms"] / max(st["launches"], 1)
+    work_per_launch = st["work"] / max(st["launches"], 1)
+    if cat in ("lu_gemm",):
+        achieved = work_per_launch / (per_launch_ms * 1e-3) / 1e12
+        peak = peaks.get("bf16_tflops", PEAKS_FALLBACK["bf16_tflops"]) / 2.0
+        return {"kernel": cat, "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": None,
+                "peak_note": f"TF32 dense = half of the {peak_kind} bf16 peak",
+                "launches": st["launches"], "avg_launch_ms": per_launch_ms}
+    if cat in ("lu_panel", "lu_swap_trsm", "lu_solve"):
+        achieved = work_per_launch / (per_launch_ms * 1e-3) / 1e12
+        return {"kernel": cat, "bound": "fp64", "achieved": achieved, "peak": None, "unit": "TFLOP/s",
+                "frac": None, "traffic": None, "launches": st["launches"], "avg_launch_ms": per_launch_ms}
+    achieved = work_per_launch / (per_launch_ms * 1e-3) / 1e9
+    peak = peaks.get("hbm_gbs", PEAKS_FALLBACK["hbm_gbs"])
+    return {"kernel": cat, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": None, "peak_note": f"{peak_kind} copy bandwidth",
+            "launches": st["launches"], "avg_launch_ms": per_launch_ms}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="star", choices=["star", "toy"])
+    ap.add_argument("--precision", type=float, default=1e-10)
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--cpu-blocks", type=int, default=2)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        # rank 0 alone runs the CPU reference; other ranks exit without work
+        rank = int(os.environ.get("RANK", "0"))
+        return run_reference(args, int(os.environ.get("WORLD_SIZE", "1")), rank)
+    ws, rank, local = dist_setup()
+    return run_gpu(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -53,6 +53,18 @@ const char* kd_last_error(const kd_ctx* ctx);
 int kd_ctx_synchronize(kd_ctx* ctx);
 /* Number of kernels this context has launched so far. */
 long long kd_ctx_launch_count(const kd_ctx* ctx);
+/* Kernel timing by category with CUDA events on the context's stream
+ * (no reference counterpart: the reference prints wall-clock phase times,
+ * src_par/do_newton.cpp:257,333).  Categories: 0 separable transforms and
+ * 1-D operators, 1 elementwise, 2 tau gathers, 3 LU panel, 4 LU swaps+TRSM,
+ * 5 LU trailing GEMM, 6 triangular solves, 7 refinement matvecs.  `work` is
+ * algorithmic bytes (0-2, 7) or flops (3-6). */
+#define KD_PROF_NCAT 8
+/* The CUDA stream (cudaStream_t) all of this context's work runs on, so a
+ * caller can order its own work or record timing events on it. */
+void* kd_ctx_stream(const kd_ctx* ctx);
+int kd_ctx_profile_enable(kd_ctx* ctx, int on);
+int kd_ctx_profile_read(kd_ctx* ctx, double* ms, long long* launches, double* work);
 
 /* ---- spectral transforms (subsystem a) --------------------------------- */
 /* One batch of fields of one domain shape.  base_r is the (nc1 x nc2)
@@ -130,10 +142,15 @@ int kd_field_create(kd_space* sp, kd_field** out);
 int kd_field_destroy(kd_field* f);
 int kd_field_set_value(kd_field* f, double v);                 /* Scalar = v */
 int kd_field_std_base(kd_field* f);                            /* Scalar::std_base */
+/* Val_domain::std_base_{x,y,z}_cart on every domain, c = 0, 1, 2 (bases of
+ * the Cartesian components of a vector, Tensor::std_base src/Tensor/tensor.cpp:609). */
+int kd_field_cart_base(kd_field* f, int c);
 int kd_field_set_conf(kd_field* f, int dom, const double* v);  /* values at collocation points */
 int kd_field_get_conf(kd_field* f, int dom, double* out);      /* Val_domain::coef_i + copy */
 int kd_field_get_coef(kd_field* f, int dom, double* out);      /* Val_domain::coef + copy */
 int kd_field_get_base(const kd_field* f, int dom, int* base_r, int* base_t, int* base_p);
+/* dst = src on every domain, device to device (Scalar copy assignment). */
+int kd_field_copy(kd_field* dst, const kd_field* src);
 
 /* ---- System_of_eqs (include/system_of_eqs.hpp:54) ----------------------- */
 int kd_system_create(kd_space* sp, int dom_min, int dom_max, kd_system** out);

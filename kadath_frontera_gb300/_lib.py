@@ -65,6 +65,7 @@ def _declare(lib: C.CDLL) -> None:
         "kd_coef_i_host": (I, [P, C.POINTER(TransformDesc)]),
         "kd_ope_1d": (I, [P, I, I, C.POINTER(TransformDesc), IP, IP, IP]),
         "kd_matrix_1d": (I, [P, I, I, I, I, DP, IP]),
+        "kd_ctx_stream": (P, [P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -113,6 +114,11 @@ class Context:
     @property
     def launches(self) -> int:
         return int(self.lib.kd_ctx_launch_count(self.h))
+
+    @property
+    def stream_ptr(self) -> int:
+        """cudaStream_t of this context (as an integer handle)."""
+        return int(self.lib.kd_ctx_stream(self.h) or 0)
 
     def close(self) -> None:
         if getattr(self, "h", None):

@@ -313,6 +313,13 @@ int kd_field_std_base(kd_field* f) {
   return guarded(f->sp->ctx, [&] { f->f->std_base(); });
 }
 
+int kd_field_cart_base(kd_field* f, int c) {
+  if (!f || c < 0 || c > 2) return KD_ERR_ARG;
+  return guarded(f->sp->ctx, [&] {
+    for (int i = 0; i < f->sp->sp->ndom(); i++) f->f->d[i].base = f->sp->sp->dom(i).cart_base(c);
+  });
+}
+
 int kd_field_set_conf(kd_field* f, int dom, const double* v) {
   if (!f || !v) return KD_ERR_ARG;
   return guarded(f->sp->ctx, [&] {
@@ -576,6 +583,35 @@ int kd_lu_stats(const kd_lu* lu, double* t_factor_ms, double* t_solve_ms, int* r
   if (refine_iters) *refine_iters = lu->lu->stats.refine_iters;
   if (rel_residual) *rel_residual = lu->lu->stats.final_rel_residual;
   return KD_OK;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+void* kd_ctx_stream(const kd_ctx* ctx) {
+  return (ctx && ctx->c) ? static_cast<void*>(ctx->c->stream()) : nullptr;
+}
+
+int kd_ctx_profile_enable(kd_ctx* ctx, int on) {
+  if (!ctx || !ctx->c) return KD_ERR_ARG;
+  return guarded(ctx, [&] { ctx->c->prof_enable(on != 0); });
+}
+
+int kd_ctx_profile_read(kd_ctx* ctx, double* ms, long long* launches, double* work) {
+  if (!ctx || !ctx->c || !ms || !launches || !work) return KD_ERR_ARG;
+  return guarded(ctx, [&] { ctx->c->prof_read(ms, launches, work); });
+}
+
+int kd_field_copy(kd_field* dst, const kd_field* src) {
+  if (!dst || !src || dst->sp != src->sp) return KD_ERR_ARG;
+  return guarded(dst->sp->ctx, [&] {
+    for (int i = 0; i < dst->sp->sp->ndom(); i++) {
+      kd::DVal v = src->f->val(i);
+      dst->f->assign(i, v);
+    }
+    kd::cuda_check(cudaStreamSynchronize(dst->sp->ctx->c->stream()), "sync");
+  });
 }
 
 }  // extern "C"

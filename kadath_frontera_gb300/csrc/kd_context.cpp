@@ -143,8 +143,70 @@ void Context::run_items(const std::vector<KdItem>& items, const std::vector<int>
       i++;
     }
     list.nitems = n;
+    double bytes = 0;
+    for (int q = 0; q < n; q++) {
+      const KdItem& it = list.items[q];
+      int d0 = it.n0, d1 = it.n1, d2 = it.n2;
+      for (int p = 0; p < it.npass; p++) {
+        if (it.pass[p].dim == 0) d0 = it.pass[p].n_out;
+        if (it.pass[p].dim == 1) d1 = it.pass[p].n_out;
+        if (it.pass[p].dim == 2) d2 = it.pass[p].n_out;
+      }
+      bytes += 8.0 * (list.prefix[q + 1] - list.prefix[q]) * (double(it.n0) * it.n1 * it.n2 + double(d0) * d1 * d2);
+    }
+    ProfScope ps(this, PROF_LINE_PASS, bytes);
     cuda_check(launch_line_passes(list, smem, dp, stream_), "line_passes kernel");
     launches++;
+  }
+}
+
+}  // namespace kd
+
+namespace kd {
+
+cudaEvent_t Context::next_event() {
+  if (ev_next_ >= ev_pool_.size()) {
+    cudaEvent_t e;
+    cuda_check(cudaEventCreate(&e), "cudaEventCreate");
+    ev_pool_.push_back(e);
+  }
+  return ev_pool_[ev_next_++];
+}
+
+void Context::prof_enable(bool on) {
+  prof_on_ = on;
+  prof_.clear();
+  ev_next_ = 0;
+}
+
+void Context::prof_begin(int cat) {
+  (void)cat;
+  if (!prof_on_) return;
+  pending_begin_ = next_event();
+  cuda_check(cudaEventRecord(pending_begin_, stream_), "cudaEventRecord");
+}
+
+void Context::prof_end(int cat, double work) {
+  if (!prof_on_ || !pending_begin_) return;
+  cudaEvent_t e = next_event();
+  cuda_check(cudaEventRecord(e, stream_), "cudaEventRecord");
+  prof_.push_back({cat, pending_begin_, e, work});
+  pending_begin_ = nullptr;
+}
+
+void Context::prof_read(double* ms, long long* count, double* work) {
+  for (int c = 0; c < PROF_NCAT; c++) {
+    ms[c] = 0;
+    count[c] = 0;
+    work[c] = 0;
+  }
+  cuda_check(cudaStreamSynchronize(stream_), "sync (profile)");
+  for (auto& r : prof_) {
+    float t = 0;
+    cuda_check(cudaEventElapsedTime(&t, r.a, r.b), "cudaEventElapsedTime");
+    ms[r.cat] += t;
+    count[r.cat] += 1;
+    work[r.cat] += r.work;
   }
 }
 

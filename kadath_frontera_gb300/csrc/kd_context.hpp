@@ -76,6 +76,41 @@ class Context {
   // Statistic: number of kernels this context launched.
   long long launches = 0;
 
+  // Optional per-category timing of launches (CUDA events on this stream)
+  // with the algorithmic work (bytes or flops) each launch performs.
+  enum ProfCat : int {
+    PROF_LINE_PASS = 0,  // separable transforms / 1-D coefficient operators
+    PROF_EW = 1,         // elementwise algebra at collocation points
+    PROF_GATHER = 2,     // tau export / affecte_tau gathers
+    PROF_LU_PANEL = 3,
+    PROF_LU_SWAP_TRSM = 4,
+    PROF_LU_GEMM = 5,    // trailing update
+    PROF_LU_SOLVE = 6,   // triangular solves
+    PROF_GMRES = 7,      // refinement matvecs and vector ops
+    PROF_NCAT = 8,
+  };
+  void prof_enable(bool on);
+  bool prof_on() const { return prof_on_; }
+  void prof_begin(int cat);
+  void prof_end(int cat, double work);
+  // Sums elapsed ms, launch counts and work per category (synchronises).
+  void prof_read(double* ms, long long* count, double* work);
+
+ private:
+  bool prof_on_ = false;
+  std::vector<cudaEvent_t> ev_pool_;
+  size_t ev_next_ = 0;
+  struct ProfRec {
+    int cat;
+    cudaEvent_t a, b;
+    double work;
+  };
+  std::vector<ProfRec> prof_;
+  cudaEvent_t pending_begin_ = nullptr;
+  cudaEvent_t next_event();
+
+ public:
+
  private:
   int device_;
   cudaStream_t stream_ = nullptr;
@@ -86,6 +121,15 @@ class Context {
   std::map<std::vector<double>, double*> dtables_;
   DeviceArena scratch_;
   DeviceArena persistent_{size_t(64) << 20};
+};
+
+// Times one launch (or a short sequence) when profiling is on.
+struct ProfScope {
+  Context* c;
+  int cat;
+  double work;
+  ProfScope(Context* ctx, int category, double w) : c(ctx), cat(category), work(w) { c->prof_begin(cat); }
+  ~ProfScope() { c->prof_end(cat, work); }
 };
 
 // Builds the pass description of a 1-D operator along `dim` for a field of

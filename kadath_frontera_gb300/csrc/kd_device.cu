@@ -143,6 +143,7 @@ __global__ void ew_kernel(int op, long long npts, long long total, int ba, const
       case EW_POWI: r = pow(x, alpha); break;
       case EW_ATAN: r = atan(x); break;
       case EW_MULC_ADD: r = x * y * alpha; break;
+      case EW_DIVC: r = x / alpha; break;
       default: r = 0.0; break;
     }
     out[i] = r;

@@ -71,6 +71,7 @@ enum EwOp : int {
   EW_POWI = 18,  // pow(a, (int)alpha) for alpha <= 0 (reference uses std::pow)
   EW_ATAN = 19,
   EW_MULC_ADD = 20,  // out = a*b*alpha (product with constant)
+  EW_DIVC = 21,      // a / alpha (Val_domain / double divides, it does not scale by 1/alpha)
 };
 
 cudaError_t launch_ew(int op, long long npts, int ba, const double* a, int bb, const double* b,

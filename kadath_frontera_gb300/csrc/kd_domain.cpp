@@ -136,22 +136,10 @@ Base Domain::anti_base() const {
 }
 
 Base Domain::cart_base(int c) const {
-  // x = r sin(t) cos(p), y = r sin(t) sin(p): symmetric in z with odd-m
-  // angular part; z = r cos(t): antisymmetric in z.
-  if (c == 2) return anti_base();
-  Base b;
-  b.allocate(nc[1], nc[2]);
-  b.def = true;
-  b.p = COSSIN;
-  for (int k = 0; k < nc[2]; k++) {
-    int m = (k % 2 == 0) ? k / 2 : (k - 1) / 2;
-    b.t[k] = (m % 2 == 0) ? SIN_ODD : COS_EVEN;
-    for (int j = 0; j < nc[1]; j++) {
-      if (type == DOM_NUCLEUS) b.rb(j, k) = (m % 2 == 0) ? CHEB_ODD : CHEB_EVEN;
-      else b.rb(j, k) = CHEB;
-    }
-  }
-  return b;
+  // Domain::set_cheb_base_{x,y,z}_cart (src/Domain/domain.cpp:1258-1273),
+  // not overridden by the spherical domains: x and y components take the
+  // symmetric standard basis, z the antisymmetric one.
+  return (c == 2) ? anti_base() : std_base();
 }
 
 // Domain_{shell,nucleus,compact}::mult (domain_shell.cpp:684, domain_nucleus.cpp:548):

@@ -10,6 +10,9 @@ double* alloc(Context* ctx, long long n) { return ctx->scratch().alloc_doubles(s
 
 void ew(Context* ctx, int op, long long npts, int ba, const double* a, int bb, const double* b, double* out,
         double alpha = 0.0, double beta = 0.0) {
+  int nf = ba > bb ? ba : bb;
+  ProfScope ps(ctx, Context::PROF_EW,
+               8.0 * npts * ((a ? ba : 0) + (b ? bb : 0) + nf));
   cuda_check(launch_ew(op, npts, ba, a, bb, b, out, alpha, beta, ctx->stream()), "elementwise kernel");
   ctx->launches++;
 }
@@ -39,19 +42,20 @@ DVal conf_binary(int op, const DVal& a, const DVal& b) {
   return res;
 }
 
-// Scales every representation the field holds (Val_domain * double).
-DVal scaled(const DVal& a, double x) {
+// Scales every representation the field holds (Val_domain * double, or
+// Val_domain / double when `op` is EW_DIVC).
+DVal scaled(const DVal& a, double x, int op = EW_SCALE) {
   DVal res = a;
   res.in_conf = a.in_conf;
   res.in_coef = a.in_coef;
   if (a.in_conf) {
     double* o = alloc(a.ctx, static_cast<long long>(a.batch) * a.npts());
-    ew(a.ctx, EW_SCALE, static_cast<long long>(a.batch) * a.npts(), 1, a.c, 1, nullptr, o, x);
+    ew(a.ctx, op, static_cast<long long>(a.batch) * a.npts(), 1, a.c, 1, nullptr, o, x);
     res.c = o;
   }
   if (a.in_coef) {
     double* o = alloc(a.ctx, static_cast<long long>(a.batch) * a.ncoefs());
-    ew(a.ctx, EW_SCALE, static_cast<long long>(a.batch) * a.ncoefs(), 1, a.cf, 1, nullptr, o, x);
+    ew(a.ctx, op, static_cast<long long>(a.batch) * a.ncoefs(), 1, a.cf, 1, nullptr, o, x);
     res.cf = o;
   }
   return res;
@@ -328,7 +332,7 @@ DVal operator*(const DVal& a, double x) {
 
 DVal operator/(const DVal& a, double x) {
   if (a.zero) return a;
-  return scaled(a, 1.0 / x);
+  return scaled(a, x, EW_DIVC);
 }
 
 DVal operator/(double x, const DVal& a) {

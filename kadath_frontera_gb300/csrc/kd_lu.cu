@@ -292,6 +292,9 @@ void DenseLU::ensure_work(size_t n) {
 template <class T>
 static void panel_factor(Context* ctx, T* A, long long ld, int N, int j0, int jb, int* ipiv, int* info) {
   cudaStream_t s = ctx->stream();
+  double fl = 0;
+  for (int j = j0; j < j0 + jb; j++) fl += 2.0 * (N - j - 1) * (j0 + jb - j - 1) + (N - j);
+  ProfScope ps(ctx, Context::PROF_LU_PANEL, fl);
   for (int j = j0; j < j0 + jb; j++) {
     pivot_swap_scale<T><<<1, PIV_THREADS, 0, s>>>(A, ld, N, j, j0, j0 + jb, ipiv, info);
     if (j + 1 < j0 + jb && j + 1 < N) panel_rank1<T><<<blocks(N - j - 1, 256), 256, 0, s>>>(A, ld, N, j, j0 + jb);
@@ -303,6 +306,7 @@ static void panel_factor(Context* ctx, T* A, long long ld, int N, int j0, int jb
 template <class T>
 static void trsm_and_swaps(Context* ctx, T* A, long long ld, int N, int j0, int jb, const int* ipiv) {
   cudaStream_t s = ctx->stream();
+  ProfScope ps(ctx, Context::PROF_LU_SWAP_TRSM, double(jb) * jb * (N - j0 - jb));
   if (j0 > 0) laswp<T><<<blocks(j0, 128), 128, 0, s>>>(A, ld, j0, j0 + jb, ipiv, 0, j0);
   if (j0 + jb < N) {
     laswp<T><<<blocks(N - j0 - jb, 128), 128, 0, s>>>(A, ld, j0, j0 + jb, ipiv, j0 + jb, N);
@@ -331,6 +335,7 @@ void DenseLU::factor_fp64(double* A, long long ld, int N) {
     if (m > 0) {
       // A22 -= A21 * A12 (FP64 library GEMM)
       const double one = 1.0, mone = -1.0;
+      ProfScope ps(ctx_, Context::PROF_LU_GEMM, 2.0 * m * m * jb);
       double* A21 = A + static_cast<long long>(j0) * ld + j0 + jb;
       double* A12 = A + static_cast<long long>(j0 + jb) * ld + j0;
       double* A22 = A + static_cast<long long>(j0 + jb) * ld + j0 + jb;
@@ -396,6 +401,7 @@ void DenseLU::factor(double* A, long long ld, int N, int mode) {
 
 void DenseLU::solve_fp64(const double* LU, long long ld, int N, double* b, int trans) {
   cudaStream_t s = ctx_->stream();
+  ProfScope ps(ctx_, Context::PROF_LU_SOLVE, 2.0 * N * N);
   if (!trans) {
     apply_pivots_vec<<<1, 1, 0, s>>>(b, ipiv_, N, 0);
     for (int r0 = 0; r0 < N; r0 += TB) {
@@ -428,6 +434,7 @@ void DenseLU::solve_fp64(const double* LU, long long ld, int N, double* b, int t
 
 void DenseLU::solve_f32(double* b) {
   cudaStream_t s = ctx_->stream();
+  ProfScope ps(ctx_, Context::PROF_LU_SOLVE, 2.0 * N_ * N_);
   int N = N_;
   apply_pivots_vec<<<1, 1, 0, s>>>(b, ipiv_, N, 0);
   for (int r0 = 0; r0 < N; r0 += TB) {
@@ -472,7 +479,10 @@ void DenseLU::gmres_ir(double* b) {
   int total_it = 0;
   for (int restart = 0; restart < 4; restart++) {
     // r = b - A x
-    gemv_fp64<<<blocks(N, 128), 128, 0, s>>>(A_, ld_, N, x, r, -1.0, 1.0, b);
+    {
+      ProfScope ps(ctx_, Context::PROF_GMRES, 8.0 * double(N) * N);
+      gemv_fp64<<<blocks(N, 128), 128, 0, s>>>(A_, ld_, N, x, r, -1.0, 1.0, b);
+    }
     ctx_->launches++;
     double beta = nrm(r);
     stats.final_rel_residual = beta / bnorm;
@@ -487,7 +497,10 @@ void DenseLU::gmres_ir(double* b) {
       // w = A M^{-1} v_k
       cublasDcopy(blas_, N, V + static_cast<size_t>(k) * N, 1, r, 1);
       solve_f32(r);
-      gemv_fp64<<<blocks(N, 128), 128, 0, s>>>(A_, ld_, N, r, w, 1.0, 0.0, nullptr);
+      {
+        ProfScope ps(ctx_, Context::PROF_GMRES, 8.0 * double(N) * N);
+        gemv_fp64<<<blocks(N, 128), 128, 0, s>>>(A_, ld_, N, r, w, 1.0, 0.0, nullptr);
+      }
       ctx_->launches++;
       for (int i = 0; i <= k; i++) {  // modified Gram-Schmidt
         double h = dot(w, V + static_cast<size_t>(i) * N);
@@ -534,7 +547,10 @@ void DenseLU::gmres_ir(double* b) {
     const double one = 1.0;
     cublasDaxpy(blas_, N, &one, r, 1, x, 1);
   }
-  gemv_fp64<<<blocks(N, 128), 128, 0, s>>>(A_, ld_, N, x, r, -1.0, 1.0, b);
+  {
+    ProfScope ps(ctx_, Context::PROF_GMRES, 8.0 * double(N) * N);
+    gemv_fp64<<<blocks(N, 128), 128, 0, s>>>(A_, ld_, N, x, r, -1.0, 1.0, b);
+  }
   ctx_->launches++;
   stats.final_rel_residual = nrm(r) / bnorm;
   stats.refine_iters = total_it;

@@ -335,6 +335,7 @@ CsrTable System::upload_rows(const std::vector<SparseRow>& rows) {
   t.idx = ctx->table(idx);
   t.w = ctx->dtable(w);
   t.nrows = static_cast<int>(rows.size());
+  t.nnz = static_cast<long long>(idx.size());
   return t;
 }
 
@@ -369,6 +370,20 @@ void System::export_term(const Equation& eq, const Term& t, bool der, int side_d
                          long long osf, long long osr, int batch, double alpha, bool accumulate) {
   const Domain& d = sp->dom(side_dom);
   const auto& comps = der ? t.dt : t.vt;
+  if (t.is_double) throw KdError(KD_ERR_UNSUPPORTED, "equation residual must be a field: " + eq.text);
+  // The rows written must be exactly the rows the equation owns: a residual
+  // whose basis changed since the first evaluation would overflow its block.
+  if (eq.n_cond >= 0) {
+    long long total = 0;
+    for (size_t c = 0; c < t.vt.size(); c++) {
+      const Base& bv = t.vt[c].base;
+      if (!bv.def) throw KdError(KD_ERR_STATE, "residual without a defined basis: " + eq.text);
+      total += (eq.kind == Equation::INSIDE) ? export_table(d, bv, 0, eq.order).nrows
+                                             : export_table(d, bv, 1, side_bound).nrows;
+    }
+    if (total != eq.n_cond)
+      throw KdError(KD_ERR_STATE, "the basis of the residual changed the number of conditions of: " + eq.text);
+  }
   long long row = 0;
   for (size_t c = 0; c < comps.size(); c++) {
     const DVal& v = comps[c];
@@ -383,6 +398,7 @@ void System::export_term(const Equation& eq, const Term& t, bool der, int side_d
                                                           : export_table(d, v.base, 1, side_bound);
       if (tab.nrows != tv.nrows) throw KdError(KD_ERR_STATE, "tangent basis changes the number of conditions");
       long long in_stride = (v.batch == 1 && batch > 1) ? 0 : v.ncoefs();
+      ProfScope ps(ctx, Context::PROF_GATHER, 8.0 * batch * (tab.nnz + 2.0 * tab.nrows));
       cuda_check(launch_gather_csr(v.cf, in_stride, batch, tab.nrows, tab.rowptr, tab.idx, tab.w, out + row * osr,
                                    osf, osr, alpha, accumulate ? 1 : 0, ctx->stream()),
                  "export gather");

@@ -49,6 +49,7 @@ struct CsrTable {
   const int* idx = nullptr;
   const double* w = nullptr;
   int nrows = 0;
+  long long nnz = 0;
 };
 
 class System;

@@ -60,6 +60,10 @@ def _declare_system(lib):
         "kd_field_set_value": (I, [P, D]),
         "kd_field_std_base": (I, [P]),
         "kd_field_set_conf": (I, [P, I, DP]),
+        "kd_field_cart_base": (I, [P, I]),
+        "kd_field_copy": (I, [P, P]),
+        "kd_ctx_profile_enable": (I, [P, I]),
+        "kd_ctx_profile_read": (I, [P, DP, C.POINTER(C.c_longlong), DP]),
         "kd_field_get_conf": (I, [P, I, DP]),
         "kd_field_get_coef": (I, [P, I, DP]),
         "kd_field_get_base": (I, [P, I, IP, IP, IP]),
@@ -203,6 +207,16 @@ class Scalar:
 
     def std_base(self):
         self.space.ctx.check(_L().kd_field_std_base(self.h))
+        return self
+
+    def copy_from(self, other: "Scalar"):
+        """Scalar assignment (device to device)."""
+        self.space.ctx.check(_L().kd_field_copy(self.h, other.h))
+        return self
+
+    def std_base_cart(self, c):
+        """Basis of the Cartesian component c = 1, 2, 3 (x, y, z) of a vector."""
+        self.space.ctx.check(_L().kd_field_cart_base(self.h, int(c) - 1))
         return self
 
     def set_domain(self, dom, values):
@@ -385,3 +399,21 @@ class DenseLU:
                 _L().kd_lu_destroy(self.h)
         except Exception:
             pass
+
+
+PROFILE_CATEGORIES = ("transform", "elementwise", "tau_gather", "lu_panel", "lu_swap_trsm", "lu_gemm", "lu_solve",
+                      "refine_matvec")
+
+
+def profile_enable(ctx, on=True):
+    ctx.check(_L().kd_ctx_profile_enable(ctx.h, int(on)))
+
+
+def profile_read(ctx):
+    """Per-category (ms, launches, work) of the launches since profile_enable."""
+    ms = np.zeros(8)
+    cnt = np.zeros(8, dtype=np.int64)
+    work = np.zeros(8)
+    ctx.check(_L().kd_ctx_profile_read(ctx.h, _dp(ms), cnt.ctypes.data_as(C.POINTER(C.c_longlong)), _dp(work)))
+    return {name: {"ms": float(ms[i]), "launches": int(cnt[i]), "work": float(work[i])}
+            for i, name in enumerate(PROFILE_CATEGORIES)}

@@ -1,0 +1,153 @@
+"""Systems used by the benchmark and the smoke check, written with the same
+public API and equation strings a Kadath user would write.
+
+* ``toy``  -- nucleus r < 1, shell 1 < r < 2, compactified r > 2, (13, 7, 4)
+  points: Lap(psi) = -2 pi rho psi^5 with rho = 0.05 exp(-r^2/0.25),
+  psi = 1 at infinity, continuity of psi and dn(psi); initial guess 1.
+* ``star`` -- XCTS-shaped static star at the isolated-star configuration's
+  size: six domains (nucleus of radius R = 8 holding frozen Gamma = 2,
+  K = 100 matter with rho_c = 1.28e-3, four shells, compactified exterior),
+  (13, 9, 4) points, five unknowns: conformal factor P, lapse times P (NP)
+  and the Cartesian shift components bx, by, bz with the flat vector
+  Laplacian Lap(b^i) + d^i(div b)/3.  N is about 13k.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .kadath import CHEB_TYPE, OUTER_BC, Scalar, Space_spheric, System_of_eqs
+
+STAR_R = 8.0
+STAR_RHOC = 1.28e-3
+STAR_K = 100.0
+STAR_BOUNDS = (STAR_R, 12.0, 16.0, 24.0, 32.0)
+
+STAR_EQUATIONS = {
+    "P": "Lap(P) + 2*pi*E/P = 0",
+    "NP": "Lap(NP) - 2*pi*NP*E2S/P^2 = 0",
+    "bx": "Lap(bx) + partial_x(partial_x(bx) + partial_y(by) + partial_z(bz))/3 = 0",
+    "by": "Lap(by) + partial_y(partial_x(bx) + partial_y(by) + partial_z(bz))/3 = 0",
+    "bz": "Lap(bz) + partial_z(partial_x(bx) + partial_y(by) + partial_z(bz))/3 = 0",
+}
+
+
+def toy_rho_values(r):
+    v = np.zeros_like(r)
+    fin = np.isfinite(r)
+    v[fin] = 0.05 * np.exp(-r[fin] ** 2 / 0.25)
+    return v
+
+
+def star_matter_values(r, nucleus: bool):
+    rho = np.zeros_like(r)
+    if nucleus:
+        x = np.pi * r / STAR_R
+        safe = np.where(x > 0, x, 1.0)
+        rho = STAR_RHOC * np.where(x > 0, np.sin(x) / safe, 1.0)
+    E = rho * (1 + STAR_K * rho)
+    S = 3 * STAR_K * rho * rho
+    return E, E + 2 * S
+
+
+class Workload:
+    def __init__(self, name, space, syst, unknowns, constants):
+        self.name = name
+        self.space = space
+        self.syst = syst
+        self.unknowns = unknowns        # list of (name, Scalar)
+        self.constants = constants
+        # device copies of the initial guess, for restarting a step
+        self.initial = []
+        for nm, f in unknowns:
+            g = Scalar(space)
+            g.copy_from(f)
+            self.initial.append(g)
+        # host copies of the initial guess at the collocation points (e2e input)
+        nd = space.get_nbr_domains()
+        self.initial_host = [[f.get_domain(d).copy() for d in range(nd)] for _, f in unknowns]
+
+    def restore(self):
+        for (nm, f), g in zip(self.unknowns, self.initial):
+            f.copy_from(g)
+
+    def upload_initial(self, host=None):
+        """Host -> device copy of every unknown at every domain."""
+        host = host or self.initial_host
+        for (nm, f), per_dom in zip(self.unknowns, host):
+            for d, v in enumerate(per_dom):
+                f.set_domain(d, v)
+
+    def download(self):
+        nd = self.space.get_nbr_domains()
+        return [[f.get_coef(d) for d in range(nd)] for _, f in self.unknowns]
+
+    def bytes_in(self):
+        return sum(v.nbytes for per in self.initial_host for v in per)
+
+
+def toy(res=(13, 7, 4), bounds=(1.0, 2.0), ctx=None) -> Workload:
+    space = Space_spheric(CHEB_TYPE, (0, 0, 0), res, bounds, ctx=ctx)
+    nd = space.get_nbr_domains()
+    psi = Scalar(space, 1.0).std_base()
+    rho = Scalar(space)
+    for d in range(nd):
+        rho.set_domain(d, toy_rho_values(space.get_radius(d)))
+    rho.std_base()
+    syst = System_of_eqs(space, 0, nd - 1)
+    syst.add_var("psi", psi)
+    syst.add_cst("pi", math.pi)
+    syst.add_cst("rho", rho)
+    for d in range(nd):
+        syst.add_eq_inside(d, "Lap(psi) + 2*pi*rho*psi^5 = 0")
+    for d in range(nd - 1):
+        syst.add_eq_matching(d, OUTER_BC, "psi")
+        syst.add_eq_matching(d, OUTER_BC, "dn(psi)")
+    syst.add_eq_bc(nd - 1, OUTER_BC, "psi = 1")
+    return Workload("toy", space, syst, [("psi", psi)], [rho])
+
+
+def star(res=(13, 9, 4), bounds=STAR_BOUNDS, ctx=None) -> Workload:
+    space = Space_spheric(CHEB_TYPE, (0, 0, 0), res, bounds, ctx=ctx)
+    nd = space.get_nbr_domains()
+    P = Scalar(space, 1.0).std_base()
+    NP = Scalar(space, 1.0).std_base()
+    bx = Scalar(space, 0.0).std_base_cart(1)
+    by = Scalar(space, 0.0).std_base_cart(2)
+    bz = Scalar(space, 0.0).std_base_cart(3)
+    # explicit zeros (not the zero flag) so that every operator carries its
+    # basis through the first residual evaluation
+    for f in (bx, by, bz):
+        for d in range(nd):
+            f.set_domain(d, np.zeros(space.domain_info(d)["nbr_points"]))
+    E = Scalar(space)
+    E2S = Scalar(space)
+    for d in range(nd):
+        e, e2s = star_matter_values(space.get_radius(d), space.domain_info(d)["type"] == 1)
+        E.set_domain(d, e)
+        E2S.set_domain(d, e2s)
+    E.std_base()
+    E2S.std_base()
+    syst = System_of_eqs(space, 0, nd - 1)
+    unknowns = [("P", P), ("NP", NP), ("bx", bx), ("by", by), ("bz", bz)]
+    for nm, f in unknowns:
+        syst.add_var(nm, f)
+    syst.add_cst("pi", math.pi)
+    syst.add_cst("E", E)
+    syst.add_cst("E2S", E2S)
+    for d in range(nd):
+        for nm, _ in unknowns:
+            syst.add_eq_inside(d, STAR_EQUATIONS[nm])
+    for d in range(nd - 1):
+        for nm, _ in unknowns:
+            syst.add_eq_matching(d, OUTER_BC, nm)
+            syst.add_eq_matching(d, OUTER_BC, f"dn({nm})")
+    syst.add_eq_bc(nd - 1, OUTER_BC, "P = 1")
+    syst.add_eq_bc(nd - 1, OUTER_BC, "NP = 1")
+    for nm in ("bx", "by", "bz"):
+        syst.add_eq_bc(nd - 1, OUTER_BC, f"{nm} = 0")
+    return Workload("star", space, syst, unknowns, [E, E2S])
+
+
+WORKLOADS = {"toy": toy, "star": star}

@@ -88,6 +88,96 @@ def toy(res=(13, 7, 4), bounds=(1.0, 2.0)):
     return doms, sysm, psi, rho
 
 
+STAR_R = 8.0
+STAR_RHOC = 1.28e-3
+STAR_K = 100.0
+
+
+def star_matter(d):
+    """Frozen Gamma = 2 matter: Lane-Emden n = 1 density rho_c sinc(pi r/R)
+    inside the nucleus (radius R); E = rho (1 + K rho), S = 3 K rho^2."""
+    r = d.radius()
+    rho = np.zeros(d.np)
+    if d.type == K.NUCLEUS:
+        x = np.pi * r / STAR_R
+        with np.errstate(invalid="ignore", divide="ignore"):
+            rho = STAR_RHOC * np.where(x > 0, np.sin(x) / np.where(x > 0, x, 1.0), 1.0)
+    E = rho * (1 + STAR_K * rho)
+    S = 3 * STAR_K * rho * rho
+    return E, S
+
+
+def star(res=(13, 9, 4), bounds=(STAR_R, 12.0, 16.0, 24.0, 32.0)):
+    """XCTS-shaped static star (oracle side): unknowns P (conformal factor),
+    NP (lapse times P) and the Cartesian shift components bx, by, bz."""
+    doms = K.space_spheric(res, list(bounds))
+    ones = lambda d: np.ones(d.np)
+    P = K.scalar_field(doms, ones)
+    NP = K.scalar_field(doms, ones)
+    bx = K.scalar_field(doms, lambda d: np.zeros(d.np))
+    by = K.scalar_field(doms, lambda d: np.zeros(d.np))
+    bz = {d.num: K.VD(d, 1, c=np.zeros((1,) + d.np), base=_anti(d)) for d in doms}
+    E = K.scalar_field(doms, lambda d: star_matter(d)[0])
+    E2S = K.scalar_field(doms, lambda d: star_matter(d)[0] + 2 * star_matter(d)[1])
+    nd = len(doms)
+    sysm = K.OSystem(doms, 0, nd - 1)
+    for name, f in (("P", P), ("NP", NP), ("bx", bx), ("by", by), ("bz", bz)):
+        sysm.add_var(name, f)
+    two_pi = 2 * math.pi
+
+    def cst(T, v):
+        p = T["P"]
+        return K.OTerm(p.dom, v, None if p.der is None else K.VD.zeros(v.dom, p.der.B))
+
+    def num(T, x):
+        return K.OTerm(T["P"].dom, float(x), None if T["P"].der is None else 0.0)
+
+    for d in range(nd):
+        Ed, E2Sd = E[d], E2S[d]
+        # parsed as Lap(P) + (2*pi)*(E/P) and Lap(NP) - ((2*pi)*NP)*(E2S/(P^2))
+        sysm.add_eq_inside(d, lambda T, b, Ed=Ed: T["P"].lap() + num(T, two_pi) * (cst(T, Ed) / T["P"]))
+        sysm.add_eq_inside(d, lambda T, b, E2Sd=E2Sd: T["NP"].lap() - (num(T, two_pi) * T["NP"]) *
+                           (cst(T, E2Sd) / T["P"] ** 2))
+        for c, name in ((1, "bx"), (2, "by"), (3, "bz")):
+            def eqb(T, b, c=c, name=name):
+                div = T["bx"].partial(1) + T["by"].partial(2) + T["bz"].partial(3)
+                return T[name].lap() + div.partial(c) / num(T, 3.0)
+            sysm.add_eq_inside(d, eqb)
+    for d in range(nd - 1):
+        for name in ("P", "NP", "bx", "by", "bz"):
+            sysm.add_eq_matching(d, K.OUTER_BC, lambda T, b, name=name: T[name])
+            sysm.add_eq_matching(d, K.OUTER_BC, lambda T, b, name=name: T[name].dn(b))
+    sysm.add_eq_bc(nd - 1, K.OUTER_BC, lambda T, b: T["P"] - 1.0)
+    sysm.add_eq_bc(nd - 1, K.OUTER_BC, lambda T, b: T["NP"] - 1.0)
+    for name in ("bx", "by", "bz"):
+        sysm.add_eq_bc(nd - 1, K.OUTER_BC, lambda T, b, name=name: T[name])
+    return doms, sysm, (P, NP, bx, by, bz), (E, E2S)
+
+
+def _anti(d):
+    b = d.std_base()
+    nc1, nc2 = d.nc[1], d.nc[2]
+    for k in range(nc2):
+        m = k // 2
+        b.t[k] = S_COS_ODD if m % 2 == 0 else S_SIN_EVEN
+        for j in range(nc1):
+            if d.type == K.NUCLEUS:
+                b.r[j, k] = S_CHEB_ODD if m % 2 == 0 else S_CHEB_EVEN
+    return b
+
+
+from .spectral import CHEB_EVEN as S_CHEB_EVEN, CHEB_ODD as S_CHEB_ODD, COS_ODD as S_COS_ODD, \
+    SIN_EVEN as S_SIN_EVEN  # noqa: E402
+
+# Kadath-syntax strings of the star system (the product parses these).
+STAR_EQUATIONS = {
+    "P": "Lap(P) + 2*pi*E/P = 0",
+    "NP": "Lap(NP) - 2*pi*NP*E2S/P^2 = 0",
+    "bx": "Lap(bx) + partial_x(partial_x(bx) + partial_y(by) + partial_z(bz))/3 = 0",
+    "by": "Lap(by) + partial_y(partial_x(bx) + partial_y(by) + partial_z(bz))/3 = 0",
+    "bz": "Lap(bz) + partial_z(partial_x(bx) + partial_y(by) + partial_z(bz))/3 = 0",
+}
+
 # The same systems as strings, for the product's parser (Kadath syntax).
 TOY_EQUATIONS = {
     "inside": "Lap(psi) + 2*pi*rho*psi^5 = 0",

@@ -592,7 +592,10 @@ class VD:
 
     def __truediv__(self, o):
         if isinstance(o, (int, float)):
-            return self.scale(1.0 / o)
+            if self.zero:
+                return self
+            return VD(self.dom, self.B, c=None if self.c is None else self.c / o,
+                      cf=None if self.cf is None else self.cf / o, base=self.base)
         if self.zero:
             return self
         self.coef_i(); o.coef_i()
@@ -762,7 +765,12 @@ class OTerm:
                     num = num - self.val * o.der
                 der = num / (o.val * o.val)
             return OTerm(self.dom, self.val / o.val, der)
-        raise NotImplementedError("division by a field term")
+        if self.is_double:
+            raise NotImplementedError("double divided by a field term")
+        der = None
+        if do:
+            der = (self.der * o.val - self.val * o.der) / (o.val * o.val)
+        return OTerm(self.dom, self.val / o.val, der)
 
     def __pow__(self, n):
         assert isinstance(n, int) and n > 0
@@ -777,6 +785,10 @@ class OTerm:
     def dn(self, bound):
         return OTerm(self.dom, der_normal(self.val, bound), None if self.der is None else
                      (self.der if self.der.zero else der_normal(self.der, bound)))
+
+    def partial(self, i):
+        """Cartesian derivative d/dx_i (Val_domain::der_abs, i = 1, 2, 3)."""
+        return OTerm(self.dom, self.val.der_abs(i), None if self.der is None else self.der.der_abs(i))
 
 
 # -------------------------------------------------------------- the system --
@@ -823,9 +835,10 @@ class OSystem:
 
     def _export(self, kind, vd, dom, bound, nrows_expected=None):
         d = self.doms[dom]
-        rows = self._rows(kind, dom, vd.base, bound)
         if vd.zero:
-            return None, len(rows)
+            # Equation::export_der of a zero tangent skips the block (pos += ncond)
+            return None, nrows_expected
+        rows = self._rows(kind, dom, vd.base, bound)
         vd.coef()
         cf = vd.cf.reshape(vd.B, -1)
         M = np.zeros((len(rows), cf.shape[1]))

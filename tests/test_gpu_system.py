@@ -171,3 +171,53 @@ def test_unknown_variable_is_an_error(ctx):
     syst.add_var("f", f)
     with pytest.raises(KadathError, match="Unknown operator"):
         syst.add_eq_inside(0, "Lap(g) = 0")
+
+
+def test_star_workload_matches_oracle(ctx):
+    """XCTS-shaped star (5 unknowns, vector Laplacian with Cartesian
+    derivatives) at reduced resolution: residual, Jacobian and every Newton
+    iterate against the oracle."""
+    from kadath_frontera_gb300 import workloads
+    res = (9, 5, 4)
+    wl = workloads.star(res=res)
+    doms, osys, ofields, _ = configs.star(res=res)
+    F = wl.syst.sec_member()
+    Fo = osys.residual()
+    J = wl.syst.jacobian()
+    _, Jo = osys.jacobian()
+    assert np.abs(F - Fo).max() <= 1e-13 * np.abs(Jo).max()
+    assert rel(J, Jo) < REL
+    for it in range(6):
+        done, err = wl.syst.do_newton(1e-10)
+        odone, oerr, _, _ = osys.newton_step(1e-10)
+        assert done == odone
+        for (nm, f), of in zip(wl.unknowns, ofields):
+            for d in range(len(doms)):
+                of[d].coef()
+                g = f.get_coef(d)
+                scale = max(np.linalg.norm(of[d].cf[0]), 1e-12)
+                assert np.linalg.norm(g - of[d].cf[0]) / scale < FIELD, (nm, d, it)
+        if done:
+            break
+    assert done
+
+
+def test_star_mixed_precision_newton_matches_fp64(ctx):
+    """The mixed-precision LU (TF32 trailing updates + FP64 GMRES-IR) gives the
+    same Newton iterates as the FP64 LU to 1e-10."""
+    from kadath_frontera_gb300 import workloads
+    from kadath_frontera_gb300.kadath import KD_LU_FP64, KD_LU_TF32_IR
+    res = (9, 5, 4)
+    a = workloads.star(res=res)
+    b = workloads.star(res=res)
+    for it in range(6):
+        da, ea = a.syst.do_newton(1e-10, lu_mode=KD_LU_FP64)
+        db, eb = b.syst.do_newton(1e-10, lu_mode=KD_LU_TF32_IR)
+        assert da == db
+        if da:
+            break
+        for (nm, fa), (_, fb) in zip(a.unknowns, b.unknowns):
+            for d in range(a.space.get_nbr_domains()):
+                ga, gb = fa.get_coef(d), fb.get_coef(d)
+                assert np.linalg.norm(ga - gb) <= 1e-10 * max(np.linalg.norm(ga), 1e-12)
+    assert da
