@@ -93,6 +93,30 @@ int kd_coef_i_many(kd_ctx* ctx, int n, const kd_transform_desc* descs);
 int kd_coef_host(kd_ctx* ctx, const kd_transform_desc* desc);
 int kd_coef_i_host(kd_ctx* ctx, const kd_transform_desc* desc);
 
+/* Same result as kd_coef_host, but the call allocates no device memory.
+ * No counterpart in the reference (its transforms run on the host).
+ *
+ * For callers that may not allocate on the GPU: code that runs while the
+ * process holds a stream in global-mode graph capture (cudaMalloc is then an
+ * invalid call), and applications that reserve their whole GPU memory budget
+ * up front -- e.g. an evolution code importing initial data through its own
+ * memory pool -- where a library allocating on its own would break the budget.
+ * The device staging buffers and basis tables are fixed arrays compiled into
+ * the library (2 x KD_NOALLOC_MAX_DOUBLES doubles and KD_NOALLOC_MAX_TABLE
+ * ints), held by every GPU that loads the library until the process exits.
+ *
+ * Limits: batch * nbr_points product and batch * nbr_coefs product must each
+ * be at most KD_NOALLOC_MAX_DOUBLES (KD_ERR_ARG otherwise); the per-line basis
+ * tables (1 + nc2 + nc1*nc2 entries) at most KD_NOALLOC_MAX_TABLE.
+ * The first call on a device looks up the device addresses of those arrays
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the arrays and leave the last call's data in them; calls
+ * whose GPU work overlaps (several host threads or contexts on one device)
+ * race.  desc->in and desc->out are HOST pointers. */
+#define KD_NOALLOC_MAX_DOUBLES (1 << 20)
+#define KD_NOALLOC_MAX_TABLE (1 << 14)
+int kd_coef_host_noalloc(kd_ctx* ctx, const kd_transform_desc* desc);
+
 /* Base_spectral::ope_1d (src/Ope_1d/ope_1d.cpp:25) with one of the 1-D
  * operators below along dimension `dim` (0=r, 1=theta, 2=phi) of coefficient
  * arrays.  The output basis table of that dimension is written to

@@ -8,6 +8,7 @@
 
 #include "kadath_gb300.h"
 #include "kd_context.hpp"
+#include "kd_noalloc.hpp"
 #include "kd_spectral.hpp"
 
 struct kd_ctx {
@@ -145,6 +146,16 @@ int kd_coef_host(kd_ctx* ctx, const kd_transform_desc* desc) {
 int kd_coef_i_host(kd_ctx* ctx, const kd_transform_desc* desc) {
   if (!ctx || !ctx->c) return KD_ERR_ARG;
   return guarded(ctx, [&] { transform_host(ctx, desc, true); });
+}
+
+int kd_coef_host_noalloc(kd_ctx* ctx, const kd_transform_desc* desc) {
+  if (!ctx || !ctx->c) return KD_ERR_ARG;
+  return guarded(ctx, [&] {
+    if (!desc) throw kd::KdError(KD_ERR_ARG, "null descriptor");
+    check_desc(*desc);
+    kd::Base b = base_from_desc(*desc);
+    kd::coef_host_noalloc(*ctx->c, b, desc->nbr_points, desc->nbr_coefs, desc->batch, desc->in, desc->out);
+  });
 }
 
 int kd_ope_1d(kd_ctx* ctx, int op, int dim, const kd_transform_desc* desc, int* base_out_r, int* base_out_t,
