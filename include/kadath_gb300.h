@@ -242,6 +242,12 @@ int kd_lu_factor(kd_lu* lu, double* dA, long long ld, int n, int mode);
 int kd_lu_solve(kd_lu* lu, double* db, int trans);
 int kd_lu_stats(const kd_lu* lu, double* t_factor_ms, double* t_solve_ms, int* refine_iters,
                 double* rel_residual);
+/* The LU's trailing update on its own: C -= A * B on the tcgen05 tensor
+ * cores in TF32 with FP32 accumulation (replaces the pdgemm/dgemm inside
+ * pdgesv/dgetrf, src_par/do_newton.cpp:317).  Column-major FP32 device
+ * matrices: A is m x k (lda), B is k x n (ldb), C is m x n (ldc); k <= 128. */
+int kd_tf32_gemm_update(kd_ctx* ctx, int m, int n, int k, const float* A, long long lda, const float* B,
+                        long long ldb, float* C, long long ldc);
 
 #ifdef __cplusplus
 }

@@ -1,16 +1,289 @@
-// Trailing-update GEMM for the mixed-precision LU (C -= A * B, FP32 storage).
+// Trailing update of the mixed-precision LU, C -= A * B, on the tcgen05
+// tensor cores in TF32 with FP32 accumulation in tensor memory.
+//
+// The LU works on a column-major FP32 matrix, so the panel L21 (m x k) is
+// contiguous along m.  Both operands are first packed K-major with K padded
+// to a multiple of 32 (one 128-byte swizzle row of TF32): At[i][kk] = A(i, kk)
+// and Bt[j][kk] = B(kk, j).  Each CTA then owns a 128 x 128 tile of C:
+//   1. 128 threads copy the tile's operand rows into shared memory in the
+//      128-byte-swizzled K-major layout (16-byte chunk c of row r stored at
+//      chunk c ^ (r % 8)), then fence them for the async proxy;
+//   2. one thread issues K/8 tcgen05.mma.kind::tf32 (M = 128, N = 128,
+//      K = 8 each) accumulating into 128 TMEM columns, and commits to an
+//      mbarrier;
+//   3. four warps wait on the mbarrier (bounded), read the accumulators with
+//      tcgen05.ld (warp w owns lanes 32w..32w+31 = tile rows) and update C
+//      with coalesced column-major read-modify-writes.
+// K of one panel is at most 128, so the whole K extent of a tile fits in
+// shared memory and needs no pipelining; the update is bound by the HBM
+// traffic of C.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
 #include "kd_gemm_tc.hpp"
 
 namespace kd {
 
+namespace {
+
+constexpr int TC_M = 128;
+constexpr int TC_N = 128;
+constexpr int TC_KBLK = 32;        // TF32 elements per 128-byte row
+constexpr int TC_MAXK = 128;       // largest panel width supported
+constexpr int TC_THREADS = 128;
+constexpr unsigned TC_TMEM_COLS = 128;
+constexpr size_t TC_MIN_SMEM = 56 * 1024;
+constexpr long long TC_WAIT_LIMIT = 1LL << 26;  // try_wait polls before giving up
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart (stride byte offset), descriptor version 1.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= static_cast<uint64_t>((saddr & 0x3FFFF) >> 4);   // start address
+  d |= static_cast<uint64_t>(1) << 16;                   // leading byte offset (unused with swizzle)
+  d |= static_cast<uint64_t>(1024 >> 4) << 32;           // stride byte offset
+  d |= static_cast<uint64_t>(1) << 46;                   // version
+  d |= static_cast<uint64_t>(2) << 61;                   // SWIZZLE_128B
+  return d;
+}
+
+// Instruction descriptor: D = F32, A = B = TF32, both K-major, M x N.
+__host__ __device__ constexpr uint32_t tf32_idesc(int M, int N) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | (static_cast<uint32_t>(N >> 3) << 17) |
+         (static_cast<uint32_t>(M >> 4) << 24);
+}
+
+// Packs a column-major panel into a K-major, zero-padded buffer:
+//   out[r * kpad + kk] = src(r, kk) for r < rows, kk < k; 0 elsewhere.
+// src(r, kk) = col_major ? src[kk * ld + r] : src[r * ld + kk].
+__global__ void pack_kmajor(const float* __restrict__ src, long long ld, int rows, int k, int col_major,
+                            float* __restrict__ out, int rows_pad, int kpad) {
+  long long total = static_cast<long long>(rows_pad) * kpad;
+  for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < total;
+       t += static_cast<long long>(gridDim.x) * blockDim.x) {
+    int r, kk;
+    if (col_major) {  // read coalesced along r
+      r = static_cast<int>(t % rows_pad);
+      kk = static_cast<int>(t / rows_pad);
+    } else {          // read coalesced along kk
+      kk = static_cast<int>(t % kpad);
+      r = static_cast<int>(t / kpad);
+    }
+    float v = 0.0f;
+    if (r < rows && kk < k) v = col_major ? src[static_cast<long long>(kk) * ld + r] : src[static_cast<long long>(r) * ld + kk];
+    out[static_cast<long long>(r) * kpad + kk] = v;
+  }
+}
+
+// Copies rows [row0, row0+128) of a K-major buffer (kpad columns) into
+// shared memory, one 128 x 32 swizzled block per 32 K-columns.
+__device__ __forceinline__ void load_tile_sw128(const float* __restrict__ src, int row0, int kpad, char* smem) {
+  const int nkb = kpad / TC_KBLK;
+  const int chunks = 128 * 8 * nkb;  // 16-byte chunks
+  for (int c = threadIdx.x; c < chunks; c += blockDim.x) {
+    int kb = c / (128 * 8);
+    int rem = c % (128 * 8);
+    int r = rem / 8;
+    int ch = rem % 8;
+    const float4* g = reinterpret_cast<const float4*>(src + static_cast<long long>(row0 + r) * kpad + kb * TC_KBLK) + ch;
+    float4 v = __ldg(g);
+    char* dst = smem + kb * (128 * 128) + r * 128 + ((ch ^ (r & 7)) << 4);
+    *reinterpret_cast<float4*>(dst) = v;
+  }
+}
+
+__global__ void __launch_bounds__(TC_THREADS) tf32_update_kernel(const float* __restrict__ At,
+                                                                 const float* __restrict__ Bt, int kpad,
+                                                                 float* __restrict__ C, long long ldc, int m, int n,
+                                                                 int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  // 1024-byte aligned operand area: A blocks then B blocks (16 KiB each)
+  char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const int nkb = kpad / TC_KBLK;
+  char* sA = base;
+  char* sB = base + nkb * (128 * 128);
+  __shared__ uint64_t mbar;
+  __shared__ uint32_t tmem_base_sh;
+  __shared__ int timed_out;
+
+  const int tile_m = blockIdx.x * TC_M;
+  const int tile_n = blockIdx.y * TC_N;
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    timed_out = 0;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar)), "r"(1));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_sh)),
+                 "r"(TC_TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  load_tile_sw128(At, tile_m, kpad, sA);
+  load_tile_sw128(Bt, tile_n, kpad, sB);
+  // make the generic-proxy shared-memory writes visible to the tensor cores
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base_sh;
+
+  if (threadIdx.x == 0) {
+    const uint32_t idesc = tf32_idesc(TC_M, TC_N);
+    const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+    for (int kb = 0; kb < nkb; kb++) {
+      for (int k = 0; k < TC_KBLK / 8; k++) {
+        uint64_t ad = sw128_desc(a0 + kb * (128 * 128)) + static_cast<uint64_t>((k * 32) >> 4);
+        uint64_t bd = sw128_desc(b0 + kb * (128 * 128)) + static_cast<uint64_t>((k * 32) >> 4);
+        uint32_t acc = (kb | k) ? 1u : 0u;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+      }
+    }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(&mbar))
+                 : "memory");
+  }
+  // bounded wait for the MMAs to land in TMEM
+  {
+    uint32_t done = 0;
+    long long it = 0;
+    while (!done) {
+      asm volatile(
+          "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+          : "=r"(done)
+          : "r"(smem_u32(&mbar)), "r"(0));
+      if (!done && ++it > TC_WAIT_LIMIT) {
+        timed_out = 1;
+        break;
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (!timed_out) {
+    const int row = tile_m + warp * 32 + lane;
+    for (int c0 = 0; c0 < TC_N; c0 += 16) {
+      uint32_t r[16];
+      const uint32_t taddr = tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(c0);
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (row < m) {
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+          int col = tile_n + c0 + q;
+          if (col < n) {
+            float* p = C + static_cast<long long>(col) * ldc + row;
+            *p -= __uint_as_float(r[q]);
+          }
+        }
+      }
+    }
+  } else if (threadIdx.x == 0) {
+    atomicExch(err, 1);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS));
+}
+
+struct TcWork {
+  float* at = nullptr;
+  float* bt = nullptr;
+  size_t cap_a = 0, cap_b = 0;
+  int* err = nullptr;
+};
+TcWork g_tc;
+
+int grid_for(long long n) {
+  long long g = (n + 255) / 256;
+  if (g > 152 * 8) g = 152 * 8;
+  return static_cast<int>(g < 1 ? 1 : g);
+}
+
+}  // namespace
+
+bool tf32_gemm_supported(int k) { return k > 0 && k <= TC_MAXK; }
+
+void tf32_gemm_update(Context* ctx, int m, int n, int k, const float* A, long long lda, const float* B, long long ldb,
+                      float* C, long long ldc) {
+  if (m <= 0 || n <= 0 || k <= 0) return;
+  if (k > TC_MAXK) throw KdError(KD_ERR_ARG, "tcgen05 trailing update: panel width above 128");
+  cudaStream_t s = ctx->stream();
+  const int kpad = ((k + TC_KBLK - 1) / TC_KBLK) * TC_KBLK;
+  const int mpad = ((m + TC_M - 1) / TC_M) * TC_M;
+  const int npad = ((n + TC_N - 1) / TC_N) * TC_N;
+  size_t need_a = static_cast<size_t>(mpad) * kpad, need_b = static_cast<size_t>(npad) * kpad;
+  if (need_a > g_tc.cap_a) {
+    cudaFree(g_tc.at);
+    cuda_check(cudaMalloc(&g_tc.at, need_a * sizeof(float)), "cudaMalloc(At)");
+    g_tc.cap_a = need_a;
+  }
+  if (need_b > g_tc.cap_b) {
+    cudaFree(g_tc.bt);
+    cuda_check(cudaMalloc(&g_tc.bt, need_b * sizeof(float)), "cudaMalloc(Bt)");
+    g_tc.cap_b = need_b;
+  }
+  if (!g_tc.err) {
+    cuda_check(cudaMalloc(&g_tc.err, sizeof(int)), "cudaMalloc(err)");
+    cuda_check(cudaMemsetAsync(g_tc.err, 0, sizeof(int), s), "memset err");
+  }
+  // A is column-major m x k (contiguous along m); B is column-major k x n
+  // (contiguous along k).
+  pack_kmajor<<<grid_for(need_a), 256, 0, s>>>(A, lda, m, k, 1, g_tc.at, mpad, kpad);
+  pack_kmajor<<<grid_for(need_b), 256, 0, s>>>(B, ldb, n, k, 0, g_tc.bt, npad, kpad);
+  const int nkb = kpad / TC_KBLK;
+  // Each CTA holds 128 TMEM columns of the SM's 512: asking for at least
+  // 56 KiB of shared memory keeps at most four CTAs on one SM, so an
+  // allocation never has to wait for another CTA to finish.
+  size_t smem = 1024 + static_cast<size_t>(2 * nkb) * 128 * 128;
+  if (smem < TC_MIN_SMEM) smem = TC_MIN_SMEM;
+  static bool attr = false;
+  if (!attr) {
+    cuda_check(cudaFuncSetAttribute(tf32_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    1024 + 2 * (TC_MAXK / TC_KBLK) * 128 * 128),
+               "cudaFuncSetAttribute(tf32)");
+    attr = true;
+  }
+  dim3 grid(mpad / TC_M, npad / TC_N);
+  tf32_update_kernel<<<grid, TC_THREADS, smem, s>>>(g_tc.at, g_tc.bt, kpad, C, ldc, m, n, g_tc.err);
+  ctx->launches += 3;
+  cuda_check(cudaGetLastError(), "tcgen05 trailing update");
+}
+
+int tf32_gemm_error_flag(Context* ctx) {
+  if (!g_tc.err) return 0;
+  int h = 0;
+  cuda_check(cudaMemcpyAsync(&h, g_tc.err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream()), "D2H err");
+  cuda_check(cudaStreamSynchronize(ctx->stream()), "sync");
+  if (h) cuda_check(cudaMemsetAsync(g_tc.err, 0, sizeof(int), ctx->stream()), "reset err");
+  return h;
+}
+
 void gemm_update_f32(Context* ctx, cublasHandle_t blas, int m, int n, int k, const float* A, long long lda,
                      const float* B, long long ldb, float* C, long long ldc, bool tf32) {
-  const float one = 1.0f, mone = -1.0f;
   ProfScope ps(ctx, Context::PROF_LU_GEMM, 2.0 * m * n * k);
-  cublasComputeType_t ct = tf32 ? CUBLAS_COMPUTE_32F_FAST_TF32 : CUBLAS_COMPUTE_32F;
+  if (tf32 && tf32_gemm_supported(k)) {
+    tf32_gemm_update(ctx, m, n, k, A, lda, B, ldb, C, ldc);
+    return;
+  }
+  // plain FP32 product (the FP32-IR mode): library SGEMM
+  const float one = 1.0f, mone = -1.0f;
   cublasStatus_t st = cublasGemmEx(blas, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &mone, A, CUDA_R_32F, static_cast<int>(lda),
-                                   B, CUDA_R_32F, static_cast<int>(ldb), &one, C, CUDA_R_32F, static_cast<int>(ldc), ct,
-                                   CUBLAS_GEMM_DEFAULT);
+                                   B, CUDA_R_32F, static_cast<int>(ldb), &one, C, CUDA_R_32F, static_cast<int>(ldc),
+                                   CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
   if (st != CUBLAS_STATUS_SUCCESS) throw KdError(KD_ERR_CUDA, "cublasGemmEx (trailing update) failed");
   ctx->launches++;
 }

@@ -1,6 +1,6 @@
 // Trailing-update GEMM of the mixed-precision LU: C -= A * B with FP32
-// storage, column-major.  `tf32` selects TF32 tensor-core products with FP32
-// accumulation; otherwise plain FP32.
+// storage, column-major.  `tf32` selects the tcgen05 TF32 tensor-core kernel
+// (FP32 accumulation in tensor memory); otherwise a plain FP32 product.
 #pragma once
 #include <cublas_v2.h>
 
@@ -10,5 +10,13 @@ namespace kd {
 
 void gemm_update_f32(Context* ctx, cublasHandle_t blas, int m, int n, int k, const float* A, long long lda,
                      const float* B, long long ldb, float* C, long long ldc, bool tf32);
+
+// The tcgen05 kernel on its own (k <= 128).
+bool tf32_gemm_supported(int k);
+void tf32_gemm_update(Context* ctx, int m, int n, int k, const float* A, long long lda, const float* B, long long ldb,
+                      float* C, long long ldc);
+// Returns (and clears) the flag a CTA sets when its wait for the tensor-core
+// results ran out of polls.
+int tf32_gemm_error_flag(Context* ctx);
 
 }  // namespace kd

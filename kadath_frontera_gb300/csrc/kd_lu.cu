@@ -4,6 +4,7 @@
 // U row block with the unit-lower L11 staged in shared memory; trailing
 // update as a GEMM (FP64 library GEMM, or the TF32 tensor-core kernel of
 // kd_gemm_tc.cu for the mixed mode).
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -163,84 +164,106 @@ __global__ void d2s(const double* __restrict__ A, long long lda, float* __restri
 // ---- triangular solves on one right-hand side (blocked by TB rows) --------
 constexpr int TB = 64;
 
-__global__ void apply_pivots_vec(double* b, const int* ipiv, int N, int reverse) {
+// perm such that (P b)[i] = b[perm[i]] for the sequential row swaps ipiv.
+__global__ void build_perm(const int* __restrict__ ipiv, int N, int* __restrict__ perm) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  if (!reverse) {
-    for (int j = 0; j < N; j++) {
-      int p = ipiv[j];
-      if (p != j) {
-        double t = b[j];
-        b[j] = b[p];
-        b[p] = t;
-      }
-    }
-  } else {
-    for (int j = N - 1; j >= 0; j--) {
-      int p = ipiv[j];
-      if (p != j) {
-        double t = b[j];
-        b[j] = b[p];
-        b[p] = t;
-      }
-    }
+  for (int i = 0; i < N; i++) perm[i] = i;
+  for (int j = 0; j < N; j++) {
+    int p = ipiv[j];
+    int t = perm[j];
+    perm[j] = perm[p];
+    perm[p] = t;
   }
 }
 
-// Solves the diagonal block [r0, r1) of M x = b with M = A or A^T (trans):
-// forward or backward substitution, unit or stored diagonal.
+__global__ void gather_perm(const double* __restrict__ b, const int* __restrict__ perm, int N, double* __restrict__ out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) out[i] = b[perm[i]];
+}
+
+__global__ void scatter_perm(const double* __restrict__ z, const int* __restrict__ perm, int N, double* __restrict__ out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) out[perm[i]] = z[i];
+}
+
+// One CTA per TB x TB diagonal block: inverse of its unit-lower part (L) and
+// of its upper part (U), row-major, zero padded to TB x TB.  Thread c builds
+// column c of each inverse by substitution in FP64.
 template <class T>
-__global__ void trsv_block(const T* __restrict__ A, long long ld, double* b, int r0, int r1, int unit, int forward,
-                           int trans) {
-  __shared__ double x[TB];
-  int n = r1 - r0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = b[r0 + i];
+__global__ void invert_diag_blocks(const T* __restrict__ A, long long ld, int N, double* __restrict__ Linv,
+                                   double* __restrict__ Uinv) {
+  extern __shared__ double sm[];
+  double* D = sm;                 // D[i*TB + k]
+  double* XL = sm + TB * TB;      // XL[i*TB + c]
+  double* XU = sm + 2 * TB * TB;  // XU[i*TB + c]
+  const int blk = blockIdx.x;
+  const int r0 = blk * TB;
+  const int n = (N - r0 < TB) ? N - r0 : TB;
+  for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
+    int i = e / TB, k = e % TB;
+    D[e] = (i < n && k < n) ? static_cast<double>(A[static_cast<long long>(r0 + k) * ld + r0 + i]) : 0.0;
+    XL[e] = 0.0;
+    XU[e] = 0.0;
+  }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    auto M = [&](int i, int k) -> double {
-      return trans ? static_cast<double>(A[static_cast<long long>(r0 + i) * ld + r0 + k])
-                   : static_cast<double>(A[static_cast<long long>(r0 + k) * ld + r0 + i]);
-    };
-    if (forward) {
-      for (int i = 0; i < n; i++) {
-        double s = x[i];
-        for (int k = 0; k < i; k++) s -= M(i, k) * x[k];
-        x[i] = unit ? s : s / M(i, i);
-      }
-    } else {
-      for (int i = n - 1; i >= 0; i--) {
-        double s = x[i];
-        for (int k = i + 1; k < n; k++) s -= M(i, k) * x[k];
-        x[i] = unit ? s : s / M(i, i);
-      }
+  const int c = threadIdx.x;
+  if (c < n) {
+    XL[c * TB + c] = 1.0;
+    for (int i = c + 1; i < n; i++) {
+      double s = 0.0;
+      for (int k = c; k < i; k++) s += D[i * TB + k] * XL[k * TB + c];
+      XL[i * TB + c] = -s;
+    }
+    XU[c * TB + c] = 1.0 / D[c * TB + c];
+    for (int i = c - 1; i >= 0; i--) {
+      double s = 0.0;
+      for (int k = i + 1; k <= c; k++) s += D[i * TB + k] * XU[k * TB + c];
+      XU[i * TB + c] = -s / D[i * TB + i];
     }
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < n; i += blockDim.x) b[r0 + i] = x[i];
+  double* lo = Linv + static_cast<size_t>(blk) * TB * TB;
+  double* uo = Uinv + static_cast<size_t>(blk) * TB * TB;
+  for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
+    lo[e] = XL[e];
+    uo[e] = XU[e];
+  }
 }
 
-// b[rows] -= M[rows, r0:r1] * b[r0:r1]  (M = A or A^T), rows = [q0, q1)
+// One block step of a triangular solve with M = A (trans = 0) or A^T:
+//   x = Dinv * b[r0 : r0+n]  (Dinv^T when dinv_t),  y[r0 : r0+n] = x,
+//   b[row] -= sum_k M(row, r0+k) x_k  for row in [q0, q1).
+// Rows of the block itself are only read, so every CTA sees the same x.
 template <class T>
-__global__ void gemv_update(const T* __restrict__ A, long long ld, double* b, int r0, int r1, int q0, int q1,
-                            int trans) {
-  __shared__ double x[TB];
-  int n = r1 - r0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = b[r0 + i];
+__global__ void trsv_step(const T* __restrict__ A, long long ld, double* __restrict__ b, double* __restrict__ y, int r0,
+                          int n, const double* __restrict__ Dinv, int dinv_t, int q0, int q1, int trans) {
+  __shared__ double bb[TB];
+  __shared__ double xx[TB];
+  for (int i = threadIdx.x; i < TB; i += blockDim.x) bb[i] = (i < n) ? b[r0 + i] : 0.0;
   __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double s = 0.0;
+    for (int k = 0; k < n; k++) s += (dinv_t ? Dinv[k * TB + i] : Dinv[i * TB + k]) * bb[k];
+    xx[i] = s;
+  }
+  __syncthreads();
+  if (blockIdx.x == 0)
+    for (int i = threadIdx.x; i < n; i += blockDim.x) y[r0 + i] = xx[i];
+  if (q1 <= q0) return;
   if (!trans) {
     int row = q0 + blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= q1) return;
     double s = 0.0;
-    for (int k = 0; k < n; k++) s += static_cast<double>(A[static_cast<long long>(r0 + k) * ld + row]) * x[k];
+    for (int k = 0; k < n; k++) s += static_cast<double>(A[static_cast<long long>(r0 + k) * ld + row]) * xx[k];
     b[row] -= s;
   } else {
-    // one warp per output row: M^T[row, k] = A[k, row] is contiguous in k
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     int row = q0 + warp;
     if (row >= q1) return;
-    double s = 0.0;
     const T* colp = A + static_cast<long long>(row) * ld + r0;
-    for (int k = lane; k < n; k += 32) s += static_cast<double>(colp[k]) * x[k];
+    double s = 0.0;
+    for (int k = lane; k < n; k += 32) s += static_cast<double>(colp[k]) * xx[k];
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     if (lane == 0) b[row] -= s;
   }
@@ -279,6 +302,10 @@ DenseLU::~DenseLU() {
   cudaFree(d_info_);
   cudaFree(work_);
   cudaFree(work32_);
+  cudaFree(dinv_l_);
+  cudaFree(dinv_u_);
+  cudaFree(perm_);
+  cudaFree(tri_work_);
 }
 
 void DenseLU::ensure_work(size_t n) {
@@ -289,18 +316,152 @@ void DenseLU::ensure_work(size_t n) {
   }
 }
 
+// Panel of jb columns factored by one thread-block cluster: CTA r owns a
+// contiguous slice of the rows [j0, N).  Per column: local arg-max, cluster
+// barrier, every CTA reads the CL candidates from distributed shared memory
+// and agrees on the pivot, CTA 0 swaps the two rows of the panel, cluster
+// barrier, then each CTA scales and rank-1-updates its own rows.  Panel data
+// stays in global memory (it fits in L2).
+constexpr int PANEL_CL = 8;
+constexpr int PANEL_THREADS = 1024;
+
+template <class T>
+__global__ void panel_cluster_kernel(T* __restrict__ A, long long ld, int N, int j0, int jb, int* __restrict__ ipiv,
+                                     int* __restrict__ info) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  __shared__ double cand_v[1];
+  __shared__ int cand_i[1];
+  __shared__ double red_v[32];
+  __shared__ int red_i[32];
+  __shared__ double prow[128];  // pivot row segment (jb <= 128)
+  __shared__ int s_piv;
+  const int rank = static_cast<int>(cluster.block_rank());
+  const int nrows = N - j0;
+  const int per = (nrows + PANEL_CL - 1) / PANEL_CL;
+  const int my0 = j0 + rank * per;
+  const int my1 = (my0 + per < N) ? my0 + per : N;
+  const int c1 = j0 + jb;
+  for (int j = j0; j < c1; j++) {
+    // 1. local arg-max of |A[i, j]| over my rows i >= j
+    const T* col = A + static_cast<long long>(j) * ld;
+    double best = -1.0;
+    int bi = N;  // "no row" sentinel, larger than any row index
+    int start = my0 > j ? my0 : j;
+    for (int i = start + threadIdx.x; i < my1; i += blockDim.x) {
+      double v = fabs(static_cast<double>(col[i]));
+      if (v > best || (v == best && i < bi)) {
+        best = v;
+        bi = i;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      double ov = __shfl_xor_sync(0xffffffffu, best, o);
+      int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > best || (ov == best && oi < bi)) {
+        best = ov;
+        bi = oi;
+      }
+    }
+    if ((threadIdx.x & 31) == 0) {
+      red_v[threadIdx.x >> 5] = best;
+      red_i[threadIdx.x >> 5] = bi;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      int nw = blockDim.x >> 5;
+      best = (threadIdx.x < nw) ? red_v[threadIdx.x] : -1.0;
+      bi = (threadIdx.x < nw) ? red_i[threadIdx.x] : N;
+      for (int o = 16; o > 0; o >>= 1) {
+        double ov = __shfl_xor_sync(0xffffffffu, best, o);
+        int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ov > best || (ov == best && oi < bi)) {
+          best = ov;
+          bi = oi;
+        }
+      }
+      if (threadIdx.x == 0) {
+        cand_v[0] = best;
+        cand_i[0] = bi;
+      }
+    }
+    __threadfence();
+    cluster.sync();
+    // 2. every CTA combines the CL candidates (same order, same result)
+    if (threadIdx.x == 0) {
+      double gb = -1.0;
+      int gi = N;
+      for (int r = 0; r < PANEL_CL; r++) {
+        double v = *cluster.map_shared_rank(&cand_v[0], r);
+        int ii = *cluster.map_shared_rank(&cand_i[0], r);
+        if (v > gb || (v == gb && ii < gi)) {
+          gb = v;
+          gi = ii;
+        }
+      }
+      if (gi >= N) gi = j;  // empty column below the diagonal
+      s_piv = gi;
+      if (rank == 0) {
+        ipiv[j] = gi;
+        if (!(gb > 0.0) && *info == 0) *info = j + 1;  // zero or NaN pivot
+      }
+    }
+    __syncthreads();
+    const int p = s_piv;
+    // 3. CTA 0 swaps rows j and p inside the panel
+    if (rank == 0 && p != j)
+      for (int c = j0 + threadIdx.x; c < c1; c += blockDim.x) {
+        T* cc = A + static_cast<long long>(c) * ld;
+        T t = cc[j];
+        cc[j] = cc[p];
+        cc[p] = t;
+      }
+    __threadfence();
+    cluster.sync();
+    // 4. scale and rank-1 update of my rows below j
+    for (int k = threadIdx.x; k < c1 - j; k += blockDim.x)
+      prow[k] = static_cast<double>(A[static_cast<long long>(j + k) * ld + j]);
+    __syncthreads();
+    const double piv = prow[0];
+    if (piv != 0.0) {
+      // the update runs in the storage precision (FP32 for the mixed modes)
+      const T inv = static_cast<T>(1.0 / piv);
+      int rs = my0 > j + 1 ? my0 : j + 1;
+      for (int i = rs + threadIdx.x; i < my1; i += blockDim.x) {
+        T* ci = A + static_cast<long long>(j) * ld + i;
+        T l = *ci * inv;
+        *ci = l;
+        for (int k = 1; k < c1 - j; k++) {
+          T* ck = A + static_cast<long long>(j + k) * ld + i;
+          *ck = fma(-l, static_cast<T>(prow[k]), *ck);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
 template <class T>
 static void panel_factor(Context* ctx, T* A, long long ld, int N, int j0, int jb, int* ipiv, int* info) {
   cudaStream_t s = ctx->stream();
   double fl = 0;
   for (int j = j0; j < j0 + jb; j++) fl += 2.0 * (N - j - 1) * (j0 + jb - j - 1) + (N - j);
   ProfScope ps(ctx, Context::PROF_LU_PANEL, fl);
-  for (int j = j0; j < j0 + jb; j++) {
-    pivot_swap_scale<T><<<1, PIV_THREADS, 0, s>>>(A, ld, N, j, j0, j0 + jb, ipiv, info);
-    if (j + 1 < j0 + jb && j + 1 < N) panel_rank1<T><<<blocks(N - j - 1, 256), 256, 0, s>>>(A, ld, N, j, j0 + jb);
-    ctx->launches += 2;
-  }
-  cuda_check(cudaGetLastError(), "panel kernels");
+  if (jb > 128) throw KdError(KD_ERR_ARG, "panel width above 128");
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(PANEL_CL, 1, 1);
+  cfg.blockDim = dim3(PANEL_THREADS, 1, 1);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = PANEL_CL;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cuda_check(cudaLaunchKernelEx(&cfg, panel_cluster_kernel<T>, A, ld, N, j0, jb, ipiv, info), "panel cluster kernel");
+  ctx->launches += 1;
 }
 
 template <class T>
@@ -381,6 +542,7 @@ void DenseLU::factor(double* A, long long ld, int N, int mode) {
   stats.flops = static_cast<long long>(2.0 / 3.0 * double(N) * N * N);
   if (mode == LU_FP64) {
     factor_fp64(A, ld, N);
+    prepare_solves<double>(A, ld, N);
   } else {
     size_t need = static_cast<size_t>(N) * N;
     if (need > a32_cap_) {
@@ -391,64 +553,100 @@ void DenseLU::factor(double* A, long long ld, int N, int mode) {
     d2s<<<152 * 8, 256, 0, ctx_->stream()>>>(A, ld, A32_, N, N);
     ctx_->launches++;
     factor_f32(A32_, N, N, mode == LU_TF32_IR);
+    prepare_solves<float>(A32_, N, N);
   }
   int info = 0;
   cuda_check(cudaMemcpyAsync(&info, d_info_, sizeof(int), cudaMemcpyDeviceToHost, ctx_->stream()), "D2H info");
   cuda_check(cudaStreamSynchronize(ctx_->stream()), "sync after LU");
   stats.t_factor_ms = now_ms() - t0;
+  if (mode == LU_TF32_IR && tf32_gemm_error_flag(ctx_))
+    throw KdError(KD_ERR_TIMEOUT, "tensor-core trailing update timed out waiting for its MMAs");
   if (info != 0) throw KdError(KD_ERR_SINGULAR, "Jacobian is singular (zero pivot at column " + std::to_string(info) + ")");
 }
 
-void DenseLU::solve_fp64(const double* LU, long long ld, int N, double* b, int trans) {
+// Triangular solves by 64-row blocks with precomputed inverses of the
+// diagonal blocks: one launch per block computes the block's unknowns as a
+// small GEMV and subtracts their contribution from the remaining rows.
+template <class T>
+void DenseLU::tri_solve(const T* LU, long long ld, int N, double* b, int trans) {
   cudaStream_t s = ctx_->stream();
   ProfScope ps(ctx_, Context::PROF_LU_SOLVE, 2.0 * N * N);
+  const int nblk = (N + TB - 1) / TB;
+  double* w1 = tri_work_;
+  double* w2 = tri_work_ + N;
+  const size_t bs = static_cast<size_t>(TB) * TB;
   if (!trans) {
-    apply_pivots_vec<<<1, 1, 0, s>>>(b, ipiv_, N, 0);
-    for (int r0 = 0; r0 < N; r0 += TB) {
-      int r1 = r0 + TB < N ? r0 + TB : N;
-      trsv_block<double><<<1, 64, 0, s>>>(LU, ld, b, r0, r1, 1, 1, 0);
-      if (r1 < N) gemv_update<double><<<blocks(N - r1, 256), 256, 0, s>>>(LU, ld, b, r0, r1, r1, N, 0);
+    gather_perm<<<blocks(N, 256), 256, 0, s>>>(b, perm_, N, w1);
+    for (int k = 0; k < nblk; k++) {
+      int r0 = k * TB, n = (N - r0 < TB) ? N - r0 : TB;
+      int q0 = r0 + n, q1 = N;
+      int g = q1 > q0 ? blocks(q1 - q0, 256) : 1;
+      trsv_step<T><<<g, 256, 0, s>>>(LU, ld, w1, w2, r0, n, dinv_l_ + k * bs, 0, q0, q1, 0);
     }
-    for (int r1 = N; r1 > 0; r1 -= TB) {
-      int r0 = r1 - TB > 0 ? r1 - TB : 0;
-      trsv_block<double><<<1, 64, 0, s>>>(LU, ld, b, r0, r1, 0, 0, 0);
-      if (r0 > 0) gemv_update<double><<<blocks(r0, 256), 256, 0, s>>>(LU, ld, b, r0, r1, 0, r0, 0);
+    for (int k = nblk - 1; k >= 0; k--) {
+      int r0 = k * TB, n = (N - r0 < TB) ? N - r0 : TB;
+      int q0 = 0, q1 = r0;
+      int g = q1 > q0 ? blocks(q1 - q0, 256) : 1;
+      trsv_step<T><<<g, 256, 0, s>>>(LU, ld, w2, b, r0, n, dinv_u_ + k * bs, 0, q0, q1, 0);
     }
   } else {
-    // A^T = U^T L^T P: solve U^T y = b (forward), L^T z = y (backward), x = P^T z
-    for (int r0 = 0; r0 < N; r0 += TB) {
-      int r1 = r0 + TB < N ? r0 + TB : N;
-      trsv_block<double><<<1, 64, 0, s>>>(LU, ld, b, r0, r1, 0, 1, 1);
-      if (r1 < N) gemv_update<double><<<blocks(static_cast<long long>(N - r1) * 32, 256), 256, 0, s>>>(LU, ld, b, r0, r1, r1, N, 1);
+    // A^T = U^T L^T P: U^T y = b (forward, lower), L^T z = y (backward), x = P^T z
+    for (int k = 0; k < nblk; k++) {
+      int r0 = k * TB, n = (N - r0 < TB) ? N - r0 : TB;
+      int q0 = r0 + n, q1 = N;
+      int g = q1 > q0 ? blocks(static_cast<long long>(q1 - q0) * 32, 256) : 1;
+      trsv_step<T><<<g, 256, 0, s>>>(LU, ld, b, w2, r0, n, dinv_u_ + k * bs, 1, q0, q1, 1);
     }
-    for (int r1 = N; r1 > 0; r1 -= TB) {
-      int r0 = r1 - TB > 0 ? r1 - TB : 0;
-      trsv_block<double><<<1, 64, 0, s>>>(LU, ld, b, r0, r1, 1, 0, 1);
-      if (r0 > 0) gemv_update<double><<<blocks(static_cast<long long>(r0) * 32, 256), 256, 0, s>>>(LU, ld, b, r0, r1, 0, r0, 1);
+    for (int k = nblk - 1; k >= 0; k--) {
+      int r0 = k * TB, n = (N - r0 < TB) ? N - r0 : TB;
+      int q0 = 0, q1 = r0;
+      int g = q1 > q0 ? blocks(static_cast<long long>(q1 - q0) * 32, 256) : 1;
+      trsv_step<T><<<g, 256, 0, s>>>(LU, ld, w2, w1, r0, n, dinv_l_ + k * bs, 1, q0, q1, 1);
     }
-    apply_pivots_vec<<<1, 1, 0, s>>>(b, ipiv_, N, 1);
+    scatter_perm<<<blocks(N, 256), 256, 0, s>>>(w1, perm_, N, b);
   }
-  ctx_->launches += 4 * ((N + TB - 1) / TB) + 1;
+  ctx_->launches += 2 * nblk + 1;
   cuda_check(cudaGetLastError(), "triangular solve");
 }
 
-void DenseLU::solve_f32(double* b) {
+void DenseLU::solve_fp64(const double* LU, long long ld, int N, double* b, int trans) {
+  tri_solve<double>(LU, ld, N, b, trans);
+}
+
+void DenseLU::solve_f32(double* b) { tri_solve<float>(A32_, N_, N_, b, 0); }
+
+// After factorisation: pivots as one permutation, inverses of the 64 x 64
+// diagonal blocks of L (unit lower) and U.
+template <class T>
+void DenseLU::prepare_solves(const T* LU, long long ld, int N) {
   cudaStream_t s = ctx_->stream();
-  ProfScope ps(ctx_, Context::PROF_LU_SOLVE, 2.0 * N_ * N_);
-  int N = N_;
-  apply_pivots_vec<<<1, 1, 0, s>>>(b, ipiv_, N, 0);
-  for (int r0 = 0; r0 < N; r0 += TB) {
-    int r1 = r0 + TB < N ? r0 + TB : N;
-    trsv_block<float><<<1, 64, 0, s>>>(A32_, N, b, r0, r1, 1, 1, 0);
-    if (r1 < N) gemv_update<float><<<blocks(N - r1, 256), 256, 0, s>>>(A32_, N, b, r0, r1, r1, N, 0);
+  const int nblk = (N + TB - 1) / TB;
+  size_t need = static_cast<size_t>(nblk) * TB * TB;
+  if (need > dinv_cap_) {
+    cudaFree(dinv_l_);
+    cudaFree(dinv_u_);
+    cuda_check(cudaMalloc(&dinv_l_, need * sizeof(double)), "cudaMalloc(Linv)");
+    cuda_check(cudaMalloc(&dinv_u_, need * sizeof(double)), "cudaMalloc(Uinv)");
+    dinv_cap_ = need;
   }
-  for (int r1 = N; r1 > 0; r1 -= TB) {
-    int r0 = r1 - TB > 0 ? r1 - TB : 0;
-    trsv_block<float><<<1, 64, 0, s>>>(A32_, N, b, r0, r1, 0, 0, 0);
-    if (r0 > 0) gemv_update<float><<<blocks(r0, 256), 256, 0, s>>>(A32_, N, b, r0, r1, 0, r0, 0);
+  if (static_cast<size_t>(N) > perm_cap_) {
+    cudaFree(perm_);
+    cudaFree(tri_work_);
+    cuda_check(cudaMalloc(&perm_, sizeof(int) * N), "cudaMalloc(perm)");
+    cuda_check(cudaMalloc(&tri_work_, sizeof(double) * 2 * N), "cudaMalloc(tri work)");
+    perm_cap_ = N;
   }
-  ctx_->launches += 4 * ((N + TB - 1) / TB) + 1;
-  cuda_check(cudaGetLastError(), "fp32 triangular solve");
+  build_perm<<<1, 1, 0, s>>>(ipiv_, N, perm_);
+  size_t smem = sizeof(double) * 3 * TB * TB;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(invert_diag_blocks<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    cudaFuncSetAttribute(invert_diag_blocks<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    attr_set = true;
+  }
+  invert_diag_blocks<T><<<nblk, TB, smem, s>>>(LU, ld, N, dinv_l_, dinv_u_);
+  ctx_->launches += 2;
+  cuda_check(cudaGetLastError(), "solve preparation");
 }
 
 // Right-preconditioned GMRES(m) in FP64 with the FP32 LU as preconditioner:

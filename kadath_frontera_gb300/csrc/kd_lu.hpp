@@ -65,6 +65,16 @@ class DenseLU {
   void factor_f32(float* A, long long ld, int N, bool tf32);
   void solve_fp64(const double* LU, long long ld, int N, double* b, int trans);
   void solve_f32(double* b);  // applies the FP32 factors to an FP64 vector
+  template <class T>
+  void tri_solve(const T* LU, long long ld, int N, double* b, int trans);
+  template <class T>
+  void prepare_solves(const T* LU, long long ld, int N);
+  double* dinv_l_ = nullptr;  // inverses of the 64 x 64 diagonal blocks
+  double* dinv_u_ = nullptr;
+  size_t dinv_cap_ = 0;
+  int* perm_ = nullptr;       // pivots as one permutation
+  double* tri_work_ = nullptr;
+  size_t perm_cap_ = 0;
   void gmres_ir(double* b);
 };
 

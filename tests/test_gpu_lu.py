@@ -65,3 +65,35 @@ def test_singular_matrix_reports_status(ctx):
     with pytest.raises(KadathError) as e:
         lu.factor(dA.data_ptr(), n, n, 0)
     assert e.value.status == 3  # KD_ERR_SINGULAR
+
+
+@pytest.mark.parametrize("m,n,k", [(128, 128, 32), (256, 384, 96), (200, 130, 96), (1000, 777, 64), (33, 257, 17)])
+def test_tcgen05_tf32_update_matches_fp64_product(ctx, m, n, k):
+    """C -= A B on the tcgen05 tensor cores (TF32 inputs, FP32 accumulation)
+    against the FP64 product; tolerance from the TF32 unit roundoff 2^-11."""
+    import ctypes as C
+    lib = ctx.lib
+    lib.kd_tf32_gemm_update.restype = C.c_int
+    lib.kd_tf32_gemm_update.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_longlong, C.c_void_p,
+                                        C.c_longlong, C.c_void_p, C.c_longlong]
+    rng = np.random.default_rng(m * 7 + n + k)
+    lda, ldb, ldc = m + 3, k + 1, m + 5
+    A = rng.standard_normal((k, lda)).astype(np.float32)  # column-major storage: column c at A[c]
+    B = rng.standard_normal((n, ldb)).astype(np.float32)
+    Cm = rng.standard_normal((n, ldc)).astype(np.float32)
+    dA = torch.tensor(A, device="cuda")
+    dB = torch.tensor(B, device="cuda")
+    dC = torch.tensor(Cm, device="cuda")
+    torch.cuda.synchronize()
+    st = lib.kd_tf32_gemm_update(ctx.h, m, n, k, dA.data_ptr(), lda, dB.data_ptr(), ldb, dC.data_ptr(), ldc)
+    assert st == 0, lib.kd_last_error(ctx.h)
+    ctx.synchronize()
+    got = dC.cpu().numpy()
+    Am = A[:, :m].T.astype(np.float64)          # m x k
+    Bm = B[:, :k].T.astype(np.float64)          # k x n
+    ref = Cm[:, :m].T.astype(np.float64) - Am @ Bm
+    err = np.abs(got[:, :m].T - ref).max()
+    scale = np.abs(Am).max() * np.abs(Bm).max() * k
+    assert err <= 4 * 2.0 ** -11 * scale, (err, scale)
+    # padding rows beyond m (ldc > m) untouched
+    assert np.array_equal(got[:, m:], Cm[:, m:])
