@@ -1,9 +1,13 @@
 // Dense LU with partial pivoting (column-major) and triangular solves.
-// Panel: one kernel per column (pivot search + row swap + scaling in one
-// CTA, then a multi-CTA rank-1 update of the rest of the panel); TRSM of the
-// U row block with the unit-lower L11 staged in shared memory; trailing
-// update as a GEMM (FP64 library GEMM, or the TF32 tensor-core kernel of
-// kd_gemm_tc.cu for the mixed mode).
+// Blocked right-looking factorisation, per panel of jb <= 96 columns:
+//   panel    one cooperative kernel over the whole GPU, rows of the panel
+//            held in shared memory, one grid barrier per column;
+//   swaps    the panel's row exchanges as one list of row moves, applied
+//            to the other columns by one warp per column;
+//   TRSM     U12 = L11^{-1} A12 with L11 staged in shared memory;
+//   update   A22 -= L21 U12 as a GEMM (FP64 library GEMM, or the TF32
+//            tensor-core kernel of kd_gemm_tc.cu for the mixed modes).
+// Solves use inverses of the 64 x 64 diagonal blocks (one launch per block).
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -18,103 +22,6 @@
 namespace kd {
 
 namespace {
-
-constexpr int PIV_THREADS = 1024;
-
-template <class T>
-__global__ void pivot_swap_scale(T* __restrict__ A, long long ld, int N, int j, int c0, int c1, int* ipiv,
-                                 int* info) {
-  // argmax |A[i, j]| over i in [j, N)
-  __shared__ double sv[32];
-  __shared__ int si[32];
-  double best = -1.0;
-  int bi = j;
-  const T* col = A + static_cast<long long>(j) * ld;
-  for (int i = j + threadIdx.x; i < N; i += blockDim.x) {
-    double v = fabs(static_cast<double>(col[i]));
-    if (v > best) {
-      best = v;
-      bi = i;
-    }
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    double ov = __shfl_xor_sync(0xffffffffu, best, o);
-    int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-    if (ov > best || (ov == best && oi < bi)) {
-      best = ov;
-      bi = oi;
-    }
-  }
-  if ((threadIdx.x & 31) == 0) {
-    sv[threadIdx.x >> 5] = best;
-    si[threadIdx.x >> 5] = bi;
-  }
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    int nw = blockDim.x >> 5;
-    best = (threadIdx.x < nw) ? sv[threadIdx.x] : -1.0;
-    bi = (threadIdx.x < nw) ? si[threadIdx.x] : j;
-    for (int o = 16; o > 0; o >>= 1) {
-      double ov = __shfl_xor_sync(0xffffffffu, best, o);
-      int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-      if (ov > best || (ov == best && oi < bi)) {
-        best = ov;
-        bi = oi;
-      }
-    }
-    if (threadIdx.x == 0) {
-      si[0] = bi;
-      sv[0] = best;
-      ipiv[j] = bi;
-      if (!(best > 0.0) && *info == 0) *info = j + 1;  // zero (or NaN) pivot
-    }
-  }
-  __syncthreads();
-  const int p = si[0];
-  // swap rows j and p inside the panel columns [c0, c1)
-  if (p != j)
-    for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
-      T* cc = A + static_cast<long long>(c) * ld;
-      T t = cc[j];
-      cc[j] = cc[p];
-      cc[p] = t;
-    }
-  __syncthreads();
-  double piv = static_cast<double>(col[j]);
-  if (piv != 0.0) {
-    double inv = 1.0 / piv;
-    T* cj = A + static_cast<long long>(j) * ld;
-    for (int i = j + 1 + threadIdx.x; i < N; i += blockDim.x) cj[i] = static_cast<T>(static_cast<double>(cj[i]) * inv);
-  }
-}
-
-// A[i, k] -= A[i, j] * A[j, k]  for i in (j, N), k in (j, c1)
-template <class T>
-__global__ void panel_rank1(T* __restrict__ A, long long ld, int N, int j, int c1) {
-  int i = j + 1 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= N) return;
-  double lij = static_cast<double>(A[static_cast<long long>(j) * ld + i]);
-  for (int k = j + 1; k < c1; k++) {
-    T* ck = A + static_cast<long long>(k) * ld;
-    ck[i] = static_cast<T>(static_cast<double>(ck[i]) - lij * static_cast<double>(ck[j]));
-  }
-}
-
-// Applies the pivots ipiv[j0..j1) to columns [c0, c1) (dlaswp).
-template <class T>
-__global__ void laswp(T* __restrict__ A, long long ld, int j0, int j1, const int* __restrict__ ipiv, int c0, int c1) {
-  int c = c0 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= c1) return;
-  T* cc = A + static_cast<long long>(c) * ld;
-  for (int j = j0; j < j1; j++) {
-    int p = ipiv[j];
-    if (p != j) {
-      T t = cc[j];
-      cc[j] = cc[p];
-      cc[p] = t;
-    }
-  }
-}
 
 // A12 := L11^{-1} A12, L11 unit lower (nb x nb at (j0, j0)), A12 = rows
 // [j0, j0+nb) of columns [c0, c1).  One thread per column, TRSM_COLS columns
@@ -292,6 +199,17 @@ DenseLU::DenseLU(Context* ctx) : ctx_(ctx) {
   if (cublasCreate(&blas_) != CUBLAS_STATUS_SUCCESS) throw KdError(KD_ERR_CUDA, "cublasCreate failed");
   cublasSetStream(blas_, ctx_->stream());
   cuda_check(cudaMalloc(&d_info_, sizeof(int)), "cudaMalloc(info)");
+  int dev = 0;
+  cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  cuda_check(cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev), "SM count");
+  // panel exchange slots (sized for FP64 rows), barrier counter, error flag,
+  // then the row-move list of one panel
+  const size_t slot_bytes = sizeof(double) * (2 * 128 * static_cast<size_t>(nsm_) + 2 * nsm_ + 2 * 128) +
+                            sizeof(int) * 2 * static_cast<size_t>(nsm_) + 32;
+  cuda_check(cudaMalloc(&slot_mem_, slot_bytes + sizeof(int) * (1 + 4 * 128)), "cudaMalloc(panel slots)");
+  cuda_check(cudaMemset(slot_mem_, 0, slot_bytes), "memset panel slots");
+  swap_map_ = reinterpret_cast<int*>(static_cast<char*>(slot_mem_) + slot_bytes);
+  panel_err_ = reinterpret_cast<int*>(static_cast<char*>(slot_mem_) + slot_bytes - 16);
 }
 
 DenseLU::~DenseLU() {
@@ -300,6 +218,7 @@ DenseLU::~DenseLU() {
   cudaFree(A32_);
   cudaFree(ipiv_);
   cudaFree(d_info_);
+  cudaFree(slot_mem_);
   cudaFree(work_);
   cudaFree(work32_);
   cudaFree(dinv_l_);
@@ -441,13 +360,342 @@ __global__ void panel_cluster_kernel(T* __restrict__ A, long long ld, int N, int
   }
 }
 
+// ---- panel over the whole GPU (cooperative launch) ------------------------
+// CTA b owns rows [j0 + b*per, j0 + (b+1)*per) of the panel and keeps them in
+// shared memory, column-major (tile[k*per + r]), for the whole panel.  Per
+// column j, ONE grid barrier:
+//   before it, every CTA publishes its local arg-max |a(i, j)| with the full
+//   panel row of that candidate, and the CTA owning row j publishes row j
+//   (double-buffered slots, indexed by the column's parity);
+//   after it, every CTA reduces the candidates in the same order (largest
+//   modulus, ties to the lowest row, as idamax), reads the winning row as the
+//   pivot row, the owner of the pivot row takes row j in its place, the owner
+//   of row j takes the pivot row, and each CTA scales and rank-1-updates its
+//   own rows.
+// Slot reuse is safe: a CTA writes slot (jj & 1) at column jj only after
+// barrier jj-1, by which every CTA has finished reading that slot (column
+// jj-2).  Cross-CTA data is read with L1-bypassing loads.
+constexpr int GP_THREADS = 256;
+constexpr int GP_MIN_ROWS = 32;
+constexpr size_t GP_MAX_SMEM = 200 * 1024;
+constexpr unsigned long long GP_WAIT_NS = 2000000000ull;  // 2 s per barrier
+
 template <class T>
-static void panel_factor(Context* ctx, T* A, long long ld, int N, int j0, int jb, int* ipiv, int* info) {
+struct PanelSlots {
+  T* cand_rows;     // [2][nblk][jb]
+  double* cand_v;   // [2][nblk]
+  int* cand_i;      // [2][nblk]
+  T* jrow;          // [2][jb]
+  unsigned* bar;    // arrival counter, zeroed before the launch
+  int* err;         // set when a barrier wait runs out
+};
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Grid barrier for a cooperative launch (all CTAs resident).  Returns false,
+// with *err set, when the counter did not reach `target` within the limit.
+__device__ bool grid_barrier(unsigned* bar, unsigned target, int* err, int* s_ok) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(bar, 1u);
+    const unsigned long long t0 = globaltimer_ns();
+    int ok = 1;
+    while (*reinterpret_cast<volatile unsigned*>(bar) < target) {
+      if (globaltimer_ns() - t0 > GP_WAIT_NS) {
+        ok = 0;
+        atomicExch(err, 1);
+        break;
+      }
+      __nanosleep(20);
+    }
+    __threadfence();
+    *s_ok = ok;
+  }
+  __syncthreads();
+  return *s_ok != 0;
+}
+
+__device__ __forceinline__ bool better(double v, int i, double bv, int bi) { return v > bv || (v == bv && i < bi); }
+
+// Block-wide arg-max of (v, i) carrying a tag; every thread gets the result.
+__device__ void block_argmax(double& v, int& i, int& tag, double* rv, int* ri, int* rt) {
+  for (int o = 16; o > 0; o >>= 1) {
+    double ov = __shfl_xor_sync(0xffffffffu, v, o);
+    int oi = __shfl_xor_sync(0xffffffffu, i, o);
+    int ot = __shfl_xor_sync(0xffffffffu, tag, o);
+    if (better(ov, oi, v, i)) {
+      v = ov;
+      i = oi;
+      tag = ot;
+    }
+  }
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    rv[w] = v;
+    ri[w] = i;
+    rt[w] = tag;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int q = 1; q < static_cast<int>(blockDim.x >> 5); q++)
+      if (better(rv[q], ri[q], rv[0], ri[0])) {
+        rv[0] = rv[q];
+        ri[0] = ri[q];
+        rt[0] = rt[q];
+      }
+  }
+  __syncthreads();
+  v = rv[0];
+  i = ri[0];
+  tag = rt[0];
+  __syncthreads();
+}
+
+template <class T>
+__global__ void __launch_bounds__(GP_THREADS) panel_grid_kernel(T* __restrict__ A, long long ld, int N, int j0, int jb,
+                                                                int per, int* __restrict__ ipiv,
+                                                                int* __restrict__ info, PanelSlots<T> ps) {
+  extern __shared__ __align__(16) unsigned char gp_raw[];
+  T* tile = reinterpret_cast<T*>(gp_raw);
+  __shared__ double prow[128];
+  __shared__ double rv[GP_THREADS / 32];
+  __shared__ int ri[GP_THREADS / 32], rt[GP_THREADS / 32];
+  __shared__ int s_ok;
+  const int nblk = gridDim.x, b = blockIdx.x, tid = threadIdx.x, bd = blockDim.x;
+  const int r0 = j0 + b * per;
+  const int r1 = (r0 + per < N) ? r0 + per : N;
+  const int nr = r1 - r0;
+  for (int e = tid; e < jb * nr; e += bd) {
+    int k = e / nr, r = e % nr;
+    tile[k * per + r] = A[static_cast<long long>(j0 + k) * ld + r0 + r];
+  }
+  __syncthreads();
+  for (int jj = 0; jj < jb; jj++) {
+    const int j = j0 + jj;
+    const int slot = jj & 1;
+    // 1. local candidate
+    double best = -1.0;
+    int bi = N, tag = 0;
+    for (int i = (r0 > j ? r0 : j) + tid; i < r1; i += bd) {
+      double v = fabs(static_cast<double>(tile[jj * per + i - r0]));
+      if (better(v, i, best, bi)) {
+        best = v;
+        bi = i;
+      }
+    }
+    block_argmax(best, bi, tag, rv, ri, rt);
+    // 2. publish it (and row j when this CTA owns it)
+    T* mine = ps.cand_rows + (static_cast<size_t>(slot) * nblk + b) * jb;
+    if (bi < N)
+      for (int k = tid; k < jb; k += bd) mine[k] = tile[k * per + bi - r0];
+    if (tid == 0) {
+      ps.cand_v[slot * nblk + b] = best;
+      ps.cand_i[slot * nblk + b] = bi;
+    }
+    if (j >= r0 && j < r1)
+      for (int k = tid; k < jb; k += bd) ps.jrow[slot * jb + k] = tile[k * per + j - r0];
+    // 3. one barrier per column
+    if (!grid_barrier(ps.bar, static_cast<unsigned>(nblk) * (jj + 1), ps.err, &s_ok)) return;
+    // 4. every CTA reduces the candidates identically
+    best = -1.0;
+    bi = N;
+    tag = -1;
+    for (int t = tid; t < nblk; t += bd) {
+      double v = __ldcg(ps.cand_v + slot * nblk + t);
+      int ii = __ldcg(ps.cand_i + slot * nblk + t);
+      if (better(v, ii, best, bi)) {
+        best = v;
+        bi = ii;
+        tag = t;
+      }
+    }
+    block_argmax(best, bi, tag, rv, ri, rt);
+    int gi = bi;
+    if (gi >= N) {  // nothing usable below the diagonal: no swap
+      gi = j;
+      tag = -1;
+    }
+    if (b == 0 && tid == 0) {
+      ipiv[j] = gi;
+      if (!(best > 0.0) && *info == 0) *info = j + 1;  // zero (or NaN) pivot
+    }
+    // 5. pivot row, row exchange
+    const T* src = (tag >= 0) ? ps.cand_rows + (static_cast<size_t>(slot) * nblk + tag) * jb : ps.jrow + slot * jb;
+    for (int k = tid; k < jb; k += bd) prow[k] = static_cast<double>(__ldcg(src + k));
+    if (gi != j && gi >= r0 && gi < r1)
+      for (int k = tid; k < jb; k += bd) tile[k * per + gi - r0] = __ldcg(ps.jrow + slot * jb + k);
+    __syncthreads();
+    if (j >= r0 && j < r1)
+      for (int k = tid; k < jb; k += bd) tile[k * per + j - r0] = static_cast<T>(prow[k]);
+    // 6. scale the column below the pivot, rank-1 update of the rest
+    const double piv = prow[jj];
+    const int rs = (r0 > j + 1) ? r0 : j + 1;
+    __syncthreads();
+    if (piv != 0.0 && rs < r1) {
+      const T inv = static_cast<T>(1.0 / piv);
+      for (int i = rs + tid; i < r1; i += bd) tile[jj * per + i - r0] *= inv;
+      __syncthreads();
+      const int nrr = r1 - rs, ncols = jb - jj - 1;
+      for (int e = tid; e < ncols * nrr; e += bd) {
+        int k = jj + 1 + e / nrr;
+        int i = rs - r0 + e % nrr;
+        tile[k * per + i] = fma(-tile[jj * per + i], static_cast<T>(prow[k]), tile[k * per + i]);
+      }
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < jb * nr; e += bd) {
+    int k = e / nr, r = e % nr;
+    A[static_cast<long long>(j0 + k) * ld + r0 + r] = tile[k * per + r];
+  }
+}
+
+// The row exchanges of one panel (ipiv[j0 .. j0+jb)) as a list of moves
+// row dst[t] <- row src[t] over the rows they touch (at most 2 jb): rows
+// j0 .. j0+jb-1 first, then the pivot rows below the panel.  One warp.
+__global__ void build_swap_map(const int* __restrict__ ipiv, int j0, int jb, int* __restrict__ map) {
+  // map[0] = count, map[1 .. 1+2jb) = dst, map[1+2jb .. 1+4jb) = src
+  __shared__ int rows[256], content[256];
+  __shared__ int cnt;
+  const int lane = threadIdx.x;
+  for (int t = lane; t < jb; t += 32) {
+    rows[t] = j0 + t;
+    content[t] = j0 + t;
+  }
+  if (lane == 0) cnt = jb;
+  __syncwarp();
+  for (int jj = 0; jj < jb; jj++) {
+    const int p = ipiv[j0 + jj];
+    int idx;
+    if (p < j0 + jb) {
+      idx = p - j0;
+    } else {
+      idx = -1;
+      for (int t0 = jb; t0 < cnt; t0 += 32) {
+        unsigned m = __ballot_sync(0xffffffffu, t0 + lane < cnt && rows[t0 + lane] == p);
+        if (m) {
+          idx = t0 + __ffs(m) - 1;
+          break;
+        }
+      }
+      if (idx < 0) {
+        idx = cnt;
+        if (lane == 0) {
+          rows[idx] = p;
+          content[idx] = p;
+        }
+      }
+    }
+    __syncwarp();
+    if (lane == 0) {
+      if (idx == cnt) cnt = cnt + 1;
+      int t = content[jj];
+      content[jj] = content[idx];
+      content[idx] = t;
+    }
+    __syncwarp();
+  }
+  const int n = cnt;
+  for (int t = lane; t < n; t += 32) {
+    map[1 + t] = rows[t];
+    map[1 + 2 * jb + t] = content[t];
+  }
+  if (lane == 0) map[0] = n;
+}
+
+// Applies a panel's row moves to every column outside the panel, one warp
+// per column: all sources are read into registers before any write.
+constexpr int SWAP_PER_LANE = 8;  // 2 jb <= 256 = 32 x 8 moves
+template <class T>
+__global__ void laswp_map(T* __restrict__ A, long long ld, int N, int j0, int jb, const int* __restrict__ map) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int ncol = N - jb;
+  if (warp >= ncol) return;
+  const int c = (warp < j0) ? warp : warp + jb;
+  T* col = A + static_cast<long long>(c) * ld;
+  const int n = map[0];
+  const int* dst = map + 1;
+  const int* src = map + 1 + 2 * jb;
+  T v[SWAP_PER_LANE];
+#pragma unroll
+  for (int q = 0; q < SWAP_PER_LANE; q++) {
+    int t = lane + 32 * q;
+    if (t < n) v[q] = col[src[t]];
+  }
+  __syncwarp();
+#pragma unroll
+  for (int q = 0; q < SWAP_PER_LANE; q++) {
+    int t = lane + 32 * q;
+    if (t < n && dst[t] != src[t]) col[dst[t]] = v[q];
+  }
+}
+
+template <class T>
+static bool panel_grid(Context* ctx, T* A, long long ld, int N, int j0, int jb, int* ipiv, int* info, int nsm,
+                       const PanelSlots<T>& slots) {
+  const int rows = N - j0;
+  int nblk = (rows + GP_MIN_ROWS - 1) / GP_MIN_ROWS;
+  if (nblk > nsm) nblk = nsm;
+  const int per = (rows + nblk - 1) / nblk;
+  nblk = (rows + per - 1) / per;
+  const size_t smem = static_cast<size_t>(per) * jb * sizeof(T);
+  if (smem > GP_MAX_SMEM) return false;
+  static bool attr = false;
+  if (!attr) {
+    cuda_check(cudaFuncSetAttribute(panel_grid_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(GP_MAX_SMEM)),
+               "cudaFuncSetAttribute(panel)");
+    attr = true;
+  }
+  cudaStream_t s = ctx->stream();
+  cuda_check(cudaMemsetAsync(slots.bar, 0, sizeof(unsigned), s), "memset barrier");
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nblk, 1, 1);
+  cfg.blockDim = dim3(GP_THREADS, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cuda_check(cudaLaunchKernelEx(&cfg, panel_grid_kernel<T>, A, ld, N, j0, jb, per, ipiv, info, slots),
+             "panel grid kernel");
+  ctx->launches += 1;
+  return true;
+}
+
+template <class T>
+static void panel_factor(Context* ctx, T* A, long long ld, int N, int j0, int jb, int* ipiv, int* info, int nsm,
+                         void* slot_mem) {
   cudaStream_t s = ctx->stream();
   double fl = 0;
   for (int j = j0; j < j0 + jb; j++) fl += 2.0 * (N - j - 1) * (j0 + jb - j - 1) + (N - j);
   ProfScope ps(ctx, Context::PROF_LU_PANEL, fl);
   if (jb > 128) throw KdError(KD_ERR_ARG, "panel width above 128");
+  PanelSlots<T> slots;
+  {
+    char* p = static_cast<char*>(slot_mem);
+    slots.cand_rows = reinterpret_cast<T*>(p);
+    p += sizeof(double) * 2 * 128 * static_cast<size_t>(nsm);
+    slots.cand_v = reinterpret_cast<double*>(p);
+    p += sizeof(double) * 2 * static_cast<size_t>(nsm);
+    slots.jrow = reinterpret_cast<T*>(p);
+    p += sizeof(double) * 2 * 128;
+    slots.cand_i = reinterpret_cast<int*>(p);
+    p += sizeof(int) * 2 * static_cast<size_t>(nsm);
+    slots.bar = reinterpret_cast<unsigned*>(p);
+    slots.err = reinterpret_cast<int*>(p + 16);
+  }
+  if (panel_grid<T>(ctx, A, ld, N, j0, jb, ipiv, info, nsm, slots)) return;
+  // Panels too tall for the shared memory of the GPU: one 8-CTA cluster
+  // working on the panel in global memory.
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(PANEL_CL, 1, 1);
   cfg.blockDim = dim3(PANEL_THREADS, 1, 1);
@@ -465,12 +713,15 @@ static void panel_factor(Context* ctx, T* A, long long ld, int N, int j0, int jb
 }
 
 template <class T>
-static void trsm_and_swaps(Context* ctx, T* A, long long ld, int N, int j0, int jb, const int* ipiv) {
+static void trsm_and_swaps(Context* ctx, T* A, long long ld, int N, int j0, int jb, const int* ipiv, int* map) {
   cudaStream_t s = ctx->stream();
   ProfScope ps(ctx, Context::PROF_LU_SWAP_TRSM, double(jb) * jb * (N - j0 - jb));
-  if (j0 > 0) laswp<T><<<blocks(j0, 128), 128, 0, s>>>(A, ld, j0, j0 + jb, ipiv, 0, j0);
+  if (N > jb) {
+    build_swap_map<<<1, 32, 0, s>>>(ipiv, j0, jb, map);
+    laswp_map<T><<<blocks(static_cast<long long>(N - jb) * 32, 256), 256, 0, s>>>(A, ld, N, j0, jb, map);
+    ctx->launches += 2;
+  }
   if (j0 + jb < N) {
-    laswp<T><<<blocks(N - j0 - jb, 128), 128, 0, s>>>(A, ld, j0, j0 + jb, ipiv, j0 + jb, N);
     size_t smem = sizeof(double) * (static_cast<size_t>(jb) * jb + static_cast<size_t>(jb) * TRSM_COLS);
     static bool attr_set = false;
     if (!attr_set) {
@@ -480,7 +731,6 @@ static void trsm_and_swaps(Context* ctx, T* A, long long ld, int N, int j0, int 
     trsm_unit_lower<T><<<blocks(N - j0 - jb, TRSM_COLS), TRSM_COLS, smem, s>>>(A, ld, j0, jb, j0 + jb, N);
     ctx->launches += 1;
   }
-  ctx->launches += 2;
   cuda_check(cudaGetLastError(), "laswp/trsm kernels");
 }
 
@@ -490,8 +740,8 @@ void DenseLU::factor_fp64(double* A, long long ld, int N) {
   cuda_check(cudaMemsetAsync(d_info_, 0, sizeof(int), s), "memset info");
   for (int j0 = 0; j0 < N; j0 += NB) {
     int jb = (N - j0 < NB) ? N - j0 : NB;
-    panel_factor<double>(ctx_, A, ld, N, j0, jb, ipiv_, d_info_);
-    trsm_and_swaps<double>(ctx_, A, ld, N, j0, jb, ipiv_);
+    panel_factor<double>(ctx_, A, ld, N, j0, jb, ipiv_, d_info_, nsm_, slot_mem_);
+    trsm_and_swaps<double>(ctx_, A, ld, N, j0, jb, ipiv_, swap_map_);
     int m = N - j0 - jb;
     if (m > 0) {
       // A22 -= A21 * A12 (FP64 library GEMM)
@@ -514,8 +764,8 @@ void DenseLU::factor_f32(float* A, long long ld, int N, bool tf32) {
   cuda_check(cudaMemsetAsync(d_info_, 0, sizeof(int), s), "memset info");
   for (int j0 = 0; j0 < N; j0 += NB) {
     int jb = (N - j0 < NB) ? N - j0 : NB;
-    panel_factor<float>(ctx_, A, ld, N, j0, jb, ipiv_, d_info_);
-    trsm_and_swaps<float>(ctx_, A, ld, N, j0, jb, ipiv_);
+    panel_factor<float>(ctx_, A, ld, N, j0, jb, ipiv_, d_info_, nsm_, slot_mem_);
+    trsm_and_swaps<float>(ctx_, A, ld, N, j0, jb, ipiv_, swap_map_);
     int m = N - j0 - jb;
     if (m > 0) {
       float* A21 = A + static_cast<long long>(j0) * ld + j0 + jb;
@@ -559,6 +809,12 @@ void DenseLU::factor(double* A, long long ld, int N, int mode) {
   cuda_check(cudaMemcpyAsync(&info, d_info_, sizeof(int), cudaMemcpyDeviceToHost, ctx_->stream()), "D2H info");
   cuda_check(cudaStreamSynchronize(ctx_->stream()), "sync after LU");
   stats.t_factor_ms = now_ms() - t0;
+  int perr = 0;
+  cuda_check(cudaMemcpy(&perr, panel_err_, sizeof(int), cudaMemcpyDeviceToHost), "D2H panel flag");
+  if (perr) {
+    cuda_check(cudaMemset(panel_err_, 0, sizeof(int)), "reset panel flag");
+    throw KdError(KD_ERR_TIMEOUT, "panel factorisation: a grid barrier wait ran out");
+  }
   if (mode == LU_TF32_IR && tf32_gemm_error_flag(ctx_))
     throw KdError(KD_ERR_TIMEOUT, "tensor-core trailing update timed out waiting for its MMAs");
   if (info != 0) throw KdError(KD_ERR_SINGULAR, "Jacobian is singular (zero pivot at column " + std::to_string(info) + ")");

@@ -55,6 +55,10 @@ class DenseLU {
   int* ipiv_ = nullptr;        // device pivots
   size_t ipiv_cap_ = 0;
   int* d_info_ = nullptr;
+  int nsm_ = 0;                // SM count (grid of the panel kernel)
+  void* slot_mem_ = nullptr;   // panel exchange slots, barrier, row-move list
+  int* swap_map_ = nullptr;
+  int* panel_err_ = nullptr;
   double* work_ = nullptr;     // solver workspace
   size_t work_cap_ = 0;
   float* work32_ = nullptr;
