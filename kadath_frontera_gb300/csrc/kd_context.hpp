@@ -61,7 +61,15 @@ class Context {
   // Device copy of a double table, cached by content.
   const double* dtable(const std::vector<double>& content);
 
-  DeviceArena& scratch() { return scratch_; }
+  // Arena every DVal operation allocates from.  Normally the per-pass
+  // scratch arena; redirect_scratch() points it at another arena (the
+  // system's cache of node values) and returns the previous one.
+  DeviceArena& scratch() { return *active_scratch_; }
+  DeviceArena* redirect_scratch(DeviceArena* a) {
+    DeviceArena* old = active_scratch_;
+    active_scratch_ = a ? a : &scratch_;
+    return old;
+  }
   DeviceArena& persistent() { return persistent_; }
 
   // While a CUDA graph is being captured no host->device upload may happen;
@@ -120,6 +128,7 @@ class Context {
   std::map<std::vector<int>, int*> itables_;
   std::map<std::vector<double>, double*> dtables_;
   DeviceArena scratch_;
+  DeviceArena* active_scratch_ = &scratch_;
   DeviceArena persistent_{size_t(64) << 20};
 };
 

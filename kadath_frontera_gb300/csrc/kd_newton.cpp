@@ -42,7 +42,7 @@ bool Newton::step(const NewtonOpts& o, NewtonReport& rep) {
   if (sys_->nbr_conditions() < 0) sys_->residual(nullptr);  // fixes nbr_conditions on the first call
   int N = sys_->nbr_conditions();
   ensure(N);
-  sys_->residual(d_F);
+  sys_->residual(d_F, true);  // node values kept for the Jacobian
   double* d_err = ctx->scratch().alloc_doubles(1);
   cuda_check(launch_absmax(d_F, N, d_err, s), "absmax");
   double err = 0;
@@ -61,7 +61,7 @@ bool Newton::step(const NewtonOpts& o, NewtonReport& rep) {
     throw KdError(KD_ERR_STATE, "Number of unknowns (" + std::to_string(nu) +
                                     ") is different from the number of equations (" + std::to_string(N) + ")");
   auto t1 = std::chrono::steady_clock::now();
-  sys_->jacobian(d_J, ld);
+  sys_->jacobian(d_J, ld, true);
   cuda_check(cudaStreamSynchronize(s), "sync assembly");
   rep.t_assembly_ms = ms_since(t1);
   lu_->gmres_tol = o.gmres_tol;

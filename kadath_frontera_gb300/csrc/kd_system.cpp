@@ -170,10 +170,45 @@ Term EvalState::def_term(int which, int dom) {
   auto it = def_cache.find(key);
   if (it != def_cache.end()) return it->second;
   const auto& df = sys->defs_.at(which);
-  Term t = df.ope->action(*this);
+  Term t = df.ope->eval(*this);
   def_cache[key] = t;
   return t;
 }
+
+// ------------------------------------------------------------ node values --
+void ValueCache::store(const Ope* node, const Term& t) {
+  Term v;
+  v.dom = t.dom;
+  v.is_double = t.is_double;
+  v.vd = t.vd;
+  v.valence = t.valence;
+  v.vt = t.vt;
+  for (auto& x : v.vt)
+    if (!x.zero && !x.in_conf && x.base.def) x.coef_i();
+  vals[node] = std::move(v);
+}
+
+Term Ope::eval(EvalState& st) const {
+  ValueCache* vc = st.vcache;
+  if (!vc || !cacheable()) return action(st, nullptr);
+  if (st.with_der) {
+    auto it = vc->vals.find(this);
+    return action(st, it != vc->vals.end() ? &it->second : nullptr);
+  }
+  Term t = action(st, nullptr);
+  if (st.record) vc->store(this, t);
+  return t;
+}
+
+namespace {
+// Sends every DVal allocation to another arena for the guard's lifetime.
+struct ScratchRedirect {
+  Context* ctx;
+  DeviceArena* prev;
+  ScratchRedirect(Context* c, DeviceArena* a) : ctx(c), prev(c->redirect_scratch(a)) {}
+  ~ScratchRedirect() { ctx->redirect_scratch(prev); }
+};
+}  // namespace
 
 // ----------------------------------------------------------------- System --
 System::System(Context* c, const Space* s, int dmin, int dmax) : ctx(c), sp(s), dom_min(dmin), dom_max(dmax) {
@@ -207,7 +242,7 @@ bool split_eq(const std::string& s, std::string& l, std::string& r) {
 class OpeSubEq : public Ope {
  public:
   OpeSubEq(int dom, OpePtr a, OpePtr b) : Ope(dom), a(std::move(a)), b(std::move(b)) {}
-  Term action(EvalState& st) const override { return a->action(st) - b->action(st); }
+  Term action(EvalState& st, const Term* cv) const override { return t_sub(a->eval(st), b->eval(st), cv); }
   OpePtr a, b;
 };
 }  // namespace
@@ -428,16 +463,22 @@ int System::nbr_unknowns() {
   return nbr_unknowns_;
 }
 
-void System::residual(double* d_F) {
+void System::residual(double* d_F, bool record) {
   ctx->scratch().reset();
+  vcache_.clear();
+  std::unique_ptr<ScratchRedirect> redirect;
+  if (record) redirect = std::make_unique<ScratchRedirect>(ctx, &vcache_.arena);
   EvalState st;
   st.sys = this;
   st.with_der = false;
+  st.vcache = record ? &vcache_ : nullptr;
+  st.record = record;
   std::vector<Term> lhs(eqs_.size()), rhs(eqs_.size());
   for (size_t i = 0; i < eqs_.size(); i++) {
-    lhs[i] = eqs_[i].lhs->action(st);
-    if (eqs_[i].kind == Equation::MATCHING) rhs[i] = eqs_[i].rhs->action(st);
+    lhs[i] = eqs_[i].lhs->eval(st);
+    if (eqs_[i].kind == Equation::MATCHING) rhs[i] = eqs_[i].rhs->eval(st);
   }
+  vcache_.valid = record;
   if (nbr_conditions_ < 0) {
     int row = 0;
     for (size_t i = 0; i < eqs_.size(); i++) {
@@ -478,9 +519,9 @@ const double* System::seed_block(int var, int dom, int& B, Base& base) {
   return p;
 }
 
-void System::jacobian(double* d_J, long long ld) {
+void System::jacobian(double* d_J, long long ld, bool reuse) {
   int N = nbr_unknowns();
-  if (nbr_conditions_ < 0) residual(nullptr);
+  if (!reuse || !vcache_.valid) residual(nullptr, true);
   if (nbr_conditions_ != N) {
     std::ostringstream os;
     os << "Number of unknowns (" << N << ") is different from the number of equations (" << nbr_conditions_ << ")";
@@ -502,16 +543,17 @@ void System::jacobian(double* d_J, long long ld) {
       st.seed_var = static_cast<int>(v);
       st.seed_dom = dd;
       st.seed = DVal::from_coef(ctx, &sp->dom(dd), B, seeds, base);
+      st.vcache = &vcache_;
       int col0 = col0_[{static_cast<int>(v), dd}];
       double* Jblock = d_J + static_cast<long long>(col0) * ld;
       for (auto& eq : eqs_) {
         if (!eq.take_into_account(dd)) continue;
         if (eq.kind != Equation::MATCHING || dd == eq.dom) {
-          Term t = eq.lhs->action(st);
+          Term t = eq.lhs->eval(st);
           export_term(eq, t, true, eq.dom, eq.bound, Jblock + eq.row0, ld, 1, B, 1.0, true);
         }
         if (eq.kind == Equation::MATCHING && dd == eq.other_dom) {
-          Term t = eq.rhs->action(st);
+          Term t = eq.rhs->eval(st);
           export_term(eq, t, true, eq.other_dom, eq.other_bound, Jblock + eq.row0, ld, 1, B, -1.0, true);
         }
       }
@@ -521,6 +563,7 @@ void System::jacobian(double* d_J, long long ld) {
 void System::update_from_x(const double* d_x) {
   int N = nbr_unknowns();
   (void)N;
+  vcache_.clear();
   ctx->scratch().reset();
   // doubles first
   if (!vdoubles_.empty()) {

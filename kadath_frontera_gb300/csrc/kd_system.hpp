@@ -6,6 +6,7 @@
 // (xx_to_vars, src/System_of_eqs/system_of_eqs.cpp:597).
 #pragma once
 #include <map>
+#include <unordered_map>
 #include <memory>
 #include <string>
 #include <vector>
@@ -55,6 +56,24 @@ struct CsrTable {
 class System;
 
 // State of one evaluation pass (residual or one batched Jacobian block).
+// Node values of one iterate, recorded by a value pass (the residual) and
+// reused by every tangent pass of the Jacobian at the same iterate.  The
+// values live in their own arena, so the per-seed-block scratch resets do
+// not touch them.
+struct ValueCache {
+  std::unordered_map<const Ope*, Term> vals;
+  DeviceArena arena{size_t(64) << 20};
+  bool valid = false;
+  void clear() {
+    vals.clear();
+    arena.reset();
+    valid = false;
+  }
+  // Keeps the value part of t; fields known only by coefficients also get
+  // their collocation values now, since tangent products need them.
+  void store(const Ope* node, const Term& t);
+};
+
 struct EvalState {
   System* sys = nullptr;
   bool with_der = false;
@@ -64,6 +83,8 @@ struct EvalState {
   int seed_var_double = -1;
   DVal seed;               // batch-B coefficient patterns
   std::map<std::pair<int, int>, Term> def_cache;
+  ValueCache* vcache = nullptr;  // node values: recorded (record) or reused (with_der)
+  bool record = false;
 
   Term var_term(int which, int dom);
   Term var_double_term(int which, int dom);
@@ -119,9 +140,12 @@ class System {
   const Equation& equation(int i) const { return eqs_[i]; }
 
   // F(u) into a device vector of nbr_conditions doubles.
-  void residual(double* d_F);
+  // record: keep every node value for a following jacobian(..., true).
+  void residual(double* d_F, bool record = false);
   // Column-major dense Jacobian (ld >= nbr_conditions) on the device.
-  void jacobian(double* d_J, long long ld);
+  // reuse: take node values from the preceding residual(..., true) at the
+  // same iterate; otherwise a value pass is run first.
+  void jacobian(double* d_J, long long ld, bool reuse = false);
   // J * x for a device vector x (System_of_eqs::do_JX, solver.cpp:87).
   void jx(const double* d_x, double* d_out);
   // var = old - (fields built from x)  (do_newton's update, src_par/do_newton.cpp:397-414)
@@ -170,6 +194,7 @@ class System {
   std::map<std::pair<int, int>, const double*> seeds_;  // device seed blocks
   std::map<std::pair<int, int>, CsrTable> xmaps_;      // affecte_tau maps
   std::map<std::vector<int>, CsrTable> tables_;
+  ValueCache vcache_;
 
   void compute_unknowns();
   void apply(Equation& eq, EvalState& st, Term& lhs, Term& rhs, bool do_lhs, bool do_rhs);

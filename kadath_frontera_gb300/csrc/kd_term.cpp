@@ -36,7 +36,11 @@ void check_valence(const Term& a, const Term& b) {
 
 }  // namespace
 
-Term operator+(const Term& a, const Term& b) {
+// Each operation takes an optional `cv`: the value of its result, already
+// known (a node value cached from the value pass of the same iterate).  The
+// value is then adopted instead of recomputed and only the tangent is
+// evaluated; tangents only ever use the operands' values, never the result's.
+Term t_add(const Term& a, const Term& b, const Term* cv) {
   check_dom(a, b);
   bool do_der = a.has_der() && b.has_der();
   if (a.is_double && b.is_double) {
@@ -51,7 +55,9 @@ Term operator+(const Term& a, const Term& b) {
     const Term& t = a.is_double ? b : a;
     const Term& d = a.is_double ? a : b;
     Term r = tensor_like(t);
-    for (auto& v : t.vt) r.vt.push_back(v + d.vd);
+    if (cv) r.vt = cv->vt;
+    else
+      for (auto& v : t.vt) r.vt.push_back(v + d.vd);
     if (do_der) {
       r.has_dt = true;
       for (int i = 0; i < ncomp(t); i++) r.dt.push_back(d.dd == 0.0 ? t.dt[i] : t.dt[i] + d.dd);
@@ -60,7 +66,9 @@ Term operator+(const Term& a, const Term& b) {
   }
   check_valence(a, b);
   Term r = tensor_like(a);
-  for (int i = 0; i < ncomp(a); i++) r.vt.push_back(a.vt[i] + b.vt[i]);
+  if (cv) r.vt = cv->vt;
+  else
+    for (int i = 0; i < ncomp(a); i++) r.vt.push_back(a.vt[i] + b.vt[i]);
   if (do_der) {
     r.has_dt = true;
     for (int i = 0; i < ncomp(a); i++) r.dt.push_back(a.dt[i] + b.dt[i]);
@@ -68,7 +76,7 @@ Term operator+(const Term& a, const Term& b) {
   return r;
 }
 
-Term operator-(const Term& a, const Term& b) {
+Term t_sub(const Term& a, const Term& b, const Term* cv) {
   check_dom(a, b);
   bool do_der = a.has_der() && b.has_der();
   if (a.is_double && b.is_double) {
@@ -81,7 +89,9 @@ Term operator-(const Term& a, const Term& b) {
   }
   if (b.is_double) {
     Term r = tensor_like(a);
-    for (auto& v : a.vt) r.vt.push_back(v - b.vd);
+    if (cv) r.vt = cv->vt;
+    else
+      for (auto& v : a.vt) r.vt.push_back(v - b.vd);
     if (do_der) {
       r.has_dt = true;
       for (int i = 0; i < ncomp(a); i++) r.dt.push_back(b.dd == 0.0 ? a.dt[i] : a.dt[i] - b.dd);
@@ -90,7 +100,9 @@ Term operator-(const Term& a, const Term& b) {
   }
   if (a.is_double) {
     Term r = tensor_like(b);
-    for (auto& v : b.vt) r.vt.push_back(a.vd - v);
+    if (cv) r.vt = cv->vt;
+    else
+      for (auto& v : b.vt) r.vt.push_back(a.vd - v);
     if (do_der) {
       r.has_dt = true;
       for (int i = 0; i < ncomp(b); i++) r.dt.push_back(a.dd == 0.0 ? -b.dt[i] : a.dd - b.dt[i]);
@@ -99,7 +111,9 @@ Term operator-(const Term& a, const Term& b) {
   }
   check_valence(a, b);
   Term r = tensor_like(a);
-  for (int i = 0; i < ncomp(a); i++) r.vt.push_back(a.vt[i] - b.vt[i]);
+  if (cv) r.vt = cv->vt;
+  else
+    for (int i = 0; i < ncomp(a); i++) r.vt.push_back(a.vt[i] - b.vt[i]);
   if (do_der) {
     r.has_dt = true;
     for (int i = 0; i < ncomp(a); i++) r.dt.push_back(a.dt[i] - b.dt[i]);
@@ -107,7 +121,7 @@ Term operator-(const Term& a, const Term& b) {
   return r;
 }
 
-Term operator-(const Term& a) {
+Term t_neg(const Term& a, const Term* cv) {
   // Term_eq operator-(aa) = -1. * aa
   if (a.is_double) {
     Term r = Term::dbl(a.dom, -a.vd);
@@ -118,7 +132,9 @@ Term operator-(const Term& a) {
     return r;
   }
   Term r = tensor_like(a);
-  for (auto& v : a.vt) r.vt.push_back(v * -1.0);
+  if (cv) r.vt = cv->vt;
+  else
+    for (auto& v : a.vt) r.vt.push_back(v * -1.0);
   if (a.has_dt) {
     r.has_dt = true;
     for (auto& v : a.dt) r.dt.push_back(v * -1.0);
@@ -126,7 +142,7 @@ Term operator-(const Term& a) {
   return r;
 }
 
-Term operator*(const Term& a, const Term& b) {
+Term t_mul(const Term& a, const Term& b, const Term* cv) {
   check_dom(a, b);
   bool do_der = a.has_der() && b.has_der();
   if (a.is_double && b.is_double) {
@@ -141,7 +157,9 @@ Term operator*(const Term& a, const Term& b) {
     const Term& t = a.is_double ? b : a;
     const Term& d = a.is_double ? a : b;
     Term r = tensor_like(t);
-    for (auto& v : t.vt) r.vt.push_back(v * d.vd);
+    if (cv) r.vt = cv->vt;
+    else
+      for (auto& v : t.vt) r.vt.push_back(v * d.vd);
     if (do_der) {
       r.has_dt = true;
       for (int i = 0; i < ncomp(t); i++) {
@@ -158,7 +176,9 @@ Term operator*(const Term& a, const Term& b) {
   const Term& t = (a.vt.size() == 1) ? b : a;
   bool s_first = (&s == &a);
   Term r = tensor_like(t);
-  for (int i = 0; i < ncomp(t); i++) r.vt.push_back(s_first ? s.vt[0] * t.vt[i] : t.vt[i] * s.vt[0]);
+  if (cv) r.vt = cv->vt;
+  else
+    for (int i = 0; i < ncomp(t); i++) r.vt.push_back(s_first ? s.vt[0] * t.vt[i] : t.vt[i] * s.vt[0]);
   if (do_der) {
     r.has_dt = true;
     for (int i = 0; i < ncomp(t); i++) {
@@ -173,7 +193,7 @@ Term operator*(const Term& a, const Term& b) {
   return r;
 }
 
-Term operator/(const Term& a, const Term& b) {
+Term t_div(const Term& a, const Term& b, const Term* cv) {
   check_dom(a, b);
   bool do_der = a.has_der() && b.has_der();
   if (a.is_double && b.is_double) {
@@ -186,7 +206,9 @@ Term operator/(const Term& a, const Term& b) {
   }
   if (b.is_double) {
     Term r = tensor_like(a);
-    for (auto& v : a.vt) r.vt.push_back(v / b.vd);
+    if (cv) r.vt = cv->vt;
+    else
+      for (auto& v : a.vt) r.vt.push_back(v / b.vd);
     if (do_der) {
       r.has_dt = true;
       for (int i = 0; i < ncomp(a); i++) {
@@ -200,7 +222,9 @@ Term operator/(const Term& a, const Term& b) {
   if (b.vt.size() != 1) throw KdError(KD_ERR_UNSUPPORTED, "division by a non-scalar tensor");
   if (a.is_double) {
     Term r = tensor_like(b);
-    r.vt.push_back(a.vd / b.vt[0]);
+    if (cv) r.vt = cv->vt;
+    else
+      r.vt.push_back(a.vd / b.vt[0]);
     if (do_der) {
       r.has_dt = true;
       DVal num = (dd_zero(a) ? DVal::zeros(b.vt[0].ctx, b.vt[0].dom, 1) : b.vt[0] * a.dd) - b.dt[0] * a.vd;
@@ -209,7 +233,9 @@ Term operator/(const Term& a, const Term& b) {
     return r;
   }
   Term r = tensor_like(a);
-  for (int i = 0; i < ncomp(a); i++) r.vt.push_back(a.vt[i] / b.vt[0]);
+  if (cv) r.vt = cv->vt;
+  else
+    for (int i = 0; i < ncomp(a); i++) r.vt.push_back(a.vt[i] / b.vt[0]);
   if (do_der) {
     r.has_dt = true;
     DVal bb = b.vt[0] * b.vt[0];
@@ -218,17 +244,25 @@ Term operator/(const Term& a, const Term& b) {
   return r;
 }
 
-Term term_pow(const Term& a, int n) {
-  // pow(Term_eq, int), term_eq_math.cpp:547
+Term operator+(const Term& a, const Term& b) { return t_add(a, b, nullptr); }
+Term operator-(const Term& a, const Term& b) { return t_sub(a, b, nullptr); }
+Term operator*(const Term& a, const Term& b) { return t_mul(a, b, nullptr); }
+Term operator/(const Term& a, const Term& b) { return t_div(a, b, nullptr); }
+Term operator-(const Term& a) { return t_neg(a, nullptr); }
+
+Term term_pow(const Term& a, int n, const Term* cv) {
+  // pow(Term_eq, int), term_eq_math.cpp:547.  Intermediate powers keep
+  // their values (the next product's tangent needs them); only the last
+  // product may adopt a cached value.
   if (n > 0) {
     Term r = a;
-    for (int i = 1; i < n; i++) r = r * a;
+    for (int i = 1; i < n; i++) r = t_mul(r, a, (i == n - 1) ? cv : nullptr);
     return r;
   }
   if (a.is_double) {
     Term one = Term::dbl_der(a.dom, 1.0, 0.0);
     Term r = one;
-    for (int i = 0; i < -n; i++) r = r / a;
+    for (int i = 0; i < -n; i++) r = t_div(r, a, (i == -n - 1) ? cv : nullptr);
     return r;
   }
   Term one = tensor_like(a);
@@ -238,17 +272,19 @@ Term term_pow(const Term& a, int n) {
   one.has_dt = true;
   one.dt.push_back(DVal::zeros(a.vt[0].ctx, a.vt[0].dom, 1));
   Term r = one;
-  for (int i = 0; i < -n; i++) r = r / a;
+  for (int i = 0; i < -n; i++) r = t_div(r, a, (i == -n - 1) ? cv : nullptr);
   return r;
 }
 
 // --------------------------------------------------------------- Ope tree --
 namespace {
 
-Term comp_by_comp(const Term& t, const std::function<DVal(const DVal&)>& f) {
+Term comp_by_comp(const Term& t, const std::function<DVal(const DVal&)>& f, const Term* cv) {
   if (t.is_double) throw KdError(KD_ERR_UNSUPPORTED, "operator only defined for tensor terms");
   Term r = tensor_like(t);
-  for (auto& v : t.vt) r.vt.push_back(v.zero ? v : f(v));
+  if (cv) r.vt = cv->vt;
+  else
+    for (auto& v : t.vt) r.vt.push_back(v.zero ? v : f(v));
   if (t.has_dt) {
     r.has_dt = true;
     for (auto& v : t.dt) r.dt.push_back(v.zero ? v : f(v));
@@ -259,14 +295,14 @@ Term comp_by_comp(const Term& t, const std::function<DVal(const DVal&)>& f) {
 class OpeBin : public Ope {
  public:
   OpeBin(int dom, char op, OpePtr a, OpePtr b) : Ope(dom), op(op), a(std::move(a)), b(std::move(b)) {}
-  Term action(EvalState& st) const override {
-    Term x = a->action(st);
-    Term y = b->action(st);
+  Term action(EvalState& st, const Term* cv) const override {
+    Term x = a->eval(st);
+    Term y = b->eval(st);
     switch (op) {
-      case '+': return x + y;
-      case '-': return x - y;
-      case '*': return x * y;
-      default: return x / y;
+      case '+': return t_add(x, y, cv);
+      case '-': return t_sub(x, y, cv);
+      case '*': return t_mul(x, y, cv);
+      default: return t_div(x, y, cv);
     }
   }
   char op;
@@ -276,14 +312,14 @@ class OpeBin : public Ope {
 class OpeMinus : public Ope {
  public:
   OpeMinus(int dom, OpePtr a) : Ope(dom), a(std::move(a)) {}
-  Term action(EvalState& st) const override { return -a->action(st); }
+  Term action(EvalState& st, const Term* cv) const override { return t_neg(a->eval(st), cv); }
   OpePtr a;
 };
 
 class OpePow : public Ope {
  public:
   OpePow(int dom, int n, OpePtr a) : Ope(dom), n(n), a(std::move(a)) {}
-  Term action(EvalState& st) const override { return term_pow(a->action(st), n); }
+  Term action(EvalState& st, const Term* cv) const override { return term_pow(a->eval(st), n, cv); }
   int n;
   OpePtr a;
 };
@@ -293,20 +329,20 @@ class OpeUnary : public Ope {
  public:
   enum Kind { LAP, DN, DR, MULTR, DIVR, DIVSINT, MULTSINT, DIVCOST };
   OpeUnary(int dom, Kind k, int bound, OpePtr a) : Ope(dom), kind(k), bound(bound), a(std::move(a)) {}
-  Term action(EvalState& st) const override {
-    Term t = a->action(st);
+  Term action(EvalState& st, const Term* cv) const override {
+    Term t = a->eval(st);
     switch (kind) {
-      case LAP: return comp_by_comp(t, [](const DVal& v) { return laplacian(v); });
+      case LAP: return comp_by_comp(t, [](const DVal& v) { return laplacian(v); }, cv);
       case DN: {
         int b = bound;
-        return comp_by_comp(t, [b](const DVal& v) { return der_normal(v, b); });
+        return comp_by_comp(t, [b](const DVal& v) { return der_normal(v, b); }, cv);
       }
-      case DR: return comp_by_comp(t, [](const DVal& v) { return der_r(v); });
-      case MULTR: return comp_by_comp(t, [](const DVal& v) { return mult_r(v); });
-      case DIVR: return comp_by_comp(t, [](const DVal& v) { return div_r(v); });
-      case DIVSINT: return comp_by_comp(t, [](const DVal& v) { return div_sin_theta(v); });
-      case MULTSINT: return comp_by_comp(t, [](const DVal& v) { return mult_sin_theta(v); });
-      default: return comp_by_comp(t, [](const DVal& v) { return div_cos_theta(v); });
+      case DR: return comp_by_comp(t, [](const DVal& v) { return der_r(v); }, cv);
+      case MULTR: return comp_by_comp(t, [](const DVal& v) { return mult_r(v); }, cv);
+      case DIVR: return comp_by_comp(t, [](const DVal& v) { return div_r(v); }, cv);
+      case DIVSINT: return comp_by_comp(t, [](const DVal& v) { return div_sin_theta(v); }, cv);
+      case MULTSINT: return comp_by_comp(t, [](const DVal& v) { return mult_sin_theta(v); }, cv);
+      default: return comp_by_comp(t, [](const DVal& v) { return div_cos_theta(v); }, cv);
     }
   }
   Kind kind;
@@ -319,8 +355,8 @@ class OpeFunc : public Ope {
  public:
   enum Kind { EXP, SQRT, LOG };
   OpeFunc(int dom, Kind k, OpePtr a) : Ope(dom), kind(k), a(std::move(a)) {}
-  Term action(EvalState& st) const override {
-    Term t = a->action(st);
+  Term action(EvalState& st, const Term* cv) const override {
+    Term t = a->eval(st);
     if (t.is_double) {
       double v = kind == EXP ? std::exp(t.vd) : kind == SQRT ? std::sqrt(t.vd) : std::log(t.vd);
       Term r = Term::dbl(t.dom, v);
@@ -333,14 +369,17 @@ class OpeFunc : public Ope {
     if (t.vt.size() != 1) throw KdError(KD_ERR_UNSUPPORTED, "exp/sqrt/log only defined for a scalar");
     Term r = tensor_like(t);
     const DVal& v = t.vt[0];
-    if (kind == EXP) r.vt.push_back(vd_exp(v));
+    if (cv) r.vt = cv->vt;
+    else if (kind == EXP) r.vt.push_back(vd_exp(v));
     else if (kind == SQRT) r.vt.push_back(v.zero ? v : vd_sqrt(v));
     else r.vt.push_back(vd_log(v));
     if (t.has_dt) {
+      // der exp(u) = u' exp(u), der sqrt(u) = u' / 2 / sqrt(u): the result's
+      // value is exp(u) / sqrt(u) itself
       r.has_dt = true;
       const DVal& d = t.dt[0];
-      if (kind == EXP) r.dt.push_back(d * vd_exp(v));
-      else if (kind == SQRT) r.dt.push_back(d.zero ? d : d / 2. / vd_sqrt(v));
+      if (kind == EXP) r.dt.push_back(d * r.vt[0]);
+      else if (kind == SQRT) r.dt.push_back(d.zero ? d : d / 2. / r.vt[0]);
       else r.dt.push_back(d / v);
     }
     return r;
@@ -353,13 +392,15 @@ class OpeFunc : public Ope {
 class OpeGrad : public Ope {
  public:
   OpeGrad(int dom, OpePtr a) : Ope(dom), a(std::move(a)) {}
-  Term action(EvalState& st) const override {
-    Term t = a->action(st);
+  Term action(EvalState& st, const Term* cv) const override {
+    Term t = a->eval(st);
     if (t.is_double || t.vt.size() != 1) throw KdError(KD_ERR_UNSUPPORTED, "grad only defined for scalars");
     Term r;
     r.dom = t.dom;
     r.valence = 1;
-    for (int i = 1; i <= 3; i++) r.vt.push_back(t.vt[0].der_abs(i));
+    if (cv) r.vt = cv->vt;
+    else
+      for (int i = 1; i <= 3; i++) r.vt.push_back(t.vt[0].der_abs(i));
     if (t.has_dt) {
       r.has_dt = true;
       for (int i = 1; i <= 3; i++) r.dt.push_back(t.dt[0].der_abs(i));
@@ -373,16 +414,20 @@ class OpeGrad : public Ope {
 class OpeScal : public Ope {
  public:
   OpeScal(int dom, OpePtr a, OpePtr b) : Ope(dom), a(std::move(a)), b(std::move(b)) {}
-  Term action(EvalState& st) const override {
-    Term x = a->action(st);
-    Term y = b->action(st);
+  Term action(EvalState& st, const Term* cv) const override {
+    Term x = a->eval(st);
+    Term y = b->eval(st);
     if (x.vt.size() != 3 || y.vt.size() != 3) throw KdError(KD_ERR_UNSUPPORTED, "scal needs two vectors");
     Term r;
     r.dom = x.dom;
     r.valence = 0;
-    DVal v = x.vt[0] * y.vt[0];
-    for (int i = 1; i < 3; i++) v = v + x.vt[i] * y.vt[i];
-    r.vt.push_back(v);
+    if (cv) {
+      r.vt = cv->vt;
+    } else {
+      DVal v = x.vt[0] * y.vt[0];
+      for (int i = 1; i < 3; i++) v = v + x.vt[i] * y.vt[i];
+      r.vt.push_back(v);
+    }
     if (x.has_dt && y.has_dt) {
       r.has_dt = true;
       DVal d = x.dt[0] * y.vt[0] + x.vt[0] * y.dt[0];
@@ -398,9 +443,9 @@ class OpeScal : public Ope {
 class OpePartial : public Ope {
  public:
   OpePartial(int dom, int i, OpePtr a) : Ope(dom), i(i), a(std::move(a)) {}
-  Term action(EvalState& st) const override {
+  Term action(EvalState& st, const Term* cv) const override {
     int ii = i;
-    return comp_by_comp(a->action(st), [ii](const DVal& v) { return v.der_abs(ii); });
+    return comp_by_comp(a->eval(st), [ii](const DVal& v) { return v.der_abs(ii); }, cv);
   }
   int i;
   OpePtr a;
@@ -410,13 +455,14 @@ class OpeLeaf : public Ope {
  public:
   enum Kind { VAR, VAR_DOUBLE, CST, HARD, DEF };
   OpeLeaf(int dom, Kind k, int which, double v = 0.0) : Ope(dom), kind(k), which(which), val(v) {}
-  Term action(EvalState& st) const override;
+  Term action(EvalState& st, const Term* cv) const override;
+  bool cacheable() const override { return false; }
   Kind kind;
   int which;
   double val;
 };
 
-Term OpeLeaf::action(EvalState& st) const {
+Term OpeLeaf::action(EvalState& st, const Term*) const {
   switch (kind) {
     case VAR: return st.var_term(which, dom);
     case VAR_DOUBLE: return st.var_double_term(which, dom);

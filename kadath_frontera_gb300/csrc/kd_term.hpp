@@ -48,7 +48,14 @@ Term operator-(const Term& a, const Term& b);
 Term operator*(const Term& a, const Term& b);
 Term operator/(const Term& a, const Term& b);
 Term operator-(const Term& a);
-Term term_pow(const Term& a, int n);
+// The same operations with the result's value supplied (cv != nullptr): the
+// value is adopted and only the tangent is computed.
+Term t_add(const Term& a, const Term& b, const Term* cv);
+Term t_sub(const Term& a, const Term& b, const Term* cv);
+Term t_mul(const Term& a, const Term& b, const Term* cv);
+Term t_div(const Term& a, const Term& b, const Term* cv);
+Term t_neg(const Term& a, const Term* cv);
+Term term_pow(const Term& a, int n, const Term* cv = nullptr);
 
 class System;
 struct EvalState;
@@ -58,7 +65,15 @@ class Ope {
  public:
   explicit Ope(int dom) : dom(dom) {}
   virtual ~Ope() = default;
-  virtual Term action(EvalState& st) const = 0;
+  // Evaluates the node.  When the pass carries a value cache, a value pass
+  // records the node's value and a tangent pass reuses it: the value part of
+  // a Term does not depend on the Jacobian seeds, so it is computed once per
+  // iterate instead of once per seed block.
+  Term eval(EvalState& st) const;
+  // cv: this node's value, already known (tangent-only evaluation), or null.
+  virtual Term action(EvalState& st, const Term* cv) const = 0;
+  // Leaves are cheap (views of fields or doubles) and are not cached.
+  virtual bool cacheable() const { return true; }
   int dom;
 };
 using OpePtr = std::shared_ptr<Ope>;

@@ -151,3 +151,31 @@ def star(res=(13, 9, 4), bounds=STAR_BOUNDS, ctx=None) -> Workload:
 
 
 WORKLOADS = {"toy": toy, "star": star}
+
+
+def main(argv=None) -> int:
+    """Runs Newton steps of a workload from its initial guess: the command a
+    profiler wraps (`python -m kadath_frontera_gb300.workloads --steps 1`)."""
+    import argparse
+
+    from . import kadath as KD
+    ap = argparse.ArgumentParser(description=main.__doc__)
+    ap.add_argument("--workload", default="star", choices=sorted(WORKLOADS))
+    ap.add_argument("--mode", default="mixed", choices=["mixed", "fp64", "fp32"])
+    ap.add_argument("--warmup", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1)
+    ap.add_argument("--precision", type=float, default=1e-10)
+    args = ap.parse_args(argv)
+    mode = {"mixed": KD.KD_LU_TF32_IR, "fp64": KD.KD_LU_FP64, "fp32": KD.KD_LU_FP32_IR}[args.mode]
+    wl = WORKLOADS[args.workload]()
+    for i in range(args.warmup + args.steps):
+        wl.restore()
+        done, err = wl.syst.do_newton(args.precision, lu_mode=mode)
+        rep = wl.syst.last_report
+        print(f"step {i}: |F| = {err:.3e}, factor {rep['t_factor_ms']:.1f} ms, assembly {rep['t_assembly_ms']:.1f} ms",
+              flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
