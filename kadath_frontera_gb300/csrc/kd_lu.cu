@@ -176,13 +176,40 @@ __global__ void trsv_step(const T* __restrict__ A, long long ld, double* __restr
   }
 }
 
-// y = A x (FP64, column-major), one warp per 32-row stripe, FP64 accumulate.
-__global__ void gemv_fp64(const double* __restrict__ A, long long ld, int N, const double* __restrict__ x,
-                          double* __restrict__ y, double alpha, double beta, const double* __restrict__ b) {
-  int row = blockIdx.x * blockDim.x + threadIdx.x;
+// y = alpha A x + beta b (FP64, column-major).  The columns are split into
+// chunks so that the grid covers the GPU: gemv_partial writes one partial
+// sum per (chunk, row), gemv_finish adds them in chunk order (deterministic).
+constexpr int GEMV_ROWS = 256;
+__global__ void __launch_bounds__(GEMV_ROWS) gemv_partial(const double* __restrict__ A, long long ld, int N,
+                                                          const double* __restrict__ x, int chunk,
+                                                          double* __restrict__ part) {
+  const int row = blockIdx.x * GEMV_ROWS + threadIdx.x;
+  if (row >= N) return;
+  const int c0 = blockIdx.y * chunk;
+  const int c1 = (c0 + chunk < N) ? c0 + chunk : N;
+  const double* a = A + static_cast<long long>(c0) * ld + row;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  int k = c0;
+  for (; k + 3 < c1; k += 4) {
+    s0 = fma(a[0], x[k], s0);
+    s1 = fma(a[ld], x[k + 1], s1);
+    s2 = fma(a[2 * ld], x[k + 2], s2);
+    s3 = fma(a[3 * ld], x[k + 3], s3);
+    a += 4 * ld;
+  }
+  for (; k < c1; k++) {
+    s0 = fma(a[0], x[k], s0);
+    a += ld;
+  }
+  part[static_cast<size_t>(blockIdx.y) * N + row] = (s0 + s1) + (s2 + s3);
+}
+
+__global__ void gemv_finish(const double* __restrict__ part, int nchunk, int N, double alpha, double beta,
+                            const double* __restrict__ b, double* __restrict__ y) {
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
   if (row >= N) return;
   double s = 0.0;
-  for (int k = 0; k < N; k++) s = fma(A[static_cast<long long>(k) * ld + row], x[k], s);
+  for (int c = 0; c < nchunk; c++) s += part[static_cast<size_t>(c) * N + row];
   y[row] = alpha * s + (b ? beta * b[row] : 0.0);
 }
 
@@ -206,9 +233,11 @@ DenseLU::DenseLU(Context* ctx) : ctx_(ctx) {
   // then the row-move list of one panel
   const size_t slot_bytes = sizeof(double) * (2 * 128 * static_cast<size_t>(nsm_) + 2 * nsm_ + 2 * 128) +
                             sizeof(int) * 2 * static_cast<size_t>(nsm_) + 32;
-  cuda_check(cudaMalloc(&slot_mem_, slot_bytes + sizeof(int) * (1 + 4 * 128)), "cudaMalloc(panel slots)");
-  cuda_check(cudaMemset(slot_mem_, 0, slot_bytes), "memset panel slots");
+  const size_t map_bytes = sizeof(int) * (1 + 4 * 128) + 60;  // + padding to 16 bytes
+  cuda_check(cudaMalloc(&slot_mem_, slot_bytes + map_bytes + 16), "cudaMalloc(panel slots)");
+  cuda_check(cudaMemset(slot_mem_, 0, slot_bytes + map_bytes + 16), "memset panel slots");
   swap_map_ = reinterpret_cast<int*>(static_cast<char*>(slot_mem_) + slot_bytes);
+  tri_bar_ = reinterpret_cast<unsigned*>(static_cast<char*>(slot_mem_) + slot_bytes + map_bytes);
   panel_err_ = reinterpret_cast<int*>(static_cast<char*>(slot_mem_) + slot_bytes - 16);
 }
 
@@ -219,6 +248,7 @@ DenseLU::~DenseLU() {
   cudaFree(ipiv_);
   cudaFree(d_info_);
   cudaFree(slot_mem_);
+  cudaFree(part_);
   cudaFree(work_);
   cudaFree(work32_);
   cudaFree(dinv_l_);
@@ -454,6 +484,84 @@ __device__ void block_argmax(double& v, int& i, int& tag, double* rv, int* ri, i
   i = ri[0];
   tag = rt[0];
   __syncthreads();
+}
+
+// A whole triangular sweep with the factors in one cooperative launch: per
+// 64-row block k (in order for L, reversed for U), every CTA forms
+// x_k = Dinv_k b[block] (Dinv_k row-major; warp w owns rows 8w..8w+7, lanes
+// along the row, all loads issued before the reductions), CTA 0 stores x_k
+// in y, and the rows below (L) or above (U) get b[row] -= A(row, block) x_k;
+// then one grid barrier.  Rows go by 64-row tiles, tile t to CTA t % grid:
+// within a CTA, warp w takes rows 32 (w >> 2) .. + 31 of the tile and the
+// 16 block columns 16 (w & 3) .. + 15 (16 independent loads per thread), and
+// the four column quarters are added in shared memory.  A row of b is only
+// ever written by its tile's CTA; block rows written by other CTAs are read
+// past L1.
+constexpr int SW_TILE = 64;
+template <class T>
+__global__ void __launch_bounds__(256) trsv_sweep(const T* __restrict__ A, long long ld, int N, double* b,
+                                                  double* __restrict__ y, const double* __restrict__ Dinv,
+                                                  int lower, unsigned* bar, int* err) {
+  __shared__ double bb[TB];
+  __shared__ double xx[TB];
+  __shared__ double part[4][SW_TILE];
+  __shared__ int s_ok;
+  const int nblk = (N + TB - 1) / TB;
+  const int ntiles = (N + SW_TILE - 1) / SW_TILE;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int quarter = warp & 3, half = warp >> 2;
+  for (int step = 0; step < nblk; step++) {
+    const int k = lower ? step : nblk - 1 - step;
+    const int r0 = k * TB;
+    const int n = (N - r0 < TB) ? N - r0 : TB;
+    if (tid < TB) bb[tid] = (tid < n) ? __ldcg(b + r0 + tid) : 0.0;
+    __syncthreads();
+    {
+      const double* D = Dinv + static_cast<size_t>(k) * TB * TB + static_cast<size_t>(warp) * 8 * TB;
+      double lo[8], hi[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        lo[q] = D[q * TB + lane];
+        hi[q] = D[q * TB + lane + 32];
+      }
+      const double b0 = bb[lane], b1 = bb[lane + 32];
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        double p = lo[q] * b0 + hi[q] * b1;
+        for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
+        if (lane == 0) xx[warp * 8 + q] = p;
+      }
+    }
+    __syncthreads();
+    if (blockIdx.x == 0 && tid < n) y[r0 + tid] = xx[tid];
+    const int q0 = lower ? r0 + n : 0;
+    const int q1 = lower ? N : r0;
+    const int t0 = q0 / SW_TILE, t1 = (q1 + SW_TILE - 1) / SW_TILE;
+    int first = t0 - (t0 % static_cast<int>(gridDim.x)) + static_cast<int>(blockIdx.x);
+    if (first < t0) first += gridDim.x;
+    for (int t = first; t < t1 && t < ntiles; t += gridDim.x) {
+      const int row = t * SW_TILE + half * 32 + lane;
+      const int c0 = quarter * 16;
+      double acc = 0.0;
+      if (row >= q0 && row < q1) {
+        const T* a = A + static_cast<long long>(r0 + c0) * ld + row;
+        T v[16];
+#pragma unroll
+        for (int j = 0; j < 16; j++) v[j] = (c0 + j < n) ? a[static_cast<long long>(j) * ld] : T(0);
+#pragma unroll
+        for (int j = 0; j < 16; j++) acc = fma(static_cast<double>(v[j]), xx[c0 + j], acc);
+      }
+      part[quarter][half * 32 + lane] = acc;
+      __syncthreads();
+      if (tid < SW_TILE) {
+        const int r = t * SW_TILE + tid;
+        if (r >= q0 && r < q1)
+          b[r] = __ldcg(b + r) - ((part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]));
+      }
+      __syncthreads();
+    }
+    if (!grid_barrier(bar, gridDim.x * static_cast<unsigned>(step + 1), err, &s_ok)) return;
+  }
 }
 
 template <class T>
@@ -833,18 +941,28 @@ void DenseLU::tri_solve(const T* LU, long long ld, int N, double* b, int trans) 
   const size_t bs = static_cast<size_t>(TB) * TB;
   if (!trans) {
     gather_perm<<<blocks(N, 256), 256, 0, s>>>(b, perm_, N, w1);
-    for (int k = 0; k < nblk; k++) {
-      int r0 = k * TB, n = (N - r0 < TB) ? N - r0 : TB;
-      int q0 = r0 + n, q1 = N;
-      int g = q1 > q0 ? blocks(q1 - q0, 256) : 1;
-      trsv_step<T><<<g, 256, 0, s>>>(LU, ld, w1, w2, r0, n, dinv_l_ + k * bs, 0, q0, q1, 0);
-    }
-    for (int k = nblk - 1; k >= 0; k--) {
-      int r0 = k * TB, n = (N - r0 < TB) ? N - r0 : TB;
-      int q0 = 0, q1 = r0;
-      int g = q1 > q0 ? blocks(q1 - q0, 256) : 1;
-      trsv_step<T><<<g, 256, 0, s>>>(LU, ld, w2, b, r0, n, dinv_u_ + k * bs, 0, q0, q1, 0);
-    }
+    // L y = P b, then U x = y: one cooperative launch per sweep
+    int g = blocks(N, SW_TILE);
+    if (g > nsm_) g = nsm_;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(g, 1, 1);
+    cfg.blockDim = dim3(256, 1, 1);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cuda_check(cudaMemsetAsync(tri_bar_, 0, 2 * sizeof(unsigned), s), "memset sweep barriers");
+    cuda_check(cudaLaunchKernelEx(&cfg, trsv_sweep<T>, LU, ld, N, w1, w2, static_cast<const double*>(dinv_l_), 1,
+                                  tri_bar_, panel_err_),
+               "forward sweep");
+    cuda_check(cudaLaunchKernelEx(&cfg, trsv_sweep<T>, LU, ld, N, w2, b, static_cast<const double*>(dinv_u_), 0,
+                                  tri_bar_ + 1, panel_err_),
+               "backward sweep");
+    ctx_->launches += 3;
+    cuda_check(cudaGetLastError(), "triangular solve");
+    return;
   } else {
     // A^T = U^T L^T P: U^T y = b (forward, lower), L^T z = y (backward), x = P^T z
     for (int k = 0; k < nblk; k++) {
@@ -908,6 +1026,26 @@ void DenseLU::prepare_solves(const T* LU, long long ld, int N) {
 // Right-preconditioned GMRES(m) in FP64 with the FP32 LU as preconditioner:
 // solves A x = b to a relative residual below gmres_tol.  Small dense
 // Hessenberg algebra runs on the host (m <= 50), vectors stay on the device.
+void DenseLU::gemv(const double* x, double* y, double alpha, double beta, const double* b) {
+  const int N = N_;
+  cudaStream_t s = ctx_->stream();
+  const int rb = blocks(N, GEMV_ROWS);
+  int nchunk = (4 * nsm_ + rb - 1) / rb;
+  if (nchunk > 32) nchunk = 32;
+  if (nchunk < 1) nchunk = 1;
+  const int chunk = (N + nchunk - 1) / nchunk;
+  nchunk = (N + chunk - 1) / chunk;
+  const size_t need = static_cast<size_t>(32) * N;
+  if (need > part_cap_) {
+    cudaFree(part_);
+    cuda_check(cudaMalloc(&part_, need * sizeof(double)), "cudaMalloc(gemv partials)");
+    part_cap_ = need;
+  }
+  gemv_partial<<<dim3(rb, nchunk), GEMV_ROWS, 0, s>>>(A_, ld_, N, x, chunk, part_);
+  gemv_finish<<<blocks(N, 256), 256, 0, s>>>(part_, nchunk, N, alpha, beta, b, y);
+  ctx_->launches += 2;
+}
+
 void DenseLU::gmres_ir(double* b) {
   const int N = N_;
   const int m = gmres_max_iter;
@@ -935,9 +1073,8 @@ void DenseLU::gmres_ir(double* b) {
     // r = b - A x
     {
       ProfScope ps(ctx_, Context::PROF_GMRES, 8.0 * double(N) * N);
-      gemv_fp64<<<blocks(N, 128), 128, 0, s>>>(A_, ld_, N, x, r, -1.0, 1.0, b);
+      gemv(x, r, -1.0, 1.0, b);
     }
-    ctx_->launches++;
     double beta = nrm(r);
     stats.final_rel_residual = beta / bnorm;
     if (beta / bnorm < gmres_tol) break;
@@ -953,9 +1090,8 @@ void DenseLU::gmres_ir(double* b) {
       solve_f32(r);
       {
         ProfScope ps(ctx_, Context::PROF_GMRES, 8.0 * double(N) * N);
-        gemv_fp64<<<blocks(N, 128), 128, 0, s>>>(A_, ld_, N, r, w, 1.0, 0.0, nullptr);
+        gemv(r, w, 1.0, 0.0, nullptr);
       }
-      ctx_->launches++;
       for (int i = 0; i <= k; i++) {  // modified Gram-Schmidt
         double h = dot(w, V + static_cast<size_t>(i) * N);
         H[i * m + k] = h;
@@ -1003,9 +1139,8 @@ void DenseLU::gmres_ir(double* b) {
   }
   {
     ProfScope ps(ctx_, Context::PROF_GMRES, 8.0 * double(N) * N);
-    gemv_fp64<<<blocks(N, 128), 128, 0, s>>>(A_, ld_, N, x, r, -1.0, 1.0, b);
+    gemv(x, r, -1.0, 1.0, b);
   }
-  ctx_->launches++;
   stats.final_rel_residual = nrm(r) / bnorm;
   stats.refine_iters = total_it;
   cublasDcopy(blas_, N, x, 1, b, 1);
@@ -1023,6 +1158,12 @@ void DenseLU::solve(double* b, int trans) {
                                        std::to_string(stats.final_rel_residual) + ")");
   }
   cuda_check(cudaStreamSynchronize(ctx_->stream()), "sync after solve");
+  int perr = 0;
+  cuda_check(cudaMemcpy(&perr, panel_err_, sizeof(int), cudaMemcpyDeviceToHost), "D2H sweep flag");
+  if (perr) {
+    cuda_check(cudaMemset(panel_err_, 0, sizeof(int)), "reset sweep flag");
+    throw KdError(KD_ERR_TIMEOUT, "triangular solve: a grid barrier wait ran out");
+  }
   stats.t_solve_ms = now_ms() - t0;
 }
 

@@ -58,7 +58,11 @@ class DenseLU {
   int nsm_ = 0;                // SM count (grid of the panel kernel)
   void* slot_mem_ = nullptr;   // panel exchange slots, barrier, row-move list
   int* swap_map_ = nullptr;
-  int* panel_err_ = nullptr;
+  int* panel_err_ = nullptr;   // set when a grid barrier wait runs out (panel or sweep)
+  unsigned* tri_bar_ = nullptr;  // barrier counters of the two triangular sweeps
+  double* part_ = nullptr;     // split-K partial sums of the FP64 matvec
+  size_t part_cap_ = 0;
+  void gemv(const double* x, double* y, double alpha, double beta, const double* b);
   double* work_ = nullptr;     // solver workspace
   size_t work_cap_ = 0;
   float* work32_ = nullptr;
