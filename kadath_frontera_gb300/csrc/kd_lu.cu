@@ -14,6 +14,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "kd_gemm_tc.hpp"
@@ -57,6 +58,40 @@ __global__ void trsm_unit_lower(T* __restrict__ A, long long ld, int j0, int nbk
     int col = cbase + cc;
     if (col < c1) A[static_cast<long long>(col) * ld + j0 + i] = static_cast<T>(X[i * TRSM_COLS + cc]);
   }
+}
+
+// FP32 version for the mixed modes, one thread per column with the column
+// (x, NB values) in registers: L11 (jb x jb, zero-padded to NB) sits
+// row-major in shared memory and every thread reads the same L entry at the
+// same time (broadcast).  Rows past jb hold zeros and stay zero.
+constexpr int TRSM32_NB = 96;
+constexpr int TRSM32_THREADS = 128;
+__global__ void __launch_bounds__(TRSM32_THREADS) trsm_unit_lower_f32(float* __restrict__ A, long long ld, int j0,
+                                                                      int jb, int c0, int c1) {
+  __shared__ __align__(16) float L[TRSM32_NB * TRSM32_NB];
+  for (int e = threadIdx.x; e < TRSM32_NB * TRSM32_NB; e += blockDim.x) {
+    const int i = e % TRSM32_NB, k = e / TRSM32_NB;  // column-major walk: coalesced reads of L11
+    L[i * TRSM32_NB + k] = (i < jb && k < jb && k < i) ? A[static_cast<long long>(j0 + k) * ld + j0 + i] : 0.0f;
+  }
+  __syncthreads();
+  const int col = c0 + blockIdx.x * TRSM32_THREADS + threadIdx.x;
+  if (col >= c1) return;
+  float* xc = A + static_cast<long long>(col) * ld + j0;
+  float x[TRSM32_NB];
+#pragma unroll
+  for (int i = 0; i < TRSM32_NB; i++) x[i] = (i < jb) ? xc[i] : 0.0f;
+  // forward substitution, column by column (right-looking): every index
+  // into x is a compile-time constant, so x stays in registers
+#pragma unroll
+  for (int k = 0; k < TRSM32_NB - 1; k++) {
+    const float xk = x[k];
+#pragma unroll
+    for (int i = 0; i < TRSM32_NB; i++)
+      if (i > k) x[i] = fmaf(-L[i * TRSM32_NB + k], xk, x[i]);
+  }
+#pragma unroll
+  for (int i = 0; i < TRSM32_NB; i++)
+    if (i < jb) xc[i] = x[i];
 }
 
 __global__ void d2s(const double* __restrict__ A, long long lda, float* __restrict__ B, long long ldb, int N) {
@@ -648,11 +683,18 @@ __global__ void __launch_bounds__(GP_THREADS) panel_grid_kernel(T* __restrict__ 
       const T inv = static_cast<T>(1.0 / piv);
       for (int i = rs + tid; i < r1; i += bd) tile[jj * per + i - r0] *= inv;
       __syncthreads();
-      const int nrr = r1 - rs, ncols = jb - jj - 1;
-      for (int e = tid; e < ncols * nrr; e += bd) {
-        int k = jj + 1 + e / nrr;
-        int i = rs - r0 + e % nrr;
-        tile[k * per + i] = fma(-tile[jj * per + i], static_cast<T>(prow[k]), tile[k * per + i]);
+      // thread -> (row, column phase): rows along the low 7 bits (conflict-free
+      // shared memory), columns strided by the number of phases
+      const int nrr = r1 - rs;
+      const int nph = bd >> 7, ph = tid >> 7;
+      for (int i0 = 0; i0 < nrr; i0 += 128) {
+        const int ii = i0 + (tid & 127);
+        if (ii < nrr) {
+          const int li = rs - r0 + ii;
+          const T l = tile[jj * per + li];
+          for (int k = jj + 1 + ph; k < jb; k += nph)
+            tile[k * per + li] = fma(-l, static_cast<T>(prow[k]), tile[k * per + li]);
+        }
       }
     }
     __syncthreads();
@@ -668,9 +710,10 @@ __global__ void __launch_bounds__(GP_THREADS) panel_grid_kernel(T* __restrict__ 
 // j0 .. j0+jb-1 first, then the pivot rows below the panel.  One warp.
 __global__ void build_swap_map(const int* __restrict__ ipiv, int j0, int jb, int* __restrict__ map) {
   // map[0] = count, map[1 .. 1+2jb) = dst, map[1+2jb .. 1+4jb) = src
-  __shared__ int rows[256], content[256];
+  __shared__ int rows[256], content[256], piv[128];
   __shared__ int cnt;
   const int lane = threadIdx.x;
+  for (int t = lane; t < jb; t += 32) piv[t] = ipiv[j0 + t];
   for (int t = lane; t < jb; t += 32) {
     rows[t] = j0 + t;
     content[t] = j0 + t;
@@ -678,7 +721,7 @@ __global__ void build_swap_map(const int* __restrict__ ipiv, int j0, int jb, int
   if (lane == 0) cnt = jb;
   __syncwarp();
   for (int jj = 0; jj < jb; jj++) {
-    const int p = ipiv[j0 + jj];
+    const int p = piv[jj];
     int idx;
     if (p < j0 + jb) {
       idx = p - j0;
@@ -836,6 +879,14 @@ static void trsm_and_swaps(Context* ctx, T* A, long long ld, int N, int j0, int 
       cudaFuncSetAttribute(trsm_unit_lower<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
       attr_set = true;
     }
+    if constexpr (std::is_same<T, float>::value) {
+      if (jb <= TRSM32_NB) {
+        trsm_unit_lower_f32<<<blocks(N - j0 - jb, TRSM32_THREADS), TRSM32_THREADS, 0, s>>>(A, ld, j0, jb, j0 + jb, N);
+        ctx->launches += 1;
+        cuda_check(cudaGetLastError(), "trsm kernel");
+        return;
+      }
+    }
     trsm_unit_lower<T><<<blocks(N - j0 - jb, TRSM_COLS), TRSM_COLS, smem, s>>>(A, ld, j0, jb, j0 + jb, N);
     ctx->launches += 1;
   }
@@ -902,16 +953,17 @@ void DenseLU::factor(double* A, long long ld, int N, int mode) {
     factor_fp64(A, ld, N);
     prepare_solves<double>(A, ld, N);
   } else {
-    size_t need = static_cast<size_t>(N) * N;
+    ld32_ = ((static_cast<long long>(N) + 31) / 32) * 32;  // 128-byte aligned columns
+    const size_t need = static_cast<size_t>(ld32_) * N;
     if (need > a32_cap_) {
       cudaFree(A32_);
       cuda_check(cudaMalloc(&A32_, need * sizeof(float)), "cudaMalloc(A32)");
       a32_cap_ = need;
     }
-    d2s<<<152 * 8, 256, 0, ctx_->stream()>>>(A, ld, A32_, N, N);
+    d2s<<<152 * 8, 256, 0, ctx_->stream()>>>(A, ld, A32_, ld32_, N);
     ctx_->launches++;
-    factor_f32(A32_, N, N, mode == LU_TF32_IR);
-    prepare_solves<float>(A32_, N, N);
+    factor_f32(A32_, ld32_, N, mode == LU_TF32_IR);
+    prepare_solves<float>(A32_, ld32_, N);
   }
   int info = 0;
   cuda_check(cudaMemcpyAsync(&info, d_info_, sizeof(int), cudaMemcpyDeviceToHost, ctx_->stream()), "D2H info");
@@ -987,7 +1039,7 @@ void DenseLU::solve_fp64(const double* LU, long long ld, int N, double* b, int t
   tri_solve<double>(LU, ld, N, b, trans);
 }
 
-void DenseLU::solve_f32(double* b) { tri_solve<float>(A32_, N_, N_, b, 0); }
+void DenseLU::solve_f32(double* b) { tri_solve<float>(A32_, ld32_, N_, b, 0); }
 
 // After factorisation: pivots as one permutation, inverses of the 64 x 64
 // diagonal blocks of L (unit lower) and U.

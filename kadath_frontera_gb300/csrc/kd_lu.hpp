@@ -50,7 +50,8 @@ class DenseLU {
   int mode_ = 0, N_ = 0;
   long long ld_ = 0;
   double* A_ = nullptr;        // FP64 matrix (factors in FP64 mode, operator in mixed modes)
-  float* A32_ = nullptr;       // FP32 factors (mixed modes)
+  float* A32_ = nullptr;       // FP32 factors (mixed modes), leading dimension ld32_
+  long long ld32_ = 0;
   size_t a32_cap_ = 0;
   int* ipiv_ = nullptr;        // device pivots
   size_t ipiv_cap_ = 0;
