@@ -608,7 +608,7 @@ int kd_tf32_gemm_update(kd_ctx* ctx, int m, int n, int k, const float* A, long l
     if (m < 0 || n < 0 || k < 1 || k > 128) throw kd::KdError(KD_ERR_ARG, "need m, n >= 0 and 1 <= k <= 128");
     if ((m > 0 && lda < m) || ldb < k || (m > 0 && ldc < m)) throw kd::KdError(KD_ERR_ARG, "leading dimension too small");
     if (!A || !B || !C) throw kd::KdError(KD_ERR_ARG, "null matrix");
-    kd::tf32_gemm_update(ctx->c.get(), m, n, k, A, lda, B, ldb, C, ldc);
+    kd::tf32_gemm_update(ctx->c.get(), m, n, k, A, lda, B, ldb, C, ldc, m);
     if (kd::tf32_gemm_error_flag(ctx->c.get()))
       throw kd::KdError(KD_ERR_TIMEOUT, "tensor-core update timed out waiting for its MMAs");
   });

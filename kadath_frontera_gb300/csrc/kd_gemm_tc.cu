@@ -17,9 +17,12 @@
 // K of one panel is at most 128, so the whole K extent of a tile fits in
 // shared memory and needs no pipelining; the update is bound by the HBM
 // traffic of C.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <mutex>
+#include <string>
 
 #include "kd_gemm_tc.hpp"
 
@@ -76,7 +79,10 @@ __global__ void pack_kmajor(const float* __restrict__ src, long long ld, int row
     }
     float v = 0.0f;
     if (r < rows && kk < k) v = col_major ? src[static_cast<long long>(kk) * ld + r] : src[static_cast<long long>(r) * ld + kk];
-    out[static_cast<long long>(r) * kpad + kk] = v;
+    // round to the nearest TF32 value (the tensor cores would truncate)
+    uint32_t rounded;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(rounded) : "f"(v));
+    out[static_cast<long long>(r) * kpad + kk] = __uint_as_float(rounded);
   }
 }
 
@@ -199,6 +205,267 @@ __global__ void __launch_bounds__(TC_THREADS) tf32_update_kernel(const float* __
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS));
 }
 
+// ---------------------------------------------------------------------------
+// Persistent, warp-specialised version (used when C allows TMA: 16-byte
+// aligned base, ldc a multiple of 4 floats).  One CTA per SM walks the
+// 128 x 128 tiles of C (tile t -> CTA t % grid):
+//   warp 0  producer: TMA loads of the tile's operand blocks (128-byte
+//           swizzled, K-major) and of C in 128 x 32 chunks through a ring of
+//           four shared-memory slots;
+//   warp 1  allocates 256 TMEM columns (two 128-column accumulators) and
+//           issues the MMAs of a tile into one accumulator while the
+//           epilogue drains the other;
+//   warps 2-5 epilogue: per C chunk, tcgen05.ld of 32 accumulator columns,
+//           C -= acc in shared memory, TMA store of the chunk.
+// Every mbarrier wait gives up after GP_TC_WAIT_NS; the CTA then sets the
+// error flag, lets its roles fall out of their loops and frees its TMEM.
+constexpr int P_THREADS = 192;
+constexpr int P_CSLOTS = 4;
+constexpr int P_CCOLS = 32;                              // columns per C chunk
+constexpr int P_CHUNK_BYTES = TC_M * P_CCOLS * 4;        // 16 KiB
+constexpr int P_OPBLK_BYTES = 128 * 128;                 // 128 rows x 32 TF32
+constexpr unsigned long long P_WAIT_NS = 2000000000ull;  // 2 s
+
+__device__ __forceinline__ unsigned long long p_now() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait for phase `parity` of an mbarrier; false when it ran out.
+__device__ __forceinline__ bool p_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t a = smem_u32(bar);
+  uint32_t done = 0;
+  unsigned long long t0 = 0;
+  for (int spin = 0;; spin++) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (spin == 0) t0 = p_now();
+    else if ((spin & 255) == 0 && p_now() - t0 > P_WAIT_NS) return false;
+  }
+}
+
+__device__ __forceinline__ void p_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void p_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void p_tma_load(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void p_tma_store(const CUtensorMap* map, const void* src, int x, int y) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(smem_u32(src)), "r"(x), "r"(y)
+               : "memory");
+}
+
+__global__ void __launch_bounds__(P_THREADS, 1)
+    tf32_update_persistent(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                           const __grid_constant__ CUtensorMap mapC, int nkb, int ntm, int ntiles,
+                           int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char p_raw[];
+  char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(p_raw) + 1023) & ~uintptr_t(1023));
+  char* sA = base;
+  char* sB = sA + nkb * P_OPBLK_BYTES;
+  char* sC = sB + nkb * P_OPBLK_BYTES;
+  __shared__ uint64_t op_full, op_empty, acc_full[2], acc_empty[2], c_full[P_CSLOTS], c_empty[P_CSLOTS];
+  __shared__ uint32_t tmem_base_sh;
+  __shared__ int abort_flag, epi_abort;
+  volatile int* abort_v = &abort_flag;  // written by one role, polled by the others
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    abort_flag = 0;
+    epi_abort = 0;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&op_full)));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&op_empty)));
+    for (int i = 0; i < 2; i++) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&acc_full[i])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&acc_empty[i])));
+    }
+    for (int i = 0; i < P_CSLOTS; i++) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&c_full[i])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&c_empty[i])));
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapA)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapB)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapC)) : "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_sh)),
+                 "r"(256));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base_sh;
+
+  if (warp == 0) {
+    if (lane == 0) {  // ------------------------------------------- producer
+      int it = 0, cchunk = 0;
+      for (int tile = blockIdx.x; tile < ntiles && !*abort_v; tile += gridDim.x, it++) {
+        const int tm = tile % ntm, tn = tile / ntm;
+        if (it > 0 && !p_wait(&op_empty, (it - 1) & 1)) {
+          *abort_v = 1;
+          break;
+        }
+        p_expect_tx(&op_full, 2u * nkb * P_OPBLK_BYTES);
+        for (int kb = 0; kb < nkb; kb++) {
+          p_tma_load(sA + kb * P_OPBLK_BYTES, &mapA, kb * TC_KBLK, tm * TC_M, &op_full);
+          p_tma_load(sB + kb * P_OPBLK_BYTES, &mapB, kb * TC_KBLK, tn * TC_N, &op_full);
+        }
+        for (int ch = 0; ch < TC_N / P_CCOLS; ch++, cchunk++) {
+          const int slot = cchunk % P_CSLOTS, use = cchunk / P_CSLOTS;
+          if (use > 0 && !p_wait(&c_empty[slot], (use - 1) & 1)) {
+            *abort_v = 1;
+            break;
+          }
+          p_expect_tx(&c_full[slot], P_CHUNK_BYTES);
+          p_tma_load(sC + slot * P_CHUNK_BYTES, &mapC, tm * TC_M, tn * TC_N + ch * P_CCOLS, &c_full[slot]);
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {  // ------------------------------------------- MMA issuer
+      const uint32_t idesc = tf32_idesc(TC_M, TC_N);
+      const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+      int it = 0;
+      for (int tile = blockIdx.x; tile < ntiles && !*abort_v; tile += gridDim.x, it++) {
+        const int acc = it & 1, use = it >> 1;
+        if (use > 0 && !p_wait(&acc_empty[acc], (use - 1) & 1)) {
+          *abort_v = 1;
+          break;
+        }
+        if (!p_wait(&op_full, it & 1)) {
+          *abort_v = 1;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t d = tmem + static_cast<uint32_t>(acc * TC_N);
+        for (int kb = 0; kb < nkb; kb++) {
+          for (int k = 0; k < TC_KBLK / 8; k++) {
+            uint64_t ad = sw128_desc(a0 + kb * P_OPBLK_BYTES) + static_cast<uint64_t>((k * 32) >> 4);
+            uint64_t bd = sw128_desc(b0 + kb * P_OPBLK_BYTES) + static_cast<uint64_t>((k * 32) >> 4);
+            uint32_t accum = (kb | k) ? 1u : 0u;
+            asm volatile(
+                "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
+                "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
+          }
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                         smem_u32(&op_empty))
+                     : "memory");
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                         smem_u32(&acc_full[acc]))
+                     : "memory");
+      }
+    }
+  } else {  // -------------------------------------------------------- epilogue
+    const int et = threadIdx.x - 64;      // 0..127
+    const int quarter = warp & 3;         // TMEM lanes this warp may read
+    const int row = quarter * 32 + lane;  // tile row
+    int it = 0, cchunk = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, it++) {
+      const int tm = tile % ntm, tn = tile / ntm;
+      const int acc = it & 1;
+      if (et == 0 && (*abort_v || !p_wait(&acc_full[acc], (it >> 1) & 1))) epi_abort = 1;
+      asm volatile("bar.sync 1, 128;" ::: "memory");
+      if (epi_abort) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      for (int ch = 0; ch < TC_N / P_CCOLS; ch++, cchunk++) {
+        const int slot = cchunk % P_CSLOTS;
+        if (et == 0 && !p_wait(&c_full[slot], (cchunk / P_CSLOTS) & 1)) epi_abort = 1;
+        asm volatile("bar.sync 1, 128;" ::: "memory");
+        if (epi_abort) break;
+        float* cs = reinterpret_cast<float*>(sC + slot * P_CHUNK_BYTES);  // [column][row]
+        for (int c16 = 0; c16 < P_CCOLS; c16 += 16) {
+          uint32_t r[16];
+          const uint32_t taddr = tmem + (static_cast<uint32_t>(quarter * 32) << 16) +
+                                 static_cast<uint32_t>(acc * TC_N + ch * P_CCOLS + c16);
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+              "[%16];"
+              : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+              : "r"(taddr));
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int q = 0; q < 16; q++) cs[(c16 + q) * TC_M + row] -= __uint_as_float(r[q]);
+        }
+        // generic-proxy writes -> visible to the TMA store
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        asm volatile("bar.sync 1, 128;" ::: "memory");
+        if (et == 0) {
+          p_tma_store(&mapC, cs, tm * TC_M, tn * TC_N + ch * P_CCOLS);
+          asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+          asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+          p_arrive(&c_empty[slot]);
+          if (ch == TC_N / P_CCOLS - 1) p_arrive(&acc_empty[acc]);  // all 128 threads are past their loads
+        }
+      }
+      if (epi_abort) break;
+    }
+    if (et == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && (*abort_v || epi_abort)) atomicExch(err, 1);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256));
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no
+// link-time dependency on the driver library).
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
+// 2-D FP32 tensor map: inner extent `inner` (contiguous), `outer` rows
+// `stride_bytes` apart, box box0 x box1.
+void make_map(CUtensorMap* m, const void* ptr, long long inner, long long outer, long long stride_bytes, int box0,
+              int box1, bool swizzle128) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) throw KdError(KD_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+  cuuint64_t dims[2] = {static_cast<cuuint64_t>(inner), static_cast<cuuint64_t>(outer)};
+  cuuint64_t strides[1] = {static_cast<cuuint64_t>(stride_bytes)};
+  cuuint32_t box[2] = {static_cast<cuuint32_t>(box0), static_cast<cuuint32_t>(box1)};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(ptr), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw KdError(KD_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string(r) + ")");
+}
+
 struct TcWork {
   float* at = nullptr;
   float* bt = nullptr;
@@ -218,7 +485,7 @@ int grid_for(long long n) {
 bool tf32_gemm_supported(int k) { return k > 0 && k <= TC_MAXK; }
 
 void tf32_gemm_update(Context* ctx, int m, int n, int k, const float* A, long long lda, const float* B, long long ldb,
-                      float* C, long long ldc) {
+                      float* C, long long ldc, int c_rows_writable) {
   if (m <= 0 || n <= 0 || k <= 0) return;
   if (k > TC_MAXK) throw KdError(KD_ERR_ARG, "tcgen05 trailing update: panel width above 128");
   cudaStream_t s = ctx->stream();
@@ -245,6 +512,35 @@ void tf32_gemm_update(Context* ctx, int m, int n, int k, const float* A, long lo
   pack_kmajor<<<grid_for(need_a), 256, 0, s>>>(A, lda, m, k, 1, g_tc.at, mpad, kpad);
   pack_kmajor<<<grid_for(need_b), 256, 0, s>>>(B, ldb, n, k, 0, g_tc.bt, npad, kpad);
   const int nkb = kpad / TC_KBLK;
+  // TMA clips the stored rows at 16-byte granularity: rows up to m rounded
+  // to 4 may be written (with their unchanged values or zeros), so the
+  // persistent path needs them to be scratch (c_rows_writable).
+  const int m4 = (m + 3) / 4 * 4;
+  if (reinterpret_cast<uintptr_t>(C) % 16 == 0 && ldc % 4 == 0 && m4 <= c_rows_writable && encode_fn()) {
+    // persistent TMA pipeline
+    CUtensorMap mA, mB, mC;
+    make_map(&mA, g_tc.at, kpad, mpad, static_cast<long long>(kpad) * 4, TC_KBLK, TC_M, true);
+    make_map(&mB, g_tc.bt, kpad, npad, static_cast<long long>(kpad) * 4, TC_KBLK, TC_N, true);
+    make_map(&mC, C, m, n, ldc * 4, TC_M, P_CCOLS, false);
+    static int nsm = 0;
+    static bool pattr = false;
+    if (!pattr) {
+      int dev = 0;
+      cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+      cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "SM count");
+      cuda_check(cudaFuncSetAttribute(tf32_update_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      1024 + 2 * (TC_MAXK / TC_KBLK) * P_OPBLK_BYTES + P_CSLOTS * P_CHUNK_BYTES),
+                 "cudaFuncSetAttribute(tf32 persistent)");
+      pattr = true;
+    }
+    const int ntm = mpad / TC_M, ntiles = ntm * (npad / TC_N);
+    const int grid = ntiles < nsm ? ntiles : nsm;
+    const size_t psmem = 1024 + static_cast<size_t>(2 * nkb) * P_OPBLK_BYTES + P_CSLOTS * P_CHUNK_BYTES;
+    tf32_update_persistent<<<grid, P_THREADS, psmem, s>>>(mA, mB, mC, nkb, ntm, ntiles, g_tc.err);
+    ctx->launches += 3;
+    cuda_check(cudaGetLastError(), "tcgen05 trailing update (persistent)");
+    return;
+  }
   // Each CTA holds 128 TMEM columns of the SM's 512: asking for at least
   // 56 KiB of shared memory keeps at most four CTAs on one SM, so an
   // allocation never has to wait for another CTA to finish.
@@ -273,10 +569,10 @@ int tf32_gemm_error_flag(Context* ctx) {
 }
 
 void gemm_update_f32(Context* ctx, cublasHandle_t blas, int m, int n, int k, const float* A, long long lda,
-                     const float* B, long long ldb, float* C, long long ldc, bool tf32) {
+                     const float* B, long long ldb, float* C, long long ldc, bool tf32, int c_rows_writable) {
   ProfScope ps(ctx, Context::PROF_LU_GEMM, 2.0 * m * n * k);
   if (tf32 && tf32_gemm_supported(k)) {
-    tf32_gemm_update(ctx, m, n, k, A, lda, B, ldb, C, ldc);
+    tf32_gemm_update(ctx, m, n, k, A, lda, B, ldb, C, ldc, c_rows_writable);
     return;
   }
   // plain FP32 product (the FP32-IR mode): library SGEMM

@@ -930,7 +930,8 @@ void DenseLU::factor_f32(float* A, long long ld, int N, bool tf32) {
       float* A21 = A + static_cast<long long>(j0) * ld + j0 + jb;
       float* A12 = A + static_cast<long long>(j0 + jb) * ld + j0;
       float* A22 = A + static_cast<long long>(j0 + jb) * ld + j0 + jb;
-      gemm_update_f32(ctx_, blas_, m, m, jb, A21, ld, A12, ld, A22, ld, tf32);
+      // rows N .. ld of the working matrix are padding
+      gemm_update_f32(ctx_, blas_, m, m, jb, A21, ld, A12, ld, A22, ld, tf32, static_cast<int>(ld - j0 - jb));
     }
   }
 }

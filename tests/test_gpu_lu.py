@@ -67,17 +67,23 @@ def test_singular_matrix_reports_status(ctx):
     assert e.value.status == 3  # KD_ERR_SINGULAR
 
 
-@pytest.mark.parametrize("m,n,k", [(128, 128, 32), (256, 384, 96), (200, 130, 96), (1000, 777, 64), (33, 257, 17)])
-def test_tcgen05_tf32_update_matches_fp64_product(ctx, m, n, k):
+@pytest.mark.parametrize("aligned", [False, True])
+@pytest.mark.parametrize("m,n,k", [(128, 128, 32), (256, 384, 96), (200, 130, 96), (1000, 777, 64), (33, 257, 17),
+                                   (2000, 1500, 128)])
+def test_tcgen05_tf32_update_matches_fp64_product(ctx, m, n, k, aligned):
     """C -= A B on the tcgen05 tensor cores (TF32 inputs, FP32 accumulation)
-    against the FP64 product; tolerance from the TF32 unit roundoff 2^-11."""
+    against the FP64 product; tolerance from the TF32 unit roundoff 2^-11.
+    aligned: ldc a multiple of 4 floats, which selects the persistent TMA
+    pipeline (edge tiles exercise its clipped stores); otherwise the
+    one-tile-per-CTA kernel."""
     import ctypes as C
     lib = ctx.lib
     lib.kd_tf32_gemm_update.restype = C.c_int
     lib.kd_tf32_gemm_update.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_longlong, C.c_void_p,
                                         C.c_longlong, C.c_void_p, C.c_longlong]
     rng = np.random.default_rng(m * 7 + n + k)
-    lda, ldb, ldc = m + 3, k + 1, m + 5
+    lda, ldb = m + 3, k + 1
+    ldc = ((m + 3) // 4) * 4 + 4 if aligned else m + 5
     A = rng.standard_normal((k, lda)).astype(np.float32)  # column-major storage: column c at A[c]
     B = rng.standard_normal((n, ldb)).astype(np.float32)
     Cm = rng.standard_normal((n, ldc)).astype(np.float32)
