@@ -248,6 +248,12 @@ int kd_lu_stats(const kd_lu* lu, double* t_factor_ms, double* t_solve_ms, int* r
  * matrices: A is m x k (lda), B is k x n (ldb), C is m x n (ldc); k <= 128. */
 int kd_tf32_gemm_update(kd_ctx* ctx, int m, int n, int k, const float* A, long long lda, const float* B,
                         long long ldb, float* C, long long ldc);
+/* The same update with 3xTF32 products (A = Ah + Al, B = Bh + Bl in TF32,
+ * C -= Al Bh + Ah Bl + Ah Bh), about FP32 accurate; the update the mixed LU
+ * uses.  Needs k <= 96, C 16-byte aligned, ldc a multiple of 4 and m a
+ * multiple of 4 (else KD_ERR_UNSUPPORTED). */
+int kd_tf32x3_gemm_update(kd_ctx* ctx, int m, int n, int k, const float* A, long long lda, const float* B,
+                          long long ldb, float* C, long long ldc);
 
 #ifdef __cplusplus
 }

@@ -614,6 +614,19 @@ int kd_tf32_gemm_update(kd_ctx* ctx, int m, int n, int k, const float* A, long l
   });
 }
 
+int kd_tf32x3_gemm_update(kd_ctx* ctx, int m, int n, int k, const float* A, long long lda, const float* B,
+                          long long ldb, float* C, long long ldc) {
+  if (!ctx || !ctx->c) return KD_ERR_ARG;
+  return guarded(ctx, [&] {
+    if (m < 0 || n < 0 || k < 1 || k > 96) throw kd::KdError(KD_ERR_ARG, "need m, n >= 0 and 1 <= k <= 96");
+    if ((m > 0 && lda < m) || ldb < k || (m > 0 && ldc < m)) throw kd::KdError(KD_ERR_ARG, "leading dimension too small");
+    if (!A || !B || !C) throw kd::KdError(KD_ERR_ARG, "null matrix");
+    kd::tf32_gemm_update(ctx->c.get(), m, n, k, A, lda, B, ldb, C, ldc, m, 3);
+    if (kd::tf32_gemm_error_flag(ctx->c.get()))
+      throw kd::KdError(KD_ERR_TIMEOUT, "tensor-core update timed out waiting for its MMAs");
+  });
+}
+
 void* kd_ctx_stream(const kd_ctx* ctx) {
   return (ctx && ctx->c) ? static_cast<void*>(ctx->c->stream()) : nullptr;
 }

@@ -64,8 +64,10 @@ __host__ __device__ constexpr uint32_t tf32_idesc(int M, int N) {
 // Packs a column-major panel into a K-major, zero-padded buffer:
 //   out[r * kpad + kk] = src(r, kk) for r < rows, kk < k; 0 elsewhere.
 // src(r, kk) = col_major ? src[kk * ld + r] : src[r * ld + kk].
+// out_lo != nullptr: also the TF32 rounding of the remainder (v - hi), so
+// that hi + lo carries about 21 significant bits (3xTF32 products).
 __global__ void pack_kmajor(const float* __restrict__ src, long long ld, int rows, int k, int col_major,
-                            float* __restrict__ out, int rows_pad, int kpad) {
+                            float* __restrict__ out, float* __restrict__ out_lo, int rows_pad, int kpad) {
   long long total = static_cast<long long>(rows_pad) * kpad;
   for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < total;
        t += static_cast<long long>(gridDim.x) * blockDim.x) {
@@ -82,7 +84,13 @@ __global__ void pack_kmajor(const float* __restrict__ src, long long ld, int row
     // round to the nearest TF32 value (the tensor cores would truncate)
     uint32_t rounded;
     asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(rounded) : "f"(v));
-    out[static_cast<long long>(r) * kpad + kk] = __uint_as_float(rounded);
+    const float hi = __uint_as_float(rounded);
+    out[static_cast<long long>(r) * kpad + kk] = hi;
+    if (out_lo) {
+      uint32_t rlo;
+      asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(rlo) : "f"(v - hi));
+      out_lo[static_cast<long long>(r) * kpad + kk] = __uint_as_float(rlo);
+    }
   }
 }
 
@@ -225,6 +233,7 @@ constexpr int P_CCOLS = 32;                              // columns per C chunk
 constexpr int P_CHUNK_BYTES = TC_M * P_CCOLS * 4;        // 16 KiB
 constexpr int P_OPBLK_BYTES = 128 * 128;                 // 128 rows x 32 TF32
 constexpr unsigned long long P_WAIT_NS = 2000000000ull;  // 2 s
+constexpr size_t P_MAX_SMEM = 226 * 1024;  // + 1 KiB static shared memory = the 227 KiB per-CTA limit
 
 __device__ __forceinline__ unsigned long long p_now() {
   unsigned long long t;
@@ -272,15 +281,25 @@ __device__ __forceinline__ void p_tma_store(const CUtensorMap* map, const void* 
                : "memory");
 }
 
+__device__ __forceinline__ void tf32_mma(uint32_t d, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t accum) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
+      "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
+}
+
 __global__ void __launch_bounds__(P_THREADS, 1)
     tf32_update_persistent(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
-                           const __grid_constant__ CUtensorMap mapC, int nkb, int ntm, int ntiles,
-                           int* __restrict__ err) {
+                           const __grid_constant__ CUtensorMap mapAlo, const __grid_constant__ CUtensorMap mapBlo,
+                           const __grid_constant__ CUtensorMap mapC, int nkb, int ntm, int ntiles, int split3,
+                           int ncs, int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char p_raw[];
   char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(p_raw) + 1023) & ~uintptr_t(1023));
   char* sA = base;
   char* sB = sA + nkb * P_OPBLK_BYTES;
-  char* sC = sB + nkb * P_OPBLK_BYTES;
+  char* sAl = sB + nkb * P_OPBLK_BYTES;                 // lo parts (split3 only)
+  char* sBl = sAl + nkb * P_OPBLK_BYTES;
+  char* sC = split3 ? sBl + nkb * P_OPBLK_BYTES : sAl;  // ring of ncs C chunks
   __shared__ uint64_t op_full, op_empty, acc_full[2], acc_empty[2], c_full[P_CSLOTS], c_empty[P_CSLOTS];
   __shared__ uint32_t tmem_base_sh;
   __shared__ int abort_flag, epi_abort;
@@ -324,13 +343,17 @@ __global__ void __launch_bounds__(P_THREADS, 1)
           *abort_v = 1;
           break;
         }
-        p_expect_tx(&op_full, 2u * nkb * P_OPBLK_BYTES);
+        p_expect_tx(&op_full, (split3 ? 4u : 2u) * nkb * P_OPBLK_BYTES);
         for (int kb = 0; kb < nkb; kb++) {
           p_tma_load(sA + kb * P_OPBLK_BYTES, &mapA, kb * TC_KBLK, tm * TC_M, &op_full);
           p_tma_load(sB + kb * P_OPBLK_BYTES, &mapB, kb * TC_KBLK, tn * TC_N, &op_full);
+          if (split3) {
+            p_tma_load(sAl + kb * P_OPBLK_BYTES, &mapAlo, kb * TC_KBLK, tm * TC_M, &op_full);
+            p_tma_load(sBl + kb * P_OPBLK_BYTES, &mapBlo, kb * TC_KBLK, tn * TC_N, &op_full);
+          }
         }
         for (int ch = 0; ch < TC_N / P_CCOLS; ch++, cchunk++) {
-          const int slot = cchunk % P_CSLOTS, use = cchunk / P_CSLOTS;
+          const int slot = cchunk % ncs, use = cchunk / ncs;
           if (use > 0 && !p_wait(&c_empty[slot], (use - 1) & 1)) {
             *abort_v = 1;
             break;
@@ -344,6 +367,7 @@ __global__ void __launch_bounds__(P_THREADS, 1)
     if (lane == 0) {  // ------------------------------------------- MMA issuer
       const uint32_t idesc = tf32_idesc(TC_M, TC_N);
       const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+      const uint32_t al0 = smem_u32(sAl), bl0 = smem_u32(sBl);
       int it = 0;
       for (int tile = blockIdx.x; tile < ntiles && !*abort_v; tile += gridDim.x, it++) {
         const int acc = it & 1, use = it >> 1;
@@ -359,13 +383,18 @@ __global__ void __launch_bounds__(P_THREADS, 1)
         const uint32_t d = tmem + static_cast<uint32_t>(acc * TC_N);
         for (int kb = 0; kb < nkb; kb++) {
           for (int k = 0; k < TC_KBLK / 8; k++) {
-            uint64_t ad = sw128_desc(a0 + kb * P_OPBLK_BYTES) + static_cast<uint64_t>((k * 32) >> 4);
-            uint64_t bd = sw128_desc(b0 + kb * P_OPBLK_BYTES) + static_cast<uint64_t>((k * 32) >> 4);
+            const uint64_t koff = static_cast<uint64_t>((k * 32) >> 4);
+            const uint64_t ad = sw128_desc(a0 + kb * P_OPBLK_BYTES) + koff;
+            const uint64_t bd = sw128_desc(b0 + kb * P_OPBLK_BYTES) + koff;
             uint32_t accum = (kb | k) ? 1u : 0u;
-            asm volatile(
-                "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
-                "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
+            if (split3) {  // small terms first: lo*hi, hi*lo, then hi*hi
+              const uint64_t ald = sw128_desc(al0 + kb * P_OPBLK_BYTES) + koff;
+              const uint64_t bld = sw128_desc(bl0 + kb * P_OPBLK_BYTES) + koff;
+              tf32_mma(d, ald, bd, idesc, accum);
+              tf32_mma(d, ad, bld, idesc, 1u);
+              accum = 1u;
+            }
+            tf32_mma(d, ad, bd, idesc, accum);
           }
         }
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -389,8 +418,8 @@ __global__ void __launch_bounds__(P_THREADS, 1)
       if (epi_abort) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       for (int ch = 0; ch < TC_N / P_CCOLS; ch++, cchunk++) {
-        const int slot = cchunk % P_CSLOTS;
-        if (et == 0 && !p_wait(&c_full[slot], (cchunk / P_CSLOTS) & 1)) epi_abort = 1;
+        const int slot = cchunk % ncs;
+        if (et == 0 && !p_wait(&c_full[slot], (cchunk / ncs) & 1)) epi_abort = 1;
         asm volatile("bar.sync 1, 128;" ::: "memory");
         if (epi_abort) break;
         float* cs = reinterpret_cast<float*>(sC + slot * P_CHUNK_BYTES);  // [column][row]
@@ -484,33 +513,46 @@ int grid_for(long long n) {
 
 bool tf32_gemm_supported(int k) { return k > 0 && k <= TC_MAXK; }
 
+bool tf32x3_gemm_possible(int k, const float* C, long long ldc, int m, int c_rows_writable) {
+  const int kpad = ((k + TC_KBLK - 1) / TC_KBLK) * TC_KBLK;
+  return k > 0 && kpad <= 96 && reinterpret_cast<uintptr_t>(C) % 16 == 0 && ldc % 4 == 0 &&
+         (m + 3) / 4 * 4 <= c_rows_writable && encode_fn() != nullptr;
+}
+
 void tf32_gemm_update(Context* ctx, int m, int n, int k, const float* A, long long lda, const float* B, long long ldb,
-                      float* C, long long ldc, int c_rows_writable) {
+                      float* C, long long ldc, int c_rows_writable, int terms) {
   if (m <= 0 || n <= 0 || k <= 0) return;
   if (k > TC_MAXK) throw KdError(KD_ERR_ARG, "tcgen05 trailing update: panel width above 128");
+  const bool split3 = (terms == 3);
+  if (split3 && !tf32x3_gemm_possible(k, C, ldc, m, c_rows_writable))
+    throw KdError(KD_ERR_UNSUPPORTED, "3xTF32 update needs k <= 96 and a 16-byte aligned C with ldc % 4 == 0");
   cudaStream_t s = ctx->stream();
   const int kpad = ((k + TC_KBLK - 1) / TC_KBLK) * TC_KBLK;
   const int mpad = ((m + TC_M - 1) / TC_M) * TC_M;
   const int npad = ((n + TC_N - 1) / TC_N) * TC_N;
+  // hi parts first, lo parts (3xTF32) right after them
   size_t need_a = static_cast<size_t>(mpad) * kpad, need_b = static_cast<size_t>(npad) * kpad;
-  if (need_a > g_tc.cap_a) {
+  if (2 * need_a > g_tc.cap_a) {
     cudaFree(g_tc.at);
-    cuda_check(cudaMalloc(&g_tc.at, need_a * sizeof(float)), "cudaMalloc(At)");
-    g_tc.cap_a = need_a;
+    cuda_check(cudaMalloc(&g_tc.at, 2 * need_a * sizeof(float)), "cudaMalloc(At)");
+    g_tc.cap_a = 2 * need_a;
   }
-  if (need_b > g_tc.cap_b) {
+  if (2 * need_b > g_tc.cap_b) {
     cudaFree(g_tc.bt);
-    cuda_check(cudaMalloc(&g_tc.bt, need_b * sizeof(float)), "cudaMalloc(Bt)");
-    g_tc.cap_b = need_b;
+    cuda_check(cudaMalloc(&g_tc.bt, 2 * need_b * sizeof(float)), "cudaMalloc(Bt)");
+    g_tc.cap_b = 2 * need_b;
   }
   if (!g_tc.err) {
     cuda_check(cudaMalloc(&g_tc.err, sizeof(int)), "cudaMalloc(err)");
     cuda_check(cudaMemsetAsync(g_tc.err, 0, sizeof(int), s), "memset err");
   }
+  float* at_lo = g_tc.at + need_a;
+  float* bt_lo = g_tc.bt + need_b;
   // A is column-major m x k (contiguous along m); B is column-major k x n
   // (contiguous along k).
-  pack_kmajor<<<grid_for(need_a), 256, 0, s>>>(A, lda, m, k, 1, g_tc.at, mpad, kpad);
-  pack_kmajor<<<grid_for(need_b), 256, 0, s>>>(B, ldb, n, k, 0, g_tc.bt, npad, kpad);
+  pack_kmajor<<<grid_for(need_a), 256, 0, s>>>(A, lda, m, k, 1, g_tc.at, split3 ? at_lo : nullptr, mpad, kpad);
+  pack_kmajor<<<grid_for(need_b), 256, 0, s>>>(B, ldb, n, k, 0, g_tc.bt, split3 ? bt_lo : nullptr, npad, kpad);
+  ctx->launches += 2;
   const int nkb = kpad / TC_KBLK;
   // TMA clips the stored rows at 16-byte granularity: rows up to m rounded
   // to 4 may be written (with their unchanged values or zeros), so the
@@ -518,9 +560,11 @@ void tf32_gemm_update(Context* ctx, int m, int n, int k, const float* A, long lo
   const int m4 = (m + 3) / 4 * 4;
   if (reinterpret_cast<uintptr_t>(C) % 16 == 0 && ldc % 4 == 0 && m4 <= c_rows_writable && encode_fn()) {
     // persistent TMA pipeline
-    CUtensorMap mA, mB, mC;
+    CUtensorMap mA, mB, mAl, mBl, mC;
     make_map(&mA, g_tc.at, kpad, mpad, static_cast<long long>(kpad) * 4, TC_KBLK, TC_M, true);
     make_map(&mB, g_tc.bt, kpad, npad, static_cast<long long>(kpad) * 4, TC_KBLK, TC_N, true);
+    make_map(&mAl, at_lo, kpad, mpad, static_cast<long long>(kpad) * 4, TC_KBLK, TC_M, true);
+    make_map(&mBl, bt_lo, kpad, npad, static_cast<long long>(kpad) * 4, TC_KBLK, TC_N, true);
     make_map(&mC, C, m, n, ldc * 4, TC_M, P_CCOLS, false);
     static int nsm = 0;
     static bool pattr = false;
@@ -529,15 +573,21 @@ void tf32_gemm_update(Context* ctx, int m, int n, int k, const float* A, long lo
       cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
       cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "SM count");
       cuda_check(cudaFuncSetAttribute(tf32_update_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      1024 + 2 * (TC_MAXK / TC_KBLK) * P_OPBLK_BYTES + P_CSLOTS * P_CHUNK_BYTES),
+                                      static_cast<int>(P_MAX_SMEM)),
                  "cudaFuncSetAttribute(tf32 persistent)");
       pattr = true;
     }
+    // shared memory: operands (x2 for the lo parts) + a ring of C chunks,
+    // four slots when they fit, else two
+    const size_t ops = static_cast<size_t>(split3 ? 4 : 2) * nkb * P_OPBLK_BYTES;
+    const int ncs = (1024 + ops + P_CSLOTS * P_CHUNK_BYTES <= P_MAX_SMEM) ? P_CSLOTS : 2;
+    const size_t psmem = 1024 + ops + static_cast<size_t>(ncs) * P_CHUNK_BYTES;
+    if (psmem > P_MAX_SMEM) throw KdError(KD_ERR_UNSUPPORTED, "tcgen05 update: operands do not fit in shared memory");
     const int ntm = mpad / TC_M, ntiles = ntm * (npad / TC_N);
     const int grid = ntiles < nsm ? ntiles : nsm;
-    const size_t psmem = 1024 + static_cast<size_t>(2 * nkb) * P_OPBLK_BYTES + P_CSLOTS * P_CHUNK_BYTES;
-    tf32_update_persistent<<<grid, P_THREADS, psmem, s>>>(mA, mB, mC, nkb, ntm, ntiles, g_tc.err);
-    ctx->launches += 3;
+    tf32_update_persistent<<<grid, P_THREADS, psmem, s>>>(mA, mB, mAl, mBl, mC, nkb, ntm, ntiles, split3 ? 1 : 0, ncs,
+                                                          g_tc.err);
+    ctx->launches += 1;
     cuda_check(cudaGetLastError(), "tcgen05 trailing update (persistent)");
     return;
   }
@@ -555,7 +605,7 @@ void tf32_gemm_update(Context* ctx, int m, int n, int k, const float* A, long lo
   }
   dim3 grid(mpad / TC_M, npad / TC_N);
   tf32_update_kernel<<<grid, TC_THREADS, smem, s>>>(g_tc.at, g_tc.bt, kpad, C, ldc, m, n, g_tc.err);
-  ctx->launches += 3;
+  ctx->launches += 1;
   cuda_check(cudaGetLastError(), "tcgen05 trailing update");
 }
 
@@ -569,10 +619,12 @@ int tf32_gemm_error_flag(Context* ctx) {
 }
 
 void gemm_update_f32(Context* ctx, cublasHandle_t blas, int m, int n, int k, const float* A, long long lda,
-                     const float* B, long long ldb, float* C, long long ldc, bool tf32, int c_rows_writable) {
+                     const float* B, long long ldb, float* C, long long ldc, bool tf32, int c_rows_writable,
+                     int terms) {
   ProfScope ps(ctx, Context::PROF_LU_GEMM, 2.0 * m * n * k);
   if (tf32 && tf32_gemm_supported(k)) {
-    tf32_gemm_update(ctx, m, n, k, A, lda, B, ldb, C, ldc, c_rows_writable);
+    if (terms == 3 && !tf32x3_gemm_possible(k, C, ldc, m, c_rows_writable)) terms = 1;
+    tf32_gemm_update(ctx, m, n, k, A, lda, B, ldb, C, ldc, c_rows_writable, terms);
     return;
   }
   // plain FP32 product (the FP32-IR mode): library SGEMM

@@ -11,13 +11,17 @@ namespace kd {
 // c_rows_writable: rows [m, c_rows_writable) of every column of C are
 // scratch that the update may overwrite (the padding of a matrix whose
 // leading dimension is rounded up); pass m when there is none.
+// terms: 1 = plain TF32 products; 3 = 3xTF32 (hi*hi + hi*lo + lo*hi, about
+// FP32 accuracy), used where possible (k <= 96, TMA-aligned C).
 void gemm_update_f32(Context* ctx, cublasHandle_t blas, int m, int n, int k, const float* A, long long lda,
-                     const float* B, long long ldb, float* C, long long ldc, bool tf32, int c_rows_writable);
+                     const float* B, long long ldb, float* C, long long ldc, bool tf32, int c_rows_writable,
+                     int terms = 1);
 
 // The tcgen05 kernels on their own (k <= 128).
 bool tf32_gemm_supported(int k);
 void tf32_gemm_update(Context* ctx, int m, int n, int k, const float* A, long long lda, const float* B, long long ldb,
-                      float* C, long long ldc, int c_rows_writable);
+                      float* C, long long ldc, int c_rows_writable, int terms = 1);
+bool tf32x3_gemm_possible(int k, const float* C, long long ldc, int m, int c_rows_writable);
 // Returns (and clears) the flag a CTA sets when its wait for the tensor-core
 // results ran out of polls.
 int tf32_gemm_error_flag(Context* ctx);

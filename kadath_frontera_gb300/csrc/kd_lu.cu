@@ -485,12 +485,16 @@ __device__ bool grid_barrier(unsigned* bar, unsigned target, int* err, int* s_ok
   return *s_ok != 0;
 }
 
-__device__ __forceinline__ bool better(double v, int i, double bv, int bi) { return v > bv || (v == bv && i < bi); }
+template <class V>
+__device__ __forceinline__ bool better(V v, int i, V bv, int bi) {
+  return v > bv || (v == bv && i < bi);
+}
 
 // Block-wide arg-max of (v, i) carrying a tag; every thread gets the result.
-__device__ void block_argmax(double& v, int& i, int& tag, double* rv, int* ri, int* rt) {
+template <class V>
+__device__ void block_argmax(V& v, int& i, int& tag, V* rv, int* ri, int* rt) {
   for (int o = 16; o > 0; o >>= 1) {
-    double ov = __shfl_xor_sync(0xffffffffu, v, o);
+    V ov = __shfl_xor_sync(0xffffffffu, v, o);
     int oi = __shfl_xor_sync(0xffffffffu, i, o);
     int ot = __shfl_xor_sync(0xffffffffu, tag, o);
     if (better(ov, oi, v, i)) {
@@ -537,9 +541,12 @@ template <class T>
 __global__ void __launch_bounds__(256) trsv_sweep(const T* __restrict__ A, long long ld, int N, double* b,
                                                   double* __restrict__ y, const double* __restrict__ Dinv,
                                                   int lower, unsigned* bar, int* err) {
+  // x_k = Dinv_k b in FP64 (an explicit inverse amplifies rounding by its
+  // condition number); the row updates in the factors' precision T
   __shared__ double bb[TB];
   __shared__ double xx[TB];
-  __shared__ double part[4][SW_TILE];
+  __shared__ T xt[TB];
+  __shared__ T part[4][SW_TILE];
   __shared__ int s_ok;
   const int nblk = (N + TB - 1) / TB;
   const int ntiles = (N + SW_TILE - 1) / SW_TILE;
@@ -564,7 +571,10 @@ __global__ void __launch_bounds__(256) trsv_sweep(const T* __restrict__ A, long 
       for (int q = 0; q < 8; q++) {
         double p = lo[q] * b0 + hi[q] * b1;
         for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
-        if (lane == 0) xx[warp * 8 + q] = p;
+        if (lane == 0) {
+          xx[warp * 8 + q] = p;
+          xt[warp * 8 + q] = static_cast<T>(p);
+        }
       }
     }
     __syncthreads();
@@ -577,21 +587,21 @@ __global__ void __launch_bounds__(256) trsv_sweep(const T* __restrict__ A, long 
     for (int t = first; t < t1 && t < ntiles; t += gridDim.x) {
       const int row = t * SW_TILE + half * 32 + lane;
       const int c0 = quarter * 16;
-      double acc = 0.0;
+      T acc = T(0);
       if (row >= q0 && row < q1) {
         const T* a = A + static_cast<long long>(r0 + c0) * ld + row;
         T v[16];
 #pragma unroll
         for (int j = 0; j < 16; j++) v[j] = (c0 + j < n) ? a[static_cast<long long>(j) * ld] : T(0);
 #pragma unroll
-        for (int j = 0; j < 16; j++) acc = fma(static_cast<double>(v[j]), xx[c0 + j], acc);
+        for (int j = 0; j < 16; j++) acc = fma(v[j], xt[c0 + j], acc);
       }
       part[quarter][half * 32 + lane] = acc;
       __syncthreads();
       if (tid < SW_TILE) {
         const int r = t * SW_TILE + tid;
         if (r >= q0 && r < q1)
-          b[r] = __ldcg(b + r) - ((part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]));
+          b[r] = __ldcg(b + r) - static_cast<double>((part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]));
       }
       __syncthreads();
     }
@@ -605,8 +615,8 @@ __global__ void __launch_bounds__(GP_THREADS) panel_grid_kernel(T* __restrict__ 
                                                                 int* __restrict__ info, PanelSlots<T> ps) {
   extern __shared__ __align__(16) unsigned char gp_raw[];
   T* tile = reinterpret_cast<T*>(gp_raw);
-  __shared__ double prow[128];
-  __shared__ double rv[GP_THREADS / 32];
+  __shared__ T prow[128];
+  __shared__ T rv[GP_THREADS / 32];
   __shared__ int ri[GP_THREADS / 32], rt[GP_THREADS / 32];
   __shared__ int s_ok;
   const int nblk = gridDim.x, b = blockIdx.x, tid = threadIdx.x, bd = blockDim.x;
@@ -622,10 +632,10 @@ __global__ void __launch_bounds__(GP_THREADS) panel_grid_kernel(T* __restrict__ 
     const int j = j0 + jj;
     const int slot = jj & 1;
     // 1. local candidate
-    double best = -1.0;
+    T best = T(-1);
     int bi = N, tag = 0;
     for (int i = (r0 > j ? r0 : j) + tid; i < r1; i += bd) {
-      double v = fabs(static_cast<double>(tile[jj * per + i - r0]));
+      T v = fabs(tile[jj * per + i - r0]);
       if (better(v, i, best, bi)) {
         best = v;
         bi = i;
@@ -637,7 +647,7 @@ __global__ void __launch_bounds__(GP_THREADS) panel_grid_kernel(T* __restrict__ 
     if (bi < N)
       for (int k = tid; k < jb; k += bd) mine[k] = tile[k * per + bi - r0];
     if (tid == 0) {
-      ps.cand_v[slot * nblk + b] = best;
+      ps.cand_v[slot * nblk + b] = static_cast<double>(best);
       ps.cand_i[slot * nblk + b] = bi;
     }
     if (j >= r0 && j < r1)
@@ -645,11 +655,11 @@ __global__ void __launch_bounds__(GP_THREADS) panel_grid_kernel(T* __restrict__ 
     // 3. one barrier per column
     if (!grid_barrier(ps.bar, static_cast<unsigned>(nblk) * (jj + 1), ps.err, &s_ok)) return;
     // 4. every CTA reduces the candidates identically
-    best = -1.0;
+    best = T(-1);
     bi = N;
     tag = -1;
     for (int t = tid; t < nblk; t += bd) {
-      double v = __ldcg(ps.cand_v + slot * nblk + t);
+      T v = static_cast<T>(__ldcg(ps.cand_v + slot * nblk + t));
       int ii = __ldcg(ps.cand_i + slot * nblk + t);
       if (better(v, ii, best, bi)) {
         best = v;
@@ -665,22 +675,22 @@ __global__ void __launch_bounds__(GP_THREADS) panel_grid_kernel(T* __restrict__ 
     }
     if (b == 0 && tid == 0) {
       ipiv[j] = gi;
-      if (!(best > 0.0) && *info == 0) *info = j + 1;  // zero (or NaN) pivot
+      if (!(best > T(0)) && *info == 0) *info = j + 1;  // zero (or NaN) pivot
     }
     // 5. pivot row, row exchange
     const T* src = (tag >= 0) ? ps.cand_rows + (static_cast<size_t>(slot) * nblk + tag) * jb : ps.jrow + slot * jb;
-    for (int k = tid; k < jb; k += bd) prow[k] = static_cast<double>(__ldcg(src + k));
+    for (int k = tid; k < jb; k += bd) prow[k] = __ldcg(src + k);
     if (gi != j && gi >= r0 && gi < r1)
       for (int k = tid; k < jb; k += bd) tile[k * per + gi - r0] = __ldcg(ps.jrow + slot * jb + k);
     __syncthreads();
     if (j >= r0 && j < r1)
-      for (int k = tid; k < jb; k += bd) tile[k * per + j - r0] = static_cast<T>(prow[k]);
+      for (int k = tid; k < jb; k += bd) tile[k * per + j - r0] = prow[k];
     // 6. scale the column below the pivot, rank-1 update of the rest
-    const double piv = prow[jj];
+    const T piv = prow[jj];
     const int rs = (r0 > j + 1) ? r0 : j + 1;
     __syncthreads();
-    if (piv != 0.0 && rs < r1) {
-      const T inv = static_cast<T>(1.0 / piv);
+    if (piv != T(0) && rs < r1) {
+      const T inv = T(1) / piv;
       for (int i = rs + tid; i < r1; i += bd) tile[jj * per + i - r0] *= inv;
       __syncthreads();
       // thread -> (row, column phase): rows along the low 7 bits (conflict-free
@@ -693,7 +703,7 @@ __global__ void __launch_bounds__(GP_THREADS) panel_grid_kernel(T* __restrict__ 
           const int li = rs - r0 + ii;
           const T l = tile[jj * per + li];
           for (int k = jj + 1 + ph; k < jb; k += nph)
-            tile[k * per + li] = fma(-l, static_cast<T>(prow[k]), tile[k * per + li]);
+            tile[k * per + li] = fma(-l, prow[k], tile[k * per + li]);
         }
       }
     }
@@ -703,6 +713,258 @@ __global__ void __launch_bounds__(GP_THREADS) panel_grid_kernel(T* __restrict__ 
     int k = e / nr, r = e % nr;
     A[static_cast<long long>(j0 + k) * ld + r0 + r] = tile[k * per + r];
   }
+}
+
+// ---- panel on one 16-CTA cluster (FP32 factors) --------------------------
+// The same algorithm as panel_grid_kernel with the exchange in distributed
+// shared memory: CTA r of the cluster keeps rows [j0 + r*per, ...) of the
+// panel in its shared memory; per column each CTA writes its candidate
+// (value, row, full panel row) and, when it owns row j, row j into its own
+// double-buffered slots, one cluster barrier, then every CTA reads the 16
+// candidates and the winning row from the owners' shared memory.  A final
+// cluster barrier keeps every CTA's shared memory alive until the last
+// remote reads are done.
+constexpr int CP_CL = 16;
+constexpr int CP_THREADS = 512;
+constexpr size_t CP_MAX_SMEM = 212 * 1024;
+constexpr int CP_IB = 16;  // inner block: columns updated per column step
+
+__global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __restrict__ A, long long ld, int N,
+                                                                     int j0, int jb, int per,
+                                                                     int* __restrict__ ipiv,
+                                                                     int* __restrict__ info) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ __align__(16) unsigned char cp_raw[];
+  float* tile = reinterpret_cast<float*>(cp_raw);  // tile[k * per + r]
+  __shared__ float cand_row[2][128];
+  __shared__ float jrow[2][128];
+  __shared__ float cand_v[2];
+  __shared__ int cand_i[2];
+  __shared__ float prow[128];
+  __shared__ float ublk[CP_IB][128];  // rows of the current inner block (L11 | A12 -> U12)
+  __shared__ float rv[CP_THREADS / 32];
+  __shared__ int ri[CP_THREADS / 32], rt[CP_THREADS / 32];
+  const int rank = static_cast<int>(cluster.block_rank());
+  const int tid = threadIdx.x, bd = blockDim.x;
+  const int r0 = j0 + rank * per;
+  const int r1 = (r0 + per < N) ? r0 + per : N;
+  const int nr = r1 > r0 ? r1 - r0 : 0;
+  for (int e = tid; e < jb * nr; e += bd) {
+    int k = e / nr, r = e % nr;
+    tile[k * per + r] = A[static_cast<long long>(j0 + k) * ld + r0 + r];
+  }
+  __syncthreads();
+  for (int b0 = 0; b0 < jb; b0 += CP_IB) {
+    const int be = (b0 + CP_IB < jb) ? b0 + CP_IB : jb;
+    for (int jj = b0; jj < be; jj++) {
+      const int j = j0 + jj;
+      const int slot = jj & 1;
+      float best = -1.0f;
+      int bi = N, tag = 0;
+      for (int i = (r0 > j ? r0 : j) + tid; i < r1; i += bd) {
+        float v = fabsf(tile[jj * per + i - r0]);
+        if (better(v, i, best, bi)) {
+          best = v;
+          bi = i;
+        }
+      }
+      block_argmax(best, bi, tag, rv, ri, rt);
+      if (bi < N)
+        for (int k = tid; k < jb; k += bd) cand_row[slot][k] = tile[k * per + bi - r0];
+      if (tid == 0) {
+        cand_v[slot] = best;
+        cand_i[slot] = bi;
+      }
+      if (j >= r0 && j < r1)
+        for (int k = tid; k < jb; k += bd) jrow[slot][k] = tile[k * per + j - r0];
+      cluster.sync();
+      // every CTA reduces the 16 candidates in the same order
+      best = -1.0f;
+      bi = N;
+      tag = -1;
+      if (tid < 32) {
+        if (tid < CP_CL) {
+          best = *cluster.map_shared_rank(&cand_v[slot], tid);
+          bi = *cluster.map_shared_rank(&cand_i[slot], tid);
+          tag = tid;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+          float ov = __shfl_xor_sync(0xffffffffu, best, o);
+          int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+          int ot = __shfl_xor_sync(0xffffffffu, tag, o);
+          if (better(ov, oi, best, bi)) {
+            best = ov;
+            bi = oi;
+            tag = ot;
+          }
+        }
+        if (tid == 0) {
+          rv[0] = best;
+          ri[0] = bi;
+          rt[0] = tag;
+        }
+      }
+      __syncthreads();
+      best = rv[0];
+      int gi = ri[0];
+      tag = rt[0];
+      if (gi >= N) {  // nothing usable below the diagonal: no swap
+        gi = j;
+        tag = -1;
+      }
+      if (rank == 0 && tid == 0) {
+        ipiv[j] = gi;
+        if (!(best > 0.0f) && *info == 0) *info = j + 1;  // zero (or NaN) pivot
+      }
+      const int jowner = (j - j0) / per;
+      const float* src = (tag >= 0) ? cluster.map_shared_rank(&cand_row[slot][0], tag)
+                                    : cluster.map_shared_rank(&jrow[slot][0], jowner);
+      for (int k = tid; k < jb; k += bd) prow[k] = src[k];
+      if (gi != j && gi >= r0 && gi < r1) {
+        const float* jr = cluster.map_shared_rank(&jrow[slot][0], jowner);
+        for (int k = tid; k < jb; k += bd) tile[k * per + gi - r0] = jr[k];
+      }
+      __syncthreads();
+      if (j >= r0 && j < r1)
+        for (int k = tid; k < jb; k += bd) tile[k * per + j - r0] = prow[k];
+      const float piv = prow[jj];
+      const int rs = (r0 > j + 1) ? r0 : j + 1;
+      __syncthreads();
+      if (piv != 0.0f && rs < r1) {
+        // scale the column, rank-1 update of the inner block's columns only
+        const float inv = 1.0f / piv;
+        for (int i = rs + tid; i < r1; i += bd) tile[jj * per + i - r0] *= inv;
+        __syncthreads();
+        const int nrr = r1 - rs;
+        const int nph = bd >> 7, ph = tid >> 7;
+        for (int i0 = 0; i0 < nrr; i0 += 128) {
+          const int ii = i0 + (tid & 127);
+          if (ii < nrr) {
+            const int li = rs - r0 + ii;
+            const float l = tile[jj * per + li];
+            for (int k = jj + 1 + ph; k < be; k += nph)
+              tile[k * per + li] = fmaf(-l, prow[k], tile[k * per + li]);
+          }
+        }
+      }
+      __syncthreads();
+    }
+    if (be < jb) {
+      // Rows j0+b0 .. j0+be-1 are final in columns b0..be-1 (L11 below the
+      // diagonal); every CTA fetches them whole and forms
+      // U12 = L11^{-1} A12 for columns be..jb-1.
+      const int nbr = be - b0;
+      cluster.sync();
+      for (int e = tid; e < nbr * jb; e += bd) {
+        const int t = e / jb, k = e % jb;
+        const int row = j0 + b0 + t;
+        const int owner = (row - j0) / per;
+        const float* ot = cluster.map_shared_rank(tile, owner);
+        ublk[t][k] = ot[static_cast<long long>(k) * per + (row - (j0 + owner * per))];
+      }
+      __syncthreads();
+      for (int k = be + tid; k < jb; k += bd)  // one column of U12 per thread
+        for (int t = 1; t < nbr; t++) {
+          float acc = ublk[t][k];
+          for (int q = 0; q < t; q++) acc = fmaf(-ublk[t][b0 + q], ublk[q][k], acc);
+          ublk[t][k] = acc;
+        }
+      cluster.sync();  // remote reads of the block rows are done
+      // owners store U12; rows below the block get the rank-nbr update
+      for (int e = tid; e < nbr * (jb - be); e += bd) {
+        const int t = e / (jb - be), k = be + e % (jb - be);
+        const int row = j0 + b0 + t;
+        if (row >= r0 && row < r1) tile[k * per + row - r0] = ublk[t][k];
+      }
+      const int rs = (r0 > j0 + be) ? r0 : j0 + be;
+      if (rs < r1) {
+        const int nrr = r1 - rs;
+        const int nph = bd >> 7, ph = tid >> 7;
+        for (int i0 = 0; i0 < nrr; i0 += 128) {
+          const int ii = i0 + (tid & 127);
+          if (ii < nrr) {
+            const int li = rs - r0 + ii;
+            // (inside this branch the block is full: nbr == CP_IB)
+            float l[CP_IB];
+#pragma unroll
+            for (int q = 0; q < CP_IB; q++) l[q] = tile[(b0 + q) * per + li];
+            for (int k = be + ph; k < jb; k += nph) {
+              float acc = tile[k * per + li];
+#pragma unroll
+              for (int q = 0; q < CP_IB; q++) acc = fmaf(-l[q], ublk[q][k], acc);
+              tile[k * per + li] = acc;
+            }
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  for (int e = tid; e < jb * nr; e += bd) {
+    int k = e / nr, r = e % nr;
+    A[static_cast<long long>(j0 + k) * ld + r0 + r] = tile[k * per + r];
+  }
+  cluster.sync();  // remote readers of this CTA's shared memory are done
+}
+
+// Widest panel (96, 64 or 32 columns) whose rows fit in the shared memory of
+// one 16-CTA cluster; 0 when none does.
+static int cluster_panel_width(int rows) {
+  const int per = (rows + CP_CL - 1) / CP_CL;
+  for (int w : {96, 64, 32})
+    if (static_cast<size_t>(per) * w * sizeof(float) <= CP_MAX_SMEM) return w;
+  return 0;
+}
+
+// Launches the cluster panel; false when the GPU cannot host a 16-CTA
+// cluster of this size (the caller then uses the cooperative grid kernel).
+static bool panel_cluster16(Context* ctx, float* A, long long ld, int N, int j0, int jb, int* ipiv, int* info) {
+  const int rows = N - j0;
+  const int per = (rows + CP_CL - 1) / CP_CL;
+  const size_t smem = static_cast<size_t>(per) * jb * sizeof(float);
+  if (smem > CP_MAX_SMEM) return false;
+  static int usable = -1;
+  if (usable < 0) {
+    usable = 0;
+    if (cudaFuncSetAttribute(panel_cluster16_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+            cudaSuccess &&
+        cudaFuncSetAttribute(panel_cluster16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(CP_MAX_SMEM)) == cudaSuccess) {
+      cudaLaunchConfig_t q = {};
+      q.gridDim = dim3(CP_CL, 1, 1);
+      q.blockDim = dim3(CP_THREADS, 1, 1);
+      q.dynamicSmemBytes = CP_MAX_SMEM;
+      cudaLaunchAttribute qa[1];
+      qa[0].id = cudaLaunchAttributeClusterDimension;
+      qa[0].val.clusterDim.x = CP_CL;
+      qa[0].val.clusterDim.y = 1;
+      qa[0].val.clusterDim.z = 1;
+      q.attrs = qa;
+      q.numAttrs = 1;
+      int nclusters = 0;
+      if (cudaOccupancyMaxActiveClusters(&nclusters, panel_cluster16_kernel, &q) == cudaSuccess && nclusters > 0)
+        usable = 1;
+    }
+    cudaGetLastError();  // clear a refused attribute or query
+  }
+  if (!usable) return false;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(CP_CL, 1, 1);
+  cfg.blockDim = dim3(CP_THREADS, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = ctx->stream();
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = CP_CL;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cuda_check(cudaLaunchKernelEx(&cfg, panel_cluster16_kernel, A, ld, N, j0, jb, per, ipiv, info),
+             "panel cluster kernel");
+  ctx->launches += 1;
+  return true;
 }
 
 // The row exchanges of one panel (ipiv[j0 .. j0+jb)) as a list of moves
@@ -844,6 +1106,9 @@ static void panel_factor(Context* ctx, T* A, long long ld, int N, int j0, int jb
     slots.bar = reinterpret_cast<unsigned*>(p);
     slots.err = reinterpret_cast<int*>(p + 16);
   }
+  if constexpr (std::is_same<T, float>::value) {
+    if (panel_cluster16(ctx, A, ld, N, j0, jb, ipiv, info)) return;
+  }
   if (panel_grid<T>(ctx, A, ld, N, j0, jb, ipiv, info, nsm, slots)) return;
   // Panels too tall for the shared memory of the GPU: one 8-CTA cluster
   // working on the panel in global memory.
@@ -921,8 +1186,15 @@ void DenseLU::factor_f32(float* A, long long ld, int N, bool tf32) {
   const int NB = nb > 96 ? 96 : nb;
   cudaStream_t s = ctx_->stream();
   cuda_check(cudaMemsetAsync(d_info_, 0, sizeof(int), s), "memset info");
-  for (int j0 = 0; j0 < N; j0 += NB) {
-    int jb = (N - j0 < NB) ? N - j0 : NB;
+  for (int j0 = 0, jb = 0; j0 < N; j0 += jb) {
+    // Panel width: NB, narrowed while the panel is too tall for the shared
+    // memory of one 16-CTA cluster (blocked LU allows any widths).
+    int w = NB;
+    if (NB == 96) {
+      const int cw = cluster_panel_width(N - j0);
+      if (cw > 0) w = cw;
+    }
+    jb = (N - j0 < w) ? N - j0 : w;
     panel_factor<float>(ctx_, A, ld, N, j0, jb, ipiv_, d_info_, nsm_, slot_mem_);
     trsm_and_swaps<float>(ctx_, A, ld, N, j0, jb, ipiv_, swap_map_);
     int m = N - j0 - jb;
@@ -931,7 +1203,8 @@ void DenseLU::factor_f32(float* A, long long ld, int N, bool tf32) {
       float* A12 = A + static_cast<long long>(j0 + jb) * ld + j0;
       float* A22 = A + static_cast<long long>(j0 + jb) * ld + j0 + jb;
       // rows N .. ld of the working matrix are padding
-      gemm_update_f32(ctx_, blas_, m, m, jb, A21, ld, A12, ld, A22, ld, tf32, static_cast<int>(ld - j0 - jb));
+      gemm_update_f32(ctx_, blas_, m, m, jb, A21, ld, A12, ld, A22, ld, tf32, static_cast<int>(ld - j0 - jb),
+                      tf32_terms);
     }
   }
 }
@@ -1007,11 +1280,11 @@ void DenseLU::tri_solve(const T* LU, long long ld, int N, double* b, int trans) 
     cfg.attrs = at;
     cfg.numAttrs = 1;
     cuda_check(cudaMemsetAsync(tri_bar_, 0, 2 * sizeof(unsigned), s), "memset sweep barriers");
-    cuda_check(cudaLaunchKernelEx(&cfg, trsv_sweep<T>, LU, ld, N, w1, w2, static_cast<const double*>(dinv_l_), 1,
-                                  tri_bar_, panel_err_),
+    const double* dl = dinv_l_;
+    const double* du = dinv_u_;
+    cuda_check(cudaLaunchKernelEx(&cfg, trsv_sweep<T>, LU, ld, N, w1, w2, dl, 1, tri_bar_, panel_err_),
                "forward sweep");
-    cuda_check(cudaLaunchKernelEx(&cfg, trsv_sweep<T>, LU, ld, N, w2, b, static_cast<const double*>(dinv_u_), 0,
-                                  tri_bar_ + 1, panel_err_),
+    cuda_check(cudaLaunchKernelEx(&cfg, trsv_sweep<T>, LU, ld, N, w2, b, du, 0, tri_bar_ + 1, panel_err_),
                "backward sweep");
     ctx_->launches += 3;
     cuda_check(cudaGetLastError(), "triangular solve");

@@ -43,6 +43,9 @@ class DenseLU {
   double gmres_tol = 1e-14;
   int gmres_max_iter = 50;
   int nb = 128;
+  // TF32 mode: 3 = 3xTF32 trailing updates (about FP32 accurate factors,
+  // fewer refinement iterations), 1 = plain TF32 products.
+  int tf32_terms = 3;
 
  private:
   Context* ctx_;

@@ -103,3 +103,45 @@ def test_tcgen05_tf32_update_matches_fp64_product(ctx, m, n, k, aligned):
     assert err <= 4 * 2.0 ** -11 * scale, (err, scale)
     # padding rows beyond m (ldc > m) untouched
     assert np.array_equal(got[:, m:], Cm[:, m:])
+
+
+@pytest.mark.parametrize("m,n,k", [(128, 128, 32), (256, 384, 96), (200, 130, 96), (1000, 777, 64), (2000, 1500, 96)])
+def test_tcgen05_3xtf32_update_is_fp32_accurate(ctx, m, n, k):
+    """3xTF32 (hi/lo split of both operands, three tensor-core products) is
+    about FP32 accurate: error bound 2^-17 * max|A| max|B| k, 256 times
+    tighter than the plain TF32 bound of the test above."""
+    import ctypes as C
+    lib = ctx.lib
+    lib.kd_tf32x3_gemm_update.restype = C.c_int
+    lib.kd_tf32x3_gemm_update.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_longlong,
+                                          C.c_void_p, C.c_longlong, C.c_void_p, C.c_longlong]
+    rng = np.random.default_rng(m * 11 + n + k)
+    lda, ldb, ldc = m + 3, k + 1, m + 4
+    A = rng.standard_normal((k, lda)).astype(np.float32)
+    B = rng.standard_normal((n, ldb)).astype(np.float32)
+    Cm = rng.standard_normal((n, ldc)).astype(np.float32)
+    dA, dB, dC = (torch.tensor(x, device="cuda") for x in (A, B, Cm))
+    torch.cuda.synchronize()
+    st = lib.kd_tf32x3_gemm_update(ctx.h, m, n, k, dA.data_ptr(), lda, dB.data_ptr(), ldb, dC.data_ptr(), ldc)
+    assert st == 0, lib.kd_last_error(ctx.h)
+    ctx.synchronize()
+    got = dC.cpu().numpy()
+    Am = A[:, :m].T.astype(np.float64)
+    Bm = B[:, :k].T.astype(np.float64)
+    ref = Cm[:, :m].T.astype(np.float64) - Am @ Bm
+    err = np.abs(got[:, :m].T - ref).max()
+    scale = np.abs(Am).max() * np.abs(Bm).max() * k
+    assert err <= 2.0 ** -17 * scale, (err, scale)
+    assert np.array_equal(got[:, m:], Cm[:, m:])
+
+
+def test_tcgen05_3xtf32_rejects_unaligned(ctx):
+    import ctypes as C
+    lib = ctx.lib
+    lib.kd_tf32x3_gemm_update.restype = C.c_int
+    lib.kd_tf32x3_gemm_update.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_longlong,
+                                          C.c_void_p, C.c_longlong, C.c_void_p, C.c_longlong]
+    dA = torch.zeros(64 * 64, device="cuda")
+    dC = torch.zeros(64 * 70, device="cuda")
+    st = lib.kd_tf32x3_gemm_update(ctx.h, 62, 64, 32, dA.data_ptr(), 64, dA.data_ptr(), 64, dC.data_ptr(), 70)
+    assert st == 6  # KD_ERR_UNSUPPORTED: ldc not a multiple of 4
