@@ -198,6 +198,13 @@ int kd_system_check_equations(kd_system* s, double* errors);
  * host matrix (ld = N). */
 int kd_system_jacobian(kd_system* s, double* J);
 /* Same, into a device buffer of leading dimension ld (device pointer). */
+/* Keeps, between Jacobian assemblies, the batched tangents of the subtrees
+ * whose tangent does not depend on the iterate (Laplacians and derivatives
+ * of unknowns, matching and boundary conditions, products with numbers):
+ * later assemblies skip those subtrees.  On by default; 0 frees them.  No
+ * reference counterpart: the reference recomputes every column of the
+ * Jacobian at every step (do_col_J, src/System_of_eqs/solver.cpp:120). */
+int kd_system_cache_tangents(kd_system* s, int enable);
 int kd_system_jacobian_device(kd_system* s, double* dJ, long long ld);
 /* xx_to_vars + var = old - x (src_par/do_newton.cpp:397-414), host x. */
 int kd_system_update(kd_system* s, const double* x);

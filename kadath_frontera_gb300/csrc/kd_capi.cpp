@@ -501,6 +501,11 @@ int kd_system_check_equations(kd_system* s, double* errors) {
   });
 }
 
+int kd_system_cache_tangents(kd_system* s, int enable) {
+  if (!s || !s->sys) return KD_ERR_ARG;
+  return guarded(s->sp->ctx, [&] { s->sys->set_tangent_cache(enable != 0); });
+}
+
 int kd_system_jacobian_device(kd_system* s, double* dJ, long long ld) {
   SYS_GUARD(s) {
     if (!dJ) throw kd::KdError(KD_ERR_ARG, "null output");

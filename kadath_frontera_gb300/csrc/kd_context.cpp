@@ -143,18 +143,21 @@ void Context::run_items(const std::vector<KdItem>& items, const std::vector<int>
       i++;
     }
     list.nitems = n;
-    double bytes = 0;
+    // algorithmic FP64 work: per pass, n_in multiply-adds per output value
+    double flops = 0;
     for (int q = 0; q < n; q++) {
       const KdItem& it = list.items[q];
       int d0 = it.n0, d1 = it.n1, d2 = it.n2;
+      double f = 0;
       for (int p = 0; p < it.npass; p++) {
         if (it.pass[p].dim == 0) d0 = it.pass[p].n_out;
         if (it.pass[p].dim == 1) d1 = it.pass[p].n_out;
         if (it.pass[p].dim == 2) d2 = it.pass[p].n_out;
+        f += 2.0 * double(d0) * d1 * d2 * it.pass[p].n_in;
       }
-      bytes += 8.0 * (list.prefix[q + 1] - list.prefix[q]) * (double(it.n0) * it.n1 * it.n2 + double(d0) * d1 * d2);
+      flops += f * (list.prefix[q + 1] - list.prefix[q]);
     }
-    ProfScope ps(this, PROF_LINE_PASS, bytes);
+    ProfScope ps(this, PROF_LINE_PASS, flops);
     cuda_check(launch_line_passes(list, smem, dp, stream_), "line_passes kernel");
     launches++;
   }

@@ -87,7 +87,7 @@ class Context {
   // Optional per-category timing of launches (CUDA events on this stream)
   // with the algorithmic work (bytes or flops) each launch performs.
   enum ProfCat : int {
-    PROF_LINE_PASS = 0,  // separable transforms / 1-D coefficient operators
+    PROF_LINE_PASS = 0,  // separable transforms / 1-D coefficient operators (work: FP64 flops)
     PROF_EW = 1,         // elementwise algebra at collocation points
     PROF_GATHER = 2,     // tau export / affecte_tau gathers
     PROF_LU_PANEL = 3,

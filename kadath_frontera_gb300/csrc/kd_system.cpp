@@ -188,12 +188,64 @@ void ValueCache::store(const Ope* node, const Term& t) {
   vals[node] = std::move(v);
 }
 
+void TangentCache::store(Context* ctx, const Ope* node, int var, int dom, const Term& t) {
+  Entry e;
+  e.is_double = t.is_double;
+  e.dd = t.dd;
+  for (const DVal& d : t.dt) {
+    DVal c(d.ctx, d.dom, d.batch);
+    c.zero = d.zero;
+    c.base = d.base;
+    if (!d.zero) {
+      if (d.in_conf) {
+        const size_t n = static_cast<size_t>(d.npts()) * d.batch;
+        double* p = arena.alloc_doubles(n);
+        cuda_check(cudaMemcpyAsync(p, d.c, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream()),
+                   "tangent cache copy");
+        c.c = p;
+        c.in_conf = true;
+      }
+      if (d.in_coef) {
+        const size_t n = static_cast<size_t>(d.ncoefs()) * d.batch;
+        double* p = arena.alloc_doubles(n);
+        cuda_check(cudaMemcpyAsync(p, d.cf, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream()),
+                   "tangent cache copy");
+        c.cf = p;
+        c.in_coef = true;
+      }
+    }
+    e.dt.push_back(c);
+  }
+  ders[std::make_tuple(node, var, dom)] = std::move(e);
+}
+
 Term Ope::eval(EvalState& st) const {
   ValueCache* vc = st.vcache;
   if (!vc || !cacheable()) return action(st, nullptr);
   if (st.with_der) {
     auto it = vc->vals.find(this);
-    return action(st, it != vc->vals.end() ? &it->second : nullptr);
+    const Term* cv = it != vc->vals.end() ? &it->second : nullptr;
+    if (cache_der && st.tcache && cv) {
+      const auto key = std::make_tuple(static_cast<const Ope*>(this), st.seed_var, st.seed_dom);
+      auto tt = st.tcache->ders.find(key);
+      if (tt != st.tcache->ders.end()) {
+        // value of this iterate, tangent from an earlier assembly: the
+        // subtree is not evaluated at all
+        Term r = *cv;
+        if (tt->second.is_double) {
+          r.has_dd = true;
+          r.dd = tt->second.dd;
+        } else {
+          r.has_dt = true;
+          r.dt = tt->second.dt;
+        }
+        return r;
+      }
+      Term r = action(st, cv);
+      st.tcache->store(st.sys->ctx, this, st.seed_var, st.seed_dom, r);
+      return r;
+    }
+    return action(st, cv);
   }
   Term t = action(st, nullptr);
   if (st.record) vc->store(this, t);
@@ -241,7 +293,12 @@ bool split_eq(const std::string& s, std::string& l, std::string& r) {
 
 class OpeSubEq : public Ope {
  public:
-  OpeSubEq(int dom, OpePtr a, OpePtr b) : Ope(dom), a(std::move(a)), b(std::move(b)) {}
+  OpeSubEq(int dom, OpePtr a_, OpePtr b_) : Ope(dom), a(std::move(a_)), b(std::move(b_)) {
+    vc = a->vc && b->vc;
+    dc = a->dc && b->dc;
+    dz = a->dz && b->dz;
+  }
+  std::vector<const Ope*> kids() const override { return {a.get(), b.get()}; }
   Term action(EvalState& st, const Term* cv) const override { return t_sub(a->eval(st), b->eval(st), cv); }
   OpePtr a, b;
 };
@@ -273,23 +330,27 @@ int System::add_var(const std::string& name, Field* f) {
     throw KdError(KD_ERR_ARG, "No indices allowed in names of variables");
   for (int dd = dom_min; dd <= dom_max; dd++)
     if (!f->d[dd].base.def) throw KdError(KD_ERR_STATE, "unknown field without a basis (call std_base)");
+  tcache_.clear();  // a new symbol changes the trees that can follow
   vars_.push_back({bare(name), f});
   nbr_unknowns_ = -1;
   return static_cast<int>(vars_.size()) - 1;
 }
 
 int System::add_var_double(const std::string& name, double value) {
+  tcache_.clear();  // a new symbol changes the trees that can follow
   vdoubles_.push_back({bare(name), value});
   nbr_unknowns_ = -1;
   return static_cast<int>(vdoubles_.size()) - 1;
 }
 
 int System::add_cst(const std::string& name, double value) {
+  tcache_.clear();  // a new symbol changes the trees that can follow
   csts_.push_back({bare(name), false, value, nullptr});
   return static_cast<int>(csts_.size()) - 1;
 }
 
 int System::add_cst_field(const std::string& name, Field* f) {
+  tcache_.clear();  // a new symbol changes the trees that can follow
   csts_.push_back({bare(name), true, 0.0, f});
   return static_cast<int>(csts_.size()) - 1;
 }
@@ -302,6 +363,7 @@ void System::add_def(int dom, const std::string& text) {
     return;
   }
   DefInfo df{bare(l), dom, parse_ope(*this, dom, r, -1)};
+  tcache_.clear();  // a new symbol changes the trees that can follow
   defs_.push_back(df);
 }
 
@@ -315,6 +377,9 @@ void System::add_eq_inside(int dom, const std::string& text) {
   eq.text = text;
   eq.lhs = (bare(r) == "0") ? parse_ope(*this, dom, l, -1)
                             : std::make_shared<OpeSubEq>(dom, parse_ope(*this, dom, l, -1), parse_ope(*this, dom, r, -1));
+  mark_tangent_frontier(eq.lhs.get());
+  if (eq.rhs) mark_tangent_frontier(eq.rhs.get());
+  tcache_.clear();
   eqs_.push_back(eq);
   nbr_conditions_ = -1;
 }
@@ -331,6 +396,9 @@ void System::add_eq_bc(int dom, int bound, const std::string& text) {
   eq.lhs = (bare(r) == "0") ? parse_ope(*this, dom, l, bound)
                             : std::make_shared<OpeSubEq>(dom, parse_ope(*this, dom, l, bound),
                                                          parse_ope(*this, dom, r, bound));
+  mark_tangent_frontier(eq.lhs.get());
+  if (eq.rhs) mark_tangent_frontier(eq.rhs.get());
+  tcache_.clear();
   eqs_.push_back(eq);
   nbr_conditions_ = -1;
 }
@@ -351,6 +419,9 @@ void System::add_eq_matching(int dom, int bound, const std::string& text) {
     eq.lhs = parse_ope(*this, dom, text, bound);
     eq.rhs = parse_ope(*this, eq.other_dom, text, eq.other_bound);
   }
+  mark_tangent_frontier(eq.lhs.get());
+  if (eq.rhs) mark_tangent_frontier(eq.rhs.get());
+  tcache_.clear();
   eqs_.push_back(eq);
   nbr_conditions_ = -1;
 }
@@ -544,6 +615,7 @@ void System::jacobian(double* d_J, long long ld, bool reuse) {
       st.seed_dom = dd;
       st.seed = DVal::from_coef(ctx, &sp->dom(dd), B, seeds, base);
       st.vcache = &vcache_;
+      st.tcache = cache_tangents_ ? &tcache_ : nullptr;
       int col0 = col0_[{static_cast<int>(v), dd}];
       double* Jblock = d_J + static_cast<long long>(col0) * ld;
       for (auto& eq : eqs_) {

@@ -6,6 +6,7 @@
 // (xx_to_vars, src/System_of_eqs/system_of_eqs.cpp:597).
 #pragma once
 #include <map>
+#include <tuple>
 #include <unordered_map>
 #include <memory>
 #include <string>
@@ -74,6 +75,26 @@ struct ValueCache {
   void store(const Ope* node, const Term& t);
 };
 
+// Tangents of the outermost iterate-independent nodes (Ope::cache_der),
+// per seed block: kept from one Jacobian assembly to the next, so that the
+// linear parts of the equations (Laplacians of the unknowns, matching and
+// boundary conditions, ...) are computed once per system.
+struct TangentCache {
+  struct Entry {
+    bool is_double = false;
+    double dd = 0.0;
+    std::vector<DVal> dt;
+  };
+  std::map<std::tuple<const Ope*, int, int>, Entry> ders;
+  DeviceArena arena{size_t(256) << 20};
+  void clear() {
+    ders.clear();
+    arena.reset();
+  }
+  // Deep copy of t's tangent into the arena.
+  void store(Context* ctx, const Ope* node, int var, int dom, const Term& t);
+};
+
 struct EvalState {
   System* sys = nullptr;
   bool with_der = false;
@@ -85,6 +106,7 @@ struct EvalState {
   std::map<std::pair<int, int>, Term> def_cache;
   ValueCache* vcache = nullptr;  // node values: recorded (record) or reused (with_der)
   bool record = false;
+  TangentCache* tcache = nullptr;  // tangents of iterate-independent nodes (with_der)
 
   Term var_term(int which, int dom);
   Term var_double_term(int which, int dom);
@@ -146,6 +168,12 @@ class System {
   // reuse: take node values from the preceding residual(..., true) at the
   // same iterate; otherwise a value pass is run first.
   void jacobian(double* d_J, long long ld, bool reuse = false);
+  // Keep the tangents of iterate-independent subtrees between assemblies
+  // (default on; off frees them).
+  void set_tangent_cache(bool on) {
+    cache_tangents_ = on;
+    if (!on) tcache_.clear();
+  }
   // J * x for a device vector x (System_of_eqs::do_JX, solver.cpp:87).
   void jx(const double* d_x, double* d_out);
   // var = old - (fields built from x)  (do_newton's update, src_par/do_newton.cpp:397-414)
@@ -195,6 +223,8 @@ class System {
   std::map<std::pair<int, int>, CsrTable> xmaps_;      // affecte_tau maps
   std::map<std::vector<int>, CsrTable> tables_;
   ValueCache vcache_;
+  TangentCache tcache_;
+  bool cache_tangents_ = true;
 
   void compute_unknowns();
   void apply(Equation& eq, EvalState& st, Term& lhs, Term& rhs, bool do_lhs, bool do_rhs);

@@ -294,7 +294,14 @@ Term comp_by_comp(const Term& t, const std::function<DVal(const DVal&)>& f, cons
 
 class OpeBin : public Ope {
  public:
-  OpeBin(int dom, char op, OpePtr a, OpePtr b) : Ope(dom), op(op), a(std::move(a)), b(std::move(b)) {}
+  OpeBin(int dom, char op, OpePtr a_, OpePtr b_) : Ope(dom), op(op), a(std::move(a_)), b(std::move(b_)) {
+    vc = a->vc && b->vc;
+    dz = a->dz && b->dz;
+    if (op == '+' || op == '-') dc = a->dc && b->dc;
+    else if (op == '*') dc = (a->dz || (a->dc && b->vc)) && (b->dz || (b->dc && a->vc));  // a'b + ab'
+    else dc = (a->dz || a->dc) && b->dz && b->vc;  // (a'b - ab')/b^2 with b constant
+  }
+  std::vector<const Ope*> kids() const override { return {a.get(), b.get()}; }
   Term action(EvalState& st, const Term* cv) const override {
     Term x = a->eval(st);
     Term y = b->eval(st);
@@ -311,14 +318,24 @@ class OpeBin : public Ope {
 
 class OpeMinus : public Ope {
  public:
-  OpeMinus(int dom, OpePtr a) : Ope(dom), a(std::move(a)) {}
+  OpeMinus(int dom, OpePtr a_) : Ope(dom), a(std::move(a_)) {
+    vc = a->vc;
+    dc = a->dc;
+    dz = a->dz;
+  }
+  std::vector<const Ope*> kids() const override { return {a.get()}; }
   Term action(EvalState& st, const Term* cv) const override { return t_neg(a->eval(st), cv); }
   OpePtr a;
 };
 
 class OpePow : public Ope {
  public:
-  OpePow(int dom, int n, OpePtr a) : Ope(dom), n(n), a(std::move(a)) {}
+  OpePow(int dom, int n, OpePtr a_) : Ope(dom), n(n), a(std::move(a_)) {
+    vc = a->vc;
+    dz = a->dz;
+    dc = a->dz || (a->vc && a->dc);
+  }
+  std::vector<const Ope*> kids() const override { return {a.get()}; }
   Term action(EvalState& st, const Term* cv) const override { return term_pow(a->eval(st), n, cv); }
   int n;
   OpePtr a;
@@ -328,7 +345,12 @@ class OpePow : public Ope {
 class OpeUnary : public Ope {
  public:
   enum Kind { LAP, DN, DR, MULTR, DIVR, DIVSINT, MULTSINT, DIVCOST };
-  OpeUnary(int dom, Kind k, int bound, OpePtr a) : Ope(dom), kind(k), bound(bound), a(std::move(a)) {}
+  OpeUnary(int dom, Kind k, int bound, OpePtr a_) : Ope(dom), kind(k), bound(bound), a(std::move(a_)) {
+    vc = a->vc;  // linear operators: the tangent is the operator of the tangent
+    dc = a->dc;
+    dz = a->dz;
+  }
+  std::vector<const Ope*> kids() const override { return {a.get()}; }
   Term action(EvalState& st, const Term* cv) const override {
     Term t = a->eval(st);
     switch (kind) {
@@ -354,7 +376,12 @@ class OpeUnary : public Ope {
 class OpeFunc : public Ope {
  public:
   enum Kind { EXP, SQRT, LOG };
-  OpeFunc(int dom, Kind k, OpePtr a) : Ope(dom), kind(k), a(std::move(a)) {}
+  OpeFunc(int dom, Kind k, OpePtr a_) : Ope(dom), kind(k), a(std::move(a_)) {
+    vc = a->vc;
+    dz = a->dz;
+    dc = a->dz || (a->vc && a->dc);
+  }
+  std::vector<const Ope*> kids() const override { return {a.get()}; }
   Term action(EvalState& st, const Term* cv) const override {
     Term t = a->eval(st);
     if (t.is_double) {
@@ -391,7 +418,12 @@ class OpeFunc : public Ope {
 // grad(scalar): Cartesian components der_abs(1..3) (Domain::grad_term_eq)
 class OpeGrad : public Ope {
  public:
-  OpeGrad(int dom, OpePtr a) : Ope(dom), a(std::move(a)) {}
+  OpeGrad(int dom, OpePtr a_) : Ope(dom), a(std::move(a_)) {
+    vc = a->vc;
+    dc = a->dc;
+    dz = a->dz;
+  }
+  std::vector<const Ope*> kids() const override { return {a.get()}; }
   Term action(EvalState& st, const Term* cv) const override {
     Term t = a->eval(st);
     if (t.is_double || t.vt.size() != 1) throw KdError(KD_ERR_UNSUPPORTED, "grad only defined for scalars");
@@ -413,7 +445,12 @@ class OpeGrad : public Ope {
 // scal(a, b): flat scalar product of two Cartesian vectors (Ope_scal)
 class OpeScal : public Ope {
  public:
-  OpeScal(int dom, OpePtr a, OpePtr b) : Ope(dom), a(std::move(a)), b(std::move(b)) {}
+  OpeScal(int dom, OpePtr a_, OpePtr b_) : Ope(dom), a(std::move(a_)), b(std::move(b_)) {
+    vc = a->vc && b->vc;
+    dz = a->dz && b->dz;
+    dc = (a->dz || (a->dc && b->vc)) && (b->dz || (b->dc && a->vc));
+  }
+  std::vector<const Ope*> kids() const override { return {a.get(), b.get()}; }
   Term action(EvalState& st, const Term* cv) const override {
     Term x = a->eval(st);
     Term y = b->eval(st);
@@ -442,7 +479,12 @@ class OpeScal : public Ope {
 // partial_i (Cartesian derivative of each component), i = x, y, z
 class OpePartial : public Ope {
  public:
-  OpePartial(int dom, int i, OpePtr a) : Ope(dom), i(i), a(std::move(a)) {}
+  OpePartial(int dom, int i, OpePtr a_) : Ope(dom), i(i), a(std::move(a_)) {
+    vc = a->vc;
+    dc = a->dc;
+    dz = a->dz;
+  }
+  std::vector<const Ope*> kids() const override { return {a.get()}; }
   Term action(EvalState& st, const Term* cv) const override {
     int ii = i;
     return comp_by_comp(a->eval(st), [ii](const DVal& v) { return v.der_abs(ii); }, cv);
@@ -454,7 +496,13 @@ class OpePartial : public Ope {
 class OpeLeaf : public Ope {
  public:
   enum Kind { VAR, VAR_DOUBLE, CST, HARD, DEF };
-  OpeLeaf(int dom, Kind k, int which, double v = 0.0) : Ope(dom), kind(k), which(which), val(v) {}
+  OpeLeaf(int dom, Kind k, int which, double v = 0.0) : Ope(dom), kind(k), which(which), val(v) {
+    // unknowns: tangent = the seed (or 0); constants: zero tangent; numbers:
+    // constant value; definitions: not classified
+    vc = (k == HARD);
+    dc = (k != DEF);
+    dz = (k == CST || k == HARD);
+  }
   Term action(EvalState& st, const Term* cv) const override;
   bool cacheable() const override { return false; }
   Kind kind;
@@ -478,6 +526,17 @@ Term OpeLeaf::action(EvalState& st, const Term*) const {
     }
   }
 }
+
+void mark_tangent_frontier_rec(const Ope* n, bool parent_dc) {
+  n->cache_der = n->dc && !n->dz && !parent_dc && n->cacheable();
+  for (const Ope* k : n->kids()) mark_tangent_frontier_rec(k, n->dc);
+}
+
+}  // namespace
+
+void mark_tangent_frontier(const Ope* root) { mark_tangent_frontier_rec(root, false); }
+
+namespace {
 
 // ----------------------------------------------------------------- parser --
 int count_char(const std::string& s, char c) {

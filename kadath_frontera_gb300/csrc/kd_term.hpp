@@ -74,8 +74,20 @@ class Ope {
   virtual Term action(EvalState& st, const Term* cv) const = 0;
   // Leaves are cheap (views of fields or doubles) and are not cached.
   virtual bool cacheable() const { return true; }
+  virtual std::vector<const Ope*> kids() const { return {}; }
   int dom;
+  // Dependence classes, set at construction from the children:
+  //   vc  the value does not depend on the iterate nor on constant fields;
+  //   dc  the tangent does not depend on the iterate (only on the seeds):
+  //       linear operators of unknowns, products with constant values, ...
+  //   dz  the tangent is identically zero.
+  bool vc = false, dc = false, dz = false;
+  // Outermost dc node of its tree: its batched tangents are kept from one
+  // Jacobian assembly to the next (set by mark_tangent_frontier).
+  mutable bool cache_der = false;
 };
+
+void mark_tangent_frontier(const Ope* root);
 using OpePtr = std::shared_ptr<Ope>;
 
 // Parses an expression for domain `dom` (System_of_eqs::give_ope,

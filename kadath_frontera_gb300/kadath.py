@@ -83,6 +83,7 @@ def _declare_system(lib):
         "kd_system_residual": (I, [P, DP]),
         "kd_system_check_equations": (I, [P, DP]),
         "kd_system_jacobian": (I, [P, DP]),
+        "kd_system_cache_tangents": (I, [P, I]),
         "kd_system_jacobian_device": (I, [P, P, C.c_longlong]),
         "kd_system_update": (I, [P, DP]),
         "kd_newton_step": (I, [P, C.POINTER(NewtonOpts), C.POINTER(NewtonReport)]),
@@ -343,6 +344,11 @@ class System_of_eqs:
         out = np.zeros((n, n), order="F")
         self.ctx.check(_L().kd_system_jacobian(self.h, out.ctypes.data_as(C.POINTER(C.c_double))))
         return np.asfortranarray(out.reshape((n, n), order="F"))
+
+    def cache_tangents(self, on=True):
+        """Keep the tangents of iterate-independent subtrees between Jacobian
+        assemblies (on by default); off frees them."""
+        self.ctx.check(_L().kd_system_cache_tangents(self.h, 1 if on else 0))
 
     def do_col_J(self, cc):
         """One column of the Jacobian (System_of_eqs::do_col_J)."""

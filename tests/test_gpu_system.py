@@ -221,3 +221,24 @@ def test_star_mixed_precision_newton_matches_fp64(ctx):
                 ga, gb = fa.get_coef(d), fb.get_coef(d)
                 assert np.linalg.norm(ga - gb) <= 1e-10 * max(np.linalg.norm(ga), 1e-12)
     assert da
+
+
+def test_star_tangent_cache_is_exact(ctx):
+    """Tangents of iterate-independent subtrees kept from the first assembly
+    give bitwise the same Jacobian, at a later iterate, as a system that
+    recomputes every tangent; the iterates agree bitwise too."""
+    from kadath_frontera_gb300 import workloads
+    res = (9, 5, 4)
+    a = workloads.star(res=res)
+    b = workloads.star(res=res)
+    b.syst.cache_tangents(False)
+    for it in range(2):
+        da, _ = a.syst.do_newton(1e-10)
+        db, _ = b.syst.do_newton(1e-10)
+        assert da == db
+    Ja = a.syst.jacobian()
+    Jb = b.syst.jacobian()
+    assert np.array_equal(Ja, Jb)
+    for (nm, fa), (_, fb) in zip(a.unknowns, b.unknowns):
+        for d in range(a.space.get_nbr_domains()):
+            assert np.array_equal(fa.get_coef(d), fb.get_coef(d)), (nm, d)
