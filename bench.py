@@ -243,62 +243,94 @@ def run_gpu(args, ws, rank, local):
     N = syst.get_nbr_unknowns()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")  # 256 MB > L2
 
-    def one_step(mode, timed_events=True):
+    def one_solve(mode):
+        """A complete Newton solve from the initial guess to |F| <= precision,
+        with every cache that outlives a step (the tangents of
+        iterate-independent subtrees) cleared first: the first step pays for
+        building it.  Returns (ms, number of updates, per-call reports)."""
         wl.restore()
+        syst.cache_tangents(False)
+        syst.cache_tangents(True)
         flush.zero_()
         torch.cuda.synchronize()
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
         ev0.record(stream)
-        done, err = syst.do_newton(args.precision, lu_mode=mode)
+        reps = []
+        for _ in range(20):
+            done, err = syst.do_newton(args.precision, lu_mode=mode)
+            reps.append(dict(syst.last_report))
+            if done:
+                break
         ev1.record(stream)
         ev1.synchronize()
-        rep = dict(syst.last_report)
-        return ev0.elapsed_time(ev1), rep
+        if not done:
+            raise RuntimeError(f"Newton did not converge (mode {mode}, |F| = {err:.3e})")
+        return ev0.elapsed_time(ev1), len(reps) - 1, reps
 
     modes = {"mixed": KD.KD_LU_TF32_IR, "fp64": KD.KD_LU_FP64}
     # warm-up: builds matrices, tables, seeds, cuBLAS handles
     for _ in range(args.warmup):
         for m in modes.values():
-            one_step(m)
+            one_solve(m)
     results = {}
-    launches0 = ctx.launches
     barrier(ws)
     with ClockSampler(local) as clk:
         for name, m in modes.items():
-            times, reps = [], []
-            for _ in range(args.steps if name == "mixed" else max(1, args.fp64_steps)):
-                t, rep = one_step(m)
-                times.append(t)
-                reps.append(rep)
-            results[name] = (times, reps)
+            runs = [one_solve(m) for _ in range(args.steps if name == "mixed" else max(1, args.fp64_steps))]
+            results[name] = runs
     barrier(ws)
-    launches_mixed = sum(r["kernel_launches"] for r in results["mixed"][1]) / len(results["mixed"][1])
-    mixed_ms = max_over_ranks(ws, statistics.mean(results["mixed"][0]))
-    fp64_ms = max_over_ranks(ws, statistics.mean(results["fp64"][0]))
 
-    # end-to-end through the C ABI with host buffers (pinned), mixed LU
+    def per_step(runs):
+        return statistics.mean(ms / max(upd, 1) for ms, upd, _ in runs)
+
+    def step_split(runs):
+        """(first step of a solve, later steps) wall times from the reports."""
+        first, later = [], []
+        for _, _, reps in runs:
+            upd = [r for r in reps if not r["converged"]]
+            tot = [r["t_residual_ms"] + r["t_assembly_ms"] + r["t_factor_ms"] + r["t_solve_ms"] + r["t_update_ms"]
+                   for r in upd]
+            if tot:
+                first.append(tot[0])
+                later.extend(tot[1:])
+        return (statistics.mean(first) if first else None, statistics.mean(later) if later else None)
+
+    mixed_ms = max_over_ranks(ws, per_step(results["mixed"]))
+    fp64_ms = max_over_ranks(ws, per_step(results["fp64"]))
+    updates = results["mixed"][0][1]
+    launches_mixed = statistics.mean(sum(r["kernel_launches"] for r in reps) / max(upd, 1)
+                                     for _, upd, reps in results["mixed"])
+
+    # end-to-end through the C ABI with host buffers (pinned), mixed LU:
+    # upload of the initial guess, the solve, download of the solution
     host = [[torch.from_numpy(v).pin_memory().numpy() for v in per] for per in wl.initial_host]
     h2d = sum(v.nbytes for per in host for v in per)
     e2e_times = []
     d2h = 0
     for _ in range(args.steps):
+        syst.cache_tangents(False)
+        syst.cache_tangents(True)
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         wl.upload_initial(host)
-        syst.do_newton(args.precision, lu_mode=modes["mixed"])
+        n_upd = 0
+        for _ in range(20):
+            done, _ = syst.do_newton(args.precision, lu_mode=modes["mixed"])
+            if done:
+                break
+            n_upd += 1
         out = wl.download()
-        e2e_times.append(1e3 * (time.perf_counter() - t0))
+        e2e_times.append(1e3 * (time.perf_counter() - t0) / max(n_upd, 1))
         d2h = sum(v.nbytes for per in out for v in per)
     e2e_ms = max_over_ranks(ws, statistics.mean(e2e_times))
 
     # one instrumented step per mode: per-category kernel time and work
     prof = {}
     for name, m in modes.items():
-        wl.restore()
         KD.profile_enable(ctx, True)
-        syst.do_newton(args.precision, lu_mode=m)
+        one_solve(m)
         prof[name] = KD.profile_read(ctx)
         KD.profile_enable(ctx, False)
 
@@ -312,19 +344,32 @@ def run_gpu(args, ws, rank, local):
     # the tensor-core trailing update, for reference next to the dominant kernel
     gemm = prof["mixed"].get("lu_gemm")
     roof_gemm = roofline_for("lu_gemm", gemm, peaks, peak_kind, N) if gemm and gemm["launches"] else None
-    rep0 = results["mixed"][1][-1]
-    rep64 = results["fp64"][1][-1]
+    rep0 = results["mixed"][-1][2][0]
+    rep64 = results["fp64"][-1][2][0]
+    first_m, later_m = step_split(results["mixed"])
+    first_f, later_f = step_split(results["fp64"])
     line = {
         "metric": METRIC, "value": mixed_ms, "unit": "ms", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": mixed_ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64 (LU trailing update tf32, refined to f64)", "data": "synthetic",
         "config": {"workload": workload_label(args.workload), "N": N, "precision": args.precision,
-                   "l2": "flushed between steps (256 MB write)", "parallelism": "replicas" if ws > 1 else "single"},
+                   "step": "mean Newton step of complete solves from the initial guess to |F| <= precision "
+                           "(one timed unit = one solve; caches that outlive a step cleared per solve)",
+                   "newton_updates_per_solve": updates, "solves_timed": args.steps,
+                   "l2": "flushed between solves (256 MB write); the 1.2 GB Jacobian exceeds L2 within a solve",
+                   "parallelism": "replicas" if ws > 1 else "single"},
         "fp64_ms_per_step": fp64_ms, "mixed_speedup_vs_fp64": fp64_ms / mixed_ms if mixed_ms > 0 else None,
-        "phases_ms": {"mixed": {k: rep0[k] for k in ("t_residual_ms", "t_assembly_ms", "t_factor_ms", "t_solve_ms",
-                                                      "t_update_ms")},
-                      "fp64": {k: rep64[k] for k in ("t_residual_ms", "t_assembly_ms", "t_factor_ms", "t_solve_ms",
-                                                      "t_update_ms")}},
+        "first_step_ms": {"mixed": first_m, "fp64": first_f},
+        "later_step_ms": {"mixed": later_m, "fp64": later_f},
+        "phases_ms_first_step": {
+            "mixed": {k: rep0[k] for k in ("t_residual_ms", "t_assembly_ms", "t_factor_ms", "t_solve_ms",
+                                           "t_update_ms")},
+            "fp64": {k: rep64[k] for k in ("t_residual_ms", "t_assembly_ms", "t_factor_ms", "t_solve_ms",
+                                          "t_update_ms")}},
+        "phases_ms_later_step": {
+            "mixed": {k: results["mixed"][-1][2][1][k] for k in ("t_residual_ms", "t_assembly_ms", "t_factor_ms",
+                                                                 "t_solve_ms", "t_update_ms")}}
+        if len(results["mixed"][-1][2]) > 2 else None,
         "refine": {"iters": rep0["refine_iters"], "rel_residual": rep0["refine_rel_residual"]},
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches_mixed),
