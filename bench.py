@@ -101,15 +101,21 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def dist_setup():
+def dist_setup(backend=None):
+    """Replicas: one process per GPU (torchrun environment).  The path itself
+    has no collective; the process group only carries the barrier and the
+    max-over-ranks timing.  backend: "nccl" on GPUs, "gloo" for CPU tests."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if ws > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if backend is None:
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
     return ws, rank, local
 
 
@@ -124,7 +130,8 @@ def max_over_ranks(ws, x):
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], device="cuda", dtype=torch.float64)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], device=dev, dtype=torch.float64)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
