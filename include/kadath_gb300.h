@@ -206,6 +206,12 @@ int kd_system_jacobian(kd_system* s, double* J);
  * Jacobian at every step (do_col_J, src/System_of_eqs/solver.cpp:120). */
 int kd_system_cache_tangents(kd_system* s, int enable);
 int kd_system_jacobian_device(kd_system* s, double* dJ, long long ld);
+/* do_JX (src/System_of_eqs/solver.cpp:87-118): y = J x without forming J,
+ * every unknown seeded by x through affecte_tau (xx_to_ders,
+ * src/System_of_eqs/system_of_eqs.cpp:557) in one tangent pass.  Host
+ * vectors of length nbr_unknowns; the _device form takes device vectors. */
+int kd_system_jx(kd_system* s, const double* x, double* y);
+int kd_system_jx_device(kd_system* s, const double* dx, double* dy);
 /* xx_to_vars + var = old - x (src_par/do_newton.cpp:397-414), host x. */
 int kd_system_update(kd_system* s, const double* x);
 
@@ -236,6 +242,13 @@ typedef struct kd_newton_report {
  * include/system_of_eqs.hpp:871).  Returns KD_OK and fills rep; the fields
  * registered with add_var are updated in place on the device. */
 int kd_newton_step(kd_system* s, const kd_newton_opts* opts, kd_newton_report* rep);
+/* System_of_eqs::do_newton_with_linesearch (src_par/do_newton.cpp:454-516):
+ * Newton direction p = J^-1 F, rescaled when max(p) > stepmax, then fields
+ * = old - lambda p with lambda backtracked (quadratic, then cubic model of
+ * f = sum F^2, sufficient decrease 1e-4) for at most ntrymax tries.  lambda
+ * (may be NULL) receives the last lambda; rep->converged as do_newton. */
+int kd_newton_step_linesearch(kd_system* s, const kd_newton_opts* opts, int ntrymax, double stepmax,
+                              kd_newton_report* rep, double* lambda);
 
 /* ---- dense LU (Matrice::set_lu / solve, src/Matrice/matrice.cpp:192-249) */
 typedef struct kd_lu kd_lu;

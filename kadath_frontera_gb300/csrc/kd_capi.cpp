@@ -514,6 +514,33 @@ int kd_system_jacobian_device(kd_system* s, double* dJ, long long ld) {
   });
 }
 
+int kd_system_jx_device(kd_system* s, const double* dx, double* dy) {
+  SYS_GUARD(s) {
+    if (!dx || !dy) throw kd::KdError(KD_ERR_ARG, "null vector");
+    s->sys->jx(dx, dy);
+    kd::cuda_check(cudaStreamSynchronize(s->sp->ctx->c->stream()), "sync");
+  });
+}
+
+int kd_system_jx(kd_system* s, const double* x, double* y) {
+  SYS_GUARD(s) {
+    if (!x || !y) throw kd::KdError(KD_ERR_ARG, "null vector");
+    kd::Context* c = s->sp->ctx->c.get();
+    if (s->sys->nbr_conditions() < 0) s->sys->residual(nullptr);
+    const int n = s->sys->nbr_unknowns();
+    double* d = nullptr;
+    kd::cuda_check(cudaMalloc(&d, sizeof(double) * 2 * n), "cudaMalloc(jx)");
+    struct Free {
+      double* p;
+      ~Free() { cudaFree(p); }
+    } guard{d};
+    kd::cuda_check(cudaMemcpyAsync(d, x, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream()), "H2D x");
+    s->sys->jx(d, d + n);
+    kd::cuda_check(cudaMemcpyAsync(y, d + n, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream()), "D2H y");
+    kd::cuda_check(cudaStreamSynchronize(c->stream()), "sync");
+  });
+}
+
 int kd_system_jacobian(kd_system* s, double* J) {
   SYS_GUARD(s) {
     if (!J) throw kd::KdError(KD_ERR_ARG, "null output");
@@ -539,28 +566,49 @@ int kd_system_update(kd_system* s, const double* x) {
   });
 }
 
+namespace {
+kd::NewtonOpts to_opts(const kd_newton_opts* opts) {
+  kd::NewtonOpts o;
+  o.precision = opts->precision;
+  o.lu_mode = opts->lu_mode;
+  o.gmres_tol = opts->gmres_tol > 0 ? opts->gmres_tol : 1e-14;
+  o.max_refine = opts->max_refine > 0 ? opts->max_refine : 50;
+  o.graph_capture = opts->graph_capture;
+  return o;
+}
+
+void to_report(const kd::NewtonReport& r, kd_newton_report* rep) {
+  rep->error = r.error;
+  rep->converged = r.converged;
+  rep->n = r.n;
+  rep->t_residual_ms = r.t_residual_ms;
+  rep->t_assembly_ms = r.t_assembly_ms;
+  rep->t_factor_ms = r.t_factor_ms;
+  rep->t_solve_ms = r.t_solve_ms;
+  rep->t_update_ms = r.t_update_ms;
+  rep->refine_iters = r.refine_iters;
+  rep->refine_rel_residual = r.refine_rel_residual;
+  rep->kernel_launches = r.kernel_launches;
+}
+}  // namespace
+
 int kd_newton_step(kd_system* s, const kd_newton_opts* opts, kd_newton_report* rep) {
   SYS_GUARD(s) {
     if (!opts || !rep) throw kd::KdError(KD_ERR_ARG, "null argument");
-    kd::NewtonOpts o;
-    o.precision = opts->precision;
-    o.lu_mode = opts->lu_mode;
-    o.gmres_tol = opts->gmres_tol > 0 ? opts->gmres_tol : 1e-14;
-    o.max_refine = opts->max_refine > 0 ? opts->max_refine : 50;
-    o.graph_capture = opts->graph_capture;
     kd::NewtonReport r;
-    s->newton->step(o, r);
-    rep->error = r.error;
-    rep->converged = r.converged;
-    rep->n = r.n;
-    rep->t_residual_ms = r.t_residual_ms;
-    rep->t_assembly_ms = r.t_assembly_ms;
-    rep->t_factor_ms = r.t_factor_ms;
-    rep->t_solve_ms = r.t_solve_ms;
-    rep->t_update_ms = r.t_update_ms;
-    rep->refine_iters = r.refine_iters;
-    rep->refine_rel_residual = r.refine_rel_residual;
-    rep->kernel_launches = r.kernel_launches;
+    s->newton->step(to_opts(opts), r);
+    to_report(r, rep);
+  });
+}
+
+int kd_newton_step_linesearch(kd_system* s, const kd_newton_opts* opts, int ntrymax, double stepmax,
+                              kd_newton_report* rep, double* lambda) {
+  SYS_GUARD(s) {
+    if (!opts || !rep) throw kd::KdError(KD_ERR_ARG, "null argument");
+    if (ntrymax < 1 || !(stepmax > 0)) throw kd::KdError(KD_ERR_ARG, "need ntrymax >= 1 and stepmax > 0");
+    kd::NewtonReport r;
+    s->newton->step_linesearch(to_opts(opts), ntrymax, stepmax, r, lambda);
+    to_report(r, rep);
   });
 }
 

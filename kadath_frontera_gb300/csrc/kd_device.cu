@@ -243,6 +243,27 @@ cudaError_t launch_scatter_seeds(double* out, long long stride, int nent, const 
   return cudaGetLastError();
 }
 
+// One CTA, fixed summation order (deterministic): op 0 = sum of squares,
+// op 1 = maximum (signed).
+__global__ void reduce1_kernel(const double* __restrict__ x, long long n, int op, double* out) {
+  __shared__ double part[1024];
+  double acc = op == 0 ? 0.0 : -INFINITY;
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) acc = op == 0 ? fma(x[i], x[i], acc) : fmax(acc, x[i]);
+  part[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (static_cast<int>(threadIdx.x) < w)
+      part[threadIdx.x] = op == 0 ? part[threadIdx.x] + part[threadIdx.x + w] : fmax(part[threadIdx.x], part[threadIdx.x + w]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = part[0];
+}
+
+cudaError_t launch_reduce1(const double* x, long long n, int op, double* out_scalar, cudaStream_t s) {
+  reduce1_kernel<<<1, 1024, 0, s>>>(x, n, op, out_scalar);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_absmax(const double* x, long long n, double* out_scalar, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(out_scalar, 0, sizeof(double), s);
   if (e != cudaSuccess) return e;

@@ -86,5 +86,7 @@ cudaError_t launch_gather_csr(const double* in, long long in_stride, int batch, 
 
 // Sum over the last axis reduction helpers used by residual norms.
 cudaError_t launch_absmax(const double* x, long long n, double* out_scalar, cudaStream_t s);
+// Deterministic single-CTA reduction: op 0 = sum of squares, 1 = max.
+cudaError_t launch_reduce1(const double* x, long long n, int op, double* out_scalar, cudaStream_t s);
 
 }  // namespace kd

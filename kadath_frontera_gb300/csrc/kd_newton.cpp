@@ -1,6 +1,8 @@
 #include "kd_newton.hpp"
 
+#include <algorithm>
 #include <chrono>
+#include <cmath>
 
 namespace kd {
 
@@ -75,6 +77,148 @@ bool Newton::step(const NewtonOpts& o, NewtonReport& rep) {
   rep.refine_rel_residual = lu_->stats.final_rel_residual;
   auto t3 = std::chrono::steady_clock::now();
   sys_->update_from_x(d_F);
+  rep.t_update_ms = ms_since(t3);
+  rep.kernel_launches = ctx->launches - l0;
+  return false;
+}
+
+double Newton::device_scalar(const double* d_x, long long n, int op) {
+  Context* ctx = sys_->ctx;
+  double* d = ctx->scratch().alloc_doubles(1);
+  cuda_check(launch_reduce1(d_x, n, op, d, ctx->stream()), "reduce");
+  ctx->launches++;
+  double h = 0;
+  cuda_check(cudaMemcpyAsync(&h, d, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream()), "D2H");
+  cuda_check(cudaStreamSynchronize(ctx->stream()), "sync");
+  return h;
+}
+
+// compute_f (src_par/do_newton.cpp:594): sum of F^2 of a fresh sec_member.
+double Newton::residual_norm2() {
+  int N = sys_->nbr_conditions();
+  sys_->residual(d_F);
+  return device_scalar(d_F, N, 0);
+}
+
+bool Newton::step_linesearch(const NewtonOpts& o, int ntrymax, double stepmax, NewtonReport& rep,
+                             double* lambda_out) {
+  Context* ctx = sys_->ctx;
+  cudaStream_t s = ctx->stream();
+  long long l0 = ctx->launches;
+  rep = NewtonReport();
+  if (lambda_out) *lambda_out = 0.0;
+  auto t0 = std::chrono::steady_clock::now();
+  if (sys_->nbr_conditions() < 0) sys_->residual(nullptr);
+  const int N = sys_->nbr_conditions();
+  ensure(N);
+  sys_->residual(d_F, true);
+  double* d_err = ctx->scratch().alloc_doubles(1);
+  cuda_check(launch_absmax(d_F, N, d_err, s), "absmax");
+  double err = 0;
+  cuda_check(cudaMemcpyAsync(&err, d_err, sizeof(double), cudaMemcpyDeviceToHost, s), "D2H err");
+  cuda_check(cudaStreamSynchronize(s), "sync residual");
+  rep.t_residual_ms = ms_since(t0);
+  rep.error = err;
+  rep.n = N;
+  if (err < o.precision) {
+    rep.converged = 1;
+    rep.kernel_launches = ctx->launches - l0;
+    return true;
+  }
+  if (sys_->nbr_unknowns() != N) throw KdError(KD_ERR_STATE, "Number of unknowns is different from the number of equations");
+  const double fold = device_scalar(d_F, N, 0);
+  const double slope = -2.0 * fold;
+  if (!(slope < 0.0)) throw KdError(KD_ERR_NOCONV, "line search: the slope is not negative");  // check_negative
+  // p = J^-1 F (compute_p)
+  auto t1 = std::chrono::steady_clock::now();
+  sys_->jacobian(d_J, ld, true);
+  cuda_check(cudaStreamSynchronize(s), "sync assembly");
+  rep.t_assembly_ms = ms_since(t1);
+  lu_->gmres_tol = o.gmres_tol;
+  lu_->gmres_max_iter = o.max_refine;
+  lu_->factor(d_J, ld, N, o.lu_mode);
+  rep.t_factor_ms = lu_->stats.t_factor_ms;
+  lu_->solve(d_F, 0);
+  rep.t_solve_ms = lu_->stats.t_solve_ms;
+  rep.refine_iters = lu_->stats.refine_iters;
+  rep.refine_rel_residual = lu_->stats.final_rel_residual;
+  auto t3 = std::chrono::steady_clock::now();
+  const double pmax = device_scalar(d_F, N, 1);  // max(p), signed as in the reference
+  ctx->scratch().reset();
+  ls_arena_.reset();
+  // old fields and the fields xx_to_vars(p) would give (compute_old_and_var)
+  const int nvar = static_cast<int>(sys_->vars().size());
+  const int nd = sys_->sp->ndom();
+  std::vector<std::vector<DVal>> old(nvar), pv(nvar);
+  std::vector<double> hp(N);
+  cuda_check(cudaMemcpyAsync(hp.data(), d_F, sizeof(double) * N, cudaMemcpyDeviceToHost, s), "D2H p");
+  cuda_check(cudaStreamSynchronize(s), "sync p");
+  const double scale = (pmax > stepmax) ? stepmax / pmax : 1.0;  // rescale in case p is too large
+  {
+    DeviceArena* prev = ctx->redirect_scratch(&ls_arena_);
+    try {
+      for (int v = 0; v < nvar; v++) {
+        Field* f = sys_->vars()[v].f;
+        for (int dd = 0; dd < nd; dd++) {
+          DVal ov = copy_to_arena(ctx, f->val(dd), ls_arena_);
+          old[v].push_back(ov);
+          if (dd < sys_->dom_min || dd > sys_->dom_max) {
+            pv[v].push_back(ov);  // xx_to_vars leaves these domains as they are
+          } else {
+            DVal p = sys_->x_to_field(v, dd, d_F);
+            pv[v].push_back(scale == 1.0 ? p : p * scale);
+          }
+        }
+      }
+    } catch (...) {
+      ctx->redirect_scratch(prev);
+      throw;
+    }
+    ctx->redirect_scratch(prev);
+  }
+  std::vector<double> old_d, p_d;
+  for (int i = 0; i < sys_->n_var_doubles(); i++) {
+    old_d.push_back(sys_->var_double(i));
+    p_d.push_back(hp[i] * scale);
+  }
+  auto update_fields = [&](double lambda) {
+    ctx->scratch().reset();
+    for (int i = 0; i < static_cast<int>(old_d.size()); i++) sys_->set_var_double(i, old_d[i] - lambda * p_d[i]);
+    for (int v = 0; v < nvar; v++) {
+      Field* f = sys_->vars()[v].f;
+      for (int dd = 0; dd < nd; dd++) {
+        DVal nv = old[v][dd] - pv[v][dd] * lambda;
+        f->assign(dd, nv);
+      }
+    }
+    sys_->invalidate_values();
+  };
+  const double lambdamin = 1.0e-10, alpha = 1.0e-4;
+  double lambda = 1.0, lambdatmp = 0.0, lambda2 = 0.0, f2 = 0.0;
+  for (int itry = 1; itry <= ntrymax; ++itry) {
+    update_fields(lambda);
+    const double f = residual_norm2();
+    if (f <= 5.0e-13) break;
+    if (f <= fold + alpha * lambda * slope || lambda <= lambdamin) break;
+    if (lambda == 1.0) {
+      lambdatmp = -0.5 * slope / (f - fold - slope);
+    } else {
+      const double rhs1 = f - fold - lambda * slope;
+      const double rhs2 = f2 - fold - lambda2 * slope;
+      const double a = (rhs1 / (lambda * lambda) - rhs2 / (lambda2 * lambda2)) / (lambda - lambda2);
+      const double b = (-lambda2 * rhs1 / (lambda * lambda) + lambda * rhs2 / (lambda2 * lambda2)) / (lambda - lambda2);
+      if (a == 0.0) lambdatmp = -0.5 * slope / b;
+      const double delta = b * b - 3.0 * a * slope;
+      if (delta < 0.0) throw KdError(KD_ERR_NOCONV, "line search: negative discriminant");  // check_positive
+      lambdatmp = (-b + std::sqrt(delta)) / (3.0 * a);
+      if (lambdatmp > 0.5 * lambda) lambdatmp = 0.5 * lambda;
+    }
+    lambda2 = lambda;
+    f2 = f;
+    lambda = std::max(lambdatmp, 0.1 * lambda);
+    if (itry == ntrymax) update_fields(lambda);
+  }
+  if (lambda_out) *lambda_out = lambda;
   rep.t_update_ms = ms_since(t3);
   rep.kernel_launches = ctx->launches - l0;
   return false;

@@ -33,6 +33,13 @@ class Newton {
   explicit Newton(System* s);
   ~Newton();
   bool step(const NewtonOpts& o, NewtonReport& rep);
+  // System_of_eqs::do_newton_with_linesearch (src_par/do_newton.cpp:454-516,
+  // Numerical Recipes 2007 section 9.7.1): the Newton direction p = J^-1 F
+  // (scaled so that max(p) <= stepmax), then fields = old - lambda p with
+  // lambda backtracked (quadratic, then cubic model of f = sum F^2) until the
+  // sufficient-decrease test holds, at most ntrymax tries.  rep.linesearch_lambda
+  // gets the last lambda.
+  bool step_linesearch(const NewtonOpts& o, int ntrymax, double stepmax, NewtonReport& rep, double* lambda_out);
   // Device buffers of the last step (valid until the next call).
   double* d_F = nullptr;
   double* d_J = nullptr;
@@ -44,6 +51,9 @@ class Newton {
   System* sys_;
   std::unique_ptr<DenseLU> lu_;
   size_t capF_ = 0, capJ_ = 0;
+  DeviceArena ls_arena_{size_t(64) << 20};  // field snapshots of a line search
+  double device_scalar(const double* d_x, long long n, int op);
+  double residual_norm2();
 };
 
 }  // namespace kd

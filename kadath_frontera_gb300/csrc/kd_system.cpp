@@ -130,8 +130,14 @@ Term EvalState::var_term(int which, int dom) {
   t.vt.push_back(vi.f->val(dom));
   if (with_der) {
     t.has_dt = true;
-    if (which == seed_var && dom == seed_dom) t.dt.push_back(seed);
-    else t.dt.push_back(DVal::zeros(sys->ctx, &sys->sp->dom(dom), B));
+    if (jx_seeds) {
+      auto it = jx_seeds->find(std::make_pair(which, dom));
+      t.dt.push_back(it != jx_seeds->end() ? it->second : DVal::zeros(sys->ctx, &sys->sp->dom(dom), B));
+    } else if (which == seed_var && dom == seed_dom) {
+      t.dt.push_back(seed);
+    } else {
+      t.dt.push_back(DVal::zeros(sys->ctx, &sys->sp->dom(dom), B));
+    }
   }
   return t;
 }
@@ -140,7 +146,8 @@ Term EvalState::var_double_term(int which, int dom) {
   Term t = Term::dbl(dom, sys->vdoubles_.at(which).value);
   if (with_der) {
     t.has_dd = true;
-    t.dd = (which == seed_var_double) ? 1.0 : 0.0;
+    if (jx_doubles) t.dd = jx_doubles->at(which);
+    else t.dd = (which == seed_var_double) ? 1.0 : 0.0;
   }
   return t;
 }
@@ -188,34 +195,34 @@ void ValueCache::store(const Ope* node, const Term& t) {
   vals[node] = std::move(v);
 }
 
+DVal copy_to_arena(Context* ctx, const DVal& d, DeviceArena& arena) {
+  DVal c(d.ctx ? d.ctx : ctx, d.dom, d.batch);
+  c.zero = d.zero;
+  c.base = d.base;
+  if (!d.zero) {
+    if (d.in_conf) {
+      const size_t n = static_cast<size_t>(d.npts()) * d.batch;
+      double* p = arena.alloc_doubles(n);
+      cuda_check(cudaMemcpyAsync(p, d.c, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream()), "arena copy");
+      c.c = p;
+      c.in_conf = true;
+    }
+    if (d.in_coef) {
+      const size_t n = static_cast<size_t>(d.ncoefs()) * d.batch;
+      double* p = arena.alloc_doubles(n);
+      cuda_check(cudaMemcpyAsync(p, d.cf, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream()), "arena copy");
+      c.cf = p;
+      c.in_coef = true;
+    }
+  }
+  return c;
+}
+
 void TangentCache::store(Context* ctx, const Ope* node, int var, int dom, const Term& t) {
   Entry e;
   e.is_double = t.is_double;
   e.dd = t.dd;
-  for (const DVal& d : t.dt) {
-    DVal c(d.ctx, d.dom, d.batch);
-    c.zero = d.zero;
-    c.base = d.base;
-    if (!d.zero) {
-      if (d.in_conf) {
-        const size_t n = static_cast<size_t>(d.npts()) * d.batch;
-        double* p = arena.alloc_doubles(n);
-        cuda_check(cudaMemcpyAsync(p, d.c, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream()),
-                   "tangent cache copy");
-        c.c = p;
-        c.in_conf = true;
-      }
-      if (d.in_coef) {
-        const size_t n = static_cast<size_t>(d.ncoefs()) * d.batch;
-        double* p = arena.alloc_doubles(n);
-        cuda_check(cudaMemcpyAsync(p, d.cf, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream()),
-                   "tangent cache copy");
-        c.cf = p;
-        c.in_coef = true;
-      }
-    }
-    e.dt.push_back(c);
-  }
+  for (const DVal& d : t.dt) e.dt.push_back(copy_to_arena(ctx, d, arena));
   ders[std::make_tuple(node, var, dom)] = std::move(e);
 }
 
@@ -632,6 +639,75 @@ void System::jacobian(double* d_J, long long ld, bool reuse) {
     }
 }
 
+// x -> coefficient map of one (variable, domain): affecte_tau
+// (domain_*_affecte_tau.cpp), as a CSR table.
+const CsrTable& System::xmap(int var, int dd) {
+  auto key = std::make_pair(var, dd);
+  auto it = xmaps_.find(key);
+  if (it != xmaps_.end()) return it->second;
+  std::vector<SparseRow> rows;
+  const Domain& d = sp->dom(dd);
+  int used = d.affecte_tau_map(vars_[var].f->d[dd].base, 0, rows);
+  if (used != nunk_[key]) throw KdError(KD_ERR_STATE, "affecte_tau consumes a different number of unknowns");
+  xmaps_[key] = upload_rows(rows);
+  return xmaps_[key];
+}
+
+DVal System::x_to_field(int var, int dd, const double* d_x) {
+  nbr_unknowns();
+  const Domain& d = sp->dom(dd);
+  const CsrTable& t = xmap(var, dd);
+  double* cf = ctx->scratch().alloc_doubles(d.ncoefs());
+  cuda_check(launch_gather_csr(d_x + col0_[std::make_pair(var, dd)], 0, 1, t.nrows, t.rowptr, t.idx, t.w, cf, 0, 1, 1.0,
+                               0, ctx->stream()),
+             "affecte_tau gather");
+  ctx->launches++;
+  return DVal::from_coef(ctx, &d, 1, cf, vars_[var].f->d[dd].base);
+}
+
+void System::jx(const double* d_x, double* d_y) {
+  int N = nbr_unknowns();
+  residual(nullptr, true);  // values at the current fields (they may have changed since the last residual)
+  if (nbr_conditions_ != N) throw KdError(KD_ERR_STATE, "Number of unknowns is different from the number of equations");
+  ctx->scratch().reset();
+  std::vector<double> xd(vdoubles_.size());
+  if (!vdoubles_.empty()) {
+    cuda_check(cudaMemcpyAsync(xd.data(), d_x, sizeof(double) * xd.size(), cudaMemcpyDeviceToHost, ctx->stream()),
+               "D2H x");
+    cuda_check(cudaStreamSynchronize(ctx->stream()), "sync");
+  }
+  // xx_to_ders: the tangent of every unknown is affecte_tau(x)
+  std::map<std::pair<int, int>, DVal> seeds;
+  for (size_t v = 0; v < vars_.size(); v++)
+    for (int dd = dom_min; dd <= dom_max; dd++) {
+      auto key = std::make_pair(static_cast<int>(v), dd);
+      const Domain& d = sp->dom(dd);
+      const CsrTable& t = xmap(static_cast<int>(v), dd);
+      double* cf = ctx->scratch().alloc_doubles(d.ncoefs());
+      cuda_check(launch_gather_csr(d_x + col0_[key], 0, 1, t.nrows, t.rowptr, t.idx, t.w, cf, 0, 1, 1.0, 0,
+                                   ctx->stream()),
+                 "affecte_tau gather");
+      ctx->launches++;
+      seeds[key] = DVal::from_coef(ctx, &d, 1, cf, vars_[v].f->d[dd].base);
+    }
+  EvalState st;
+  st.sys = this;
+  st.with_der = true;
+  st.B = 1;
+  st.jx_seeds = &seeds;
+  st.jx_doubles = &xd;
+  st.vcache = &vcache_;
+  cuda_check(cudaMemsetAsync(d_y, 0, sizeof(double) * N, ctx->stream()), "memset y");
+  for (auto& eq : eqs_) {
+    Term t = eq.lhs->eval(st);
+    export_term(eq, t, true, eq.dom, eq.bound, d_y + eq.row0, 0, 1, 1, 1.0, true);
+    if (eq.kind == Equation::MATCHING) {
+      Term r = eq.rhs->eval(st);
+      export_term(eq, r, true, eq.other_dom, eq.other_bound, d_y + eq.row0, 0, 1, 1, -1.0, true);
+    }
+  }
+}
+
 void System::update_from_x(const double* d_x) {
   int N = nbr_unknowns();
   (void)N;
@@ -659,16 +735,8 @@ void System::update_from_x(const double* d_x) {
         continue;
       }
       auto key = std::make_pair(static_cast<int>(v), dd);
-      auto it = xmaps_.find(key);
-      if (it == xmaps_.end()) {
-        std::vector<SparseRow> rows;
-        int used = d.affecte_tau_map(f->d[dd].base, 0, rows);
-        if (used != nunk_[key]) throw KdError(KD_ERR_STATE, "affecte_tau consumes a different number of unknowns");
-        xmaps_[key] = upload_rows(rows);
-        it = xmaps_.find(key);
-      }
       double* cf = ctx->scratch().alloc_doubles(d.ncoefs());
-      const CsrTable& t = it->second;
+      const CsrTable& t = xmap(static_cast<int>(v), dd);
       cuda_check(launch_gather_csr(d_x + col0_[key], 0, 1, t.nrows, t.rowptr, t.idx, t.w, cf, 0, 1, 1.0, 0,
                                    ctx->stream()),
                  "affecte_tau gather");
@@ -679,12 +747,6 @@ void System::update_from_x(const double* d_x) {
     }
   }
   cuda_check(cudaStreamSynchronize(ctx->stream()), "sync after update");
-}
-
-void System::jx(const double* d_x, double* d_out) {
-  (void)d_x;
-  (void)d_out;
-  throw KdError(KD_ERR_UNSUPPORTED, "matrix-free J*x is served by the assembled Jacobian");
 }
 
 }  // namespace kd

@@ -95,6 +95,9 @@ struct TangentCache {
   void store(Context* ctx, const Ope* node, int var, int dom, const Term& t);
 };
 
+// Deep copy of a DVal's representations into an arena (metadata kept).
+DVal copy_to_arena(Context* ctx, const DVal& d, DeviceArena& arena);
+
 struct EvalState {
   System* sys = nullptr;
   bool with_der = false;
@@ -104,6 +107,10 @@ struct EvalState {
   int seed_var_double = -1;
   DVal seed;               // batch-B coefficient patterns
   std::map<std::pair<int, int>, Term> def_cache;
+  // do_JX: every unknown field seeded at once (tangent = x mapped to
+  // coefficients per (variable, domain)); var doubles get jx_doubles.
+  const std::map<std::pair<int, int>, DVal>* jx_seeds = nullptr;
+  const std::vector<double>* jx_doubles = nullptr;
   ValueCache* vcache = nullptr;  // node values: recorded (record) or reused (with_der)
   bool record = false;
   TangentCache* tcache = nullptr;  // tangents of iterate-independent nodes (with_der)
@@ -168,16 +175,23 @@ class System {
   // reuse: take node values from the preceding residual(..., true) at the
   // same iterate; otherwise a value pass is run first.
   void jacobian(double* d_J, long long ld, bool reuse = false);
+  // do_JX (src/System_of_eqs/solver.cpp:87): y = J x without forming J, one
+  // tangent pass with every unknown seeded by x through affecte_tau.
+  void jx(const double* d_x, double* d_y);
   // Keep the tangents of iterate-independent subtrees between assemblies
   // (default on; off frees them).
   void set_tangent_cache(bool on) {
     cache_tangents_ = on;
     if (!on) tcache_.clear();
   }
-  // J * x for a device vector x (System_of_eqs::do_JX, solver.cpp:87).
-  void jx(const double* d_x, double* d_out);
   // var = old - (fields built from x)  (do_newton's update, src_par/do_newton.cpp:397-414)
   void update_from_x(const double* d_x);
+  // The field xx_to_vars would give variable `var` in domain dd from x
+  // (affecte_tau), allocated from the current scratch arena.
+  DVal x_to_field(int var, int dd, const double* d_x);
+  int n_var_doubles() const { return static_cast<int>(vdoubles_.size()); }
+  // Fields changed outside update_from_x: drop the recorded node values.
+  void invalidate_values() { vcache_.clear(); }
 
   struct VarInfo {
     std::string name;
@@ -233,6 +247,7 @@ class System {
                    long long osf, long long osr, int batch, double alpha, bool accumulate);
   CsrTable upload_rows(const std::vector<SparseRow>& rows);
   const double* seed_block(int var, int dom, int& B, Base& base);
+  const CsrTable& xmap(int var, int dom);
 };
 
 }  // namespace kd

@@ -84,9 +84,11 @@ def _declare_system(lib):
         "kd_system_check_equations": (I, [P, DP]),
         "kd_system_jacobian": (I, [P, DP]),
         "kd_system_cache_tangents": (I, [P, I]),
+        "kd_system_jx": (I, [P, DP, DP]),
         "kd_system_jacobian_device": (I, [P, P, C.c_longlong]),
         "kd_system_update": (I, [P, DP]),
         "kd_newton_step": (I, [P, C.POINTER(NewtonOpts), C.POINTER(NewtonReport)]),
+        "kd_newton_step_linesearch": (I, [P, C.POINTER(NewtonOpts), I, D, C.POINTER(NewtonReport), DP]),
         "kd_lu_create": (I, [P, C.POINTER(P)]),
         "kd_lu_destroy": (I, [P]),
         "kd_lu_factor": (I, [P, P, C.c_longlong, I, I]),
@@ -345,6 +347,13 @@ class System_of_eqs:
         self.ctx.check(_L().kd_system_jacobian(self.h, out.ctypes.data_as(C.POINTER(C.c_double))))
         return np.asfortranarray(out.reshape((n, n), order="F"))
 
+    def do_JX(self, x):
+        """System_of_eqs::do_JX: J x without forming J."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros(self.get_nbr_unknowns())
+        self.ctx.check(_L().kd_system_jx(self.h, _dp(x), _dp(y)))
+        return y
+
     def cache_tangents(self, on=True):
         """Keep the tangents of iterate-independent subtrees between Jacobian
         assemblies (on by default); off frees them."""
@@ -369,6 +378,19 @@ class System_of_eqs:
         self.last_report = rep.as_dict()
         self._J = None
         return bool(rep.converged), rep.error
+
+    def do_newton_with_linesearch(self, precision, ntrymax=10, stepmax=1.0, lu_mode=None, gmres_tol=1e-14,
+                                  max_refine=50):
+        """System_of_eqs::do_newton_with_linesearch: returns (converged, error,
+        last lambda)."""
+        opts = NewtonOpts(precision, self.lu_mode if lu_mode is None else lu_mode, gmres_tol, max_refine, 0)
+        rep = NewtonReport()
+        lam = C.c_double()
+        self.ctx.check(_L().kd_newton_step_linesearch(self.h, C.byref(opts), ntrymax, stepmax, C.byref(rep),
+                                                      C.byref(lam)))
+        self.last_report = rep.as_dict()
+        self._J = None
+        return bool(rep.converged), rep.error, lam.value
 
     def __del__(self):
         try:

@@ -938,6 +938,66 @@ class OSystem:
         return False, err, F, J
 
 
+def newton_linesearch_step(sysm, precision, ntrymax=10, stepmax=1.0):
+    """do_newton_with_linesearch (src_par/do_newton.cpp:454-516; compute_f
+    :594, update_fields :667, compute_old_and_var :676), restated on OSystem.
+    Returns (converged, error, last lambda)."""
+    import scipy.linalg as sla
+    F, J = sysm.jacobian()
+    err = float(np.max(np.abs(F)))
+    if err < precision:
+        return True, err, 0.0
+    fold = float(np.sum(F * F))
+    slope = -2.0 * fold
+    assert slope < 0.0
+    p = sla.lu_solve(sla.lu_factor(J), F)
+    pmax = float(np.max(p))
+    if pmax > stepmax:
+        p = p * (stepmax / pmax)
+    layout, N = sysm.unknown_layout()
+    old = {vi: {dd: f[dd] for dd in range(len(sysm.doms))} for vi, (name, f) in enumerate(sysm.vars)}
+    pv = {vi: dict(old[vi]) for vi in old}  # xx_to_vars leaves the other domains as they are
+    for vi, dd, col, pats in layout:
+        name, f = sysm.vars[vi]
+        d = sysm.doms[dd]
+        M = d.affecte_tau_matrix(f[dd].base)
+        cf = (M @ p[col:col + M.shape[1]]).reshape((1,) + d.nc)
+        pv[vi][dd] = VD(d, 1, cf=cf, base=f[dd].base)
+
+    def update_fields(lam):
+        for vi, (name, f) in enumerate(sysm.vars):
+            for dd in range(len(sysm.doms)):
+                f[dd] = old[vi][dd] - pv[vi][dd] * lam
+
+    lambdamin, alpha = 1.0e-10, 1.0e-4
+    lam, lamtmp, lam2, f2 = 1.0, 0.0, 0.0, 0.0
+    for itry in range(1, ntrymax + 1):
+        update_fields(lam)
+        Fn = sysm.residual()
+        f = float(np.sum(Fn * Fn))
+        if f <= 5.0e-13:
+            break
+        if f <= fold + alpha * lam * slope or lam <= lambdamin:
+            break
+        if lam == 1.0:
+            lamtmp = -0.5 * slope / (f - fold - slope)
+        else:
+            rhs1 = f - fold - lam * slope
+            rhs2 = f2 - fold - lam2 * slope
+            a = (rhs1 / lam ** 2 - rhs2 / lam2 ** 2) / (lam - lam2)
+            b = (-lam2 * rhs1 / lam ** 2 + lam * rhs2 / lam2 ** 2) / (lam - lam2)
+            delta = b * b - 3.0 * a * slope
+            assert delta >= 0.0
+            lamtmp = (-b + math.sqrt(delta)) / (3.0 * a)
+            if lamtmp > 0.5 * lam:
+                lamtmp = 0.5 * lam
+        lam2, f2 = lam, f
+        lam = max(lamtmp, 0.1 * lam)
+        if itry == ntrymax:
+            update_fields(lam)
+    return False, err, lam
+
+
 def scalar_field(doms, value_fn):
     """A Scalar with std_base, values from value_fn(dom) -> (n0,n1,n2) array."""
     out = {}

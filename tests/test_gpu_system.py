@@ -242,3 +242,50 @@ def test_star_tangent_cache_is_exact(ctx):
     for (nm, fa), (_, fb) in zip(a.unknowns, b.unknowns):
         for d in range(a.space.get_nbr_domains()):
             assert np.array_equal(fa.get_coef(d), fb.get_coef(d)), (nm, d)
+
+
+@pytest.mark.parametrize("which", ["toy", "star"])
+def test_do_JX_matches_assembled_jacobian(ctx, which):
+    """do_JX (matrix-free, all unknowns seeded by x through affecte_tau) equals
+    J x with the assembled Jacobian, at the initial guess and after a step."""
+    from kadath_frontera_gb300 import workloads
+    wl = workloads.toy(res=(9, 5, 4)) if which == "toy" else workloads.star(res=(9, 5, 4))
+    n = wl.syst.get_nbr_unknowns()
+    rng = np.random.default_rng(3)
+    for it in range(2):
+        x = rng.standard_normal(n)
+        J = wl.syst.jacobian()
+        y = wl.syst.do_JX(x)
+        ref = J @ x
+        assert np.linalg.norm(y - ref) <= 1e-12 * np.linalg.norm(np.abs(J) @ np.abs(x))
+        wl.syst.do_newton(1e-10)
+
+
+def test_linesearch_newton_matches_oracle(ctx):
+    """do_newton_with_linesearch from a far initial guess (psi = 3), where the
+    full Newton step is rejected: the backtracked lambdas (quadratic, then
+    cubic model, with the max(p) <= stepmax rescaling) and every iterate
+    against the oracle's restatement."""
+    from kadath_frontera_gb300 import workloads
+    res = (9, 5, 4)
+    wl = workloads.toy(res=res)
+    psi = wl.unknowns[0][1]
+    for d in range(wl.space.get_nbr_domains()):
+        psi.set_domain(d, np.full(psi.get_domain(d).shape, 3.0))
+    psi.std_base()
+    doms, osys, opsi, _ = configs.toy(res=res)
+    for d in opsi:
+        opsi[d] = K.VD(doms[d], 1, c=np.full((1,) + tuple(doms[d].nc[:2]) + (doms[d].nc[2] - 2,), 3.0),
+                       base=doms[d].std_base())
+    lams = []
+    for it in range(4):
+        done, err, lam = wl.syst.do_newton_with_linesearch(1e-10, ntrymax=10, stepmax=1.0)
+        odone, oerr, olam = K.newton_linesearch_step(osys, 1e-10, ntrymax=10, stepmax=1.0)
+        assert done == odone
+        assert abs(err - oerr) <= 1e-9 * abs(oerr)
+        assert abs(lam - olam) <= 1e-8 * abs(olam), (it, lam, olam)
+        lams.append(lam)
+        for d in range(len(doms)):
+            opsi[d].coef()
+            assert rel(psi.get_coef(d), opsi[d].cf[0]) < 1e-9, (it, d)
+    assert min(lams) < 1.0  # the backtracking branch ran
