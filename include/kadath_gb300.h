@@ -250,6 +250,26 @@ int kd_newton_step(kd_system* s, const kd_newton_opts* opts, kd_newton_report* r
 int kd_newton_step_linesearch(kd_system* s, const kd_newton_opts* opts, int ntrymax, double stepmax,
                               kd_newton_report* rep, double* lambda);
 
+/* ---- adjoint sensitivities --------------------------------------------- */
+/* No reference counterpart for the adjoint itself: the reference obtains
+ * parameter derivatives by finite differences of full re-solves.  Pieces:
+ *  kd_system_set_cst       changes a double constant of add_cst(name, double)
+ *                          (src/System_of_eqs/system_of_eqs.cpp:340);
+ *  kd_field_val_point      Scalar::val_point (include/scalar.hpp:221);
+ *  kd_system_val_point_gradient
+ *                          g = dQ/dy for Q = var's value at a point, y the
+ *                          unknown vector (nbr_unknowns doubles, host);
+ *  kd_system_dres_dcst     dF/dp for a double constant p (host vector);
+ *  kd_adjoint              dQ/dp = dq_explicit - lambda . dF/dp with
+ *                          J^T lambda = g, J assembled at the current
+ *                          (converged) fields and factored in FP64; lambda
+ *                          (nullable) receives the adjoint vector. */
+int kd_system_set_cst(kd_system* s, const char* name, double v);
+int kd_field_val_point(kd_field* f, const double point[3], double* value);
+int kd_system_val_point_gradient(kd_system* s, const char* var, const double point[3], double* g);
+int kd_system_dres_dcst(kd_system* s, const char* cst, double* fp);
+int kd_adjoint(kd_system* s, const double* g, const char* cst, double dq_explicit, double* dqdp, double* lambda);
+
 /* ---- dense LU (Matrice::set_lu / solve, src/Matrice/matrice.cpp:192-249) */
 typedef struct kd_lu kd_lu;
 int kd_lu_create(kd_ctx* ctx, kd_lu** out);

@@ -1086,4 +1086,82 @@ int MatrixBank::get(int op, int basis, int n_in, int n_out) {
   return idx;
 }
 
+// Chebyshev values by the three-term recurrence, in the order the
+// reference's summation_1d_cheb* walks them (the even and odd variants step
+// the recurrence twice per coefficient).
+bool summation_weights_1d(int basis, int n, double x, double* w) {
+  if (n <= 0) return true;
+  switch (basis) {
+    case CHEB: {
+      double tm2 = 1.0, tm1 = x;
+      w[0] = tm2;
+      if (n > 1) w[1] = tm1;
+      for (int i = 2; i < n; i++) {
+        const double tm = 2 * x * tm1 - tm2;
+        w[i] = tm;
+        tm2 = tm1;
+        tm1 = tm;
+      }
+      return true;
+    }
+    case CHEB_EVEN: {
+      double tm2 = 1.0, tm1 = x;
+      w[0] = tm2;
+      for (int i = 1; i < n; i++) {
+        double tm = 2 * x * tm1 - tm2;
+        w[i] = tm;
+        tm2 = tm1;
+        tm1 = tm;
+        tm = 2 * x * tm1 - tm2;
+        tm2 = tm1;
+        tm1 = tm;
+      }
+      return true;
+    }
+    case CHEB_ODD: {
+      double tm2 = 1.0, tm1 = x;
+      w[0] = tm1;
+      for (int i = 1; i < n; i++) {
+        double tm = 2 * x * tm1 - tm2;
+        tm2 = tm1;
+        tm1 = tm;
+        tm = 2 * x * tm1 - tm2;
+        w[i] = tm;
+        tm2 = tm1;
+        tm1 = tm;
+      }
+      return true;
+    }
+    case COSSIN:
+      for (int i = 0; i < n; i++) w[i] = (i % 2 == 0) ? std::cos((i / 2) * x) : std::sin((i - 1) / 2 * x);
+      return true;
+    case COSSIN_EVEN:
+      for (int i = 0; i < n; i++) w[i] = (i % 2 == 0) ? std::cos(i * x) : std::sin((i - 1) * x);
+      return true;
+    case COSSIN_ODD:
+      for (int i = 0; i < n; i++) w[i] = (i % 2 == 0) ? std::cos((i + 1) * x) : std::sin(i * x);
+      return true;
+    case COS:
+      for (int i = 0; i < n; i++) w[i] = std::cos(i * x);
+      return true;
+    case SIN:
+      for (int i = 0; i < n; i++) w[i] = std::sin(i * x);
+      return true;
+    case COS_EVEN:
+      for (int i = 0; i < n; i++) w[i] = std::cos(2 * i * x);
+      return true;
+    case COS_ODD:
+      for (int i = 0; i < n; i++) w[i] = std::cos((2 * i + 1) * x);
+      return true;
+    case SIN_EVEN:
+      for (int i = 0; i < n; i++) w[i] = std::sin(2 * i * x);
+      return true;
+    case SIN_ODD:
+      for (int i = 0; i < n; i++) w[i] = std::sin((2 * i + 1) * x);
+      return true;
+    default:
+      return false;
+  }
+}
+
 }  // namespace kd

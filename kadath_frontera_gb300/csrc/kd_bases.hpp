@@ -75,6 +75,11 @@ struct Mat1d {
 // Returns false if the reference does not implement the pair.
 bool build_matrix(int op, int basis, int n_in, int n_out, Mat1d& out);
 
+// Weights of the evaluation of one coefficient line at x: the value of the
+// line is sum_i w[i] * tab[i] (summation_1d_<basis>,
+// src/Ope_1d/summation_1d.cpp:30-236).  false for an unknown basis.
+bool summation_weights_1d(int basis, int n, double x, double* w);
+
 // Host-side cache of every matrix a plan uses, uploaded as one device pool.
 class MatrixBank {
  public:

@@ -601,6 +601,60 @@ int kd_newton_step(kd_system* s, const kd_newton_opts* opts, kd_newton_report* r
   });
 }
 
+int kd_system_set_cst(kd_system* s, const char* name, double v) {
+  SYS_GUARD(s) {
+    if (!name) throw kd::KdError(KD_ERR_ARG, "null name");
+    const int i = s->sys->find_cst(name);
+    if (i < 0) throw kd::KdError(KD_ERR_ARG, std::string("unknown constant ") + name);
+    s->sys->set_cst(i, v);
+  });
+}
+
+int kd_field_val_point(kd_field* f, const double point[3], double* value) {
+  if (!f || !f->f) return KD_ERR_ARG;
+  return guarded(f->sp->ctx, [&] {
+    if (!point || !value) throw kd::KdError(KD_ERR_ARG, "null argument");
+    *value = f->f->val_point(point);
+  });
+}
+
+int kd_system_val_point_gradient(kd_system* s, const char* var, const double point[3], double* g) {
+  SYS_GUARD(s) {
+    if (!var || !point || !g) throw kd::KdError(KD_ERR_ARG, "null argument");
+    const int v = s->sys->find_var(var);
+    if (v < 0) throw kd::KdError(KD_ERR_ARG, std::string("unknown variable ") + var);
+    s->sys->val_point_gradient(v, point, g);
+  });
+}
+
+int kd_system_dres_dcst(kd_system* s, const char* cst, double* fp) {
+  SYS_GUARD(s) {
+    if (!cst || !fp) throw kd::KdError(KD_ERR_ARG, "null argument");
+    const int i = s->sys->find_cst(cst);
+    if (i < 0) throw kd::KdError(KD_ERR_ARG, std::string("unknown constant ") + cst);
+    kd::Context* c = s->sp->ctx->c.get();
+    const int n = s->sys->nbr_unknowns();
+    double* d = nullptr;
+    kd::cuda_check(cudaMalloc(&d, sizeof(double) * n), "cudaMalloc(dF/dp)");
+    struct Free {
+      double* p;
+      ~Free() { cudaFree(p); }
+    } guard{d};
+    s->sys->dres_dcst(i, d);
+    kd::cuda_check(cudaMemcpyAsync(fp, d, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream()), "D2H");
+    kd::cuda_check(cudaStreamSynchronize(c->stream()), "sync");
+  });
+}
+
+int kd_adjoint(kd_system* s, const double* g, const char* cst, double dq_explicit, double* dqdp, double* lambda) {
+  SYS_GUARD(s) {
+    if (!g || !cst || !dqdp) throw kd::KdError(KD_ERR_ARG, "null argument");
+    const int i = s->sys->find_cst(cst);
+    if (i < 0) throw kd::KdError(KD_ERR_ARG, std::string("unknown constant ") + cst);
+    *dqdp = s->newton->adjoint(g, i, dq_explicit, lambda);
+  });
+}
+
 int kd_newton_step_linesearch(kd_system* s, const kd_newton_opts* opts, int ntrymax, double stepmax,
                               kd_newton_report* rep, double* lambda) {
   SYS_GUARD(s) {

@@ -599,4 +599,49 @@ Space::Space(const double center[3], const int npts[3], const std::vector<double
   if (withzec) domains.emplace_back(nd - 1, DOM_COMPACT, npts, -0.5 / bounds[nd - 2], 0.0, center);
 }
 
+void Domain::point_weights(const Base& b, const double num[3], std::vector<double>& w) const {
+  if (!b.def) throw KdError(KD_ERR_STATE, "val_point of a field without a basis");
+  w.assign(ncoefs(), 0.0);
+  std::vector<double> wr(nc[0]), wt(nc[1]), wp(nc[2]);
+  if (!summation_weights_1d(b.p, nc[2], num[2], wp.data())) throw KdError(KD_ERR_UNSUPPORTED, "val_point: basis");
+  for (int k = 0; k < nc[2]; k++) {
+    if (!summation_weights_1d(b.t[k], nc[1], num[1], wt.data())) throw KdError(KD_ERR_UNSUPPORTED, "val_point: basis");
+    for (int j = 0; j < nc[1]; j++) {
+      if (!summation_weights_1d(b.r[static_cast<size_t>(j) * b.n2c + k], nc[0], num[0], wr.data()))
+        throw KdError(KD_ERR_UNSUPPORTED, "val_point: basis");
+      for (int i = 0; i < nc[0]; i++) w[cidx(i, j, k)] = wr[i] * wt[j] * wp[k];
+    }
+  }
+}
+
+int Space::locate(const double point[3], double num[3]) const {
+  const Domain& d0 = domains.at(0);
+  const double x = point[0] - d0.center[0], y = point[1] - d0.center[1], z = point[2] - d0.center[2];
+  const double r = std::sqrt(x * x + y * y + z * z);
+  int dd = -1;
+  for (const Domain& d : domains)
+    if (d.inner_radius() - 1e-12 <= r && r <= d.outer_radius() + 1e-12) {
+      dd = d.num;
+      break;
+    }
+  if (dd < 0) return -1;
+  const Domain& d = domains[dd];
+  if (d.type == DOM_NUCLEUS) num[0] = r / d.alpha;
+  else if (d.type == DOM_SHELL) num[0] = (r - d.beta) / d.alpha;
+  else num[0] = 1.0 + 1.0 / r / d.alpha;
+  const double rho = std::sqrt(x * x + y * y);
+  double th, ph;
+  if (rho == 0.0) {
+    th = (z >= 0) ? 0.0 : M_PI;
+    ph = 0.0;
+  } else {
+    th = (z != 0.0) ? std::atan(rho / z) : M_PI / 2;
+    ph = std::atan2(y, x);
+  }
+  if (th < 0) th += M_PI;
+  num[1] = th;
+  num[2] = ph;
+  return dd;
+}
+
 }  // namespace kd

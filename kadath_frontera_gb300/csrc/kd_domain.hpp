@@ -76,6 +76,11 @@ class Domain {
   // val_boundary as a row over the r-coefficients of line (j, k).
   void val_boundary_row(int bound, int j, int k, double w, SparseRow& row) const;
 
+  // Scalar::val_point as weights: the value at numerical coordinates
+  // num = (xi, theta, phi) is sum_c w[c] cf[c] (Base_spectral::summation,
+  // src/Ope_1d/summation_1d.cpp:272).
+  void point_weights(const Base& b, const double num[3], std::vector<double>& w) const;
+
   bool has_boundary(int bound) const;
   void find_other_dom(int dom, int bound, int& other_dom, int& other_bound) const;
 };
@@ -88,6 +93,9 @@ class Space {
   std::vector<Domain> domains;
   int ndom() const { return static_cast<int>(domains.size()); }
   const Domain& dom(int d) const { return domains.at(d); }
+  // Domain holding a Cartesian point and its numerical coordinates
+  // (xi, theta, phi); -1 when no domain does.
+  int locate(const double point[3], double num[3]) const;
 };
 
 }  // namespace kd

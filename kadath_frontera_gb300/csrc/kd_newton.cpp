@@ -224,4 +224,35 @@ bool Newton::step_linesearch(const NewtonOpts& o, int ntrymax, double stepmax, N
   return false;
 }
 
+double Newton::adjoint(const double* g, int cst, double dq_explicit, double* lambda_out) {
+  Context* ctx = sys_->ctx;
+  cudaStream_t s = ctx->stream();
+  if (sys_->nbr_conditions() < 0) sys_->residual(nullptr);
+  const int N = sys_->nbr_conditions();
+  if (sys_->nbr_unknowns() != N) throw KdError(KD_ERR_STATE, "Number of unknowns is different from the number of equations");
+  ensure(N);
+  sys_->residual(d_F, true);
+  sys_->jacobian(d_J, ld, true);
+  lu_->factor(d_J, ld, N, LU_FP64);
+  double* d = nullptr;
+  cuda_check(cudaMalloc(&d, sizeof(double) * 2 * N), "cudaMalloc(adjoint)");
+  struct Free {
+    double* p;
+    ~Free() { cudaFree(p); }
+  } guard{d};
+  double* d_lambda = d;
+  double* d_fp = d + N;
+  cuda_check(cudaMemcpyAsync(d_lambda, g, sizeof(double) * N, cudaMemcpyHostToDevice, s), "H2D g");
+  lu_->solve(d_lambda, 1);  // J^T lambda = g
+  sys_->dres_dcst(cst, d_fp);
+  std::vector<double> lam(N), fp(N);
+  cuda_check(cudaMemcpyAsync(lam.data(), d_lambda, sizeof(double) * N, cudaMemcpyDeviceToHost, s), "D2H lambda");
+  cuda_check(cudaMemcpyAsync(fp.data(), d_fp, sizeof(double) * N, cudaMemcpyDeviceToHost, s), "D2H dF/dp");
+  cuda_check(cudaStreamSynchronize(s), "sync adjoint");
+  double dot = 0.0;
+  for (int i = 0; i < N; i++) dot += lam[i] * fp[i];
+  if (lambda_out) std::copy(lam.begin(), lam.end(), lambda_out);
+  return dq_explicit - dot;
+}
+
 }  // namespace kd

@@ -40,6 +40,12 @@ class Newton {
   // sufficient-decrease test holds, at most ntrymax tries.  rep.linesearch_lambda
   // gets the last lambda.
   bool step_linesearch(const NewtonOpts& o, int ntrymax, double stepmax, NewtonReport& rep, double* lambda_out);
+  // Adjoint sensitivity at a converged state (implicit-function theorem):
+  // F(u0 + A y, p) = 0 with A the unknown coefficient patterns, so
+  // dQ/dp = dQ_explicit - lambda . dF/dp with J^T lambda = g, g = dQ/dy.
+  // J is assembled and factored in FP64 here; the transposed solve reuses
+  // those factors.  g and lambda_out (nullable) are host vectors of N.
+  double adjoint(const double* g, int cst, double dq_explicit, double* lambda_out);
   // Device buffers of the last step (valid until the next call).
   double* d_F = nullptr;
   double* d_J = nullptr;

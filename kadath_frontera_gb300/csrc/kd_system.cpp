@@ -1,5 +1,7 @@
 #include "kd_system.hpp"
 
+#include <algorithm>
+
 #include <cstring>
 #include <sstream>
 
@@ -107,6 +109,20 @@ void Field::get_conf_host(int dom, double* out) {
   ctx->scratch().release_to(mark);
 }
 
+double Field::val_point(const double point[3]) {
+  double num[3];
+  const int dd = sp->locate(point, num);
+  if (dd < 0) throw KdError(KD_ERR_ARG, "val_point: the point is in no domain");
+  const Domain& dm = sp->dom(dd);
+  if (d.at(dd).zero) return 0.0;
+  std::vector<double> cf(dm.ncoefs()), w;
+  get_coef_host(dd, cf.data());
+  dm.point_weights(d[dd].base, num, w);
+  double s = 0.0;
+  for (size_t c = 0; c < cf.size(); c++) s += w[c] * cf[c];
+  return s;
+}
+
 void Field::get_coef_host(int dom, double* out) {
   const Domain& dm = sp->dom(dom);
   if (d.at(dom).zero) {
@@ -158,7 +174,7 @@ Term EvalState::cst_term(int which, int dom) {
     Term t = Term::dbl(dom, c.value);
     if (with_der) {
       t.has_dd = true;
-      t.dd = 0.0;
+      t.dd = (which == seed_cst) ? 1.0 : 0.0;
     }
     return t;
   }
@@ -651,6 +667,59 @@ const CsrTable& System::xmap(int var, int dd) {
   if (used != nunk_[key]) throw KdError(KD_ERR_STATE, "affecte_tau consumes a different number of unknowns");
   xmaps_[key] = upload_rows(rows);
   return xmaps_[key];
+}
+
+void System::set_cst(int i, double v) {
+  if (csts_.at(i).is_field) throw KdError(KD_ERR_ARG, "set_cst: the constant is a field");
+  csts_[i].value = v;
+  vcache_.clear();
+}
+
+void System::dres_dcst(int cst, double* d_y) {
+  if (csts_.at(cst).is_field) throw KdError(KD_ERR_UNSUPPORTED, "dF/dp needs a double constant");
+  int N = nbr_unknowns();
+  residual(nullptr, true);
+  if (nbr_conditions_ != N) throw KdError(KD_ERR_STATE, "Number of unknowns is different from the number of equations");
+  ctx->scratch().reset();
+  const std::map<std::pair<int, int>, DVal> none;
+  const std::vector<double> zeros(vdoubles_.size(), 0.0);
+  EvalState st;
+  st.sys = this;
+  st.with_der = true;
+  st.B = 1;
+  st.jx_seeds = &none;  // no unknown is seeded
+  st.jx_doubles = &zeros;
+  st.seed_cst = cst;
+  st.vcache = &vcache_;
+  cuda_check(cudaMemsetAsync(d_y, 0, sizeof(double) * N, ctx->stream()), "memset y");
+  for (auto& eq : eqs_) {
+    Term t = eq.lhs->eval(st);
+    export_term(eq, t, true, eq.dom, eq.bound, d_y + eq.row0, 0, 1, 1, 1.0, true);
+    if (eq.kind == Equation::MATCHING) {
+      Term r = eq.rhs->eval(st);
+      export_term(eq, r, true, eq.other_dom, eq.other_bound, d_y + eq.row0, 0, 1, 1, -1.0, true);
+    }
+  }
+}
+
+void System::val_point_gradient(int var, const double point[3], double* g) {
+  const int N = nbr_unknowns();
+  std::fill(g, g + N, 0.0);
+  double num[3];
+  const int dd = sp->locate(point, num);
+  if (dd < 0) throw KdError(KD_ERR_ARG, "val_point: the point is in no domain");
+  if (dd < dom_min || dd > dom_max) return;  // the field there does not depend on the unknowns
+  const Domain& d = sp->dom(dd);
+  std::vector<double> w;
+  d.point_weights(vars_.at(var).f->d[dd].base, num, w);
+  std::vector<SparseRow> pats;
+  d.unknown_patterns(vars_[var].f->d[dd].base, 0, pats);
+  const int c0 = col0_.at(std::make_pair(var, dd));
+  for (size_t j = 0; j < pats.size(); j++) {
+    double s = 0.0;
+    for (auto& e : pats[j].e) s += e.second * w[e.first];
+    g[c0 + j] = s;
+  }
 }
 
 DVal System::x_to_field(int var, int dd, const double* d_x) {

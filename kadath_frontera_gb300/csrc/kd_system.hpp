@@ -41,6 +41,8 @@ class Field {
   void set_conf_host(int dom, const double* values);
   void set_value(double v);                   // Scalar = v (conf)
   void std_base();
+  // Scalar::val_point (include/scalar.hpp:221): value at a Cartesian point.
+  double val_point(const double point[3]);
   // Host read-back in the requested representation (computes it if needed).
   void get_conf_host(int dom, double* out);
   void get_coef_host(int dom, double* out);
@@ -105,6 +107,7 @@ struct EvalState {
   int seed_var = -1;       // field unknown being seeded (-1: a double unknown)
   int seed_dom = -1;
   int seed_var_double = -1;
+  int seed_cst = -1;       // double constant seeded (dF/dp passes)
   DVal seed;               // batch-B coefficient patterns
   std::map<std::pair<int, int>, Term> def_cache;
   // do_JX: every unknown field seeded at once (tangent = x mapped to
@@ -190,6 +193,17 @@ class System {
   // (affecte_tau), allocated from the current scratch arena.
   DVal x_to_field(int var, int dd, const double* d_x);
   int n_var_doubles() const { return static_cast<int>(vdoubles_.size()); }
+  // A double constant's value (add_cst(name, double)); changing it drops
+  // the recorded node values.
+  void set_cst(int i, double v);
+  double cst_value(int i) const { return csts_.at(i).value; }
+  // dF/dp for the double constant p, in one tangent pass seeding only p
+  // (device vector of nbr_conditions doubles).
+  void dres_dcst(int cst, double* d_y);
+  // Gradient of var's value at a Cartesian point with respect to the
+  // unknown vector (host, nbr_unknowns doubles): the point's summation
+  // weights mapped through the unknown coefficient patterns.
+  void val_point_gradient(int var, const double point[3], double* g);
   // Fields changed outside update_from_x: drop the recorded node values.
   void invalidate_values() { vcache_.clear(); }
 

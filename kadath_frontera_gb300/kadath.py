@@ -89,6 +89,11 @@ def _declare_system(lib):
         "kd_system_update": (I, [P, DP]),
         "kd_newton_step": (I, [P, C.POINTER(NewtonOpts), C.POINTER(NewtonReport)]),
         "kd_newton_step_linesearch": (I, [P, C.POINTER(NewtonOpts), I, D, C.POINTER(NewtonReport), DP]),
+        "kd_system_set_cst": (I, [P, C.c_char_p, D]),
+        "kd_field_val_point": (I, [P, DP, DP]),
+        "kd_system_val_point_gradient": (I, [P, C.c_char_p, DP, DP]),
+        "kd_system_dres_dcst": (I, [P, C.c_char_p, DP]),
+        "kd_adjoint": (I, [P, DP, C.c_char_p, D, DP, DP]),
         "kd_lu_create": (I, [P, C.POINTER(P)]),
         "kd_lu_destroy": (I, [P]),
         "kd_lu_factor": (I, [P, P, C.c_longlong, I, I]),
@@ -216,6 +221,13 @@ class Scalar:
         """Scalar assignment (device to device)."""
         self.space.ctx.check(_L().kd_field_copy(self.h, other.h))
         return self
+
+    def val_point(self, point):
+        """Scalar::val_point: the value at a Cartesian point."""
+        pt = np.ascontiguousarray(point, dtype=np.float64)
+        out = C.c_double()
+        self.space.ctx.check(_L().kd_field_val_point(self.h, _dp(pt), C.byref(out)))
+        return out.value
 
     def std_base_cart(self, c):
         """Basis of the Cartesian component c = 1, 2, 3 (x, y, z) of a vector."""
@@ -353,6 +365,32 @@ class System_of_eqs:
         y = np.zeros(self.get_nbr_unknowns())
         self.ctx.check(_L().kd_system_jx(self.h, _dp(x), _dp(y)))
         return y
+
+    def set_cst(self, name, value):
+        """Changes a double constant registered with add_cst(name, double)."""
+        self.ctx.check(_L().kd_system_set_cst(self.h, name.encode(), float(value)))
+
+    def val_point_gradient(self, var, point):
+        """dQ/dy for Q = var's value at a point, y the unknown vector."""
+        pt = np.ascontiguousarray(point, dtype=np.float64)
+        g = np.zeros(self.get_nbr_unknowns())
+        self.ctx.check(_L().kd_system_val_point_gradient(self.h, var.encode(), _dp(pt), _dp(g)))
+        return g
+
+    def dres_dcst(self, name):
+        """dF/dp for the double constant p = name."""
+        fp = np.zeros(self.get_nbr_unknowns())
+        self.ctx.check(_L().kd_system_dres_dcst(self.h, name.encode(), _dp(fp)))
+        return fp
+
+    def adjoint(self, g, cst, dq_explicit=0.0):
+        """dQ/dp at the current (converged) fields: dq_explicit - lambda.dF/dp
+        with J^T lambda = g.  Returns (dQ/dp, lambda)."""
+        g = np.ascontiguousarray(g, dtype=np.float64)
+        lam = np.zeros(self.get_nbr_unknowns())
+        out = C.c_double()
+        self.ctx.check(_L().kd_adjoint(self.h, _dp(g), cst.encode(), float(dq_explicit), C.byref(out), _dp(lam)))
+        return out.value, lam
 
     def cache_tangents(self, on=True):
         """Keep the tangents of iterate-independent subtrees between Jacobian
