@@ -2,6 +2,7 @@
 // per field, the field staged whole in shared memory), elementwise algebra
 // on collocation values, and the sparse gathers used by the tau/Galerkin
 // export.  All arithmetic is FP64, as in the reference.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "kd_device.hpp"
@@ -17,15 +18,17 @@ __device__ __forceinline__ int line_matrix(const KdPass& p, int c1, int c2) {
 }
 
 // One pass: X has dims (d0,d1,d2); Y has the pass dim replaced by n_out.
-__device__ void run_pass(const KdPass& p, const double* __restrict__ X, double* __restrict__ Y,
-                         int d0, int d1, int d2, const double* __restrict__ pool, double scale) {
+// Outputs e = e0 + threadIdx.x + k * estride; store(e, value) writes them.
+template <class Store>
+__device__ void run_pass_part(const KdPass& p, const double* __restrict__ X, int d0, int d1, int d2,
+                              const double* __restrict__ pool, double scale, int e0, int estride, Store store) {
   int o0 = d0, o1 = d1, o2 = d2;
   if (p.dim == 0) o0 = p.n_out;
   if (p.dim == 1) o1 = p.n_out;
   if (p.dim == 2) o2 = p.n_out;
   const int total = o0 * o1 * o2;
   const int nin = p.n_in;
-  for (int e = threadIdx.x; e < total; e += blockDim.x) {
+  for (int e = e0 + threadIdx.x; e < total; e += estride) {
     int c2 = e % o2;
     int t = e / o2;
     int c1 = t % o1;
@@ -53,8 +56,13 @@ __device__ void run_pass(const KdPass& p, const double* __restrict__ X, double* 
 #pragma unroll 4
       for (int q = 0; q < nin; q++) acc = fma(__ldg(M + q), X[base + q * stride], acc);
     }
-    Y[e] = acc * scale;
+    store(e, acc * scale);
   }
+}
+
+__device__ void run_pass(const KdPass& p, const double* __restrict__ X, double* __restrict__ Y, int d0, int d1,
+                         int d2, const double* __restrict__ pool, double scale) {
+  run_pass_part(p, X, d0, d1, d2, pool, scale, 0, blockDim.x, [Y](int e, double v) { Y[e] = v; });
 }
 
 __global__ void line_passes_kernel(const __grid_constant__ KdItemList list, const double* __restrict__ pool) {
@@ -109,6 +117,77 @@ __global__ void line_passes_kernel(const __grid_constant__ KdItemList list, cons
       for (int e = threadIdx.x; e < n_in_elems; e += blockDim.x) dst[e] = bufA[e] * it.scale;
     }
     __syncthreads();
+  }
+}
+
+// Small batches: one 8-CTA cluster per field.  Each CTA computes every
+// 8th block of a pass's outputs and stores them into all eight CTAs' shared
+// buffers (distributed shared memory), then one cluster barrier; the last
+// pass writes straight to global memory.  A field's FP64 work is spread over
+// eight SMs instead of one.
+constexpr int LP_CL = 8;
+constexpr int LP_CLUSTER_MAX_FIELDS = 32;
+__global__ void line_passes_cluster_kernel(const __grid_constant__ KdItemList list, const double* __restrict__ pool) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ double smem[];
+  const int rank = static_cast<int>(cluster.block_rank());
+  const int f = blockIdx.x / LP_CL;
+  int item = 0;
+  while (item + 1 < list.nitems && list.prefix[item + 1] <= f) item++;
+  const KdItem& it = list.items[item];
+  const int field_in_item = f - list.prefix[item];
+  const int n_in_elems = it.n0 * it.n1 * it.n2;
+  int d0 = it.n0, d1 = it.n1, d2 = it.n2;
+  int maxe = n_in_elems;
+  {
+    int e0 = d0, e1 = d1, e2 = d2;
+    for (int q = 0; q < it.npass; q++) {
+      if (it.pass[q].dim == 0) e0 = it.pass[q].n_out;
+      if (it.pass[q].dim == 1) e1 = it.pass[q].n_out;
+      if (it.pass[q].dim == 2) e2 = it.pass[q].n_out;
+      int e = e0 * e1 * e2;
+      if (e > maxe) maxe = e;
+    }
+  }
+  double* bufA = smem;
+  double* bufB = smem + maxe;
+  const double* src = it.in + static_cast<long long>(field_in_item) * it.in_stride;
+  double* dst = it.out + static_cast<long long>(field_in_item) * it.out_stride;
+  for (int e = threadIdx.x; e < n_in_elems; e += blockDim.x) bufA[e] = src[e];
+  __syncthreads();
+  double* X = bufA;
+  double* Y = bufB;
+  const int e0 = rank * blockDim.x, estride = LP_CL * blockDim.x;
+  for (int q = 0; q < it.npass; q++) {
+    const KdPass& p = it.pass[q];
+    const bool last = (q == it.npass - 1);
+    int o0 = d0, o1 = d1, o2 = d2;
+    if (p.dim == 0) o0 = p.n_out;
+    if (p.dim == 1) o1 = p.n_out;
+    if (p.dim == 2) o2 = p.n_out;
+    if (last) {
+      const double sc = it.scale;
+      run_pass_part(p, X, d0, d1, d2, pool, sc, e0, estride, [dst](int e, double v) { dst[e] = v; });
+    } else {
+      double* Yr[LP_CL];
+      for (int r = 0; r < LP_CL; r++) Yr[r] = cluster.map_shared_rank(Y, r);
+      run_pass_part(p, X, d0, d1, d2, pool, 1.0, e0, estride, [&Yr](int e, double v) {
+#pragma unroll
+        for (int r = 0; r < LP_CL; r++) Yr[r][e] = v;
+      });
+      cluster.sync();  // every CTA's Y is complete and nobody reads X any more
+    }
+    d0 = o0;
+    d1 = o1;
+    d2 = o2;
+    double* tmp = X;
+    X = Y;
+    Y = tmp;
+  }
+  if (it.npass == 0) {
+    if (rank == 0)
+      for (int e = threadIdx.x; e < n_in_elems; e += blockDim.x) dst[e] = bufA[e] * it.scale;
   }
 }
 
@@ -210,6 +289,31 @@ cudaError_t launch_line_passes(const KdItemList& list, int smem_doubles, const d
     cudaError_t e = cudaFuncSetAttribute(line_passes_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
+  }
+  if (total_fields <= LP_CLUSTER_MAX_FIELDS) {
+    // few fields: eight SMs per field
+    static bool attr = false;
+    if (!attr || smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(line_passes_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(smem > 48 * 1024 ? smem : 48 * 1024));
+      if (e != cudaSuccess) return e;
+      attr = true;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(total_fields * LP_CL, 1, 1);
+    cfg.blockDim = dim3(128, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = LP_CL;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, line_passes_cluster_kernel, list, d_pool);
+    if (e != cudaSuccess) return e;
+    return cudaGetLastError();
   }
   int grid = total_fields < 152 * 8 ? total_fields : 152 * 8;
   line_passes_kernel<<<grid, 128, smem, s>>>(list, d_pool);
