@@ -94,6 +94,64 @@ __global__ void __launch_bounds__(TRSM32_THREADS) trsm_unit_lower_f32(float* __r
     if (i < jb) xc[i] = x[i];
 }
 
+// ---- equilibration of the FP32 working copy (mixed modes) --------------
+// Row scales r_i = 2^-round(log2 max_j |A_ij|), then column scales
+// c_j = 2^-round(log2 max_i |r_i A_ij|): powers of two, so scaling is exact
+// and only the FP32 rounding remains.  The factors are those of
+// D_r A D_c; the preconditioner is M^-1 b = D_c (LU)^-1 (D_r b).
+__device__ __forceinline__ double pow2_inverse(double m) {
+  if (!(m > 0.0) || !isfinite(m)) return 1.0;
+  int e;
+  frexp(m, &e);  // m = f 2^e, f in [0.5, 1)
+  return ldexp(1.0, 1 - e);  // 2^-(e-1): scaled max in [1, 2)
+}
+
+// Maxima of |A_ij| over column chunks, merged with atomicMax on the bit
+// patterns of non-negative doubles (order-independent, deterministic).
+__global__ void row_absmax_kernel(const double* __restrict__ A, long long ld, int N, int chunk,
+                                  unsigned long long* __restrict__ rmax) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const int c0 = blockIdx.y * chunk;
+  const int c1 = (c0 + chunk < N) ? c0 + chunk : N;
+  double m = 0.0;
+  for (int j = c0; j < c1; j++) m = fmax(m, fabs(A[static_cast<long long>(j) * ld + i]));
+  atomicMax(rmax + i, static_cast<unsigned long long>(__double_as_longlong(m)));
+}
+
+__global__ void row_scale_kernel(const unsigned long long* __restrict__ rmax, int N, double* __restrict__ rs) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) rs[i] = pow2_inverse(__longlong_as_double(static_cast<long long>(rmax[i])));
+}
+
+// One CTA per column: c_j from max_i |r_i A_ij|, then the scaled FP32 column.
+__global__ void col_scale_convert_kernel(const double* __restrict__ A, long long lda, const double* __restrict__ rs,
+                                         int N, double* __restrict__ cs, float* __restrict__ B, long long ldb) {
+  __shared__ double red[32];
+  const int j = blockIdx.x;
+  const double* col = A + static_cast<long long>(j) * lda;
+  double m = 0.0;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) m = fmax(m, fabs(rs[i] * col[i]));
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    m = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (threadIdx.x == 0) red[0] = m;
+  }
+  __syncthreads();
+  const double c = pow2_inverse(red[0]);
+  if (threadIdx.x == 0) cs[j] = c;
+  float* out = B + static_cast<long long>(j) * ldb;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) out[i] = static_cast<float>(rs[i] * col[i] * c);
+}
+
+__global__ void scale_vec_kernel(double* __restrict__ x, const double* __restrict__ s, int N) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) x[i] *= s[i];
+}
+
 __global__ void d2s(const double* __restrict__ A, long long lda, float* __restrict__ B, long long ldb, int N) {
   long long total = static_cast<long long>(N) * N;
   for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < total;
@@ -283,6 +341,7 @@ DenseLU::~DenseLU() {
   cudaFree(ipiv_);
   cudaFree(d_info_);
   cudaFree(slot_mem_);
+  cudaFree(eq_buf_);
   cudaFree(part_);
   cudaFree(work_);
   cudaFree(work32_);
@@ -1234,8 +1293,31 @@ void DenseLU::factor(double* A, long long ld, int N, int mode) {
       cuda_check(cudaMalloc(&A32_, need * sizeof(float)), "cudaMalloc(A32)");
       a32_cap_ = need;
     }
-    d2s<<<152 * 8, 256, 0, ctx_->stream()>>>(A, ld, A32_, ld32_, N);
-    ctx_->launches++;
+    if (static_cast<size_t>(N) > eq_cap_) {
+      cudaFree(eq_buf_);
+      cuda_check(cudaMalloc(&eq_buf_, sizeof(double) * 3 * static_cast<size_t>(N)), "cudaMalloc(equilibration)");
+      eq_cap_ = N;
+    }
+    double* rs = eq_buf_;
+    double* cs = eq_buf_ + N;
+    unsigned long long* rmax = reinterpret_cast<unsigned long long*>(eq_buf_ + 2 * static_cast<size_t>(N));
+    cudaStream_t st = ctx_->stream();
+    if (equilibrate) {
+      cuda_check(cudaMemsetAsync(rmax, 0, sizeof(unsigned long long) * N, st), "memset row max");
+      const int rb = blocks(N, 256);
+      int nch = (4 * nsm_ + rb - 1) / rb;
+      if (nch < 1) nch = 1;
+      const int chunk = (N + nch - 1) / nch;
+      nch = (N + chunk - 1) / chunk;
+      row_absmax_kernel<<<dim3(rb, nch), 256, 0, st>>>(A, ld, N, chunk, rmax);
+      row_scale_kernel<<<rb, 256, 0, st>>>(rmax, N, rs);
+      col_scale_convert_kernel<<<N, 256, 0, st>>>(A, ld, rs, N, cs, A32_, ld32_);
+      ctx_->launches += 3;
+    } else {
+      d2s<<<152 * 8, 256, 0, st>>>(A, ld, A32_, ld32_, N);
+      ctx_->launches++;
+    }
+    scaled_ = equilibrate;
     factor_f32(A32_, ld32_, N, mode == LU_TF32_IR);
     prepare_solves<float>(A32_, ld32_, N);
   }
@@ -1313,7 +1395,19 @@ void DenseLU::solve_fp64(const double* LU, long long ld, int N, double* b, int t
   tri_solve<double>(LU, ld, N, b, trans);
 }
 
-void DenseLU::solve_f32(double* b) { tri_solve<float>(A32_, ld32_, N_, b, 0); }
+void DenseLU::solve_f32(double* b) {
+  // M^-1 b = D_c (LU)^-1 (D_r b) with the equilibrated factors
+  cudaStream_t st = ctx_->stream();
+  if (scaled_) {
+    scale_vec_kernel<<<blocks(N_, 256), 256, 0, st>>>(b, eq_buf_, N_);
+    ctx_->launches++;
+  }
+  tri_solve<float>(A32_, ld32_, N_, b, 0);
+  if (scaled_) {
+    scale_vec_kernel<<<blocks(N_, 256), 256, 0, st>>>(b, eq_buf_ + N_, N_);
+    ctx_->launches++;
+  }
+}
 
 // After factorisation: pivots as one permutation, inverses of the 64 x 64
 // diagonal blocks of L (unit lower) and U.

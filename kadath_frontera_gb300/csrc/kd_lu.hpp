@@ -46,6 +46,9 @@ class DenseLU {
   // TF32 mode: 3 = 3xTF32 trailing updates (about FP32 accurate factors,
   // fewer refinement iterations), 1 = plain TF32 products.
   int tf32_terms = 3;
+  // Mixed modes: factor D_r A D_c (power-of-two row and column scales), the
+  // refinement works on A itself.
+  bool equilibrate = true;
 
  private:
   Context* ctx_;
@@ -64,6 +67,9 @@ class DenseLU {
   int* swap_map_ = nullptr;
   int* panel_err_ = nullptr;   // set when a grid barrier wait runs out (panel or sweep)
   unsigned* tri_bar_ = nullptr;  // barrier counters of the two triangular sweeps
+  double* eq_buf_ = nullptr;   // row scales, column scales, row maxima (mixed modes)
+  size_t eq_cap_ = 0;
+  bool scaled_ = false;
   double* part_ = nullptr;     // split-K partial sums of the FP64 matvec
   size_t part_cap_ = 0;
   void gemv(const double* x, double* y, double alpha, double beta, const double* b);
