@@ -188,6 +188,20 @@ int kd_system_add_def(kd_system* s, int dom, const char* text);            /* ad
 int kd_system_add_eq_inside(kd_system* s, int dom, const char* eq);        /* add_eq_inside */
 int kd_system_add_eq_bc(kd_system* s, int dom, int bound, const char* eq); /* add_eq_bc */
 int kd_system_add_eq_matching(kd_system* s, int dom, int bound, const char* eq); /* add_eq_matching */
+/* System_of_eqs::add_ope(name, &EOS<Cold_PWPoly, var>::action, ...)
+ * (include/system_of_eqs.hpp:277, include/EOS/EOS.hh:235): registers
+ * name(h) = var of a cold piecewise polytrope at the enthalpy h, with its
+ * variation (include/EOS/EOS.hh:67-160).  var: KD_EOS_EPSILON, _PRESSURE,
+ * _DENSITY, _DHDRHO.  The polytrope is given as Margherita's polytrope files
+ * give it (eos/gam2.polytrope: npieces, rhomin, rhomax, ktab0, gamma_tab,
+ * rho_tab), geometrised units; the other pieces' K, eps and h follow from
+ * continuity as in Margherita_setup_polytrope. */
+#define KD_EOS_EPSILON 0
+#define KD_EOS_PRESSURE 1
+#define KD_EOS_DENSITY 2
+#define KD_EOS_DHDRHO 3
+int kd_system_add_ope_eos(kd_system* s, const char* name, int var, int npieces, double rhomin, double rhomax,
+                          double k0, const double* gamma_tab, const double* rho_tab);
 int kd_system_sizes(kd_system* s, int* n_unknowns, int* n_conditions);
 int kd_system_n_equations(kd_system* s, int* neq);
 /* sec_member (src/System_of_eqs/solver.cpp:49): F(u) into host F. */

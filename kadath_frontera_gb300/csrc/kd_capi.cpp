@@ -601,6 +601,39 @@ int kd_newton_step(kd_system* s, const kd_newton_opts* opts, kd_newton_report* r
   });
 }
 
+int kd_system_add_ope_eos(kd_system* s, const char* name, int var, int npieces, double rhomin, double rhomax,
+                          double k0, const double* gamma_tab, const double* rho_tab) {
+  SYS_GUARD(s) {
+    if (!name || !gamma_tab || !rho_tab) throw kd::KdError(KD_ERR_ARG, "null argument");
+    if (npieces < 1 || npieces > kd::KD_EOS_MAX_PIECES) throw kd::KdError(KD_ERR_ARG, "1..8 polytrope pieces");
+    kd::KdEos e = {};
+    e.npieces = npieces;
+    e.rhomin = rhomin;
+    e.rhomax = rhomax;
+    for (int i = 0; i < npieces; i++) {
+      e.gamma[i] = gamma_tab[i];
+      e.rho[i] = rho_tab[i];
+      if (!(gamma_tab[i] > 1.0)) throw kd::KdError(KD_ERR_ARG, "polytropic exponents must exceed 1");
+    }
+    // Margherita_setup_polytrope (include/EOS/standalone/setup_polytrope.cc),
+    // geometrised units: continuity of the pressure and of eps across pieces
+    e.k[0] = k0;
+    e.eps[0] = 0.0;
+    e.h[0] = 0.0;
+    for (int i = 1; i < npieces; i++) {
+      if (e.rho[i] <= e.rho[i - 1]) throw kd::KdError(KD_ERR_ARG, "rho_tab must increase monotonically");
+      const double gim1 = e.gamma[i] - 1.0;
+      e.k[i] = e.k[i - 1] * std::pow(e.rho[i], e.gamma[i - 1] - e.gamma[i]);
+      e.eps[i] = e.eps[i - 1] + e.k[i - 1] * std::pow(e.rho[i], e.gamma[i - 1] - 1.0) / (e.gamma[i - 1] - 1.0) -
+                 e.k[i] * std::pow(e.rho[i], gim1) / gim1;
+      const double P = e.k[i] * std::pow(e.rho[i], e.gamma[i]);
+      const double eps = e.eps[i] + P / e.rho[i] / gim1;
+      e.h[i] = 1. + eps + P / e.rho[i];
+    }
+    s->sys->add_ope_eos(name, var, e);
+  });
+}
+
 int kd_system_set_cst(kd_system* s, const char* name, double v) {
   SYS_GUARD(s) {
     if (!name) throw kd::KdError(KD_ERR_ARG, "null name");

@@ -368,6 +368,84 @@ cudaError_t launch_reduce1(const double* x, long long n, int op, double* out_sca
   return cudaGetLastError();
 }
 
+__device__ __forceinline__ double eos_clamp_rho(const KdEos& e, double rho) {
+  return rho < e.rhomin ? e.rhomin : (rho > e.rhomax ? e.rhomax : rho);  // check_range
+}
+
+__device__ __forceinline__ int eos_piece_rho(const KdEos& e, double rho) {
+  for (int nn = 1; nn < e.npieces; nn++)
+    if (rho <= e.rho[nn] && rho > e.rho[nn - 1]) return nn - 1;
+  return e.npieces - 1;
+}
+
+__device__ __forceinline__ double eos_rho_of_h(const KdEos& e, double h) {
+  if (h <= 1.0) return e.rho[0];  // rho__h_cold range check
+  int idx = e.npieces - 1;
+  for (int nn = 1; nn < e.npieces; nn++)
+    if (h <= e.h[nn] && h > e.h[nn - 1]) {
+      idx = nn - 1;
+      break;
+    }
+  const double gm1 = e.gamma[idx] - 1.0;
+  double rho = pow(gm1 * (h - 1.0 - e.eps[idx]) / (e.gamma[idx] * e.k[idx]), 1.0 / gm1);
+  return eos_clamp_rho(e, rho);
+}
+
+// press_cold_eps_cold__rho and dpress_cold_drho__rho (both clamp rho first)
+__device__ __forceinline__ double eos_press(const KdEos& e, double rho, double* eps_out) {
+  rho = eos_clamp_rho(e, rho);
+  const int i = eos_piece_rho(e, rho);
+  const double p = e.k[i] * pow(rho, e.gamma[i]);
+  if (eps_out) *eps_out = e.eps[i] + p / (rho * (e.gamma[i] - 1.0));
+  return p;
+}
+
+__device__ __forceinline__ double eos_dpdrho(const KdEos& e, double rho) {
+  rho = eos_clamp_rho(e, rho);
+  const int i = eos_piece_rho(e, rho);
+  return e.gamma[i] * e.k[i] * pow(rho, e.gamma[i]) / rho;
+}
+
+__global__ void eos_kernel(const __grid_constant__ KdEos e, int var, long long npts, const double* __restrict__ h,
+                           int B, const double* __restrict__ dh, double* __restrict__ out) {
+  const long long total = npts * (dh ? B : 1);
+  for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < total;
+       t += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const long long pt = t % npts;
+    // rho__h_cold clamps h to 1 and the later calls clamp rho to
+    // [rhomin, rhomax] in the caller's variables (all by reference)
+    const double hv = h[pt] <= 1.0 ? 1.0 : h[pt];
+    const double rho = eos_clamp_rho(e, eos_rho_of_h(e, h[pt]));
+    double epsc = 0.0;
+    const double p = eos_press(e, rho, &epsc);
+    if (!dh) {
+      double v;
+      if (var == EOS_EPSILON) v = epsc;
+      else if (var == EOS_DENSITY) v = rho;
+      else if (var == EOS_PRESSURE) v = p;
+      else v = 1.0 / hv * eos_dpdrho(e, rho);
+      out[t] = v;
+    } else {
+      const double dpdrho = eos_dpdrho(e, rho);
+      const double drho = rho * 1.0 / dpdrho * dh[t];
+      double v;
+      if (var == EOS_EPSILON) v = p / (rho * rho) * drho;
+      else if (var == EOS_PRESSURE) v = dpdrho * drho;
+      else if (var == EOS_DENSITY) v = drho;
+      else v = 0.0;  // the reference sets the variation of dH/dln(rho) to zero
+      out[t] = v;
+    }
+  }
+}
+
+cudaError_t launch_eos(const KdEos& eos, int var, long long npts, const double* h, int B, const double* dh,
+                       double* out, cudaStream_t s) {
+  const long long total = npts * (dh ? B : 1);
+  if (total <= 0) return cudaSuccess;
+  eos_kernel<<<grid_for(total, 256), 256, 0, s>>>(eos, var, npts, h, B, dh, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_absmax(const double* x, long long n, double* out_scalar, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(out_scalar, 0, sizeof(double), s);
   if (e != cudaSuccess) return e;

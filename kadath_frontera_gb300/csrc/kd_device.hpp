@@ -86,6 +86,23 @@ cudaError_t launch_gather_csr(const double* in, long long in_stride, int batch, 
 
 // Sum over the last axis reduction helpers used by residual norms.
 cudaError_t launch_absmax(const double* x, long long n, double* out_scalar, cudaStream_t s);
+// Cold piecewise polytrope (Margherita Cold_PWPoly, include/EOS/standalone/
+// cold_pwpoly_implementation.hh), geometrised units, tables derived as in
+// Margherita_setup_polytrope (setup_polytrope.cc).
+constexpr int KD_EOS_MAX_PIECES = 8;
+struct KdEos {
+  int npieces;
+  double rhomin, rhomax;
+  double k[KD_EOS_MAX_PIECES], gamma[KD_EOS_MAX_PIECES], rho[KD_EOS_MAX_PIECES], eps[KD_EOS_MAX_PIECES],
+      h[KD_EOS_MAX_PIECES];
+};
+enum EosVar : int { EOS_EPSILON = 0, EOS_PRESSURE = 1, EOS_DENSITY = 2, EOS_DHDRHO = 3 };
+// Value (dh == nullptr): out = var(h) pointwise (EOS::term_by_term).
+// Variation: out[b] = d var for the tangent batch dh (B fields) at h
+// (EOS::term_by_term_variation, include/EOS/EOS.hh:67-160).
+cudaError_t launch_eos(const KdEos& eos, int var, long long npts, const double* h, int B, const double* dh,
+                       double* out, cudaStream_t s);
+
 // Deterministic single-CTA reduction: op 0 = sum of squares, 1 = max.
 cudaError_t launch_reduce1(const double* x, long long n, int op, double* out_scalar, cudaStream_t s);
 

@@ -369,6 +369,41 @@ DVal vd_exp(const DVal& a) {
   return r;
 }
 
+DVal eos_value(const DVal& h, const KdEos& e, int var) {
+  if (h.zero) return h;
+  h.coef_i();
+  DVal res(h.ctx, h.dom, h.batch);
+  res.zero = false;
+  const long long n = static_cast<long long>(h.batch) * h.npts();
+  double* o = alloc(h.ctx, n);
+  ProfScope ps(h.ctx, Context::PROF_EW, 16.0 * n);
+  cuda_check(launch_eos(e, var, n, h.c, 1, nullptr, o, h.ctx->stream()), "eos kernel");
+  h.ctx->launches++;
+  res.c = o;
+  res.in_conf = true;
+  res.base = h.base;
+  return res;
+}
+
+DVal eos_variation(const DVal& dh, const DVal& h, const KdEos& e, int var) {
+  if (dh.zero) return dh;
+  if (h.zero) return DVal::zeros(dh.ctx, dh.dom, dh.batch);
+  if (h.batch != 1) throw KdError(KD_ERR_STATE, "eos variation needs a single value field");
+  dh.coef_i();
+  h.coef_i();
+  DVal res(dh.ctx, dh.dom, dh.batch);
+  res.zero = false;
+  const long long npts = h.npts();
+  double* o = alloc(dh.ctx, npts * dh.batch);
+  ProfScope ps(dh.ctx, Context::PROF_EW, 16.0 * npts * dh.batch);
+  cuda_check(launch_eos(e, var, npts, h.c, dh.batch, dh.c, o, dh.ctx->stream()), "eos variation kernel");
+  dh.ctx->launches++;
+  res.c = o;
+  res.in_conf = true;
+  res.base = dh.base;
+  return res;
+}
+
 DVal vd_log(const DVal& a) {
   DVal r = conf_unary(EW_LOG, a);
   r.base = a.base;

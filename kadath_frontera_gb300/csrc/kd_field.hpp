@@ -90,4 +90,10 @@ DVal der_normal(const DVal& so, int bound);
 DVal laplacian(const DVal& so);  // Domain::laplacian (domain.cpp:155)
 DVal radius_field(Context* ctx, const Domain* d);
 
+// EOS<eos, var>::action pieces (include/EOS/EOS.hh:67-160): the value of
+// var at the enthalpy h (term_by_term) and its variation for a tangent
+// batch dh at h (term_by_term_variation), pointwise at collocation points.
+DVal eos_value(const DVal& h, const KdEos& e, int var);
+DVal eos_variation(const DVal& dh, const DVal& h, const KdEos& e, int var);
+
 }  // namespace kd

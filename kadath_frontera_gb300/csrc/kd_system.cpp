@@ -669,6 +669,12 @@ const CsrTable& System::xmap(int var, int dd) {
   return xmaps_[key];
 }
 
+void System::add_ope_eos(const std::string& name, int var, const KdEos& eos) {
+  if (var < EOS_EPSILON || var > EOS_DHDRHO) throw KdError(KD_ERR_ARG, "unknown EOS variable");
+  tcache_.clear();
+  user_opes_.push_back({name, eos, var});
+}
+
 void System::set_cst(int i, double v) {
   if (csts_.at(i).is_field) throw KdError(KD_ERR_ARG, "set_cst: the constant is a field");
   csts_[i].value = v;

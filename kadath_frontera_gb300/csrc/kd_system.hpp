@@ -162,6 +162,17 @@ class System {
   int find_cst(const std::string& n) const;
   int find_def(const std::string& n, int dom) const;
 
+  // User-defined operators of the EOS kind (System_of_eqs::add_ope with
+  // EOS<eos, var>::action, include/system_of_eqs.hpp:277): name(h) gives var
+  // of a cold piecewise polytrope at the enthalpy h.
+  struct UserOpe {
+    std::string name;
+    KdEos eos;
+    int var;
+  };
+  void add_ope_eos(const std::string& name, int var, const KdEos& eos);
+  const std::vector<UserOpe>& user_opes() const { return user_opes_; }
+
   double var_double(int i) const { return vdoubles_[i].value; }
   void set_var_double(int i, double v) { vdoubles_[i].value = v; }
 
@@ -243,6 +254,7 @@ class System {
   std::vector<VarDouble> vdoubles_;
   std::vector<CstInfo> csts_;
   std::vector<DefInfo> defs_;
+  std::vector<UserOpe> user_opes_;
   std::vector<Equation> eqs_;
   int nbr_conditions_ = -1;
   int nbr_unknowns_ = -1;

@@ -493,6 +493,34 @@ class OpePartial : public Ope {
   OpePtr a;
 };
 
+// User-defined EOS operator: Ope_user with EOS<eos, var>::action
+// (include/EOS/EOS.hh:235-270).  The tangent depends on the value.
+class OpeEos : public Ope {
+ public:
+  OpeEos(int dom, const KdEos& e, int var, OpePtr a_) : Ope(dom), eos(e), var(var), a(std::move(a_)) {
+    vc = a->vc;
+    dz = a->dz;
+    dc = a->dz;
+  }
+  std::vector<const Ope*> kids() const override { return {a.get()}; }
+  Term action(EvalState& st, const Term* cv) const override {
+    Term t = a->eval(st);
+    if (t.is_double || t.vt.size() != 1) throw KdError(KD_ERR_UNSUPPORTED, "EOS only defined with respect for a scalar");
+    Term r = tensor_like(t);
+    const DVal& h = t.vt[0];
+    if (cv) r.vt = cv->vt;
+    else r.vt.push_back(eos_value(h, eos, var));
+    if (t.has_dt) {
+      r.has_dt = true;
+      r.dt.push_back(h.zero ? DVal::zeros(h.ctx, h.dom, t.dt[0].batch) : eos_variation(t.dt[0], h, eos, var));
+    }
+    return r;
+  }
+  KdEos eos;
+  int var;
+  OpePtr a;
+};
+
 class OpeLeaf : public Ope {
  public:
   enum Kind { VAR, VAR_DOUBLE, CST, HARD, DEF };
@@ -723,6 +751,10 @@ OpePtr parse_ope(const System& sys, int dd, const std::string& expr, int bound) 
   if (is_double_str(name, v)) return std::make_shared<OpeLeaf>(dd, OpeLeaf::HARD, -1, v);
   which = sys.find_def(bare, dd);
   if (which >= 0) return std::make_shared<OpeLeaf>(dd, OpeLeaf::DEF, which);
+  // user-defined operators come last, as in give_ope.cpp:1107
+  for (const auto& u : sys.user_opes())
+    if (is_ope_uni(name, p1, u.name.c_str()))
+      return std::make_shared<OpeEos>(dd, u.eos, u.var, parse_ope(sys, dd, p1, bound));
   throw KdError(KD_ERR_ARG, "Unknown operator " + bare);
 }
 

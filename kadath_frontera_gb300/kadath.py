@@ -27,6 +27,7 @@ OUTER_BC, INNER_BC = 0, 1
 NEWTON_RAPHSON = 0
 
 KD_LU_FP64, KD_LU_TF32_IR, KD_LU_FP32_IR = 0, 1, 2
+KD_EOS_EPSILON, KD_EOS_PRESSURE, KD_EOS_DENSITY, KD_EOS_DHDRHO = 0, 1, 2, 3
 
 
 class NewtonOpts(C.Structure):
@@ -90,6 +91,7 @@ def _declare_system(lib):
         "kd_newton_step": (I, [P, C.POINTER(NewtonOpts), C.POINTER(NewtonReport)]),
         "kd_newton_step_linesearch": (I, [P, C.POINTER(NewtonOpts), I, D, C.POINTER(NewtonReport), DP]),
         "kd_system_set_cst": (I, [P, C.c_char_p, D]),
+        "kd_system_add_ope_eos": (I, [P, C.c_char_p, I, I, D, D, D, DP, DP]),
         "kd_field_val_point": (I, [P, DP, DP]),
         "kd_system_val_point_gradient": (I, [P, C.c_char_p, DP, DP]),
         "kd_system_dres_dcst": (I, [P, C.c_char_p, DP]),
@@ -365,6 +367,15 @@ class System_of_eqs:
         y = np.zeros(self.get_nbr_unknowns())
         self.ctx.check(_L().kd_system_jx(self.h, _dp(x), _dp(y)))
         return y
+
+    def add_ope_eos(self, name, var, gamma_tab=(2.0,), rho_tab=(0.0,), k0=100.0, rhomin=1e-19, rhomax=1.0):
+        """add_ope(name, &EOS<Cold_PWPoly, var>::action): name(h) in equations.
+        var: KD_EOS_EPSILON / PRESSURE / DENSITY / DHDRHO.  Defaults: the
+        Gamma = 2, K = 100 polytrope of eos/gam2.polytrope."""
+        g = np.ascontiguousarray(gamma_tab, dtype=np.float64)
+        r = np.ascontiguousarray(rho_tab, dtype=np.float64)
+        self.ctx.check(_L().kd_system_add_ope_eos(self.h, name.encode(), int(var), len(g), float(rhomin),
+                                                  float(rhomax), float(k0), _dp(g), _dp(r)))
 
     def set_cst(self, name, value):
         """Changes a double constant registered with add_cst(name, double)."""

@@ -938,6 +938,81 @@ class OSystem:
         return False, err, F, J
 
 
+# ---------------------------------------------------------------- EOS ops --
+def polytrope(npieces=1, rhomin=1e-19, rhomax=1.0, k0=100.0, gamma_tab=(2.0,), rho_tab=(0.0,)):
+    """Cold piecewise polytrope tables as Margherita_setup_polytrope builds
+    them (include/EOS/standalone/setup_polytrope.cc), geometrised units."""
+    g = list(gamma_tab)
+    r = list(rho_tab)
+    k = [k0] + [0.0] * (npieces - 1)
+    eps = [0.0] * npieces
+    h = [0.0] * npieces
+    for i in range(1, npieces):
+        k[i] = k[i - 1] * r[i] ** (g[i - 1] - g[i])
+        eps[i] = eps[i - 1] + k[i - 1] * r[i] ** (g[i - 1] - 1.0) / (g[i - 1] - 1.0) - k[i] * r[i] ** (g[i] - 1.0) / (g[i] - 1.0)
+        P = k[i] * r[i] ** g[i]
+        e = eps[i] + P / r[i] / (g[i] - 1.0)
+        h[i] = 1.0 + e + P / r[i]
+    return dict(n=npieces, rhomin=rhomin, rhomax=rhomax, k=k, gamma=g, rho=r, eps=eps, h=h)
+
+
+def _eos_point(e, var, hv, dh=None):
+    """EOS::term_by_term / term_by_term_variation at one point
+    (include/EOS/EOS.hh:67-160, cold_pwpoly_implementation.hh)."""
+    def clamp(x):
+        return min(max(x, e["rhomin"]), e["rhomax"])
+
+    def piece_rho(x):
+        for nn in range(1, e["n"]):
+            if e["rho"][nn - 1] < x <= e["rho"][nn]:
+                return nn - 1
+        return e["n"] - 1
+    if hv <= 1.0:
+        rho, hh = e["rho"][0], 1.0
+    else:
+        hh = hv
+        idx = e["n"] - 1
+        for nn in range(1, e["n"]):
+            if e["h"][nn - 1] < hv <= e["h"][nn]:
+                idx = nn - 1
+                break
+        gm1 = e["gamma"][idx] - 1.0
+        rho = (gm1 * (hv - 1.0 - e["eps"][idx]) / (e["gamma"][idx] * e["k"][idx])) ** (1.0 / gm1)
+    rho = clamp(rho)
+    i = piece_rho(rho)
+    P = e["k"][i] * rho ** e["gamma"][i]
+    epsc = e["eps"][i] + P / (rho * (e["gamma"][i] - 1.0))
+    dpdrho = e["gamma"][i] * P / rho
+    if dh is None:
+        return [epsc, P, rho, 1.0 / hh * dpdrho][var]
+    drho = rho * 1.0 / dpdrho * dh
+    return [P / rho ** 2 * drho, dpdrho * drho, drho, 0.0][var]
+
+
+def eos_term(t, e, var):
+    """Ope_user with EOS<eos, var>::action on an OTerm (value and tangent)."""
+    v = t.val
+    if v.zero:
+        val = v
+    else:
+        v.coef_i()
+        flat = v.c.reshape(-1)
+        val = VD(v.dom, 1, c=np.array([_eos_point(e, var, x) for x in flat]).reshape(v.c.shape), base=v.base)
+    der = None
+    if t.der is not None:
+        d = t.der
+        if d.zero or v.zero:
+            der = VD.zeros(d.dom, d.B)
+        else:
+            d.coef_i()
+            hv = v.c[0]
+            out = np.empty_like(d.c)
+            for b in range(d.B):
+                out[b] = np.vectorize(lambda x, y: _eos_point(e, var, x, y))(hv, d.c[b])
+            der = VD(d.dom, d.B, c=out, base=d.base)
+    return OTerm(t.dom, val, der)
+
+
 def newton_linesearch_step(sysm, precision, ntrymax=10, stepmax=1.0):
     """do_newton_with_linesearch (src_par/do_newton.cpp:454-516; compute_f
     :594, update_fields :667, compute_old_and_var :676), restated on OSystem.

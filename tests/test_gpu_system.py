@@ -289,3 +289,61 @@ def test_linesearch_newton_matches_oracle(ctx):
             opsi[d].coef()
             assert rel(psi.get_coef(d), opsi[d].cf[0]) < 1e-9, (it, d)
     assert min(lams) < 1.0  # the backtracking branch ran
+
+
+def test_eos_operators_match_oracle(ctx):
+    """User EOS operators eps/press/rho/dHdlnrho (add_ope with
+    EOS<Cold_PWPoly, var>::action) of the Gamma = 2, K = 100 polytrope inside
+    an equation: residual, Jacobian and Newton iterates against the oracle."""
+    from kadath_frontera_gb300.kadath import (CHEB_TYPE, OUTER_BC, KD_EOS_DENSITY, KD_EOS_DHDRHO, KD_EOS_EPSILON,
+                                              KD_EOS_PRESSURE, Scalar, Space_spheric, System_of_eqs)
+    res = (9, 5, 4)
+    space = Space_spheric(CHEB_TYPE, (0, 0, 0), res, (1.0, 2.0))
+    nd = space.get_nbr_domains()
+    psi = Scalar(space, 1.0).std_base()
+    syst = System_of_eqs(space, 0, nd - 1)
+    syst.add_var("psi", psi)
+    for nm, v in (("eps", KD_EOS_EPSILON), ("press", KD_EOS_PRESSURE), ("rho", KD_EOS_DENSITY),
+                  ("dHdlnrho", KD_EOS_DHDRHO)):
+        syst.add_ope_eos(nm, v)
+    eq = "Lap(psi) + 30*rho(1.001*psi^2) + 2*press(1.001*psi^2) - 3*eps(1.001*psi^2) + 0.1*dHdlnrho(1.001*psi^2) = 0"
+    for d in range(nd):
+        syst.add_eq_inside(d, eq)
+    for d in range(nd - 1):
+        syst.add_eq_matching(d, OUTER_BC, "psi")
+        syst.add_eq_matching(d, OUTER_BC, "dn(psi)")
+    syst.add_eq_bc(nd - 1, OUTER_BC, "psi = 1")
+
+    doms = K.space_spheric(res, [1.0, 2.0])
+    opsi = K.scalar_field(doms, lambda d: np.ones(d.np))
+    osys = K.OSystem(doms, 0, nd - 1)
+    osys.add_var("psi", opsi)
+    E = K.polytrope()
+
+    def oeq(T, b):
+        p = T["psi"]
+        c = lambda x: K.OTerm(p.dom, x, None if p.der is None else 0.0)  # noqa: E731
+        h = c(1.001) * p ** 2
+        return (p.lap() + c(30.0) * K.eos_term(h, E, 2) + c(2.0) * K.eos_term(h, E, 1)
+                - c(3.0) * K.eos_term(h, E, 0) + c(0.1) * K.eos_term(h, E, 3))
+    for d in range(nd):
+        osys.add_eq_inside(d, oeq)
+    for d in range(nd - 1):
+        osys.add_eq_matching(d, K.OUTER_BC, lambda T, b: T["psi"])
+        osys.add_eq_matching(d, K.OUTER_BC, lambda T, b: T["psi"].dn(b))
+    osys.add_eq_bc(nd - 1, K.OUTER_BC, lambda T, b: T["psi"] - 1.0)
+
+    F = syst.sec_member()
+    J = syst.jacobian()
+    Fo, Jo = osys.jacobian()
+    assert np.abs(F - Fo).max() <= 1e-12 * max(np.abs(Fo).max(), 1.0)
+    assert rel(J, Jo) < REL
+    for it in range(5):
+        done, err = syst.do_newton(1e-10)
+        odone, oerr, _, _ = osys.newton_step(1e-10)
+        assert done == odone
+        for d in range(nd):
+            opsi[d].coef()
+            assert rel(psi.get_coef(d), opsi[d].cf[0]) < FIELD, (it, d)
+        if done:
+            break
