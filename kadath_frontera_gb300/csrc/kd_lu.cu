@@ -596,6 +596,77 @@ __device__ void block_argmax(V& v, int& i, int& tag, V* rv, int* ri, int* rt) {
 // ever written by its tile's CTA; block rows written by other CTAs are read
 // past L1.
 constexpr int SW_TILE = 64;
+
+// Geometry of one block step of a sweep.
+struct SweepStep {
+  int k, r0, n, q0, q1, first, t1;
+};
+
+__device__ __forceinline__ SweepStep sweep_step(int step, int nblk, int N, int lower, int ntiles) {
+  SweepStep s;
+  s.k = lower ? step : nblk - 1 - step;
+  s.r0 = s.k * TB;
+  s.n = (N - s.r0 < TB) ? N - s.r0 : TB;
+  s.q0 = lower ? s.r0 + s.n : 0;
+  s.q1 = lower ? N : s.r0;
+  const int t0 = s.q0 / SW_TILE;
+  s.t1 = (s.q1 + SW_TILE - 1) / SW_TILE;
+  if (s.t1 > ntiles) s.t1 = ntiles;
+  s.first = t0 - (t0 % static_cast<int>(gridDim.x)) + static_cast<int>(blockIdx.x);
+  if (s.first < t0) s.first += gridDim.x;
+  return s;
+}
+
+// The values this thread needs from Dinv_k and from the factor's block
+// columns for its first two tiles: loaded one step ahead, before the grid
+// barrier, since they do not depend on b.
+template <class T>
+struct SweepPrefetch {
+  double lo[8], hi[8];
+  T va[16], vb[16];
+};
+
+template <class T>
+__device__ __forceinline__ void sweep_prefetch(const T* __restrict__ A, long long ld, const double* __restrict__ Dinv,
+                                               const SweepStep& s, SweepPrefetch<T>& pf) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int quarter = warp & 3, half = warp >> 2;
+  const double* D = Dinv + static_cast<size_t>(s.k) * TB * TB + static_cast<size_t>(warp) * 8 * TB;
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    pf.lo[q] = D[q * TB + lane];
+    pf.hi[q] = D[q * TB + lane + 32];
+  }
+  const int c0 = quarter * 16;
+  {
+    const int t = s.first;
+    const int row = t * SW_TILE + half * 32 + lane;
+    const bool act = t < s.t1 && row >= s.q0 && row < s.q1;
+    const T* a = A + static_cast<long long>(s.r0 + c0) * ld + row;
+#pragma unroll
+    for (int j = 0; j < 16; j++) pf.va[j] = (act && c0 + j < s.n) ? a[static_cast<long long>(j) * ld] : T(0);
+  }
+  {
+    const int t = s.first + gridDim.x;
+    const int row = t * SW_TILE + half * 32 + lane;
+    const bool act = t < s.t1 && row >= s.q0 && row < s.q1;
+    const T* a = A + static_cast<long long>(s.r0 + c0) * ld + row;
+#pragma unroll
+    for (int j = 0; j < 16; j++) pf.vb[j] = (act && c0 + j < s.n) ? a[static_cast<long long>(j) * ld] : T(0);
+  }
+}
+
+// A whole triangular sweep with the factors in one cooperative launch: per
+// 64-row block k (in order for L, reversed for U), every CTA forms
+// x_k = Dinv_k b[block] in FP64 (Dinv_k row-major; warp w owns rows
+// 8w..8w+7, lanes along the row), CTA 0 stores x_k in y, and the rows below
+// (L) or above (U) get b[row] -= A(row, block) x_k; then one grid barrier.
+// Rows go by 64-row tiles, tile t to CTA t % grid: within a CTA, warp w
+// takes rows 32 (w >> 2) .. + 31 of the tile and the 16 block columns
+// 16 (w & 3) .. + 15, and the four column quarters are added in shared
+// memory.  Dinv_k and the block columns of the first two tiles are loaded
+// a step ahead (before the barrier).  A row of b is only ever written by
+// its tile's CTA; block rows written by other CTAs are read past L1.
 template <class T>
 __global__ void __launch_bounds__(256) trsv_sweep(const T* __restrict__ A, long long ld, int N, double* b,
                                                   double* __restrict__ y, const double* __restrict__ Dinv,
@@ -611,24 +682,17 @@ __global__ void __launch_bounds__(256) trsv_sweep(const T* __restrict__ A, long 
   const int ntiles = (N + SW_TILE - 1) / SW_TILE;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int quarter = warp & 3, half = warp >> 2;
+  SweepPrefetch<T> pf;
+  sweep_prefetch(A, ld, Dinv, sweep_step(0, nblk, N, lower, ntiles), pf);
   for (int step = 0; step < nblk; step++) {
-    const int k = lower ? step : nblk - 1 - step;
-    const int r0 = k * TB;
-    const int n = (N - r0 < TB) ? N - r0 : TB;
-    if (tid < TB) bb[tid] = (tid < n) ? __ldcg(b + r0 + tid) : 0.0;
+    const SweepStep s = sweep_step(step, nblk, N, lower, ntiles);
+    if (tid < TB) bb[tid] = (tid < s.n) ? __ldcg(b + s.r0 + tid) : 0.0;
     __syncthreads();
     {
-      const double* D = Dinv + static_cast<size_t>(k) * TB * TB + static_cast<size_t>(warp) * 8 * TB;
-      double lo[8], hi[8];
-#pragma unroll
-      for (int q = 0; q < 8; q++) {
-        lo[q] = D[q * TB + lane];
-        hi[q] = D[q * TB + lane + 32];
-      }
       const double b0 = bb[lane], b1 = bb[lane + 32];
 #pragma unroll
       for (int q = 0; q < 8; q++) {
-        double p = lo[q] * b0 + hi[q] * b1;
+        double p = pf.lo[q] * b0 + pf.hi[q] * b1;
         for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
         if (lane == 0) {
           xx[warp * 8 + q] = p;
@@ -637,21 +701,23 @@ __global__ void __launch_bounds__(256) trsv_sweep(const T* __restrict__ A, long 
       }
     }
     __syncthreads();
-    if (blockIdx.x == 0 && tid < n) y[r0 + tid] = xx[tid];
-    const int q0 = lower ? r0 + n : 0;
-    const int q1 = lower ? N : r0;
-    const int t0 = q0 / SW_TILE, t1 = (q1 + SW_TILE - 1) / SW_TILE;
-    int first = t0 - (t0 % static_cast<int>(gridDim.x)) + static_cast<int>(blockIdx.x);
-    if (first < t0) first += gridDim.x;
-    for (int t = first; t < t1 && t < ntiles; t += gridDim.x) {
+    if (blockIdx.x == 0 && tid < s.n) y[s.r0 + tid] = xx[tid];
+    const int c0 = quarter * 16;
+    int tix = 0;
+    for (int t = s.first; t < s.t1; t += gridDim.x, tix++) {
       const int row = t * SW_TILE + half * 32 + lane;
-      const int c0 = quarter * 16;
       T acc = T(0);
-      if (row >= q0 && row < q1) {
-        const T* a = A + static_cast<long long>(r0 + c0) * ld + row;
+      if (tix == 0) {
+#pragma unroll
+        for (int j = 0; j < 16; j++) acc = fma(pf.va[j], xt[c0 + j], acc);
+      } else if (tix == 1) {
+#pragma unroll
+        for (int j = 0; j < 16; j++) acc = fma(pf.vb[j], xt[c0 + j], acc);
+      } else if (row >= s.q0 && row < s.q1) {
+        const T* a = A + static_cast<long long>(s.r0 + c0) * ld + row;
         T v[16];
 #pragma unroll
-        for (int j = 0; j < 16; j++) v[j] = (c0 + j < n) ? a[static_cast<long long>(j) * ld] : T(0);
+        for (int j = 0; j < 16; j++) v[j] = (c0 + j < s.n) ? a[static_cast<long long>(j) * ld] : T(0);
 #pragma unroll
         for (int j = 0; j < 16; j++) acc = fma(v[j], xt[c0 + j], acc);
       }
@@ -659,11 +725,12 @@ __global__ void __launch_bounds__(256) trsv_sweep(const T* __restrict__ A, long 
       __syncthreads();
       if (tid < SW_TILE) {
         const int r = t * SW_TILE + tid;
-        if (r >= q0 && r < q1)
+        if (r >= s.q0 && r < s.q1)
           b[r] = __ldcg(b + r) - static_cast<double>((part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]));
       }
       __syncthreads();
     }
+    if (step + 1 < nblk) sweep_prefetch(A, ld, Dinv, sweep_step(step + 1, nblk, N, lower, ntiles), pf);
     if (!grid_barrier(bar, gridDim.x * static_cast<unsigned>(step + 1), err, &s_ok)) return;
   }
 }
