@@ -63,16 +63,48 @@ void DeviceArena::release_to(size_t m) {
 Context::Context(int device) : device_(device) {
   cuda_check(cudaSetDevice(device), "cudaSetDevice");
   cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+  cur_ = stream_;
   pool_cap_ = size_t(4) << 20;  // 4 Mi doubles = 32 MB of operator matrices
   cuda_check(cudaMalloc(&d_pool_, pool_cap_ * sizeof(double)), "cudaMalloc(matrix pool)");
 }
 
 Context::~Context() {
+  for (auto st : side_) cudaStreamSynchronize(st);
   cudaStreamSynchronize(stream_);
+  for (auto st : side_) cudaStreamDestroy(st);
+  for (auto e : side_ev_) cudaEventDestroy(e);
+  if (fork_ev_) cudaEventDestroy(fork_ev_);
   for (auto& kv : itables_) cudaFree(kv.second);
   for (auto& kv : dtables_) cudaFree(kv.second);
   cudaFree(d_pool_);
   cudaStreamDestroy(stream_);
+}
+
+void Context::fork(int n) {
+  if (n < 1) n = 1;
+  if (!fork_ev_) cuda_check(cudaEventCreateWithFlags(&fork_ev_, cudaEventDisableTiming), "cudaEventCreate");
+  while (static_cast<int>(side_.size()) < n) {
+    cudaStream_t st;
+    cudaEvent_t e;
+    cuda_check(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate(side)");
+    cuda_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate(side)");
+    side_.push_back(st);
+    side_ev_.push_back(e);
+  }
+  cuda_check(cudaEventRecord(fork_ev_, stream_), "record fork");
+  for (int i = 0; i < n; i++) cuda_check(cudaStreamWaitEvent(side_[i], fork_ev_, 0), "side waits main");
+  nfork_ = n;
+}
+
+void Context::use(int i) { cur_ = (i < 0 || nfork_ == 0) ? stream_ : side_[i % nfork_]; }
+
+void Context::join() {
+  for (int i = 0; i < nfork_; i++) {
+    cuda_check(cudaEventRecord(side_ev_[i], side_[i]), "record join");
+    cuda_check(cudaStreamWaitEvent(stream_, side_ev_[i], 0), "main waits side");
+  }
+  nfork_ = 0;
+  cur_ = stream_;
 }
 
 const double* Context::pool() {
@@ -158,7 +190,7 @@ void Context::run_items(const std::vector<KdItem>& items, const std::vector<int>
       flops += f * (list.prefix[q + 1] - list.prefix[q]);
     }
     ProfScope ps(this, PROF_LINE_PASS, flops);
-    cuda_check(launch_line_passes(list, smem, dp, stream_), "line_passes kernel");
+    cuda_check(launch_line_passes(list, smem, dp, stream()), "line_passes kernel");
     launches++;
   }
 }
@@ -186,13 +218,13 @@ void Context::prof_begin(int cat) {
   (void)cat;
   if (!prof_on_) return;
   pending_begin_ = next_event();
-  cuda_check(cudaEventRecord(pending_begin_, stream_), "cudaEventRecord");
+  cuda_check(cudaEventRecord(pending_begin_, stream()), "cudaEventRecord");
 }
 
 void Context::prof_end(int cat, double work) {
   if (!prof_on_ || !pending_begin_) return;
   cudaEvent_t e = next_event();
-  cuda_check(cudaEventRecord(e, stream_), "cudaEventRecord");
+  cuda_check(cudaEventRecord(e, stream()), "cudaEventRecord");
   prof_.push_back({cat, pending_begin_, e, work});
   pending_begin_ = nullptr;
 }

@@ -51,7 +51,17 @@ class Context {
   ~Context();
 
   int device() const { return device_; }
-  cudaStream_t stream() const { return stream_; }
+  // The stream work is issued on: the context's main stream, or one of the
+  // side streams between fork() and join().
+  cudaStream_t stream() const { return cur_; }
+  cudaStream_t main_stream() const { return stream_; }
+  // Side streams for independent work (the per-domain equations of a value
+  // pass): fork() makes n side streams wait for the main stream's work so
+  // far, use(i) issues on side stream i % n (i < 0: the main stream), join()
+  // makes the main stream wait for every side stream and goes back to it.
+  void fork(int n);
+  void use(int i);
+  void join();
 
   MatrixBank& bank() { return bank_; }
   // Makes sure every matrix in the bank is present in the device pool.
@@ -122,6 +132,11 @@ class Context {
  private:
   int device_;
   cudaStream_t stream_ = nullptr;
+  cudaStream_t cur_ = nullptr;
+  std::vector<cudaStream_t> side_;
+  std::vector<cudaEvent_t> side_ev_;
+  cudaEvent_t fork_ev_ = nullptr;
+  int nfork_ = 0;
   MatrixBank bank_;
   double* d_pool_ = nullptr;
   size_t pool_cap_ = 0, pool_uploaded_ = 0;

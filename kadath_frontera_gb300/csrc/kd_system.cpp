@@ -568,7 +568,19 @@ void System::residual(double* d_F, bool record) {
   st.vcache = record ? &vcache_ : nullptr;
   st.record = record;
   std::vector<Term> lhs(eqs_.size()), rhs(eqs_.size());
+  if (d_F && nbr_conditions_ >= 0)
+    cuda_check(cudaMemsetAsync(d_F, 0, sizeof(double) * nbr_conditions_, ctx->main_stream()), "memset F");
+  // The equations of different domains are independent (fields are only
+  // read, temporaries come from the pass's arena): one side stream per
+  // domain, so that their small kernels overlap on the GPU.
+  struct Fork {
+    Context* c;
+    Fork(Context* c_, int n) : c(c_) { c->fork(n); }
+    ~Fork() { c->join(); }
+  } fork(ctx, ndom() < 8 ? ndom() : 8);
+  auto stream_of = [&](const Equation& eq) { return eq.dom - dom_min; };
   for (size_t i = 0; i < eqs_.size(); i++) {
+    ctx->use(stream_of(eqs_[i]));
     lhs[i] = eqs_[i].lhs->eval(st);
     if (eqs_[i].kind == Equation::MATCHING) rhs[i] = eqs_[i].rhs->eval(st);
   }
@@ -581,11 +593,17 @@ void System::residual(double* d_F, bool record) {
       row += eqs_[i].n_cond;
     }
     nbr_conditions_ = row;
+    if (d_F) {
+      ctx->use(-1);
+      cuda_check(cudaMemsetAsync(d_F, 0, sizeof(double) * nbr_conditions_, ctx->main_stream()), "memset F");
+      ctx->join();
+      ctx->fork(ndom() < 8 ? ndom() : 8);
+    }
   }
   if (!d_F) return;
-  cuda_check(cudaMemsetAsync(d_F, 0, sizeof(double) * nbr_conditions_, ctx->stream()), "memset F");
   for (size_t i = 0; i < eqs_.size(); i++) {
     Equation& eq = eqs_[i];
+    ctx->use(stream_of(eq));
     double* out = d_F + eq.row0;
     if (eq.kind == Equation::MATCHING) {
       export_term(eq, lhs[i], false, eq.dom, eq.bound, out, 0, 1, 1, 1.0, false);
