@@ -641,13 +641,26 @@ void System::jacobian(double* d_J, long long ld, bool reuse) {
   }
   if (!vdoubles_.empty()) throw KdError(KD_ERR_UNSUPPORTED, "double unknowns are not supported yet");
   cuda_check(cudaMemsetAsync(d_J, 0, sizeof(double) * ld * N, ctx->stream()), "memset J");
+  // Seed blocks write disjoint column blocks: a wave of them runs on side
+  // streams; the scratch arena is reset only between waves.
+  std::vector<std::pair<int, int>> blocks;
   for (size_t v = 0; v < vars_.size(); v++)
-    for (int dd = dom_min; dd <= dom_max; dd++) {
+    for (int dd = dom_min; dd <= dom_max; dd++) blocks.emplace_back(static_cast<int>(v), dd);
+  const int wave = 6;
+  for (size_t w0 = 0; w0 < blocks.size(); w0 += wave) {
+    ctx->scratch().reset();
+    struct Fork {
+      Context* c;
+      Fork(Context* c_, int n) : c(c_) { c->fork(n); }
+      ~Fork() { c->join(); }
+    } fork(ctx, wave);
+    for (size_t bix = w0; bix < blocks.size() && bix < w0 + wave; bix++) {
+      const int v = blocks[bix].first, dd = blocks[bix].second;
+      ctx->use(static_cast<int>(bix - w0));
       int B;
       Base base;
       const double* seeds = seed_block(static_cast<int>(v), dd, B, base);
       if (B == 0) continue;
-      ctx->scratch().reset();
       EvalState st;
       st.sys = this;
       st.with_der = true;
@@ -671,6 +684,7 @@ void System::jacobian(double* d_J, long long ld, bool reuse) {
         }
       }
     }
+  }
 }
 
 // x -> coefficient map of one (variable, domain): affecte_tau
