@@ -77,7 +77,23 @@ Context::~Context() {
   for (auto& kv : itables_) cudaFree(kv.second);
   for (auto& kv : dtables_) cudaFree(kv.second);
   cudaFree(d_pool_);
+  for (void* w : ws_) cudaFree(w);
   cudaStreamDestroy(stream_);
+}
+
+void* Context::workspace(int slot, size_t bytes, bool* fresh) {
+  if (slot < 0 || slot >= WS_NSLOT) throw KdError(KD_ERR_ARG, "workspace slot out of range");
+  if (fresh) *fresh = false;
+  if (bytes > ws_cap_[slot]) {
+    if (capturing) throw KdError(KD_ERR_STATE, "workspace grew during graph capture");
+    cudaFree(ws_[slot]);  // synchronises the device: no launch still reads it
+    ws_[slot] = nullptr;
+    ws_cap_[slot] = 0;
+    cuda_check(cudaMalloc(&ws_[slot], bytes), "cudaMalloc(workspace)");
+    ws_cap_[slot] = bytes;
+    if (fresh) *fresh = true;
+  }
+  return ws_[slot];
 }
 
 void Context::fork(int n) {
@@ -128,9 +144,13 @@ const int* Context::table(const std::vector<int>& content) {
   int* p = nullptr;
   size_t n = content.empty() ? 1 : content.size();
   cuda_check(cudaMalloc(&p, n * sizeof(int)), "cudaMalloc(table)");
-  if (!content.empty())
-    cuda_check(cudaMemcpy(p, content.data(), content.size() * sizeof(int), cudaMemcpyHostToDevice),
+  if (!content.empty()) {
+    // ordered on this context's (non-blocking) stream and finished before
+    // any later launch, whichever stream that launch goes to
+    cuda_check(cudaMemcpyAsync(p, content.data(), content.size() * sizeof(int), cudaMemcpyHostToDevice, stream_),
                "upload table");
+    cuda_check(cudaStreamSynchronize(stream_), "sync after table upload");
+  }
   itables_[content] = p;
   return p;
 }
@@ -142,9 +162,13 @@ const double* Context::dtable(const std::vector<double>& content) {
   double* p = nullptr;
   size_t n = content.empty() ? 1 : content.size();
   cuda_check(cudaMalloc(&p, n * sizeof(double)), "cudaMalloc(dtable)");
-  if (!content.empty())
-    cuda_check(cudaMemcpy(p, content.data(), content.size() * sizeof(double), cudaMemcpyHostToDevice),
+  if (!content.empty()) {
+    // ordered on this context's (non-blocking) stream and finished before
+    // any later launch, whichever stream that launch goes to
+    cuda_check(cudaMemcpyAsync(p, content.data(), content.size() * sizeof(double), cudaMemcpyHostToDevice, stream_),
                "upload dtable");
+    cuda_check(cudaStreamSynchronize(stream_), "sync after dtable upload");
+  }
   dtables_[content] = p;
   return p;
 }

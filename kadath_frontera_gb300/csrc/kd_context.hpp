@@ -82,6 +82,13 @@ class Context {
   }
   DeviceArena& persistent() { return persistent_; }
 
+  // Device workspaces owned by the context, one per slot, grown on demand
+  // (contents are not kept across growth; *fresh tells the caller the
+  // buffer is new).  Work of one context is ordered on its streams, so
+  // contexts driven from different host threads never share a workspace.
+  enum WorkSlot : int { WS_TC_A = 0, WS_TC_B = 1, WS_TC_FLAG = 2, WS_NSLOT = 3 };
+  void* workspace(int slot, size_t bytes, bool* fresh = nullptr);
+
   // While a CUDA graph is being captured no host->device upload may happen;
   // the first (uncaptured) evaluation fills every cache.
   bool capturing = false;
@@ -145,6 +152,8 @@ class Context {
   DeviceArena scratch_;
   DeviceArena* active_scratch_ = &scratch_;
   DeviceArena persistent_{size_t(64) << 20};
+  void* ws_[WS_NSLOT] = {};
+  size_t ws_cap_[WS_NSLOT] = {};
 };
 
 // Times one launch (or a short sequence) when profiling is on.

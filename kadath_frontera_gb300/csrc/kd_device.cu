@@ -292,12 +292,10 @@ cudaError_t launch_line_passes(const KdItemList& list, int smem_doubles, const d
   }
   if (total_fields <= LP_CLUSTER_MAX_FIELDS) {
     // few fields: eight SMs per field
-    static bool attr = false;
-    if (!attr || smem > 48 * 1024) {
+    if (smem > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(line_passes_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           static_cast<int>(smem > 48 * 1024 ? smem : 48 * 1024));
+                                           static_cast<int>(smem));
       if (e != cudaSuccess) return e;
-      attr = true;
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(total_fields * LP_CL, 1, 1);

@@ -495,13 +495,6 @@ void make_map(CUtensorMap* m, const void* ptr, long long inner, long long outer,
   if (r != CUDA_SUCCESS) throw KdError(KD_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string(r) + ")");
 }
 
-struct TcWork {
-  float* at = nullptr;
-  float* bt = nullptr;
-  size_t cap_a = 0, cap_b = 0;
-  int* err = nullptr;
-};
-TcWork g_tc;
 
 int grid_for(long long n) {
   long long g = (n + 255) / 256;
@@ -532,26 +525,18 @@ void tf32_gemm_update(Context* ctx, int m, int n, int k, const float* A, long lo
   const int npad = ((n + TC_N - 1) / TC_N) * TC_N;
   // hi parts first, lo parts (3xTF32) right after them
   size_t need_a = static_cast<size_t>(mpad) * kpad, need_b = static_cast<size_t>(npad) * kpad;
-  if (2 * need_a > g_tc.cap_a) {
-    cudaFree(g_tc.at);
-    cuda_check(cudaMalloc(&g_tc.at, 2 * need_a * sizeof(float)), "cudaMalloc(At)");
-    g_tc.cap_a = 2 * need_a;
-  }
-  if (2 * need_b > g_tc.cap_b) {
-    cudaFree(g_tc.bt);
-    cuda_check(cudaMalloc(&g_tc.bt, 2 * need_b * sizeof(float)), "cudaMalloc(Bt)");
-    g_tc.cap_b = 2 * need_b;
-  }
-  if (!g_tc.err) {
-    cuda_check(cudaMalloc(&g_tc.err, sizeof(int)), "cudaMalloc(err)");
-    cuda_check(cudaMemsetAsync(g_tc.err, 0, sizeof(int), s), "memset err");
-  }
-  float* at_lo = g_tc.at + need_a;
-  float* bt_lo = g_tc.bt + need_b;
+  // packed operands and the timeout flag live in the context's workspaces
+  float* at = static_cast<float*>(ctx->workspace(Context::WS_TC_A, 2 * need_a * sizeof(float)));
+  float* bt = static_cast<float*>(ctx->workspace(Context::WS_TC_B, 2 * need_b * sizeof(float)));
+  bool fresh = false;
+  int* err = static_cast<int*>(ctx->workspace(Context::WS_TC_FLAG, sizeof(int), &fresh));
+  if (fresh) cuda_check(cudaMemsetAsync(err, 0, sizeof(int), s), "memset err");
+  float* at_lo = at + need_a;
+  float* bt_lo = bt + need_b;
   // A is column-major m x k (contiguous along m); B is column-major k x n
   // (contiguous along k).
-  pack_kmajor<<<grid_for(need_a), 256, 0, s>>>(A, lda, m, k, 1, g_tc.at, split3 ? at_lo : nullptr, mpad, kpad);
-  pack_kmajor<<<grid_for(need_b), 256, 0, s>>>(B, ldb, n, k, 0, g_tc.bt, split3 ? bt_lo : nullptr, npad, kpad);
+  pack_kmajor<<<grid_for(need_a), 256, 0, s>>>(A, lda, m, k, 1, at, split3 ? at_lo : nullptr, mpad, kpad);
+  pack_kmajor<<<grid_for(need_b), 256, 0, s>>>(B, ldb, n, k, 0, bt, split3 ? bt_lo : nullptr, npad, kpad);
   ctx->launches += 2;
   const int nkb = kpad / TC_KBLK;
   // TMA clips the stored rows at 16-byte granularity: rows up to m rounded
@@ -561,22 +546,21 @@ void tf32_gemm_update(Context* ctx, int m, int n, int k, const float* A, long lo
   if (reinterpret_cast<uintptr_t>(C) % 16 == 0 && ldc % 4 == 0 && m4 <= c_rows_writable && encode_fn()) {
     // persistent TMA pipeline
     CUtensorMap mA, mB, mAl, mBl, mC;
-    make_map(&mA, g_tc.at, kpad, mpad, static_cast<long long>(kpad) * 4, TC_KBLK, TC_M, true);
-    make_map(&mB, g_tc.bt, kpad, npad, static_cast<long long>(kpad) * 4, TC_KBLK, TC_N, true);
+    make_map(&mA, at, kpad, mpad, static_cast<long long>(kpad) * 4, TC_KBLK, TC_M, true);
+    make_map(&mB, bt, kpad, npad, static_cast<long long>(kpad) * 4, TC_KBLK, TC_N, true);
     make_map(&mAl, at_lo, kpad, mpad, static_cast<long long>(kpad) * 4, TC_KBLK, TC_M, true);
     make_map(&mBl, bt_lo, kpad, npad, static_cast<long long>(kpad) * 4, TC_KBLK, TC_N, true);
     make_map(&mC, C, m, n, ldc * 4, TC_M, P_CCOLS, false);
     static int nsm = 0;
-    static bool pattr = false;
-    if (!pattr) {
+    static std::once_flag pattr;
+    std::call_once(pattr, [] {
       int dev = 0;
       cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
       cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "SM count");
       cuda_check(cudaFuncSetAttribute(tf32_update_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       static_cast<int>(P_MAX_SMEM)),
                  "cudaFuncSetAttribute(tf32 persistent)");
-      pattr = true;
-    }
+    });
     // shared memory: operands (x2 for the lo parts) + a ring of C chunks,
     // four slots when they fit, else two
     const size_t ops = static_cast<size_t>(split3 ? 4 : 2) * nkb * P_OPBLK_BYTES;
@@ -586,7 +570,7 @@ void tf32_gemm_update(Context* ctx, int m, int n, int k, const float* A, long lo
     const int ntm = mpad / TC_M, ntiles = ntm * (npad / TC_N);
     const int grid = ntiles < nsm ? ntiles : nsm;
     tf32_update_persistent<<<grid, P_THREADS, psmem, s>>>(mA, mB, mAl, mBl, mC, nkb, ntm, ntiles, split3 ? 1 : 0, ncs,
-                                                          g_tc.err);
+                                                          err);
     ctx->launches += 1;
     cuda_check(cudaGetLastError(), "tcgen05 trailing update (persistent)");
     return;
@@ -596,25 +580,29 @@ void tf32_gemm_update(Context* ctx, int m, int n, int k, const float* A, long lo
   // allocation never has to wait for another CTA to finish.
   size_t smem = 1024 + static_cast<size_t>(2 * nkb) * 128 * 128;
   if (smem < TC_MIN_SMEM) smem = TC_MIN_SMEM;
-  static bool attr = false;
-  if (!attr) {
+  static std::once_flag attr;
+  std::call_once(attr, [] {
     cuda_check(cudaFuncSetAttribute(tf32_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     1024 + 2 * (TC_MAXK / TC_KBLK) * 128 * 128),
                "cudaFuncSetAttribute(tf32)");
-    attr = true;
-  }
+  });
   dim3 grid(mpad / TC_M, npad / TC_N);
-  tf32_update_kernel<<<grid, TC_THREADS, smem, s>>>(g_tc.at, g_tc.bt, kpad, C, ldc, m, n, g_tc.err);
+  tf32_update_kernel<<<grid, TC_THREADS, smem, s>>>(at, bt, kpad, C, ldc, m, n, err);
   ctx->launches += 1;
   cuda_check(cudaGetLastError(), "tcgen05 trailing update");
 }
 
 int tf32_gemm_error_flag(Context* ctx) {
-  if (!g_tc.err) return 0;
+  bool fresh = false;
+  int* err = static_cast<int*>(ctx->workspace(Context::WS_TC_FLAG, sizeof(int), &fresh));
+  if (fresh) {  // no update has run on this context yet
+    cuda_check(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream()), "memset err");
+    return 0;
+  }
   int h = 0;
-  cuda_check(cudaMemcpyAsync(&h, g_tc.err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream()), "D2H err");
+  cuda_check(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream()), "D2H err");
   cuda_check(cudaStreamSynchronize(ctx->stream()), "sync");
-  if (h) cuda_check(cudaMemsetAsync(g_tc.err, 0, sizeof(int), ctx->stream()), "reset err");
+  if (h) cuda_check(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream()), "reset err");
   return h;
 }
 

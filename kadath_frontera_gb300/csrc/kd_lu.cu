@@ -13,6 +13,7 @@
 
 #include <chrono>
 #include <cmath>
+#include <mutex>
 #include <cstring>
 #include <type_traits>
 #include <vector>
@@ -306,6 +307,58 @@ __global__ void gemv_finish(const double* __restrict__ part, int nchunk, int N, 
   y[row] = alpha * s + (b ? beta * b[row] : 0.0);
 }
 
+// ---- vector algebra of GMRES (fixed reduction order: bitwise reproducible) --
+constexpr int VA_THREADS = 256;
+
+// h[i] = V_i . w for the k basis vectors V_i = V + i N: one CTA per i.
+__global__ void basis_dots(const double* __restrict__ V, int N, int k, const double* __restrict__ w,
+                           double* __restrict__ h) {
+  __shared__ double part[VA_THREADS];
+  const int i = blockIdx.x;
+  const double* v = V + static_cast<size_t>(i) * N;
+  double acc = 0.0;
+  for (int t = threadIdx.x; t < N; t += VA_THREADS) acc = fma(v[t], w[t], acc);
+  part[threadIdx.x] = acc;
+  __syncthreads();
+  for (int st = VA_THREADS / 2; st > 0; st >>= 1) {
+    if (static_cast<int>(threadIdx.x) < st) part[threadIdx.x] += part[threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && i < k) h[i] = part[0];
+}
+
+// w -= sum_i h[i] V_i over the k basis vectors.
+__global__ void basis_subtract(const double* __restrict__ V, int N, int k, const double* __restrict__ h,
+                               double* __restrict__ w) {
+  const int t = blockIdx.x * VA_THREADS + threadIdx.x;
+  if (t >= N) return;
+  double acc = 0.0;
+  for (int i = 0; i < k; i++) acc = fma(h[i], V[static_cast<size_t>(i) * N + t], acc);
+  w[t] -= acc;
+}
+
+// out = sum_t x[t]^2 (a single CTA, fixed order).
+__global__ void sum_squares(const double* __restrict__ x, int N, double* __restrict__ out) {
+  __shared__ double part[VA_THREADS];
+  double acc = 0.0;
+  for (int t = threadIdx.x; t < N; t += VA_THREADS) acc = fma(x[t], x[t], acc);
+  part[threadIdx.x] = acc;
+  __syncthreads();
+  for (int st = VA_THREADS / 2; st > 0; st >>= 1) {
+    if (static_cast<int>(threadIdx.x) < st) part[threadIdx.x] += part[threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = part[0];
+}
+
+// y = alpha x, or y += alpha x when accumulate is set.
+__global__ void scaled_copy(int N, double alpha, const double* __restrict__ x, double* __restrict__ y,
+                            int accumulate) {
+  const int t = blockIdx.x * VA_THREADS + threadIdx.x;
+  if (t >= N) return;
+  y[t] = accumulate ? fma(alpha, x[t], y[t]) : alpha * x[t];
+}
+
 int blocks(long long n, int t) { return static_cast<int>((n + t - 1) / t); }
 
 double now_ms() {
@@ -328,7 +381,7 @@ DenseLU::DenseLU(Context* ctx) : ctx_(ctx) {
                             sizeof(int) * 2 * static_cast<size_t>(nsm_) + 32;
   const size_t map_bytes = sizeof(int) * (1 + 4 * 128) + 60;  // + padding to 16 bytes
   cuda_check(cudaMalloc(&slot_mem_, slot_bytes + map_bytes + 16), "cudaMalloc(panel slots)");
-  cuda_check(cudaMemset(slot_mem_, 0, slot_bytes + map_bytes + 16), "memset panel slots");
+  cuda_check(cudaMemsetAsync(slot_mem_, 0, slot_bytes + map_bytes + 16, ctx_->stream()), "memset panel slots");
   swap_map_ = reinterpret_cast<int*>(static_cast<char*>(slot_mem_) + slot_bytes);
   tri_bar_ = reinterpret_cast<unsigned*>(static_cast<char*>(slot_mem_) + slot_bytes + map_bytes);
   panel_err_ = reinterpret_cast<int*>(static_cast<char*>(slot_mem_) + slot_bytes - 16);
@@ -344,6 +397,7 @@ DenseLU::~DenseLU() {
   cudaFree(eq_buf_);
   cudaFree(part_);
   cudaFree(work_);
+  if (hproj_) cudaFreeHost(hproj_);
   cudaFree(work32_);
   cudaFree(dinv_l_);
   cudaFree(dinv_u_);
@@ -1050,9 +1104,9 @@ static bool panel_cluster16(Context* ctx, float* A, long long ld, int N, int j0,
   const int per = (rows + CP_CL - 1) / CP_CL;
   const size_t smem = static_cast<size_t>(per) * jb * sizeof(float);
   if (smem > CP_MAX_SMEM) return false;
-  static int usable = -1;
-  if (usable < 0) {
-    usable = 0;
+  static int usable = 0;
+  static std::once_flag probe;
+  std::call_once(probe, [] {
     if (cudaFuncSetAttribute(panel_cluster16_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
             cudaSuccess &&
         cudaFuncSetAttribute(panel_cluster16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1073,7 +1127,7 @@ static bool panel_cluster16(Context* ctx, float* A, long long ld, int N, int j0,
         usable = 1;
     }
     cudaGetLastError();  // clear a refused attribute or query
-  }
+  });
   if (!usable) return false;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(CP_CL, 1, 1);
@@ -1185,13 +1239,12 @@ static bool panel_grid(Context* ctx, T* A, long long ld, int N, int j0, int jb, 
   nblk = (rows + per - 1) / per;
   const size_t smem = static_cast<size_t>(per) * jb * sizeof(T);
   if (smem > GP_MAX_SMEM) return false;
-  static bool attr = false;
-  if (!attr) {
+  static std::once_flag attr;
+  std::call_once(attr, [] {
     cuda_check(cudaFuncSetAttribute(panel_grid_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     static_cast<int>(GP_MAX_SMEM)),
                "cudaFuncSetAttribute(panel)");
-    attr = true;
-  }
+  });
   cudaStream_t s = ctx->stream();
   cuda_check(cudaMemsetAsync(slots.bar, 0, sizeof(unsigned), s), "memset barrier");
   cudaLaunchConfig_t cfg = {};
@@ -1265,11 +1318,9 @@ static void trsm_and_swaps(Context* ctx, T* A, long long ld, int N, int j0, int 
   }
   if (j0 + jb < N) {
     size_t smem = sizeof(double) * (static_cast<size_t>(jb) * jb + static_cast<size_t>(jb) * TRSM_COLS);
-    static bool attr_set = false;
-    if (!attr_set) {
-      cudaFuncSetAttribute(trsm_unit_lower<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-      attr_set = true;
-    }
+    static std::once_flag attr_set;
+    std::call_once(attr_set,
+                   [] { cudaFuncSetAttribute(trsm_unit_lower<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); });
     if constexpr (std::is_same<T, float>::value) {
       if (jb <= TRSM32_NB) {
         trsm_unit_lower_f32<<<blocks(N - j0 - jb, TRSM32_THREADS), TRSM32_THREADS, 0, s>>>(A, ld, j0, jb, j0 + jb, N);
@@ -1393,9 +1444,11 @@ void DenseLU::factor(double* A, long long ld, int N, int mode) {
   cuda_check(cudaStreamSynchronize(ctx_->stream()), "sync after LU");
   stats.t_factor_ms = now_ms() - t0;
   int perr = 0;
-  cuda_check(cudaMemcpy(&perr, panel_err_, sizeof(int), cudaMemcpyDeviceToHost), "D2H panel flag");
+  cuda_check(cudaMemcpyAsync(&perr, panel_err_, sizeof(int), cudaMemcpyDeviceToHost, ctx_->stream()),
+             "D2H panel flag");
+  cuda_check(cudaStreamSynchronize(ctx_->stream()), "sync panel flag");
   if (perr) {
-    cuda_check(cudaMemset(panel_err_, 0, sizeof(int)), "reset panel flag");
+    cuda_check(cudaMemsetAsync(panel_err_, 0, sizeof(int), ctx_->stream()), "reset panel flag");
     throw KdError(KD_ERR_TIMEOUT, "panel factorisation: a grid barrier wait ran out");
   }
   if (mode == LU_TF32_IR && tf32_gemm_error_flag(ctx_))
@@ -1499,12 +1552,11 @@ void DenseLU::prepare_solves(const T* LU, long long ld, int N) {
   }
   build_perm<<<1, 1, 0, s>>>(ipiv_, N, perm_);
   size_t smem = sizeof(double) * 3 * TB * TB;
-  static bool attr_set = false;
-  if (!attr_set) {
+  static std::once_flag attr_set;
+  std::call_once(attr_set, [smem] {
     cudaFuncSetAttribute(invert_diag_blocks<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     cudaFuncSetAttribute(invert_diag_blocks<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-    attr_set = true;
-  }
+  });
   invert_diag_blocks<T><<<nblk, TB, smem, s>>>(LU, ld, N, dinv_l_, dinv_u_);
   ctx_->launches += 2;
   cuda_check(cudaGetLastError(), "solve preparation");
@@ -1534,26 +1586,47 @@ void DenseLU::gemv(const double* x, double* y, double alpha, double beta, const 
 }
 
 void DenseLU::gmres_ir(double* b) {
+  // Right-preconditioned GMRES(m), M^-1 = the FP32 factors.  The basis is
+  // orthogonalised by classical Gram-Schmidt run twice (CGS2): per
+  // iteration two rounds of dot products and one norm on the device, one
+  // copy of the results to the host; the small Hessenberg least-squares
+  // problem is solved on the host.  Restarted at most 4 times.
   const int N = N_;
   const int m = gmres_max_iter;
   cudaStream_t s = ctx_->stream();
-  ensure_work(static_cast<size_t>(N) * (m + 4));
-  double* V = work_;                                  // m+1 basis vectors
+  const size_t hn_at = 2 * static_cast<size_t>(m + 1);  // projections of both rounds, then |w|^2
+  ensure_work(static_cast<size_t>(N) * (m + 4) + hn_at + 1);
+  if (hproj_cap_ < hn_at + 1) {
+    if (hproj_) cudaFreeHost(hproj_);
+    hproj_ = nullptr;
+    hproj_cap_ = 0;
+    cuda_check(cudaMallocHost(&hproj_, (hn_at + 1) * sizeof(double)), "cudaMallocHost(projections)");
+    hproj_cap_ = hn_at + 1;
+  }
+  double* V = work_;  // m + 1 basis vectors
   double* w = work_ + static_cast<size_t>(N) * (m + 1);
   double* x = w + N;
   double* r = x + N;
-  auto dot = [&](const double* a, const double* c) {
-    double res;
-    cublasDdot(blas_, N, a, 1, c, 1, &res);
-    return res;
+  double* dproj = r + N;  // [0, m+1): round 1, [m+1, 2m+2): round 2, [2m+2]: |w|^2
+  const int nb = blocks(N, VA_THREADS);
+  auto copy_scaled = [&](const double* src, double alpha, double* dst) {
+    scaled_copy<<<nb, VA_THREADS, 0, s>>>(N, alpha, src, dst, 0);
+    ctx_->launches++;
   };
-  auto nrm = [&](const double* a) {
-    double res;
-    cublasDnrm2(blas_, N, a, 1, &res);
-    return res;
+  auto add_scaled = [&](const double* src, double alpha, double* dst) {
+    scaled_copy<<<nb, VA_THREADS, 0, s>>>(N, alpha, src, dst, 1);
+    ctx_->launches++;
   };
-  cudaMemsetAsync(x, 0, sizeof(double) * N, s);
-  double bnorm = nrm(b);
+  auto norm = [&](const double* v) {
+    sum_squares<<<1, VA_THREADS, 0, s>>>(v, N, dproj + hn_at);
+    ctx_->launches++;
+    cuda_check(cudaMemcpyAsync(hproj_ + hn_at, dproj + hn_at, sizeof(double), cudaMemcpyDeviceToHost, s),
+               "D2H norm");
+    cuda_check(cudaStreamSynchronize(s), "sync norm");
+    return std::sqrt(hproj_[hn_at]);
+  };
+  cuda_check(cudaMemsetAsync(x, 0, sizeof(double) * N, s), "memset x");
+  const double bnorm = norm(b);
   if (bnorm == 0) return;
   int total_it = 0;
   for (int restart = 0; restart < 4; restart++) {
@@ -1562,43 +1635,45 @@ void DenseLU::gmres_ir(double* b) {
       ProfScope ps(ctx_, Context::PROF_GMRES, 8.0 * double(N) * N);
       gemv(x, r, -1.0, 1.0, b);
     }
-    double beta = nrm(r);
+    const double beta = norm(r);
     stats.final_rel_residual = beta / bnorm;
     if (beta / bnorm < gmres_tol) break;
     std::vector<double> H(static_cast<size_t>(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1, 0.0);
     g[0] = beta;
-    double inv = 1.0 / beta;
-    cublasDcopy(blas_, N, r, 1, V, 1);
-    cublasDscal(blas_, N, &inv, V, 1);
+    copy_scaled(r, 1.0 / beta, V);
     int k = 0;
     for (; k < m; k++) {
-      // w = A M^{-1} v_k
-      cublasDcopy(blas_, N, V + static_cast<size_t>(k) * N, 1, r, 1);
+      // w = A M^-1 v_k
+      copy_scaled(V + static_cast<size_t>(k) * N, 1.0, r);
       solve_f32(r);
       {
         ProfScope ps(ctx_, Context::PROF_GMRES, 8.0 * double(N) * N);
         gemv(r, w, 1.0, 0.0, nullptr);
       }
-      for (int i = 0; i <= k; i++) {  // modified Gram-Schmidt
-        double h = dot(w, V + static_cast<size_t>(i) * N);
-        H[i * m + k] = h;
-        double mh = -h;
-        cublasDaxpy(blas_, N, &mh, V + static_cast<size_t>(i) * N, 1, w, 1);
+      // two rounds of w -= V (V^T w) over v_0 .. v_k, then |w|^2
+      const int kk = k + 1;
+      for (int round = 0; round < 2; round++) {
+        double* h = dproj + static_cast<size_t>(round) * (m + 1);
+        basis_dots<<<kk, VA_THREADS, 0, s>>>(V, N, kk, w, h);
+        basis_subtract<<<nb, VA_THREADS, 0, s>>>(V, N, kk, h, w);
+        ctx_->launches += 2;
       }
-      double hn = nrm(w);
-      H[(k + 1) * m + k] = hn;
-      if (hn > 0) {
-        double ih = 1.0 / hn;
-        cublasDcopy(blas_, N, w, 1, V + static_cast<size_t>(k + 1) * N, 1);
-        cublasDscal(blas_, N, &ih, V + static_cast<size_t>(k + 1) * N, 1);
-      }
+      sum_squares<<<1, VA_THREADS, 0, s>>>(w, N, dproj + hn_at);
+      ctx_->launches++;
+      cuda_check(cudaMemcpyAsync(hproj_, dproj, (hn_at + 1) * sizeof(double), cudaMemcpyDeviceToHost, s),
+                 "D2H projections");
+      cuda_check(cudaStreamSynchronize(s), "sync projections");
+      const double hn = std::sqrt(hproj_[hn_at]);
+      for (int i = 0; i <= k; i++) H[static_cast<size_t>(i) * m + k] = hproj_[i] + hproj_[m + 1 + i];
+      H[static_cast<size_t>(k + 1) * m + k] = hn;
+      if (hn > 0) copy_scaled(w, 1.0 / hn, V + static_cast<size_t>(k + 1) * N);
       for (int i = 0; i < k; i++) {
-        double t = cs[i] * H[i * m + k] + sn[i] * H[(i + 1) * m + k];
+        const double t = cs[i] * H[i * m + k] + sn[i] * H[(i + 1) * m + k];
         H[(i + 1) * m + k] = -sn[i] * H[i * m + k] + cs[i] * H[(i + 1) * m + k];
         H[i * m + k] = t;
       }
-      double a = H[k * m + k], c = H[(k + 1) * m + k];
-      double d = std::sqrt(a * a + c * c);
+      const double a = H[k * m + k], c = H[(k + 1) * m + k];
+      const double d = std::sqrt(a * a + c * c);
       cs[k] = d > 0 ? a / d : 1.0;
       sn[k] = d > 0 ? c / d : 0.0;
       H[k * m + k] = d;
@@ -1611,26 +1686,25 @@ void DenseLU::gmres_ir(double* b) {
         break;
       }
     }
-    // y = H^{-1} g, x += M^{-1} V y
+    // y = H^-1 g, x += M^-1 V y
     std::vector<double> y(k, 0.0);
     for (int i = k - 1; i >= 0; i--) {
       double sum = g[i];
       for (int j = i + 1; j < k; j++) sum -= H[i * m + j] * y[j];
       y[i] = sum / H[i * m + i];
     }
-    cudaMemsetAsync(r, 0, sizeof(double) * N, s);
-    for (int i = 0; i < k; i++) cublasDaxpy(blas_, N, &y[i], V + static_cast<size_t>(i) * N, 1, r, 1);
+    cuda_check(cudaMemsetAsync(r, 0, sizeof(double) * N, s), "memset r");
+    for (int i = 0; i < k; i++) add_scaled(V + static_cast<size_t>(i) * N, y[i], r);
     solve_f32(r);
-    const double one = 1.0;
-    cublasDaxpy(blas_, N, &one, r, 1, x, 1);
+    add_scaled(r, 1.0, x);
   }
   {
     ProfScope ps(ctx_, Context::PROF_GMRES, 8.0 * double(N) * N);
     gemv(x, r, -1.0, 1.0, b);
   }
-  stats.final_rel_residual = nrm(r) / bnorm;
+  stats.final_rel_residual = norm(r) / bnorm;
   stats.refine_iters = total_it;
-  cublasDcopy(blas_, N, x, 1, b, 1);
+  cuda_check(cudaMemcpyAsync(b, x, sizeof(double) * N, cudaMemcpyDeviceToDevice, s), "copy x");
 }
 
 void DenseLU::solve(double* b, int trans) {
@@ -1646,9 +1720,11 @@ void DenseLU::solve(double* b, int trans) {
   }
   cuda_check(cudaStreamSynchronize(ctx_->stream()), "sync after solve");
   int perr = 0;
-  cuda_check(cudaMemcpy(&perr, panel_err_, sizeof(int), cudaMemcpyDeviceToHost), "D2H sweep flag");
+  cuda_check(cudaMemcpyAsync(&perr, panel_err_, sizeof(int), cudaMemcpyDeviceToHost, ctx_->stream()),
+             "D2H sweep flag");
+  cuda_check(cudaStreamSynchronize(ctx_->stream()), "sync sweep flag");
   if (perr) {
-    cuda_check(cudaMemset(panel_err_, 0, sizeof(int)), "reset sweep flag");
+    cuda_check(cudaMemsetAsync(panel_err_, 0, sizeof(int), ctx_->stream()), "reset sweep flag");
     throw KdError(KD_ERR_TIMEOUT, "triangular solve: a grid barrier wait ran out");
   }
   stats.t_solve_ms = now_ms() - t0;

@@ -75,6 +75,8 @@ class DenseLU {
   void gemv(const double* x, double* y, double alpha, double beta, const double* b);
   double* work_ = nullptr;     // solver workspace
   size_t work_cap_ = 0;
+  double* hproj_ = nullptr;    // pinned host copy of one GMRES step's projections and norm
+  size_t hproj_cap_ = 0;
   float* work32_ = nullptr;
   size_t work32_cap_ = 0;
 
