@@ -341,6 +341,8 @@ def run_gpu(args, ws, rank, local):
         prof[name] = KD.profile_read(ctx)
         KD.profile_enable(ctx, False)
 
+    batch = run_batch(args, local) if args.batch > 0 else None
+
     if rank != 0:
         return 0
     peaks, peak_kind = load_peaks()
@@ -385,6 +387,7 @@ def run_gpu(args, ws, rank, local):
         "roofline_lu_gemm": roof_gemm,
         "fp64_peak_tflops_measured": fp64_tflops,
         "clocks": clk.summary(),
+        "batch": batch,
     }
     if not args.no_cpu:
         cb = cpu_step_sample(args.workload, blocks=args.cpu_blocks)
@@ -393,6 +396,42 @@ def run_gpu(args, ws, rank, local):
                                 "phases_ms": {k: cb[k] for k in ("residual_ms", "assembly_ms", "lu_solve_ms")}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def run_batch(args, local):
+    """Batched uneven solves: `--batch` independent isolated stars (central
+    density uniform in [8e-4, 2e-3], nr in {9, ..., 17}) solved from scratch
+    (context, space, system, Newton to the precision), one at a time and
+    then concurrently, one context per instance from `--batch-threads` host
+    threads.  Returns solves/s of both and the concurrent speed-up."""
+    import gc
+
+    import torch
+
+    from kadath_frontera_gb300 import kadath as KD
+    from kadath_frontera_gb300 import workloads
+
+    cfgs = workloads.star_batch_configs(args.batch, seed=0)
+    # warm-up: one instance of every resolution (module load, kernel attributes)
+    seen = {}
+    for c in cfgs:
+        seen.setdefault(c["res"], c)
+    workloads.solve_batch(list(seen.values()), 1, args.precision, KD.KD_LU_TF32_IR, local, keep=False)
+    gc.collect()
+    out = {"instances": args.batch, "threads": args.batch_threads,
+           "res": sorted({c["res"] for c in cfgs}), "unit": "solves/s",
+           "lu": "mixed (tf32 trailing update, f64 GMRES-IR)",
+           "includes": "per instance: context, space and system set-up, Newton solve to |F| <= precision"}
+    for name, threads in (("serial", 1), ("concurrent", args.batch_threads)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        upd = workloads.solve_batch(cfgs, threads, args.precision, KD.KD_LU_TF32_IR, local, keep=False)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        gc.collect()
+        out[name] = {"s": dt, "solves_per_s": len(cfgs) / dt, "newton_updates": int(sum(upd))}
+    out["concurrent_speedup"] = out["serial"]["s"] / out["concurrent"]["s"]
+    return out
 
 
 def measure_fp64_peak(device):
@@ -462,6 +501,8 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--cpu-blocks", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--batch", type=int, default=16, help="instances of the batched-solve measurement (0: skip)")
+    ap.add_argument("--batch-threads", type=int, default=8)
     args = ap.parse_args()
     if args.impl == "reference":
         # rank 0 alone runs the CPU reference; other ranks exit without work

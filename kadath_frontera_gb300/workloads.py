@@ -40,12 +40,12 @@ def toy_rho_values(r):
     return v
 
 
-def star_matter_values(r, nucleus: bool):
+def star_matter_values(r, nucleus: bool, rho_c=STAR_RHOC):
     rho = np.zeros_like(r)
     if nucleus:
         x = np.pi * r / STAR_R
         safe = np.where(x > 0, x, 1.0)
-        rho = STAR_RHOC * np.where(x > 0, np.sin(x) / safe, 1.0)
+        rho = rho_c * np.where(x > 0, np.sin(x) / safe, 1.0)
     E = rho * (1 + STAR_K * rho)
     S = 3 * STAR_K * rho * rho
     return E, E + 2 * S
@@ -108,7 +108,7 @@ def toy(res=(13, 7, 4), bounds=(1.0, 2.0), ctx=None) -> Workload:
     return Workload("toy", space, syst, [("psi", psi)], [rho])
 
 
-def star(res=(13, 9, 4), bounds=STAR_BOUNDS, ctx=None) -> Workload:
+def star(res=(13, 9, 4), bounds=STAR_BOUNDS, ctx=None, rho_c=STAR_RHOC) -> Workload:
     space = Space_spheric(CHEB_TYPE, (0, 0, 0), res, bounds, ctx=ctx)
     nd = space.get_nbr_domains()
     P = Scalar(space, 1.0).std_base()
@@ -124,7 +124,7 @@ def star(res=(13, 9, 4), bounds=STAR_BOUNDS, ctx=None) -> Workload:
     E = Scalar(space)
     E2S = Scalar(space)
     for d in range(nd):
-        e, e2s = star_matter_values(space.get_radius(d), space.domain_info(d)["type"] == 1)
+        e, e2s = star_matter_values(space.get_radius(d), space.domain_info(d)["type"] == 1, rho_c)
         E.set_domain(d, e)
         E2S.set_domain(d, e2s)
     E.std_base()
@@ -151,6 +151,61 @@ def star(res=(13, 9, 4), bounds=STAR_BOUNDS, ctx=None) -> Workload:
 
 
 WORKLOADS = {"toy": toy, "star": star}
+
+
+def solve(wl: Workload, precision=1e-10, lu_mode=None, max_steps=20) -> int:
+    """Newton steps from the current fields until |F| < precision; returns the
+    number of updates made."""
+    err = math.inf
+    for it in range(max_steps):
+        done, err = wl.syst.do_newton(precision, lu_mode=lu_mode)
+        if done:
+            return it
+    raise RuntimeError(f"{wl.name}: no convergence in {max_steps} steps (|F| = {err:.3e})")
+
+
+def batch_ntheta(nr):
+    """ntheta of a batch instance: nr // 2 + 1, raised to the next odd number.
+    With an even number of theta points the nucleus's Galerkin/tau system is
+    singular (the oracle's Jacobian of the toy problem has condition number
+    ~1e22 at (9, 6, 4) against ~1e9 at (9, 5, 4); shells alone are regular),
+    and Kadath's own codes use odd theta resolutions."""
+    nt = nr // 2 + 1
+    return nt if nt % 2 == 1 else nt + 1
+
+
+def star_batch_configs(n, seed=0):
+    """Independent isolated stars with central densities uniform in
+    [8e-4, 2e-3] and nr in {9, 11, 13, 15, 17} per instance
+    (ntheta = batch_ntheta(nr), nphi = 4), from a fixed seed."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        nr = int(rng.choice([9, 11, 13, 15, 17]))
+        out.append({"res": (nr, batch_ntheta(nr), 4), "rho_c": float(rng.uniform(8e-4, 2e-3))})
+    return out
+
+
+def solve_batch(configs, threads, precision=1e-10, lu_mode=None, device=0, keep=True):
+    """Builds and solves every configuration, each instance on its own
+    context (its own CUDA streams and workspaces) from a pool of `threads`
+    host threads, so that instances overlap on the GPU.  Returns the
+    converged workloads in configuration order, or with keep=False only
+    their numbers of Newton updates (each instance's device memory is then
+    released as soon as it has converged)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from ._lib import Context
+
+    def one(cfg):
+        wl = star(res=cfg["res"], rho_c=cfg["rho_c"], ctx=Context(device))
+        updates = solve(wl, precision, lu_mode)
+        return wl if keep else updates
+
+    if threads <= 1:
+        return [one(c) for c in configs]
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        return list(ex.map(one, configs))
 
 
 def main(argv=None) -> int:
