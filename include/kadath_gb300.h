@@ -188,6 +188,23 @@ int kd_system_add_def(kd_system* s, int dom, const char* text);            /* ad
 int kd_system_add_eq_inside(kd_system* s, int dom, const char* eq);        /* add_eq_inside */
 int kd_system_add_eq_bc(kd_system* s, int dom, int bound, const char* eq); /* add_eq_bc */
 int kd_system_add_eq_matching(kd_system* s, int dom, int bound, const char* eq); /* add_eq_matching */
+/* Integral-type equations (Eq_int, include/system_of_eqs.hpp:1352): one
+ * condition each, placed before all other equations (sec_member,
+ * src/System_of_eqs/solver.cpp:49).
+ * - int_volume: "integvolume(f) = c" over domains dom_min..dom_max
+ *   (Space_spheric::add_eq_int_volume, src/Space/Spheric/spheric_add_eq.cpp:81);
+ * - int_inf: "integ(f) = c" with integ() at the outer boundary of the
+ *   compactified domain (Domain_compact::integ, domain_compact.cpp:89);
+ * - val: the expression vanishes at collocation point pos = (i, j, k) of
+ *   dom (System_of_eqs::add_eq_val, src/System_of_eqs/add_eq.cpp:343);
+ * - point: the expression vanishes at a Cartesian point, summed in dom
+ *   (System_of_eqs::add_eq_point, add_eq.cpp:355).
+ * Double unknowns (kd_system_add_var_double) get their own Jacobian columns,
+ * first in the unknown order (do_col_J, solver.cpp:120). */
+int kd_system_add_eq_int_volume(kd_system* s, int dom_min, int dom_max, const char* eq);
+int kd_system_add_eq_int_inf(kd_system* s, const char* eq);
+int kd_system_add_eq_val(kd_system* s, int dom, const char* eq, const int pos[3]);
+int kd_system_add_eq_point(kd_system* s, int dom, const char* eq, const double point[3]);
 /* System_of_eqs::add_ope(name, &EOS<Cold_PWPoly, var>::action, ...)
  * (include/system_of_eqs.hpp:277, include/EOS/EOS.hh:235): registers
  * name(h) = var of a cold piecewise polytrope at the enthalpy h, with its

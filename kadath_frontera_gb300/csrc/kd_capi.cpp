@@ -452,6 +452,34 @@ int kd_system_add_eq_matching(kd_system* s, int dom, int bound, const char* eq) 
   });
 }
 
+int kd_system_add_eq_int_volume(kd_system* s, int dom_min, int dom_max, const char* eq) {
+  SYS_GUARD(s) {
+    if (!eq) throw kd::KdError(KD_ERR_ARG, "null equation");
+    s->sys->add_eq_int_volume(dom_min, dom_max, eq);
+  });
+}
+
+int kd_system_add_eq_int_inf(kd_system* s, const char* eq) {
+  SYS_GUARD(s) {
+    if (!eq) throw kd::KdError(KD_ERR_ARG, "null equation");
+    s->sys->add_eq_int_inf(eq);
+  });
+}
+
+int kd_system_add_eq_val(kd_system* s, int dom, const char* eq, const int pos[3]) {
+  SYS_GUARD(s) {
+    if (!eq || !pos) throw kd::KdError(KD_ERR_ARG, "null argument");
+    s->sys->add_eq_val(dom, eq, pos);
+  });
+}
+
+int kd_system_add_eq_point(kd_system* s, int dom, const char* eq, const double point[3]) {
+  SYS_GUARD(s) {
+    if (!eq || !point) throw kd::KdError(KD_ERR_ARG, "null argument");
+    s->sys->add_eq_point(dom, eq, point);
+  });
+}
+
 int kd_system_sizes(kd_system* s, int* n_unknowns, int* n_conditions) {
   SYS_GUARD(s) {
     if (s->sys->nbr_conditions() < 0) s->sys->residual(nullptr);

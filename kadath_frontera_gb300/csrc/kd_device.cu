@@ -366,6 +366,19 @@ cudaError_t launch_reduce1(const double* x, long long n, int op, double* out_sca
   return cudaGetLastError();
 }
 
+__global__ void lincomb2_kernel(int n, double ca, const double* __restrict__ a, double as, double cb,
+                                const double* __restrict__ b, double bs, double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = ca * (a ? a[i] : as) + cb * (b ? b[i] : bs);
+}
+
+cudaError_t launch_lincomb2(int n, double ca, const double* a, double as, double cb, const double* b, double bs,
+                            double* out, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  lincomb2_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, ca, a, as, cb, b, bs, out);
+  return cudaGetLastError();
+}
+
 __device__ __forceinline__ double eos_clamp_rho(const KdEos& e, double rho) {
   return rho < e.rhomin ? e.rhomin : (rho > e.rhomax ? e.rhomax : rho);  // check_range
 }

@@ -105,5 +105,9 @@ cudaError_t launch_eos(const KdEos& eos, int var, long long npts, const double* 
 
 // Deterministic single-CTA reduction: op 0 = sum of squares, 1 = max.
 cudaError_t launch_reduce1(const double* x, long long n, int op, double* out_scalar, cudaStream_t s);
+// out[i] = ca * (a ? a[i] : as) + cb * (b ? b[i] : bs), i < n: the tangent of
+// a linear combination of doubles whose tangents differ from seed to seed.
+cudaError_t launch_lincomb2(int n, double ca, const double* a, double as, double cb, const double* b, double bs,
+                            double* out, cudaStream_t s);
 
 }  // namespace kd

@@ -186,6 +186,44 @@ void Domain::val_boundary_row(int bound, int j, int k, double w, SparseRow& row)
   }
 }
 
+void Domain::integ_volume_row(const Base& b, SparseRow& row) const {
+  row.e.clear();
+  if (b.t.at(0) != SIN_ODD) throw KdError(KD_ERR_UNSUPPORTED, "integ_volume: theta basis of m = 0 is not SIN_ODD");
+  const int want = (type == DOM_NUCLEUS) ? CHEB_EVEN : CHEB;
+  for (int j = 0; j < nc[1]; j++) {
+    if (b.rb(j, 0) != want) throw KdError(KD_ERR_UNSUPPORTED, "integ_volume: unexpected radial basis");
+    const double wt = 2.0 / (2.0 * j + 1) * 2 * M_PI;
+    for (int i = 0; i < nc[0]; i++) {
+      double w1;
+      if (want == CHEB_EVEN) {
+        w1 = -1.0 / (4.0 * i * i - 1);  // integral_1d_cheb_even
+      } else {
+        if (i % 2 == 1) continue;
+        w1 = -2.0 / (i * i - 1.0);  // integral_1d_cheb
+      }
+      row.add(cidx(i, j, 0), wt * w1);
+    }
+  }
+}
+
+void Domain::integ_surface_row(const Base& b, int bound, SparseRow& row) const {
+  row.e.clear();
+  if (type != DOM_COMPACT) throw KdError(KD_ERR_UNSUPPORTED, "integ() is only defined in the compactified domain");
+  switch (b.t.at(0)) {
+    case COS_ODD:
+    case SIN_EVEN:
+      break;
+    case COS_EVEN:
+      val_boundary_row(bound, 0, 0, M_PI * 2 * M_PI, row);
+      break;
+    case SIN_ODD:
+      for (int j = 0; j < nc[1]; j++) val_boundary_row(bound, j, 0, 2.0 / (2 * double(j) + 1) * 2 * M_PI, row);
+      break;
+    default:
+      throw KdError(KD_ERR_UNSUPPORTED, "integ: theta basis not handled");
+  }
+}
+
 bool Domain::has_boundary(int bound) const {
   if (type == DOM_NUCLEUS) return bound == OUTER_BC;
   if (type == DOM_COMPACT) return true;
@@ -625,7 +663,15 @@ int Space::locate(const double point[3], double num[3]) const {
       break;
     }
   if (dd < 0) return -1;
-  const Domain& d = domains[dd];
+  absol_to_num(dd, point, num);
+  return dd;
+}
+
+void Space::absol_to_num(int dd, const double point[3], double num[3]) const {
+  const Domain& d0 = domains.at(0);
+  const double x = point[0] - d0.center[0], y = point[1] - d0.center[1], z = point[2] - d0.center[2];
+  const double r = std::sqrt(x * x + y * y + z * z);
+  const Domain& d = domains.at(dd);
   if (d.type == DOM_NUCLEUS) num[0] = r / d.alpha;
   else if (d.type == DOM_SHELL) num[0] = (r - d.beta) / d.alpha;
   else num[0] = 1.0 + 1.0 / r / d.alpha;
@@ -641,7 +687,6 @@ int Space::locate(const double point[3], double num[3]) const {
   if (th < 0) th += M_PI;
   num[1] = th;
   num[2] = ph;
-  return dd;
 }
 
 }  // namespace kd

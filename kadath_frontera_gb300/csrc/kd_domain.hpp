@@ -81,6 +81,16 @@ class Domain {
   // src/Ope_1d/summation_1d.cpp:272).
   void point_weights(const Base& b, const double num[3], std::vector<double>& w) const;
 
+  // Domain_*::integ_volume (domain_{nucleus,shell,compact}_ope.cpp) as
+  // weights on the coefficients of the integrand, i.e. of the field already
+  // multiplied by r^2 sin(theta) alpha (nucleus, shell) or by
+  // -r^4 sin(theta) alpha (compact): the k = 0 modes only, 2/(2j+1) per
+  // SIN_ODD theta mode, integral_1d (src/Ope_1d/integral_1d.cpp) along r.
+  void integ_volume_row(const Base& integrand, SparseRow& row) const;
+  // Domain_compact::integ (domain_compact.cpp:89) at `bound`, as weights on
+  // the coefficients of r^2 sin(theta) times the field.
+  void integ_surface_row(const Base& integrand, int bound, SparseRow& row) const;
+
   bool has_boundary(int bound) const;
   void find_other_dom(int dom, int bound, int& other_dom, int& other_bound) const;
 };
@@ -96,6 +106,9 @@ class Space {
   // Domain holding a Cartesian point and its numerical coordinates
   // (xi, theta, phi); -1 when no domain does.
   int locate(const double point[3], double num[3]) const;
+  // Numerical coordinates of a Cartesian point in domain dd
+  // (Domain_*::absol_to_num), whether or not the point lies in it.
+  void absol_to_num(int dd, const double point[3], double num[3]) const;
 };
 
 }  // namespace kd

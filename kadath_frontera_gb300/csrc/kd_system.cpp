@@ -238,6 +238,12 @@ void TangentCache::store(Context* ctx, const Ope* node, int var, int dom, const 
   Entry e;
   e.is_double = t.is_double;
   e.dd = t.dd;
+  if (t.ddv) {
+    double* p = arena.alloc_doubles(t.ddb);
+    cuda_check(cudaMemcpyAsync(p, t.ddv, sizeof(double) * t.ddb, cudaMemcpyDeviceToDevice, ctx->stream()), "arena copy");
+    e.ddv = p;
+    e.ddb = t.ddb;
+  }
   for (const DVal& d : t.dt) e.dt.push_back(copy_to_arena(ctx, d, arena));
   ders[std::make_tuple(node, var, dom)] = std::move(e);
 }
@@ -258,6 +264,9 @@ Term Ope::eval(EvalState& st) const {
         if (tt->second.is_double) {
           r.has_dd = true;
           r.dd = tt->second.dd;
+          r.ddv = tt->second.ddv;
+          r.ddb = tt->second.ddb;
+          r.ddctx = st.sys->ctx;
         } else {
           r.has_dt = true;
           r.dt = tt->second.dt;
@@ -313,6 +322,19 @@ bool split_eq(const std::string& s, std::string& l, std::string& r) {
     }
   return false;
 }
+
+// Ope_minus of the constant side of an integral equation.
+class OpeMinusPart : public Ope {
+ public:
+  OpeMinusPart(int dom, OpePtr a_) : Ope(dom), a(std::move(a_)) {
+    vc = a->vc;
+    dc = a->dc;
+    dz = a->dz;
+  }
+  std::vector<const Ope*> kids() const override { return {a.get()}; }
+  Term action(EvalState& st, const Term* cv) const override { return t_neg(a->eval(st), cv); }
+  OpePtr a;
+};
 
 class OpeSubEq : public Ope {
  public:
@@ -449,6 +471,85 @@ void System::add_eq_matching(int dom, int bound, const std::string& text) {
   nbr_conditions_ = -1;
 }
 
+void System::add_int_equation(IntEquation ie) {
+  for (auto& p : ie.parts) mark_tangent_frontier(p.get());
+  tcache_.clear();
+  ieqs_.push_back(std::move(ie));
+  nbr_conditions_ = -1;
+}
+
+void System::add_eq_int_volume(int dmin, int dmax, const std::string& text) {
+  std::string l, r;
+  if (!split_eq(text, l, r)) throw KdError(KD_ERR_ARG, "= needed for equations");
+  if (dmin < 0 || dmax >= sp->ndom() || dmin > dmax) throw KdError(KD_ERR_ARG, "bad domain range for the integral");
+  IntEquation ie;
+  ie.text = text;
+  for (int d = dmin; d <= dmax; d++) ie.parts.push_back(parse_ope(*this, d, l, -1));
+  // the constant side, as Ope_minus(give_ope(...)) in the first domain
+  ie.parts.push_back(std::make_shared<OpeMinusPart>(dmin, parse_ope(*this, dmin, r, -1)));
+  add_int_equation(std::move(ie));
+}
+
+void System::add_eq_int_inf(const std::string& text) {
+  std::string l, r;
+  if (!split_eq(text, l, r)) throw KdError(KD_ERR_ARG, "= needed for equations");
+  const int last = sp->ndom() - 1;
+  if (sp->dom(last).type != DOM_COMPACT) throw KdError(KD_ERR_ARG, "integral at infinity needs a compactified domain");
+  IntEquation ie;
+  ie.text = text;
+  ie.parts.push_back(parse_ope(*this, last, l, OUTER_BC));
+  ie.parts.push_back(std::make_shared<OpeMinusPart>(last, parse_ope(*this, last, r, OUTER_BC)));
+  add_int_equation(std::move(ie));
+}
+
+void System::add_eq_val(int dom, const std::string& text, const int pos[3]) {
+  if (dom < 0 || dom >= sp->ndom()) throw KdError(KD_ERR_ARG, "bad domain");
+  const Domain& d = sp->dom(dom);
+  for (int i = 0; i < 3; i++)
+    if (pos[i] < 0 || pos[i] >= d.np[i]) throw KdError(KD_ERR_ARG, "add_eq_val: collocation index out of range");
+  IntEquation ie;
+  ie.text = text;
+  ie.parts.push_back(make_value_at(dom, parse_ope(*this, dom, text, -1), pos));
+  add_int_equation(std::move(ie));
+}
+
+void System::add_eq_point(int dom, const std::string& text, const double point[3]) {
+  if (dom < 0 || dom >= sp->ndom()) throw KdError(KD_ERR_ARG, "bad domain");
+  double num[3];
+  sp->absol_to_num(dom, point, num);
+  IntEquation ie;
+  ie.text = text;
+  ie.parts.push_back(make_value_at_point(dom, parse_ope(*this, dom, text, -1), num));
+  add_int_equation(std::move(ie));
+}
+
+void System::export_int_ders(EvalState& st, int dom, double* out, long long osf, int B) {
+  static const std::vector<int> rp = {0, 1}, one_idx = {0};
+  static const std::vector<double> one_w = {1.0};
+  for (auto& ie : ieqs_)
+    for (auto& p : ie.parts) {
+      if (dom >= 0 && p->dom != dom) continue;
+      Term t = p->eval(st);
+      if (!t.is_double) throw KdError(KD_ERR_STATE, "an integral equation's part is not a number: " + ie.text);
+      if (!t.has_dd) continue;
+      const double* v = t.ddv;
+      if (!v) {
+        if (t.dd == 0.0) continue;
+        double* tmp = ctx->scratch().alloc_doubles(B);
+        cuda_check(launch_lincomb2(B, 1.0, nullptr, t.dd, 0.0, nullptr, 0.0, tmp, ctx->stream()), "constant tangent");
+        ctx->launches++;
+        v = tmp;
+      } else if (t.ddb != B) {
+        throw KdError(KD_ERR_STATE, "integral tangent of another batch size");
+      }
+      // out[row + b * osf] += v[b]
+      cuda_check(launch_gather_csr(v, 1, B, 1, ctx->table(rp), ctx->table(one_idx), ctx->dtable(one_w), out + ie.row,
+                                   osf, 0, 1.0, 1, ctx->stream()),
+                 "integral row");
+      ctx->launches++;
+    }
+}
+
 CsrTable System::upload_rows(const std::vector<SparseRow>& rows) {
   std::vector<int> rp(rows.size() + 1, 0), idx;
   std::vector<double> w;
@@ -579,6 +680,18 @@ void System::residual(double* d_F, bool record) {
     ~Fork() { c->join(); }
   } fork(ctx, ndom() < 8 ? ndom() : 8);
   auto stream_of = [&](const Equation& eq) { return eq.dom - dom_min; };
+  // integral equations: sums of numbers, on the main stream
+  std::vector<double> ivals(ieqs_.size(), 0.0);
+  ctx->use(-1);
+  for (size_t i = 0; i < ieqs_.size(); i++) {
+    double v = 0.0;
+    for (auto& p : ieqs_[i].parts) {
+      Term t = p->eval(st);
+      if (!t.is_double) throw KdError(KD_ERR_STATE, "an integral equation's part is not a number: " + ieqs_[i].text);
+      v += t.vd;
+    }
+    ivals[i] = v;
+  }
   for (size_t i = 0; i < eqs_.size(); i++) {
     ctx->use(stream_of(eqs_[i]));
     lhs[i] = eqs_[i].lhs->eval(st);
@@ -587,6 +700,7 @@ void System::residual(double* d_F, bool record) {
   vcache_.valid = record;
   if (nbr_conditions_ < 0) {
     int row = 0;
+    for (auto& ie : ieqs_) ie.row = row++;
     for (size_t i = 0; i < eqs_.size(); i++) {
       eqs_[i].n_cond = count_rows(eqs_[i], lhs[i]);
       eqs_[i].row0 = row;
@@ -601,6 +715,12 @@ void System::residual(double* d_F, bool record) {
     }
   }
   if (!d_F) return;
+  if (!ivals.empty()) {
+    ctx->use(-1);
+    cuda_check(cudaMemcpyAsync(d_F, ivals.data(), sizeof(double) * ivals.size(), cudaMemcpyHostToDevice,
+                               ctx->main_stream()),
+               "integral rows");
+  }
   for (size_t i = 0; i < eqs_.size(); i++) {
     Equation& eq = eqs_[i];
     ctx->use(stream_of(eq));
@@ -639,8 +759,35 @@ void System::jacobian(double* d_J, long long ld, bool reuse) {
     os << "Number of unknowns (" << N << ") is different from the number of equations (" << nbr_conditions_ << ")";
     throw KdError(KD_ERR_STATE, os.str());
   }
-  if (!vdoubles_.empty()) throw KdError(KD_ERR_UNSUPPORTED, "double unknowns are not supported yet");
   cuda_check(cudaMemsetAsync(d_J, 0, sizeof(double) * ld * N, ctx->stream()), "memset J");
+  // Columns of the double unknowns (do_col_J with is_var_double): one pass
+  // each with that unknown's tangent 1, every field's 0, all equations.
+  if (!vdoubles_.empty()) {
+    const std::map<std::pair<int, int>, DVal> none;
+    for (size_t i = 0; i < vdoubles_.size(); i++) {
+      ctx->scratch().reset();
+      std::vector<double> e(vdoubles_.size(), 0.0);
+      e[i] = 1.0;
+      EvalState st;
+      st.sys = this;
+      st.with_der = true;
+      st.B = 1;
+      st.jx_seeds = &none;
+      st.jx_doubles = &e;
+      st.seed_var_double = static_cast<int>(i);
+      st.vcache = &vcache_;
+      double* Jcol = d_J + static_cast<long long>(i) * ld;
+      for (auto& eq : eqs_) {
+        Term t = eq.lhs->eval(st);
+        export_term(eq, t, true, eq.dom, eq.bound, Jcol + eq.row0, ld, 1, 1, 1.0, true);
+        if (eq.kind == Equation::MATCHING) {
+          Term r = eq.rhs->eval(st);
+          export_term(eq, r, true, eq.other_dom, eq.other_bound, Jcol + eq.row0, ld, 1, 1, -1.0, true);
+        }
+      }
+      export_int_ders(st, -1, Jcol, ld, 1);
+    }
+  }
   // Seed blocks write disjoint column blocks: a wave of them runs on side
   // streams; the scratch arena is reset only between waves.
   std::vector<std::pair<int, int>> blocks;
@@ -683,6 +830,7 @@ void System::jacobian(double* d_J, long long ld, bool reuse) {
           export_term(eq, t, true, eq.other_dom, eq.other_bound, Jblock + eq.row0, ld, 1, B, -1.0, true);
         }
       }
+      export_int_ders(st, dd, Jblock, ld, B);
     }
   }
 }
@@ -738,6 +886,7 @@ void System::dres_dcst(int cst, double* d_y) {
       export_term(eq, r, true, eq.other_dom, eq.other_bound, d_y + eq.row0, 0, 1, 1, -1.0, true);
     }
   }
+  export_int_ders(st, -1, d_y, 1, 1);
 }
 
 void System::val_point_gradient(int var, const double point[3], double* g) {
@@ -813,6 +962,7 @@ void System::jx(const double* d_x, double* d_y) {
       export_term(eq, r, true, eq.other_dom, eq.other_bound, d_y + eq.row0, 0, 1, 1, -1.0, true);
     }
   }
+  export_int_ders(st, -1, d_y, 1, 1);
 }
 
 void System::update_from_x(const double* d_x) {

@@ -85,6 +85,8 @@ struct TangentCache {
   struct Entry {
     bool is_double = false;
     double dd = 0.0;
+    const double* ddv = nullptr;  // per-seed tangent of a double (arena copy)
+    int ddb = 0;
     std::vector<DVal> dt;
   };
   std::map<std::tuple<const Ope*, int, int>, Entry> ders;
@@ -138,6 +140,16 @@ struct Equation {
   }
 };
 
+// Integral-type equation (Eq_int, include/system_of_eqs.hpp:1352): one
+// condition, the sum of the numbers its parts give (one part per domain of a
+// volume integral plus the constant side, or a single point value).  These
+// rows come before every other equation (sec_member, solver.cpp:49).
+struct IntEquation {
+  std::string text;
+  std::vector<OpePtr> parts;
+  int row = 0;
+};
+
 class System {
  public:
   System(Context* ctx, const Space* sp, int dom_min, int dom_max);
@@ -156,6 +168,19 @@ class System {
   void add_eq_inside(int dom, const std::string& eq);
   void add_eq_bc(int dom, int bound, const std::string& eq);
   void add_eq_matching(int dom, int bound, const std::string& eq);
+  // "integvolume(f) = c": the volume integral of f over domains dmin..dmax
+  // equals c (Space_spheric::add_eq_int_volume, spheric_add_eq.cpp:81).
+  void add_eq_int_volume(int dmin, int dmax, const std::string& eq);
+  // "integ(f) = c" with integ() at the outer boundary of the last
+  // (compactified) domain: the surface integral at infinity.
+  void add_eq_int_inf(const std::string& eq);
+  // The scalar expression vanishes at collocation point pos of domain dom
+  // (add_eq_val, add_eq.cpp:343).
+  void add_eq_val(int dom, const std::string& eq, const int pos[3]);
+  // The scalar expression vanishes at a Cartesian point, evaluated in domain
+  // dom by the spectral summation (add_eq_point, add_eq.cpp:355).
+  void add_eq_point(int dom, const std::string& eq, const double point[3]);
+  int n_int_equations() const { return static_cast<int>(ieqs_.size()); }
 
   int find_var(const std::string& n) const;
   int find_var_double(const std::string& n) const;
@@ -256,6 +281,7 @@ class System {
   std::vector<DefInfo> defs_;
   std::vector<UserOpe> user_opes_;
   std::vector<Equation> eqs_;
+  std::vector<IntEquation> ieqs_;
   int nbr_conditions_ = -1;
   int nbr_unknowns_ = -1;
   std::map<std::pair<int, int>, int> col0_, nunk_;
@@ -272,6 +298,10 @@ class System {
   void export_term(const Equation& eq, const Term& t, bool der, int side_dom, int side_bound, double* out,
                    long long osf, long long osr, int batch, double alpha, bool accumulate);
   CsrTable upload_rows(const std::vector<SparseRow>& rows);
+  void add_int_equation(IntEquation ie);
+  // Adds the tangents of the integral equations to out[row + b * osf],
+  // b < B: only the parts in domain dom, or every part when dom < 0.
+  void export_int_ders(EvalState& st, int dom, double* out, long long osf, int B);
   const double* seed_block(int var, int dom, int& B, Base& base);
   const CsrTable& xmap(int var, int dom);
 };

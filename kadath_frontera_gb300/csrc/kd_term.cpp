@@ -14,7 +14,15 @@ namespace kd {
 
 namespace {
 
-bool dd_zero(const Term& t) { return !t.has_dd || t.dd == 0.0; }
+bool dd_zero(const Term& t) { return !t.has_dd || (t.ddv == nullptr && t.dd == 0.0); }
+
+// A double whose tangent differs from seed to seed only combines with
+// other doubles here (the integral and point-value equations).
+void no_seed_tangent(const Term& d) {
+  if (d.ddv)
+    throw KdError(KD_ERR_UNSUPPORTED,
+                  "a double depending on the seeded fields (integral or point value) combined with a field");
+}
 
 void check_dom(const Term& a, const Term& b) {
   if (a.dom != b.dom) throw KdError(KD_ERR_ARG, "Term_eq operation across domains");
@@ -36,6 +44,27 @@ void check_valence(const Term& a, const Term& b) {
 
 }  // namespace
 
+void dbl_tangent_lincomb(Term& r, double ca, const Term& a, double cb, const Term* b) {
+  r.has_dd = true;
+  if (!a.ddv && !(b && b->ddv)) {
+    r.dd = ca * a.dd + (b ? cb * b->dd : 0.0);
+    r.ddv = nullptr;
+    return;
+  }
+  const Term& src = a.ddv ? a : *b;
+  if (a.ddv && b && b->ddv && a.ddb != b->ddb) throw KdError(KD_ERR_STATE, "double tangents of different batches");
+  Context* ctx = src.ddctx;
+  double* out = ctx->scratch().alloc_doubles(src.ddb);
+  cuda_check(launch_lincomb2(src.ddb, ca, a.ddv, a.dd, b ? cb : 0.0, b ? b->ddv : nullptr, b ? b->dd : 0.0, out,
+                             ctx->stream()),
+             "double tangent");
+  ctx->launches++;
+  r.dd = 0.0;
+  r.ddv = out;
+  r.ddb = src.ddb;
+  r.ddctx = ctx;
+}
+
 // Each operation takes an optional `cv`: the value of its result, already
 // known (a node value cached from the value pass of the same iterate).  The
 // value is then adopted instead of recomputed and only the tangent is
@@ -45,10 +74,7 @@ Term t_add(const Term& a, const Term& b, const Term* cv) {
   bool do_der = a.has_der() && b.has_der();
   if (a.is_double && b.is_double) {
     Term r = Term::dbl(a.dom, a.vd + b.vd);
-    if (do_der) {
-      r.has_dd = true;
-      r.dd = a.dd + b.dd;
-    }
+    if (do_der) dbl_tangent_lincomb(r, 1.0, a, 1.0, &b);
     return r;
   }
   if (a.is_double || b.is_double) {
@@ -59,6 +85,7 @@ Term t_add(const Term& a, const Term& b, const Term* cv) {
     else
       for (auto& v : t.vt) r.vt.push_back(v + d.vd);
     if (do_der) {
+      no_seed_tangent(d);
       r.has_dt = true;
       for (int i = 0; i < ncomp(t); i++) r.dt.push_back(d.dd == 0.0 ? t.dt[i] : t.dt[i] + d.dd);
     }
@@ -81,10 +108,7 @@ Term t_sub(const Term& a, const Term& b, const Term* cv) {
   bool do_der = a.has_der() && b.has_der();
   if (a.is_double && b.is_double) {
     Term r = Term::dbl(a.dom, a.vd - b.vd);
-    if (do_der) {
-      r.has_dd = true;
-      r.dd = a.dd - b.dd;
-    }
+    if (do_der) dbl_tangent_lincomb(r, 1.0, a, -1.0, &b);
     return r;
   }
   if (b.is_double) {
@@ -93,6 +117,7 @@ Term t_sub(const Term& a, const Term& b, const Term* cv) {
     else
       for (auto& v : a.vt) r.vt.push_back(v - b.vd);
     if (do_der) {
+      no_seed_tangent(b);
       r.has_dt = true;
       for (int i = 0; i < ncomp(a); i++) r.dt.push_back(b.dd == 0.0 ? a.dt[i] : a.dt[i] - b.dd);
     }
@@ -104,6 +129,7 @@ Term t_sub(const Term& a, const Term& b, const Term* cv) {
     else
       for (auto& v : b.vt) r.vt.push_back(a.vd - v);
     if (do_der) {
+      no_seed_tangent(a);
       r.has_dt = true;
       for (int i = 0; i < ncomp(b); i++) r.dt.push_back(a.dd == 0.0 ? -b.dt[i] : a.dd - b.dt[i]);
     }
@@ -125,10 +151,7 @@ Term t_neg(const Term& a, const Term* cv) {
   // Term_eq operator-(aa) = -1. * aa
   if (a.is_double) {
     Term r = Term::dbl(a.dom, -a.vd);
-    if (a.has_dd) {
-      r.has_dd = true;
-      r.dd = -a.dd;
-    }
+    if (a.has_dd) dbl_tangent_lincomb(r, -1.0, a, 0.0, nullptr);
     return r;
   }
   Term r = tensor_like(a);
@@ -147,10 +170,7 @@ Term t_mul(const Term& a, const Term& b, const Term* cv) {
   bool do_der = a.has_der() && b.has_der();
   if (a.is_double && b.is_double) {
     Term r = Term::dbl(a.dom, a.vd * b.vd);
-    if (do_der) {
-      r.has_dd = true;
-      r.dd = a.dd * b.vd + a.vd * b.dd;
-    }
+    if (do_der) dbl_tangent_lincomb(r, b.vd, a, a.vd, &b);
     return r;
   }
   if (a.is_double || b.is_double) {
@@ -161,6 +181,7 @@ Term t_mul(const Term& a, const Term& b, const Term* cv) {
     else
       for (auto& v : t.vt) r.vt.push_back(v * d.vd);
     if (do_der) {
+      no_seed_tangent(d);
       r.has_dt = true;
       for (int i = 0; i < ncomp(t); i++) {
         DVal part = t.dt[i] * d.vd;
@@ -199,8 +220,12 @@ Term t_div(const Term& a, const Term& b, const Term* cv) {
   if (a.is_double && b.is_double) {
     Term r = Term::dbl(a.dom, a.vd / b.vd);
     if (do_der) {
-      r.has_dd = true;
-      r.dd = (a.dd * b.vd - a.vd * b.dd) / (b.vd * b.vd);
+      if (a.ddv || b.ddv) {
+        dbl_tangent_lincomb(r, 1.0 / b.vd, a, -a.vd / (b.vd * b.vd), &b);
+      } else {
+        r.has_dd = true;
+        r.dd = (a.dd * b.vd - a.vd * b.dd) / (b.vd * b.vd);
+      }
     }
     return r;
   }
@@ -210,6 +235,7 @@ Term t_div(const Term& a, const Term& b, const Term* cv) {
     else
       for (auto& v : a.vt) r.vt.push_back(v / b.vd);
     if (do_der) {
+      no_seed_tangent(b);
       r.has_dt = true;
       for (int i = 0; i < ncomp(a); i++) {
         DVal num = a.dt[i] * b.vd;
@@ -226,6 +252,7 @@ Term t_div(const Term& a, const Term& b, const Term* cv) {
     else
       r.vt.push_back(a.vd / b.vt[0]);
     if (do_der) {
+      no_seed_tangent(a);
       r.has_dt = true;
       DVal num = (dd_zero(a) ? DVal::zeros(b.vt[0].ctx, b.vt[0].dom, 1) : b.vt[0] * a.dd) - b.dt[0] * a.vd;
       r.dt.push_back(num / (b.vt[0] * b.vt[0]));
@@ -341,6 +368,122 @@ class OpePow : public Ope {
   OpePtr a;
 };
 
+// Linear functionals turning a scalar field into a number, with their
+// tangents (one number per seed): Ope_int_volume (ope_int_volume.cpp),
+// Ope_int (ope_int.cpp, Domain_compact::integ), Ope_val (ope_val.cpp, the
+// value at one collocation point) and Ope_point (ope_point.cpp, the value at
+// a point through the spectral summation).
+class OpeFunctional : public Ope {
+ public:
+  enum Kind { INTEG_VOLUME, INTEG, VAL, POINT };
+  OpeFunctional(int dom, Kind k, OpePtr a_, int bound, const int pos[3], const double num[3])
+      : Ope(dom), kind(k), a(std::move(a_)), bound(bound) {
+    for (int i = 0; i < 3; i++) {
+      p[i] = pos ? pos[i] : 0;
+      x[i] = num ? num[i] : 0.0;
+    }
+    vc = a->vc;
+    dc = a->dc;
+    dz = a->dz;
+  }
+  std::vector<const Ope*> kids() const override { return {a.get()}; }
+  Term action(EvalState& st, const Term* cv) const override {
+    Term t = a->eval(st);
+    if (t.is_double || t.vt.size() != 1)
+      throw KdError(KD_ERR_UNSUPPORTED, "integrals and point values are only defined for a scalar field");
+    Term r = Term::dbl(dom, 0.0);
+    if (cv) {
+      r.vd = cv->vd;
+    } else if (!t.vt[0].zero) {
+      Context* ctx = t.vt[0].ctx;
+      double* out = apply(t.vt[0]);
+      cuda_check(cudaMemcpyAsync(&r.vd, out, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream()), "D2H integral");
+      cuda_check(cudaStreamSynchronize(ctx->stream()), "sync integral");
+    }
+    if (t.has_dt) {
+      r.has_dd = true;
+      const DVal& d = t.dt[0];
+      if (!d.zero) {
+        r.ddv = apply(d);
+        r.ddb = d.batch;
+        r.ddctx = d.ctx;
+      }
+    }
+    return r;
+  }
+  // The functional of every batch member of v, into `batch` doubles of the
+  // pass's arena.
+  double* apply(const DVal& v) const {
+    Context* ctx = v.ctx;
+    const Domain& d = *v.dom;
+    SparseRow row;
+    const double* src = nullptr;
+    long long stride = 0;
+    DVal w;
+    switch (kind) {
+      case INTEG_VOLUME: {
+        // nucleus, shell: mult_r(mult_r(mult_sin_theta(so))) * alpha;
+        // compact: -mult_r^4(mult_sin_theta(so)) * alpha
+        w = mult_r(mult_r(mult_sin_theta(v)));
+        if (d.type == DOM_COMPACT) w = mult_r(mult_r(w)) * (-d.alpha);
+        else w = w * d.alpha;
+        w.coef();
+        d.integ_volume_row(w.base, row);
+        src = w.cf;
+        stride = d.ncoefs();
+        break;
+      }
+      case INTEG: {
+        w = mult_r(mult_r(mult_sin_theta(v)));
+        w.coef();
+        d.integ_surface_row(w.base, bound, row);
+        src = w.cf;
+        stride = d.ncoefs();
+        break;
+      }
+      case VAL: {
+        w = v;
+        w.coef_i();
+        row.add(d.pidx(p[0], p[1], p[2]), 1.0);
+        src = w.c;
+        stride = d.npts();
+        break;
+      }
+      default: {
+        w = v;
+        w.coef();
+        std::vector<double> pw;
+        d.point_weights(w.base, x, pw);
+        for (size_t c = 0; c < pw.size(); c++)
+          if (pw[c] != 0.0) row.add(static_cast<int>(c), pw[c]);
+        src = w.cf;
+        stride = d.ncoefs();
+      }
+    }
+    std::vector<int> rp = {0, static_cast<int>(row.e.size())}, idx;
+    std::vector<double> wt;
+    for (auto& e : row.e) {
+      idx.push_back(e.first);
+      wt.push_back(e.second);
+    }
+    double* out = ctx->scratch().alloc_doubles(v.batch);
+    if (row.e.empty()) {
+      cuda_check(cudaMemsetAsync(out, 0, sizeof(double) * v.batch, ctx->stream()), "memset functional");
+      return out;
+    }
+    cuda_check(launch_gather_csr(src, stride, v.batch, 1, ctx->table(rp), ctx->table(idx), ctx->dtable(wt), out, 1, 0,
+                                 1.0, 0, ctx->stream()),
+               "functional gather");
+    ctx->launches++;
+    return out;
+  }
+  Kind kind;
+  OpePtr a;
+  int bound;
+  int p[3];
+  double x[3];
+};
+
 // Unary operators acting component by component on value and tangent.
 class OpeUnary : public Ope {
  public:
@@ -387,7 +530,10 @@ class OpeFunc : public Ope {
     if (t.is_double) {
       double v = kind == EXP ? std::exp(t.vd) : kind == SQRT ? std::sqrt(t.vd) : std::log(t.vd);
       Term r = Term::dbl(t.dom, v);
-      if (t.has_dd) {
+      if (t.has_dd && t.ddv) {
+        const double f1 = kind == EXP ? std::exp(t.vd) : kind == SQRT ? 0.5 / std::sqrt(t.vd) : 1.0 / t.vd;
+        dbl_tangent_lincomb(r, f1, t, 0.0, nullptr);
+      } else if (t.has_dd) {
         r.has_dd = true;
         r.dd = kind == EXP ? t.dd * std::exp(t.vd) : kind == SQRT ? t.dd / 2. / std::sqrt(t.vd) : t.dd / t.vd;
       }
@@ -717,6 +863,12 @@ OpePtr parse_ope(const System& sys, int dd, const std::string& expr, int bound) 
       return std::make_shared<OpeUnary>(dd, u.k, bound, parse_ope(sys, dd, p1, bound));
     }
   if (is_ope_uni(name, p1, "grad")) return std::make_shared<OpeGrad>(dd, parse_ope(sys, dd, p1, bound));
+  if (is_ope_uni(name, p1, "integ"))
+    return std::make_shared<OpeFunctional>(dd, OpeFunctional::INTEG, parse_ope(sys, dd, p1, bound), bound, nullptr,
+                                           nullptr);
+  if (is_ope_uni(name, p1, "integvolume"))
+    return std::make_shared<OpeFunctional>(dd, OpeFunctional::INTEG_VOLUME, parse_ope(sys, dd, p1, bound), bound,
+                                           nullptr, nullptr);
   if (is_ope_uni(name, p1, "sqrt"))
     return std::make_shared<OpeFunc>(dd, OpeFunc::SQRT, parse_ope(sys, dd, p1, bound));
   if (is_ope_uni(name, p1, "exp")) return std::make_shared<OpeFunc>(dd, OpeFunc::EXP, parse_ope(sys, dd, p1, bound));
@@ -756,6 +908,14 @@ OpePtr parse_ope(const System& sys, int dd, const std::string& expr, int bound) 
     if (is_ope_uni(name, p1, u.name.c_str()))
       return std::make_shared<OpeEos>(dd, u.eos, u.var, parse_ope(sys, dd, p1, bound));
   throw KdError(KD_ERR_ARG, "Unknown operator " + bare);
+}
+
+OpePtr make_value_at(int dom, OpePtr target, const int pos[3]) {
+  return std::make_shared<OpeFunctional>(dom, OpeFunctional::VAL, std::move(target), -1, pos, nullptr);
+}
+
+OpePtr make_value_at_point(int dom, OpePtr target, const double num[3]) {
+  return std::make_shared<OpeFunctional>(dom, OpeFunctional::POINT, std::move(target), -1, nullptr, num);
 }
 
 }  // namespace kd

@@ -21,6 +21,12 @@ struct Term {
   double vd = 0.0;
   bool has_dd = false;
   double dd = 0.0;  // tangent of a double (same for every seed)
+  // Tangent of a double that differs from seed to seed (an integral or a
+  // point value of a seeded field): ddb doubles on the device, from the
+  // pass's arena; null when every seed has the tangent dd.
+  const double* ddv = nullptr;
+  int ddb = 0;
+  Context* ddctx = nullptr;
   // tensor data: valence 0 (one component) or 1 (three Cartesian components)
   int valence = 0;
   std::vector<DVal> vt;
@@ -56,6 +62,9 @@ Term t_mul(const Term& a, const Term& b, const Term* cv);
 Term t_div(const Term& a, const Term& b, const Term* cv);
 Term t_neg(const Term& a, const Term* cv);
 Term term_pow(const Term& a, int n, const Term* cv = nullptr);
+// r's tangent = ca a' + cb b' for doubles a and b (b may be null); per seed
+// when either operand's tangent is.
+void dbl_tangent_lincomb(Term& r, double ca, const Term& a, double cb, const Term* b);
 
 class System;
 struct EvalState;
@@ -94,6 +103,13 @@ using OpePtr = std::shared_ptr<Ope>;
 // src/System_of_eqs/give_ope.cpp:1127).  `bound` is the boundary used by
 // dn(); -1 inside the domain.
 OpePtr parse_ope(const System& sys, int dom, const std::string& expr, int bound);
+
+// Ope_val (src/Ope_eq/ope_val.cpp): the value of a scalar expression at the
+// collocation point pos (r, theta, phi indices) of domain dom.
+OpePtr make_value_at(int dom, OpePtr target, const int pos[3]);
+// Ope_point (src/Ope_eq/ope_point.cpp): the value at numerical coordinates
+// num = (xi, theta, phi) of domain dom, by the spectral summation.
+OpePtr make_value_at_point(int dom, OpePtr target, const double num[3]);
 
 // Trims spaces the way Kadath's trim_spaces does (single spaces, one trailing).
 std::string trim_expr(const std::string& s);

@@ -79,6 +79,10 @@ def _declare_system(lib):
         "kd_system_add_eq_inside": (I, [P, I, C.c_char_p]),
         "kd_system_add_eq_bc": (I, [P, I, I, C.c_char_p]),
         "kd_system_add_eq_matching": (I, [P, I, I, C.c_char_p]),
+        "kd_system_add_eq_int_volume": (I, [P, I, I, C.c_char_p]),
+        "kd_system_add_eq_int_inf": (I, [P, C.c_char_p]),
+        "kd_system_add_eq_val": (I, [P, I, C.c_char_p, IP]),
+        "kd_system_add_eq_point": (I, [P, I, C.c_char_p, DP]),
         "kd_system_sizes": (I, [P, IP, IP]),
         "kd_system_n_equations": (I, [P, IP]),
         "kd_system_residual": (I, [P, DP]),
@@ -180,6 +184,16 @@ class Space_spheric:
     def add_matching(self, syst, eq):
         for dd in range(syst.dom_min, syst.dom_max):
             syst.add_eq_matching(dd, OUTER_BC, eq)
+
+    def add_eq_int_volume(self, syst, eq):
+        """Space_spheric::add_eq_int_volume: "integvolume(f) = c" over every
+        domain of the space."""
+        syst.add_eq_int_volume(0, self.get_nbr_domains() - 1, eq)
+
+    def add_eq_ori(self, syst, eq):
+        """Space_spheric::add_eq_ori: eq vanishes at the origin (the first
+        collocation point of the nucleus)."""
+        syst.add_eq_val(0, eq, (0, 0, 0))
 
     def add_eq(self, syst, eq, rac=None, rac_der=None):
         if rac is None:
@@ -329,6 +343,24 @@ class System_of_eqs:
 
     def add_eq_matching(self, dom, bound, eq):
         self.ctx.check(_L().kd_system_add_eq_matching(self.h, dom, bound, eq.encode()))
+
+    def add_eq_int_volume(self, dom_min, dom_max, eq):
+        """Integral equation "integvolume(f) = c" over domains dom_min..dom_max."""
+        self.ctx.check(_L().kd_system_add_eq_int_volume(self.h, dom_min, dom_max, eq.encode()))
+
+    def add_eq_int_inf(self, eq):
+        """Integral equation "integ(f) = c", integ() at infinity."""
+        self.ctx.check(_L().kd_system_add_eq_int_inf(self.h, eq.encode()))
+
+    def add_eq_val(self, dom, eq, pos):
+        """eq vanishes at collocation point pos = (i, j, k) of dom."""
+        p = (C.c_int * 3)(*[int(v) for v in pos])
+        self.ctx.check(_L().kd_system_add_eq_val(self.h, dom, eq.encode(), p))
+
+    def add_eq_point(self, dom, eq, point):
+        """eq vanishes at a Cartesian point, evaluated in domain dom."""
+        p = (C.c_double * 3)(*[float(v) for v in point])
+        self.ctx.check(_L().kd_system_add_eq_point(self.h, dom, eq.encode(), p))
 
     def sizes(self):
         nu, nc = C.c_int(), C.c_int()

@@ -184,3 +184,44 @@ TOY_EQUATIONS = {
     "matching": ["psi", "dn(psi)"],
     "outer": "psi = 1",
 }
+
+
+def eigen_nucleus(res=(11, 5, 4), normalise="val", lam0=9.0):
+    """Lap(u) + lam u = 0 in a nucleus of radius 1, u = 0 on its surface,
+    with the eigenvalue lam a double unknown and one normalisation: u = 1 at
+    the origin (add_eq_ori, "val") or integvolume(u) = 4/pi over the nucleus
+    (add_eq_int_volume, "integral").  Known answer: u = sin(pi r)/(pi r),
+    lam = pi^2.  Initial guess u = 1 - 0.9 r^2 in the nucleus, lam = lam0."""
+    doms = K.space_spheric(res, [1.0, 2.0])
+    u = K.scalar_field(doms, lambda d: (1 - 0.9 * d.radius() ** 2) if d.type == K.NUCLEUS else np.zeros(d.np))
+    sysm = K.OSystem(doms, 0, 0)
+    sysm.add_var("u", u)
+    sysm.add_var_double("lam", lam0)
+    sysm.add_eq_inside(0, lambda T, b: T["u"].lap() + T["lam"] * T["u"])
+    sysm.add_eq_bc(0, K.OUTER_BC, lambda T, b: T["u"])
+    if normalise == "val":
+        sysm.add_eq_val(0, lambda T: T["u"] - 1.0, (0, 0, 0))
+    else:
+        sysm.add_eq_int_volume(0, 0, lambda T: T["u"], lambda T: K.OTerm(0, 4.0 / math.pi, 0.0))
+    return doms, sysm, u
+
+
+def mass_at_infinity(res=(11, 5, 4), m0=0.5):
+    """Lap(P) = 0 in two shells and the compactified domain (bounds 1, 2, 4),
+    P = 2 at r = 1, P = 1 at infinity, and a double unknown M fixed by the
+    surface integral at infinity integ(dn(P)) + 4 pi M = 0.  Known answer:
+    P = 1 + 1/r, M = 1.  Initial guess P = 1, M = m0."""
+    doms = K.space_spheric(res, [1.0, 2.0, 4.0])
+    P = K.scalar_field(doms, lambda d: np.ones(d.np))
+    sysm = K.OSystem(doms, 1, 3)
+    sysm.add_var("P", P)
+    sysm.add_var_double("M", m0)
+    for d in range(1, 4):
+        sysm.add_eq_inside(d, lambda T, b: T["P"].lap())
+    sysm.add_eq_bc(1, K.INNER_BC, lambda T, b: T["P"] - 2.0)
+    for d in range(1, 3):
+        sysm.add_eq_matching(d, K.OUTER_BC, lambda T, b: T["P"])
+        sysm.add_eq_matching(d, K.OUTER_BC, lambda T, b: T["P"].dn(b))
+    sysm.add_eq_bc(3, K.OUTER_BC, lambda T, b: T["P"] - 1.0)
+    sysm.add_eq_int([(3, K.OUTER_BC, lambda T, b: T["P"].dn(b).integ(b) + 4 * math.pi * T["M"])])
+    return doms, sysm, P

@@ -684,6 +684,141 @@ def der_normal(so, bound):
     return so.der_var(1) / d.alpha
 
 
+def mult_r(so):
+    """Domain_*::mult_r (domain_nucleus_ope.cpp:214, domain_shell_ope.cpp:156,
+    domain_compact_ope.cpp:173)."""
+    if so.zero:
+        return so
+    d = so.dom
+    if d.type == NUCLEUS:
+        return opc(so, S.OP_MULT_X, 0) * d.alpha
+    if d.type == SHELL:
+        so.coef()
+        mx = opc(so, S.OP_MULT_X, 0)
+        return VD(d, so.B, cf=mx.cf * d.alpha + so.cf * d.beta, base=mx.base)
+    return opc(so, S.OP_DIV_XM1, 0) / d.alpha
+
+
+def integral_1d(base, cf):
+    """integral_1d (src/Ope_1d/integral_1d.cpp) of coefficient rows cf[..., i]."""
+    n = cf.shape[-1]
+    res = np.zeros(cf.shape[:-1])
+    if base == S.CHEB_EVEN:
+        for i in range(n):
+            res = res + -cf[..., i] / (4. * i * i - 1)
+    elif base == S.CHEB:
+        for i in range(0, n, 2):
+            res = res + -2 * cf[..., i] / (i * i - 1.)
+    else:
+        raise NotImplementedError(f"integral_1d of basis {base}")
+    return res
+
+
+def integ_volume(so):
+    """Domain_*::integ_volume (domain_nucleus_ope.cpp:260,
+    domain_shell_ope.cpp:281, domain_compact_ope.cpp:228), per batch member."""
+    if so.zero:
+        return np.zeros(so.B)
+    d = so.dom
+    w = mult_r(mult_r(opc(so, S.OP_MULT_SIN, 1)))
+    if d.type == COMPACT:
+        w = -mult_r(mult_r(w)) * d.alpha
+    else:
+        w = w * d.alpha
+    w.coef()
+    assert int(w.base.t[0]) == S.SIN_ODD
+    val = np.zeros(so.B)
+    for j in range(d.nc[1]):
+        baser = int(w.base.r[j, 0])
+        assert baser == (S.CHEB_EVEN if d.type == NUCLEUS else S.CHEB)
+        val = val + 2. / (2. * j + 1) * integral_1d(baser, w.cf[:, :, j, 0])
+    return val * 2 * math.pi
+
+
+def integ_surface(so, bound):
+    """Domain_compact::integ (domain_compact.cpp:89), per batch member."""
+    d = so.dom
+    assert d.type == COMPACT
+    if so.zero:
+        return np.zeros(so.B)
+    rr = mult_r(mult_r(opc(so, S.OP_MULT_SIN, 1)))
+    rr.coef()
+
+    def vb(j):
+        sg = np.array([(1.0 if i % 2 == 0 else -1.0) if bound == INNER_BC else 1.0 for i in range(d.nc[0])])
+        return rr.cf[:, :, j, 0] @ sg
+
+    res = np.zeros(so.B)
+    bt = int(rr.base.t[0])
+    if bt == S.COS_EVEN:
+        res = res + math.pi * vb(0)
+    elif bt == S.SIN_ODD:
+        for j in range(d.nc[1]):
+            res = res + 2. / (2 * j + 1) * vb(j)
+    elif bt not in (S.COS_ODD, S.SIN_EVEN):
+        raise NotImplementedError("integ: theta basis")
+    return res * 2 * math.pi
+
+
+def value_at(so, pos):
+    """Ope_val (src/Ope_eq/ope_val.cpp): the value at collocation point pos."""
+    if so.zero:
+        return np.zeros(so.B)
+    so.coef_i()
+    i, j, k = pos
+    return so.c[:, i, j, k].copy()
+
+
+def summation(so, num):
+    """Base_spectral::summation at numerical coordinates num, per batch member."""
+    if so.zero:
+        return np.zeros(so.B)
+    so.coef()
+    d, b = so.dom, so.base
+    xi, th, ph = num
+    nc0, nc1, nc2 = d.nc
+    out = np.zeros(so.B)
+    for m in range(so.B):
+        cf = so.cf[m]
+        lines = np.zeros((nc1, nc2))
+        for j in range(nc1):
+            for k in range(nc2):
+                lines[j, k] = S.summation_1d(int(b.r[j, k]), xi, cf[:, j, k])
+        tvals = np.array([S.summation_1d(int(b.t[k]), th, lines[:, k]) for k in range(nc2)])
+        out[m] = S.summation_1d(int(b.p), ph, tvals)
+    return out
+
+
+def absol_to_num(d, point):
+    """Domain_*::absol_to_num for a spheric domain centred at the origin."""
+    x, y, z = point
+    r = math.sqrt(x * x + y * y + z * z)
+    if d.type == NUCLEUS:
+        xi = r / d.alpha
+    elif d.type == SHELL:
+        xi = (r - d.beta) / d.alpha
+    else:
+        xi = 1. + 1. / r / d.alpha
+    rho = math.sqrt(x * x + y * y)
+    if rho == 0:
+        th, ph = (0.0 if z >= 0 else math.pi), 0.0
+    else:
+        th = math.atan(rho / z) if z != 0 else math.pi / 2
+        ph = math.atan2(y, x)
+    if th < 0:
+        th += math.pi
+    return xi, th, ph
+
+
+def _zero_der(x):
+    return not isinstance(x, np.ndarray) and x == 0.0
+
+
+def _no_seed_der(d):
+    if isinstance(d.der, np.ndarray):
+        raise NotImplementedError("a double depending on the seeded fields combined with a field")
+
+
 # ----------------------------------------------------------------- Term_eq --
 class OTerm:
     """Scalar Term_eq: value (VD or float) and optional batched tangent."""
@@ -709,6 +844,7 @@ class OTerm:
             t, dd = (o, self) if self.is_double else (self, o)
             der = None
             if do:
+                _no_seed_der(dd)
                 der = t.der if dd.der == 0.0 else t.der + dd.der
             return OTerm(self.dom, t.val + dd.val, der)
         return OTerm(self.dom, self.val + o.val, self.der + o.der if do else None)
@@ -721,10 +857,13 @@ class OTerm:
         if self.is_double and o.is_double:
             return OTerm(self.dom, self.val - o.val, self.der - o.der if do else None)
         if o.is_double:
+            if do:
+                _no_seed_der(o)
             return OTerm(self.dom, self.val - o.val, (self.der if o.der == 0.0 else self.der - o.der) if do else None)
         if self.is_double:
             der = None
             if do:
+                _no_seed_der(self)
                 der = -o.der if self.der == 0.0 else o.der.rsub(self.der)
             return OTerm(self.dom, o.val.rsub(self.val), der)
         return OTerm(self.dom, self.val - o.val, self.der - o.der if do else None)
@@ -746,6 +885,7 @@ class OTerm:
             t, dd = (o, self) if self.is_double else (self, o)
             der = None
             if do:
+                _no_seed_der(dd)
                 der = t.der * dd.val
                 if dd.der != 0.0:
                     der = der + t.val * dd.der
@@ -760,10 +900,14 @@ class OTerm:
         if o.is_double:
             der = None
             if do:
-                num = self.der * o.val
-                if o.der != 0.0:
-                    num = num - self.val * o.der
-                der = num / (o.val * o.val)
+                if self.is_double:
+                    der = (self.der * o.val - self.val * o.der) / (o.val * o.val)
+                else:
+                    _no_seed_der(o)
+                    num = self.der * o.val
+                    if not _zero_der(o.der):
+                        num = num - self.val * o.der
+                    der = num / (o.val * o.val)
             return OTerm(self.dom, self.val / o.val, der)
         if self.is_double:
             raise NotImplementedError("double divided by a field term")
@@ -790,6 +934,29 @@ class OTerm:
         """Cartesian derivative d/dx_i (Val_domain::der_abs, i = 1, 2, 3)."""
         return OTerm(self.dom, self.val.der_abs(i), None if self.der is None else self.der.der_abs(i))
 
+    def _functional(self, f):
+        val = 0.0 if self.val.zero else float(f(self.val)[0])
+        der = None
+        if self.der is not None:
+            der = 0.0 if self.der.zero else f(self.der)
+        return OTerm(self.dom, val, der)
+
+    def integvolume(self):
+        """Ope_int_volume (src/Ope_eq/ope_int_volume.cpp)."""
+        return self._functional(integ_volume)
+
+    def integ(self, bound):
+        """Ope_int (src/Ope_eq/ope_int.cpp) in the compactified domain."""
+        return self._functional(lambda v: integ_surface(v, bound))
+
+    def val_at(self, pos):
+        """Ope_val (src/Ope_eq/ope_val.cpp)."""
+        return self._functional(lambda v: value_at(v, pos))
+
+    def val_point(self, num):
+        """Ope_point (src/Ope_eq/ope_point.cpp)."""
+        return self._functional(lambda v: summation(v, num))
+
 
 # -------------------------------------------------------------- the system --
 class OSystem:
@@ -799,11 +966,39 @@ class OSystem:
     def __init__(self, doms, dom_min, dom_max):
         self.doms, self.dmin, self.dmax = doms, dom_min, dom_max
         self.vars = []       # (name, dict dom -> VD with B=1)
+        self.vdoubles = []   # [name, value]: unknowns that are numbers
         self.eqs = []        # (kind, dom, bound, fn_lhs, other_dom, other_bound, fn_rhs)
+        self.ieqs = []       # integral-type equations: lists of parts (dom, bound, fn -> double OTerm)
         self.nbr_conditions = None
 
     def add_var(self, name, fields):
         self.vars.append((name, fields))
+
+    def add_var_double(self, name, value):
+        """add_var(name, double&) (system_of_eqs.cpp:284)."""
+        self.vdoubles.append([name, float(value)])
+
+    def add_eq_int(self, parts):
+        """An Eq_int (eq_int.cpp): its value is the sum of its parts, each a
+        (dom, bound, fn(T, bound) -> double OTerm); one condition, placed
+        before every other equation (sec_member, solver.cpp:49)."""
+        self.ieqs.append(list(parts))
+
+    def add_eq_int_volume(self, dmin, dmax, fn_integrand, fn_const):
+        """Space_spheric::add_eq_int_volume (spheric_add_eq.cpp:81):
+        sum_d integvolume(f) in every domain, minus the constant side."""
+        parts = [(d, None, (lambda T, b, fn=fn_integrand: fn(T).integvolume())) for d in range(dmin, dmax + 1)]
+        parts.append((dmin, None, lambda T, b: -fn_const(T)))
+        self.add_eq_int(parts)
+
+    def add_eq_val(self, dom, fn, pos):
+        """add_eq_val (add_eq.cpp:343): fn vanishes at collocation point pos."""
+        self.add_eq_int([(dom, None, lambda T, b: fn(T).val_at(pos))])
+
+    def add_eq_point(self, dom, fn, point):
+        """add_eq_point (add_eq.cpp:355): fn vanishes at a Cartesian point."""
+        num = absol_to_num(self.doms[dom], point)
+        self.add_eq_int([(dom, None, lambda T, b: fn(T).val_point(num))])
 
     def add_eq_inside(self, dom, fn):
         self.eqs.append(("inside", dom, None, fn, None, None, None))
@@ -817,14 +1012,38 @@ class OSystem:
         self.eqs.append(("matching", dom, bound, fn_lhs, other, other_bound, fn_rhs or fn_lhs))
 
     def _terms(self, dom, seed=None):
+        """Unknowns as Term_eqs; seed = (var, dom, batch seed VD) for a field
+        block, or ("double", i) for the column of double unknown i."""
         out = {}
+        dseed = seed is not None and seed[0] == "double"
         for vi, (name, f) in enumerate(self.vars):
             val = f[dom]
             der = None
             if seed is not None:
-                sv, sd, sb = seed
-                der = sb if (vi == sv and dom == sd) else VD.zeros(self.doms[dom], sb.B)
+                if dseed:
+                    der = VD.zeros(self.doms[dom], 1)
+                else:
+                    sv, sd, sb = seed
+                    der = sb if (vi == sv and dom == sd) else VD.zeros(self.doms[dom], sb.B)
             out[name] = OTerm(dom, val, der)
+        for i, (name, v) in enumerate(self.vdoubles):
+            der = None
+            if seed is not None:
+                der = 1.0 if (dseed and seed[1] == i) else 0.0
+            out[name] = OTerm(dom, float(v), der)
+        return out
+
+    def _int_rows(self, seed=None, only_dom=None):
+        """Values (seed None) or tangents of the integral equations."""
+        out = []
+        for parts in self.ieqs:
+            acc = 0.0
+            for (d, b, fn) in parts:
+                if only_dom is not None and d != only_dom:
+                    continue
+                t = fn(self._terms(d, seed), b)
+                acc = acc + (t.val if seed is None else t.der)
+            out.append(acc)
         return out
 
     def _rows(self, kind, dom, base, bound):
@@ -848,7 +1067,7 @@ class OSystem:
         return cf @ M.T, len(rows)
 
     def residual(self):
-        F = []
+        F = [np.array([v]) for v in self._int_rows()]
         for (kind, dom, bound, fn, odom, obound, fnr) in self.eqs:
             t = fn(self._terms(dom), bound)
             v, n = self._export(kind, t.val, dom, bound)
@@ -865,7 +1084,7 @@ class OSystem:
 
     def unknown_layout(self):
         layout = []
-        col = 0
+        col = len(self.vdoubles)
         for vi, (name, f) in enumerate(self.vars):
             for dd in range(self.dmin, self.dmax + 1):
                 pats = self.doms[dd].unknown_patterns(f[dd].base)
@@ -879,12 +1098,29 @@ class OSystem:
         assert N == len(F), (N, len(F))
         J = np.zeros((N, N))
         row0 = []
-        r = 0
+        nint = len(self.ieqs)
+        r = nint
         for eq in self.eqs:
             kind, dom, bound, fn, odom, obound, fnr = eq
             _, n = self._export(kind, fn(self._terms(dom), bound).val, dom, bound)
             row0.append((r, n))
             r += n
+        # columns of the double unknowns: every equation (do_col_J, is_var_double)
+        for i in range(len(self.vdoubles)):
+            seed = ("double", i)
+            for e, (kind, dom, bound, fn, odom, obound, fnr) in enumerate(self.eqs):
+                r0, n = row0[e]
+                t = fn(self._terms(dom, seed), bound)
+                v, _ = self._export(kind, t.der, dom, bound)
+                if v is not None:
+                    J[r0:r0 + n, i] += v[0]
+                if kind == "matching":
+                    t = fnr(self._terms(odom, seed), obound)
+                    v, _ = self._export(kind, t.der, odom, obound)
+                    if v is not None:
+                        J[r0:r0 + n, i] -= v[0]
+            for k, dv in enumerate(self._int_rows(seed)):
+                J[k, i] = float(np.asarray(dv).reshape(-1)[0]) if isinstance(dv, np.ndarray) else dv
         for vi, dd, col, pats in layout:
             d = self.doms[dd]
             B = len(pats)
@@ -906,11 +1142,15 @@ class OSystem:
                     v, _ = self._export(kind, t.der, odom, obound)
                     if v is not None:
                         J[r0:r0 + n, col:col + B] -= v.T
+            for k, dv in enumerate(self._int_rows((vi, dd, sb), only_dom=dd)):
+                J[k, col:col + B] += dv
         return F, J
 
     def update(self, x):
         """xx_to_vars then var = old - new (do_newton_seq, src_par/do_newton.cpp:558-566)."""
         layout, N = self.unknown_layout()
+        for i in range(len(self.vdoubles)):
+            self.vdoubles[i][1] -= x[i]
         for vi, dd, col, pats in layout:
             name, f = self.vars[vi]
             d = self.doms[dd]
