@@ -341,6 +341,7 @@ def run_gpu(args, ws, rank, local):
         prof[name] = KD.profile_read(ctx)
         KD.profile_enable(ctx, False)
 
+    exporter = run_exporter(args, ctx, wl, stream, local) if args.export_points > 0 else None
     batch = run_batch(args, local) if args.batch > 0 else None
 
     if rank != 0:
@@ -388,6 +389,7 @@ def run_gpu(args, ws, rank, local):
         "fp64_peak_tflops_measured": fp64_tflops,
         "clocks": clk.summary(),
         "batch": batch,
+        "exporter": exporter,
     }
     if not args.no_cpu:
         cb = cpu_step_sample(args.workload, blocks=args.cpu_blocks)
@@ -396,6 +398,59 @@ def run_gpu(args, ws, rank, local):
                                 "phases_ms": {k: cb[k] for k in ("residual_ms", "assembly_ms", "lu_solve_ms")}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def run_exporter(args, ctx, wl, stream, local):
+    """The converged fields evaluated at --export-points random Cartesian
+    points (radii up to 4x the outer shell, every domain including the
+    compactified one) on the GPU: kd_fields_val_points_device, all unknown
+    fields at once, points already resident in HBM.  Work per point and
+    field: 2 flops per coefficient of the domain holding the point."""
+    import numpy as np
+    import torch
+
+    from kadath_frontera_gb300 import kadath as KD
+
+    n = args.export_points
+    fields = [f for _, f in wl.unknowns]
+    g = torch.Generator(device=f"cuda:{local}").manual_seed(0)
+    r = 128.0 * torch.rand(n, device=f"cuda:{local}", dtype=torch.float64, generator=g) ** 2
+    v = torch.randn(n, 3, device=f"cuda:{local}", dtype=torch.float64, generator=g)
+    xyz = (v / v.norm(dim=1, keepdim=True) * r[:, None]).contiguous()
+    out = torch.empty(len(fields), n, device=f"cuda:{local}", dtype=torch.float64)
+    torch.cuda.synchronize()
+    for _ in range(2):
+        KD.val_points_device(fields, xyz.data_ptr(), out.data_ptr(), n)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    reps = 5
+    ev0.record(stream)
+    for _ in range(reps):
+        KD.val_points_device(fields, xyz.data_ptr(), out.data_ptr(), n)
+    ev1.record(stream)
+    ev1.synchronize()
+    ms = ev0.elapsed_time(ev1) / reps
+    # algorithmic flops: 2 per coefficient of the point's domain, per field
+    space = wl.space
+    radii = r.cpu().numpy()
+    ncoef = []
+    for d in range(space.get_nbr_domains()):
+        info = space.domain_info(d)
+        nc = info["nbr_coefs"]
+        ncoef.append(int(nc[0] * nc[1] * nc[2]))
+    edges = list(workloads_bounds(wl))
+    dom_of = np.searchsorted(np.asarray(edges), radii, side="left")
+    flops = 2.0 * len(fields) * float(np.sum(np.asarray(ncoef)[np.minimum(dom_of, len(ncoef) - 1)]))
+    achieved = flops / (ms * 1e-3) / 1e12
+    return {"points": n, "fields": len(fields), "ms": ms, "points_per_s": n / (ms * 1e-3),
+            "kernel": "val_points_kernel", "achieved_tflops_fp64": achieved,
+            "work": "2 flops per coefficient of the point's domain per field (spectral summation)"}
+
+
+def workloads_bounds(wl):
+    """Outer radii of the star workload's domains (the last one infinite)."""
+    from kadath_frontera_gb300 import workloads
+    return list(workloads.STAR_BOUNDS) if wl.name == "star" else [1.0, 2.0]
 
 
 def run_batch(args, local):
@@ -502,6 +557,8 @@ def main():
     ap.add_argument("--cpu-blocks", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--batch", type=int, default=16, help="instances of the batched-solve measurement (0: skip)")
+    ap.add_argument("--export-points", type=int, default=1 << 20,
+                    help="points of the exporter measurement (0: skip)")
     ap.add_argument("--batch-threads", type=int, default=8)
     args = ap.parse_args()
     if args.impl == "reference":

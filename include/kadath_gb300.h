@@ -281,6 +281,19 @@ int kd_newton_step(kd_system* s, const kd_newton_opts* opts, kd_newton_report* r
 int kd_newton_step_linesearch(kd_system* s, const kd_newton_opts* opts, int ntrymax, double stepmax,
                               kd_newton_report* rep, double* lambda);
 
+/* ---- evaluation at arbitrary points (exporters) ------------------------ */
+/* Scalar::val_point (include/scalar.hpp:221) for many points and up to 8
+ * fields of one space at once: the evaluation the reference's exporters
+ * (src/Utilities/Exporters) do point by point, here one GPU thread per
+ * point.  out[f * npts + p] = fields[f] at the Cartesian point
+ * (xyz[3p], xyz[3p+1], xyz[3p+2]); NaN for a point in no domain.  Host
+ * pointers, synchronous. */
+int kd_fields_val_points(int nfields, kd_field* const* fields, long long npts, const double* xyz, double* out);
+/* The same with device pointers (d_xyz, d_out) on the context's stream;
+ * returns once the values are written. */
+int kd_fields_val_points_device(int nfields, kd_field* const* fields, long long npts, const double* d_xyz,
+                                double* d_out);
+
 /* ---- adjoint sensitivities --------------------------------------------- */
 /* No reference counterpart for the adjoint itself: the reference obtains
  * parameter derivatives by finite differences of full re-solves.  Pieces:

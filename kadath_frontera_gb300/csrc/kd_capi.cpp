@@ -7,6 +7,7 @@
 #include <string>
 
 #include "kadath_gb300.h"
+#include "kd_points.hpp"
 #include "kd_context.hpp"
 #include "kd_noalloc.hpp"
 #include "kd_spectral.hpp"
@@ -676,6 +677,57 @@ int kd_field_val_point(kd_field* f, const double point[3], double* value) {
   return guarded(f->sp->ctx, [&] {
     if (!point || !value) throw kd::KdError(KD_ERR_ARG, "null argument");
     *value = f->f->val_point(point);
+  });
+}
+
+static std::vector<const kd::Field*> field_list(int nfields, kd_field* const* fields) {
+  if (nfields <= 0 || !fields) throw kd::KdError(KD_ERR_ARG, "no fields");
+  std::vector<const kd::Field*> out;
+  for (int f = 0; f < nfields; f++) {
+    if (!fields[f] || !fields[f]->f) throw kd::KdError(KD_ERR_ARG, "null field");
+    if (fields[f]->sp != fields[0]->sp) throw kd::KdError(KD_ERR_ARG, "fields on different spaces");
+    out.push_back(fields[f]->f.get());
+  }
+  return out;
+}
+
+int kd_fields_val_points(int nfields, kd_field* const* fields, long long npts, const double* xyz, double* out) {
+  if (nfields <= 0 || !fields || !fields[0] || !fields[0]->f) return KD_ERR_ARG;
+  return guarded(fields[0]->sp->ctx, [&] {
+    auto list = field_list(nfields, fields);
+    if (npts < 0 || (npts > 0 && (!xyz || !out))) throw kd::KdError(KD_ERR_ARG, "null argument");
+    if (npts == 0) return;
+    kd::Context& c = *fields[0]->sp->ctx->c;
+    cudaStream_t s = c.stream();
+    double *d_xyz = nullptr, *d_out = nullptr;
+    kd::cuda_check(cudaMalloc(&d_xyz, sizeof(double) * 3 * npts), "cudaMalloc(points)");
+    if (cudaMalloc(&d_out, sizeof(double) * nfields * npts) != cudaSuccess) {
+      cudaFree(d_xyz);
+      throw kd::KdError(KD_ERR_CUDA, "cudaMalloc(values)");
+    }
+    try {
+      kd::cuda_check(cudaMemcpyAsync(d_xyz, xyz, sizeof(double) * 3 * npts, cudaMemcpyHostToDevice, s), "H2D points");
+      kd::fields_val_points(&c, list, npts, d_xyz, d_out);
+      kd::cuda_check(cudaMemcpyAsync(out, d_out, sizeof(double) * nfields * npts, cudaMemcpyDeviceToHost, s),
+                     "D2H values");
+      kd::cuda_check(cudaStreamSynchronize(s), "sync");
+    } catch (...) {
+      cudaFree(d_xyz);
+      cudaFree(d_out);
+      throw;
+    }
+    cudaFree(d_xyz);
+    cudaFree(d_out);
+  });
+}
+
+int kd_fields_val_points_device(int nfields, kd_field* const* fields, long long npts, const double* d_xyz,
+                                double* d_out) {
+  if (nfields <= 0 || !fields || !fields[0] || !fields[0]->f) return KD_ERR_ARG;
+  return guarded(fields[0]->sp->ctx, [&] {
+    auto list = field_list(nfields, fields);
+    if (npts < 0 || (npts > 0 && (!d_xyz || !d_out))) throw kd::KdError(KD_ERR_ARG, "null argument");
+    kd::fields_val_points(fields[0]->sp->ctx->c.get(), list, npts, d_xyz, d_out);
   });
 }
 

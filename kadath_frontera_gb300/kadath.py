@@ -97,6 +97,8 @@ def _declare_system(lib):
         "kd_system_set_cst": (I, [P, C.c_char_p, D]),
         "kd_system_add_ope_eos": (I, [P, C.c_char_p, I, I, D, D, D, DP, DP]),
         "kd_field_val_point": (I, [P, DP, DP]),
+        "kd_fields_val_points": (I, [I, C.POINTER(P), C.c_longlong, DP, DP]),
+        "kd_fields_val_points_device": (I, [I, C.POINTER(P), C.c_longlong, P, P]),
         "kd_system_val_point_gradient": (I, [P, C.c_char_p, DP, DP]),
         "kd_system_dres_dcst": (I, [P, C.c_char_p, DP]),
         "kd_adjoint": (I, [P, DP, C.c_char_p, D, DP, DP]),
@@ -212,6 +214,26 @@ class Space_spheric:
                 _L().kd_space_destroy(self.h)
         except Exception:
             pass
+
+
+def val_points(fields, xyz):
+    """Values of one or several Scalars of one space at Cartesian points
+    xyz (array (n, 3)), evaluated on the GPU: an array (nfields, n), NaN for
+    points in no domain (Scalar::val_point for many points)."""
+    fields = list(fields)
+    pts = np.ascontiguousarray(np.asarray(xyz, dtype=np.float64).reshape(-1, 3))
+    out = np.zeros((len(fields), pts.shape[0]))
+    arr = (C.c_void_p * len(fields))(*[f.h for f in fields])
+    fields[0].space.ctx.check(_L().kd_fields_val_points(len(fields), arr, pts.shape[0], _dp(pts), _dp(out)))
+    return out
+
+
+def val_points_device(fields, d_xyz, d_out, npts):
+    """val_points with device pointers (d_xyz: 3 npts doubles, d_out:
+    nfields npts doubles), on the fields' context stream."""
+    fields = list(fields)
+    arr = (C.c_void_p * len(fields))(*[f.h for f in fields])
+    fields[0].space.ctx.check(_L().kd_fields_val_points_device(len(fields), arr, int(npts), C.c_void_p(d_xyz), C.c_void_p(d_out)))
 
 
 class Scalar:
