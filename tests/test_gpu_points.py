@@ -60,7 +60,8 @@ def test_points_outside_every_domain_are_nan(ctx):
 
 
 def test_analytic_field_at_points(ctx):
-    """x y z r^-? : a field known in closed form, evaluated away from the
+    """1 + (x y + z^2) / (1 + r^4): a field known in closed form, even in z
+    as the symmetric spheric space requires, evaluated away from the
     collocation points (spectral accuracy of the summation itself)."""
     from kadath_frontera_gb300.kadath import CHEB_TYPE, Scalar, Space_spheric, val_points
     space = Space_spheric(CHEB_TYPE, (0, 0, 0), (17, 9, 8), (1.0, 2.0, 4.0))
@@ -69,11 +70,11 @@ def test_analytic_field_at_points(ctx):
         x, y, z = (space.get_cart(d, c) for c in (1, 2, 3))
         r = space.get_radius(d)
         with np.errstate(invalid="ignore", divide="ignore"):
-            v = np.where(np.isfinite(r), 1.0 + x * z / (1.0 + r ** 4), 1.0)
+            v = np.where(np.isfinite(r), 1.0 + (x * y + z * z) / (1.0 + r ** 4), 1.0)
         f.set_domain(d, v)
     f.std_base()
     pts = _points(np.random.default_rng(5), 300, 30.0)[:-2]
     got = val_points([f], pts)[0]
     r = np.linalg.norm(pts, axis=1)
-    exact = 1.0 + pts[:, 0] * pts[:, 2] / (1.0 + r ** 4)
-    assert np.abs(got - exact).max() < 1e-6
+    exact = 1.0 + (pts[:, 0] * pts[:, 1] + pts[:, 2] ** 2) / (1.0 + r ** 4)
+    assert np.abs(got - exact).max() < 1e-9
