@@ -898,16 +898,37 @@ __global__ void __launch_bounds__(GP_THREADS) panel_grid_kernel(T* __restrict__ 
 // ---- panel on one 16-CTA cluster (FP32 factors) --------------------------
 // The same algorithm as panel_grid_kernel with the exchange in distributed
 // shared memory: CTA r of the cluster keeps rows [j0 + r*per, ...) of the
-// panel in its shared memory; per column each CTA writes its candidate
-// (value, row, full panel row) and, when it owns row j, row j into its own
-// double-buffered slots, one cluster barrier, then every CTA reads the 16
-// candidates and the winning row from the owners' shared memory.  A final
-// cluster barrier keeps every CTA's shared memory alive until the last
-// remote reads are done.
+// panel in its shared memory.  Per column, one block barrier and one cluster
+// barrier:
+//  - every thread already holds its best candidate for the column (found
+//    while updating it in the previous column step); a warp reduction and
+//    one block barrier give the CTA's candidate;
+//  - warp 0 pushes (value, row, the row's inner-block segment) into every
+//    CTA's receive slot, and warp 1 of the owner of row j pushes row j's
+//    segment; the CTA keeps its candidate's full row and row j locally;
+//  - after the cluster barrier every thread picks the winner from its own
+//    receive slot (same order everywhere), and the owner threads of rows j
+//    and gi swap the inner-block segments; each thread then scales column
+//    j, updates its rows in the inner block's columns and tracks its
+//    candidate for column j + 1, all in one pass;
+//  - the other columns of the two swapped rows are fetched from the owners'
+//    shared memory off the critical path (they are read again only after
+//    the next cluster barrier).
+// Receive slots, candidate rows and row j are double-buffered by column
+// parity: a CTA can only overwrite a slot after every CTA has passed the
+// next cluster barrier, i.e. has finished reading it.
 constexpr int CP_CL = 16;
 constexpr int CP_THREADS = 512;
+constexpr int CP_WARPS = CP_THREADS / 32;
 constexpr size_t CP_MAX_SMEM = 212 * 1024;
 constexpr int CP_IB = 16;  // inner block: columns updated per column step
+
+struct CpSlot {
+  float seg[CP_CL][CP_IB];  // candidate row segments [jj, be), by source CTA
+  float v[CP_CL];           // candidate |values|, by source CTA
+  int i[CP_CL];             // candidate rows (N: none), by source CTA
+  float jseg[CP_IB];        // row j's segment [jj, be)
+};
 
 __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __restrict__ A, long long ld, int N,
                                                                      int j0, int jb, int per,
@@ -919,14 +940,13 @@ __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __re
   float* tile = reinterpret_cast<float*>(cp_raw);  // tile[k * per + r]
   __shared__ float cand_row[2][128];
   __shared__ float jrow[2][128];
-  __shared__ float cand_v[2];
-  __shared__ int cand_i[2];
-  __shared__ float prow[128];
+  __shared__ CpSlot recv[2];
   __shared__ float ublk[CP_IB][128];  // rows of the current inner block (L11 | A12 -> U12)
-  __shared__ float rv[CP_THREADS / 32];
-  __shared__ int ri[CP_THREADS / 32], rt[CP_THREADS / 32];
+  __shared__ float wv[CP_WARPS];
+  __shared__ int wi[CP_WARPS];
   const int rank = static_cast<int>(cluster.block_rank());
   const int tid = threadIdx.x, bd = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5;
   const int r0 = j0 + rank * per;
   const int r1 = (r0 + per < N) ? r0 + per : N;
   const int nr = r1 > r0 ? r1 - r0 : 0;
@@ -937,98 +957,124 @@ __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __re
   __syncthreads();
   for (int b0 = 0; b0 < jb; b0 += CP_IB) {
     const int be = (b0 + CP_IB < jb) ? b0 + CP_IB : jb;
+    // this thread's candidate for the block's first column
+    float best = -1.0f;
+    int bi = N;
+    for (int li = tid; li < nr; li += bd) {
+      const int i = r0 + li;
+      if (i < j0 + b0) continue;
+      const float v = fabsf(tile[b0 * per + li]);
+      if (better(v, i, best, bi)) {
+        best = v;
+        bi = i;
+      }
+    }
     for (int jj = b0; jj < be; jj++) {
       const int j = j0 + jj;
       const int slot = jj & 1;
-      float best = -1.0f;
-      int bi = N, tag = 0;
-      for (int i = (r0 > j ? r0 : j) + tid; i < r1; i += bd) {
-        float v = fabsf(tile[jj * per + i - r0]);
-        if (better(v, i, best, bi)) {
-          best = v;
-          bi = i;
+      const int w = be - jj;  // segment [jj, be)
+      for (int o = 16; o > 0; o >>= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (better(ov, oi, best, bi)) {
+          best = ov;
+          bi = oi;
         }
       }
-      block_argmax(best, bi, tag, rv, ri, rt);
-      if (bi < N)
-        for (int k = tid; k < jb; k += bd) cand_row[slot][k] = tile[k * per + bi - r0];
-      if (tid == 0) {
-        cand_v[slot] = best;
-        cand_i[slot] = bi;
+      if (lane == 0) {
+        wv[warp] = best;
+        wi[warp] = bi;
       }
-      if (j >= r0 && j < r1)
-        for (int k = tid; k < jb; k += bd) jrow[slot][k] = tile[k * per + j - r0];
-      cluster.sync();
-      // every CTA reduces the 16 candidates in the same order
-      best = -1.0f;
-      bi = N;
-      tag = -1;
-      if (tid < 32) {
-        if (tid < CP_CL) {
-          best = *cluster.map_shared_rank(&cand_v[slot], tid);
-          bi = *cluster.map_shared_rank(&cand_i[slot], tid);
-          tag = tid;
-        }
+      __syncthreads();  // also orders the previous column step's tile writes
+      if (warp == 0) {
+        float cv = (lane < CP_WARPS) ? wv[lane] : -1.0f;
+        int ci = (lane < CP_WARPS) ? wi[lane] : N;
         for (int o = 16; o > 0; o >>= 1) {
-          float ov = __shfl_xor_sync(0xffffffffu, best, o);
-          int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-          int ot = __shfl_xor_sync(0xffffffffu, tag, o);
-          if (better(ov, oi, best, bi)) {
-            best = ov;
-            bi = oi;
-            tag = ot;
+          const float ov = __shfl_xor_sync(0xffffffffu, cv, o);
+          const int oi = __shfl_xor_sync(0xffffffffu, ci, o);
+          if (better(ov, oi, cv, ci)) {
+            cv = ov;
+            ci = oi;
           }
         }
-        if (tid == 0) {
-          rv[0] = best;
-          ri[0] = bi;
-          rt[0] = tag;
+        if (ci < N)
+          for (int k = lane; k < jb; k += 32) cand_row[slot][k] = tile[k * per + ci - r0];
+        CpSlot* R = cluster.map_shared_rank(&recv[slot], lane & (CP_CL - 1));
+        if (lane < CP_CL) {
+          R->v[rank] = cv;
+          R->i[rank] = ci;
+        }
+        for (int k = lane >> 4; k < w; k += 2) R->seg[rank][k] = (ci < N) ? tile[(jj + k) * per + ci - r0] : 0.0f;
+      } else if (warp == 1 && j >= r0 && j < r1) {
+        for (int k = lane; k < jb; k += 32) jrow[slot][k] = tile[k * per + j - r0];
+        CpSlot* R = cluster.map_shared_rank(&recv[slot], lane & (CP_CL - 1));
+        for (int k = lane >> 4; k < w; k += 2) R->jseg[k] = tile[(jj + k) * per + j - r0];
+      }
+      cluster.sync();
+      // the winner, from this CTA's own receive slot (same order everywhere)
+      float gv = -1.0f;
+      int gi = N, tag = -1;
+      for (int q = 0; q < CP_CL; q++) {
+        const float v = recv[slot].v[q];
+        const int i = recv[slot].i[q];
+        if (better(v, i, gv, gi)) {
+          gv = v;
+          gi = i;
+          tag = q;
         }
       }
-      __syncthreads();
-      best = rv[0];
-      int gi = ri[0];
-      tag = rt[0];
       if (gi >= N) {  // nothing usable below the diagonal: no swap
         gi = j;
         tag = -1;
       }
       if (rank == 0 && tid == 0) {
         ipiv[j] = gi;
-        if (!(best > 0.0f) && *info == 0) *info = j + 1;  // zero (or NaN) pivot
+        if (!(gv > 0.0f) && *info == 0) *info = j + 1;  // zero (or NaN) pivot
       }
-      const int jowner = (j - j0) / per;
-      const float* src = (tag >= 0) ? cluster.map_shared_rank(&cand_row[slot][0], tag)
-                                    : cluster.map_shared_rank(&jrow[slot][0], jowner);
-      for (int k = tid; k < jb; k += bd) prow[k] = src[k];
-      if (gi != j && gi >= r0 && gi < r1) {
-        const float* jr = cluster.map_shared_rank(&jrow[slot][0], jowner);
-        for (int k = tid; k < jb; k += bd) tile[k * per + gi - r0] = jr[k];
-      }
-      __syncthreads();
-      if (j >= r0 && j < r1)
-        for (int k = tid; k < jb; k += bd) tile[k * per + j - r0] = prow[k];
-      const float piv = prow[jj];
-      const int rs = (r0 > j + 1) ? r0 : j + 1;
-      __syncthreads();
-      if (piv != 0.0f && rs < r1) {
-        // scale the column, rank-1 update of the inner block's columns only
-        const float inv = 1.0f / piv;
-        for (int i = rs + tid; i < r1; i += bd) tile[jj * per + i - r0] *= inv;
-        __syncthreads();
-        const int nrr = r1 - rs;
-        const int nph = bd >> 7, ph = tid >> 7;
-        for (int i0 = 0; i0 < nrr; i0 += 128) {
-          const int ii = i0 + (tid & 127);
-          if (ii < nrr) {
-            const int li = rs - r0 + ii;
-            const float l = tile[jj * per + li];
-            for (int k = jj + 1 + ph; k < be; k += nph)
-              tile[k * per + li] = fmaf(-l, prow[k], tile[k * per + li]);
+      const float* pseg = (tag >= 0) ? recv[slot].seg[tag] : recv[slot].jseg;  // pivot row segment
+      const float* jseg = recv[slot].jseg;
+      const float piv = pseg[0];
+      const float inv = (piv != 0.0f) ? 1.0f / piv : 0.0f;
+      best = -1.0f;
+      bi = N;
+      for (int li = tid; li < nr; li += bd) {
+        const int i = r0 + li;
+        if (i == j) {  // row j becomes the pivot row (inner-block segment)
+          for (int k = 0; k < w; k++) tile[(jj + k) * per + li] = pseg[k];
+          continue;
+        }
+        if (i < j) continue;
+        if (i == gi)  // row gi takes row j's place (inner-block segment)
+          for (int k = 0; k < w; k++) tile[(jj + k) * per + li] = jseg[k];
+        if (piv != 0.0f) {
+          const float l = tile[jj * per + li] * inv;
+          tile[jj * per + li] = l;
+          for (int k = 1; k < w; k++) {
+            const float t = fmaf(-l, pseg[k], tile[(jj + k) * per + li]);
+            tile[(jj + k) * per + li] = t;
+            if (k == 1 && better(fabsf(t), i, best, bi)) {
+              best = fabsf(t);
+              bi = i;
+            }
           }
+        } else if (w > 1 && better(fabsf(tile[(jj + 1) * per + li]), i, best, bi)) {
+          best = fabsf(tile[(jj + 1) * per + li]);
+          bi = i;
         }
       }
-      __syncthreads();
+      // the swapped rows' other columns, from the owners' shared memory
+      if (gi != j) {
+        if (gi >= r0 && gi < r1) {
+          const float* src = cluster.map_shared_rank(&jrow[slot][0], (j - j0) / per);
+          for (int k = tid; k < jb; k += bd)
+            if (k < jj || k >= be) tile[k * per + gi - r0] = src[k];
+        }
+        if (j >= r0 && j < r1) {
+          const float* src = cluster.map_shared_rank(&cand_row[slot][0], tag);
+          for (int k = tid; k < jb; k += bd)
+            if (k < jj || k >= be) tile[k * per + j - r0] = src[k];
+        }
+      }
     }
     if (be < jb) {
       // Rows j0+b0 .. j0+be-1 are final in columns b0..be-1 (L11 below the
@@ -1081,6 +1127,7 @@ __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __re
       __syncthreads();
     }
   }
+  __syncthreads();
   for (int e = tid; e < jb * nr; e += bd) {
     int k = e / nr, r = e % nr;
     A[static_cast<long long>(j0 + k) * ld + r0 + r] = tile[k * per + r];
