@@ -1011,16 +1011,23 @@ __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __re
         for (int k = lane >> 4; k < w; k += 2) R->jseg[k] = tile[(jj + k) * per + j - r0];
       }
       cluster.sync();
-      // the winner, from this CTA's own receive slot (same order everywhere)
+      // the winner, from this CTA's own receive slot: every warp reduces the
+      // 16 candidates across its lanes (same result everywhere)
       float gv = -1.0f;
       int gi = N, tag = -1;
-      for (int q = 0; q < CP_CL; q++) {
-        const float v = recv[slot].v[q];
-        const int i = recv[slot].i[q];
-        if (better(v, i, gv, gi)) {
-          gv = v;
-          gi = i;
-          tag = q;
+      if (lane < CP_CL) {
+        gv = recv[slot].v[lane];
+        gi = recv[slot].i[lane];
+        tag = lane;
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, gv, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, gi, o);
+        const int ot = __shfl_xor_sync(0xffffffffu, tag, o);
+        if (better(ov, oi, gv, gi)) {
+          gv = ov;
+          gi = oi;
+          tag = ot;
         }
       }
       if (gi >= N) {  // nothing usable below the diagonal: no swap
@@ -1037,30 +1044,37 @@ __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __re
       const float inv = (piv != 0.0f) ? 1.0f / piv : 0.0f;
       best = -1.0f;
       bi = N;
+      float ps[CP_IB];
+#pragma unroll
+      for (int k = 0; k < CP_IB; k++) ps[k] = (k < w) ? pseg[k] : 0.0f;
       for (int li = tid; li < nr; li += bd) {
         const int i = r0 + li;
         if (i == j) {  // row j becomes the pivot row (inner-block segment)
-          for (int k = 0; k < w; k++) tile[(jj + k) * per + li] = pseg[k];
+#pragma unroll
+          for (int k = 0; k < CP_IB; k++)
+            if (k < w) tile[(jj + k) * per + li] = ps[k];
           continue;
         }
         if (i < j) continue;
-        if (i == gi)  // row gi takes row j's place (inner-block segment)
-          for (int k = 0; k < w; k++) tile[(jj + k) * per + li] = jseg[k];
+        // the row's inner-block segment in registers (row gi takes row j's)
+        float t[CP_IB];
+#pragma unroll
+        for (int k = 0; k < CP_IB; k++)
+          if (k < w) t[k] = (i == gi) ? jseg[k] : tile[(jj + k) * per + li];
         if (piv != 0.0f) {
-          const float l = tile[jj * per + li] * inv;
-          tile[jj * per + li] = l;
-          for (int k = 1; k < w; k++) {
-            const float t = fmaf(-l, pseg[k], tile[(jj + k) * per + li]);
-            tile[(jj + k) * per + li] = t;
-            if (k == 1 && better(fabsf(t), i, best, bi)) {
-              best = fabsf(t);
-              bi = i;
-            }
-          }
-        } else if (w > 1 && better(fabsf(tile[(jj + 1) * per + li]), i, best, bi)) {
-          best = fabsf(tile[(jj + 1) * per + li]);
+          const float l = t[0] * inv;
+          t[0] = l;
+#pragma unroll
+          for (int k = 1; k < CP_IB; k++)
+            if (k < w) t[k] = fmaf(-l, ps[k], t[k]);
+        }
+        if (w > 1 && better(fabsf(t[1]), i, best, bi)) {
+          best = fabsf(t[1]);
           bi = i;
         }
+#pragma unroll
+        for (int k = 0; k < CP_IB; k++)
+          if (k < w) tile[(jj + k) * per + li] = t[k];
       }
       // the swapped rows' other columns, from the owners' shared memory
       if (gi != j) {
