@@ -898,18 +898,19 @@ __global__ void __launch_bounds__(GP_THREADS) panel_grid_kernel(T* __restrict__ 
 // ---- panel on one 16-CTA cluster (FP32 factors) --------------------------
 // The same algorithm as panel_grid_kernel with the exchange in distributed
 // shared memory: CTA r of the cluster keeps rows [j0 + r*per, ...) of the
-// panel in its shared memory.  Per column, one block barrier and one cluster
-// barrier:
+// panel in its shared memory, row by row (stride cp_row_stride(jb) floats,
+// so that a row's 16-column inner block is four aligned 128-bit words and
+// eight consecutive rows hit distinct banks).  Per column, one block
+// barrier and one cluster barrier:
 //  - every thread already holds its best candidate for the column (found
 //    while updating it in the previous column step); a warp reduction and
 //    one block barrier give the CTA's candidate;
-//  - warp 0 pushes (value, row, the row's inner-block segment) into every
-//    CTA's receive slot, and warp 1 of the owner of row j pushes row j's
-//    segment; the CTA keeps its candidate's full row and row j locally;
-//  - after the cluster barrier every thread picks the winner from its own
-//    receive slot (same order everywhere), and the owner threads of rows j
-//    and gi swap the inner-block segments; each thread then scales column
-//    j, updates its rows in the inner block's columns and tracks its
+//  - warp 0 pushes (value, row, the row's inner block) into every CTA's
+//    receive slot, and warp 1 of the owner of row j pushes row j's inner
+//    block; the CTA keeps its candidate's full row and row j locally;
+//  - after the cluster barrier every warp picks the winner from its own
+//    receive slot (same order everywhere); each thread then swaps, scales
+//    and updates the inner block of its rows in registers and tracks its
 //    candidate for column j + 1, all in one pass;
 //  - the other columns of the two swapped rows are fetched from the owners'
 //    shared memory off the critical path (they are read again only after
@@ -923,11 +924,15 @@ constexpr int CP_WARPS = CP_THREADS / 32;
 constexpr size_t CP_MAX_SMEM = 212 * 1024;
 constexpr int CP_IB = 16;  // inner block: columns updated per column step
 
+// Row stride (floats) of the panel in shared memory: whole 16-column inner
+// blocks plus 4, i.e. an odd number of 16-byte words.
+__host__ __device__ constexpr int cp_row_stride(int jb) { return ((jb + 15) / 16) * 16 + 4; }
+
 struct CpSlot {
-  float seg[CP_CL][CP_IB];  // candidate row segments [jj, be), by source CTA
-  float v[CP_CL];           // candidate |values|, by source CTA
-  int i[CP_CL];             // candidate rows (N: none), by source CTA
-  float jseg[CP_IB];        // row j's segment [jj, be)
+  float4 seg[CP_CL][CP_IB / 4];  // candidate rows' inner blocks, by source CTA
+  float4 jseg[CP_IB / 4];        // row j's inner block
+  float v[CP_CL];                // candidate |values|, by source CTA
+  int i[CP_CL];                  // candidate rows (N: none), by source CTA
 };
 
 __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __restrict__ A, long long ld, int N,
@@ -937,13 +942,14 @@ __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __re
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   extern __shared__ __align__(16) unsigned char cp_raw[];
-  float* tile = reinterpret_cast<float*>(cp_raw);  // tile[k * per + r]
-  __shared__ float cand_row[2][128];
-  __shared__ float jrow[2][128];
-  __shared__ CpSlot recv[2];
-  __shared__ float ublk[CP_IB][128];  // rows of the current inner block (L11 | A12 -> U12)
+  float* tile = reinterpret_cast<float*>(cp_raw);  // tile[r * S + k]
+  __shared__ __align__(16) float cand_row[2][128];
+  __shared__ __align__(16) float jrow[2][128];
+  __shared__ __align__(16) CpSlot recv[2];
+  __shared__ __align__(16) float ublk[CP_IB][128];  // rows of the current inner block (L11 | A12 -> U12)
   __shared__ float wv[CP_WARPS];
   __shared__ int wi[CP_WARPS];
+  const int S = cp_row_stride(jb);
   const int rank = static_cast<int>(cluster.block_rank());
   const int tid = threadIdx.x, bd = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5;
@@ -952,18 +958,19 @@ __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __re
   const int nr = r1 > r0 ? r1 - r0 : 0;
   for (int e = tid; e < jb * nr; e += bd) {
     int k = e / nr, r = e % nr;
-    tile[k * per + r] = A[static_cast<long long>(j0 + k) * ld + r0 + r];
+    tile[r * S + k] = A[static_cast<long long>(j0 + k) * ld + r0 + r];
   }
   __syncthreads();
   for (int b0 = 0; b0 < jb; b0 += CP_IB) {
     const int be = (b0 + CP_IB < jb) ? b0 + CP_IB : jb;
+    const int nb = be - b0;
     // this thread's candidate for the block's first column
     float best = -1.0f;
     int bi = N;
     for (int li = tid; li < nr; li += bd) {
       const int i = r0 + li;
       if (i < j0 + b0) continue;
-      const float v = fabsf(tile[b0 * per + li]);
+      const float v = fabsf(tile[li * S + b0]);
       if (better(v, i, best, bi)) {
         best = v;
         bi = i;
@@ -972,7 +979,7 @@ __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __re
     for (int jj = b0; jj < be; jj++) {
       const int j = j0 + jj;
       const int slot = jj & 1;
-      const int w = be - jj;  // segment [jj, be)
+      const int q0 = jj - b0;  // column jj within the inner block
       for (int o = 16; o > 0; o >>= 1) {
         const float ov = __shfl_xor_sync(0xffffffffu, best, o);
         const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
@@ -997,18 +1004,25 @@ __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __re
             ci = oi;
           }
         }
+        const int crow = (ci < N) ? ci - r0 : 0;  // row 0's words stand in when there is no candidate
         if (ci < N)
-          for (int k = lane; k < jb; k += 32) cand_row[slot][k] = tile[k * per + ci - r0];
+          for (int k = lane; k < jb; k += 32) cand_row[slot][k] = tile[crow * S + k];
         CpSlot* R = cluster.map_shared_rank(&recv[slot], lane & (CP_CL - 1));
         if (lane < CP_CL) {
           R->v[rank] = cv;
           R->i[rank] = ci;
         }
-        for (int k = lane >> 4; k < w; k += 2) R->seg[rank][k] = (ci < N) ? tile[(jj + k) * per + ci - r0] : 0.0f;
+        const float4* src = reinterpret_cast<const float4*>(tile + static_cast<size_t>(crow) * S + b0);
+        const int c0 = (lane >> 4) * 2;
+        R->seg[rank][c0] = src[c0];
+        R->seg[rank][c0 + 1] = src[c0 + 1];
       } else if (warp == 1 && j >= r0 && j < r1) {
-        for (int k = lane; k < jb; k += 32) jrow[slot][k] = tile[k * per + j - r0];
+        for (int k = lane; k < jb; k += 32) jrow[slot][k] = tile[(j - r0) * S + k];
         CpSlot* R = cluster.map_shared_rank(&recv[slot], lane & (CP_CL - 1));
-        for (int k = lane >> 4; k < w; k += 2) R->jseg[k] = tile[(jj + k) * per + j - r0];
+        const float4* src = reinterpret_cast<const float4*>(tile + static_cast<size_t>(j - r0) * S + b0);
+        const int c0 = (lane >> 4) * 2;
+        R->jseg[c0] = src[c0];
+        R->jseg[c0 + 1] = src[c0 + 1];
       }
       cluster.sync();
       // the winner, from this CTA's own receive slot: every warp reduces the
@@ -1038,55 +1052,77 @@ __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __re
         ipiv[j] = gi;
         if (!(gv > 0.0f) && *info == 0) *info = j + 1;  // zero (or NaN) pivot
       }
-      const float* pseg = (tag >= 0) ? recv[slot].seg[tag] : recv[slot].jseg;  // pivot row segment
-      const float* jseg = recv[slot].jseg;
-      const float piv = pseg[0];
+      // the pivot row's inner block
+      const float4* p4 = (tag >= 0) ? recv[slot].seg[tag] : recv[slot].jseg;
+      float ps[CP_IB];
+#pragma unroll
+      for (int c = 0; c < CP_IB / 4; c++) {
+        const float4 x = p4[c];
+        ps[4 * c] = x.x;
+        ps[4 * c + 1] = x.y;
+        ps[4 * c + 2] = x.z;
+        ps[4 * c + 3] = x.w;
+      }
+      float piv = ps[0];
+#pragma unroll
+      for (int q = 1; q < CP_IB; q++)
+        if (q == q0) piv = ps[q];
       const float inv = (piv != 0.0f) ? 1.0f / piv : 0.0f;
       best = -1.0f;
       bi = N;
-      float ps[CP_IB];
-#pragma unroll
-      for (int k = 0; k < CP_IB; k++) ps[k] = (k < w) ? pseg[k] : 0.0f;
       for (int li = tid; li < nr; li += bd) {
         const int i = r0 + li;
-        if (i == j) {  // row j becomes the pivot row (inner-block segment)
+        if (i < j) continue;
+        float4* row = reinterpret_cast<float4*>(tile + static_cast<size_t>(li) * S + b0);
+        if (i == j) {  // row j becomes the pivot row (inner block)
 #pragma unroll
-          for (int k = 0; k < CP_IB; k++)
-            if (k < w) tile[(jj + k) * per + li] = ps[k];
+          for (int c = 0; c < CP_IB / 4; c++) row[c] = make_float4(ps[4 * c], ps[4 * c + 1], ps[4 * c + 2], ps[4 * c + 3]);
           continue;
         }
-        if (i < j) continue;
-        // the row's inner-block segment in registers (row gi takes row j's)
+        // the row's inner block in registers (row gi takes row j's)
+        const float4* in = (i == gi) ? recv[slot].jseg : row;
         float t[CP_IB];
 #pragma unroll
-        for (int k = 0; k < CP_IB; k++)
-          if (k < w) t[k] = (i == gi) ? jseg[k] : tile[(jj + k) * per + li];
+        for (int c = 0; c < CP_IB / 4; c++) {
+          const float4 x = in[c];
+          t[4 * c] = x.x;
+          t[4 * c + 1] = x.y;
+          t[4 * c + 2] = x.z;
+          t[4 * c + 3] = x.w;
+        }
         if (piv != 0.0f) {
-          const float l = t[0] * inv;
-          t[0] = l;
+          float l = t[0];
 #pragma unroll
-          for (int k = 1; k < CP_IB; k++)
-            if (k < w) t[k] = fmaf(-l, ps[k], t[k]);
+          for (int q = 1; q < CP_IB; q++)
+            if (q == q0) l = t[q];
+          l *= inv;
+#pragma unroll
+          for (int q = 0; q < CP_IB; q++) t[q] = (q == q0) ? l : ((q > q0) ? fmaf(-l, ps[q], t[q]) : t[q]);
         }
-        if (w > 1 && better(fabsf(t[1]), i, best, bi)) {
-          best = fabsf(t[1]);
-          bi = i;
+        if (q0 + 1 < nb) {
+          float nxt = t[0];
+#pragma unroll
+          for (int q = 1; q < CP_IB; q++)
+            if (q == q0 + 1) nxt = t[q];
+          if (better(fabsf(nxt), i, best, bi)) {
+            best = fabsf(nxt);
+            bi = i;
+          }
         }
 #pragma unroll
-        for (int k = 0; k < CP_IB; k++)
-          if (k < w) tile[(jj + k) * per + li] = t[k];
+        for (int c = 0; c < CP_IB / 4; c++) row[c] = make_float4(t[4 * c], t[4 * c + 1], t[4 * c + 2], t[4 * c + 3]);
       }
       // the swapped rows' other columns, from the owners' shared memory
       if (gi != j) {
         if (gi >= r0 && gi < r1) {
           const float* src = cluster.map_shared_rank(&jrow[slot][0], (j - j0) / per);
           for (int k = tid; k < jb; k += bd)
-            if (k < jj || k >= be) tile[k * per + gi - r0] = src[k];
+            if (k < b0 || k >= be) tile[(gi - r0) * S + k] = src[k];
         }
         if (j >= r0 && j < r1) {
           const float* src = cluster.map_shared_rank(&cand_row[slot][0], tag);
           for (int k = tid; k < jb; k += bd)
-            if (k < jj || k >= be) tile[k * per + j - r0] = src[k];
+            if (k < b0 || k >= be) tile[(j - r0) * S + k] = src[k];
         }
       }
     }
@@ -1094,48 +1130,57 @@ __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __re
       // Rows j0+b0 .. j0+be-1 are final in columns b0..be-1 (L11 below the
       // diagonal); every CTA fetches them whole and forms
       // U12 = L11^{-1} A12 for columns be..jb-1.
-      const int nbr = be - b0;
       cluster.sync();
-      for (int e = tid; e < nbr * jb; e += bd) {
+      for (int e = tid; e < nb * jb; e += bd) {
         const int t = e / jb, k = e % jb;
         const int row = j0 + b0 + t;
         const int owner = (row - j0) / per;
         const float* ot = cluster.map_shared_rank(tile, owner);
-        ublk[t][k] = ot[static_cast<long long>(k) * per + (row - (j0 + owner * per))];
+        ublk[t][k] = ot[static_cast<long long>(row - (j0 + owner * per)) * S + k];
       }
       __syncthreads();
       for (int k = be + tid; k < jb; k += bd)  // one column of U12 per thread
-        for (int t = 1; t < nbr; t++) {
+        for (int t = 1; t < nb; t++) {
           float acc = ublk[t][k];
           for (int q = 0; q < t; q++) acc = fmaf(-ublk[t][b0 + q], ublk[q][k], acc);
           ublk[t][k] = acc;
         }
       cluster.sync();  // remote reads of the block rows are done
-      // owners store U12; rows below the block get the rank-nbr update
-      for (int e = tid; e < nbr * (jb - be); e += bd) {
+      // owners store U12; rows below the block get the rank-16 update, one
+      // row per thread with its 16 multipliers in registers and four
+      // columns per step
+      for (int e = tid; e < nb * (jb - be); e += bd) {
         const int t = e / (jb - be), k = be + e % (jb - be);
         const int row = j0 + b0 + t;
-        if (row >= r0 && row < r1) tile[k * per + row - r0] = ublk[t][k];
+        if (row >= r0 && row < r1) tile[(row - r0) * S + k] = ublk[t][k];
       }
       const int rs = (r0 > j0 + be) ? r0 : j0 + be;
-      if (rs < r1) {
-        const int nrr = r1 - rs;
-        const int nph = bd >> 7, ph = tid >> 7;
-        for (int i0 = 0; i0 < nrr; i0 += 128) {
-          const int ii = i0 + (tid & 127);
-          if (ii < nrr) {
-            const int li = rs - r0 + ii;
-            // (inside this branch the block is full: nbr == CP_IB)
-            float l[CP_IB];
+      for (int i = rs + tid; i < r1; i += bd) {
+        const int li = i - r0;
+        const float4* lrow = reinterpret_cast<const float4*>(tile + static_cast<size_t>(li) * S + b0);
+        float l[CP_IB];
 #pragma unroll
-            for (int q = 0; q < CP_IB; q++) l[q] = tile[(b0 + q) * per + li];
-            for (int k = be + ph; k < jb; k += nph) {
-              float acc = tile[k * per + li];
+        for (int c = 0; c < CP_IB / 4; c++) {
+          const float4 x = lrow[c];
+          l[4 * c] = x.x;
+          l[4 * c + 1] = x.y;
+          l[4 * c + 2] = x.z;
+          l[4 * c + 3] = x.w;
+        }
+        float4* arow = reinterpret_cast<float4*>(tile + static_cast<size_t>(li) * S);
+        // (inside this branch the block is full: nb == CP_IB; columns past
+        // jb up to the stride are padding, updated but never read)
+        for (int k4 = be / 4; k4 < (jb + 3) / 4; k4++) {
+          float4 acc = arow[k4];
 #pragma unroll
-              for (int q = 0; q < CP_IB; q++) acc = fmaf(-l[q], ublk[q][k], acc);
-              tile[k * per + li] = acc;
-            }
+          for (int q = 0; q < CP_IB; q++) {
+            const float4 u = *reinterpret_cast<const float4*>(&ublk[q][4 * k4]);
+            acc.x = fmaf(-l[q], u.x, acc.x);
+            acc.y = fmaf(-l[q], u.y, acc.y);
+            acc.z = fmaf(-l[q], u.z, acc.z);
+            acc.w = fmaf(-l[q], u.w, acc.w);
           }
+          arow[k4] = acc;
         }
       }
       __syncthreads();
@@ -1144,7 +1189,7 @@ __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __re
   __syncthreads();
   for (int e = tid; e < jb * nr; e += bd) {
     int k = e / nr, r = e % nr;
-    A[static_cast<long long>(j0 + k) * ld + r0 + r] = tile[k * per + r];
+    A[static_cast<long long>(j0 + k) * ld + r0 + r] = tile[r * S + k];
   }
   cluster.sync();  // remote readers of this CTA's shared memory are done
 }
@@ -1154,7 +1199,7 @@ __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __re
 static int cluster_panel_width(int rows) {
   const int per = (rows + CP_CL - 1) / CP_CL;
   for (int w : {96, 64, 32})
-    if (static_cast<size_t>(per) * w * sizeof(float) <= CP_MAX_SMEM) return w;
+    if (static_cast<size_t>(per) * cp_row_stride(w) * sizeof(float) <= CP_MAX_SMEM) return w;
   return 0;
 }
 
@@ -1163,7 +1208,7 @@ static int cluster_panel_width(int rows) {
 static bool panel_cluster16(Context* ctx, float* A, long long ld, int N, int j0, int jb, int* ipiv, int* info) {
   const int rows = N - j0;
   const int per = (rows + CP_CL - 1) / CP_CL;
-  const size_t smem = static_cast<size_t>(per) * jb * sizeof(float);
+  const size_t smem = static_cast<size_t>(per) * cp_row_stride(jb) * sizeof(float);
   if (smem > CP_MAX_SMEM) return false;
   static int usable = 0;
   static std::once_flag probe;
