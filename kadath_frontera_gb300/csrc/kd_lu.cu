@@ -935,6 +935,58 @@ struct CpSlot {
   int i[CP_CL];                  // candidate rows (N: none), by source CTA
 };
 
+// One column step on this thread's rows of the inner block, for column Q0
+// of the block: swap (row j <- pivot row, row gi <- row j), scale column
+// Q0, update columns Q0+1..15, and the thread's candidate for column Q0+1.
+// Q0 is a template parameter so that the column selections cost nothing.
+template <int Q0>
+__device__ __forceinline__ void cp_column_step(float* __restrict__ tile, int S, int b0, int r0, int nr, int j, int gi,
+                                               int nb, const float (&ps)[CP_IB], const float4* jseg4, float inv,
+                                               bool nonzero, int N, float& best, int& bi) {
+  best = -1.0f;
+  bi = N;
+  for (int li = threadIdx.x; li < nr; li += blockDim.x) {
+    const int i = r0 + li;
+    if (i < j) continue;
+    float4* row = reinterpret_cast<float4*>(tile + static_cast<size_t>(li) * S + b0);
+    if (i == j) {  // row j becomes the pivot row (inner block)
+#pragma unroll
+      for (int c = 0; c < CP_IB / 4; c++) row[c] = make_float4(ps[4 * c], ps[4 * c + 1], ps[4 * c + 2], ps[4 * c + 3]);
+      continue;
+    }
+    // the row's inner block in registers (row gi takes row j's)
+    const float4* in = (i == gi) ? jseg4 : row;
+    float t[CP_IB];
+#pragma unroll
+    for (int c = 0; c < CP_IB / 4; c++) {
+      const float4 x = in[c];
+      t[4 * c] = x.x;
+      t[4 * c + 1] = x.y;
+      t[4 * c + 2] = x.z;
+      t[4 * c + 3] = x.w;
+    }
+    if (nonzero) {
+      const float l = t[Q0] * inv;
+      t[Q0] = l;
+#pragma unroll
+      for (int q = Q0 + 1; q < CP_IB; q++) t[q] = fmaf(-l, ps[q], t[q]);
+    }
+    if (Q0 + 1 < CP_IB && Q0 + 1 < nb) {
+      const float v = fabsf(t[(Q0 + 1) % CP_IB]);
+      if (better(v, i, best, bi)) {
+        best = v;
+        bi = i;
+      }
+    }
+    // columns before Q0 only change in the swapped rows
+    constexpr int cfirst = Q0 / 4;
+    const int cstart = (i == gi) ? 0 : cfirst;
+#pragma unroll
+    for (int c = 0; c < CP_IB / 4; c++)
+      if (c >= cstart) row[c] = make_float4(t[4 * c], t[4 * c + 1], t[4 * c + 2], t[4 * c + 3]);
+  }
+}
+
 __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __restrict__ A, long long ld, int N,
                                                                      int j0, int jb, int per,
                                                                      int* __restrict__ ipiv,
@@ -1068,49 +1120,15 @@ __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __re
       for (int q = 1; q < CP_IB; q++)
         if (q == q0) piv = ps[q];
       const float inv = (piv != 0.0f) ? 1.0f / piv : 0.0f;
-      best = -1.0f;
-      bi = N;
-      for (int li = tid; li < nr; li += bd) {
-        const int i = r0 + li;
-        if (i < j) continue;
-        float4* row = reinterpret_cast<float4*>(tile + static_cast<size_t>(li) * S + b0);
-        if (i == j) {  // row j becomes the pivot row (inner block)
-#pragma unroll
-          for (int c = 0; c < CP_IB / 4; c++) row[c] = make_float4(ps[4 * c], ps[4 * c + 1], ps[4 * c + 2], ps[4 * c + 3]);
-          continue;
-        }
-        // the row's inner block in registers (row gi takes row j's)
-        const float4* in = (i == gi) ? recv[slot].jseg : row;
-        float t[CP_IB];
-#pragma unroll
-        for (int c = 0; c < CP_IB / 4; c++) {
-          const float4 x = in[c];
-          t[4 * c] = x.x;
-          t[4 * c + 1] = x.y;
-          t[4 * c + 2] = x.z;
-          t[4 * c + 3] = x.w;
-        }
-        if (piv != 0.0f) {
-          float l = t[0];
-#pragma unroll
-          for (int q = 1; q < CP_IB; q++)
-            if (q == q0) l = t[q];
-          l *= inv;
-#pragma unroll
-          for (int q = 0; q < CP_IB; q++) t[q] = (q == q0) ? l : ((q > q0) ? fmaf(-l, ps[q], t[q]) : t[q]);
-        }
-        if (q0 + 1 < nb) {
-          float nxt = t[0];
-#pragma unroll
-          for (int q = 1; q < CP_IB; q++)
-            if (q == q0 + 1) nxt = t[q];
-          if (better(fabsf(nxt), i, best, bi)) {
-            best = fabsf(nxt);
-            bi = i;
-          }
-        }
-#pragma unroll
-        for (int c = 0; c < CP_IB / 4; c++) row[c] = make_float4(t[4 * c], t[4 * c + 1], t[4 * c + 2], t[4 * c + 3]);
+      const float4* jseg4 = recv[slot].jseg;
+      switch (q0) {
+#define KD_CP_CASE(Q) \
+  case Q: cp_column_step<Q>(tile, S, b0, r0, nr, j, gi, nb, ps, jseg4, inv, piv != 0.0f, N, best, bi); break;
+        KD_CP_CASE(0) KD_CP_CASE(1) KD_CP_CASE(2) KD_CP_CASE(3) KD_CP_CASE(4) KD_CP_CASE(5) KD_CP_CASE(6)
+        KD_CP_CASE(7) KD_CP_CASE(8) KD_CP_CASE(9) KD_CP_CASE(10) KD_CP_CASE(11) KD_CP_CASE(12) KD_CP_CASE(13)
+        KD_CP_CASE(14) KD_CP_CASE(15)
+#undef KD_CP_CASE
+        default: break;
       }
       // the swapped rows' other columns, from the owners' shared memory
       if (gi != j) {
