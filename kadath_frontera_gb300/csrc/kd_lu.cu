@@ -401,6 +401,8 @@ DenseLU::~DenseLU() {
   cudaFree(work32_);
   cudaFree(dinv_l_);
   cudaFree(dinv_u_);
+  cudaFree(dinv2_l_);
+  cudaFree(dinv2_u_);
   cudaFree(perm_);
   cudaFree(tri_work_);
 }
@@ -676,20 +678,64 @@ __device__ __forceinline__ SweepStep sweep_step(int step, int nblk, int N, int l
 // barrier, since they do not depend on b.
 template <class T>
 struct SweepPrefetch {
-  double lo[8], hi[8];
+  double lo[8], hi[8];  // Dinv_k entries (FP64 factors)
+  float2 dlo[8], dhi[8];  // Dinv_k entries as (hi, lo) FP32 pairs (FP32 factors)
   T va[16], vb[16];
 };
 
+// Double-float arithmetic (a value is an unevaluated sum hi + lo of two
+// floats): Dekker's product with a fused multiply-add and Knuth's two-sum,
+// about 48 significant bits on the FP32 pipe.
+struct DF {
+  float h, l;
+};
+__device__ __forceinline__ DF df_mul(float ah, float al, float bh, float bl) {
+  const float p = ah * bh;
+  float e = fmaf(ah, bh, -p);
+  e = fmaf(ah, bl, fmaf(al, bh, e));
+  const float s = p + e;
+  return {s, e - (s - p)};
+}
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+  const float s = a.h + b.h;
+  const float v = s - a.h;
+  float e = (a.h - (s - v)) + (b.h - v);
+  e += a.l + b.l;
+  const float r = s + e;
+  return {r, e - (r - s)};
+}
+
+// FP64 inverse blocks as (hi, lo) FP32 pairs: hi = fl32(d), lo = fl32(d - hi).
+__global__ void split_df_kernel(const double* __restrict__ d, float2* __restrict__ out, long long n) {
+  for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < n;
+       t += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const double v = d[t];
+    const float h = static_cast<float>(v);
+    out[t] = make_float2(h, static_cast<float>(v - static_cast<double>(h)));
+  }
+}
+
 template <class T>
 __device__ __forceinline__ void sweep_prefetch(const T* __restrict__ A, long long ld, const double* __restrict__ Dinv,
-                                               const SweepStep& s, SweepPrefetch<T>& pf) {
+                                               const float2* __restrict__ Dinv2, const SweepStep& s,
+                                               SweepPrefetch<T>& pf) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int quarter = warp & 3, half = warp >> 2;
-  const double* D = Dinv + static_cast<size_t>(s.k) * TB * TB + static_cast<size_t>(warp) * 8 * TB;
+  const size_t dofs = static_cast<size_t>(s.k) * TB * TB + static_cast<size_t>(warp) * 8 * TB;
+  if constexpr (std::is_same<T, float>::value) {
+    const float2* D = Dinv2 + dofs;
 #pragma unroll
-  for (int q = 0; q < 8; q++) {
-    pf.lo[q] = D[q * TB + lane];
-    pf.hi[q] = D[q * TB + lane + 32];
+    for (int q = 0; q < 8; q++) {
+      pf.dlo[q] = D[q * TB + lane];
+      pf.dhi[q] = D[q * TB + lane + 32];
+    }
+  } else {
+    const double* D = Dinv + dofs;
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      pf.lo[q] = D[q * TB + lane];
+      pf.hi[q] = D[q * TB + lane + 32];
+    }
   }
   const int c0 = quarter * 16;
   {
@@ -724,10 +770,14 @@ __device__ __forceinline__ void sweep_prefetch(const T* __restrict__ A, long lon
 template <class T>
 __global__ void __launch_bounds__(256) trsv_sweep(const T* __restrict__ A, long long ld, int N, double* b,
                                                   double* __restrict__ y, const double* __restrict__ Dinv,
-                                                  int lower, unsigned* bar, int* err) {
-  // x_k = Dinv_k b in FP64 (an explicit inverse amplifies rounding by its
-  // condition number); the row updates in the factors' precision T
+                                                  const float2* __restrict__ Dinv2, int lower, unsigned* bar,
+                                                  int* err) {
+  // x_k = Dinv_k b in FP64, or in double-float with FP32 factors (an
+  // explicit inverse amplifies rounding by its condition number, so a plain
+  // FP32 product would cost refinement iterations); the row updates in the
+  // factors' precision T
   __shared__ double bb[TB];
+  __shared__ float bh[TB], bl[TB];
   __shared__ double xx[TB];
   __shared__ T xt[TB];
   __shared__ T part[4][SW_TILE];
@@ -737,12 +787,35 @@ __global__ void __launch_bounds__(256) trsv_sweep(const T* __restrict__ A, long 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int quarter = warp & 3, half = warp >> 2;
   SweepPrefetch<T> pf;
-  sweep_prefetch(A, ld, Dinv, sweep_step(0, nblk, N, lower, ntiles), pf);
+  sweep_prefetch(A, ld, Dinv, Dinv2, sweep_step(0, nblk, N, lower, ntiles), pf);
   for (int step = 0; step < nblk; step++) {
     const SweepStep s = sweep_step(step, nblk, N, lower, ntiles);
-    if (tid < TB) bb[tid] = (tid < s.n) ? __ldcg(b + s.r0 + tid) : 0.0;
+    if (tid < TB) {
+      const double v = (tid < s.n) ? __ldcg(b + s.r0 + tid) : 0.0;
+      bb[tid] = v;
+      const float h = static_cast<float>(v);
+      bh[tid] = h;
+      bl[tid] = static_cast<float>(v - static_cast<double>(h));
+    }
     __syncthreads();
-    {
+    if constexpr (std::is_same<T, float>::value) {
+      const float b0h = bh[lane], b0l = bl[lane], b1h = bh[lane + 32], b1l = bl[lane + 32];
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        DF p = df_add(df_mul(pf.dlo[q].x, pf.dlo[q].y, b0h, b0l), df_mul(pf.dhi[q].x, pf.dhi[q].y, b1h, b1l));
+        for (int o = 16; o > 0; o >>= 1) {
+          DF r;
+          r.h = __shfl_xor_sync(0xffffffffu, p.h, o);
+          r.l = __shfl_xor_sync(0xffffffffu, p.l, o);
+          p = df_add(p, r);
+        }
+        if (lane == 0) {
+          const double x = static_cast<double>(p.h) + static_cast<double>(p.l);
+          xx[warp * 8 + q] = x;
+          xt[warp * 8 + q] = static_cast<T>(x);
+        }
+      }
+    } else {
       const double b0 = bb[lane], b1 = bb[lane + 32];
 #pragma unroll
       for (int q = 0; q < 8; q++) {
@@ -784,7 +857,7 @@ __global__ void __launch_bounds__(256) trsv_sweep(const T* __restrict__ A, long 
       }
       __syncthreads();
     }
-    if (step + 1 < nblk) sweep_prefetch(A, ld, Dinv, sweep_step(step + 1, nblk, N, lower, ntiles), pf);
+    if (step + 1 < nblk) sweep_prefetch(A, ld, Dinv, Dinv2, sweep_step(step + 1, nblk, N, lower, ntiles), pf);
     if (!grid_barrier(bar, gridDim.x * static_cast<unsigned>(step + 1), err, &s_ok)) return;
   }
 }
@@ -1608,9 +1681,11 @@ void DenseLU::tri_solve(const T* LU, long long ld, int N, double* b, int trans) 
     cuda_check(cudaMemsetAsync(tri_bar_, 0, 2 * sizeof(unsigned), s), "memset sweep barriers");
     const double* dl = dinv_l_;
     const double* du = dinv_u_;
-    cuda_check(cudaLaunchKernelEx(&cfg, trsv_sweep<T>, LU, ld, N, w1, w2, dl, 1, tri_bar_, panel_err_),
+    const float2* dl2 = std::is_same<T, float>::value ? dinv2_l_ : nullptr;
+    const float2* du2 = std::is_same<T, float>::value ? dinv2_u_ : nullptr;
+    cuda_check(cudaLaunchKernelEx(&cfg, trsv_sweep<T>, LU, ld, N, w1, w2, dl, dl2, 1, tri_bar_, panel_err_),
                "forward sweep");
-    cuda_check(cudaLaunchKernelEx(&cfg, trsv_sweep<T>, LU, ld, N, w2, b, du, 0, tri_bar_ + 1, panel_err_),
+    cuda_check(cudaLaunchKernelEx(&cfg, trsv_sweep<T>, LU, ld, N, w2, b, du, du2, 0, tri_bar_ + 1, panel_err_),
                "backward sweep");
     ctx_->launches += 3;
     cuda_check(cudaGetLastError(), "triangular solve");
@@ -1665,6 +1740,11 @@ void DenseLU::prepare_solves(const T* LU, long long ld, int N) {
     cudaFree(dinv_u_);
     cuda_check(cudaMalloc(&dinv_l_, need * sizeof(double)), "cudaMalloc(Linv)");
     cuda_check(cudaMalloc(&dinv_u_, need * sizeof(double)), "cudaMalloc(Uinv)");
+    cudaFree(dinv2_l_);
+    cudaFree(dinv2_u_);
+    dinv2_l_ = dinv2_u_ = nullptr;
+    cuda_check(cudaMalloc(&dinv2_l_, need * sizeof(float2)), "cudaMalloc(Linv pairs)");
+    cuda_check(cudaMalloc(&dinv2_u_, need * sizeof(float2)), "cudaMalloc(Uinv pairs)");
     dinv_cap_ = need;
   }
   if (static_cast<size_t>(N) > perm_cap_) {
@@ -1682,6 +1762,12 @@ void DenseLU::prepare_solves(const T* LU, long long ld, int N) {
     cudaFuncSetAttribute(invert_diag_blocks<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   });
   invert_diag_blocks<T><<<nblk, TB, smem, s>>>(LU, ld, N, dinv_l_, dinv_u_);
+  if constexpr (std::is_same<T, float>::value) {
+    const long long n2 = static_cast<long long>(nblk) * TB * TB;
+    split_df_kernel<<<blocks(n2, 256) < 152 * 8 ? blocks(n2, 256) : 152 * 8, 256, 0, s>>>(dinv_l_, dinv2_l_, n2);
+    split_df_kernel<<<blocks(n2, 256) < 152 * 8 ? blocks(n2, 256) : 152 * 8, 256, 0, s>>>(dinv_u_, dinv2_u_, n2);
+    ctx_->launches += 2;
+  }
   ctx_->launches += 2;
   cuda_check(cudaGetLastError(), "solve preparation");
 }

@@ -91,6 +91,8 @@ class DenseLU {
   void prepare_solves(const T* LU, long long ld, int N);
   double* dinv_l_ = nullptr;  // inverses of the 64 x 64 diagonal blocks
   double* dinv_u_ = nullptr;
+  float2* dinv2_l_ = nullptr;  // the same as (hi, lo) FP32 pairs (sweeps with FP32 factors)
+  float2* dinv2_u_ = nullptr;
   size_t dinv_cap_ = 0;
   int* perm_ = nullptr;       // pivots as one permutation
   double* tri_work_ = nullptr;
