@@ -968,6 +968,68 @@ __global__ void __launch_bounds__(GP_THREADS) panel_grid_kernel(T* __restrict__ 
   }
 }
 
+// The row exchanges of one panel (pivots piv[0 .. jb), rows j0 .. ) as a
+// list of moves row dst[t] <- row src[t] over the rows they touch (at most
+// 2 jb): rows j0 .. j0+jb-1 first, then the pivot rows below the panel.
+// One warp; piv, rows (2 jb), content (2 jb) and cnt in shared memory.
+// map[0] = count, map[1 .. 1+2jb) = dst, map[1+2jb .. 1+4jb) = src.
+__device__ void swap_map_warp(const int* piv, int j0, int jb, int* __restrict__ map, int* rows, int* content,
+                              int* cnt_s) {
+  const int lane = threadIdx.x & 31;
+  for (int t = lane; t < jb; t += 32) {
+    rows[t] = j0 + t;
+    content[t] = j0 + t;
+  }
+  if (lane == 0) *cnt_s = jb;
+  __syncwarp();
+  for (int jj = 0; jj < jb; jj++) {
+    const int p = piv[jj];
+    const int cnt = *cnt_s;
+    int idx;
+    if (p < j0 + jb) {
+      idx = p - j0;
+    } else {
+      idx = -1;
+      for (int t0 = jb; t0 < cnt; t0 += 32) {
+        unsigned m = __ballot_sync(0xffffffffu, t0 + lane < cnt && rows[t0 + lane] == p);
+        if (m) {
+          idx = t0 + __ffs(m) - 1;
+          break;
+        }
+      }
+      if (idx < 0) {
+        idx = cnt;
+        if (lane == 0) {
+          rows[idx] = p;
+          content[idx] = p;
+        }
+      }
+    }
+    __syncwarp();
+    if (lane == 0) {
+      if (idx == cnt) *cnt_s = cnt + 1;
+      int t = content[jj];
+      content[jj] = content[idx];
+      content[idx] = t;
+    }
+    __syncwarp();
+  }
+  const int n = *cnt_s;
+  for (int t = lane; t < n; t += 32) {
+    map[1 + t] = rows[t];
+    map[1 + 2 * jb + t] = content[t];
+  }
+  if (lane == 0) map[0] = n;
+}
+
+__global__ void build_swap_map(const int* __restrict__ ipiv, int j0, int jb, int* __restrict__ map) {
+  __shared__ int rows[256], content[256], piv[128];
+  __shared__ int cnt;
+  for (int t = threadIdx.x; t < jb; t += 32) piv[t] = ipiv[j0 + t];
+  __syncwarp();
+  swap_map_warp(piv, j0, jb, map, rows, content, &cnt);
+}
+
 // ---- panel on one 16-CTA cluster (FP32 factors) --------------------------
 // The same algorithm as panel_grid_kernel with the exchange in distributed
 // shared memory: CTA r of the cluster keeps rows [j0 + r*per, ...) of the
@@ -1063,11 +1125,13 @@ __device__ __forceinline__ void cp_column_step(float* __restrict__ tile, int S, 
 __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __restrict__ A, long long ld, int N,
                                                                      int j0, int jb, int per,
                                                                      int* __restrict__ ipiv,
-                                                                     int* __restrict__ info) {
+                                                                     int* __restrict__ info,
+                                                                     int* __restrict__ swap_map) {
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   extern __shared__ __align__(16) unsigned char cp_raw[];
   float* tile = reinterpret_cast<float*>(cp_raw);  // tile[r * S + k]
+  __shared__ int pivs[128];  // the panel's pivots (CTA 0)
   __shared__ __align__(16) float cand_row[2][128];
   __shared__ __align__(16) float jrow[2][128];
   __shared__ __align__(16) CpSlot recv[2];
@@ -1175,6 +1239,7 @@ __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __re
       }
       if (rank == 0 && tid == 0) {
         ipiv[j] = gi;
+        pivs[jj] = gi;
         if (!(gv > 0.0f) && *info == 0) *info = j + 1;  // zero (or NaN) pivot
       }
       // the pivot row's inner block
@@ -1283,6 +1348,11 @@ __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __re
     A[static_cast<long long>(j0 + k) * ld + r0 + r] = tile[r * S + k];
   }
   cluster.sync();  // remote readers of this CTA's shared memory are done
+  // the panel's row moves for the swaps outside it (ublk is free now)
+  if (swap_map && rank == 0 && warp == 0) {
+    int* rows = reinterpret_cast<int*>(&ublk[0][0]);
+    swap_map_warp(pivs, j0, jb, swap_map, rows, rows + 256, rows + 512);
+  }
 }
 
 // Widest panel (96, 64 or 32 columns) whose rows fit in the shared memory of
@@ -1296,7 +1366,8 @@ static int cluster_panel_width(int rows) {
 
 // Launches the cluster panel; false when the GPU cannot host a 16-CTA
 // cluster of this size (the caller then uses the cooperative grid kernel).
-static bool panel_cluster16(Context* ctx, float* A, long long ld, int N, int j0, int jb, int* ipiv, int* info) {
+static bool panel_cluster16(Context* ctx, float* A, long long ld, int N, int j0, int jb, int* ipiv, int* info,
+                            int* swap_map) {
   const int rows = N - j0;
   const int per = (rows + CP_CL - 1) / CP_CL;
   const size_t smem = static_cast<size_t>(per) * cp_row_stride(jb) * sizeof(float);
@@ -1338,64 +1409,10 @@ static bool panel_cluster16(Context* ctx, float* A, long long ld, int N, int j0,
   at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  cuda_check(cudaLaunchKernelEx(&cfg, panel_cluster16_kernel, A, ld, N, j0, jb, per, ipiv, info),
+  cuda_check(cudaLaunchKernelEx(&cfg, panel_cluster16_kernel, A, ld, N, j0, jb, per, ipiv, info, swap_map),
              "panel cluster kernel");
   ctx->launches += 1;
   return true;
-}
-
-// The row exchanges of one panel (ipiv[j0 .. j0+jb)) as a list of moves
-// row dst[t] <- row src[t] over the rows they touch (at most 2 jb): rows
-// j0 .. j0+jb-1 first, then the pivot rows below the panel.  One warp.
-__global__ void build_swap_map(const int* __restrict__ ipiv, int j0, int jb, int* __restrict__ map) {
-  // map[0] = count, map[1 .. 1+2jb) = dst, map[1+2jb .. 1+4jb) = src
-  __shared__ int rows[256], content[256], piv[128];
-  __shared__ int cnt;
-  const int lane = threadIdx.x;
-  for (int t = lane; t < jb; t += 32) piv[t] = ipiv[j0 + t];
-  for (int t = lane; t < jb; t += 32) {
-    rows[t] = j0 + t;
-    content[t] = j0 + t;
-  }
-  if (lane == 0) cnt = jb;
-  __syncwarp();
-  for (int jj = 0; jj < jb; jj++) {
-    const int p = piv[jj];
-    int idx;
-    if (p < j0 + jb) {
-      idx = p - j0;
-    } else {
-      idx = -1;
-      for (int t0 = jb; t0 < cnt; t0 += 32) {
-        unsigned m = __ballot_sync(0xffffffffu, t0 + lane < cnt && rows[t0 + lane] == p);
-        if (m) {
-          idx = t0 + __ffs(m) - 1;
-          break;
-        }
-      }
-      if (idx < 0) {
-        idx = cnt;
-        if (lane == 0) {
-          rows[idx] = p;
-          content[idx] = p;
-        }
-      }
-    }
-    __syncwarp();
-    if (lane == 0) {
-      if (idx == cnt) cnt = cnt + 1;
-      int t = content[jj];
-      content[jj] = content[idx];
-      content[idx] = t;
-    }
-    __syncwarp();
-  }
-  const int n = cnt;
-  for (int t = lane; t < n; t += 32) {
-    map[1 + t] = rows[t];
-    map[1 + 2 * jb + t] = content[t];
-  }
-  if (lane == 0) map[0] = n;
 }
 
 // Applies a panel's row moves to every column outside the panel, one warp
@@ -1461,8 +1478,10 @@ static bool panel_grid(Context* ctx, T* A, long long ld, int N, int j0, int jb, 
 }
 
 template <class T>
-static void panel_factor(Context* ctx, T* A, long long ld, int N, int j0, int jb, int* ipiv, int* info, int nsm,
-                         void* slot_mem) {
+// Factors one panel; returns true when the panel kernel also wrote the
+// panel's row-move list into swap_map (the FP32 cluster path).
+static bool panel_factor(Context* ctx, T* A, long long ld, int N, int j0, int jb, int* ipiv, int* info, int nsm,
+                         void* slot_mem, int* swap_map) {
   cudaStream_t s = ctx->stream();
   double fl = 0;
   for (int j = j0; j < j0 + jb; j++) fl += 2.0 * (N - j - 1) * (j0 + jb - j - 1) + (N - j);
@@ -1483,9 +1502,9 @@ static void panel_factor(Context* ctx, T* A, long long ld, int N, int j0, int jb
     slots.err = reinterpret_cast<int*>(p + 16);
   }
   if constexpr (std::is_same<T, float>::value) {
-    if (panel_cluster16(ctx, A, ld, N, j0, jb, ipiv, info)) return;
+    if (panel_cluster16(ctx, A, ld, N, j0, jb, ipiv, info, swap_map)) return true;
   }
-  if (panel_grid<T>(ctx, A, ld, N, j0, jb, ipiv, info, nsm, slots)) return;
+  if (panel_grid<T>(ctx, A, ld, N, j0, jb, ipiv, info, nsm, slots)) return false;
   // Panels too tall for the shared memory of the GPU: one 8-CTA cluster
   // working on the panel in global memory.
   cudaLaunchConfig_t cfg = {};
@@ -1502,16 +1521,21 @@ static void panel_factor(Context* ctx, T* A, long long ld, int N, int j0, int jb
   cfg.numAttrs = 1;
   cuda_check(cudaLaunchKernelEx(&cfg, panel_cluster_kernel<T>, A, ld, N, j0, jb, ipiv, info), "panel cluster kernel");
   ctx->launches += 1;
+  return false;
 }
 
 template <class T>
-static void trsm_and_swaps(Context* ctx, T* A, long long ld, int N, int j0, int jb, const int* ipiv, int* map) {
+static void trsm_and_swaps(Context* ctx, T* A, long long ld, int N, int j0, int jb, const int* ipiv, int* map,
+                           bool map_ready) {
   cudaStream_t s = ctx->stream();
   ProfScope ps(ctx, Context::PROF_LU_SWAP_TRSM, double(jb) * jb * (N - j0 - jb));
   if (N > jb) {
-    build_swap_map<<<1, 32, 0, s>>>(ipiv, j0, jb, map);
+    if (!map_ready) {
+      build_swap_map<<<1, 32, 0, s>>>(ipiv, j0, jb, map);
+      ctx->launches += 1;
+    }
     laswp_map<T><<<blocks(static_cast<long long>(N - jb) * 32, 256), 256, 0, s>>>(A, ld, N, j0, jb, map);
-    ctx->launches += 2;
+    ctx->launches += 1;
   }
   if (j0 + jb < N) {
     size_t smem = sizeof(double) * (static_cast<size_t>(jb) * jb + static_cast<size_t>(jb) * TRSM_COLS);
@@ -1538,8 +1562,8 @@ void DenseLU::factor_fp64(double* A, long long ld, int N) {
   cuda_check(cudaMemsetAsync(d_info_, 0, sizeof(int), s), "memset info");
   for (int j0 = 0; j0 < N; j0 += NB) {
     int jb = (N - j0 < NB) ? N - j0 : NB;
-    panel_factor<double>(ctx_, A, ld, N, j0, jb, ipiv_, d_info_, nsm_, slot_mem_);
-    trsm_and_swaps<double>(ctx_, A, ld, N, j0, jb, ipiv_, swap_map_);
+    const bool map_ready = panel_factor<double>(ctx_, A, ld, N, j0, jb, ipiv_, d_info_, nsm_, slot_mem_, swap_map_);
+    trsm_and_swaps<double>(ctx_, A, ld, N, j0, jb, ipiv_, swap_map_, map_ready);
     int m = N - j0 - jb;
     if (m > 0) {
       // A22 -= A21 * A12 (FP64 library GEMM)
@@ -1569,8 +1593,8 @@ void DenseLU::factor_f32(float* A, long long ld, int N, bool tf32) {
       if (cw > 0) w = cw;
     }
     jb = (N - j0 < w) ? N - j0 : w;
-    panel_factor<float>(ctx_, A, ld, N, j0, jb, ipiv_, d_info_, nsm_, slot_mem_);
-    trsm_and_swaps<float>(ctx_, A, ld, N, j0, jb, ipiv_, swap_map_);
+    const bool map_ready = panel_factor<float>(ctx_, A, ld, N, j0, jb, ipiv_, d_info_, nsm_, slot_mem_, swap_map_);
+    trsm_and_swaps<float>(ctx_, A, ld, N, j0, jb, ipiv_, swap_map_, map_ready);
     int m = N - j0 - jb;
     if (m > 0) {
       float* A21 = A + static_cast<long long>(j0) * ld + j0 + jb;
