@@ -970,50 +970,48 @@ __global__ void __launch_bounds__(GP_THREADS) panel_grid_kernel(T* __restrict__ 
 
 // The row exchanges of one panel (pivots piv[0 .. jb), rows j0 .. ) as a
 // list of moves row dst[t] <- row src[t] over the rows they touch (at most
-// 2 jb): rows j0 .. j0+jb-1 first, then the pivot rows below the panel.
-// One warp; piv, rows (2 jb), content (2 jb) and cnt in shared memory.
+// 2 jb): rows j0 .. j0+jb-1 first, then the pivot rows below the panel in
+// order of first appearance.  One warp: lane 0 replays the exchanges with
+// the rows below the panel found through a small hash table.  piv, rows
+// (2 jb), content (2 jb), hkey and hidx (256 each) and cnt in shared memory.
 // map[0] = count, map[1 .. 1+2jb) = dst, map[1+2jb .. 1+4jb) = src.
+constexpr int SWAP_HASH = 256;
 __device__ void swap_map_warp(const int* piv, int j0, int jb, int* __restrict__ map, int* rows, int* content,
-                              int* cnt_s) {
+                              int* hkey, int* hidx, int* cnt_s) {
   const int lane = threadIdx.x & 31;
   for (int t = lane; t < jb; t += 32) {
     rows[t] = j0 + t;
     content[t] = j0 + t;
   }
-  if (lane == 0) *cnt_s = jb;
+  for (int t = lane; t < SWAP_HASH; t += 32) hkey[t] = -1;
   __syncwarp();
-  for (int jj = 0; jj < jb; jj++) {
-    const int p = piv[jj];
-    const int cnt = *cnt_s;
-    int idx;
-    if (p < j0 + jb) {
-      idx = p - j0;
-    } else {
-      idx = -1;
-      for (int t0 = jb; t0 < cnt; t0 += 32) {
-        unsigned m = __ballot_sync(0xffffffffu, t0 + lane < cnt && rows[t0 + lane] == p);
-        if (m) {
-          idx = t0 + __ffs(m) - 1;
-          break;
-        }
-      }
-      if (idx < 0) {
-        idx = cnt;
-        if (lane == 0) {
+  if (lane == 0) {
+    int cnt = jb;
+    for (int jj = 0; jj < jb; jj++) {
+      const int p = piv[jj];
+      int idx;
+      if (p < j0 + jb) {
+        idx = p - j0;
+      } else {
+        unsigned h = (static_cast<unsigned>(p) * 2654435761u) >> 24;  // 8 bits
+        while (hkey[h] != -1 && hkey[h] != p) h = (h + 1) & (SWAP_HASH - 1);
+        if (hkey[h] == p) {
+          idx = hidx[h];
+        } else {
+          idx = cnt++;
+          hkey[h] = p;
+          hidx[h] = idx;
           rows[idx] = p;
           content[idx] = p;
         }
       }
-    }
-    __syncwarp();
-    if (lane == 0) {
-      if (idx == cnt) *cnt_s = cnt + 1;
-      int t = content[jj];
+      const int t = content[jj];
       content[jj] = content[idx];
       content[idx] = t;
     }
-    __syncwarp();
+    *cnt_s = cnt;
   }
+  __syncwarp();
   const int n = *cnt_s;
   for (int t = lane; t < n; t += 32) {
     map[1 + t] = rows[t];
@@ -1023,11 +1021,11 @@ __device__ void swap_map_warp(const int* piv, int j0, int jb, int* __restrict__ 
 }
 
 __global__ void build_swap_map(const int* __restrict__ ipiv, int j0, int jb, int* __restrict__ map) {
-  __shared__ int rows[256], content[256], piv[128];
+  __shared__ int rows[256], content[256], piv[128], hkey[SWAP_HASH], hidx[SWAP_HASH];
   __shared__ int cnt;
   for (int t = threadIdx.x; t < jb; t += 32) piv[t] = ipiv[j0 + t];
   __syncwarp();
-  swap_map_warp(piv, j0, jb, map, rows, content, &cnt);
+  swap_map_warp(piv, j0, jb, map, rows, content, hkey, hidx, &cnt);
 }
 
 // ---- panel on one 16-CTA cluster (FP32 factors) --------------------------
@@ -1351,7 +1349,8 @@ __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __re
   // the panel's row moves for the swaps outside it (ublk is free now)
   if (swap_map && rank == 0 && warp == 0) {
     int* rows = reinterpret_cast<int*>(&ublk[0][0]);
-    swap_map_warp(pivs, j0, jb, swap_map, rows, rows + 256, rows + 512);
+    swap_map_warp(pivs, j0, jb, swap_map, rows, rows + 256, rows + 512, rows + 512 + SWAP_HASH,
+                  rows + 512 + 2 * SWAP_HASH);
   }
 }
 
