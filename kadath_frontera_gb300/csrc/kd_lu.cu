@@ -578,22 +578,26 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
 
 // Grid barrier for a cooperative launch (all CTAs resident).  Returns false,
 // with *err set, when the counter did not reach `target` within the limit.
+// Grid-wide barrier of a cooperative launch: the CTA's writes are published
+// by thread 0's release increment (after the block barrier), the other
+// CTAs' writes acquired by its polling loads; gives up after GP_WAIT_NS.
 __device__ bool grid_barrier(unsigned* bar, unsigned target, int* err, int* s_ok) {
   __syncthreads();
   if (threadIdx.x == 0) {
-    __threadfence();
-    atomicAdd(bar, 1u);
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(bar), "r"(1u) : "memory");
     const unsigned long long t0 = globaltimer_ns();
     int ok = 1;
-    while (*reinterpret_cast<volatile unsigned*>(bar) < target) {
-      if (globaltimer_ns() - t0 > GP_WAIT_NS) {
+    for (unsigned it = 0;; it++) {
+      unsigned v;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(bar) : "memory");
+      if (v >= target) break;
+      if ((it & 31) == 31 && globaltimer_ns() - t0 > GP_WAIT_NS) {
         ok = 0;
         atomicExch(err, 1);
         break;
       }
       __nanosleep(20);
     }
-    __threadfence();
     *s_ok = ok;
   }
   __syncthreads();
