@@ -512,8 +512,36 @@ bool tf32x3_gemm_possible(int k, const float* C, long long ldc, int m, int c_row
          (m + 3) / 4 * 4 <= c_rows_writable && encode_fn() != nullptr;
 }
 
+int tf32_update_max_clusters16() {
+  static int maxc = 0;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    if (cudaFuncSetAttribute(tf32_update_persistent, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
+        cudaFuncSetAttribute(tf32_update_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(P_MAX_SMEM)) != cudaSuccess) {
+      cudaGetLastError();
+      return;
+    }
+    cudaLaunchConfig_t q = {};
+    q.gridDim = dim3(16, 1, 1);
+    q.blockDim = dim3(P_THREADS, 1, 1);
+    q.dynamicSmemBytes = P_MAX_SMEM;
+    cudaLaunchAttribute qa[1];
+    qa[0].id = cudaLaunchAttributeClusterDimension;
+    qa[0].val.clusterDim.x = 16;
+    qa[0].val.clusterDim.y = 1;
+    qa[0].val.clusterDim.z = 1;
+    q.attrs = qa;
+    q.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, tf32_update_persistent, &q) == cudaSuccess) maxc = n;
+    cudaGetLastError();
+  });
+  return maxc;
+}
+
 void tf32_gemm_update(Context* ctx, int m, int n, int k, const float* A, long long lda, const float* B, long long ldb,
-                      float* C, long long ldc, int c_rows_writable, int terms) {
+                      float* C, long long ldc, int c_rows_writable, int terms, bool spare_gpc) {
   if (m <= 0 || n <= 0 || k <= 0) return;
   if (k > TC_MAXK) throw KdError(KD_ERR_ARG, "tcgen05 trailing update: panel width above 128");
   const bool split3 = (terms == 3);
@@ -568,6 +596,29 @@ void tf32_gemm_update(Context* ctx, int m, int n, int k, const float* A, long lo
     const size_t psmem = 1024 + ops + static_cast<size_t>(ncs) * P_CHUNK_BYTES;
     if (psmem > P_MAX_SMEM) throw KdError(KD_ERR_UNSUPPORTED, "tcgen05 update: operands do not fit in shared memory");
     const int ntm = mpad / TC_M, ntiles = ntm * (npad / TC_N);
+    const int maxc = spare_gpc ? tf32_update_max_clusters16() : 0;
+    if (maxc >= 2) {
+      // 16-CTA clusters (the CTAs share nothing), one fewer than fit
+      int ncl = (ntiles + 15) / 16;
+      if (ncl > maxc - 1) ncl = maxc - 1;
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(16 * ncl, 1, 1);
+      cfg.blockDim = dim3(P_THREADS, 1, 1);
+      cfg.dynamicSmemBytes = psmem;
+      cfg.stream = s;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = 16;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      cuda_check(cudaLaunchKernelEx(&cfg, tf32_update_persistent, mA, mB, mAl, mBl, mC, nkb, ntm, ntiles,
+                                    split3 ? 1 : 0, ncs, err),
+                 "tcgen05 trailing update (clusters)");
+      ctx->launches += 1;
+      return;
+    }
     const int grid = ntiles < nsm ? ntiles : nsm;
     tf32_update_persistent<<<grid, P_THREADS, psmem, s>>>(mA, mB, mAl, mBl, mC, nkb, ntm, ntiles, split3 ? 1 : 0, ncs,
                                                           err);
@@ -608,11 +659,11 @@ int tf32_gemm_error_flag(Context* ctx) {
 
 void gemm_update_f32(Context* ctx, cublasHandle_t blas, int m, int n, int k, const float* A, long long lda,
                      const float* B, long long ldb, float* C, long long ldc, bool tf32, int c_rows_writable,
-                     int terms) {
+                     int terms, bool spare_gpc) {
   ProfScope ps(ctx, Context::PROF_LU_GEMM, 2.0 * m * n * k);
   if (tf32 && tf32_gemm_supported(k)) {
     if (terms == 3 && !tf32x3_gemm_possible(k, C, ldc, m, c_rows_writable)) terms = 1;
-    tf32_gemm_update(ctx, m, n, k, A, lda, B, ldb, C, ldc, c_rows_writable, terms);
+    tf32_gemm_update(ctx, m, n, k, A, lda, B, ldb, C, ldc, c_rows_writable, terms, spare_gpc);
     return;
   }
   // plain FP32 product (the FP32-IR mode): library SGEMM

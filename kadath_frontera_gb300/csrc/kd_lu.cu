@@ -1587,27 +1587,54 @@ void DenseLU::factor_f32(float* A, long long ld, int N, bool tf32) {
   const int NB = nb > 96 ? 96 : nb;
   cudaStream_t s = ctx_->stream();
   cuda_check(cudaMemsetAsync(d_info_, 0, sizeof(int), s), "memset info");
-  for (int j0 = 0, jb = 0; j0 < N; j0 += jb) {
-    // Panel width: NB, narrowed while the panel is too tall for the shared
-    // memory of one 16-CTA cluster (blocked LU allows any widths).
+  // Panel width: NB, narrowed while the panel is too tall for the shared
+  // memory of one 16-CTA cluster (blocked LU allows any widths).
+  auto width = [&](int j0) {
     int w = NB;
     if (NB == 96) {
       const int cw = cluster_panel_width(N - j0);
       if (cw > 0) w = cw;
     }
-    jb = (N - j0 < w) ? N - j0 : w;
-    const bool map_ready = panel_factor<float>(ctx_, A, ld, N, j0, jb, ipiv_, d_info_, nsm_, slot_mem_, swap_map_);
-    trsm_and_swaps<float>(ctx_, A, ld, N, j0, jb, ipiv_, swap_map_, map_ready);
-    int m = N - j0 - jb;
-    if (m > 0) {
-      float* A21 = A + static_cast<long long>(j0) * ld + j0 + jb;
-      float* A12 = A + static_cast<long long>(j0 + jb) * ld + j0;
-      float* A22 = A + static_cast<long long>(j0 + jb) * ld + j0 + jb;
-      // rows N .. ld of the working matrix are padding
-      gemm_update_f32(ctx_, blas_, m, m, jb, A21, ld, A12, ld, A22, ld, tf32, static_cast<int>(ld - j0 - jb),
-                      tf32_terms);
+    return (N - j0 < w) ? N - j0 : w;
+  };
+  // Look-ahead (tensor-core update only): the columns of the next panel are
+  // updated first, then the rest of the trailing update runs on a side
+  // stream as 16-CTA clusters that leave one GPC free, while the next panel
+  // is factored on the main stream; the next row exchanges wait for both.
+  const bool lookahead = tf32 && tf32_update_max_clusters16() >= 2;
+  int j0 = 0, jb = width(0);
+  bool map_ready = panel_factor<float>(ctx_, A, ld, N, j0, jb, ipiv_, d_info_, nsm_, slot_mem_, swap_map_);
+  bool side_pending = false;
+  for (;;) {
+    if (side_pending) {
+      ctx_->join();
+      side_pending = false;
     }
+    trsm_and_swaps<float>(ctx_, A, ld, N, j0, jb, ipiv_, swap_map_, map_ready);
+    const int m = N - j0 - jb;
+    if (m <= 0) break;
+    const int j0n = j0 + jb, jbn = width(j0n);
+    float* A21 = A + static_cast<long long>(j0) * ld + j0 + jb;
+    float* A12 = A + static_cast<long long>(j0 + jb) * ld + j0;
+    float* A22 = A + static_cast<long long>(j0 + jb) * ld + j0 + jb;
+    // rows N .. ld of the working matrix are padding
+    const int writable = static_cast<int>(ld - j0 - jb);
+    if (lookahead && m > jbn) {
+      gemm_update_f32(ctx_, blas_, m, jbn, jb, A21, ld, A12, ld, A22, ld, tf32, writable, tf32_terms);
+      ctx_->fork(1);
+      ctx_->use(0);
+      gemm_update_f32(ctx_, blas_, m, m - jbn, jb, A21, ld, A12 + static_cast<long long>(jbn) * ld, ld,
+                      A22 + static_cast<long long>(jbn) * ld, ld, tf32, writable, tf32_terms, true);
+      ctx_->use(-1);
+      side_pending = true;
+    } else {
+      gemm_update_f32(ctx_, blas_, m, m, jb, A21, ld, A12, ld, A22, ld, tf32, writable, tf32_terms);
+    }
+    map_ready = panel_factor<float>(ctx_, A, ld, N, j0n, jbn, ipiv_, d_info_, nsm_, slot_mem_, swap_map_);
+    j0 = j0n;
+    jb = jbn;
   }
+  if (side_pending) ctx_->join();
 }
 
 void DenseLU::factor(double* A, long long ld, int N, int mode) {
