@@ -1142,6 +1142,7 @@ __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __re
   __shared__ int wi[CP_WARPS];
   const int S = cp_row_stride(jb);
   const int rank = static_cast<int>(cluster.block_rank());
+  const int ncl = static_cast<int>(cluster.num_blocks());  // 2, 4, 8 or 16 CTAs
   const int tid = threadIdx.x, bd = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5;
   const int r0 = j0 + rank * per;
@@ -1198,29 +1199,33 @@ __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __re
         const int crow = (ci < N) ? ci - r0 : 0;  // row 0's words stand in when there is no candidate
         if (ci < N)
           for (int k = lane; k < jb; k += 32) cand_row[slot][k] = tile[crow * S + k];
-        CpSlot* R = cluster.map_shared_rank(&recv[slot], lane & (CP_CL - 1));
-        if (lane < CP_CL) {
-          R->v[rank] = cv;
-          R->i[rank] = ci;
-        }
         const float4* src = reinterpret_cast<const float4*>(tile + static_cast<size_t>(crow) * S + b0);
-        const int c0 = (lane >> 4) * 2;
-        R->seg[rank][c0] = src[c0];
-        R->seg[rank][c0 + 1] = src[c0 + 1];
+        for (int e = lane; e < 2 * ncl; e += 32) {  // (destination CTA, half of the inner block)
+          CpSlot* R = cluster.map_shared_rank(&recv[slot], e >> 1);
+          const int c0 = (e & 1) * 2;
+          R->seg[rank][c0] = src[c0];
+          R->seg[rank][c0 + 1] = src[c0 + 1];
+          if ((e & 1) == 0) {
+            R->v[rank] = cv;
+            R->i[rank] = ci;
+          }
+        }
       } else if (warp == 1 && j >= r0 && j < r1) {
         for (int k = lane; k < jb; k += 32) jrow[slot][k] = tile[(j - r0) * S + k];
-        CpSlot* R = cluster.map_shared_rank(&recv[slot], lane & (CP_CL - 1));
         const float4* src = reinterpret_cast<const float4*>(tile + static_cast<size_t>(j - r0) * S + b0);
-        const int c0 = (lane >> 4) * 2;
-        R->jseg[c0] = src[c0];
-        R->jseg[c0 + 1] = src[c0 + 1];
+        for (int e = lane; e < 2 * ncl; e += 32) {
+          CpSlot* R = cluster.map_shared_rank(&recv[slot], e >> 1);
+          const int c0 = (e & 1) * 2;
+          R->jseg[c0] = src[c0];
+          R->jseg[c0 + 1] = src[c0 + 1];
+        }
       }
       cluster.sync();
       // the winner, from this CTA's own receive slot: every warp reduces the
-      // 16 candidates across its lanes (same result everywhere)
+      // candidates across its lanes (same result everywhere)
       float gv = -1.0f;
       int gi = N, tag = -1;
-      if (lane < CP_CL) {
+      if (lane < ncl) {
         gv = recv[slot].v[lane];
         gi = recv[slot].i[lane];
         tag = lane;
@@ -1367,12 +1372,18 @@ static int cluster_panel_width(int rows) {
   return 0;
 }
 
-// Launches the cluster panel; false when the GPU cannot host a 16-CTA
-// cluster of this size (the caller then uses the cooperative grid kernel).
+// Launches the cluster panel on the smallest cluster (2, 4, 8 or 16 CTAs)
+// whose shared memory holds the panel; false when none does or the GPU
+// cannot host a 16-CTA cluster (the caller then uses the cooperative grid
+// kernel).
 static bool panel_cluster16(Context* ctx, float* A, long long ld, int N, int j0, int jb, int* ipiv, int* info,
                             int* swap_map) {
   const int rows = N - j0;
-  const int per = (rows + CP_CL - 1) / CP_CL;
+  int ncl = 2;
+  while (ncl < CP_CL &&
+         static_cast<size_t>((rows + ncl - 1) / ncl) * cp_row_stride(jb) * sizeof(float) > CP_MAX_SMEM)
+    ncl *= 2;
+  const int per = (rows + ncl - 1) / ncl;
   const size_t smem = static_cast<size_t>(per) * cp_row_stride(jb) * sizeof(float);
   if (smem > CP_MAX_SMEM) return false;
   static int usable = 0;
@@ -1401,13 +1412,13 @@ static bool panel_cluster16(Context* ctx, float* A, long long ld, int N, int j0,
   });
   if (!usable) return false;
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(CP_CL, 1, 1);
+  cfg.gridDim = dim3(ncl, 1, 1);
   cfg.blockDim = dim3(CP_THREADS, 1, 1);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = ctx->stream();
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = CP_CL;
+  at[0].val.clusterDim.x = ncl;
   at[0].val.clusterDim.y = 1;
   at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
