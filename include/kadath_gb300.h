@@ -273,6 +273,12 @@ typedef struct kd_newton_report {
  * include/system_of_eqs.hpp:871).  Returns KD_OK and fills rep; the fields
  * registered with add_var are updated in place on the device. */
 int kd_newton_step(kd_system* s, const kd_newton_opts* opts, kd_newton_report* rep);
+/* do_newton(precision, error, GAUSS_NEWTON) (include/system_of_eqs.hpp:134,
+ * src_par/do_newton.cpp:264-311): for a system with at least as many
+ * conditions m as unknowns n, solves the normal equations
+ * (J^T J) x = J^T F (J is m x n; J^T J and J^T F in FP64; J^T J factored in
+ * opts->lu_mode) and updates fields <- fields - x.  rep->n is n. */
+int kd_newton_step_gauss_newton(kd_system* s, const kd_newton_opts* opts, kd_newton_report* rep);
 /* System_of_eqs::do_newton_with_linesearch (src_par/do_newton.cpp:454-516):
  * Newton direction p = J^-1 F, rescaled when max(p) > stepmax, then fields
  * = old - lambda p with lambda backtracked (quadratic, then cubic model of

@@ -630,6 +630,15 @@ int kd_newton_step(kd_system* s, const kd_newton_opts* opts, kd_newton_report* r
   });
 }
 
+int kd_newton_step_gauss_newton(kd_system* s, const kd_newton_opts* opts, kd_newton_report* rep) {
+  SYS_GUARD(s) {
+    if (!opts || !rep) throw kd::KdError(KD_ERR_ARG, "null argument");
+    kd::NewtonReport r;
+    s->newton->step_gauss_newton(to_opts(opts), r);
+    to_report(r, rep);
+  });
+}
+
 int kd_system_add_ope_eos(kd_system* s, const char* name, int var, int npieces, double rhomin, double rhomax,
                           double k0, const double* gamma_tab, const double* rho_tab) {
   SYS_GUARD(s) {

@@ -18,6 +18,9 @@ Newton::~Newton() {
   cudaStreamSynchronize(sys_->ctx->stream());
   cudaFree(d_F);
   cudaFree(d_J);
+  cudaFree(d_JtJ_);
+  cudaFree(d_JtF_);
+  if (blas_) cublasDestroy(blas_);
 }
 
 void Newton::ensure(int N) {
@@ -77,6 +80,81 @@ bool Newton::step(const NewtonOpts& o, NewtonReport& rep) {
   rep.refine_rel_residual = lu_->stats.final_rel_residual;
   auto t3 = std::chrono::steady_clock::now();
   sys_->update_from_x(d_F);
+  rep.t_update_ms = ms_since(t3);
+  rep.kernel_launches = ctx->launches - l0;
+  return false;
+}
+
+bool Newton::step_gauss_newton(const NewtonOpts& o, NewtonReport& rep) {
+  Context* ctx = sys_->ctx;
+  cudaStream_t s = ctx->stream();
+  long long l0 = ctx->launches;
+  rep = NewtonReport();
+  auto t0 = std::chrono::steady_clock::now();
+  if (sys_->nbr_conditions() < 0) sys_->residual(nullptr);
+  const int m = sys_->nbr_conditions();
+  const int n = sys_->nbr_unknowns();
+  if (m < n)
+    throw KdError(KD_ERR_STATE, "Gauss-Newton needs at least as many conditions (" + std::to_string(m) +
+                                    ") as unknowns (" + std::to_string(n) + ")");
+  if (static_cast<size_t>(m) > capF_) {
+    cudaFree(d_F);
+    d_F = nullptr;
+    cuda_check(cudaMalloc(&d_F, sizeof(double) * m), "cudaMalloc(F)");
+    capF_ = m;
+  }
+  if (static_cast<size_t>(m) * n > capJ_) {
+    cudaFree(d_J);
+    d_J = nullptr;
+    cuda_check(cudaMalloc(&d_J, sizeof(double) * static_cast<size_t>(m) * n), "cudaMalloc(J)");
+    capJ_ = static_cast<size_t>(m) * n;
+  }
+  if (static_cast<size_t>(n) > capN_) {
+    cudaFree(d_JtJ_);
+    cudaFree(d_JtF_);
+    d_JtJ_ = d_JtF_ = nullptr;
+    cuda_check(cudaMalloc(&d_JtJ_, sizeof(double) * static_cast<size_t>(n) * n), "cudaMalloc(JtJ)");
+    cuda_check(cudaMalloc(&d_JtF_, sizeof(double) * n), "cudaMalloc(JtF)");
+    capN_ = n;
+  }
+  ld = m;
+  sys_->residual(d_F, true);
+  double* d_err = ctx->scratch().alloc_doubles(1);
+  cuda_check(launch_absmax(d_F, m, d_err, s), "absmax");
+  double err = 0;
+  cuda_check(cudaMemcpyAsync(&err, d_err, sizeof(double), cudaMemcpyDeviceToHost, s), "D2H err");
+  cuda_check(cudaStreamSynchronize(s), "sync residual");
+  rep.t_residual_ms = ms_since(t0);
+  rep.error = err;
+  rep.n = n;
+  if (err < o.precision) {
+    rep.converged = 1;
+    rep.kernel_launches = ctx->launches - l0;
+    return true;
+  }
+  auto t1 = std::chrono::steady_clock::now();
+  sys_->jacobian(d_J, m, true, true);
+  // J^T F and J^T J (library FP64 products, as pdgemv / pdgemm)
+  if (!blas_ && cublasCreate(&blas_) != CUBLAS_STATUS_SUCCESS) throw KdError(KD_ERR_CUDA, "cublasCreate failed");
+  cublasSetStream(blas_, s);
+  const double one = 1.0, zero = 0.0;
+  if (cublasDgemv(blas_, CUBLAS_OP_T, m, n, &one, d_J, m, d_F, 1, &zero, d_JtF_, 1) != CUBLAS_STATUS_SUCCESS ||
+      cublasDgemm(blas_, CUBLAS_OP_T, CUBLAS_OP_N, n, n, m, &one, d_J, m, d_J, m, &zero, d_JtJ_, n) !=
+          CUBLAS_STATUS_SUCCESS)
+    throw KdError(KD_ERR_CUDA, "normal equations (cuBLAS) failed");
+  ctx->launches += 2;
+  cuda_check(cudaStreamSynchronize(s), "sync assembly");
+  rep.t_assembly_ms = ms_since(t1);
+  lu_->gmres_tol = o.gmres_tol;
+  lu_->gmres_max_iter = o.max_refine;
+  lu_->factor(d_JtJ_, n, n, o.lu_mode);
+  rep.t_factor_ms = lu_->stats.t_factor_ms;
+  lu_->solve(d_JtF_, 0);
+  rep.t_solve_ms = lu_->stats.t_solve_ms;
+  rep.refine_iters = lu_->stats.refine_iters;
+  rep.refine_rel_residual = lu_->stats.final_rel_residual;
+  auto t3 = std::chrono::steady_clock::now();
+  sys_->update_from_x(d_JtF_);
   rep.t_update_ms = ms_since(t3);
   rep.kernel_launches = ctx->launches - l0;
   return false;

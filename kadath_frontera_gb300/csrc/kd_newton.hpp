@@ -33,6 +33,11 @@ class Newton {
   explicit Newton(System* s);
   ~Newton();
   bool step(const NewtonOpts& o, NewtonReport& rep);
+  // The Gauss-Newton variant (do_newton with SOLVER GAUSS_NEWTON,
+  // src_par/do_newton.cpp:264-311): for nbr_conditions m >= nbr_unknowns n,
+  // solve the normal equations (J^T J) x = J^T F (the m x n Jacobian,
+  // J^T J and J^T F in FP64), then fields <- fields - x.
+  bool step_gauss_newton(const NewtonOpts& o, NewtonReport& rep);
   // System_of_eqs::do_newton_with_linesearch (src_par/do_newton.cpp:454-516,
   // Numerical Recipes 2007 section 9.7.1): the Newton direction p = J^-1 F
   // (scaled so that max(p) <= stepmax), then fields = old - lambda p with
@@ -57,6 +62,10 @@ class Newton {
   System* sys_;
   std::unique_ptr<DenseLU> lu_;
   size_t capF_ = 0, capJ_ = 0;
+  double* d_JtJ_ = nullptr;  // Gauss-Newton normal matrix and right-hand side
+  double* d_JtF_ = nullptr;
+  size_t capN_ = 0;
+  cublasHandle_t blas_ = nullptr;
   DeviceArena ls_arena_{size_t(64) << 20};  // field snapshots of a line search
   double device_scalar(const double* d_x, long long n, int op);
   double residual_norm2();

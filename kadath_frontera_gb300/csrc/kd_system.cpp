@@ -751,10 +751,10 @@ const double* System::seed_block(int var, int dom, int& B, Base& base) {
   return p;
 }
 
-void System::jacobian(double* d_J, long long ld, bool reuse) {
+void System::jacobian(double* d_J, long long ld, bool reuse, bool rectangular) {
   int N = nbr_unknowns();
   if (!reuse || !vcache_.valid) residual(nullptr, true);
-  if (nbr_conditions_ != N) {
+  if (rectangular ? (nbr_conditions_ < N || ld < nbr_conditions_) : (nbr_conditions_ != N)) {
     std::ostringstream os;
     os << "Number of unknowns (" << N << ") is different from the number of equations (" << nbr_conditions_ << ")";
     throw KdError(KD_ERR_STATE, os.str());

@@ -213,7 +213,9 @@ class System {
   // Column-major dense Jacobian (ld >= nbr_conditions) on the device.
   // reuse: take node values from the preceding residual(..., true) at the
   // same iterate; otherwise a value pass is run first.
-  void jacobian(double* d_J, long long ld, bool reuse = false);
+  // rectangular: allow more conditions than unknowns (Gauss-Newton), J is
+  // nbr_conditions x nbr_unknowns with ld >= nbr_conditions.
+  void jacobian(double* d_J, long long ld, bool reuse = false, bool rectangular = false);
   // do_JX (src/System_of_eqs/solver.cpp:87): y = J x without forming J, one
   // tangent pass with every unknown seeded by x through affecte_tau.
   void jx(const double* d_x, double* d_y);

@@ -24,7 +24,7 @@ from ._lib import KadathError, default_context
 
 CHEB_TYPE = 1
 OUTER_BC, INNER_BC = 0, 1
-NEWTON_RAPHSON = 0
+NEWTON_RAPHSON, GAUSS_NEWTON = 0, 1  # System_of_eqs::SOLVER (include/system_of_eqs.hpp:134)
 
 KD_LU_FP64, KD_LU_TF32_IR, KD_LU_FP32_IR = 0, 1, 2
 KD_EOS_EPSILON, KD_EOS_PRESSURE, KD_EOS_DENSITY, KD_EOS_DHDRHO = 0, 1, 2, 3
@@ -93,6 +93,7 @@ def _declare_system(lib):
         "kd_system_jacobian_device": (I, [P, P, C.c_longlong]),
         "kd_system_update": (I, [P, DP]),
         "kd_newton_step": (I, [P, C.POINTER(NewtonOpts), C.POINTER(NewtonReport)]),
+        "kd_newton_step_gauss_newton": (I, [P, C.POINTER(NewtonOpts), C.POINTER(NewtonReport)]),
         "kd_newton_step_linesearch": (I, [P, C.POINTER(NewtonOpts), I, D, C.POINTER(NewtonReport), DP]),
         "kd_system_set_cst": (I, [P, C.c_char_p, D]),
         "kd_system_add_ope_eos": (I, [P, C.c_char_p, I, I, D, D, D, DP, DP]),
@@ -473,11 +474,13 @@ class System_of_eqs:
         self.ctx.check(_L().kd_system_update(self.h, _dp(x)))
         self._J = None
 
-    def do_newton(self, precision, lu_mode=None, gmres_tol=1e-14, max_refine=50):
-        """System_of_eqs::do_newton: returns (converged, error)."""
+    def do_newton(self, precision, lu_mode=None, gmres_tol=1e-14, max_refine=50, solver=None):
+        """System_of_eqs::do_newton(precision, error, solver): returns
+        (converged, error); solver NEWTON_RAPHSON (default) or GAUSS_NEWTON."""
         opts = NewtonOpts(precision, self.lu_mode if lu_mode is None else lu_mode, gmres_tol, max_refine, 0)
         rep = NewtonReport()
-        self.ctx.check(_L().kd_newton_step(self.h, C.byref(opts), C.byref(rep)))
+        fn = _L().kd_newton_step_gauss_newton if solver == GAUSS_NEWTON else _L().kd_newton_step
+        self.ctx.check(fn(self.h, C.byref(opts), C.byref(rep)))
         self.last_report = rep.as_dict()
         self._J = None
         return bool(rep.converged), rep.error

@@ -206,7 +206,7 @@ def eigen_nucleus(res=(11, 5, 4), normalise="val", lam0=9.0):
     return doms, sysm, u
 
 
-def mass_at_infinity(res=(11, 5, 4), m0=0.5):
+def mass_at_infinity(res=(11, 5, 4), m0=0.5, redundant=False):
     """Lap(P) = 0 in two shells and the compactified domain (bounds 1, 2, 4),
     P = 2 at r = 1, P = 1 at infinity, and a double unknown M fixed by the
     surface integral at infinity integ(dn(P)) + 4 pi M = 0.  Known answer:
@@ -223,5 +223,7 @@ def mass_at_infinity(res=(11, 5, 4), m0=0.5):
         sysm.add_eq_matching(d, K.OUTER_BC, lambda T, b: T["P"])
         sysm.add_eq_matching(d, K.OUTER_BC, lambda T, b: T["P"].dn(b))
     sysm.add_eq_bc(3, K.OUTER_BC, lambda T, b: T["P"] - 1.0)
+    if redundant:  # the outer condition once more: an overdetermined, consistent system
+        sysm.add_eq_bc(3, K.OUTER_BC, lambda T, b: T["P"] - 1.0)
     sysm.add_eq_int([(3, K.OUTER_BC, lambda T, b: T["P"].dn(b).integ(b) + 4 * math.pi * T["M"])])
     return doms, sysm, P

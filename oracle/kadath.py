@@ -1092,11 +1092,11 @@ class OSystem:
                 col += len(pats)
         return layout, col
 
-    def jacobian(self):
+    def jacobian(self, rectangular=False):
         F = self.residual()
         layout, N = self.unknown_layout()
-        assert N == len(F), (N, len(F))
-        J = np.zeros((N, N))
+        assert (len(F) >= N) if rectangular else (N == len(F)), (N, len(F))
+        J = np.zeros((len(F), N))
         row0 = []
         nint = len(self.ieqs)
         r = nint
@@ -1164,13 +1164,17 @@ class OSystem:
                     if not f[dd].zero:
                         f[dd] = f[dd] - f[dd]
 
-    def newton_step(self, precision, solve=None):
+    def newton_step(self, precision, solve=None, gauss_newton=False):
+        """One step of do_newton; gauss_newton: the SOLVER GAUSS_NEWTON branch
+        (src_par/do_newton.cpp:264-311), x = (J^T J)^-1 J^T F."""
         import scipy.linalg as sla
-        F, J = self.jacobian()
+        F, J = self.jacobian(rectangular=gauss_newton)
         err = float(np.max(np.abs(F)))
         if err < precision:
             return True, err, F, J
-        if solve is None:
+        if gauss_newton:
+            x = sla.lu_solve(sla.lu_factor(J.T @ J), J.T @ F)
+        elif solve is None:
             x = sla.lu_solve(sla.lu_factor(J), F)
         else:
             x = solve(J, F)
