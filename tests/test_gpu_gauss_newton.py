@@ -58,7 +58,7 @@ def test_gauss_newton_matches_oracle(ctx):
             break
     assert done and odone
     for d in range(nd):
-        g = psi.get_coef(d)
+        g = np.asarray(psi.get_coef(d)).ravel()
         o = opsi[d]
         o.coef()
         assert np.linalg.norm(g - o.cf[0].ravel()) <= 1e-9 * max(np.linalg.norm(o.cf[0]), 1e-12)
