@@ -443,7 +443,8 @@ def run_exporter(args, ctx, wl, stream, local):
     flops = 2.0 * len(fields) * float(np.sum(np.asarray(ncoef)[np.minimum(dom_of, len(ncoef) - 1)]))
     achieved = flops / (ms * 1e-3) / 1e12
     return {"points": n, "fields": len(fields), "ms": ms, "points_per_s": n / (ms * 1e-3),
-            "kernel": "val_points_kernel", "achieved_tflops_fp64": achieved,
+            "kernel": "pt_classify + pt_scatter + val_points_sorted_kernel", "achieved_tflops_fp64": achieved,
+            "fp64_peak_tflops": None,
             "work": "2 flops per coefficient of the point's domain per field (spectral summation)"}
 
 
