@@ -391,6 +391,8 @@ def run_gpu(args, ws, rank, local):
         "batch": batch,
         "exporter": exporter,
     }
+    if exporter:
+        exporter["frac_of_fp64_peak"] = exporter["achieved_tflops_fp64"] / fp64_tflops if fp64_tflops else None
     if not args.no_cpu:
         cb = cpu_step_sample(args.workload, blocks=args.cpu_blocks)
         line["cpu_baseline"] = {"value": cb["ms"], "unit": "ms", "cores": os.cpu_count(), "kind": "port",
@@ -444,7 +446,6 @@ def run_exporter(args, ctx, wl, stream, local):
     achieved = flops / (ms * 1e-3) / 1e12
     return {"points": n, "fields": len(fields), "ms": ms, "points_per_s": n / (ms * 1e-3),
             "kernel": "pt_classify + pt_scatter + val_points_sorted_kernel", "achieved_tflops_fp64": achieved,
-            "fp64_peak_tflops": None,
             "work": "2 flops per coefficient of the point's domain per field (spectral summation)"}
 
 
