@@ -49,6 +49,10 @@ typedef struct kd_ctx kd_ctx;
 /* ---- context ----------------------------------------------------------- */
 int kd_ctx_create(kd_ctx** out, int device);
 int kd_ctx_destroy(kd_ctx* ctx);
+/* No reference counterpart (the reference runs one system per process):
+ * at most `sms` SMs for this context's grid-wide solver kernels (0: all),
+ * so that contexts driven side by side share the GPU. */
+int kd_ctx_set_sm_budget(kd_ctx* ctx, int sms);
 const char* kd_last_error(const kd_ctx* ctx);
 int kd_ctx_synchronize(kd_ctx* ctx);
 /* Number of kernels this context has launched so far. */

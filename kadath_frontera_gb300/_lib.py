@@ -56,6 +56,7 @@ def _declare(lib: C.CDLL) -> None:
     sig = {
         "kd_ctx_create": (I, [C.POINTER(P), I]),
         "kd_ctx_destroy": (I, [P]),
+        "kd_ctx_set_sm_budget": (I, [P, I]),
         "kd_last_error": (C.c_char_p, [P]),
         "kd_ctx_synchronize": (I, [P]),
         "kd_ctx_launch_count": (C.c_longlong, [P]),
@@ -110,6 +111,11 @@ class Context:
 
     def synchronize(self) -> None:
         self.check(self.lib.kd_ctx_synchronize(self.h))
+
+    def set_sm_budget(self, sms: int) -> None:
+        """At most `sms` SMs for this context's grid-wide solver kernels
+        (0: all of them), for contexts that run side by side."""
+        self.check(self.lib.kd_ctx_set_sm_budget(self.h, int(sms)))
 
     @property
     def launches(self) -> int:

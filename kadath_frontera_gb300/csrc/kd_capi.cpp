@@ -114,6 +114,13 @@ int kd_ctx_create(kd_ctx** out, int device) {
   return KD_OK;
 }
 
+int kd_ctx_set_sm_budget(kd_ctx* ctx, int sms) {
+  if (!ctx || !ctx->c) return KD_ERR_ARG;
+  if (sms < 0) return KD_ERR_ARG;
+  ctx->c->set_sm_budget(sms);
+  return KD_OK;
+}
+
 int kd_ctx_destroy(kd_ctx* ctx) {
   if (!ctx) return KD_ERR_ARG;
   delete ctx;

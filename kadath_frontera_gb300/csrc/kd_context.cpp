@@ -62,6 +62,7 @@ void DeviceArena::release_to(size_t m) {
 
 Context::Context(int device) : device_(device) {
   cuda_check(cudaSetDevice(device), "cudaSetDevice");
+  cuda_check(cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, device), "SM count");
   cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
   cur_ = stream_;
   pool_cap_ = size_t(4) << 20;  // 4 Mi doubles = 32 MB of operator matrices

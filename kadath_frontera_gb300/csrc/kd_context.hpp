@@ -51,6 +51,12 @@ class Context {
   ~Context();
 
   int device() const { return device_; }
+  // SMs the context's grid-wide kernels may spread over (the LU's sweeps,
+  // matvecs, cooperative panels and trailing updates): all of the device's
+  // unless a budget is set, so that contexts run side by side (concurrent
+  // instances) share the GPU instead of taking turns.
+  int sms() const { return (sm_budget_ > 0 && sm_budget_ < nsm_) ? sm_budget_ : nsm_; }
+  void set_sm_budget(int n) { sm_budget_ = n; }
   // The stream work is issued on: the context's main stream, or one of the
   // side streams between fork() and join().
   cudaStream_t stream() const { return cur_; }
@@ -138,6 +144,7 @@ class Context {
 
  private:
   int device_;
+  int nsm_ = 0, sm_budget_ = 0;
   cudaStream_t stream_ = nullptr;
   cudaStream_t cur_ = nullptr;
   std::vector<cudaStream_t> side_;

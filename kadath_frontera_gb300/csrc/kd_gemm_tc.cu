@@ -619,7 +619,8 @@ void tf32_gemm_update(Context* ctx, int m, int n, int k, const float* A, long lo
       ctx->launches += 1;
       return;
     }
-    const int grid = ntiles < nsm ? ntiles : nsm;
+    const int cap = ctx->sms() < nsm ? ctx->sms() : nsm;
+    const int grid = ntiles < cap ? ntiles : cap;
     tf32_update_persistent<<<grid, P_THREADS, psmem, s>>>(mA, mB, mAl, mBl, mC, nkb, ntm, ntiles, split3 ? 1 : 0, ncs,
                                                           err);
     ctx->launches += 1;

@@ -1518,7 +1518,7 @@ static bool panel_factor(Context* ctx, T* A, long long ld, int N, int j0, int jb
   if constexpr (std::is_same<T, float>::value) {
     if (panel_cluster16(ctx, A, ld, N, j0, jb, ipiv, info, swap_map)) return true;
   }
-  if (panel_grid<T>(ctx, A, ld, N, j0, jb, ipiv, info, nsm, slots)) return false;
+  if (panel_grid<T>(ctx, A, ld, N, j0, jb, ipiv, info, nsm < ctx->sms() ? nsm : ctx->sms(), slots)) return false;
   // Panels too tall for the shared memory of the GPU: one 8-CTA cluster
   // working on the panel in global memory.
   cudaLaunchConfig_t cfg = {};
@@ -1733,7 +1733,7 @@ void DenseLU::tri_solve(const T* LU, long long ld, int N, double* b, int trans) 
     gather_perm<<<blocks(N, 256), 256, 0, s>>>(b, perm_, N, w1);
     // L y = P b, then U x = y: one cooperative launch per sweep
     int g = blocks(N, SW_TILE);
-    if (g > nsm_) g = nsm_;
+    if (g > ctx_->sms()) g = ctx_->sms();
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(g, 1, 1);
     cfg.blockDim = dim3(256, 1, 1);
@@ -1844,7 +1844,7 @@ void DenseLU::gemv(const double* x, double* y, double alpha, double beta, const 
   const int N = N_;
   cudaStream_t s = ctx_->stream();
   const int rb = blocks(N, GEMV_ROWS);
-  int nchunk = (4 * nsm_ + rb - 1) / rb;
+  int nchunk = (4 * nsm_ + rb - 1) / rb;  // the device's SMs: the split of the sums stays fixed
   if (nchunk > 32) nchunk = 32;
   if (nchunk < 1) nchunk = 1;
   const int chunk = (N + nchunk - 1) / nchunk;

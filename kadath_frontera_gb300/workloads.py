@@ -186,19 +186,30 @@ def star_batch_configs(n, seed=0):
     return out
 
 
-def solve_batch(configs, threads, precision=1e-10, lu_mode=None, device=0, keep=True):
+def solve_batch(configs, threads, precision=1e-10, lu_mode=None, device=0, keep=True, sm_share=None):
     """Builds and solves every configuration, each instance on its own
     context (its own CUDA streams and workspaces) from a pool of `threads`
     host threads, so that instances overlap on the GPU.  Returns the
     converged workloads in configuration order, or with keep=False only
     their numbers of Newton updates (each instance's device memory is then
-    released as soon as it has converged)."""
+    released as soon as it has converged).  With several threads each
+    context's grid-wide solver kernels get sm_share SMs (default: the
+    device's SMs divided by the number of threads, at least 16), so that the
+    instances' factorisations and sweeps run side by side."""
     from concurrent.futures import ThreadPoolExecutor
+
+    if sm_share is None and threads > 1:
+        import torch
+        nsm = torch.cuda.get_device_properties(device).multi_processor_count
+        sm_share = max(16, nsm // threads)
 
     from ._lib import Context
 
     def one(cfg):
-        wl = star(res=cfg["res"], rho_c=cfg["rho_c"], ctx=Context(device))
+        ctx = Context(device)
+        if threads > 1 and sm_share:
+            ctx.set_sm_budget(sm_share)
+        wl = star(res=cfg["res"], rho_c=cfg["rho_c"], ctx=ctx)
         updates = solve(wl, precision, lu_mode)
         return wl if keep else updates
 
