@@ -189,6 +189,19 @@ int kd_system_get_var_double(const kd_system* s, const char* name, double* v);
 int kd_system_add_cst(kd_system* s, const char* name, double v);           /* add_cst(name, double) */
 int kd_system_add_cst_field(kd_system* s, const char* name, kd_field* f);  /* add_cst(name, Tensor) */
 int kd_system_add_def(kd_system* s, int dom, const char* text);            /* add_def; dom < 0: all */
+/* Cartesian vectors (add_var(name, Tensor&) / add_cst(name, const Tensor&)
+ * with a Vector of CARTESIAN_BASIS, src/System_of_eqs/system_of_eqs.cpp:404
+ * and :436): components x, y, z as three fields, each with its component's
+ * basis (kd_field_cart_base).  Equations write the vector with one index
+ * ("bet^i", "bet_j") or none.  Its unknowns follow xx_to_vars
+ * (system_of_eqs.cpp:597): domain by domain, the three components inside
+ * each domain. */
+int kd_system_add_var_vector(kd_system* s, const char* name, kd_field* fx, kd_field* fy, kd_field* fz);
+int kd_system_add_cst_vector(kd_system* s, const char* name, kd_field* fx, kd_field* fy, kd_field* fz);
+/* Metric_flat::set_system (src/Metric/metric_flat.cpp:501) with a Cartesian
+ * basis: D_i / D^i become the flat derivatives and `name` with two indices
+ * ("g_ij") the metric tensor.  A second metric is an error. */
+int kd_system_set_metric_flat(kd_system* s, const char* name);
 int kd_system_add_eq_inside(kd_system* s, int dom, const char* eq);        /* add_eq_inside */
 int kd_system_add_eq_bc(kd_system* s, int dom, int bound, const char* eq); /* add_eq_bc */
 int kd_system_add_eq_matching(kd_system* s, int dom, int bound, const char* eq); /* add_eq_matching */

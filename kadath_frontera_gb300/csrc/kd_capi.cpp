@@ -432,6 +432,29 @@ int kd_system_add_cst_field(kd_system* s, const char* name, kd_field* f) {
   });
 }
 
+int kd_system_add_var_vector(kd_system* s, const char* name, kd_field* fx, kd_field* fy, kd_field* fz) {
+  SYS_GUARD(s) {
+    if (!name || !fx || !fy || !fz) throw kd::KdError(KD_ERR_ARG, "null argument");
+    kd::Field* const comps[3] = {fx->f.get(), fy->f.get(), fz->f.get()};
+    s->sys->add_var_vector(name, comps);
+  });
+}
+
+int kd_system_add_cst_vector(kd_system* s, const char* name, kd_field* fx, kd_field* fy, kd_field* fz) {
+  SYS_GUARD(s) {
+    if (!name || !fx || !fy || !fz) throw kd::KdError(KD_ERR_ARG, "null argument");
+    kd::Field* const comps[3] = {fx->f.get(), fy->f.get(), fz->f.get()};
+    s->sys->add_cst_vector(name, comps);
+  });
+}
+
+int kd_system_set_metric_flat(kd_system* s, const char* name) {
+  SYS_GUARD(s) {
+    if (!name) throw kd::KdError(KD_ERR_ARG, "null name");
+    s->sys->set_metric_flat(name);
+  });
+}
+
 int kd_system_add_def(kd_system* s, int dom, const char* text) {
   SYS_GUARD(s) {
     if (!text) throw kd::KdError(KD_ERR_ARG, "null text");

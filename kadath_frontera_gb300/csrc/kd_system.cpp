@@ -194,7 +194,70 @@ Term EvalState::def_term(int which, int dom) {
   if (it != def_cache.end()) return it->second;
   const auto& df = sys->defs_.at(which);
   Term t = df.ope->eval(*this);
+  if (!df.idx.empty()) {
+    if (t.is_double || static_cast<int>(df.idx.size()) != t.valence)
+      throw KdError(KD_ERR_ARG, "the definition of " + df.name + " has " + std::to_string(df.idx.size()) +
+                                    " indices, its value another valence");
+    if (!t.idx.empty()) {
+      Term names;
+      names.idx = df.idx;
+      t = align_to(t, names);
+    }
+    t.idx = df.idx;
+  }
   def_cache[key] = t;
+  return t;
+}
+
+Term EvalState::var_vector_term(int first, int dom) {
+  Term t;
+  t.dom = dom;
+  t.valence = 1;
+  for (int c = 0; c < 3; c++) {
+    Term k = var_term(first + c, dom);
+    t.vt.push_back(k.vt[0]);
+    if (k.has_dt) {
+      t.has_dt = true;
+      t.dt.push_back(k.dt[0]);
+    }
+  }
+  return t;
+}
+
+Term EvalState::cst_vector_term(int first, int dom) {
+  Term t;
+  t.dom = dom;
+  t.valence = 1;
+  for (int c = 0; c < 3; c++) {
+    Term k = cst_term(first + c, dom);
+    t.vt.push_back(k.vt[0]);
+    if (k.has_dt) {
+      t.has_dt = true;
+      t.dt.push_back(k.dt[0]);
+    }
+  }
+  return t;
+}
+
+Term EvalState::metric_term(int dom) {
+  const Domain* dm = &sys->sp->dom(dom);
+  Term t;
+  t.dom = dom;
+  t.valence = 2;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      if (i == j) {
+        DVal one = DVal::constant(sys->ctx, dm, 1.0);
+        one.base = dm->std_base();
+        t.vt.push_back(one);
+      } else {
+        t.vt.push_back(DVal::zeros(sys->ctx, dm, 1));
+      }
+    }
+  if (with_der) {
+    t.has_dt = true;
+    for (int c = 0; c < 9; c++) t.dt.push_back(DVal::zeros(sys->ctx, dm, B));
+  }
   return t;
 }
 
@@ -205,6 +268,7 @@ void ValueCache::store(const Ope* node, const Term& t) {
   v.is_double = t.is_double;
   v.vd = t.vd;
   v.valence = t.valence;
+  v.idx = t.idx;
   v.vt = t.vt;
   for (auto& x : v.vt)
     if (!x.zero && !x.in_conf && x.base.def) x.coef_i();
@@ -351,7 +415,17 @@ class OpeSubEq : public Ope {
 
 int System::find_var(const std::string& n) const {
   for (size_t i = 0; i < vars_.size(); i++)
-    if (vars_[i].name == n) return static_cast<int>(i);
+    if (vars_[i].ncmp == 1 && vars_[i].name == n) return static_cast<int>(i);
+  return -1;
+}
+int System::find_var_vector(const std::string& n) const {
+  for (size_t i = 0; i < vars_.size(); i++)
+    if (vars_[i].ncmp == 3 && vars_[i].cmp == 0 && vars_[i].name == n) return static_cast<int>(i);
+  return -1;
+}
+int System::find_cst_vector(const std::string& n) const {
+  for (size_t i = 0; i < csts_.size(); i++)
+    if (csts_[i].ncmp == 3 && csts_[i].cmp == 0 && csts_[i].name == n) return static_cast<int>(i);
   return -1;
 }
 int System::find_var_double(const std::string& n) const {
@@ -361,7 +435,7 @@ int System::find_var_double(const std::string& n) const {
 }
 int System::find_cst(const std::string& n) const {
   for (size_t i = 0; i < csts_.size(); i++)
-    if (csts_[i].name == n) return static_cast<int>(i);
+    if (csts_[i].ncmp == 1 && csts_[i].name == n) return static_cast<int>(i);
   return -1;
 }
 int System::find_def(const std::string& n, int dom) const {
@@ -379,6 +453,37 @@ int System::add_var(const std::string& name, Field* f) {
   vars_.push_back({bare(name), f});
   nbr_unknowns_ = -1;
   return static_cast<int>(vars_.size()) - 1;
+}
+
+int System::add_var_vector(const std::string& name, Field* const comps[3]) {
+  if (name.find('_') != std::string::npos || name.find('^') != std::string::npos)
+    throw KdError(KD_ERR_ARG, "No indices allowed in names of variables");
+  for (int c = 0; c < 3; c++)
+    for (int dd = dom_min; dd <= dom_max; dd++)
+      if (!comps[c]->d[dd].base.def) throw KdError(KD_ERR_STATE, "vector component without a basis (call std_base)");
+  tcache_.clear();
+  const int first = static_cast<int>(vars_.size());
+  for (int c = 0; c < 3; c++) vars_.push_back({bare(name), comps[c], 3, c});
+  nbr_unknowns_ = -1;
+  return first;
+}
+
+int System::add_cst_vector(const std::string& name, Field* const comps[3]) {
+  if (name.find('_') != std::string::npos || name.find('^') != std::string::npos)
+    throw KdError(KD_ERR_ARG, "No indices allowed in names of constants");
+  tcache_.clear();
+  const int first = static_cast<int>(csts_.size());
+  for (int c = 0; c < 3; c++) csts_.push_back({bare(name), true, 0.0, comps[c], 3, c});
+  return first;
+}
+
+void System::set_metric_flat(const std::string& name) {
+  const std::string n = bare(name);
+  if (n.empty() || n.find('_') != std::string::npos || n.find('^') != std::string::npos)
+    throw KdError(KD_ERR_ARG, "bad name for the metric");
+  if (!metric_.empty()) throw KdError(KD_ERR_STATE, "Metric already set for the system");
+  tcache_.clear();
+  metric_ = n;
 }
 
 int System::add_var_double(const std::string& name, double value) {
@@ -407,7 +512,19 @@ void System::add_def(int dom, const std::string& text) {
     for (int dd = dom_min; dd <= dom_max; dd++) add_def(dd, text);
     return;
   }
-  DefInfo df{bare(l), dom, parse_ope(*this, dom, r, -1)};
+  // "A_ij": the name, then the index letters after '_' / '^' (is_tensor,
+  // src/Utilities/name_tools.cpp:187)
+  std::string nm = bare(l), idx;
+  const size_t p = nm.find_first_of("_^");
+  if (p != std::string::npos) {
+    for (size_t i = p; i < nm.size(); i++)
+      if (nm[i] != '_' && nm[i] != '^') idx.push_back(nm[i]);
+    nm = nm.substr(0, p);
+    for (size_t i = 0; i < idx.size(); i++)
+      if (idx.find(idx[i], i + 1) != std::string::npos)
+        throw KdError(KD_ERR_ARG, "repeated index on the left of a definition");
+  }
+  DefInfo df{nm, dom, parse_ope(*this, dom, r, -1), idx};
   tcache_.clear();  // a new symbol changes the trees that can follow
   defs_.push_back(df);
 }
@@ -642,14 +759,18 @@ void System::compute_unknowns() {
   col0_.clear();
   nunk_.clear();
   int n = static_cast<int>(vdoubles_.size());
-  for (size_t v = 0; v < vars_.size(); v++)
-    for (int dd = dom_min; dd <= dom_max; dd++) {
-      std::vector<SparseRow> pats;
-      sp->dom(dd).unknown_patterns(vars_[v].f->d[dd].base, 0, pats);
-      col0_[{static_cast<int>(v), dd}] = n;
-      nunk_[{static_cast<int>(v), dd}] = static_cast<int>(pats.size());
-      n += static_cast<int>(pats.size());
-    }
+  // xx_to_vars (system_of_eqs.cpp:597): variable by variable, domain by
+  // domain; a vector's components are consecutive inside each domain
+  for (size_t v = 0; v < vars_.size(); v += vars_[v].ncmp)
+    for (int dd = dom_min; dd <= dom_max; dd++)
+      for (int c = 0; c < vars_[v].ncmp; c++) {
+        const int w = static_cast<int>(v) + c;
+        std::vector<SparseRow> pats;
+        sp->dom(dd).unknown_patterns(vars_[w].f->d[dd].base, 0, pats);
+        col0_[{w, dd}] = n;
+        nunk_[{w, dd}] = static_cast<int>(pats.size());
+        n += static_cast<int>(pats.size());
+      }
   nbr_unknowns_ = n;
 }
 

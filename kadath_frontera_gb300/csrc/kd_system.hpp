@@ -124,6 +124,11 @@ struct EvalState {
   Term var_double_term(int which, int dom);
   Term cst_term(int which, int dom);
   Term def_term(int which, int dom);
+  // Cartesian vectors: the three component entries from `first` on.
+  Term var_vector_term(int first, int dom);
+  Term cst_vector_term(int first, int dom);
+  // The flat metric g_ij = delta_ij (Metric_flat with a Cartesian basis).
+  Term metric_term(int dom);
 };
 
 struct Equation {
@@ -164,6 +169,19 @@ class System {
   int add_var_double(const std::string& name, double value);
   int add_cst(const std::string& name, double value);
   int add_cst_field(const std::string& name, Field* f);
+  // A Cartesian vector unknown or constant (add_var / add_cst with a Vector
+  // of Cartesian basis): three fields, components x, y, z, each with the
+  // basis of its component.  Equations name it with one index ("bet^i").
+  // Its unknowns come domain by domain, the three components inside each
+  // domain (xx_to_vars and affecte_tau of a Tensor).
+  int add_var_vector(const std::string& name, Field* const comps[3]);
+  int add_cst_vector(const std::string& name, Field* const comps[3]);
+  // Metric_flat::set_system: D_i / D^i become the flat covariant
+  // derivatives and `name` (with two indices) the metric tensor.
+  void set_metric_flat(const std::string& name);
+  bool has_metric() const { return !metric_.empty(); }
+  const std::string& metric_name() const { return metric_; }
+  // "A_ij = ..." defines a tensor whose index order is the left side's.
   void add_def(int dom, const std::string& text);
   void add_eq_inside(int dom, const std::string& eq);
   void add_eq_bc(int dom, int bound, const std::string& eq);
@@ -186,6 +204,8 @@ class System {
   int find_var_double(const std::string& n) const;
   int find_cst(const std::string& n) const;
   int find_def(const std::string& n, int dom) const;
+  int find_var_vector(const std::string& n) const;
+  int find_cst_vector(const std::string& n) const;
 
   // User-defined operators of the EOS kind (System_of_eqs::add_ope with
   // EOS<eos, var>::action, include/system_of_eqs.hpp:277): name(h) gives var
@@ -248,6 +268,8 @@ class System {
   struct VarInfo {
     std::string name;
     Field* f;
+    int ncmp = 1;  // 3 for the components of a vector
+    int cmp = 0;   // component 0, 1, 2 of a vector
   };
   struct VarDouble {
     std::string name;
@@ -258,11 +280,14 @@ class System {
     bool is_field;
     double value;
     Field* f;
+    int ncmp = 1;
+    int cmp = 0;
   };
   struct DefInfo {
     std::string name;
     int dom;
     OpePtr ope;
+    std::string idx;  // index names of the left side, in order
   };
   const std::vector<VarInfo>& vars() const { return vars_; }
 
@@ -284,6 +309,7 @@ class System {
   std::vector<UserOpe> user_opes_;
   std::vector<Equation> eqs_;
   std::vector<IntEquation> ieqs_;
+  std::string metric_;
   int nbr_conditions_ = -1;
   int nbr_unknowns_ = -1;
   std::map<std::pair<int, int>, int> col0_, nunk_;

@@ -1,5 +1,6 @@
 #include "kd_term.hpp"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 
@@ -32,6 +33,7 @@ Term tensor_like(const Term& t) {
   Term r;
   r.dom = t.dom;
   r.valence = t.valence;
+  r.idx = t.idx;
   return r;
 }
 
@@ -40,6 +42,141 @@ int ncomp(const Term& t) { return static_cast<int>(t.vt.size()); }
 void check_valence(const Term& a, const Term& b) {
   if (a.vt.size() != b.vt.size())
     throw KdError(KD_ERR_UNSUPPORTED, "tensor operation between different valences");
+}
+
+int pow3(int n) {
+  int r = 1;
+  for (int i = 0; i < n; i++) r *= 3;
+  return r;
+}
+
+// Component position of multi-index m (row-major, 3 values per index).
+int flat_index(const int* m, int n) {
+  int f = 0;
+  for (int i = 0; i < n; i++) f = 3 * f + m[i];
+  return f;
+}
+
+void unflatten(int f, int n, int* m) {
+  for (int i = n - 1; i >= 0; i--) {
+    m[i] = f % 3;
+    f /= 3;
+  }
+}
+
+}  // namespace
+
+// b's components in the index order of a (sums of named tensors with the
+// same indices in another order, as Ope_add/Ope_sub match name_ind).
+Term align_to(const Term& b, const Term& a) {
+  if (a.idx.empty() || b.idx.empty() || a.idx == b.idx) return b;
+  const int n = static_cast<int>(a.idx.size());
+  std::string sa = a.idx, sb = b.idx;
+  std::sort(sa.begin(), sa.end());
+  std::sort(sb.begin(), sb.end());
+  if (sa != sb || static_cast<int>(b.idx.size()) != n)
+    throw KdError(KD_ERR_ARG, "sum of tensors with different indices: " + a.idx + " and " + b.idx);
+  int where[8];
+  for (int i = 0; i < n; i++) where[i] = static_cast<int>(b.idx.find(a.idx[i]));
+  Term r = b;
+  r.idx = a.idx;
+  int ma[8], mb[8];
+  for (int f = 0; f < pow3(n); f++) {
+    unflatten(f, n, ma);
+    for (int i = 0; i < n; i++) mb[where[i]] = ma[i];
+    const int g = flat_index(mb, n);
+    r.vt[f] = b.vt[g];
+    if (b.has_dt) r.dt[f] = b.dt[g];
+  }
+  return r;
+}
+
+// Sum over every index name that appears twice in t (Einstein convention,
+// flat metric): the terms in the order 1, 2, 3 of the repeated index.
+Term contract_self(const Term& t) {
+  const int n = static_cast<int>(t.idx.size());
+  int p = -1, q = -1;
+  for (int i = 0; i < n && p < 0; i++)
+    for (int j = i + 1; j < n; j++)
+      if (t.idx[i] == t.idx[j]) {
+        p = i;
+        q = j;
+        break;
+      }
+  if (p < 0) return t;
+  Term r;
+  r.dom = t.dom;
+  for (int i = 0; i < n; i++)
+    if (i != p && i != q) r.idx.push_back(t.idx[i]);
+  r.valence = n - 2;
+  r.has_dt = t.has_dt;
+  int mr[8], mt[8];
+  for (int f = 0; f < pow3(n - 2); f++) {
+    unflatten(f, n - 2, mr);
+    for (int i = 0, k = 0; i < n; i++)
+      if (i != p && i != q) mt[i] = mr[k++];
+    DVal v, d;
+    for (int c = 0; c < 3; c++) {
+      mt[p] = mt[q] = c;
+      const int g = flat_index(mt, n);
+      v = (c == 0) ? t.vt[g] : v + t.vt[g];
+      if (t.has_dt) d = (c == 0) ? t.dt[g] : d + t.dt[g];
+    }
+    r.vt.push_back(v);
+    if (t.has_dt) r.dt.push_back(d);
+  }
+  return contract_self(r);
+}
+
+namespace {
+
+// Product of two named tensors: outer product, then the sum over the index
+// names the two share; value sum_c a_c b_c and tangent sum_c (a'_c b_c +
+// a_c b'_c), the terms in the order of the contracted components.
+Term tensor_product(const Term& a, const Term& b, const Term* cv, bool do_der) {
+  if (a.idx.empty() || b.idx.empty())
+    throw KdError(KD_ERR_UNSUPPORTED, "product of two non-scalar tensors without index names: use scal()");
+  const int na = static_cast<int>(a.idx.size()), nb = static_cast<int>(b.idx.size());
+  std::string free_a, free_b, shared;
+  for (char c : a.idx)
+    if (b.idx.find(c) == std::string::npos) free_a.push_back(c);
+    else shared.push_back(c);
+  for (char c : b.idx)
+    if (a.idx.find(c) == std::string::npos) free_b.push_back(c);
+  Term r;
+  r.dom = a.dom;
+  r.idx = free_a + free_b;
+  r.valence = static_cast<int>(r.idx.size());
+  r.has_dt = do_der;
+  const int nr = r.valence, ns = static_cast<int>(shared.size());
+  int mr[8], ms[8], ma[8], mb[8];
+  for (int f = 0; f < pow3(nr); f++) {
+    unflatten(f, nr, mr);
+    DVal v, d;
+    for (int g = 0; g < pow3(ns); g++) {
+      unflatten(g, ns, ms);
+      auto value_of = [&](char c) {
+        size_t k = r.idx.find(c);
+        if (k != std::string::npos) return mr[k];
+        return ms[shared.find(c)];
+      };
+      for (int i = 0; i < na; i++) ma[i] = value_of(a.idx[i]);
+      for (int i = 0; i < nb; i++) mb[i] = value_of(b.idx[i]);
+      const int ia = flat_index(ma, na), ib = flat_index(mb, nb);
+      if (!cv) {
+        DVal pv = a.vt[ia] * b.vt[ib];
+        v = (g == 0) ? pv : v + pv;
+      }
+      if (do_der) {
+        DVal pd = a.dt[ia] * b.vt[ib] + a.vt[ia] * b.dt[ib];
+        d = (g == 0) ? pd : d + pd;
+      }
+    }
+    if (!cv) r.vt.push_back(v);
+    if (do_der) r.dt.push_back(d);
+  }
+  if (cv) r.vt = cv->vt;
+  return r;
 }
 
 }  // namespace
@@ -92,13 +229,14 @@ Term t_add(const Term& a, const Term& b, const Term* cv) {
     return r;
   }
   check_valence(a, b);
+  const Term bb = align_to(b, a);
   Term r = tensor_like(a);
   if (cv) r.vt = cv->vt;
   else
-    for (int i = 0; i < ncomp(a); i++) r.vt.push_back(a.vt[i] + b.vt[i]);
+    for (int i = 0; i < ncomp(a); i++) r.vt.push_back(a.vt[i] + bb.vt[i]);
   if (do_der) {
     r.has_dt = true;
-    for (int i = 0; i < ncomp(a); i++) r.dt.push_back(a.dt[i] + b.dt[i]);
+    for (int i = 0; i < ncomp(a); i++) r.dt.push_back(a.dt[i] + bb.dt[i]);
   }
   return r;
 }
@@ -136,13 +274,14 @@ Term t_sub(const Term& a, const Term& b, const Term* cv) {
     return r;
   }
   check_valence(a, b);
+  const Term bb = align_to(b, a);
   Term r = tensor_like(a);
   if (cv) r.vt = cv->vt;
   else
-    for (int i = 0; i < ncomp(a); i++) r.vt.push_back(a.vt[i] - b.vt[i]);
+    for (int i = 0; i < ncomp(a); i++) r.vt.push_back(a.vt[i] - bb.vt[i]);
   if (do_der) {
     r.has_dt = true;
-    for (int i = 0; i < ncomp(a); i++) r.dt.push_back(a.dt[i] - b.dt[i]);
+    for (int i = 0; i < ncomp(a); i++) r.dt.push_back(a.dt[i] - bb.dt[i]);
   }
   return r;
 }
@@ -191,8 +330,7 @@ Term t_mul(const Term& a, const Term& b, const Term* cv) {
     }
     return r;
   }
-  if (a.vt.size() != 1 && b.vt.size() != 1)
-    throw KdError(KD_ERR_UNSUPPORTED, "product of two non-scalar tensors: use scal()");
+  if (a.vt.size() != 1 && b.vt.size() != 1) return tensor_product(a, b, cv, do_der);
   const Term& s = (a.vt.size() == 1) ? a : b;
   const Term& t = (a.vt.size() == 1) ? b : a;
   bool s_first = (&s == &a);
@@ -639,6 +777,67 @@ class OpePartial : public Ope {
   OpePtr a;
 };
 
+// D_i / D^i of the flat metric (Metric_flat::derive_partial_cart,
+// src/Metric/metric_flat.cpp:150) and partial_i (Ope_partial): the Cartesian
+// derivative of every component, the derivative index first.  When the
+// derivative index repeats one of the operand's, that pair is summed over
+// (the divergence), term by term in the order 1, 2, 3 of the index; only
+// the summed components are differentiated.  Upper and lower indices share
+// their components in a flat Cartesian frame.
+class OpeDer : public Ope {
+ public:
+  OpeDer(int dom, char ind, OpePtr a_) : Ope(dom), ind(ind), a(std::move(a_)) {
+    vc = a->vc;
+    dc = a->dc;
+    dz = a->dz;
+  }
+  std::vector<const Ope*> kids() const override { return {a.get()}; }
+  Term action(EvalState& st, const Term* cv) const override {
+    Term t = a->eval(st);
+    if (t.is_double) throw KdError(KD_ERR_UNSUPPORTED, "derivative of a number");
+    // names only when the operand has them (or is a scalar), as donames
+    const bool names = !t.idx.empty() || t.valence == 0;
+    const size_t p = names ? t.idx.find(ind) : std::string::npos;
+    const int n = ncomp(t);
+    Term r;
+    r.dom = t.dom;
+    r.has_dt = t.has_dt;
+    if (p == std::string::npos) {
+      r.valence = t.valence + 1;
+      if (names) r.idx = std::string(1, ind) + t.idx;
+      for (int k = 1; k <= 3; k++)
+        for (int c = 0; c < n; c++) {
+          if (!cv) r.vt.push_back(t.vt[c].der_abs(k));
+          if (t.has_dt) r.dt.push_back(t.dt[c].der_abs(k));
+        }
+    } else {
+      const int pp = static_cast<int>(p), nt = t.valence;
+      r.valence = nt - 1;
+      r.idx = t.idx;
+      r.idx.erase(p, 1);
+      int mr[8], mt[8];
+      for (int f = 0; f < pow3(nt - 1); f++) {
+        unflatten(f, nt - 1, mr);
+        for (int i = 0, k = 0; i < nt; i++)
+          if (i != pp) mt[i] = mr[k++];
+        DVal v, d;
+        for (int c = 0; c < 3; c++) {
+          mt[pp] = c;
+          const int g = flat_index(mt, nt);
+          if (!cv) v = (c == 0) ? t.vt[g].der_abs(c + 1) : v + t.vt[g].der_abs(c + 1);
+          if (t.has_dt) d = (c == 0) ? t.dt[g].der_abs(c + 1) : d + t.dt[g].der_abs(c + 1);
+        }
+        if (!cv) r.vt.push_back(v);
+        if (t.has_dt) r.dt.push_back(d);
+      }
+    }
+    if (cv) r.vt = cv->vt;
+    return r;
+  }
+  char ind;
+  OpePtr a;
+};
+
 // User-defined EOS operator: Ope_user with EOS<eos, var>::action
 // (include/EOS/EOS.hh:235-270).  The tangent depends on the value.
 class OpeEos : public Ope {
@@ -669,27 +868,42 @@ class OpeEos : public Ope {
 
 class OpeLeaf : public Ope {
  public:
-  enum Kind { VAR, VAR_DOUBLE, CST, HARD, DEF };
-  OpeLeaf(int dom, Kind k, int which, double v = 0.0) : Ope(dom), kind(k), which(which), val(v) {
-    // unknowns: tangent = the seed (or 0); constants: zero tangent; numbers:
-    // constant value; definitions: not classified
-    vc = (k == HARD);
+  enum Kind { VAR, VAR_DOUBLE, CST, HARD, DEF, VAR_VECTOR, CST_VECTOR, METRIC };
+  OpeLeaf(int dom, Kind k, int which, double v = 0.0, std::string idx = std::string())
+      : Ope(dom), kind(k), which(which), val(v), idx(std::move(idx)) {
+    // unknowns: tangent = the seed (or 0); constants: zero tangent; numbers
+    // and the metric: constant value; definitions: not classified
+    vc = (k == HARD || k == METRIC);
     dc = (k != DEF);
-    dz = (k == CST || k == HARD);
+    dz = (k == CST || k == HARD || k == CST_VECTOR || k == METRIC);
   }
   Term action(EvalState& st, const Term* cv) const override;
   bool cacheable() const override { return false; }
   Kind kind;
   int which;
   double val;
+  // index names written after the symbol ("bet^i", "A_ij"): given to the
+  // tensor in order, then repeated names summed (Ope_id with name_ind)
+  std::string idx;
 };
+
+Term name_indices(Term t, const std::string& idx) {
+  if (idx.empty()) return t;
+  if (t.is_double || t.valence != static_cast<int>(idx.size()))
+    throw KdError(KD_ERR_ARG, "wrong number of indices: " + idx);
+  t.idx = idx;
+  return contract_self(t);
+}
 
 Term OpeLeaf::action(EvalState& st, const Term*) const {
   switch (kind) {
     case VAR: return st.var_term(which, dom);
     case VAR_DOUBLE: return st.var_double_term(which, dom);
     case CST: return st.cst_term(which, dom);
-    case DEF: return st.def_term(which, dom);
+    case DEF: return name_indices(st.def_term(which, dom), idx);
+    case VAR_VECTOR: return name_indices(st.var_vector_term(which, dom), idx);
+    case CST_VECTOR: return name_indices(st.cst_vector_term(which, dom), idx);
+    case METRIC: return name_indices(st.metric_term(dom), idx);
     default: {
       Term t = Term::dbl(dom, val);
       if (st.with_der) {
@@ -880,6 +1094,14 @@ OpePtr parse_ope(const System& sys, int dd, const std::string& expr, int bound) 
     std::string pn = std::string("partial_") + "xyz"[i];
     if (is_ope_uni(name, p1, pn)) return std::make_shared<OpePartial>(dd, i + 1, parse_ope(sys, dd, p1, bound));
   }
+  // D_i X, D^i X (is_ope_deriv, give_ope.cpp:385) and partial_i X
+  // (is_ope_partial, give_ope.cpp:491): one index letter, then the operand
+  if (name.size() > 3 && name[0] == 'D' && (name[1] == '_' || name[1] == '^') && name[2] != ' ') {
+    if (!sys.has_metric()) throw KdError(KD_ERR_ARG, "D_i needs a metric (Metric_flat::set_system): " + name);
+    return std::make_shared<OpeDer>(dd, name[2], parse_ope(sys, dd, name.substr(3), bound));
+  }
+  if (name.size() > 9 && name.compare(0, 8, "partial_") == 0 && name[8] != ' ')
+    return std::make_shared<OpeDer>(dd, name[8], parse_ope(sys, dd, name.substr(9), bound));
   // integer power: split at the last '^' (is_ope_pow, give_ope.cpp:519)
   if (count_char(name, '^') >= 1) {
     if (get_parts(name, p1, p2, '^', 0)) {
@@ -903,6 +1125,29 @@ OpePtr parse_ope(const System& sys, int dd, const std::string& expr, int bound) 
   if (is_double_str(name, v)) return std::make_shared<OpeLeaf>(dd, OpeLeaf::HARD, -1, v);
   which = sys.find_def(bare, dd);
   if (which >= 0) return std::make_shared<OpeLeaf>(dd, OpeLeaf::DEF, which);
+  // tensors, with or without index names (is_tensor, name_tools.cpp:187):
+  // one word, the name up to the first '_' or '^', then the index letters
+  if (bare.find(' ') == std::string::npos) {
+    std::string base = bare, idx;
+    const size_t p = bare.find_first_of("_^");
+    if (p != std::string::npos) {
+      base = bare.substr(0, p);
+      for (size_t i = p; i < bare.size(); i++)
+        if (bare[i] != '_' && bare[i] != '^') idx.push_back(bare[i]);
+    }
+    if (!base.empty()) {
+      which = sys.find_var_vector(base);
+      if (which >= 0) return std::make_shared<OpeLeaf>(dd, OpeLeaf::VAR_VECTOR, which, 0.0, idx);
+      if (sys.has_metric() && base == sys.metric_name() && idx.size() == 2)
+        return std::make_shared<OpeLeaf>(dd, OpeLeaf::METRIC, -1, 0.0, idx);
+      which = sys.find_cst_vector(base);
+      if (which >= 0) return std::make_shared<OpeLeaf>(dd, OpeLeaf::CST_VECTOR, which, 0.0, idx);
+      if (!idx.empty()) {
+        which = sys.find_def(base, dd);
+        if (which >= 0) return std::make_shared<OpeLeaf>(dd, OpeLeaf::DEF, which, 0.0, idx);
+      }
+    }
+  }
   // user-defined operators come last, as in give_ope.cpp:1107
   for (const auto& u : sys.user_opes())
     if (is_ope_uni(name, p1, u.name.c_str()))

@@ -27,8 +27,12 @@ struct Term {
   const double* ddv = nullptr;
   int ddb = 0;
   Context* ddctx = nullptr;
-  // tensor data: valence 0 (one component) or 1 (three Cartesian components)
+  // tensor data: 3^valence Cartesian components, row-major over the indices
   int valence = 0;
+  // index names, one letter per index (Kadath's name_ind), when the tensor
+  // came from index notation ("bet^i", "D_j ..."); empty otherwise.  With
+  // the flat Cartesian metric, upper and lower indices share components.
+  std::string idx;
   std::vector<DVal> vt;
   bool has_dt = false;
   std::vector<DVal> dt;
@@ -65,6 +69,13 @@ Term term_pow(const Term& a, int n, const Term* cv = nullptr);
 // r's tangent = ca a' + cb b' for doubles a and b (b may be null); per seed
 // when either operand's tangent is.
 void dbl_tangent_lincomb(Term& r, double ca, const Term& a, double cb, const Term* b);
+
+// b's components reordered to a's index names (both named, same letters);
+// b itself when either has no names.
+Term align_to(const Term& b, const Term& a);
+// Sums over every index name that appears twice (flat metric), the terms in
+// the order 1, 2, 3 of the summed index (Tensor::do_summation_one_dom).
+Term contract_self(const Term& t);
 
 class System;
 struct EvalState;

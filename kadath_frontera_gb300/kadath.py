@@ -76,6 +76,9 @@ def _declare_system(lib):
         "kd_system_add_cst": (I, [P, C.c_char_p, D]),
         "kd_system_add_cst_field": (I, [P, C.c_char_p, P]),
         "kd_system_add_def": (I, [P, I, C.c_char_p]),
+        "kd_system_add_var_vector": (I, [P, C.c_char_p, P, P, P]),
+        "kd_system_add_cst_vector": (I, [P, C.c_char_p, P, P, P]),
+        "kd_system_set_metric_flat": (I, [P, C.c_char_p]),
         "kd_system_add_eq_inside": (I, [P, I, C.c_char_p]),
         "kd_system_add_eq_bc": (I, [P, I, I, C.c_char_p]),
         "kd_system_add_eq_matching": (I, [P, I, I, C.c_char_p]),
@@ -310,6 +313,56 @@ class Scalar:
             pass
 
 
+CARTESIAN_BASIS = 0
+
+
+class Vector:
+    """Vector(space, CARTESIAN_BASIS): three Scalar components, v(1) = x,
+    v(2) = y, v(3) = z (Tensor with valence 1, include/tensor.hpp)."""
+
+    def __init__(self, space: Space_spheric, type_tensor=None, basis=CARTESIAN_BASIS):
+        if basis != CARTESIAN_BASIS:
+            raise KadathError(_lib.KD_ERR_UNSUPPORTED, "only the Cartesian tensorial basis is supported")
+        self.space = space
+        self.cmp = [Scalar(space) for _ in range(3)]
+
+    def __call__(self, i):
+        return self.cmp[i - 1]
+
+    def set(self, i):
+        return self.cmp[i - 1]
+
+    def std_base(self):
+        """Each component gets the basis of its Cartesian component."""
+        for c in range(3):
+            self.cmp[c].std_base_cart(c + 1)
+        return self
+
+    def set_value(self, v):
+        for c in self.cmp:
+            c.set_value(v)
+        return self
+
+    def copy_from(self, other: "Vector"):
+        for a, b in zip(self.cmp, other.cmp):
+            a.copy_from(b)
+        return self
+
+
+class Metric_flat:
+    """Metric_flat(space, basis) with a Cartesian basis; set_system(syst,
+    name) gives the system its covariant derivatives D_i / D^i and the
+    metric tensor `name` (src/Metric/metric_flat.cpp:501)."""
+
+    def __init__(self, space: Space_spheric, basis=CARTESIAN_BASIS):
+        if basis != CARTESIAN_BASIS:
+            raise KadathError(_lib.KD_ERR_UNSUPPORTED, "only the Cartesian tensorial basis is supported")
+        self.space = space
+
+    def set_system(self, syst: "System_of_eqs", name):
+        syst.ctx.check(_L().kd_system_set_metric_flat(syst.h, name.encode()))
+
+
 class System_of_eqs:
     """System_of_eqs(space, dom_min, dom_max)."""
 
@@ -339,6 +392,9 @@ class System_of_eqs:
         if isinstance(field, Scalar):
             self._keep.append(field)
             self.ctx.check(_L().kd_system_add_var(self.h, name.encode(), field.h))
+        elif isinstance(field, Vector):
+            self._keep.append(field)
+            self.ctx.check(_L().kd_system_add_var_vector(self.h, name.encode(), *[c.h for c in field.cmp]))
         else:
             self.ctx.check(_L().kd_system_add_var_double(self.h, name.encode(), float(field)))
 
@@ -351,6 +407,9 @@ class System_of_eqs:
         if isinstance(value, Scalar):
             self._keep.append(value)
             self.ctx.check(_L().kd_system_add_cst_field(self.h, name.encode(), value.h))
+        elif isinstance(value, Vector):
+            self._keep.append(value)
+            self.ctx.check(_L().kd_system_add_cst_vector(self.h, name.encode(), *[c.h for c in value.cmp]))
         else:
             self.ctx.check(_L().kd_system_add_cst(self.h, name.encode(), float(value)))
 

@@ -150,7 +150,58 @@ def star(res=(13, 9, 4), bounds=STAR_BOUNDS, ctx=None, rho_c=STAR_RHOC) -> Workl
     return Workload("star", space, syst, unknowns, [E, E2S])
 
 
-WORKLOADS = {"toy": toy, "star": star}
+STAR_VECTOR_EQUATIONS = {
+    "P": "Lap(P) + 2*pi*E/P = 0",
+    "NP": "Lap(NP) - 2*pi*NP*E2S/P^2 = 0",
+    "bet": "D_j D^j bet^i + D^i D_j bet^j / 3 = 0",
+}
+
+
+def star_vector(res=(13, 9, 4), bounds=STAR_BOUNDS, ctx=None, rho_c=STAR_RHOC) -> Workload:
+    """The star with the shift as one Cartesian vector unknown ``bet`` and its
+    equation in index notation with the flat metric: the form Kadath codes
+    write.  Same fields and matter as ``star``; the unknowns of bet come
+    domain by domain, x, y, z inside each domain."""
+    from .kadath import Metric_flat, Vector
+    space = Space_spheric(CHEB_TYPE, (0, 0, 0), res, bounds, ctx=ctx)
+    nd = space.get_nbr_domains()
+    P = Scalar(space, 1.0).std_base()
+    NP = Scalar(space, 1.0).std_base()
+    bet = Vector(space).std_base()
+    for c in (1, 2, 3):
+        for d in range(nd):
+            bet(c).set_domain(d, np.zeros(space.domain_info(d)["nbr_points"]))
+    E = Scalar(space)
+    E2S = Scalar(space)
+    for d in range(nd):
+        e, e2s = star_matter_values(space.get_radius(d), space.domain_info(d)["type"] == 1, rho_c)
+        E.set_domain(d, e)
+        E2S.set_domain(d, e2s)
+    E.std_base()
+    E2S.std_base()
+    syst = System_of_eqs(space, 0, nd - 1)
+    Metric_flat(space).set_system(syst, "f")
+    syst.add_var("P", P)
+    syst.add_var("NP", NP)
+    syst.add_var("bet", bet)
+    syst.add_cst("pi", math.pi)
+    syst.add_cst("E", E)
+    syst.add_cst("E2S", E2S)
+    for d in range(nd):
+        for nm in ("P", "NP", "bet"):
+            syst.add_eq_inside(d, STAR_VECTOR_EQUATIONS[nm])
+    for d in range(nd - 1):
+        for nm in ("P", "NP", "bet^i"):
+            syst.add_eq_matching(d, OUTER_BC, nm)
+            syst.add_eq_matching(d, OUTER_BC, f"dn({nm})")
+    syst.add_eq_bc(nd - 1, OUTER_BC, "P = 1")
+    syst.add_eq_bc(nd - 1, OUTER_BC, "NP = 1")
+    syst.add_eq_bc(nd - 1, OUTER_BC, "bet^i = 0")
+    unknowns = [("P", P), ("NP", NP), ("bet_x", bet(1)), ("bet_y", bet(2)), ("bet_z", bet(3))]
+    return Workload("star_vector", space, syst, unknowns, [E, E2S])
+
+
+WORKLOADS = {"toy": toy, "star": star, "star_vector": star_vector}
 
 
 def solve(wl: Workload, precision=1e-10, lu_mode=None, max_steps=20) -> int:

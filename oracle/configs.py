@@ -154,6 +154,66 @@ def star(res=(13, 9, 4), bounds=(STAR_R, 12.0, 16.0, 24.0, 32.0)):
     return doms, sysm, (P, NP, bx, by, bz), (E, E2S)
 
 
+def star_vector(res=(13, 9, 4), bounds=(STAR_R, 12.0, 16.0, 24.0, 32.0)):
+    """The static star with the shift as one Cartesian vector unknown bet and
+    its equations in index notation with the flat metric, as the product
+    parses them:
+      D_j D^j bet^i + D^i D_j bet^j / 3 = 0,  bet^i and dn(bet^i) matched,
+      bet^i = 0 at infinity.
+    D_j D^j X^i is sum_j d_j(d_j X^i) and D_j X^j is sum_j d_j X^j, each sum
+    in the order j = 1, 2, 3 (Metric_flat::derive_partial_cart, then
+    Tensor::do_summation_one_dom).  The unknowns of bet come domain by domain,
+    x, y, z inside each domain (xx_to_vars)."""
+    doms, _, (P, NP, bx, by, bz), (E, E2S) = star(res, bounds)
+    nd = len(doms)
+    sysm = K.OSystem(doms, 0, nd - 1)
+    sysm.add_var("P", P)
+    sysm.add_var("NP", NP)
+    sysm.add_var_vector("bet", (bx, by, bz))
+    two_pi = 2 * math.pi
+
+    def cst(T, v):
+        p = T["P"]
+        return K.OTerm(p.dom, v, None if p.der is None else K.VD.zeros(v.dom, p.der.B))
+
+    def num(T, x):
+        return K.OTerm(T["P"].dom, float(x), None if T["P"].der is None else 0.0)
+
+    def shift_eq(T, b):
+        bet = T["bet"]
+        div = bet[0].partial(1) + bet[1].partial(2) + bet[2].partial(3)
+        out = []
+        for i in range(3):
+            d2 = [bet[i].partial(j).partial(j) for j in (1, 2, 3)]
+            out.append((d2[0] + d2[1] + d2[2]) + div.partial(i + 1) / num(T, 3.0))
+        return out
+
+    for d in range(nd):
+        Ed, E2Sd = E[d], E2S[d]
+        sysm.add_eq_inside(d, lambda T, b, Ed=Ed: T["P"].lap() + num(T, two_pi) * (cst(T, Ed) / T["P"]))
+        sysm.add_eq_inside(d, lambda T, b, E2Sd=E2Sd: T["NP"].lap() - (num(T, two_pi) * T["NP"]) *
+                           (cst(T, E2Sd) / T["P"] ** 2))
+        sysm.add_eq_inside(d, shift_eq)
+    for d in range(nd - 1):
+        for name in ("P", "NP"):
+            sysm.add_eq_matching(d, K.OUTER_BC, lambda T, b, name=name: T[name])
+            sysm.add_eq_matching(d, K.OUTER_BC, lambda T, b, name=name: T[name].dn(b))
+        sysm.add_eq_matching(d, K.OUTER_BC, lambda T, b: list(T["bet"]))
+        sysm.add_eq_matching(d, K.OUTER_BC, lambda T, b: [x.dn(b) for x in T["bet"]])
+    sysm.add_eq_bc(nd - 1, K.OUTER_BC, lambda T, b: T["P"] - 1.0)
+    sysm.add_eq_bc(nd - 1, K.OUTER_BC, lambda T, b: T["NP"] - 1.0)
+    sysm.add_eq_bc(nd - 1, K.OUTER_BC, lambda T, b: list(T["bet"]))
+    return doms, sysm, (P, NP, bx, by, bz), (E, E2S)
+
+
+# The vector star in Kadath's index notation (the product parses these).
+STAR_VECTOR_EQUATIONS = {
+    "P": "Lap(P) + 2*pi*E/P = 0",
+    "NP": "Lap(NP) - 2*pi*NP*E2S/P^2 = 0",
+    "bet": "D_j D^j bet^i + D^i D_j bet^j / 3 = 0",
+}
+
+
 def _anti(d):
     b = d.std_base()
     nc1, nc2 = d.nc[1], d.nc[2]

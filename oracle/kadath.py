@@ -960,12 +960,15 @@ class OTerm:
 
 # -------------------------------------------------------------- the system --
 class OSystem:
-    """System_of_eqs restricted to scalar unknowns and the equation kinds
-    Eq_inside (order 2), Eq_bc and Eq_matching."""
+    """System_of_eqs with scalar and Cartesian vector unknowns and the
+    equation kinds Eq_inside (order 2), Eq_bc and Eq_matching.  An equation
+    function returns one OTerm, or a list of OTerms for a vector equation
+    (its rows component by component, Eq_inside::export_val)."""
 
     def __init__(self, doms, dom_min, dom_max):
         self.doms, self.dmin, self.dmax = doms, dom_min, dom_max
         self.vars = []       # (name, dict dom -> VD with B=1)
+        self.vectors = {}    # name -> index in vars of its x component
         self.vdoubles = []   # [name, value]: unknowns that are numbers
         self.eqs = []        # (kind, dom, bound, fn_lhs, other_dom, other_bound, fn_rhs)
         self.ieqs = []       # integral-type equations: lists of parts (dom, bound, fn -> double OTerm)
@@ -973,6 +976,13 @@ class OSystem:
 
     def add_var(self, name, fields):
         self.vars.append((name, fields))
+
+    def add_var_vector(self, name, comps):
+        """add_var(name, Tensor&) with a Cartesian Vector (system_of_eqs.cpp:404):
+        T[name] is the list of its three component OTerms."""
+        self.vectors[name] = len(self.vars)
+        for c in range(3):
+            self.vars.append((f"{name}#{c + 1}", comps[c]))
 
     def add_var_double(self, name, value):
         """add_var(name, double&) (system_of_eqs.cpp:284)."""
@@ -1031,7 +1041,27 @@ class OSystem:
             if seed is not None:
                 der = 1.0 if (dseed and seed[1] == i) else 0.0
             out[name] = OTerm(dom, float(v), der)
+        for name, first in self.vectors.items():
+            out[name] = [out[self.vars[first + c][0]] for c in range(3)]
         return out
+
+    def _value_rows(self, kind, t, dom, bound):
+        """Value rows of an equation's term and the row count of each component."""
+        blocks, ns = [], []
+        for c in (t if isinstance(t, list) else [t]):
+            v, n = self._export(kind, c.val, dom, bound)
+            blocks.append(np.zeros(n) if v is None else v[0].copy())
+            ns.append(len(blocks[-1]))
+        return np.concatenate(blocks), ns
+
+    def _der_rows(self, kind, t, dom, bound, ns):
+        """(row offset, B x n tangent rows) of each component whose tangent is not zero."""
+        off = 0
+        for c, n in zip((t if isinstance(t, list) else [t]), ns):
+            v, _ = self._export(kind, c.der, dom, bound)
+            if v is not None:
+                yield off, v
+            off += n
 
     def _int_rows(self, seed=None, only_dom=None):
         """Values (seed None) or tangents of the integral equations."""
@@ -1069,27 +1099,31 @@ class OSystem:
     def residual(self):
         F = [np.array([v]) for v in self._int_rows()]
         for (kind, dom, bound, fn, odom, obound, fnr) in self.eqs:
-            t = fn(self._terms(dom), bound)
-            v, n = self._export(kind, t.val, dom, bound)
-            block = np.zeros(n) if v is None else v[0].copy()
+            block, _ = self._value_rows(kind, fn(self._terms(dom), bound), dom, bound)
             if kind == "matching":
-                t2 = fnr(self._terms(odom), obound)
-                v2, _ = self._export(kind, t2.val, odom, obound)
-                if v2 is not None:
-                    block = block - v2[0]
+                v2, _ = self._value_rows(kind, fnr(self._terms(odom), obound), odom, obound)
+                block = block - v2
             F.append(block)
         F = np.concatenate(F)
         self.nbr_conditions = len(F)
         return F
 
     def unknown_layout(self):
+        """xx_to_vars (system_of_eqs.cpp:597): variable by variable, domain by
+        domain; a vector's three components inside each domain."""
         layout = []
         col = len(self.vdoubles)
-        for vi, (name, f) in enumerate(self.vars):
+        firsts = set(self.vectors.values())
+        vi = 0
+        while vi < len(self.vars):
+            ncmp = 3 if vi in firsts else 1
             for dd in range(self.dmin, self.dmax + 1):
-                pats = self.doms[dd].unknown_patterns(f[dd].base)
-                layout.append((vi, dd, col, pats))
-                col += len(pats)
+                for c in range(ncmp):
+                    f = self.vars[vi + c][1]
+                    pats = self.doms[dd].unknown_patterns(f[dd].base)
+                    layout.append((vi + c, dd, col, pats))
+                    col += len(pats)
+            vi += ncmp
         return layout, col
 
     def jacobian(self, rectangular=False):
@@ -1102,23 +1136,19 @@ class OSystem:
         r = nint
         for eq in self.eqs:
             kind, dom, bound, fn, odom, obound, fnr = eq
-            _, n = self._export(kind, fn(self._terms(dom), bound).val, dom, bound)
-            row0.append((r, n))
-            r += n
+            _, ns = self._value_rows(kind, fn(self._terms(dom), bound), dom, bound)
+            row0.append((r, ns))
+            r += sum(ns)
         # columns of the double unknowns: every equation (do_col_J, is_var_double)
         for i in range(len(self.vdoubles)):
             seed = ("double", i)
             for e, (kind, dom, bound, fn, odom, obound, fnr) in enumerate(self.eqs):
-                r0, n = row0[e]
-                t = fn(self._terms(dom, seed), bound)
-                v, _ = self._export(kind, t.der, dom, bound)
-                if v is not None:
-                    J[r0:r0 + n, i] += v[0]
+                r0, ns = row0[e]
+                for off, v in self._der_rows(kind, fn(self._terms(dom, seed), bound), dom, bound, ns):
+                    J[r0 + off:r0 + off + v.shape[1], i] += v[0]
                 if kind == "matching":
-                    t = fnr(self._terms(odom, seed), obound)
-                    v, _ = self._export(kind, t.der, odom, obound)
-                    if v is not None:
-                        J[r0:r0 + n, i] -= v[0]
+                    for off, v in self._der_rows(kind, fnr(self._terms(odom, seed), obound), odom, obound, ns):
+                        J[r0 + off:r0 + off + v.shape[1], i] -= v[0]
             for k, dv in enumerate(self._int_rows(seed)):
                 J[k, i] = float(np.asarray(dv).reshape(-1)[0]) if isinstance(dv, np.ndarray) else dv
         for vi, dd, col, pats in layout:
@@ -1131,17 +1161,15 @@ class OSystem:
             base = self.vars[vi][1][dd].base
             sb = VD(d, B, cf=seed.reshape((B,) + d.nc), base=base)
             for e, (kind, dom, bound, fn, odom, obound, fnr) in enumerate(self.eqs):
-                r0, n = row0[e]
+                r0, ns = row0[e]
                 if dom == dd:
                     t = fn(self._terms(dom, (vi, dd, sb)), bound)
-                    v, _ = self._export(kind, t.der, dom, bound)
-                    if v is not None:
-                        J[r0:r0 + n, col:col + B] += v.T
+                    for off, v in self._der_rows(kind, t, dom, bound, ns):
+                        J[r0 + off:r0 + off + v.shape[1], col:col + B] += v.T
                 if kind == "matching" and odom == dd:
                     t = fnr(self._terms(odom, (vi, dd, sb)), obound)
-                    v, _ = self._export(kind, t.der, odom, obound)
-                    if v is not None:
-                        J[r0:r0 + n, col:col + B] -= v.T
+                    for off, v in self._der_rows(kind, t, odom, obound, ns):
+                        J[r0 + off:r0 + off + v.shape[1], col:col + B] -= v.T
             for k, dv in enumerate(self._int_rows((vi, dd, sb), only_dom=dd)):
                 J[k, col:col + B] += dv
         return F, J
