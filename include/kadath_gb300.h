@@ -205,6 +205,19 @@ int kd_system_set_metric_flat(kd_system* s, const char* name);
 int kd_system_add_eq_inside(kd_system* s, int dom, const char* eq);        /* add_eq_inside */
 int kd_system_add_eq_bc(kd_system* s, int dom, int bound, const char* eq); /* add_eq_bc */
 int kd_system_add_eq_matching(kd_system* s, int dom, int bound, const char* eq); /* add_eq_matching */
+/* add_eq_order (src/System_of_eqs/add_eq.cpp:80, Eq_order): the tau export
+ * drops `order` radial coefficients (0, 1 or 2; add_eq_inside is order 2).
+ * add_eq_full (add_eq.cpp:291, Eq_full) is order 0: every coefficient. */
+int kd_system_add_eq_order(kd_system* s, int dom, int order, const char* eq);
+int kd_system_add_eq_full(kd_system* s, int dom, const char* eq);
+/* add_eq_first_integral (add_eq.cpp:414, Eq_first_integral,
+ * src/Equation/eq_first_integral.cpp): integ_part is constant over domains
+ * dom_min..dom_max, with cst_part = 0 at the first collocation point of
+ * dom_min.  Conditions: every coefficient of integ_part minus its value at
+ * that point, in each domain; in dom_min the points of radial index 0 carry
+ * cst_part's value there instead. */
+int kd_system_add_eq_first_integral(kd_system* s, int dom_min, int dom_max, const char* integ_part,
+                                    const char* cst_part);
 /* Integral-type equations (Eq_int, include/system_of_eqs.hpp:1352): one
  * condition each, placed before all other equations (sec_member,
  * src/System_of_eqs/solver.cpp:49).

@@ -432,6 +432,28 @@ int kd_system_add_cst_field(kd_system* s, const char* name, kd_field* f) {
   });
 }
 
+int kd_system_add_eq_order(kd_system* s, int dom, int order, const char* eq) {
+  SYS_GUARD(s) {
+    if (!eq) throw kd::KdError(KD_ERR_ARG, "null equation");
+    s->sys->add_eq_order(dom, order, eq);
+  });
+}
+
+int kd_system_add_eq_full(kd_system* s, int dom, const char* eq) {
+  SYS_GUARD(s) {
+    if (!eq) throw kd::KdError(KD_ERR_ARG, "null equation");
+    s->sys->add_eq_full(dom, eq);
+  });
+}
+
+int kd_system_add_eq_first_integral(kd_system* s, int dom_min, int dom_max, const char* integ_part,
+                                    const char* cst_part) {
+  SYS_GUARD(s) {
+    if (!integ_part || !cst_part) throw kd::KdError(KD_ERR_ARG, "null expression");
+    s->sys->add_eq_first_integral(dom_min, dom_max, integ_part, cst_part);
+  });
+}
+
 int kd_system_add_var_vector(kd_system* s, const char* name, kd_field* fx, kd_field* fy, kd_field* fz) {
   SYS_GUARD(s) {
     if (!name || !fx || !fy || !fz) throw kd::KdError(KD_ERR_ARG, "null argument");

@@ -379,6 +379,29 @@ cudaError_t launch_lincomb2(int n, double ca, const double* a, double as, double
   return cudaGetLastError();
 }
 
+__global__ void first_integral_kernel(int B, int npts, int n0, const double* __restrict__ v, long long vs,
+                                      const double* __restrict__ ori, long long os, int inject,
+                                      const double* __restrict__ cst, long long cs, double cst_scalar,
+                                      double* __restrict__ out) {
+  const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= static_cast<long long>(B) * npts) return;
+  const int b = static_cast<int>(i / npts), p = static_cast<int>(i % npts);
+  double r;
+  if (inject && p < n0) r = cst ? cst[b * cs] : cst_scalar;
+  else r = (v ? v[b * vs + p] : 0.0) - (ori ? ori[b * os] : 0.0);
+  out[i] = r;
+}
+
+cudaError_t launch_first_integral(int B, int npts, int n0, const double* v, long long vs, const double* ori,
+                                  long long os, int inject, const double* cst, long long cs, double cst_scalar,
+                                  double* out, cudaStream_t s) {
+  const long long n = static_cast<long long>(B) * npts;
+  if (n <= 0) return cudaSuccess;
+  first_integral_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(B, npts, n0, v, vs, ori, os, inject,
+                                                                              cst, cs, cst_scalar, out);
+  return cudaGetLastError();
+}
+
 __device__ __forceinline__ double eos_clamp_rho(const KdEos& e, double rho) {
   return rho < e.rhomin ? e.rhomin : (rho > e.rhomax ? e.rhomax : rho);  // check_range
 }

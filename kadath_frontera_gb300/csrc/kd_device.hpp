@@ -110,4 +110,13 @@ cudaError_t launch_reduce1(const double* x, long long n, int op, double* out_sca
 cudaError_t launch_lincomb2(int n, double ca, const double* a, double as, double cb, const double* b, double bs,
                             double* out, cudaStream_t s);
 
+// The first integral's residual in one domain (Eq_first_integral::export_val /
+// export_der, src/Equation/eq_first_integral.cpp:44-120), for B seeds:
+//   out[b][p] = (v ? v[b*vs + p] : 0) - (ori ? ori[b*os] : 0),
+// and, when inject != 0, the first n0 points (radial index 0) replaced by
+// (cst ? cst[b*cs] : cst_scalar).  All arrays at the collocation points.
+cudaError_t launch_first_integral(int B, int npts, int n0, const double* v, long long vs, const double* ori,
+                                  long long os, int inject, const double* cst, long long cs, double cst_scalar,
+                                  double* out, cudaStream_t s);
+
 }  // namespace kd

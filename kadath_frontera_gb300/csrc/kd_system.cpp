@@ -189,7 +189,7 @@ Term EvalState::cst_term(int which, int dom) {
 }
 
 Term EvalState::def_term(int which, int dom) {
-  auto key = std::make_pair(which, dom);
+  auto key = std::make_tuple(which, dom, sys->ctx->stream());
   auto it = def_cache.find(key);
   if (it != def_cache.end()) return it->second;
   const auto& df = sys->defs_.at(which);
@@ -588,6 +588,38 @@ void System::add_eq_matching(int dom, int bound, const std::string& text) {
   nbr_conditions_ = -1;
 }
 
+void System::add_eq_order(int dom, int order, const std::string& text) {
+  if (order < 0 || order > 2) throw KdError(KD_ERR_ARG, "order of an equation must be 0, 1 or 2");
+  std::string l, r;
+  if (!split_eq(text, l, r)) throw KdError(KD_ERR_ARG, "= needed for equations");
+  Equation eq;
+  eq.kind = Equation::INSIDE;
+  eq.dom = dom;
+  eq.order = order;
+  eq.text = text;
+  eq.lhs = (bare(r) == "0") ? parse_ope(*this, dom, l, -1)
+                            : std::make_shared<OpeSubEq>(dom, parse_ope(*this, dom, l, -1), parse_ope(*this, dom, r, -1));
+  mark_tangent_frontier(eq.lhs.get());
+  tcache_.clear();
+  eqs_.push_back(eq);
+  nbr_conditions_ = -1;
+}
+
+void System::add_eq_first_integral(int dmin, int dmax, const std::string& integ_part, const std::string& cst_part) {
+  if (dmin < dom_min || dmax > dom_max || dmin > dmax) throw KdError(KD_ERR_ARG, "bad domains for a first integral");
+  Equation eq;
+  eq.kind = Equation::FIRST_INTEGRAL;
+  eq.dom = dmin;
+  eq.other_dom = dmax;
+  eq.text = integ_part;
+  eq.parts.push_back(parse_ope(*this, dmin, cst_part, -1));
+  for (int d = dmin; d <= dmax; d++) eq.parts.push_back(parse_ope(*this, d, integ_part, -1));
+  for (auto& p : eq.parts) mark_tangent_frontier(p.get());
+  tcache_.clear();
+  eqs_.push_back(eq);
+  nbr_conditions_ = -1;
+}
+
 void System::add_int_equation(IntEquation ie) {
   for (auto& p : ie.parts) mark_tangent_frontier(p.get());
   tcache_.clear();
@@ -755,6 +787,119 @@ void System::export_term(const Equation& eq, const Term& t, bool der, int side_d
   }
 }
 
+std::vector<Term> System::eval_parts(const Equation& eq, EvalState& st) {
+  std::vector<Term> t;
+  for (auto& p : eq.parts) t.push_back(p->eval(st));
+  return t;
+}
+
+int System::count_rows_fi(Equation& eq, const std::vector<Term>& parts) {
+  eq.n_cond_dom.clear();
+  int n = 0;
+  for (int d = eq.dom; d <= eq.other_dom; d++) {
+    const Term& t = parts[1 + d - eq.dom];
+    if (t.is_double || t.vt.size() != 1) throw KdError(KD_ERR_UNSUPPORTED, "a first integral must be a scalar field");
+    if (!t.vt[0].base.def) throw KdError(KD_ERR_STATE, "first integral without a defined basis: " + eq.text);
+    const int r = export_table(sp->dom(d), t.vt[0].base, 0, 0).nrows;
+    eq.n_cond_dom.push_back(r);
+    n += r;
+  }
+  return n;
+}
+
+// Eq_first_integral::export_val / export_der (eq_first_integral.cpp:44-120):
+// in every domain the first integral minus its value at the first
+// collocation point of dom_min; in dom_min the radial-index-0 points carry
+// the constant part's value at that point; all coefficients exported.
+void System::export_first_integral(const Equation& eq, const std::vector<Term>& parts, bool der, double* out,
+                                   long long osf, long long osr, int batch, bool accumulate) {
+  const Term& cst = parts[0];
+  const int dmin = eq.dom;
+  auto comp = [&](const Term& t) -> const DVal& { return der ? t.dt[0] : t.vt[0]; };
+  const DVal& vmin = comp(parts[1]);
+  const Domain& dm0 = sp->dom(dmin);
+  const double* ori = nullptr;
+  long long os = 0;
+  if (!vmin.zero) {
+    vmin.coef_i();
+    ori = vmin.c;
+    os = (vmin.batch == 1) ? 0 : dm0.npts();
+  }
+  const double* cstp = nullptr;
+  long long cs = 0;
+  double cst_scalar = 0.0;
+  if (cst.is_double) {
+    if (der) {
+      if (cst.ddv) throw KdError(KD_ERR_UNSUPPORTED, "first integral: a seeded number as constant part");
+      cst_scalar = cst.has_dd ? cst.dd : 0.0;
+    } else {
+      cst_scalar = cst.vd;
+    }
+  } else {
+    if (cst.vt.size() != 1 || cst.vt[0].dom != &dm0)
+      throw KdError(KD_ERR_UNSUPPORTED, "first integral: the constant part must be a scalar of the first domain");
+    const DVal& c = comp(cst);
+    if (!c.zero) {
+      c.coef_i();
+      cstp = c.c;
+      cs = (c.batch == 1) ? 0 : dm0.npts();
+    }
+  }
+  long long row = 0;
+  for (int d = dmin; d <= eq.other_dom; d++) {
+    const Term& t = parts[1 + d - dmin];
+    const Domain& dm = sp->dom(d);
+    const DVal& v = comp(t);
+    const bool inject = (d == dmin);
+    const long long nrows = eq.n_cond_dom.at(d - dmin);
+    if (v.zero && !ori && !(inject && (cstp || cst_scalar != 0.0))) {
+      row += nrows;
+      continue;
+    }
+    const double* vp = nullptr;
+    long long vs = 0;
+    if (!v.zero) {
+      v.coef_i();
+      vp = v.c;
+      vs = (v.batch == 1) ? 0 : dm.npts();
+    }
+    double* w = ctx->scratch().alloc_doubles(static_cast<long long>(batch) * dm.npts());
+    cuda_check(launch_first_integral(batch, dm.npts(), dm.np[1] * dm.np[2], vp, vs, ori, os, inject ? 1 : 0, cstp, cs,
+                                     cst_scalar, w, ctx->stream()),
+               "first integral");
+    ctx->launches++;
+    const Base& base = (!v.zero && v.base.def) ? v.base : t.vt[0].base;
+    DVal wd(ctx, &dm, batch);
+    wd.zero = false;
+    wd.c = w;
+    wd.in_conf = true;
+    wd.base = base;
+    wd.coef();
+    const CsrTable& tab = export_table(dm, base, 0, 0);
+    if (tab.nrows != nrows) throw KdError(KD_ERR_STATE, "the basis of the first integral changed its conditions");
+    ProfScope ps(ctx, Context::PROF_GATHER, 8.0 * batch * (tab.nnz + 2.0 * tab.nrows));
+    cuda_check(launch_gather_csr(wd.cf, dm.ncoefs(), batch, tab.nrows, tab.rowptr, tab.idx, tab.w, out + row * osr, osf,
+                                 osr, 1.0, accumulate ? 1 : 0, ctx->stream()),
+               "first integral gather");
+    ctx->launches++;
+    row += nrows;
+  }
+}
+
+void System::export_tangent(Equation& eq, EvalState& st, double* out, long long osf, int batch) {
+  if (eq.kind == Equation::FIRST_INTEGRAL) {
+    std::vector<Term> parts = eval_parts(eq, st);
+    export_first_integral(eq, parts, true, out + eq.row0, osf, 1, batch, true);
+    return;
+  }
+  Term t = eq.lhs->eval(st);
+  export_term(eq, t, true, eq.dom, eq.bound, out + eq.row0, osf, 1, batch, 1.0, true);
+  if (eq.kind == Equation::MATCHING) {
+    Term r = eq.rhs->eval(st);
+    export_term(eq, r, true, eq.other_dom, eq.other_bound, out + eq.row0, osf, 1, batch, -1.0, true);
+  }
+}
+
 void System::compute_unknowns() {
   col0_.clear();
   nunk_.clear();
@@ -790,6 +935,7 @@ void System::residual(double* d_F, bool record) {
   st.vcache = record ? &vcache_ : nullptr;
   st.record = record;
   std::vector<Term> lhs(eqs_.size()), rhs(eqs_.size());
+  std::vector<std::vector<Term>> fparts(eqs_.size());
   if (d_F && nbr_conditions_ >= 0)
     cuda_check(cudaMemsetAsync(d_F, 0, sizeof(double) * nbr_conditions_, ctx->main_stream()), "memset F");
   // The equations of different domains are independent (fields are only
@@ -815,6 +961,10 @@ void System::residual(double* d_F, bool record) {
   }
   for (size_t i = 0; i < eqs_.size(); i++) {
     ctx->use(stream_of(eqs_[i]));
+    if (eqs_[i].kind == Equation::FIRST_INTEGRAL) {
+      fparts[i] = eval_parts(eqs_[i], st);
+      continue;
+    }
     lhs[i] = eqs_[i].lhs->eval(st);
     if (eqs_[i].kind == Equation::MATCHING) rhs[i] = eqs_[i].rhs->eval(st);
   }
@@ -823,7 +973,8 @@ void System::residual(double* d_F, bool record) {
     int row = 0;
     for (auto& ie : ieqs_) ie.row = row++;
     for (size_t i = 0; i < eqs_.size(); i++) {
-      eqs_[i].n_cond = count_rows(eqs_[i], lhs[i]);
+      eqs_[i].n_cond = (eqs_[i].kind == Equation::FIRST_INTEGRAL) ? count_rows_fi(eqs_[i], fparts[i])
+                                                                  : count_rows(eqs_[i], lhs[i]);
       eqs_[i].row0 = row;
       row += eqs_[i].n_cond;
     }
@@ -846,7 +997,9 @@ void System::residual(double* d_F, bool record) {
     Equation& eq = eqs_[i];
     ctx->use(stream_of(eq));
     double* out = d_F + eq.row0;
-    if (eq.kind == Equation::MATCHING) {
+    if (eq.kind == Equation::FIRST_INTEGRAL) {
+      export_first_integral(eq, fparts[i], false, out, 0, 1, 1, false);
+    } else if (eq.kind == Equation::MATCHING) {
       export_term(eq, lhs[i], false, eq.dom, eq.bound, out, 0, 1, 1, 1.0, false);
       export_term(eq, rhs[i], false, eq.other_dom, eq.other_bound, out, 0, 1, 1, -1.0, true);
     } else {
@@ -898,14 +1051,7 @@ void System::jacobian(double* d_J, long long ld, bool reuse, bool rectangular) {
       st.seed_var_double = static_cast<int>(i);
       st.vcache = &vcache_;
       double* Jcol = d_J + static_cast<long long>(i) * ld;
-      for (auto& eq : eqs_) {
-        Term t = eq.lhs->eval(st);
-        export_term(eq, t, true, eq.dom, eq.bound, Jcol + eq.row0, ld, 1, 1, 1.0, true);
-        if (eq.kind == Equation::MATCHING) {
-          Term r = eq.rhs->eval(st);
-          export_term(eq, r, true, eq.other_dom, eq.other_bound, Jcol + eq.row0, ld, 1, 1, -1.0, true);
-        }
-      }
+      for (auto& eq : eqs_) export_tangent(eq, st, Jcol, ld, 1);
       export_int_ders(st, -1, Jcol, ld, 1);
     }
   }
@@ -942,6 +1088,11 @@ void System::jacobian(double* d_J, long long ld, bool reuse, bool rectangular) {
       double* Jblock = d_J + static_cast<long long>(col0) * ld;
       for (auto& eq : eqs_) {
         if (!eq.take_into_account(dd)) continue;
+        if (eq.kind == Equation::FIRST_INTEGRAL) {
+          std::vector<Term> parts = eval_parts(eq, st);
+          export_first_integral(eq, parts, true, Jblock + eq.row0, ld, 1, B, true);
+          continue;
+        }
         if (eq.kind != Equation::MATCHING || dd == eq.dom) {
           Term t = eq.lhs->eval(st);
           export_term(eq, t, true, eq.dom, eq.bound, Jblock + eq.row0, ld, 1, B, 1.0, true);
@@ -999,14 +1150,7 @@ void System::dres_dcst(int cst, double* d_y) {
   st.seed_cst = cst;
   st.vcache = &vcache_;
   cuda_check(cudaMemsetAsync(d_y, 0, sizeof(double) * N, ctx->stream()), "memset y");
-  for (auto& eq : eqs_) {
-    Term t = eq.lhs->eval(st);
-    export_term(eq, t, true, eq.dom, eq.bound, d_y + eq.row0, 0, 1, 1, 1.0, true);
-    if (eq.kind == Equation::MATCHING) {
-      Term r = eq.rhs->eval(st);
-      export_term(eq, r, true, eq.other_dom, eq.other_bound, d_y + eq.row0, 0, 1, 1, -1.0, true);
-    }
-  }
+  for (auto& eq : eqs_) export_tangent(eq, st, d_y, 0, 1);
   export_int_ders(st, -1, d_y, 1, 1);
 }
 
@@ -1075,14 +1219,7 @@ void System::jx(const double* d_x, double* d_y) {
   st.jx_doubles = &xd;
   st.vcache = &vcache_;
   cuda_check(cudaMemsetAsync(d_y, 0, sizeof(double) * N, ctx->stream()), "memset y");
-  for (auto& eq : eqs_) {
-    Term t = eq.lhs->eval(st);
-    export_term(eq, t, true, eq.dom, eq.bound, d_y + eq.row0, 0, 1, 1, 1.0, true);
-    if (eq.kind == Equation::MATCHING) {
-      Term r = eq.rhs->eval(st);
-      export_term(eq, r, true, eq.other_dom, eq.other_bound, d_y + eq.row0, 0, 1, 1, -1.0, true);
-    }
-  }
+  for (auto& eq : eqs_) export_tangent(eq, st, d_y, 0, 1);
   export_int_ders(st, -1, d_y, 1, 1);
 }
 

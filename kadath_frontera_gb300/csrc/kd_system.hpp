@@ -111,7 +111,11 @@ struct EvalState {
   int seed_var_double = -1;
   int seed_cst = -1;       // double constant seeded (dF/dp passes)
   DVal seed;               // batch-B coefficient patterns
-  std::map<std::pair<int, int>, Term> def_cache;
+  // definition values by (definition, domain, stream): equations of
+  // different domains run on different streams, and a value is only reused
+  // on the stream that computed it (no cross-stream hazard on its buffers or
+  // its lazily computed representations)
+  std::map<std::tuple<int, int, cudaStream_t>, Term> def_cache;
   // do_JX: every unknown field seeded at once (tangent = x mapped to
   // coefficients per (variable, domain)); var doubles get jx_doubles.
   const std::map<std::pair<int, int>, DVal>* jx_seeds = nullptr;
@@ -132,15 +136,23 @@ struct EvalState {
 };
 
 struct Equation {
-  enum Kind { INSIDE, BC, MATCHING };
+  // INSIDE with order 2 is Eq_inside, any other order Eq_order (order 0:
+  // Eq_full, every coefficient); FIRST_INTEGRAL is Eq_first_integral over
+  // domains dom..other_dom.
+  enum Kind { INSIDE, BC, MATCHING, FIRST_INTEGRAL };
   Kind kind;
   int dom, bound = -1, other_dom = -1, other_bound = -1;
   int order = 2;
   std::string text;
   OpePtr lhs, rhs;
+  // FIRST_INTEGRAL: parts[0] the constant part (in dom), parts[1 + k] the
+  // first integral in domain dom + k; n_cond_dom the rows of each domain
+  std::vector<OpePtr> parts;
+  std::vector<int> n_cond_dom;
   int n_cond = -1;
   int row0 = 0;
   bool take_into_account(int d) const {
+    if (kind == FIRST_INTEGRAL) return d >= dom && d <= other_dom;
     return d == dom || (kind == MATCHING && d == other_dom);
   }
 };
@@ -186,6 +198,15 @@ class System {
   void add_eq_inside(int dom, const std::string& eq);
   void add_eq_bc(int dom, int bound, const std::string& eq);
   void add_eq_matching(int dom, int bound, const std::string& eq);
+  // add_eq_order (add_eq.cpp:80): the tau export drops `order` radial
+  // coefficients; add_eq_full (add_eq.cpp:291, Eq_full) is order 0.
+  void add_eq_order(int dom, int order, const std::string& eq);
+  void add_eq_full(int dom, const std::string& eq) { add_eq_order(dom, 0, eq); }
+  // add_eq_first_integral (add_eq.cpp:414, Eq_first_integral): integ_part
+  // minus its value at the first collocation point of dom_min, on every
+  // coefficient of dom_min..dom_max; in dom_min the points of radial index
+  // 0 carry cst_part's value at that point instead.
+  void add_eq_first_integral(int dom_min, int dom_max, const std::string& integ_part, const std::string& cst_part);
   // "integvolume(f) = c": the volume integral of f over domains dmin..dmax
   // equals c (Space_spheric::add_eq_int_volume, spheric_add_eq.cpp:81).
   void add_eq_int_volume(int dmin, int dmax, const std::string& eq);
@@ -325,6 +346,12 @@ class System {
   int count_rows(const Equation& eq, const Term& t);
   void export_term(const Equation& eq, const Term& t, bool der, int side_dom, int side_bound, double* out,
                    long long osf, long long osr, int batch, double alpha, bool accumulate);
+  std::vector<Term> eval_parts(const Equation& eq, EvalState& st);
+  int count_rows_fi(Equation& eq, const std::vector<Term>& parts);
+  void export_first_integral(const Equation& eq, const std::vector<Term>& parts, bool der, double* out, long long osf,
+                             long long osr, int batch, bool accumulate);
+  // One equation's tangent rows (every side), added into out.
+  void export_tangent(Equation& eq, EvalState& st, double* out, long long osf, int batch);
   CsrTable upload_rows(const std::vector<SparseRow>& rows);
   void add_int_equation(IntEquation ie);
   // Adds the tangents of the integral equations to out[row + b * osf],

@@ -77,6 +77,9 @@ def _declare_system(lib):
         "kd_system_add_cst_field": (I, [P, C.c_char_p, P]),
         "kd_system_add_def": (I, [P, I, C.c_char_p]),
         "kd_system_add_var_vector": (I, [P, C.c_char_p, P, P, P]),
+        "kd_system_add_eq_order": (I, [P, I, I, C.c_char_p]),
+        "kd_system_add_eq_full": (I, [P, I, C.c_char_p]),
+        "kd_system_add_eq_first_integral": (I, [P, I, I, C.c_char_p, C.c_char_p]),
         "kd_system_add_cst_vector": (I, [P, C.c_char_p, P, P, P]),
         "kd_system_set_metric_flat": (I, [P, C.c_char_p]),
         "kd_system_add_eq_inside": (I, [P, I, C.c_char_p]),
@@ -195,6 +198,11 @@ class Space_spheric:
         """Space_spheric::add_eq_int_volume: "integvolume(f) = c" over every
         domain of the space."""
         syst.add_eq_int_volume(0, self.get_nbr_domains() - 1, eq)
+
+    def add_eq_full(self, syst, eq):
+        """Space_spheric::add_eq_full: Eq_full in every domain of the system."""
+        for dd in range(syst.dom_min, syst.dom_max + 1):
+            syst.add_eq_full(dd, eq)
 
     def add_eq_ori(self, syst, eq):
         """Space_spheric::add_eq_ori: eq vanishes at the origin (the first
@@ -422,6 +430,16 @@ class System_of_eqs:
 
     def add_eq_bc(self, dom, bound, eq):
         self.ctx.check(_L().kd_system_add_eq_bc(self.h, dom, bound, eq.encode()))
+
+    def add_eq_order(self, dom, order, eq):
+        self.ctx.check(_L().kd_system_add_eq_order(self.h, dom, int(order), eq.encode()))
+
+    def add_eq_full(self, dom, eq):
+        self.ctx.check(_L().kd_system_add_eq_full(self.h, dom, eq.encode()))
+
+    def add_eq_first_integral(self, dom_min, dom_max, integ_part, cst_part):
+        self.ctx.check(_L().kd_system_add_eq_first_integral(self.h, dom_min, dom_max, integ_part.encode(),
+                                                             cst_part.encode()))
 
     def add_eq_matching(self, dom, bound, eq):
         self.ctx.check(_L().kd_system_add_eq_matching(self.h, dom, bound, eq.encode()))

@@ -201,7 +201,65 @@ def star_vector(res=(13, 9, 4), bounds=STAR_BOUNDS, ctx=None, rho_c=STAR_RHOC) -
     return Workload("star_vector", space, syst, unknowns, [E, E2S])
 
 
-WORKLOADS = {"toy": toy, "star": star, "star_vector": star_vector}
+NS_BOUNDS = (3.5, 7.0, 12.0, 18.0, 24.0)
+NS_RHOC = 1.28e-3
+NS_DEFS_ALL = ["NP = P*N", "h = exp(H)", "rho = rho(h)", "eps = eps(h)", "press = press(h)",
+               "delta = h - eps - 1."]
+NS_DEFS_MATTER = ["Etilde = press * h - press * delta", "Stilde = 3 * press * delta",
+                  "eqP = delta * D^i D_i P + 4piG / 2. * P^5 * Etilde",
+                  "eqNP = delta * D^i D_i NP - 4piG / 2. * N * P^5 * (Etilde + 2. * Stilde)",
+                  "firstint = H + log(N)"]
+NS_DEFS_VACUUM = ["eqP = D^i D_i P", "eqNP = D^i D_i NP"]
+
+
+def ns_tov(res=(13, 9, 4), bounds=NS_BOUNDS, ctx=None, rho_c=NS_RHOC) -> Workload:
+    """Static TOV star with the log-enthalpy H as unknown, in the shape of
+    the non-rotating stage of Kadath's NS solver: the Gamma = 2, K = 100
+    polytrope through the EOS operators, lapse N and conformal factor P,
+    matter in domains 0 and 1 whose outer radius is fixed (7), H = 0 on every
+    coefficient outside (add_eq_full), the first integral H + log(N) =
+    const in the matter with H = Hc at the centre (add_eq_first_integral).
+    The equations are the solver's strings.  Initial guess H = Hc in the
+    matter, P = N = 1."""
+    from .kadath import KD_EOS_DENSITY, KD_EOS_DHDRHO, KD_EOS_EPSILON, KD_EOS_PRESSURE, Metric_flat
+    space = Space_spheric(CHEB_TYPE, (0, 0, 0), res, bounds, ctx=ctx)
+    nd = space.get_nbr_domains()
+    hc = math.log(1.0 + 2.0 * 100.0 * rho_c)
+    H = Scalar(space)
+    for d in range(nd):
+        H.set_domain(d, np.full(space.domain_info(d)["nbr_points"], hc if d <= 1 else 0.0))
+    H.std_base()
+    P = Scalar(space, 1.0).std_base()
+    N = Scalar(space, 1.0).std_base()
+    syst = System_of_eqs(space, 0, nd - 1)
+    syst.add_var("H", H)
+    Metric_flat(space).set_system(syst, "f")
+    syst.add_cst("4piG", 4 * math.pi)
+    syst.add_var("P", P)
+    syst.add_var("N", N)
+    syst.add_cst("Hc", hc)
+    for name, var in (("eps", KD_EOS_EPSILON), ("press", KD_EOS_PRESSURE), ("rho", KD_EOS_DENSITY),
+                      ("dHdlnrho", KD_EOS_DHDRHO)):
+        syst.add_ope_eos(name, var)
+    for df in NS_DEFS_ALL:
+        syst.add_def(df)
+    for d in range(nd):
+        if d <= 1:
+            for df in NS_DEFS_MATTER:
+                syst.add_def(d, df)
+        else:
+            syst.add_eq_full(d, "H = 0")
+            for df in NS_DEFS_VACUUM:
+                syst.add_def(d, df)
+    space.add_eq(syst, "eqNP= 0", "N", "dn(N)")
+    space.add_eq(syst, "eqP = 0", "P", "dn(P)")
+    syst.add_eq_bc(nd - 1, OUTER_BC, "N=1")
+    syst.add_eq_bc(nd - 1, OUTER_BC, "P=1")
+    syst.add_eq_first_integral(0, 1, "firstint", "H - Hc")
+    return Workload("ns_tov", space, syst, [("H", H), ("P", P), ("N", N)], [])
+
+
+WORKLOADS = {"toy": toy, "star": star, "star_vector": star_vector, "ns_tov": ns_tov}
 
 
 def solve(wl: Workload, precision=1e-10, lu_mode=None, max_steps=20) -> int:

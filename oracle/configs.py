@@ -206,6 +206,97 @@ def star_vector(res=(13, 9, 4), bounds=(STAR_R, 12.0, 16.0, 24.0, 32.0)):
     return doms, sysm, (P, NP, bx, by, bz), (E, E2S)
 
 
+# Static TOV star with the log-enthalpy as unknown, in the shape of the
+# reference's non-rotating NS stage (include/Solvers/ns_3d_xcts/
+# ns_3d_xcts_stages.cpp:63-140, syst_init in ns_3d_xcts_solver_imp.cpp:89):
+# the matter fills domains 0 and 1 and its outer radius is fixed (the
+# "fixed" branch, here with a domain boundary that is not adapted).
+NS_BOUNDS = (3.5, 7.0, 12.0, 18.0, 24.0)
+NS_RHOC = 1.28e-3
+NS_QPIG = 4 * math.pi
+
+
+def ns_hc(rho_c=NS_RHOC, k=100.0):
+    """log h at the centre of a Gamma = 2 polytrope: h = 1 + eps + p/rho = 1 + 2 K rho."""
+    return math.log(1.0 + 2.0 * k * rho_c)
+
+
+NS_DEFS_ALL = ["NP = P*N", "h = exp(H)", "rho = rho(h)", "eps = eps(h)", "press = press(h)",
+               "delta = h - eps - 1."]
+NS_DEFS_MATTER = ["Etilde = press * h - press * delta", "Stilde = 3 * press * delta",
+                  "eqP = delta * D^i D_i P + 4piG / 2. * P^5 * Etilde",
+                  "eqNP = delta * D^i D_i NP - 4piG / 2. * N * P^5 * (Etilde + 2. * Stilde)",
+                  "firstint = H + log(N)"]
+NS_DEFS_VACUUM = ["eqP = D^i D_i P", "eqNP = D^i D_i NP"]
+
+
+def ns_tov(res=(9, 5, 4), bounds=NS_BOUNDS, rho_c=NS_RHOC):
+    """Oracle side of the TOV system: unknowns H (log enthalpy), P, N in that
+    order; H = 0 on every coefficient outside the matter (Eq_full); the first
+    integral H + log(N) = const in domains 0..1 with H - Hc at the centre
+    (Eq_first_integral); eqNP and eqP inside with N, dn(N), P, dn(P) matched
+    (Space_spheric::add_eq); N = P = 1 at infinity.  Initial guess H = Hc in
+    the matter and 0 outside, P = N = 1."""
+    doms = K.space_spheric(res, list(bounds))
+    nd = len(doms)
+    eos = K.polytrope()
+    hc = ns_hc(rho_c)
+    H = K.scalar_field(doms, lambda d: np.full(d.np, hc) if d.num <= 1 else np.zeros(d.np))
+    P = K.scalar_field(doms, lambda d: np.ones(d.np))
+    N = K.scalar_field(doms, lambda d: np.ones(d.np))
+    sysm = K.OSystem(doms, 0, nd - 1)
+    sysm.add_var("H", H)
+    sysm.add_var("P", P)
+    sysm.add_var("N", N)
+
+    def num(T, x):
+        return K.OTerm(T["P"].dom, float(x), None if T["P"].der is None else 0.0)
+
+    def matter(T):
+        h = T["H"].exp()
+        eps = K.eos_term(h, eos, K.EOS_EPSILON)
+        press = K.eos_term(h, eos, K.EOS_PRESSURE)
+        delta = (h - eps) - num(T, 1.0)
+        Etilde = press * h - press * delta
+        Stilde = (num(T, 3.0) * press) * delta
+        return delta, Etilde, Stilde
+
+    def lapD(t):
+        # D^i D_i X: sum over i of d_i d_i X, in the order 1, 2, 3
+        d2 = [t.partial(i).partial(i) for i in (1, 2, 3)]
+        return K.OTerm(t.dom, (d2[0].val + d2[1].val) + d2[2].val,
+                       None if t.der is None else (d2[0].der + d2[1].der) + d2[2].der)
+
+    qpig2 = lambda T: num(T, NS_QPIG) / num(T, 2.0)
+
+    def eqP(T, b):
+        if T["P"].dom > 1:
+            return lapD(T["P"])
+        delta, Et, _ = matter(T)
+        return delta * lapD(T["P"]) + (qpig2(T) * T["P"] ** 5) * Et
+
+    def eqNP(T, b):
+        NP = T["P"] * T["N"]
+        if T["P"].dom > 1:
+            return lapD(NP)
+        delta, Et, St = matter(T)
+        return delta * lapD(NP) - ((qpig2(T) * T["N"]) * T["P"] ** 5) * (Et + num(T, 2.0) * St)
+
+    for d in range(2, nd):
+        sysm.add_eq_full(d, lambda T, b: T["H"])
+    for eq, rac in ((eqNP, "N"), (eqP, "P")):
+        for d in range(nd - 1):
+            sysm.add_eq_inside(d, eq)
+            sysm.add_eq_matching(d, K.OUTER_BC, lambda T, b, rac=rac: T[rac])
+            sysm.add_eq_matching(d, K.OUTER_BC, lambda T, b, rac=rac: T[rac].dn(b))
+        sysm.add_eq_inside(nd - 1, eq)
+    sysm.add_eq_bc(nd - 1, K.OUTER_BC, lambda T, b: T["N"] - 1.0)
+    sysm.add_eq_bc(nd - 1, K.OUTER_BC, lambda T, b: T["P"] - 1.0)
+    sysm.add_eq_first_integral(0, 1, lambda T, b: T["H"] + T["N"].log(),
+                               lambda T, b: T["H"] - num(T, hc))
+    return doms, sysm, (H, P, N), eos
+
+
 # The vector star in Kadath's index notation (the product parses these).
 STAR_VECTOR_EQUATIONS = {
     "P": "Lap(P) + 2*pi*E/P = 0",

@@ -605,6 +605,18 @@ class VD:
         self.coef_i()
         return VD(self.dom, self.B, c=x / self.c, base=self.dom.std_base())
 
+    def exp(self):
+        """exp(Val_domain) (val_domain_math.cpp): at the collocation points,
+        the basis kept; exp(0) is 1 with no basis."""
+        if self.zero:
+            return VD(self.dom, self.B, c=np.ones((self.B,) + self.dom.np))
+        self.coef_i()
+        return VD(self.dom, self.B, c=np.exp(self.c), base=self.base)
+
+    def log(self):
+        self.coef_i()
+        return VD(self.dom, self.B, c=np.log(self.c), base=self.base)
+
 
 def radius_vd(dom):
     return VD(dom, 1, c=dom.radius()[None])
@@ -926,6 +938,16 @@ class OTerm:
     def lap(self):
         return OTerm(self.dom, laplacian(self.val), None if self.der is None else laplacian(self.der))
 
+    def exp(self):
+        """Ope_exp (src/Ope_eq/ope_exp.cpp), term_eq_math.cpp exp: der = u' exp(u)."""
+        v = self.val.exp()
+        return OTerm(self.dom, v, None if self.der is None else self.der * v)
+
+    def log(self):
+        """Ope_log: der = u' / u."""
+        v = self.val.log()
+        return OTerm(self.dom, v, None if self.der is None else self.der / self.val)
+
     def dn(self, bound):
         return OTerm(self.dom, der_normal(self.val, bound), None if self.der is None else
                      (self.der if self.der.zero else der_normal(self.der, bound)))
@@ -1013,6 +1035,23 @@ class OSystem:
     def add_eq_inside(self, dom, fn):
         self.eqs.append(("inside", dom, None, fn, None, None, None))
 
+    def add_eq_order(self, dom, order, fn):
+        """add_eq_order (add_eq.cpp:80): Eq_order, the tau export dropping
+        `order` radial coefficients; order 0 is add_eq_full (Eq_full,
+        eq_full.cpp: every coefficient)."""
+        self.eqs.append(("order", dom, order, fn, None, None, None))
+
+    def add_eq_full(self, dom, fn):
+        self.add_eq_order(dom, 0, fn)
+
+    def add_eq_first_integral(self, dom_min, dom_max, fn_integ, fn_cst):
+        """add_eq_first_integral (add_eq.cpp:414), Eq_first_integral
+        (eq_first_integral.cpp): fn_integ minus its value at the first
+        collocation point of dom_min, in every domain dom_min..dom_max, all
+        coefficients; in dom_min the points of radial index 0 carry fn_cst's
+        value at that first point instead."""
+        self.eqs.append(("first_integral", dom_min, dom_max, fn_integ, None, None, fn_cst))
+
     def add_eq_bc(self, dom, bound, fn):
         self.eqs.append(("bc", dom, bound, fn, None, None, None))
 
@@ -1080,6 +1119,8 @@ class OSystem:
         d = self.doms[dom]
         if kind == "inside":
             return d.export_tau(base, 2)
+        if kind in ("order", "first_integral"):
+            return d.export_tau(base, bound)
         return d.export_tau_boundary(base, bound)
 
     def _export(self, kind, vd, dom, bound, nrows_expected=None):
@@ -1096,9 +1137,62 @@ class OSystem:
                 M[r, idx] += w
         return cf @ M.T, len(rows)
 
+    def _first_integral(self, eq, seed=None):
+        """Eq_first_integral::export_val (seed None) / export_der
+        (eq_first_integral.cpp:44-120): per domain dom_min..dom_max, the
+        B x rows block (None: exactly zero) and the row count of the value."""
+        _, dmin, dmax, fn_integ, _, _, fn_cst = eq
+        use_der = seed is not None
+        Tmin = self._terms(dmin, seed)
+        cst = fn_cst(Tmin, None)
+        integ = {d: fn_integ(Tmin if d == dmin else self._terms(d, seed), None) for d in range(dmin, dmax + 1)}
+
+        def part(t):
+            return t.der if use_der else t.val
+
+        def point0(vd):
+            if vd is None or vd.zero:
+                return None
+            vd.coef_i()
+            return vd.c[:, 0, 0, 0].copy()
+        val_cst = point0(part(cst))
+        val_ori = point0(part(integ[dmin]))
+        blocks, ns = [], []
+        for d in range(dmin, dmax + 1):
+            dm = self.doms[d]
+            val = integ[d].val
+            nrow = len(dm.export_tau(val.base, 0))
+            ns.append(nrow)
+            v = part(integ[d])
+            inject = d == dmin
+            if v.zero and val_ori is None and not (inject and val_cst is not None):
+                blocks.append(None)
+                continue
+            B = max(1 if v.zero else v.B, 1 if val_ori is None else len(val_ori),
+                    1 if val_cst is None else len(val_cst))
+            if v.zero:
+                c = np.zeros((B,) + dm.np)
+            else:
+                v.coef_i()
+                c = np.broadcast_to(v.c, (B,) + dm.np).copy()
+            if val_ori is not None:
+                c = c - val_ori.reshape((-1, 1, 1, 1))
+            if inject:
+                c[:, 0, :, :] = 0.0 if val_cst is None else val_cst.reshape((-1, 1, 1))
+            base = v.base if (not v.zero and v.base.defined) else val.base
+            out, n = self._export("first_integral", VD(dm, B, c=c, base=base), d, 0)
+            assert n == nrow
+            blocks.append(out)
+        return blocks, ns
+
     def residual(self):
         F = [np.array([v]) for v in self._int_rows()]
-        for (kind, dom, bound, fn, odom, obound, fnr) in self.eqs:
+        for eq in self.eqs:
+            if eq[0] == "first_integral":
+                blocks, ns = self._first_integral(eq)
+                F.append(np.concatenate([np.zeros(n) if b is None else b[0] for b, n in zip(blocks, ns)]))
+                continue
+            (kind, dom, bound, fn, odom, obound, fnr) = eq
             block, _ = self._value_rows(kind, fn(self._terms(dom), bound), dom, bound)
             if kind == "matching":
                 v2, _ = self._value_rows(kind, fnr(self._terms(odom), obound), odom, obound)
@@ -1136,14 +1230,29 @@ class OSystem:
         r = nint
         for eq in self.eqs:
             kind, dom, bound, fn, odom, obound, fnr = eq
-            _, ns = self._value_rows(kind, fn(self._terms(dom), bound), dom, bound)
+            if kind == "first_integral":
+                _, ns = self._first_integral(eq)
+            else:
+                _, ns = self._value_rows(kind, fn(self._terms(dom), bound), dom, bound)
             row0.append((r, ns))
             r += sum(ns)
+
+        def add_fi(e, seed, cols, sign=1.0):
+            r0, ns = row0[e]
+            blocks, _ = self._first_integral(self.eqs[e], seed)
+            off = r0
+            for b, n in zip(blocks, ns):
+                if b is not None:
+                    J[off:off + n, cols] += sign * (b[0] if isinstance(cols, int) else b.T)
+                off += n
         # columns of the double unknowns: every equation (do_col_J, is_var_double)
         for i in range(len(self.vdoubles)):
             seed = ("double", i)
             for e, (kind, dom, bound, fn, odom, obound, fnr) in enumerate(self.eqs):
                 r0, ns = row0[e]
+                if kind == "first_integral":
+                    add_fi(e, seed, i)
+                    continue
                 for off, v in self._der_rows(kind, fn(self._terms(dom, seed), bound), dom, bound, ns):
                     J[r0 + off:r0 + off + v.shape[1], i] += v[0]
                 if kind == "matching":
@@ -1162,6 +1271,10 @@ class OSystem:
             sb = VD(d, B, cf=seed.reshape((B,) + d.nc), base=base)
             for e, (kind, dom, bound, fn, odom, obound, fnr) in enumerate(self.eqs):
                 r0, ns = row0[e]
+                if kind == "first_integral":
+                    if dom <= dd <= bound:
+                        add_fi(e, (vi, dd, sb), slice(col, col + B))
+                    continue
                 if dom == dd:
                     t = fn(self._terms(dom, (vi, dd, sb)), bound)
                     for off, v in self._der_rows(kind, t, dom, bound, ns):
@@ -1211,6 +1324,10 @@ class OSystem:
 
 
 # ---------------------------------------------------------------- EOS ops --
+# EOS variables (Margherita's EPSILON, PRESSURE, DENSITY, DHDRHO)
+EOS_EPSILON, EOS_PRESSURE, EOS_DENSITY, EOS_DHDRHO = 0, 1, 2, 3
+
+
 def polytrope(npieces=1, rhomin=1e-19, rhomax=1.0, k0=100.0, gamma_tab=(2.0,), rho_tab=(0.0,)):
     """Cold piecewise polytrope tables as Margherita_setup_polytrope builds
     them (include/EOS/standalone/setup_polytrope.cc), geometrised units."""
@@ -1261,6 +1378,40 @@ def _eos_point(e, var, hv, dh=None):
     return [P / rho ** 2 * drho, dpdrho * drho, drho, 0.0][var]
 
 
+def _eos_array(e, var, hv, dh=None):
+    """_eos_point over arrays (the same branches, element by element);
+    dh broadcasts against hv."""
+    hv = np.asarray(hv, dtype=np.float64)
+    n = e["n"]
+    gam, kk, ee, hh_t, rr = (np.array(e[x], dtype=np.float64) for x in ("gamma", "k", "eps", "h", "rho"))
+    above = hv > 1.0
+    hh = np.where(above, hv, 1.0)
+    idx = np.full(hv.shape, n - 1)
+    found = np.zeros(hv.shape, bool)
+    for nn in range(1, n):
+        m = (~found) & (hh_t[nn - 1] < hv) & (hv <= hh_t[nn])
+        idx = np.where(m, nn - 1, idx)
+        found |= m
+    gm1 = gam[idx] - 1.0
+    with np.errstate(invalid="ignore", divide="ignore"):
+        rho_a = (gm1 * (hv - 1.0 - ee[idx]) / (gam[idx] * kk[idx])) ** (1.0 / gm1)
+    rho = np.where(above, rho_a, rr[0])
+    rho = np.minimum(np.maximum(rho, e["rhomin"]), e["rhomax"])
+    i = np.full(hv.shape, n - 1)
+    found = np.zeros(hv.shape, bool)
+    for nn in range(1, n):
+        m = (~found) & (rr[nn - 1] < rho) & (rho <= rr[nn])
+        i = np.where(m, nn - 1, i)
+        found |= m
+    P = kk[i] * rho ** gam[i]
+    epsc = ee[i] + P / (rho * (gam[i] - 1.0))
+    dpdrho = gam[i] * P / rho
+    if dh is None:
+        return [epsc, P, rho, 1.0 / hh * dpdrho][var]
+    drho = rho * 1.0 / dpdrho * dh
+    return [P / rho ** 2 * drho, dpdrho * drho, drho, np.zeros_like(drho)][var]
+
+
 def eos_term(t, e, var):
     """Ope_user with EOS<eos, var>::action on an OTerm (value and tangent)."""
     v = t.val
@@ -1268,8 +1419,7 @@ def eos_term(t, e, var):
         val = v
     else:
         v.coef_i()
-        flat = v.c.reshape(-1)
-        val = VD(v.dom, 1, c=np.array([_eos_point(e, var, x) for x in flat]).reshape(v.c.shape), base=v.base)
+        val = VD(v.dom, 1, c=_eos_array(e, var, v.c), base=v.base)
     der = None
     if t.der is not None:
         d = t.der
@@ -1277,11 +1427,7 @@ def eos_term(t, e, var):
             der = VD.zeros(d.dom, d.B)
         else:
             d.coef_i()
-            hv = v.c[0]
-            out = np.empty_like(d.c)
-            for b in range(d.B):
-                out[b] = np.vectorize(lambda x, y: _eos_point(e, var, x, y))(hv, d.c[b])
-            der = VD(d.dom, d.B, c=out, base=d.base)
+            der = VD(d.dom, d.B, c=_eos_array(e, var, v.c[0][None], d.c), base=d.base)
     return OTerm(t.dom, val, der)
 
 
