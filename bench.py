@@ -547,6 +547,83 @@ def roofline_for(cat, st, peaks, peak_kind, N, fp64_tflops=None):
             "launches": st["launches"], "avg_launch_ms": per_launch_ms}
 
 
+def run_large(args, local):
+    """The binary-BH configuration's size (twelve domains at (11, 9, 8),
+    N = 40,081, a 12.9 GB FP64 Jacobian) on a spherical space: complete
+    Newton solves with the mixed LU and with the FP64 LU from the same
+    initial guess, timed per step with CUDA events, and the difference of
+    the two converged solutions."""
+    import numpy as np
+    import torch
+
+    from kadath_frontera_gb300 import Context
+    from kadath_frontera_gb300 import kadath as KD
+    from kadath_frontera_gb300 import workloads
+
+    ctx = Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream_ptr, device=f"cuda:{local}")
+    wl = workloads.star_large(ctx=ctx)
+    syst = wl.syst
+    N = syst.get_nbr_unknowns()
+
+    def solve(mode):
+        wl.restore()
+        syst.cache_tangents(False)
+        syst.cache_tangents(True)
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        reps = []
+        for _ in range(12):
+            done, err = syst.do_newton(args.precision, lu_mode=mode)
+            reps.append(dict(syst.last_report))
+            if done:
+                break
+        ev1.record(stream)
+        ev1.synchronize()
+        if not done:
+            raise RuntimeError(f"large: no convergence (|F| = {err:.3e})")
+        return ev0.elapsed_time(ev1) / max(len(reps) - 1, 1), len(reps) - 1, reps
+
+    solve(KD.KD_LU_TF32_IR)  # warm-up: matrices, tables, seeds, workspaces
+    with ClockSampler(local) as clk:
+        mixed = [solve(KD.KD_LU_TF32_IR) for _ in range(max(1, args.steps))]
+        sol_mixed = wl.download()
+        fp64 = solve(KD.KD_LU_FP64)
+        sol_fp64 = wl.download()
+    # one instrumented mixed solve: kernel time and work per category
+    KD.profile_enable(ctx, True)
+    solve(KD.KD_LU_TF32_IR)
+    prof = KD.profile_read(ctx)
+    KD.profile_enable(ctx, False)
+    diff = 0.0
+    for fa, fb in zip(sol_mixed, sol_fp64):
+        for a, b in zip(fa, fb):
+            diff = max(diff, float(np.abs(a - b).max() / max(1.0, np.abs(b).max())))
+
+    def phases(rep):
+        return {k: rep[k] for k in ("t_residual_ms", "t_assembly_ms", "t_factor_ms", "t_solve_ms", "t_update_ms")}
+    mixed_ms = statistics.mean(m[0] for m in mixed)
+    line = {
+        "metric": METRIC + " (binary-BH size, spherical space)", "value": mixed_ms, "unit": "ms",
+        "n_gpus": 1, "steps": len(mixed), "higher_is_better": False, "data": "synthetic",
+        "config": {"workload": "star, 12 domains at (11,9,8), matter inside r = 8", "N": N,
+                   "jacobian_gb_fp64": 8.0 * N * N / 1e9, "precision": args.precision,
+                   "step": "mean Newton step of complete solves (CUDA events)"},
+        "fp64_ms_per_step": fp64[0], "mixed_speedup_vs_fp64": fp64[0] / mixed_ms,
+        "updates": {"mixed": mixed[0][1], "fp64": fp64[1]},
+        "phases_ms_first_step": {"mixed": phases(mixed[-1][2][0]), "fp64": phases(fp64[2][0])},
+        "refine": {"iters": mixed[-1][2][0]["refine_iters"],
+                   "rel_residual": mixed[-1][2][0]["refine_rel_residual"]},
+        "mixed_vs_fp64_solution_max_rel_diff": diff,
+        "kernel_profile_ms": {k: round(v["ms"], 3) for k, v in prof.items()},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -562,12 +639,16 @@ def main():
     ap.add_argument("--export-points", type=int, default=1 << 20,
                     help="points of the exporter measurement (0: skip)")
     ap.add_argument("--batch-threads", type=int, default=8)
+    ap.add_argument("--large", action="store_true",
+                    help="only the binary-BH-size measurement (N = 40,081): mixed and FP64 solves")
     args = ap.parse_args()
     if args.impl == "reference":
         # rank 0 alone runs the CPU reference; other ranks exit without work
         rank = int(os.environ.get("RANK", "0"))
         return run_reference(args, int(os.environ.get("WORLD_SIZE", "1")), rank)
     ws, rank, local = dist_setup()
+    if args.large:
+        return run_large(args, local)
     return run_gpu(args, ws, rank, local)
 
 

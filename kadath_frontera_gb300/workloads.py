@@ -108,7 +108,7 @@ def toy(res=(13, 7, 4), bounds=(1.0, 2.0), ctx=None) -> Workload:
     return Workload("toy", space, syst, [("psi", psi)], [rho])
 
 
-def star(res=(13, 9, 4), bounds=STAR_BOUNDS, ctx=None, rho_c=STAR_RHOC) -> Workload:
+def star(res=(13, 9, 4), bounds=STAR_BOUNDS, ctx=None, rho_c=STAR_RHOC, matter_domains=1) -> Workload:
     space = Space_spheric(CHEB_TYPE, (0, 0, 0), res, bounds, ctx=ctx)
     nd = space.get_nbr_domains()
     P = Scalar(space, 1.0).std_base()
@@ -124,7 +124,7 @@ def star(res=(13, 9, 4), bounds=STAR_BOUNDS, ctx=None, rho_c=STAR_RHOC) -> Workl
     E = Scalar(space)
     E2S = Scalar(space)
     for d in range(nd):
-        e, e2s = star_matter_values(space.get_radius(d), space.domain_info(d)["type"] == 1, rho_c)
+        e, e2s = star_matter_values(space.get_radius(d), d < matter_domains, rho_c)
         E.set_domain(d, e)
         E2S.set_domain(d, e2s)
     E.std_base()
@@ -148,6 +148,17 @@ def star(res=(13, 9, 4), bounds=STAR_BOUNDS, ctx=None, rho_c=STAR_RHOC) -> Workl
     for nm in ("bx", "by", "bz"):
         syst.add_eq_bc(nd - 1, OUTER_BC, f"{nm} = 0")
     return Workload("star", space, syst, unknowns, [E, E2S])
+
+
+# The binary-BH configuration's size on a spherical space: twelve domains
+# (nucleus, ten shells, compactified exterior) at (11, 9, 8), the star's
+# five unknowns, matter in the four domains inside r = 8: N = 40,081.
+LARGE_RES = (11, 9, 8)
+LARGE_BOUNDS = (2.0, 4.0, 6.0, 8.0, 10.0, 12.0, 16.0, 20.0, 24.0, 28.0, 32.0)
+
+
+def star_large(ctx=None) -> Workload:
+    return star(LARGE_RES, LARGE_BOUNDS, ctx=ctx, matter_domains=4)
 
 
 STAR_VECTOR_EQUATIONS = {
@@ -259,7 +270,7 @@ def ns_tov(res=(13, 9, 4), bounds=NS_BOUNDS, ctx=None, rho_c=NS_RHOC) -> Workloa
     return Workload("ns_tov", space, syst, [("H", H), ("P", P), ("N", N)], [])
 
 
-WORKLOADS = {"toy": toy, "star": star, "star_vector": star_vector, "ns_tov": ns_tov}
+WORKLOADS = {"toy": toy, "star": star, "star_vector": star_vector, "ns_tov": ns_tov, "star_large": star_large}
 
 
 def solve(wl: Workload, precision=1e-10, lu_mode=None, max_steps=20) -> int:

@@ -93,12 +93,13 @@ STAR_RHOC = 1.28e-3
 STAR_K = 100.0
 
 
-def star_matter(d):
+def star_matter(d, matter_domains=1):
     """Frozen Gamma = 2 matter: Lane-Emden n = 1 density rho_c sinc(pi r/R)
-    inside the nucleus (radius R); E = rho (1 + K rho), S = 3 K rho^2."""
+    in the first matter_domains domains (the nucleus of radius R by default);
+    E = rho (1 + K rho), S = 3 K rho^2."""
     r = d.radius()
     rho = np.zeros(d.np)
-    if d.type == K.NUCLEUS:
+    if d.num < matter_domains:
         x = np.pi * r / STAR_R
         with np.errstate(invalid="ignore", divide="ignore"):
             rho = STAR_RHOC * np.where(x > 0, np.sin(x) / np.where(x > 0, x, 1.0), 1.0)
@@ -107,7 +108,7 @@ def star_matter(d):
     return E, S
 
 
-def star(res=(13, 9, 4), bounds=(STAR_R, 12.0, 16.0, 24.0, 32.0)):
+def star(res=(13, 9, 4), bounds=(STAR_R, 12.0, 16.0, 24.0, 32.0), matter_domains=1):
     """XCTS-shaped static star (oracle side): unknowns P (conformal factor),
     NP (lapse times P) and the Cartesian shift components bx, by, bz."""
     doms = K.space_spheric(res, list(bounds))
@@ -117,8 +118,8 @@ def star(res=(13, 9, 4), bounds=(STAR_R, 12.0, 16.0, 24.0, 32.0)):
     bx = K.scalar_field(doms, lambda d: np.zeros(d.np))
     by = K.scalar_field(doms, lambda d: np.zeros(d.np))
     bz = {d.num: K.VD(d, 1, c=np.zeros((1,) + d.np), base=_anti(d)) for d in doms}
-    E = K.scalar_field(doms, lambda d: star_matter(d)[0])
-    E2S = K.scalar_field(doms, lambda d: star_matter(d)[0] + 2 * star_matter(d)[1])
+    E = K.scalar_field(doms, lambda d: star_matter(d, matter_domains)[0])
+    E2S = K.scalar_field(doms, lambda d: star_matter(d, matter_domains)[0] + 2 * star_matter(d, matter_domains)[1])
     nd = len(doms)
     sysm = K.OSystem(doms, 0, nd - 1)
     for name, f in (("P", P), ("NP", NP), ("bx", bx), ("by", by), ("bz", bz)):

@@ -202,6 +202,30 @@ def test_star_workload_matches_oracle(ctx):
     assert done
 
 
+def test_star_eight_phi_points_matter_in_shells_matches_oracle(ctx):
+    """The large configuration's shape at small size: eight phi points,
+    matter over the nucleus and three shells (r < 8), six domains."""
+    from kadath_frontera_gb300 import workloads
+    res, bounds = (7, 5, 8), (2.0, 4.0, 6.0, 8.0, 12.0)
+    wl = workloads.star(res=res, bounds=bounds, matter_domains=4)
+    doms, osys, ofields, _ = configs.star(res=res, bounds=bounds, matter_domains=4)
+    F = wl.syst.sec_member()
+    J = wl.syst.jacobian()
+    Fo, Jo = osys.jacobian()
+    assert F.shape == Fo.shape
+    assert np.abs(F - Fo).max() <= 1e-13 * np.abs(Jo).max()
+    assert rel(J, Jo) < REL
+    done, err = wl.syst.do_newton(1e-10)
+    odone, oerr, _, _ = osys.newton_step(1e-10)
+    assert abs(err - oerr) <= 1e-12 * max(1.0, oerr)
+    for (nm, f), of in zip(wl.unknowns, ofields):
+        for d in range(len(doms)):
+            of[d].coef()
+            g = f.get_coef(d)
+            scale = max(np.linalg.norm(of[d].cf[0]), 1e-12)
+            assert np.linalg.norm(g - of[d].cf[0]) / scale < FIELD, (nm, d)
+
+
 def test_star_mixed_precision_newton_matches_fp64(ctx):
     """The mixed-precision LU (TF32 trailing updates + FP64 GMRES-IR) gives the
     same Newton iterates as the FP64 LU to 1e-10."""
