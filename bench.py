@@ -590,8 +590,8 @@ def run_large(args, local):
     with ClockSampler(local) as clk:
         mixed = [solve(KD.KD_LU_TF32_IR) for _ in range(max(1, args.steps))]
         sol_mixed = wl.download()
-        fp64 = solve(KD.KD_LU_FP64)
-        sol_fp64 = wl.download()
+        fp64 = solve(KD.KD_LU_FP64) if args.fp64_steps > 0 else None
+        sol_fp64 = wl.download() if fp64 else sol_mixed
     # one instrumented mixed solve: kernel time and work per category
     KD.profile_enable(ctx, True)
     solve(KD.KD_LU_TF32_IR)
@@ -611,12 +611,13 @@ def run_large(args, local):
         "config": {"workload": "star, 12 domains at (11,9,8), matter inside r = 8", "N": N,
                    "jacobian_gb_fp64": 8.0 * N * N / 1e9, "precision": args.precision,
                    "step": "mean Newton step of complete solves (CUDA events)"},
-        "fp64_ms_per_step": fp64[0], "mixed_speedup_vs_fp64": fp64[0] / mixed_ms,
-        "updates": {"mixed": mixed[0][1], "fp64": fp64[1]},
-        "phases_ms_first_step": {"mixed": phases(mixed[-1][2][0]), "fp64": phases(fp64[2][0])},
+        "fp64_ms_per_step": fp64[0] if fp64 else None,
+        "mixed_speedup_vs_fp64": fp64[0] / mixed_ms if fp64 else None,
+        "updates": {"mixed": mixed[0][1], "fp64": fp64[1] if fp64 else None},
+        "phases_ms_first_step": {"mixed": phases(mixed[-1][2][0]), "fp64": phases(fp64[2][0]) if fp64 else None},
         "refine": {"iters": mixed[-1][2][0]["refine_iters"],
                    "rel_residual": mixed[-1][2][0]["refine_rel_residual"]},
-        "mixed_vs_fp64_solution_max_rel_diff": diff,
+        "mixed_vs_fp64_solution_max_rel_diff": diff if fp64 else None,
         "kernel_profile_ms": {k: round(v["ms"], 3) for k, v in prof.items()},
         "clocks": clk.summary(),
     }

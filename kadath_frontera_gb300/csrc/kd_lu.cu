@@ -1365,9 +1365,14 @@ __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __re
 
 // Widest panel (96, 64 or 32 columns) whose rows fit in the shared memory of
 // one 16-CTA cluster; 0 when none does.
+// Widest panel (96 or 64 columns) whose rows fit the shared memory of one
+// 16-CTA cluster; 0 when neither does.  Narrower cluster panels are not
+// used: each panel costs one pass of the trailing matrix through HBM in the
+// update, and a 32-column panel triples that traffic, more than the cluster
+// saves over the cooperative grid kernel at 96 columns.
 static int cluster_panel_width(int rows) {
   const int per = (rows + CP_CL - 1) / CP_CL;
-  for (int w : {96, 64, 32})
+  for (int w : {96, 64})
     if (static_cast<size_t>(per) * cp_row_stride(w) * sizeof(float) <= CP_MAX_SMEM) return w;
   return 0;
 }
@@ -1612,6 +1617,8 @@ void DenseLU::factor_f32(float* A, long long ld, int N, bool tf32) {
   // updated first, then the rest of the trailing update runs on a side
   // stream as 16-CTA clusters that leave one GPC free, while the next panel
   // is factored on the main stream; the next row exchanges wait for both.
+  // A panel on the cooperative grid needs every SM, so it cannot run beside
+  // the update: look-ahead only when the next panel fits a cluster.
   const bool lookahead = tf32 && tf32_update_max_clusters16() >= 2;
   int j0 = 0, jb = width(0);
   bool map_ready = panel_factor<float>(ctx_, A, ld, N, j0, jb, ipiv_, d_info_, nsm_, slot_mem_, swap_map_);
@@ -1630,7 +1637,7 @@ void DenseLU::factor_f32(float* A, long long ld, int N, bool tf32) {
     float* A22 = A + static_cast<long long>(j0 + jb) * ld + j0 + jb;
     // rows N .. ld of the working matrix are padding
     const int writable = static_cast<int>(ld - j0 - jb);
-    if (lookahead && m > jbn) {
+    if (lookahead && m > jbn && cluster_panel_width(N - j0n) > 0) {
       gemm_update_f32(ctx_, blas_, m, jbn, jb, A21, ld, A12, ld, A22, ld, tf32, writable, tf32_terms);
       ctx_->fork(1);
       ctx_->use(0);
