@@ -1365,16 +1365,22 @@ __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __re
 
 // Widest panel (96, 64 or 32 columns) whose rows fit in the shared memory of
 // one 16-CTA cluster; 0 when none does.
-// Widest panel (96 or 64 columns) whose rows fit the shared memory of one
-// 16-CTA cluster; 0 when neither does.  Narrower cluster panels are not
-// used: each panel costs one pass of the trailing matrix through HBM in the
-// update, and a 32-column panel triples that traffic, more than the cluster
-// saves over the cooperative grid kernel at 96 columns.
-static int cluster_panel_width(int rows) {
+// Widest panel (96, 64 or 32 columns, no narrower than min_w) whose rows fit
+// the shared memory of one 16-CTA cluster; 0 when none does.
+static int cluster_panel_width(int rows, int min_w = 32) {
   const int per = (rows + CP_CL - 1) / CP_CL;
-  for (int w : {96, 64})
-    if (static_cast<size_t>(per) * cp_row_stride(w) * sizeof(float) <= CP_MAX_SMEM) return w;
+  for (int w : {96, 64, 32})
+    if (w >= min_w && static_cast<size_t>(per) * cp_row_stride(w) * sizeof(float) <= CP_MAX_SMEM) return w;
   return 0;
+}
+
+// True when the cooperative grid kernel on `nsm` SMs holds a panel of this
+// height and width in shared memory (panel_grid's own test).
+static bool grid_panel_fits(int rows, int jb, int nsm, size_t elem) {
+  int nblk = (rows + GP_MIN_ROWS - 1) / GP_MIN_ROWS;
+  if (nblk > nsm) nblk = nsm;
+  const int per = (rows + nblk - 1) / nblk;
+  return static_cast<size_t>(per) * jb * elem <= GP_MAX_SMEM;
 }
 
 // Launches the cluster panel on the smallest cluster (2, 4, 8 or 16 CTAs)
@@ -1603,15 +1609,23 @@ void DenseLU::factor_f32(float* A, long long ld, int N, bool tf32) {
   const int NB = nb > 96 ? 96 : nb;
   cudaStream_t s = ctx_->stream();
   cuda_check(cudaMemsetAsync(d_info_, 0, sizeof(int), s), "memset info");
-  // Panel width: NB, narrowed while the panel is too tall for the shared
-  // memory of one 16-CTA cluster (blocked LU allows any widths).
+  // Panel width (blocked LU allows any widths).  A cluster panel of 96 or
+  // 64 columns when its rows fit one 16-CTA cluster.  Taller panels: 96
+  // columns on the cooperative grid when it holds them, since each panel
+  // costs one pass of the trailing matrix through HBM in the update and a
+  // 32-column panel triples that traffic; a 32-column cluster panel when the
+  // grid cannot (a context limited to a share of the SMs).
+  const int nsm_eff = nsm_ < ctx_->sms() ? nsm_ : ctx_->sms();
+  auto on_cluster = [&](int rows) {
+    if (NB != 96) return false;
+    if (cluster_panel_width(rows, 64) > 0) return true;
+    return !grid_panel_fits(rows, 96, nsm_eff, sizeof(float)) && cluster_panel_width(rows) > 0;
+  };
   auto width = [&](int j0) {
+    const int rows = N - j0;
     int w = NB;
-    if (NB == 96) {
-      const int cw = cluster_panel_width(N - j0);
-      if (cw > 0) w = cw;
-    }
-    return (N - j0 < w) ? N - j0 : w;
+    if (on_cluster(rows)) w = cluster_panel_width(rows);
+    return (rows < w) ? rows : w;
   };
   // Look-ahead (tensor-core update only): the columns of the next panel are
   // updated first, then the rest of the trailing update runs on a side
@@ -1637,7 +1651,7 @@ void DenseLU::factor_f32(float* A, long long ld, int N, bool tf32) {
     float* A22 = A + static_cast<long long>(j0 + jb) * ld + j0 + jb;
     // rows N .. ld of the working matrix are padding
     const int writable = static_cast<int>(ld - j0 - jb);
-    if (lookahead && m > jbn && cluster_panel_width(N - j0n) > 0) {
+    if (lookahead && m > jbn && on_cluster(N - j0n)) {
       gemm_update_f32(ctx_, blas_, m, jbn, jb, A21, ld, A12, ld, A22, ld, tf32, writable, tf32_terms);
       ctx_->fork(1);
       ctx_->use(0);
