@@ -227,8 +227,10 @@ __global__ void __launch_bounds__(TC_THREADS) tf32_update_kernel(const float* __
 //           C -= acc in shared memory, TMA store of the chunk.
 // Every mbarrier wait gives up after GP_TC_WAIT_NS; the CTA then sets the
 // error flag, lets its roles fall out of their loops and frees its TMEM.
-constexpr int P_THREADS = 192;
-constexpr int P_CSLOTS = 4;
+// warps: 0 operand producer, 1 MMA issuer, 2-5 epilogue, 6 C producer
+constexpr int P_THREADS = 224;
+constexpr int P_CSLOTS = 8;                              // most C chunks in flight
+constexpr int P_NST = 2;                                 // operand stages (one k-block each)
 constexpr int P_CCOLS = 32;                              // columns per C chunk
 constexpr int P_CHUNK_BYTES = TC_M * P_CCOLS * 4;        // 16 KiB
 constexpr int P_OPBLK_BYTES = 128 * 128;                 // 128 rows x 32 TF32
@@ -295,12 +297,13 @@ __global__ void __launch_bounds__(P_THREADS, 1)
                            int ncs, int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char p_raw[];
   char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(p_raw) + 1023) & ~uintptr_t(1023));
-  char* sA = base;
-  char* sB = sA + nkb * P_OPBLK_BYTES;
-  char* sAl = sB + nkb * P_OPBLK_BYTES;                 // lo parts (split3 only)
-  char* sBl = sAl + nkb * P_OPBLK_BYTES;
-  char* sC = split3 ? sBl + nkb * P_OPBLK_BYTES : sAl;  // ring of ncs C chunks
-  __shared__ uint64_t op_full, op_empty, acc_full[2], acc_empty[2], c_full[P_CSLOTS], c_empty[P_CSLOTS];
+  // P_NST operand stages, each one k-block of A, B (and their lo parts):
+  // the k-blocks of consecutive tiles stream through them
+  const int nplanes = split3 ? 4 : 2;
+  const int stage_bytes = nplanes * P_OPBLK_BYTES;
+  char* sC = base + P_NST * stage_bytes;  // ring of ncs C chunks
+  __shared__ uint64_t op_full[P_NST], op_empty[P_NST], acc_full[2], acc_empty[2], c_full[P_CSLOTS],
+      c_empty[P_CSLOTS];
   __shared__ uint32_t tmem_base_sh;
   __shared__ int abort_flag, epi_abort;
   volatile int* abort_v = &abort_flag;  // written by one role, polled by the others
@@ -309,8 +312,10 @@ __global__ void __launch_bounds__(P_THREADS, 1)
   if (threadIdx.x == 0) {
     abort_flag = 0;
     epi_abort = 0;
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&op_full)));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&op_empty)));
+    for (int i = 0; i < P_NST; i++) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&op_full[i])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&op_empty[i])));
+    }
     for (int i = 0; i < 2; i++) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&acc_full[i])));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&acc_empty[i])));
@@ -335,23 +340,32 @@ __global__ void __launch_bounds__(P_THREADS, 1)
   const uint32_t tmem = tmem_base_sh;
 
   if (warp == 0) {
-    if (lane == 0) {  // ------------------------------------------- producer
-      int it = 0, cchunk = 0;
-      for (int tile = blockIdx.x; tile < ntiles && !*abort_v; tile += gridDim.x, it++) {
+    if (lane == 0) {  // ---------------------------------- operand producer
+      int g = 0;  // k-blocks issued so far (all tiles)
+      for (int tile = blockIdx.x; tile < ntiles && !*abort_v; tile += gridDim.x) {
         const int tm = tile % ntm, tn = tile / ntm;
-        if (it > 0 && !p_wait(&op_empty, (it - 1) & 1)) {
-          *abort_v = 1;
-          break;
-        }
-        p_expect_tx(&op_full, (split3 ? 4u : 2u) * nkb * P_OPBLK_BYTES);
-        for (int kb = 0; kb < nkb; kb++) {
-          p_tma_load(sA + kb * P_OPBLK_BYTES, &mapA, kb * TC_KBLK, tm * TC_M, &op_full);
-          p_tma_load(sB + kb * P_OPBLK_BYTES, &mapB, kb * TC_KBLK, tn * TC_N, &op_full);
+        for (int kb = 0; kb < nkb; kb++, g++) {
+          const int st = g % P_NST, use = g / P_NST;
+          if (use > 0 && !p_wait(&op_empty[st], (use - 1) & 1)) {
+            *abort_v = 1;
+            break;
+          }
+          char* sp = base + st * stage_bytes;
+          p_expect_tx(&op_full[st], static_cast<uint32_t>(stage_bytes));
+          p_tma_load(sp, &mapA, kb * TC_KBLK, tm * TC_M, &op_full[st]);
+          p_tma_load(sp + P_OPBLK_BYTES, &mapB, kb * TC_KBLK, tn * TC_N, &op_full[st]);
           if (split3) {
-            p_tma_load(sAl + kb * P_OPBLK_BYTES, &mapAlo, kb * TC_KBLK, tm * TC_M, &op_full);
-            p_tma_load(sBl + kb * P_OPBLK_BYTES, &mapBlo, kb * TC_KBLK, tn * TC_N, &op_full);
+            p_tma_load(sp + 2 * P_OPBLK_BYTES, &mapAlo, kb * TC_KBLK, tm * TC_M, &op_full[st]);
+            p_tma_load(sp + 3 * P_OPBLK_BYTES, &mapBlo, kb * TC_KBLK, tn * TC_N, &op_full[st]);
           }
         }
+      }
+    }
+  } else if (warp == 6) {
+    if (lane == 0) {  // ---------------------------------------- C producer
+      int cchunk = 0;
+      for (int tile = blockIdx.x; tile < ntiles && !*abort_v; tile += gridDim.x) {
+        const int tm = tile % ntm, tn = tile / ntm;
         for (int ch = 0; ch < TC_N / P_CCOLS; ch++, cchunk++) {
           const int slot = cchunk % ncs, use = cchunk / ncs;
           if (use > 0 && !p_wait(&c_empty[slot], (use - 1) & 1)) {
@@ -366,50 +380,57 @@ __global__ void __launch_bounds__(P_THREADS, 1)
   } else if (warp == 1) {
     if (lane == 0) {  // ------------------------------------------- MMA issuer
       const uint32_t idesc = tf32_idesc(TC_M, TC_N);
-      const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
-      const uint32_t al0 = smem_u32(sAl), bl0 = smem_u32(sBl);
-      int it = 0;
+      int it = 0, g = 0;
       for (int tile = blockIdx.x; tile < ntiles && !*abort_v; tile += gridDim.x, it++) {
         const int acc = it & 1, use = it >> 1;
         if (use > 0 && !p_wait(&acc_empty[acc], (use - 1) & 1)) {
           *abort_v = 1;
           break;
         }
-        if (!p_wait(&op_full, it & 1)) {
-          *abort_v = 1;
-          break;
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t d = tmem + static_cast<uint32_t>(acc * TC_N);
-        for (int kb = 0; kb < nkb; kb++) {
+        bool ok = true;
+        for (int kb = 0; kb < nkb; kb++, g++) {
+          const int st = g % P_NST;
+          if (!p_wait(&op_full[st], (g / P_NST) & 1)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t sp = smem_u32(base + st * stage_bytes);
           for (int k = 0; k < TC_KBLK / 8; k++) {
             const uint64_t koff = static_cast<uint64_t>((k * 32) >> 4);
-            const uint64_t ad = sw128_desc(a0 + kb * P_OPBLK_BYTES) + koff;
-            const uint64_t bd = sw128_desc(b0 + kb * P_OPBLK_BYTES) + koff;
+            const uint64_t ad = sw128_desc(sp) + koff;
+            const uint64_t bd = sw128_desc(sp + P_OPBLK_BYTES) + koff;
             uint32_t accum = (kb | k) ? 1u : 0u;
             if (split3) {  // small terms first: lo*hi, hi*lo, then hi*hi
-              const uint64_t ald = sw128_desc(al0 + kb * P_OPBLK_BYTES) + koff;
-              const uint64_t bld = sw128_desc(bl0 + kb * P_OPBLK_BYTES) + koff;
+              const uint64_t ald = sw128_desc(sp + 2 * P_OPBLK_BYTES) + koff;
+              const uint64_t bld = sw128_desc(sp + 3 * P_OPBLK_BYTES) + koff;
               tf32_mma(d, ald, bd, idesc, accum);
               tf32_mma(d, ad, bld, idesc, 1u);
               accum = 1u;
             }
             tf32_mma(d, ad, bd, idesc, accum);
           }
+          // the stage is free once these MMAs have read it
+          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                           smem_u32(&op_empty[st]))
+                       : "memory");
         }
-        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                         smem_u32(&op_empty))
-                     : "memory");
+        if (!ok) {
+          *abort_v = 1;
+          break;
+        }
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                          smem_u32(&acc_full[acc]))
                      : "memory");
       }
     }
-  } else {  // -------------------------------------------------------- epilogue
+  } else {  // ---------------------------------------------- epilogue (2-5)
     const int et = threadIdx.x - 64;      // 0..127
     const int quarter = warp & 3;         // TMEM lanes this warp may read
     const int row = quarter * 32 + lane;  // tile row
     int it = 0, cchunk = 0;
+    int pend_slot = -1;  // slot whose TMA store may still be reading it (thread et == 0)
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, it++) {
       const int tm = tile % ntm, tn = tile / ntm;
       const int acc = it & 1;
@@ -444,14 +465,20 @@ __global__ void __launch_bounds__(P_THREADS, 1)
         if (et == 0) {
           p_tma_store(&mapC, cs, tm * TC_M, tn * TC_N + ch * P_CCOLS);
           asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-          asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-          p_arrive(&c_empty[slot]);
+          // one store stays in flight: the previous chunk's slot is free
+          // once its store has read it
+          asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+          if (pend_slot >= 0) p_arrive(&c_empty[pend_slot]);
+          pend_slot = slot;
           if (ch == TC_N / P_CCOLS - 1) p_arrive(&acc_empty[acc]);  // all 128 threads are past their loads
         }
       }
       if (epi_abort) break;
     }
-    if (et == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    if (et == 0) {
+      asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+      if (pend_slot >= 0) p_arrive(&c_empty[pend_slot]);
+    }
   }
   __syncthreads();
   if (threadIdx.x == 0 && (*abort_v || epi_abort)) atomicExch(err, 1);
@@ -589,10 +616,11 @@ void tf32_gemm_update(Context* ctx, int m, int n, int k, const float* A, long lo
                                       static_cast<int>(P_MAX_SMEM)),
                  "cudaFuncSetAttribute(tf32 persistent)");
     });
-    // shared memory: operands (x2 for the lo parts) + a ring of C chunks,
-    // four slots when they fit, else two
-    const size_t ops = static_cast<size_t>(split3 ? 4 : 2) * nkb * P_OPBLK_BYTES;
-    const int ncs = (1024 + ops + P_CSLOTS * P_CHUNK_BYTES <= P_MAX_SMEM) ? P_CSLOTS : 2;
+    // shared memory: P_NST operand stages of one k-block each (x2 for the
+    // lo parts), then as many C chunks as fit, up to P_CSLOTS
+    const size_t ops = static_cast<size_t>(P_NST) * (split3 ? 4 : 2) * P_OPBLK_BYTES;
+    int ncs = static_cast<int>((P_MAX_SMEM - 1024 - ops) / P_CHUNK_BYTES);
+    if (ncs > P_CSLOTS) ncs = P_CSLOTS;
     const size_t psmem = 1024 + ops + static_cast<size_t>(ncs) * P_CHUNK_BYTES;
     if (psmem > P_MAX_SMEM) throw KdError(KD_ERR_UNSUPPORTED, "tcgen05 update: operands do not fit in shared memory");
     const int ntm = mpad / TC_M, ntiles = ntm * (npad / TC_N);
