@@ -625,6 +625,52 @@ def run_large(args, local):
     return 0
 
 
+def run_gemm(args, local):
+    """The tensor-core trailing update C -= A B alone (kd_tf32x3_gemm_update,
+    3xTF32) at m x n x k, C column-major FP32: median of --steps timed calls
+    after --warmup, CUDA events on the library's stream."""
+    import ctypes as C
+
+    import torch
+
+    from kadath_frontera_gb300 import Context, _lib
+
+    m, n, k = (int(x) for x in args.gemm.split(","))
+    ctx = Context(local)
+    lib = _lib.load()
+    f = lib.kd_tf32x3_gemm_update
+    f.restype = C.c_int
+    f.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_longlong, C.c_void_p, C.c_longlong,
+                  C.c_void_p, C.c_longlong]
+    dev = f"cuda:{local}"
+    g = torch.Generator(device=dev).manual_seed(0)
+    A = torch.randn(k * m, device=dev, generator=g)   # m x k, lda = m
+    B = torch.randn(n * k, device=dev, generator=g)   # k x n, ldb = k
+    Cm = torch.randn(n * m, device=dev, generator=g)  # m x n, ldc = m
+    stream = torch.cuda.ExternalStream(ctx.stream_ptr, device=dev)
+
+    def call():
+        ctx.check(f(ctx.h, m, n, k, A.data_ptr(), m, B.data_ptr(), k, Cm.data_ptr(), m))
+    for _ in range(max(args.warmup, 1)):
+        call()
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(max(args.steps, 1)):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        call()
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    med = statistics.median(ms)
+    cbytes = 8.0 * m * n
+    print(json.dumps({"kernel": "tf32_update_persistent (3xTF32)", "m": m, "n": n, "k": k, "ms_median": med,
+                      "c_bytes": cbytes, "c_traffic_TBps": cbytes / med / 1e9,
+                      "useful_tflops": 2.0 * m * n * k / med / 1e9}), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -640,6 +686,8 @@ def main():
     ap.add_argument("--export-points", type=int, default=1 << 20,
                     help="points of the exporter measurement (0: skip)")
     ap.add_argument("--batch-threads", type=int, default=8)
+    ap.add_argument("--gemm", default=None, metavar="M,N,K",
+                    help="only the tensor-core trailing update at this shape")
     ap.add_argument("--large", action="store_true",
                     help="only the binary-BH-size measurement (N = 40,081): mixed and FP64 solves")
     args = ap.parse_args()
@@ -650,6 +698,8 @@ def main():
     ws, rank, local = dist_setup()
     if args.large:
         return run_large(args, local)
+    if args.gemm:
+        return run_gemm(args, local)
     return run_gpu(args, ws, rank, local)
 
 
