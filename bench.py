@@ -247,6 +247,7 @@ def run_gpu(args, ws, rank, local):
     stream = torch.cuda.ExternalStream(ctx.stream_ptr, device=f"cuda:{local}")
     wl = workloads.WORKLOADS[args.workload](ctx=ctx)
     syst = wl.syst
+    syst.graph_capture = not args.no_graph
     N = syst.get_nbr_unknowns()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")  # 256 MB > L2
 
@@ -367,6 +368,8 @@ def run_gpu(args, ws, rank, local):
                            "(one timed unit = one solve; caches that outlive a step cleared per solve)",
                    "newton_updates_per_solve": updates, "solves_timed": args.steps,
                    "l2": "flushed between solves (256 MB write); the 1.2 GB Jacobian exceeds L2 within a solve",
+                   "residual_graph": {"on": not args.no_graph,
+                                      "captures_replays": list(syst.graph_stats())},
                    "parallelism": "replicas" if ws > 1 else "single"},
         "fp64_ms_per_step": fp64_ms, "mixed_speedup_vs_fp64": fp64_ms / mixed_ms if mixed_ms > 0 else None,
         "first_step_ms": {"mixed": first_m, "fp64": first_f},
@@ -564,6 +567,7 @@ def run_large(args, local):
     stream = torch.cuda.ExternalStream(ctx.stream_ptr, device=f"cuda:{local}")
     wl = workloads.star_large(ctx=ctx)
     syst = wl.syst
+    syst.graph_capture = not args.no_graph
     N = syst.get_nbr_unknowns()
 
     def solve(mode):
@@ -688,6 +692,8 @@ def main():
     ap.add_argument("--batch-threads", type=int, default=8)
     ap.add_argument("--gemm", default=None, metavar="M,N,K",
                     help="only the tensor-core trailing update at this shape")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="run the residual's value pass without CUDA-graph replay")
     ap.add_argument("--large", action="store_true",
                     help="only the binary-BH-size measurement (N = 40,081): mixed and FP64 solves")
     args = ap.parse_args()

@@ -265,6 +265,8 @@ int kd_system_jacobian(kd_system* s, double* J);
  * later assemblies skip those subtrees.  On by default; 0 frees them.  No
  * reference counterpart: the reference recomputes every column of the
  * Jacobian at every step (do_col_J, src/System_of_eqs/solver.cpp:120). */
+/* Captures and replays of the residual's value pass (kd_newton_opts.graph_capture). */
+int kd_system_graph_stats(kd_system* s, long long* captures, long long* replays);
 int kd_system_cache_tangents(kd_system* s, int enable);
 int kd_system_jacobian_device(kd_system* s, double* dJ, long long ld);
 /* do_JX (src/System_of_eqs/solver.cpp:87-118): y = J x without forming J,
@@ -286,7 +288,11 @@ typedef struct kd_newton_opts {
   int lu_mode;       /* KD_LU_* */
   double gmres_tol;  /* relative residual target of the refinement */
   int max_refine;    /* GMRES iterations per restart */
-  int graph_capture; /* reserved */
+  int graph_capture; /* nonzero: the residual's value pass runs from a CUDA
+                        graph captured the second time the fields are in
+                        the same state (same representations, bases and
+                        numbers); systems with integral-type equations are
+                        never captured */
 } kd_newton_opts;
 
 typedef struct kd_newton_report {

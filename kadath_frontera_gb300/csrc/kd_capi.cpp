@@ -582,6 +582,13 @@ int kd_system_check_equations(kd_system* s, double* errors) {
   });
 }
 
+int kd_system_graph_stats(kd_system* s, long long* captures, long long* replays) {
+  if (!s || !s->sys || !captures || !replays) return KD_ERR_ARG;
+  *captures = s->sys->residual_graph_captures;
+  *replays = s->sys->residual_graph_replays;
+  return KD_OK;
+}
+
 int kd_system_cache_tangents(kd_system* s, int enable) {
   if (!s || !s->sys) return KD_ERR_ARG;
   return guarded(s->sp->ctx, [&] { s->sys->set_tangent_cache(enable != 0); });

@@ -44,6 +44,13 @@ class DVal {
   // Val_domain::der_var / der_abs (val_domain.cpp:603-700); var in 1..3.
   DVal der_var(int var) const;
   DVal der_abs(int var) const;
+  // The same value without its lazily computed derivatives.
+  DVal plain() const {
+    DVal d = *this;
+    d.dvar_.reset();
+    d.dabs_.reset();
+    return d;
+  }
 
  private:
   mutable std::shared_ptr<std::array<std::shared_ptr<DVal>, 3>> dvar_, dabs_;

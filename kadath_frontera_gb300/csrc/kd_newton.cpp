@@ -43,6 +43,7 @@ bool Newton::step(const NewtonOpts& o, NewtonReport& rep) {
   cudaStream_t s = ctx->stream();
   long long l0 = ctx->launches;
   rep = NewtonReport();
+  sys_->set_residual_graph(o.graph_capture != 0);
   auto t0 = std::chrono::steady_clock::now();
   if (sys_->nbr_conditions() < 0) sys_->residual(nullptr);  // fixes nbr_conditions on the first call
   int N = sys_->nbr_conditions();

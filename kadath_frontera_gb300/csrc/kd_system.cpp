@@ -363,6 +363,52 @@ System::System(Context* c, const Space* s, int dmin, int dmax) : ctx(c), sp(s), 
   if (dmin < 0 || dmax >= s->ndom() || dmin > dmax) throw KdError(KD_ERR_ARG, "bad domain range for the system");
 }
 
+System::~System() { drop_graph(); }
+
+void System::drop_graph() {
+  for (auto& g : graphs_)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+  graphs_.clear();
+  seen_sigs_.clear();
+}
+
+void System::set_residual_graph(bool on) {
+  graph_on_ = on;
+  if (!on) drop_graph();
+}
+
+// Everything the launches of a value pass depend on besides the fields'
+// data: which representations each field holds and its bases, the numbers
+// that enter kernels as arguments, the registered symbols and equations.
+std::vector<long long> System::state_signature() const {
+  std::vector<long long> g;
+  auto dbl = [&](double v) {
+    long long b;
+    std::memcpy(&b, &v, sizeof b);
+    g.push_back(b);
+  };
+  auto field = [&](const Field* f) {
+    g.push_back(reinterpret_cast<long long>(f));
+    for (const auto& p : f->d) {
+      g.push_back((p.zero ? 1 : 0) | (p.in_conf ? 2 : 0) | (p.in_coef ? 4 : 0) | (p.base.def ? 8 : 0));
+      g.push_back(p.base.p);
+      for (int v : p.base.r) g.push_back(v);
+      for (int v : p.base.t) g.push_back(v);
+    }
+  };
+  g.push_back(static_cast<long long>(eqs_.size()));
+  g.push_back(static_cast<long long>(ieqs_.size()));
+  g.push_back(static_cast<long long>(defs_.size()));
+  g.push_back(static_cast<long long>(user_opes_.size()));
+  for (const auto& v : vars_) field(v.f);
+  for (const auto& v : vdoubles_) dbl(v.value);
+  for (const auto& c : csts_) {
+    if (c.is_field) field(c.f);
+    else dbl(c.value);
+  }
+  return g;
+}
+
 namespace {
 std::string bare(const std::string& s) {
   std::string t = trim_expr(s);
@@ -925,6 +971,90 @@ int System::nbr_unknowns() {
 }
 
 void System::residual(double* d_F, bool record) {
+  const bool graphable = graph_on_ && !graph_failed_ && record && d_F && nbr_conditions_ >= 0 && ieqs_.empty() &&
+                         !ctx->prof_on() && !ctx->capturing;
+  if (!graphable) {
+    residual_pass(d_F, record);
+    return;
+  }
+  std::vector<long long> sig = state_signature();
+  cudaStream_t main = ctx->main_stream();
+  graph_clock_++;
+  for (auto& g : graphs_)
+    if (g.F == d_F && g.sig == sig) {
+      // the node values the Jacobian reads: the captured pass's (host
+      // side), refilled on the device by the replay
+      vcache_.vals = g.vals;
+      vcache_.arena.release_to(g.mark);
+      vcache_.valid = true;
+      ctx->scratch().reset();
+      cuda_check(cudaGraphLaunch(g.exec, main), "replay value pass");
+      ctx->launches += g.launches;
+      g.last_use = graph_clock_;
+      residual_graph_replays++;
+      return;
+    }
+  // a state met for the first time runs as it is (it also sizes the arenas
+  // and uploads the tables); the second time it is captured
+  if (std::find(seen_sigs_.begin(), seen_sigs_.end(), sig) == seen_sigs_.end()) {
+    if (seen_sigs_.size() >= 16) seen_sigs_.erase(seen_sigs_.begin());
+    seen_sigs_.push_back(sig);
+    residual_pass(d_F, record);
+    return;
+  }
+  cudaGraph_t graph = nullptr;
+  cuda_check(cudaStreamBeginCapture(main, cudaStreamCaptureModeThreadLocal), "begin capture");
+  ctx->capturing = true;
+  const long long l0 = ctx->launches;
+  try {
+    residual_pass(d_F, true);
+  } catch (...) {
+    ctx->capturing = false;
+    cudaStreamEndCapture(main, &graph);
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    graph_failed_ = true;  // something in the pass cannot be captured
+    residual_pass(d_F, record);
+    return;
+  }
+  ctx->capturing = false;
+  cuda_check(cudaStreamEndCapture(main, &graph), "end capture");
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t st = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (st != cudaSuccess) {
+    cudaGetLastError();
+    graph_failed_ = true;
+    residual_pass(d_F, record);
+    return;
+  }
+  if (graphs_.size() >= 4) {
+    auto lru = std::min_element(graphs_.begin(), graphs_.end(),
+                                [](const ValueGraph& a, const ValueGraph& b) { return a.last_use < b.last_use; });
+    cudaGraphExecDestroy(lru->exec);
+    graphs_.erase(lru);
+  }
+  ValueGraph g;
+  g.sig = std::move(sig);
+  g.exec = exec;
+  g.F = d_F;
+  g.launches = ctx->launches - l0;
+  for (const auto& kv : vcache_.vals) {
+    Term t = kv.second;
+    for (auto& v : t.vt) v = v.plain();
+    g.vals.emplace(kv.first, std::move(t));
+  }
+  g.mark = vcache_.arena.mark();
+  g.last_use = graph_clock_;
+  residual_graph_captures++;
+  // the capture ran nothing: the pass itself is the first replay
+  ctx->launches = l0 + g.launches;
+  vcache_.vals = g.vals;
+  cuda_check(cudaGraphLaunch(g.exec, main), "replay value pass");
+  graphs_.push_back(std::move(g));
+}
+
+void System::residual_pass(double* d_F, bool record) {
   ctx->scratch().reset();
   vcache_.clear();
   std::unique_ptr<ScratchRedirect> redirect;

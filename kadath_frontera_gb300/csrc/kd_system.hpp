@@ -170,6 +170,9 @@ struct IntEquation {
 class System {
  public:
   System(Context* ctx, const Space* sp, int dom_min, int dom_max);
+  ~System();
+  System(const System&) = delete;
+  System& operator=(const System&) = delete;
 
   Context* ctx;
   const Space* sp;
@@ -285,6 +288,13 @@ class System {
   void val_point_gradient(int var, const double point[3], double* g);
   // Fields changed outside update_from_x: drop the recorded node values.
   void invalidate_values() { vcache_.clear(); }
+  // Replays the value pass of residual(d_F, true) from a CUDA graph when the
+  // state it depends on (field representations and bases, the numbers, the
+  // equations) is the one it was captured in; captures it otherwise.
+  // Systems with integral-type equations are never captured (their values
+  // come back to the host in the pass).
+  void set_residual_graph(bool on);
+  long long residual_graph_replays = 0, residual_graph_captures = 0;
 
   struct VarInfo {
     std::string name;
@@ -340,6 +350,23 @@ class System {
   ValueCache vcache_;
   TangentCache tcache_;
   bool cache_tangents_ = true;
+  // residual graphs, one per state seen at least twice (at most 4)
+  struct ValueGraph {
+    std::vector<long long> sig;
+    cudaGraphExec_t exec = nullptr;
+    double* F = nullptr;
+    long long launches = 0;
+    std::unordered_map<const Ope*, Term> vals;
+    size_t mark = 0;
+    long long last_use = 0;
+  };
+  bool graph_on_ = false, graph_failed_ = false;
+  std::vector<ValueGraph> graphs_;
+  std::vector<std::vector<long long>> seen_sigs_;
+  long long graph_clock_ = 0;
+  std::vector<long long> state_signature() const;
+  void residual_pass(double* d_F, bool record);
+  void drop_graph();
 
   void compute_unknowns();
   void apply(Equation& eq, EvalState& st, Term& lhs, Term& rhs, bool do_lhs, bool do_rhs);

@@ -95,6 +95,7 @@ def _declare_system(lib):
         "kd_system_check_equations": (I, [P, DP]),
         "kd_system_jacobian": (I, [P, DP]),
         "kd_system_cache_tangents": (I, [P, I]),
+        "kd_system_graph_stats": (I, [P, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
         "kd_system_jx": (I, [P, DP, DP]),
         "kd_system_jacobian_device": (I, [P, P, C.c_longlong]),
         "kd_system_update": (I, [P, DP]),
@@ -387,6 +388,7 @@ class System_of_eqs:
         self.h = h
         self._keep = []
         self.lu_mode = KD_LU_FP64
+        self.graph_capture = False
         self.last_report = None
         self._J = None
 
@@ -551,16 +553,26 @@ class System_of_eqs:
         self.ctx.check(_L().kd_system_update(self.h, _dp(x)))
         self._J = None
 
-    def do_newton(self, precision, lu_mode=None, gmres_tol=1e-14, max_refine=50, solver=None):
+    def do_newton(self, precision, lu_mode=None, gmres_tol=1e-14, max_refine=50, solver=None, graph=None):
         """System_of_eqs::do_newton(precision, error, solver): returns
-        (converged, error); solver NEWTON_RAPHSON (default) or GAUSS_NEWTON."""
-        opts = NewtonOpts(precision, self.lu_mode if lu_mode is None else lu_mode, gmres_tol, max_refine, 0)
+        (converged, error); solver NEWTON_RAPHSON (default) or GAUSS_NEWTON.
+        graph: replay the residual's value pass from a CUDA graph (default:
+        the system's graph_capture attribute)."""
+        g = self.graph_capture if graph is None else graph
+        opts = NewtonOpts(precision, self.lu_mode if lu_mode is None else lu_mode, gmres_tol, max_refine,
+                          1 if g else 0)
         rep = NewtonReport()
         fn = _L().kd_newton_step_gauss_newton if solver == GAUSS_NEWTON else _L().kd_newton_step
         self.ctx.check(fn(self.h, C.byref(opts), C.byref(rep)))
         self.last_report = rep.as_dict()
         self._J = None
         return bool(rep.converged), rep.error
+
+    def graph_stats(self):
+        """(captures, replays) of the residual's value pass."""
+        c, r = C.c_longlong(), C.c_longlong()
+        self.ctx.check(_L().kd_system_graph_stats(self.h, C.byref(c), C.byref(r)))
+        return c.value, r.value
 
     def do_newton_with_linesearch(self, precision, ntrymax=10, stepmax=1.0, lu_mode=None, gmres_tol=1e-14,
                                   max_refine=50):
