@@ -180,6 +180,24 @@ int kd_field_get_base(const kd_field* f, int dom, int* base_r, int* base_t, int*
 /* dst = src on every domain, device to device (Scalar copy assignment). */
 int kd_field_copy(kd_field* dst, const kd_field* src);
 
+/* ---- Save files (Kadath's binary format, every number big-endian) ------- */
+/* The files Space_spheric::save, Scalar::save and Tensor::save write
+ * (src/Space/Spheric/space_spheric.cpp:124, src/Scalar/scalar.cpp:64,
+ * src/Tensor/tensor.cpp:361; fwrite_be, src/Utilities/fwrite_be.cpp), read
+ * back as Space_spheric(FILE*, withzec), Scalar(space, FILE*) and
+ * Tensor(space, FILE*) read them.  Items follow one another in the order
+ * they are saved, as with the reference's FILE*. */
+typedef struct kd_file kd_file;
+int kd_file_open(const char* path, const char* mode, kd_file** out); /* mode "wb" or "rb" */
+int kd_file_close(kd_file* f);
+int kd_space_save(const kd_space* sp, kd_file* f);
+int kd_space_load(kd_ctx* ctx, kd_file* f, int withzec, kd_space** out);
+int kd_field_save(kd_field* fld, kd_file* f);
+int kd_field_load(kd_field* fld, kd_file* f); /* into a field of the same space */
+/* A Vector with the Cartesian basis: type_index CON (+1) or COV (-1). */
+int kd_vector_save(kd_field* fx, kd_field* fy, kd_field* fz, int type_index, kd_file* f);
+int kd_vector_load(kd_field* fx, kd_field* fy, kd_field* fz, int* type_index, kd_file* f);
+
 /* ---- System_of_eqs (include/system_of_eqs.hpp:54) ----------------------- */
 int kd_system_create(kd_space* sp, int dom_min, int dom_max, kd_system** out);
 int kd_system_destroy(kd_system* s);

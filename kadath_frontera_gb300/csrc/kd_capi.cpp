@@ -206,6 +206,7 @@ int kd_matrix_1d(kd_ctx* ctx, int op, int basis, int n_in, int n_out, double* ma
 // ------------------------------------------------------------------------
 // Spaces, fields, systems, Newton, LU.
 #include "kd_gemm_tc.hpp"
+#include "kd_io.hpp"
 #include "kd_newton.hpp"
 
 struct kd_space {
@@ -215,6 +216,10 @@ struct kd_space {
 struct kd_field {
   kd_space* sp;
   std::unique_ptr<kd::Field> f;
+};
+struct kd_file {
+  std::FILE* f = nullptr;
+  bool writing = false;
 };
 struct kd_system {
   kd_space* sp;
@@ -250,6 +255,59 @@ int kd_space_spheric_create(kd_ctx* ctx, const double center[3], const int res[3
     std::vector<double> b(bounds, bounds + nbounds);
     auto* s = new kd_space{ctx, std::make_unique<kd::Space>(center, res, b, withzec != 0)};
     *out = s;
+  });
+}
+
+int kd_file_open(const char* path, const char* mode, kd_file** out) {
+  if (!path || !mode || !out) return KD_ERR_ARG;
+  const std::string m(mode);
+  if (m != "wb" && m != "rb") return KD_ERR_ARG;
+  std::FILE* f = std::fopen(path, mode);
+  if (!f) return KD_ERR_ARG;
+  *out = new kd_file{f, m == "wb"};
+  return KD_OK;
+}
+
+int kd_file_close(kd_file* f) {
+  if (!f) return KD_ERR_ARG;
+  const int st = std::fclose(f->f) == 0 ? KD_OK : KD_ERR_ARG;
+  delete f;
+  return st;
+}
+
+int kd_space_save(const kd_space* sp, kd_file* f) {
+  if (!sp || !f || !f->writing) return KD_ERR_ARG;
+  return guarded(sp->ctx, [&] { kd::save_space(*sp->sp, f->f); });
+}
+
+int kd_space_load(kd_ctx* ctx, kd_file* f, int withzec, kd_space** out) {
+  if (!ctx || !f || f->writing || !out) return KD_ERR_ARG;
+  return guarded(ctx, [&] { *out = new kd_space{ctx, kd::load_space(f->f, withzec != 0)}; });
+}
+
+int kd_field_save(kd_field* fld, kd_file* f) {
+  if (!fld || !f || !f->writing) return KD_ERR_ARG;
+  return guarded(fld->sp->ctx, [&] { kd::save_field(*fld->f, f->f); });
+}
+
+int kd_field_load(kd_field* fld, kd_file* f) {
+  if (!fld || !f || f->writing) return KD_ERR_ARG;
+  return guarded(fld->sp->ctx, [&] { kd::load_field(*fld->f, f->f); });
+}
+
+int kd_vector_save(kd_field* fx, kd_field* fy, kd_field* fz, int type_index, kd_file* f) {
+  if (!fx || !fy || !fz || !f || !f->writing || fx->sp != fy->sp || fx->sp != fz->sp) return KD_ERR_ARG;
+  return guarded(fx->sp->ctx, [&] {
+    kd::Field* const c[3] = {fx->f.get(), fy->f.get(), fz->f.get()};
+    kd::save_vector(c, type_index, f->f);
+  });
+}
+
+int kd_vector_load(kd_field* fx, kd_field* fy, kd_field* fz, int* type_index, kd_file* f) {
+  if (!fx || !fy || !fz || !f || f->writing || fx->sp != fy->sp || fx->sp != fz->sp) return KD_ERR_ARG;
+  return guarded(fx->sp->ctx, [&] {
+    kd::Field* const c[3] = {fx->f.get(), fy->f.get(), fz->f.get()};
+    kd::load_vector(c, type_index, f->f);
   });
 }
 

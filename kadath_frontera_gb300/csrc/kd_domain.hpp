@@ -100,6 +100,7 @@ class Domain {
 class Space {
  public:
   Space(const double center[3], const int npts[3], const std::vector<double>& bounds, bool withzec);
+  explicit Space(std::vector<Domain> doms) : domains(std::move(doms)) {}
   std::vector<Domain> domains;
   int ndom() const { return static_cast<int>(domains.size()); }
   const Domain& dom(int d) const { return domains.at(d); }

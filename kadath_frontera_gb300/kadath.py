@@ -77,6 +77,14 @@ def _declare_system(lib):
         "kd_system_add_cst_field": (I, [P, C.c_char_p, P]),
         "kd_system_add_def": (I, [P, I, C.c_char_p]),
         "kd_system_add_var_vector": (I, [P, C.c_char_p, P, P, P]),
+        "kd_file_open": (I, [C.c_char_p, C.c_char_p, C.POINTER(P)]),
+        "kd_file_close": (I, [P]),
+        "kd_space_save": (I, [P, P]),
+        "kd_space_load": (I, [P, P, I, C.POINTER(P)]),
+        "kd_field_save": (I, [P, P]),
+        "kd_field_load": (I, [P, P]),
+        "kd_vector_save": (I, [P, P, P, I, P]),
+        "kd_vector_load": (I, [P, P, P, C.POINTER(C.c_int), P]),
         "kd_system_add_eq_order": (I, [P, I, I, C.c_char_p]),
         "kd_system_add_eq_full": (I, [P, I, C.c_char_p]),
         "kd_system_add_eq_first_integral": (I, [P, I, I, C.c_char_p, C.c_char_p]),
@@ -142,6 +150,33 @@ def _ip(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_int))
 
 
+class KadathFile:
+    """A save file in Kadath's binary format, written or read item by item
+    in order, as with the reference's FILE* (fopen(name, "w") / "r")."""
+
+    def __init__(self, path, mode="r"):
+        m = {"r": "rb", "w": "wb", "rb": "rb", "wb": "wb"}[mode]
+        h = C.c_void_p()
+        st = _L().kd_file_open(str(path).encode(), m.encode(), C.byref(h))
+        if st != 0:
+            raise KadathError(st, f"cannot open {path}")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            _L().kd_file_close(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+CON, COV = 1, -1
+
+
 class Space_spheric:
     """Space_spheric(type_coloc, center, res, bounds, withzec=True)."""
 
@@ -158,6 +193,27 @@ class Space_spheric:
         self.h = h
         self.res = tuple(int(v) for v in res)
         self.bounds = tuple(float(v) for v in bounds)
+
+    @classmethod
+    def from_file(cls, f: "KadathFile", withzec=True, ctx=None):
+        """Space_spheric(FILE*, withzec)."""
+        self = cls.__new__(cls)
+        self.ctx = ctx or default_context()
+        h = C.c_void_p()
+        self.ctx.check(_L().kd_space_load(self.ctx.h, f.h, 1 if withzec else 0, C.byref(h)))
+        self.h = h
+        info = [self.domain_info(d) for d in range(self.get_nbr_domains())]
+        self.res = tuple(int(v) for v in info[0]["nbr_points"])
+        bounds = [info[0]["alpha"]]
+        for d in info[1:]:
+            if d["type"] == 2:  # shell: beta + alpha
+                bounds.append(d["beta"] + d["alpha"])
+        self.bounds = tuple(bounds)
+        return self
+
+    def save(self, f: "KadathFile"):
+        """Space_spheric::save."""
+        self.ctx.check(_L().kd_space_save(self.h, f.h))
 
     def get_nbr_domains(self):
         n = C.c_int()
@@ -280,6 +336,17 @@ class Scalar:
         self.space.ctx.check(_L().kd_field_val_point(self.h, _dp(pt), C.byref(out)))
         return out.value
 
+    @classmethod
+    def from_file(cls, space: "Space_spheric", f: "KadathFile"):
+        """Scalar(space, FILE*)."""
+        s = cls(space)
+        space.ctx.check(_L().kd_field_load(s.h, f.h))
+        return s
+
+    def save(self, f: "KadathFile"):
+        """Scalar::save."""
+        self.space.ctx.check(_L().kd_field_save(self.h, f.h))
+
     def std_base_cart(self, c):
         """Basis of the Cartesian component c = 1, 2, 3 (x, y, z) of a vector."""
         self.space.ctx.check(_L().kd_field_cart_base(self.h, int(c) - 1))
@@ -351,6 +418,19 @@ class Vector:
         for c in self.cmp:
             c.set_value(v)
         return self
+
+    def save(self, f: "KadathFile", type_index=CON):
+        """Tensor::save of the vector (Cartesian basis)."""
+        self.space.ctx.check(_L().kd_vector_save(*[c.h for c in self.cmp], int(type_index), f.h))
+
+    @classmethod
+    def from_file(cls, space: "Space_spheric", f: "KadathFile"):
+        """Vector(space, FILE*); the index type read is kept in type_index."""
+        v = cls(space)
+        ti = C.c_int()
+        space.ctx.check(_L().kd_vector_load(*[c.h for c in v.cmp], C.byref(ti), f.h))
+        v.type_index = ti.value
+        return v
 
     def copy_from(self, other: "Vector"):
         for a, b in zip(self.cmp, other.cmp):
