@@ -115,7 +115,7 @@ class Context {
     PROF_GATHER = 2,     // tau export / affecte_tau gathers
     PROF_LU_PANEL = 3,
     PROF_LU_SWAP_TRSM = 4,
-    PROF_LU_GEMM = 5,    // trailing update
+    PROF_LU_GEMM = 5,    // trailing update (work: HBM bytes of the tensor-core update, flops of the FP64 GEMM)
     PROF_LU_SOLVE = 6,   // triangular solves
     PROF_GMRES = 7,      // refinement matvecs and vector ops
     PROF_NCAT = 8,

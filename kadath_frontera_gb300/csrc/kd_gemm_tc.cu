@@ -689,7 +689,9 @@ int tf32_gemm_error_flag(Context* ctx) {
 void gemm_update_f32(Context* ctx, cublasHandle_t blas, int m, int n, int k, const float* A, long long lda,
                      const float* B, long long ldb, float* C, long long ldc, bool tf32, int c_rows_writable,
                      int terms, bool spare_gpc) {
-  ProfScope ps(ctx, Context::PROF_LU_GEMM, 2.0 * m * n * k);
+  // work: the algorithmic HBM bytes (C read and written once, A and B read
+  // once); the update is bound by the C stream
+  ProfScope ps(ctx, Context::PROF_LU_GEMM, 8.0 * m * n + 4.0 * (static_cast<double>(m) + n) * k);
   if (tf32 && tf32_gemm_supported(k)) {
     if (terms == 3 && !tf32x3_gemm_possible(k, C, ldc, m, c_rows_writable)) terms = 1;
     tf32_gemm_update(ctx, m, n, k, A, lda, B, ldb, C, ldc, c_rows_writable, terms, spare_gpc);
