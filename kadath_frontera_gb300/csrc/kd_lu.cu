@@ -656,6 +656,7 @@ __device__ void block_argmax(V& v, int& i, int& tag, V* rv, int* ri, int* rt) {
 // ever written by its tile's CTA; block rows written by other CTAs are read
 // past L1.
 constexpr int SW_TILE = 64;
+constexpr int SW_MAXT = 24;  // tiles a CTA keeps in shared memory during a sweep
 
 // Geometry of one block step of a sweep.
 struct SweepStep {
@@ -785,11 +786,21 @@ __global__ void __launch_bounds__(256) trsv_sweep(const T* __restrict__ A, long 
   __shared__ double xx[TB];
   __shared__ T xt[TB];
   __shared__ T part[4][SW_TILE];
+  // The right-hand side of the rows this CTA updates (its tiles t with
+  // t = blockIdx.x mod gridDim.x), kept in shared memory for the whole
+  // sweep; a tile goes back to global memory when it is the next block.
+  __shared__ double bown[SW_MAXT][SW_TILE];
   __shared__ int s_ok;
   const int nblk = (N + TB - 1) / TB;
   const int ntiles = (N + SW_TILE - 1) / SW_TILE;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int quarter = warp & 3, half = warp >> 2;
+  const bool own = ntiles <= SW_MAXT * static_cast<int>(gridDim.x);
+  if (own && tid < SW_TILE)
+    for (int j = 0, t = blockIdx.x; t < ntiles; j++, t += gridDim.x) {
+      const int r = t * SW_TILE + tid;
+      bown[j][tid] = (r < N) ? b[r] : 0.0;
+    }
   SweepPrefetch<T> pf;
   sweep_prefetch(A, ld, Dinv, Dinv2, sweep_step(0, nblk, N, lower, ntiles), pf);
   for (int step = 0; step < nblk; step++) {
@@ -856,8 +867,18 @@ __global__ void __launch_bounds__(256) trsv_sweep(const T* __restrict__ A, long 
       __syncthreads();
       if (tid < SW_TILE) {
         const int r = t * SW_TILE + tid;
-        if (r >= s.q0 && r < s.q1)
-          b[r] = __ldcg(b + r) - static_cast<double>((part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]));
+        if (r >= s.q0 && r < s.q1) {
+          const double sub = static_cast<double>((part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]));
+          if (own) {
+            const int j = (t - static_cast<int>(blockIdx.x)) / static_cast<int>(gridDim.x);
+            const double v = bown[j][tid] - sub;
+            bown[j][tid] = v;
+            // the next block in sweep order reads its rows from global memory
+            if (t == (lower ? s.k + 1 : s.k - 1)) b[r] = v;
+          } else {
+            b[r] = __ldcg(b + r) - sub;
+          }
+        }
       }
       __syncthreads();
     }
