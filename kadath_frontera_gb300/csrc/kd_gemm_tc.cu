@@ -276,6 +276,31 @@ __device__ __forceinline__ void p_tma_load(void* dst, const CUtensorMap* map, in
       : "memory");
 }
 
+// C is streamed once per update: its loads and stores are marked to leave
+// L2 first, so that the operand tiles every CTA re-reads stay resident.
+__device__ __forceinline__ uint64_t p_evict_first() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+
+__device__ __forceinline__ void p_tma_load_stream(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar,
+                                                  uint64_t pol) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1, {%2, "
+      "%3}], [%4], %5;" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar)), "l"(pol)
+      : "memory");
+}
+
+__device__ __forceinline__ void p_tma_store_stream(const CUtensorMap* map, const void* src, int x, int y,
+                                                   uint64_t pol) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group.L2::cache_hint [%0, {%2, %3}], [%1], %4;" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(smem_u32(src)), "r"(x), "r"(y), "l"(pol)
+               : "memory");
+}
+
 __device__ __forceinline__ void p_tma_store(const CUtensorMap* map, const void* src, int x, int y) {
   asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];" ::"l"(
                    reinterpret_cast<uint64_t>(map)),
@@ -363,6 +388,7 @@ __global__ void __launch_bounds__(P_THREADS, 1)
     }
   } else if (warp == 6) {
     if (lane == 0) {  // ---------------------------------------- C producer
+      const uint64_t pol = p_evict_first();
       int cchunk = 0;
       for (int tile = blockIdx.x; tile < ntiles && !*abort_v; tile += gridDim.x) {
         const int tm = tile % ntm, tn = tile / ntm;
@@ -373,7 +399,8 @@ __global__ void __launch_bounds__(P_THREADS, 1)
             break;
           }
           p_expect_tx(&c_full[slot], P_CHUNK_BYTES);
-          p_tma_load(sC + slot * P_CHUNK_BYTES, &mapC, tm * TC_M, tn * TC_N + ch * P_CCOLS, &c_full[slot]);
+          p_tma_load_stream(sC + slot * P_CHUNK_BYTES, &mapC, tm * TC_M, tn * TC_N + ch * P_CCOLS, &c_full[slot],
+                            pol);
         }
       }
     }
@@ -463,7 +490,7 @@ __global__ void __launch_bounds__(P_THREADS, 1)
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         asm volatile("bar.sync 1, 128;" ::: "memory");
         if (et == 0) {
-          p_tma_store(&mapC, cs, tm * TC_M, tn * TC_N + ch * P_CCOLS);
+          p_tma_store_stream(&mapC, cs, tm * TC_M, tn * TC_N + ch * P_CCOLS, p_evict_first());
           asm volatile("cp.async.bulk.commit_group;" ::: "memory");
           // one store stays in flight: the previous chunk's slot is free
           // once its store has read it
