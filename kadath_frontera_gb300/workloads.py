@@ -87,13 +87,14 @@ class Workload:
         return sum(v.nbytes for per in self.initial_host for v in per)
 
 
-def toy(res=(13, 7, 4), bounds=(1.0, 2.0), ctx=None) -> Workload:
+def toy(res=(13, 7, 4), bounds=(1.0, 2.0), ctx=None, rho_values=None) -> Workload:
+    """rho_values: optional per-domain arrays of rho at the collocation points."""
     space = Space_spheric(CHEB_TYPE, (0, 0, 0), res, bounds, ctx=ctx)
     nd = space.get_nbr_domains()
     psi = Scalar(space, 1.0).std_base()
     rho = Scalar(space)
     for d in range(nd):
-        rho.set_domain(d, toy_rho_values(space.get_radius(d)))
+        rho.set_domain(d, toy_rho_values(space.get_radius(d)) if rho_values is None else rho_values[d])
     rho.std_base()
     syst = System_of_eqs(space, 0, nd - 1)
     syst.add_var("psi", psi)
@@ -108,7 +109,9 @@ def toy(res=(13, 7, 4), bounds=(1.0, 2.0), ctx=None) -> Workload:
     return Workload("toy", space, syst, [("psi", psi)], [rho])
 
 
-def star(res=(13, 9, 4), bounds=STAR_BOUNDS, ctx=None, rho_c=STAR_RHOC, matter_domains=1) -> Workload:
+def star(res=(13, 9, 4), bounds=STAR_BOUNDS, ctx=None, rho_c=STAR_RHOC, matter_domains=1, matter=None) -> Workload:
+    """matter: optional (E, E2S), each a list of per-domain value arrays at the
+    collocation points, used instead of the Lane-Emden profile."""
     space = Space_spheric(CHEB_TYPE, (0, 0, 0), res, bounds, ctx=ctx)
     nd = space.get_nbr_domains()
     P = Scalar(space, 1.0).std_base()
@@ -124,7 +127,10 @@ def star(res=(13, 9, 4), bounds=STAR_BOUNDS, ctx=None, rho_c=STAR_RHOC, matter_d
     E = Scalar(space)
     E2S = Scalar(space)
     for d in range(nd):
-        e, e2s = star_matter_values(space.get_radius(d), d < matter_domains, rho_c)
+        if matter is None:
+            e, e2s = star_matter_values(space.get_radius(d), d < matter_domains, rho_c)
+        else:
+            e, e2s = matter[0][d], matter[1][d]
         E.set_domain(d, e)
         E2S.set_domain(d, e2s)
     E.std_base()
@@ -168,7 +174,7 @@ STAR_VECTOR_EQUATIONS = {
 }
 
 
-def star_vector(res=(13, 9, 4), bounds=STAR_BOUNDS, ctx=None, rho_c=STAR_RHOC) -> Workload:
+def star_vector(res=(13, 9, 4), bounds=STAR_BOUNDS, ctx=None, rho_c=STAR_RHOC, matter=None) -> Workload:
     """The star with the shift as one Cartesian vector unknown ``bet`` and its
     equation in index notation with the flat metric: the form Kadath codes
     write.  Same fields and matter as ``star``; the unknowns of bet come
@@ -185,7 +191,10 @@ def star_vector(res=(13, 9, 4), bounds=STAR_BOUNDS, ctx=None, rho_c=STAR_RHOC) -
     E = Scalar(space)
     E2S = Scalar(space)
     for d in range(nd):
-        e, e2s = star_matter_values(space.get_radius(d), space.domain_info(d)["type"] == 1, rho_c)
+        if matter is None:
+            e, e2s = star_matter_values(space.get_radius(d), space.domain_info(d)["type"] == 1, rho_c)
+        else:
+            e, e2s = matter[0][d], matter[1][d]
         E.set_domain(d, e)
         E2S.set_domain(d, e2s)
     E.std_base()

@@ -81,3 +81,41 @@ def test_unsupported_pair_reports_status():
     ob = C.c_int()
     # div_x is defined only for the parity Chebyshev bases
     assert lib.kd_matrix_1d(None, S.OP_DIV_X, S.CHEB, 5, 5, m, C.byref(ob)) == _lib.KD_ERR_UNSUPPORTED
+
+
+def _reference_cases():
+    from pathlib import Path
+    z = np.load(Path(__file__).resolve().parent / "golden" / "ref_spectral_1d.npz")
+    out = []
+    for key in z.files:
+        if key.endswith("_base"):
+            continue
+        op, base, nin, nout = (int(t[1:] if t[0] in "bnm" else t[2:]) for t in key.split("_"))
+        out.append((op, base, nin, nout, z[key], int(z[key + "_base"])))
+    return out
+
+
+def test_product_matrices_match_the_reference():
+    """Every 1-D matrix the GPU applies, against the reference's own coef_1d,
+    coef_i_1d and src/Ope_1d routines (tests/golden/ref_spectral_1d.npz,
+    written by tests/golden/make_ref_vectors.py from the reference compiled
+    here)."""
+    cases = _reference_cases()
+    assert len(cases) > 300
+    checked = 0
+    for op, base, nin, nout, ref, ref_base in cases:
+        lib = _lib.load()
+        m = (C.c_double * (nin * nout))()
+        ob = C.c_int()
+        st = lib.kd_matrix_1d(None, op, base, nin, nout, m, C.byref(ob))
+        if st == _lib.KD_ERR_UNSUPPORTED:
+            continue  # pairs the product does not build (none of the configurations' bases)
+        assert st == 0
+        mp = np.frombuffer(m, dtype=np.float64).reshape(nout, nin)
+        scale = max(1.0, np.abs(ref).max())
+        assert np.abs(mp - ref).max() <= 1e-13 * scale, (op, base, nin, nout, np.abs(mp - ref).max())
+        if op not in (S.OP_COEF, S.OP_COEF_I):
+            assert ob.value == ref_base, (op, base, nin)
+        checked += 1
+    print(f"{checked} of {len(cases)} reference matrices checked")
+    assert checked >= 0.8 * len(cases)
