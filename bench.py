@@ -14,9 +14,10 @@ own replica of the problem on its own GPU ("replicas only": the dense Newton
 step has no data-parallel split in this design); value is the slowest rank's
 step time.
 
---impl reference times the reference's CPU algorithm (the numpy restatement
-under oracle/, the reference itself does not build here) on a bounded sample
-of the same workload, on the host cores.
+--impl reference times the reference's CPU algorithm on the host cores: the
+oracle's restatement of do_newton_seq (oracle/, pinned to the reference's own
+outputs by tests/golden/ref_*.npz), one complete Newton step of the same
+workload per timed step.
 """
 from __future__ import annotations
 
@@ -137,11 +138,13 @@ def max_over_ranks(ws, x):
 
 
 # --------------------------------------------------------------- CPU side --
-def cpu_step_sample(workload, blocks=2):
-    """Times the oracle's Newton step on a bounded sample: the residual, a
-    subset of the Jacobian column blocks (scaled to all blocks), and the dense
-    LU factor + solve of the full-size matrix with scipy's LAPACK."""
-    import numpy as np
+def cpu_full_step(workload):
+    """One complete Newton step of the oracle (the numpy restatement of the
+    reference's do_newton_seq, src_par/do_newton.cpp:519-572) from the
+    workload's initial guess, timed on the host cores: the residual
+    (sec_member), every Jacobian column (do_col_J, vectorised per seed
+    block), LAPACK getrf/getrs on that Jacobian (scipy, all host cores) and
+    the field update.  Nothing is sampled or extrapolated."""
     import scipy.linalg as sla
     from oracle import configs
 
@@ -152,76 +155,53 @@ def cpu_step_sample(workload, blocks=2):
     t0 = time.perf_counter()
     F = sysm.residual()
     t_res = time.perf_counter() - t0
-    layout, N = sysm.unknown_layout()
-    sample = layout[:blocks] if blocks < len(layout) else layout
-    # assemble only the sampled column blocks (same code path as jacobian())
-    J = np.zeros((N, N))
     t0 = time.perf_counter()
-    _assemble_blocks(sysm, sample, N, J)
-    t_blocks = time.perf_counter() - t0
-    cols_done = sum(len(p) for _, _, _, p in sample)
-    t_asm = t_blocks * N / max(cols_done, 1)
-    # LU of a matrix of the same size (values do not change LAPACK's work)
-    rng = np.random.default_rng(0)
-    A = rng.standard_normal((N, N)) + N * np.eye(N)
+    _, J = sysm.jacobian()
+    t_asm = time.perf_counter() - t0
     t0 = time.perf_counter()
-    lu = sla.lu_factor(A, overwrite_a=True, check_finite=False)
+    lu = sla.lu_factor(J, overwrite_a=True, check_finite=False)
     x = sla.lu_solve(lu, F, check_finite=False)
     t_lu = time.perf_counter() - t0
-    total = t_res + t_asm + t_lu
+    t0 = time.perf_counter()
+    sysm.update(x)
+    t_upd = time.perf_counter() - t0
+    total = t_res + t_asm + t_lu + t_upd
+    N = len(F)
     return {"ms": 1e3 * total, "residual_ms": 1e3 * t_res, "assembly_ms": 1e3 * t_asm, "lu_solve_ms": 1e3 * t_lu,
-            "N": N, "sample": f"residual + {len(sample)}/{len(layout)} Jacobian column blocks ({cols_done}/{N} "
-                               f"columns, time scaled by N/columns) + full {N}x{N} LAPACK getrf/getrs"}
+            "update_ms": 1e3 * t_upd, "N": N,
+            "sample": f"one complete Newton step from the initial guess: residual, all {N} Jacobian columns, "
+                      f"LAPACK getrf/getrs of that {N}x{N} Jacobian, update (no extrapolation)"}
 
 
-def _assemble_blocks(sysm, blocks, N, J):
-    import numpy as np
-    from oracle import kadath as K
-    r = 0
-    row0 = []
-    for kind, dom, bound, fn, odom, obound, fnr in sysm.eqs:
-        _, n = sysm._export(kind, fn(sysm._terms(dom), bound).val, dom, bound)
-        row0.append((r, n))
-        r += n
-    for vi, dd, col, pats in blocks:
-        d = sysm.doms[dd]
-        B = len(pats)
-        seed = np.zeros((B, d.nc[0] * d.nc[1] * d.nc[2]))
-        for s, p in enumerate(pats):
-            for idx, w in p:
-                seed[s, idx] = w
-        sb = K.VD(d, B, cf=seed.reshape((B,) + d.nc), base=sysm.vars[vi][1][dd].base)
-        for e, (kind, dom, bound, fn, odom, obound, fnr) in enumerate(sysm.eqs):
-            r0, n = row0[e]
-            if dom == dd:
-                t = fn(sysm._terms(dom, (vi, dd, sb)), bound)
-                v, _ = sysm._export(kind, t.der, dom, bound, n)
-                if v is not None:
-                    J[r0:r0 + n, col:col + B] += v.T
-            if kind == "matching" and odom == dd:
-                t = fnr(sysm._terms(odom, (vi, dd, sb)), obound)
-                v, _ = sysm._export(kind, t.der, odom, obound, n)
-                if v is not None:
-                    J[r0:r0 + n, col:col + B] -= v.T
+def cpu_warmup(workload):
+    """Untimed warm-up of the CPU arm: imports and one residual."""
+    from oracle import configs
+    doms, sysm, *_ = configs.toy() if workload == "toy" else configs.star()
+    sysm.residual()
 
 
 def run_reference(args, ws, rank):
     if rank != 0:
         return 0
     cores = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_warmup(args.workload)
     times = []
     info = None
-    for i in range(args.warmup + args.steps):
-        info = cpu_step_sample(args.workload, blocks=args.cpu_blocks)
-        if i >= args.warmup:
-            times.append(info["ms"])
+    t_wall = time.perf_counter()
+    for _ in range(args.steps):
+        info = cpu_full_step(args.workload)
+        times.append(info["ms"])
+    wall = time.perf_counter() - t_wall
     ms = statistics.mean(times)
+    phases = ("residual_ms", "assembly_ms", "lu_solve_ms", "update_ms")
     line = {"impl": "reference", "metric": METRIC, "value": ms, "unit": "ms", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": workload_label(args.workload), "N": info["N"]},
+            "config": {"workload": workload_label(args.workload), "N": info["N"],
+                       "timed_wall_s": wall, "warmup": "one residual evaluation per warm-up step"},
             "cpu_baseline": {"value": ms, "unit": "ms", "cores": cores, "kind": "port", "sample": info["sample"],
-                             "phases_ms": {k: info[k] for k in ("residual_ms", "assembly_ms", "lu_solve_ms")}},
+                             "phases_ms": {k: info[k] for k in phases}},
             "e2e": {"value": ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -283,11 +263,21 @@ def run_gpu(args, ws, rank, local):
             one_solve(m)
     results = {}
     barrier(ws)
+    solutions = {}
     with ClockSampler(local) as clk:
         for name, m in modes.items():
             runs = [one_solve(m) for _ in range(args.steps if name == "mixed" else max(1, args.fp64_steps))]
             results[name] = runs
+            solutions[name] = wl.download()
     barrier(ws)
+    # the error of the mixed-precision solution against the FP64-LU solution
+    # of the same solve (coefficients of every unknown in every domain)
+    num = den = 0.0
+    for fa, fb in zip(solutions["mixed"], solutions["fp64"]):
+        for a, b in zip(fa, fb):
+            num = max(num, float(np.abs(a - b).max()))
+            den = max(den, float(np.abs(b).max()))
+    mixed_vs_fp64 = num / den if den > 0 else 0.0
 
     def per_step(runs):
         return statistics.mean(ms / max(upd, 1) for ms, upd, _ in runs)
@@ -384,6 +374,7 @@ def run_gpu(args, ws, rank, local):
                                                                  "t_solve_ms", "t_update_ms")}}
         if len(results["mixed"][-1][2]) > 2 else None,
         "refine": {"iters": rep0["refine_iters"], "rel_residual": rep0["refine_rel_residual"]},
+        "mixed_vs_fp64_solution_max_rel_diff": mixed_vs_fp64,
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches_mixed),
         "kernel_profile_ms": {name: {k: round(v["ms"], 3) for k, v in p.items()} for name, p in prof.items()},
@@ -397,10 +388,11 @@ def run_gpu(args, ws, rank, local):
     if exporter:
         exporter["frac_of_fp64_peak"] = exporter["achieved_tflops_fp64"] / fp64_tflops if fp64_tflops else None
     if not args.no_cpu:
-        cb = cpu_step_sample(args.workload, blocks=args.cpu_blocks)
+        cb = cpu_full_step(args.workload)
         line["cpu_baseline"] = {"value": cb["ms"], "unit": "ms", "cores": os.cpu_count(), "kind": "port",
                                 "sample": cb["sample"],
-                                "phases_ms": {k: cb[k] for k in ("residual_ms", "assembly_ms", "lu_solve_ms")}}
+                                "phases_ms": {k: cb[k] for k in ("residual_ms", "assembly_ms", "lu_solve_ms",
+                                                                 "update_ms")}}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -687,7 +679,6 @@ def main():
     ap.add_argument("--workload", default="star", choices=["star", "toy"])
     ap.add_argument("--precision", type=float, default=1e-10)
     ap.add_argument("--fp64-steps", type=int, default=3)
-    ap.add_argument("--cpu-blocks", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--batch", type=int, default=16, help="instances of the batched-solve measurement (0: skip)")
     ap.add_argument("--export-points", type=int, default=1 << 20,

@@ -53,6 +53,16 @@ int kd_ctx_destroy(kd_ctx* ctx);
  * at most `sms` SMs for this context's grid-wide solver kernels (0: all),
  * so that contexts driven side by side share the GPU. */
 int kd_ctx_set_sm_budget(kd_ctx* ctx, int sms);
+/* Failure detection (no reference counterpart: MPI ranks of the reference
+ * block forever on a lost peer).  Every grid-barrier wait of the solver's
+ * cooperative kernels (LU panel, triangular sweeps) gives up after
+ * `seconds` (default 2); the kernel then sets an error flag and returns, the
+ * call reports KD_ERR_TIMEOUT, and the context stays usable.
+ * kd_ctx_stall_waits(ctx, 1) injects the failure for tests: every barrier
+ * target is raised by one, so no barrier completes and every wait runs out;
+ * kd_ctx_stall_waits(ctx, 0) restores normal operation. */
+int kd_ctx_set_wait_limit(kd_ctx* ctx, double seconds);
+int kd_ctx_stall_waits(kd_ctx* ctx, int on);
 const char* kd_last_error(const kd_ctx* ctx);
 int kd_ctx_synchronize(kd_ctx* ctx);
 /* Number of kernels this context has launched so far. */
@@ -100,20 +110,23 @@ int kd_coef_i_host(kd_ctx* ctx, const kd_transform_desc* desc);
 /* Same result as kd_coef_host, but the call allocates no device memory.
  * No counterpart in the reference (its transforms run on the host).
  *
- * For callers that may not allocate on the GPU: code that runs while the
- * process holds a stream in global-mode graph capture (cudaMalloc is then an
- * invalid call), and applications that reserve their whole GPU memory budget
- * up front -- e.g. an evolution code importing initial data through its own
- * memory pool -- where a library allocating on its own would break the budget.
- * The device staging buffers and basis tables are fixed arrays compiled into
- * the library (2 x KD_NOALLOC_MAX_DOUBLES doubles and KD_NOALLOC_MAX_TABLE
- * ints), held by every GPU that loads the library until the process exits.
+ * For callers that cannot let a library allocate GPU memory: applications
+ * that reserve their whole device memory budget up front and serve it from
+ * their own pool -- e.g. an evolution code importing initial data -- where an
+ * allocation by the library fails or breaks the budget, and code running
+ * between the steps of such an application, where a cudaFree would also
+ * synchronise the whole device.  The device staging buffers and basis tables
+ * are fixed arrays compiled into the library (2 x KD_NOALLOC_MAX_DOUBLES
+ * doubles and KD_NOALLOC_MAX_TABLE ints, about 16 MiB), held by every GPU that
+ * loads the library until the process exits; the per-line matrices go into
+ * the context's matrix pool, allocated once with the context.
  *
  * Limits: batch * nbr_points product and batch * nbr_coefs product must each
  * be at most KD_NOALLOC_MAX_DOUBLES (KD_ERR_ARG otherwise); the per-line basis
  * tables (1 + nc2 + nc1*nc2 entries) at most KD_NOALLOC_MAX_TABLE.
  * The first call on a device looks up the device addresses of those arrays
- * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * (cudaGetSymbolAddress, with that device current); make that first call
+ * before any stream capture.
  * All calls share the arrays and leave the last call's data in them; calls
  * whose GPU work overlaps (several host threads or contexts on one device)
  * race.  desc->in and desc->out are HOST pointers. */
@@ -311,6 +324,11 @@ typedef struct kd_newton_opts {
                         the same state (same representations, bases and
                         numbers); systems with integral-type equations are
                         never captured */
+  int gmres_restarts; /* GMRES cycles of max_refine iterations (0: 4).  When
+                         the mixed-precision solve stops above a relative
+                         residual of 1e-10 (KD_ERR_NOCONV), the step factors
+                         the same Jacobian in FP64 and solves again
+                         (report.fp64_fallback = 1) */
 } kd_newton_opts;
 
 typedef struct kd_newton_report {
@@ -321,6 +339,9 @@ typedef struct kd_newton_report {
   int refine_iters;
   double refine_rel_residual;
   long long kernel_launches;
+  int fp64_fallback; /* 1 when the mixed-precision solve did not converge
+                        (KD_ERR_NOCONV) and the step was solved again with
+                        the FP64 LU of the same Jacobian */
 } kd_newton_report;
 
 /* System_of_eqs::do_newton (src_par/do_newton.cpp:65; decl
@@ -384,6 +405,10 @@ int kd_lu_factor(kd_lu* lu, double* dA, long long ld, int n, int mode);
 /* Solves in place on the device vector db; trans = 1 solves A^T x = b
  * with the same factors (FP64 mode). */
 int kd_lu_solve(kd_lu* lu, double* db, int trans);
+/* Refinement of the mixed modes: GMRES(iters) restarted up to `restarts`
+ * times until the relative residual is below tol (defaults 1e-14, 50, 4);
+ * kd_lu_solve returns KD_ERR_NOCONV when it ends above 1e-10. */
+int kd_lu_set_refinement(kd_lu* lu, double tol, int iters, int restarts);
 int kd_lu_stats(const kd_lu* lu, double* t_factor_ms, double* t_solve_ms, int* refine_iters,
                 double* rel_residual);
 /* The LU's trailing update on its own: C -= A * B on the tcgen05 tensor

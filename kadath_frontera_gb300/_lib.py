@@ -57,6 +57,8 @@ def _declare(lib: C.CDLL) -> None:
         "kd_ctx_create": (I, [C.POINTER(P), I]),
         "kd_ctx_destroy": (I, [P]),
         "kd_ctx_set_sm_budget": (I, [P, I]),
+        "kd_ctx_set_wait_limit": (I, [P, C.c_double]),
+        "kd_ctx_stall_waits": (I, [P, I]),
         "kd_last_error": (C.c_char_p, [P]),
         "kd_ctx_synchronize": (I, [P]),
         "kd_ctx_launch_count": (C.c_longlong, [P]),
@@ -116,6 +118,15 @@ class Context:
         """At most `sms` SMs for this context's grid-wide solver kernels
         (0: all of them), for contexts that run side by side."""
         self.check(self.lib.kd_ctx_set_sm_budget(self.h, int(sms)))
+
+    def set_wait_limit(self, seconds: float) -> None:
+        """Limit of one grid-barrier wait of the solver's cooperative kernels
+        (KD_ERR_TIMEOUT when it runs out)."""
+        self.check(self.lib.kd_ctx_set_wait_limit(self.h, float(seconds)))
+
+    def stall_waits(self, on: bool) -> None:
+        """Failure injection for tests: no grid barrier completes while on."""
+        self.check(self.lib.kd_ctx_stall_waits(self.h, 1 if on else 0))
 
     @property
     def launches(self) -> int:

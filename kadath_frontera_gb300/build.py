@@ -62,10 +62,8 @@ def build(verbose: bool = False, force: bool = False) -> Path:
 
     def compile_one(src: Path) -> None:
         cmd = [nvcc, *ARCH, *COMMON, "-c", str(src), "-o", str(_obj(src))]
-        if src.suffix == ".cu":
-            cmd += ["-Xptxas", "-v"] if verbose else []
-        else:
-            cmd += ["-x", "cu"] if False else []
+        if src.suffix == ".cu" and verbose:
+            cmd += ["-Xptxas", "-v"]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")

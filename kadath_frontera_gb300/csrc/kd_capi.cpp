@@ -121,6 +121,19 @@ int kd_ctx_set_sm_budget(kd_ctx* ctx, int sms) {
   return KD_OK;
 }
 
+int kd_ctx_set_wait_limit(kd_ctx* ctx, double seconds) {
+  if (!ctx || !ctx->c) return KD_ERR_ARG;
+  if (!(seconds > 0) || seconds > 3600) return KD_ERR_ARG;
+  ctx->c->grid_wait_ns = static_cast<unsigned long long>(seconds * 1e9);
+  return KD_OK;
+}
+
+int kd_ctx_stall_waits(kd_ctx* ctx, int on) {
+  if (!ctx || !ctx->c) return KD_ERR_ARG;
+  ctx->c->stall_waits = on ? 1 : 0;
+  return KD_OK;
+}
+
 int kd_ctx_destroy(kd_ctx* ctx) {
   if (!ctx) return KD_ERR_ARG;
   delete ctx;
@@ -719,6 +732,7 @@ kd::NewtonOpts to_opts(const kd_newton_opts* opts) {
   o.lu_mode = opts->lu_mode;
   o.gmres_tol = opts->gmres_tol > 0 ? opts->gmres_tol : 1e-14;
   o.max_refine = opts->max_refine > 0 ? opts->max_refine : 50;
+  o.gmres_restarts = opts->gmres_restarts > 0 ? opts->gmres_restarts : 4;
   o.graph_capture = opts->graph_capture;
   return o;
 }
@@ -735,6 +749,7 @@ void to_report(const kd::NewtonReport& r, kd_newton_report* rep) {
   rep->refine_iters = r.refine_iters;
   rep->refine_rel_residual = r.refine_rel_residual;
   rep->kernel_launches = r.kernel_launches;
+  rep->fp64_fallback = r.fp64_fallback;
 }
 }  // namespace
 
@@ -932,6 +947,15 @@ int kd_lu_solve(kd_lu* lu, double* db, int trans) {
     if (lu->lu->n() <= 0) throw kd::KdError(KD_ERR_STATE, "factor first");
     lu->lu->solve(db, trans);
   });
+}
+
+int kd_lu_set_refinement(kd_lu* lu, double tol, int iters, int restarts) {
+  if (!lu) return KD_ERR_ARG;
+  if (!(tol > 0) || iters < 1 || restarts < 1) return KD_ERR_ARG;
+  lu->lu->gmres_tol = tol;
+  lu->lu->gmres_max_iter = iters;
+  lu->lu->gmres_restarts = restarts;
+  return KD_OK;
 }
 
 int kd_lu_stats(const kd_lu* lu, double* t_factor_ms, double* t_solve_ms, int* refine_iters, double* rel_residual) {

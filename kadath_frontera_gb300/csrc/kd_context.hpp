@@ -56,6 +56,14 @@ class Context {
   // unless a budget is set, so that contexts run side by side (concurrent
   // instances) share the GPU instead of taking turns.
   int sms() const { return (sm_budget_ > 0 && sm_budget_ < nsm_) ? sm_budget_ : nsm_; }
+  // Limit of one grid-barrier wait in the solver's cooperative kernels (LU
+  // panel, triangular sweeps); after it the kernel sets an error flag and
+  // returns, and the call reports KD_ERR_TIMEOUT.
+  unsigned long long grid_wait_ns = 2000000000ull;
+  // Failure injection for tests of that path: nonzero raises every
+  // grid-barrier target by one, so that no barrier completes and every wait
+  // runs out after grid_wait_ns.
+  int stall_waits = 0;
   void set_sm_budget(int n) { sm_budget_ = n; }
   // The stream work is issued on: the context's main stream, or one of the
   // side streams between fork() and join().

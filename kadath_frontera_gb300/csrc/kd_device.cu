@@ -256,8 +256,10 @@ __global__ void absmax_kernel(const double* __restrict__ x, long long n, double*
   __shared__ double red[32];
   double m = 0.0;
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<long long>(gridDim.x) * blockDim.x)
-    m = fmax(m, fabs(x[i]));
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const double a = fabs(x[i]);
+    m = (a == a) ? fmax(m, a) : INFINITY;  // NaN counts as infinite (fmax would drop it)
+  }
   for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
   __syncthreads();

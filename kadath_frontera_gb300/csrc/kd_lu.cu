@@ -165,6 +165,13 @@ __global__ void d2s(const double* __restrict__ A, long long lda, float* __restri
 // ---- triangular solves on one right-hand side (blocked by TB rows) --------
 constexpr int TB = 64;
 
+// ipiv[j] = j: every pivot entry holds a valid row before the panels write
+// theirs, so that a panel which gave up (a grid barrier wait ran out) leaves
+// only in-range rows behind for the row exchanges that follow it.
+__global__ void iota_kernel(int* __restrict__ v, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] = i;
+}
+
 // perm such that (P b)[i] = b[perm[i]] for the sequential row swaps ipiv.
 __global__ void build_perm(const int* __restrict__ ipiv, int N, int* __restrict__ perm) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -558,7 +565,6 @@ __global__ void panel_cluster_kernel(T* __restrict__ A, long long ld, int N, int
 constexpr int GP_THREADS = 256;
 constexpr int GP_MIN_ROWS = 32;
 constexpr size_t GP_MAX_SMEM = 200 * 1024;
-constexpr unsigned long long GP_WAIT_NS = 2000000000ull;  // 2 s per barrier
 
 template <class T>
 struct PanelSlots {
@@ -568,6 +574,8 @@ struct PanelSlots {
   T* jrow;          // [2][jb]
   unsigned* bar;    // arrival counter, zeroed before the launch
   int* err;         // set when a barrier wait runs out
+  unsigned long long wait_ns;  // limit of one barrier wait (Context::grid_wait_ns)
+  unsigned stall;   // added to every barrier target (Context::stall_waits)
 };
 
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
@@ -576,12 +584,12 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
   return t;
 }
 
-// Grid barrier for a cooperative launch (all CTAs resident).  Returns false,
-// with *err set, when the counter did not reach `target` within the limit.
-// Grid-wide barrier of a cooperative launch: the CTA's writes are published
-// by thread 0's release increment (after the block barrier), the other
-// CTAs' writes acquired by its polling loads; gives up after GP_WAIT_NS.
-__device__ bool grid_barrier(unsigned* bar, unsigned target, int* err, int* s_ok) {
+// Grid-wide barrier of a cooperative launch (all CTAs resident): the CTA's
+// writes are published by thread 0's release increment (after the block
+// barrier), the other CTAs' writes acquired by its polling loads.  Returns
+// false, with *err set, when the counter did not reach `target` within
+// limit_ns; the caller then leaves its loops.
+__device__ bool grid_barrier(unsigned* bar, unsigned target, int* err, int* s_ok, unsigned long long limit_ns) {
   __syncthreads();
   if (threadIdx.x == 0) {
     asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(bar), "r"(1u) : "memory");
@@ -591,7 +599,7 @@ __device__ bool grid_barrier(unsigned* bar, unsigned target, int* err, int* s_ok
       unsigned v;
       asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(bar) : "memory");
       if (v >= target) break;
-      if ((it & 31) == 31 && globaltimer_ns() - t0 > GP_WAIT_NS) {
+      if ((it & 31) == 31 && globaltimer_ns() - t0 > limit_ns) {
         ok = 0;
         atomicExch(err, 1);
         break;
@@ -776,7 +784,7 @@ template <class T>
 __global__ void __launch_bounds__(256) trsv_sweep(const T* __restrict__ A, long long ld, int N, double* b,
                                                   double* __restrict__ y, const double* __restrict__ Dinv,
                                                   const float2* __restrict__ Dinv2, int lower, unsigned* bar,
-                                                  int* err) {
+                                                  int* err, unsigned long long wait_ns, unsigned stall) {
   // x_k = Dinv_k b in FP64, or in double-float with FP32 factors (an
   // explicit inverse amplifies rounding by its condition number, so a plain
   // FP32 product would cost refinement iterations); the row updates in the
@@ -883,7 +891,7 @@ __global__ void __launch_bounds__(256) trsv_sweep(const T* __restrict__ A, long 
       __syncthreads();
     }
     if (step + 1 < nblk) sweep_prefetch(A, ld, Dinv, Dinv2, sweep_step(step + 1, nblk, N, lower, ntiles), pf);
-    if (!grid_barrier(bar, gridDim.x * static_cast<unsigned>(step + 1), err, &s_ok)) return;
+    if (!grid_barrier(bar, gridDim.x * static_cast<unsigned>(step + 1) + stall, err, &s_ok, wait_ns)) return;
   }
 }
 
@@ -931,7 +939,7 @@ __global__ void __launch_bounds__(GP_THREADS) panel_grid_kernel(T* __restrict__ 
     if (j >= r0 && j < r1)
       for (int k = tid; k < jb; k += bd) ps.jrow[slot * jb + k] = tile[k * per + j - r0];
     // 3. one barrier per column
-    if (!grid_barrier(ps.bar, static_cast<unsigned>(nblk) * (jj + 1), ps.err, &s_ok)) return;
+    if (!grid_barrier(ps.bar, static_cast<unsigned>(nblk) * (jj + 1) + ps.stall, ps.err, &s_ok, ps.wait_ns)) return;
     // 4. every CTA reduces the candidates identically
     best = T(-1);
     bi = N;
@@ -1546,6 +1554,8 @@ static bool panel_factor(Context* ctx, T* A, long long ld, int N, int j0, int jb
     p += sizeof(int) * 2 * static_cast<size_t>(nsm);
     slots.bar = reinterpret_cast<unsigned*>(p);
     slots.err = reinterpret_cast<int*>(p + 16);
+    slots.wait_ns = ctx->grid_wait_ns;
+    slots.stall = ctx->stall_waits ? 1u : 0u;
   }
   if constexpr (std::is_same<T, float>::value) {
     if (panel_cluster16(ctx, A, ld, N, j0, jb, ipiv, info, swap_map)) return true;
@@ -1704,6 +1714,8 @@ void DenseLU::factor(double* A, long long ld, int N, int mode) {
   }
   stats = LuStats();
   stats.flops = static_cast<long long>(2.0 / 3.0 * double(N) * N * N);
+  iota_kernel<<<blocks(N, 256), 256, 0, ctx_->stream()>>>(ipiv_, N);
+  ctx_->launches++;
   if (mode == LU_FP64) {
     factor_fp64(A, ld, N);
     prepare_solves<double>(A, ld, N);
@@ -1790,9 +1802,13 @@ void DenseLU::tri_solve(const T* LU, long long ld, int N, double* b, int trans) 
     const double* du = dinv_u_;
     const float2* dl2 = std::is_same<T, float>::value ? dinv2_l_ : nullptr;
     const float2* du2 = std::is_same<T, float>::value ? dinv2_u_ : nullptr;
-    cuda_check(cudaLaunchKernelEx(&cfg, trsv_sweep<T>, LU, ld, N, w1, w2, dl, dl2, 1, tri_bar_, panel_err_),
+    const unsigned long long wait = ctx_->grid_wait_ns;
+    const unsigned stall = ctx_->stall_waits ? 1u : 0u;
+    cuda_check(cudaLaunchKernelEx(&cfg, trsv_sweep<T>, LU, ld, N, w1, w2, dl, dl2, 1, tri_bar_, panel_err_, wait,
+                                  stall),
                "forward sweep");
-    cuda_check(cudaLaunchKernelEx(&cfg, trsv_sweep<T>, LU, ld, N, w2, b, du, du2, 0, tri_bar_ + 1, panel_err_),
+    cuda_check(cudaLaunchKernelEx(&cfg, trsv_sweep<T>, LU, ld, N, w2, b, du, du2, 0, tri_bar_ + 1, panel_err_, wait,
+                                  stall),
                "backward sweep");
     ctx_->launches += 3;
     cuda_check(cudaGetLastError(), "triangular solve");
@@ -1907,7 +1923,7 @@ void DenseLU::gmres_ir(double* b) {
   // orthogonalised by classical Gram-Schmidt run twice (CGS2): per
   // iteration two rounds of dot products and one norm on the device, one
   // copy of the results to the host; the small Hessenberg least-squares
-  // problem is solved on the host.  Restarted at most 4 times.
+  // problem is solved on the host.  At most gmres_restarts cycles.
   const int N = N_;
   const int m = gmres_max_iter;
   cudaStream_t s = ctx_->stream();
@@ -1946,7 +1962,7 @@ void DenseLU::gmres_ir(double* b) {
   const double bnorm = norm(b);
   if (bnorm == 0) return;
   int total_it = 0;
-  for (int restart = 0; restart < 4; restart++) {
+  for (int restart = 0; restart < gmres_restarts; restart++) {
     // r = b - A x
     {
       ProfScope ps(ctx_, Context::PROF_GMRES, 8.0 * double(N) * N);
@@ -2031,10 +2047,9 @@ void DenseLU::solve(double* b, int trans) {
   } else {
     if (trans) throw KdError(KD_ERR_UNSUPPORTED, "transposed solve needs the FP64 factors");
     gmres_ir(b);
-    if (!(stats.final_rel_residual < 1e-10))
-      throw KdError(KD_ERR_NOCONV, "GMRES-IR did not converge (relative residual " +
-                                       std::to_string(stats.final_rel_residual) + ")");
   }
+  // a sweep that gave up is reported first (its garbage also stops the
+  // refinement), and its flag is cleared so the context stays usable
   cuda_check(cudaStreamSynchronize(ctx_->stream()), "sync after solve");
   int perr = 0;
   cuda_check(cudaMemcpyAsync(&perr, panel_err_, sizeof(int), cudaMemcpyDeviceToHost, ctx_->stream()),
@@ -2042,8 +2057,12 @@ void DenseLU::solve(double* b, int trans) {
   cuda_check(cudaStreamSynchronize(ctx_->stream()), "sync sweep flag");
   if (perr) {
     cuda_check(cudaMemsetAsync(panel_err_, 0, sizeof(int), ctx_->stream()), "reset sweep flag");
+    cuda_check(cudaStreamSynchronize(ctx_->stream()), "sync sweep flag reset");
     throw KdError(KD_ERR_TIMEOUT, "triangular solve: a grid barrier wait ran out");
   }
+  if (mode_ != LU_FP64 && !(stats.final_rel_residual < 1e-10))
+    throw KdError(KD_ERR_NOCONV, "GMRES-IR did not converge (relative residual " +
+                                     std::to_string(stats.final_rel_residual) + ")");
   stats.t_solve_ms = now_ms() - t0;
 }
 

@@ -41,7 +41,8 @@ class DenseLU {
   int n() const { return N_; }
   LuStats stats;
   double gmres_tol = 1e-14;
-  int gmres_max_iter = 50;
+  int gmres_max_iter = 50;   // GMRES iterations per cycle
+  int gmres_restarts = 4;    // cycles (restarts) of GMRES(gmres_max_iter)
   int nb = 128;
   // TF32 mode: 3 = 3xTF32 trailing updates (about FP32 accurate factors,
   // fewer refinement iterations), 1 = plain TF32 products.

@@ -17,6 +17,7 @@ Newton::Newton(System* s) : sys_(s), lu_(new DenseLU(s->ctx)) {}
 Newton::~Newton() {
   cudaStreamSynchronize(sys_->ctx->stream());
   cudaFree(d_F);
+  cudaFree(d_F0);
   cudaFree(d_J);
   cudaFree(d_JtJ_);
   cudaFree(d_JtF_);
@@ -26,7 +27,10 @@ Newton::~Newton() {
 void Newton::ensure(int N) {
   if (static_cast<size_t>(N) > capF_) {
     cudaFree(d_F);
+    cudaFree(d_F0);
+    d_F = d_F0 = nullptr;
     cuda_check(cudaMalloc(&d_F, sizeof(double) * N), "cudaMalloc(F)");
+    cuda_check(cudaMalloc(&d_F0, sizeof(double) * N), "cudaMalloc(F copy)");
     capF_ = N;
   }
   size_t need = static_cast<size_t>(N) * N;
@@ -57,6 +61,8 @@ bool Newton::step(const NewtonOpts& o, NewtonReport& rep) {
   rep.t_residual_ms = ms_since(t0);
   rep.error = err;
   rep.n = N;
+  if (!std::isfinite(err))
+    throw KdError(KD_ERR_ARG, "non-finite residual (the fields or constants hold NaN or Inf): no update made");
   if (err < o.precision) {
     rep.converged = 1;
     rep.kernel_launches = ctx->launches - l0;
@@ -72,10 +78,25 @@ bool Newton::step(const NewtonOpts& o, NewtonReport& rep) {
   rep.t_assembly_ms = ms_since(t1);
   lu_->gmres_tol = o.gmres_tol;
   lu_->gmres_max_iter = o.max_refine;
+  lu_->gmres_restarts = o.gmres_restarts;
+  const bool mixed = o.lu_mode != LU_FP64;
+  if (mixed)
+    cuda_check(cudaMemcpyAsync(d_F0, d_F, sizeof(double) * N, cudaMemcpyDeviceToDevice, s), "keep F");
   lu_->factor(d_J, ld, N, o.lu_mode);
   rep.t_factor_ms = lu_->stats.t_factor_ms;
   // the residual vector is solved in place
-  lu_->solve(d_F, 0);
+  try {
+    lu_->solve(d_F, 0);
+  } catch (const KdError& e) {
+    if (!mixed || e.code != KD_ERR_NOCONV) throw;
+    // the refinement did not reach the FP64 solution: factor the same
+    // Jacobian (kept by the mixed modes) in FP64 and solve again
+    rep.fp64_fallback = 1;
+    lu_->factor(d_J, ld, N, LU_FP64);
+    rep.t_factor_ms += lu_->stats.t_factor_ms;
+    cuda_check(cudaMemcpyAsync(d_F, d_F0, sizeof(double) * N, cudaMemcpyDeviceToDevice, s), "restore F");
+    lu_->solve(d_F, 0);
+  }
   rep.t_solve_ms = lu_->stats.t_solve_ms;
   rep.refine_iters = lu_->stats.refine_iters;
   rep.refine_rel_residual = lu_->stats.final_rel_residual;
@@ -148,6 +169,7 @@ bool Newton::step_gauss_newton(const NewtonOpts& o, NewtonReport& rep) {
   rep.t_assembly_ms = ms_since(t1);
   lu_->gmres_tol = o.gmres_tol;
   lu_->gmres_max_iter = o.max_refine;
+  lu_->gmres_restarts = o.gmres_restarts;
   lu_->factor(d_JtJ_, n, n, o.lu_mode);
   rep.t_factor_ms = lu_->stats.t_factor_ms;
   lu_->solve(d_JtF_, 0);
@@ -215,6 +237,7 @@ bool Newton::step_linesearch(const NewtonOpts& o, int ntrymax, double stepmax, N
   rep.t_assembly_ms = ms_since(t1);
   lu_->gmres_tol = o.gmres_tol;
   lu_->gmres_max_iter = o.max_refine;
+  lu_->gmres_restarts = o.gmres_restarts;
   lu_->factor(d_J, ld, N, o.lu_mode);
   rep.t_factor_ms = lu_->stats.t_factor_ms;
   lu_->solve(d_F, 0);

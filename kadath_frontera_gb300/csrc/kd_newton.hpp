@@ -15,6 +15,7 @@ struct NewtonOpts {
   int lu_mode = LU_FP64;
   double gmres_tol = 1e-14;
   int max_refine = 50;
+  int gmres_restarts = 4;
   int graph_capture = 0;
 };
 
@@ -26,6 +27,7 @@ struct NewtonReport {
   int refine_iters = 0;
   double refine_rel_residual = 0;
   long long kernel_launches = 0;
+  int fp64_fallback = 0;
 };
 
 class Newton {
@@ -54,6 +56,7 @@ class Newton {
   // Device buffers of the last step (valid until the next call).
   double* d_F = nullptr;
   double* d_J = nullptr;
+  double* d_F0 = nullptr;  // copy of F kept for an FP64 re-solve when the mixed solve does not converge
   long long ld = 0;
   DenseLU& lu() { return *lu_; }
   void ensure(int N);

@@ -2,10 +2,20 @@
 //
 // kd_coef_host stages its host input and output through device buffers taken
 // from the context's scratch arena, which may call cudaMalloc.  This variant
-// stages through the fixed file-scope device arrays below instead, so that a
-// caller that is not allowed to allocate device memory can still transform
-// fields.  Every GPU that loads the library holds these arrays until the
-// process exits (2 x 8 MiB of doubles plus 64 KiB of table space).
+// stages through the fixed file-scope device arrays below instead, for callers
+// that cannot let a library allocate GPU memory: applications that reserve
+// their whole device memory budget up front and hand it out from their own
+// pool, where an allocation by the library fails or breaks the budget, and
+// code running between the steps of such an application, where a cudaFree
+// would also synchronise the whole device.  Every GPU that loads the library
+// holds these arrays until the process exits (2 x 8 MiB of doubles plus
+// 64 KiB of table space).  The call allocates nothing: the per-line matrices
+// go into the context's matrix pool, which is allocated once when the context
+// is created.
+//
+// The first call on a device looks up the arrays' device addresses there
+// (cudaGetSymbolAddress, with that device current); make that first call
+// before any stream capture.
 //
 // The arrays are shared by every call on a device and keep the contents of
 // the last call; two calls whose GPU work overlaps (two host threads, or two
@@ -36,6 +46,26 @@ struct DevicePtrs {
   int* tab = nullptr;
 };
 
+// Makes `device` current for its lifetime and restores the caller's device
+// on every exit path, exceptions included.
+class DeviceGuard {
+ public:
+  explicit DeviceGuard(int device) {
+    cuda_check(cudaGetDevice(&prev_), "cudaGetDevice");
+    if (prev_ != device) cuda_check(cudaSetDevice(device), "cudaSetDevice");
+    switched_ = prev_ != device;
+  }
+  ~DeviceGuard() {
+    if (switched_) cudaSetDevice(prev_);
+  }
+  DeviceGuard(const DeviceGuard&) = delete;
+  DeviceGuard& operator=(const DeviceGuard&) = delete;
+
+ private:
+  int prev_ = -1;
+  bool switched_ = false;
+};
+
 constexpr int kMaxDevices = 64;
 DevicePtrs g_ptrs[kMaxDevices];
 std::mutex g_mu;
@@ -48,13 +78,16 @@ const DevicePtrs& device_ptrs(int device) {
   std::lock_guard<std::mutex> lock(g_mu);
   DevicePtrs& p = g_ptrs[device];
   if (!p.ready) {
-    int cur = -1;
-    cuda_check(cudaGetDevice(&cur), "cudaGetDevice");
-    if (cur != device) cuda_check(cudaSetDevice(device), "cudaSetDevice");
-    cuda_check(cudaGetSymbolAddress(reinterpret_cast<void**>(&p.in), g_noalloc_in), "cudaGetSymbolAddress(in)");
-    cuda_check(cudaGetSymbolAddress(reinterpret_cast<void**>(&p.out), g_noalloc_out), "cudaGetSymbolAddress(out)");
-    cuda_check(cudaGetSymbolAddress(reinterpret_cast<void**>(&p.tab), g_noalloc_tab), "cudaGetSymbolAddress(tab)");
-    if (cur != device) cuda_check(cudaSetDevice(cur), "cudaSetDevice");
+    DeviceGuard guard(device);
+    double* in = nullptr;
+    double* out = nullptr;
+    int* tab = nullptr;
+    cuda_check(cudaGetSymbolAddress(reinterpret_cast<void**>(&in), g_noalloc_in), "cudaGetSymbolAddress(in)");
+    cuda_check(cudaGetSymbolAddress(reinterpret_cast<void**>(&out), g_noalloc_out), "cudaGetSymbolAddress(out)");
+    cuda_check(cudaGetSymbolAddress(reinterpret_cast<void**>(&tab), g_noalloc_tab), "cudaGetSymbolAddress(tab)");
+    p.in = in;
+    p.out = out;
+    p.tab = tab;
     p.ready = true;
   }
   return p;

@@ -32,14 +32,14 @@ KD_EOS_EPSILON, KD_EOS_PRESSURE, KD_EOS_DENSITY, KD_EOS_DHDRHO = 0, 1, 2, 3
 
 class NewtonOpts(C.Structure):
     _fields_ = [("precision", C.c_double), ("lu_mode", C.c_int), ("gmres_tol", C.c_double), ("max_refine", C.c_int),
-                ("graph_capture", C.c_int)]
+                ("graph_capture", C.c_int), ("gmres_restarts", C.c_int)]
 
 
 class NewtonReport(C.Structure):
     _fields_ = [("error", C.c_double), ("converged", C.c_int), ("n", C.c_int), ("t_residual_ms", C.c_double),
                 ("t_assembly_ms", C.c_double), ("t_factor_ms", C.c_double), ("t_solve_ms", C.c_double),
                 ("t_update_ms", C.c_double), ("refine_iters", C.c_int), ("refine_rel_residual", C.c_double),
-                ("kernel_launches", C.c_longlong)]
+                ("kernel_launches", C.c_longlong), ("fp64_fallback", C.c_int)]
 
     def as_dict(self):
         return {f[0]: getattr(self, f[0]) for f in self._fields_}
@@ -123,6 +123,7 @@ def _declare_system(lib):
         "kd_lu_factor": (I, [P, P, C.c_longlong, I, I]),
         "kd_lu_solve": (I, [P, P, I]),
         "kd_lu_stats": (I, [P, DP, DP, IP, DP]),
+        "kd_lu_set_refinement": (I, [P, D, I, I]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -633,14 +634,17 @@ class System_of_eqs:
         self.ctx.check(_L().kd_system_update(self.h, _dp(x)))
         self._J = None
 
-    def do_newton(self, precision, lu_mode=None, gmres_tol=1e-14, max_refine=50, solver=None, graph=None):
+    def do_newton(self, precision, lu_mode=None, gmres_tol=1e-14, max_refine=50, solver=None, graph=None,
+                  gmres_restarts=4):
         """System_of_eqs::do_newton(precision, error, solver): returns
         (converged, error); solver NEWTON_RAPHSON (default) or GAUSS_NEWTON.
         graph: replay the residual's value pass from a CUDA graph (default:
-        the system's graph_capture attribute)."""
+        the system's graph_capture attribute).  A mixed-precision solve that
+        ends above a relative residual of 1e-10 is redone with the FP64 LU
+        (last_report["fp64_fallback"])."""
         g = self.graph_capture if graph is None else graph
         opts = NewtonOpts(precision, self.lu_mode if lu_mode is None else lu_mode, gmres_tol, max_refine,
-                          1 if g else 0)
+                          1 if g else 0, gmres_restarts)
         rep = NewtonReport()
         fn = _L().kd_newton_step_gauss_newton if solver == GAUSS_NEWTON else _L().kd_newton_step
         self.ctx.check(fn(self.h, C.byref(opts), C.byref(rep)))
@@ -658,7 +662,7 @@ class System_of_eqs:
                                   max_refine=50):
         """System_of_eqs::do_newton_with_linesearch: returns (converged, error,
         last lambda)."""
-        opts = NewtonOpts(precision, self.lu_mode if lu_mode is None else lu_mode, gmres_tol, max_refine, 0)
+        opts = NewtonOpts(precision, self.lu_mode if lu_mode is None else lu_mode, gmres_tol, max_refine, 0, 4)
         rep = NewtonReport()
         lam = C.c_double()
         self.ctx.check(_L().kd_newton_step_linesearch(self.h, C.byref(opts), ntrymax, stepmax, C.byref(rep),
@@ -689,6 +693,10 @@ class DenseLU:
 
     def solve(self, db_ptr, trans=0):
         self.ctx.check(_L().kd_lu_solve(self.h, C.c_void_p(db_ptr), trans))
+
+    def set_refinement(self, tol=1e-14, iters=50, restarts=4):
+        """GMRES(iters) with at most `restarts` cycles down to tol (mixed modes)."""
+        self.ctx.check(_L().kd_lu_set_refinement(self.h, float(tol), int(iters), int(restarts)))
 
     def stats(self):
         a, b, r = C.c_double(), C.c_double(), C.c_double()

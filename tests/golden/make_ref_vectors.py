@@ -66,9 +66,9 @@ TOY_EQUATION = "Lap(psi) + 2*pi*rho*psi^5 = 0"
 
 
 def build():
-    jobs = str(os.cpu_count() or 4)
-    subprocess.run(["make", "-f", str(ROOT / "oracle" / "Makefile.ref"), "-j", jobs, f"REF={REF}"], check=True,
-                   cwd=ROOT, stdout=subprocess.DEVNULL)
+    from oracle import build_ref
+    if not build_ref.build():
+        raise SystemExit(f"the reference's sources are not at {REF}")
 
 
 def run_spec(spec: str, workdir: Path):

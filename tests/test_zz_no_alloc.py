@@ -1,8 +1,9 @@
 """kd_coef_host_noalloc: the host-pointer forward transform for callers that
-may not allocate device memory (for example while a stream is in global-mode
-graph capture, or inside an application that owns its whole GPU memory
-budget).  It must give the same coefficients as kd_coef_host, call after
-call, while staging through the library's fixed device arrays.
+cannot let a library allocate GPU memory (an application that serves its whole
+device budget from its own pool, or code between its steps where a cudaFree
+would synchronise the device).  It must give the same coefficients as
+kd_coef_host, call after call, while staging through the library's fixed
+device arrays, and a call must leave the device's free memory unchanged.
 
 This file is collected last on purpose (tests/test_zz_*), so that a run that
 stops at the first failure has already run every other test."""
@@ -75,3 +76,47 @@ def test_noalloc_rejects_sizes_beyond_its_arrays(ctx):
     st = lib.kd_coef_host_noalloc(ctx.h, C.byref(d))
     assert st == 1  # KD_ERR_ARG
     assert b"KD_NOALLOC_MAX_DOUBLES" in lib.kd_last_error(ctx.h)
+
+
+def _declare(lib):
+    lib.kd_coef_host_noalloc.restype = C.c_int
+    lib.kd_coef_host_noalloc.argtypes = lib.kd_coef_host.argtypes
+
+
+def test_noalloc_first_call_on_a_fresh_context(ctx):
+    """The very first transform of a new context goes through the no-alloc
+    entry point, with a basis and size nothing has used before: its matrices
+    enter the context's pool during that call."""
+    from kadath_frontera_gb300._lib import Context
+    _declare(ctx.lib)
+    fresh = Context(0)
+    rng = np.random.default_rng(23)
+    shape = (15, 11, 6)
+    x = rng.standard_normal((2,) + shape)
+    got = _run(fresh, fresh.lib.kd_coef_host_noalloc, "compact", shape, 2, x, True)
+    ref = _run(fresh, fresh.lib.kd_coef_host, "compact", shape, 2, x, True)
+    assert _rel(got, ref) < TOL
+    again = _run(fresh, fresh.lib.kd_coef_host_noalloc, "compact", shape, 2, x, True)
+    assert np.array_equal(again, got)
+
+
+def test_noalloc_call_leaves_device_memory_unchanged(ctx):
+    """After a first call of each launch form (few fields: the cluster kernel;
+    many fields: the plain kernel), a call with a new shape and basis takes no
+    device memory."""
+    import torch
+    _declare(ctx.lib)
+    rng = np.random.default_rng(29)
+    for kind, shape, batch in (("shell", (9, 5, 4), 1), ("shell", (9, 5, 4), 300)):
+        x = rng.standard_normal((batch,) + shape)
+        _run(ctx, ctx.lib.kd_coef_host_noalloc, kind, shape, batch, x)
+    torch.cuda.synchronize()
+    shape, batch = (17, 13, 8), 3
+    x = rng.standard_normal((batch,) + shape)
+    free_before, _ = torch.cuda.mem_get_info()
+    got = _run(ctx, ctx.lib.kd_coef_host_noalloc, "nucleus", shape, batch, x, True)
+    torch.cuda.synchronize()
+    free_after, _ = torch.cuda.mem_get_info()
+    assert free_after == free_before, (free_before, free_after)
+    ref = _run(ctx, ctx.lib.kd_coef_host, "nucleus", shape, batch, x, True)
+    assert _rel(got, ref) < TOL
