@@ -239,6 +239,7 @@ def run_gpu(args, ws, rank, local):
         wl.restore()
         syst.cache_tangents(False)
         syst.cache_tangents(True)
+        syst.reset_pivot_order()  # the first step of every solve pivots
         flush.zero_()
         torch.cuda.synchronize()
         ev0 = torch.cuda.Event(enable_timing=True)
@@ -309,6 +310,7 @@ def run_gpu(args, ws, rank, local):
     for _ in range(args.steps):
         syst.cache_tangents(False)
         syst.cache_tangents(True)
+        syst.reset_pivot_order()
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -569,6 +571,7 @@ def run_large(args, local):
         wl.restore()
         syst.cache_tangents(False)
         syst.cache_tangents(True)
+        syst.reset_pivot_order()
         torch.cuda.synchronize()
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)

@@ -329,6 +329,13 @@ typedef struct kd_newton_opts {
                          residual of 1e-10 (KD_ERR_NOCONV), the step factors
                          the same Jacobian in FP64 and solves again
                          (report.fp64_fallback = 1) */
+  int pivot_every_step; /* 0 (default): a mixed-precision step reuses the
+                           pivot order of the last partial-pivoting
+                           factorisation of this system (static pivoting;
+                           refinement against the FP64 Jacobian restores the
+                           accuracy, and a refinement that does not converge
+                           makes the step factor again with partial
+                           pivoting); 1: partial pivoting at every step */
 } kd_newton_opts;
 
 typedef struct kd_newton_report {
@@ -342,12 +349,16 @@ typedef struct kd_newton_report {
   int fp64_fallback; /* 1 when the mixed-precision solve did not converge
                         (KD_ERR_NOCONV) and the step was solved again with
                         the FP64 LU of the same Jacobian */
+  int static_pivots; /* 1 when the step's factors used the reused pivot order */
 } kd_newton_report;
 
 /* System_of_eqs::do_newton (src_par/do_newton.cpp:65; decl
  * include/system_of_eqs.hpp:871).  Returns KD_OK and fills rep; the fields
  * registered with add_var are updated in place on the device. */
 int kd_newton_step(kd_system* s, const kd_newton_opts* opts, kd_newton_report* rep);
+/* Forgets the pivot order kept for static pivoting: the next mixed-precision
+ * step factors with partial pivoting (no reference counterpart). */
+int kd_system_reset_pivot_order(kd_system* s);
 /* do_newton(precision, error, GAUSS_NEWTON) (include/system_of_eqs.hpp:134,
  * src_par/do_newton.cpp:264-311): for a system with at least as many
  * conditions m as unknowns n, solves the normal equations
@@ -409,6 +420,15 @@ int kd_lu_solve(kd_lu* lu, double* db, int trans);
  * times until the relative residual is below tol (defaults 1e-14, 50, 4);
  * kd_lu_solve returns KD_ERR_NOCONV when it ends above 1e-10. */
 int kd_lu_set_refinement(kd_lu* lu, double tol, int iters, int restarts);
+/* Static pivoting for the mixed modes (off by default here, on for Newton
+ * steps): with on = 1, a factorisation of a matrix of the size of the last
+ * partial-pivoting one gathers the rows in that pivot order and factors
+ * without row search; a zero pivot there, or a refinement that does not
+ * converge with those factors, makes the call factor with partial pivoting
+ * instead.  kd_lu_pivot_info reports, for the last factor/solve, whether
+ * the reused order was used and whether it had to be replaced. */
+int kd_lu_set_pivot_reuse(kd_lu* lu, int on);
+int kd_lu_pivot_info(const kd_lu* lu, int* static_pivots, int* fallback);
 int kd_lu_stats(const kd_lu* lu, double* t_factor_ms, double* t_solve_ms, int* refine_iters,
                 double* rel_residual);
 /* The LU's trailing update on its own: C -= A * B on the tcgen05 tensor

@@ -733,6 +733,7 @@ kd::NewtonOpts to_opts(const kd_newton_opts* opts) {
   o.gmres_tol = opts->gmres_tol > 0 ? opts->gmres_tol : 1e-14;
   o.max_refine = opts->max_refine > 0 ? opts->max_refine : 50;
   o.gmres_restarts = opts->gmres_restarts > 0 ? opts->gmres_restarts : 4;
+  o.pivot_every_step = opts->pivot_every_step;
   o.graph_capture = opts->graph_capture;
   return o;
 }
@@ -750,6 +751,7 @@ void to_report(const kd::NewtonReport& r, kd_newton_report* rep) {
   rep->refine_rel_residual = r.refine_rel_residual;
   rep->kernel_launches = r.kernel_launches;
   rep->fp64_fallback = r.fp64_fallback;
+  rep->static_pivots = r.static_pivots;
 }
 }  // namespace
 
@@ -760,6 +762,10 @@ int kd_newton_step(kd_system* s, const kd_newton_opts* opts, kd_newton_report* r
     s->newton->step(to_opts(opts), r);
     to_report(r, rep);
   });
+}
+
+int kd_system_reset_pivot_order(kd_system* s) {
+  SYS_GUARD(s) { s->newton->lu().forget_pivots(); });
 }
 
 int kd_newton_step_gauss_newton(kd_system* s, const kd_newton_opts* opts, kd_newton_report* rep) {
@@ -955,6 +961,19 @@ int kd_lu_set_refinement(kd_lu* lu, double tol, int iters, int restarts) {
   lu->lu->gmres_tol = tol;
   lu->lu->gmres_max_iter = iters;
   lu->lu->gmres_restarts = restarts;
+  return KD_OK;
+}
+
+int kd_lu_set_pivot_reuse(kd_lu* lu, int on) {
+  if (!lu) return KD_ERR_ARG;
+  lu->lu->reuse_pivots = on != 0;
+  return KD_OK;
+}
+
+int kd_lu_pivot_info(const kd_lu* lu, int* static_pivots, int* fallback) {
+  if (!lu) return KD_ERR_ARG;
+  if (static_pivots) *static_pivots = lu->lu->stats.static_pivots;
+  if (fallback) *fallback = lu->lu->stats.static_pivot_fallback;
   return KD_OK;
 }
 

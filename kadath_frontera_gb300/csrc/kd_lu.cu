@@ -13,8 +13,10 @@
 
 #include <chrono>
 #include <cmath>
-#include <mutex>
+#include <cstdlib>
 #include <cstring>
+#include <mutex>
+#include <string>
 #include <type_traits>
 #include <vector>
 
@@ -146,6 +148,180 @@ __global__ void col_scale_convert_kernel(const double* __restrict__ A, long long
   if (threadIdx.x == 0) cs[j] = c;
   float* out = B + static_cast<long long>(j) * ldb;
   for (int i = threadIdx.x; i < N; i += blockDim.x) out[i] = static_cast<float>(rs[i] * col[i] * c);
+}
+
+// ---- panel of a static-pivot factorisation (FP32, rows in pivot order) ----
+// The rows of the working copy were gathered in the pivot order of an
+// earlier partial-pivoting factorisation, so this panel does no row search:
+// A11 = L11 U11 without exchanges, then L21 = A21 U11^-1.  Every CTA factors
+// the (at most 96 x 96) diagonal block itself in shared memory -- redundant,
+// but it removes every grid-wide synchronisation -- and then solves
+// x U11 = a for NP_THREADS rows of A21, one row per thread with the row in
+// registers.  CTA 0 writes L11 \ U11 back.  A zero or non-finite pivot sets
+// *info (the caller then factors with partial pivoting instead).
+constexpr int NP_NB = 96;
+constexpr int NP_LD = NP_NB + 1;  // odd row stride: row-wise access without bank conflicts
+constexpr int NP_THREADS = 128;
+__global__ void __launch_bounds__(NP_THREADS) panel_nopiv_kernel(float* __restrict__ A, long long ld, int N, int j0,
+                                                                 int jb, int* __restrict__ info) {
+  __shared__ float U[NP_NB * NP_LD];
+  __shared__ float rdiag[NP_NB];
+  const int tid = threadIdx.x;
+  for (int e = tid; e < NP_NB * NP_NB; e += NP_THREADS) {
+    const int i = e % NP_NB, k = e / NP_NB;  // down the columns: coalesced reads
+    float v;
+    if (i < jb && k < jb)
+      v = A[static_cast<long long>(j0 + k) * ld + j0 + i];
+    else
+      v = (i == k) ? 1.0f : 0.0f;  // identity padding past jb
+    U[i * NP_LD + k] = v;
+  }
+  __syncthreads();
+  // Elimination by 32-column chunks.  Inside a chunk, thread i owns row i
+  // and step k updates only the chunk's columns, with the row segment and
+  // the pivot row's segment held in registers (no store-to-load chains in
+  // shared memory).  At the end of a chunk the columns right of it get the
+  // chunk's contributions: U12 = L11^-1 A12 for the chunk's rows (a thread
+  // per column), then A22 -= L21 U12 for the rows below (independent dot
+  // products of length 32).
+#pragma unroll 1
+  for (int c0 = 0; c0 < jb; c0 += 32) {
+    const int c1 = (c0 + 32 < jb) ? c0 + 32 : jb;
+#pragma unroll 1
+    for (int k = c0; k < c1; k++) {
+      if (tid > k && tid < jb) {
+        float* ri = U + tid * NP_LD + c0;
+        const float* rk = U + k * NP_LD + c0;
+        float a[32], p[32];
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+          a[j] = ri[j];
+          p[j] = rk[j];
+        }
+        const int kk = k - c0;
+        float l = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 32; j++)
+          if (j == kk) l = a[j] / p[j];
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+          if (j == kk) a[j] = l;
+          else if (j > kk && c0 + j < c1) a[j] = fmaf(-l, p[j], a[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < 32; j++)
+          if (c0 + j < c1) ri[j] = a[j];
+      }
+      __syncthreads();
+    }
+    if (c1 >= jb) break;
+    // U12 of the chunk's rows: thread t takes column c1 + t
+    if (tid < jb - c1) {
+      const int col = c1 + tid;
+      float u[32];
+#pragma unroll
+      for (int r = 0; r < 32; r++) u[r] = U[(c0 + r) * NP_LD + col];
+#pragma unroll
+      for (int r = 0; r < 32; r++)
+#pragma unroll
+        for (int k = 0; k < 32; k++)
+          if (k < r) u[r] = fmaf(-U[(c0 + r) * NP_LD + c0 + k], u[k], u[r]);
+#pragma unroll
+      for (int r = 0; r < 32; r++) U[(c0 + r) * NP_LD + col] = u[r];
+    }
+    __syncthreads();
+    // A22 -= L21 U12 over the rows and columns past the chunk
+    const int w = jb - c1;
+    for (int e = tid; e < w * w; e += NP_THREADS) {
+      const int i = c1 + e / w, j = c1 + e % w;
+      const float* li = U + i * NP_LD + c0;
+      float acc = U[i * NP_LD + j];
+#pragma unroll
+      for (int k = 0; k < 32; k++) acc = fmaf(-li[k], U[(c0 + k) * NP_LD + j], acc);
+      U[i * NP_LD + j] = acc;
+    }
+    __syncthreads();
+  }
+  if (tid < NP_NB) {
+    const float d = U[tid * NP_LD + tid];
+    if (tid < jb && !(fabsf(d) > 0.0f && isfinite(d)) && blockIdx.x == 0) atomicExch(info, j0 + tid + 1);
+    rdiag[tid] = 1.0f / d;
+  }
+  __syncthreads();
+  if (blockIdx.x == 0)
+    for (int e = tid; e < jb * jb; e += NP_THREADS) {
+      const int i = e % jb, k = e / jb;
+      A[static_cast<long long>(j0 + k) * ld + j0 + i] = U[i * NP_LD + k];
+    }
+  // L21: x U11 = a for this thread's row, by 32-column chunks with the
+  // chunk in registers: a chunk first takes off the products with the
+  // finished chunks (re-read from memory), then is solved against its
+  // 32 x 32 diagonal block of U11, then written back.
+  const int row = j0 + jb + blockIdx.x * NP_THREADS + tid;
+  if (row >= N) return;
+  float* arow = A + static_cast<long long>(j0) * ld + row;  // element k at arow[k * ld]
+#pragma unroll
+  for (int c = 0; c < NP_NB / 32; c++) {
+    if (c * 32 >= jb) break;
+    float x[32];
+#pragma unroll
+    for (int j = 0; j < 32; j++) x[j] = (c * 32 + j < jb) ? arow[static_cast<long long>(c * 32 + j) * ld] : 0.0f;
+#pragma unroll
+    for (int cp = 0; cp < c; cp++) {
+#pragma unroll 2
+      for (int kk = 0; kk < 32; kk++) {
+        const float yk = arow[static_cast<long long>(cp * 32 + kk) * ld];
+        const float* urow = U + (cp * 32 + kk) * NP_LD + c * 32;
+#pragma unroll
+        for (int j = 0; j < 32; j++) x[j] = fmaf(-yk, urow[j], x[j]);
+      }
+    }
+#pragma unroll
+    for (int kk = 0; kk < 32; kk++) {
+      x[kk] *= rdiag[c * 32 + kk];
+      const float xk = x[kk];
+      const float* urow = U + (c * 32 + kk) * NP_LD + c * 32;
+#pragma unroll
+      for (int j = 0; j < 32; j++)
+        if (j > kk) x[j] = fmaf(-xk, urow[j], x[j]);
+    }
+#pragma unroll
+    for (int j = 0; j < 32; j++)
+      if (c * 32 + j < jb) arow[static_cast<long long>(c * 32 + j) * ld] = x[j];
+  }
+}
+
+// The FP32 working copy with its rows in a given order:
+// B[i][j] = r_{p(i)} A[p(i)][j] c_j, c_j = 2^-round(log2 max_i |r_i A_ij|)
+// (the same column scales as col_scale_convert_kernel, whose maximum does
+// not depend on the row order).  rs == nullptr: no scaling.
+__global__ void convert_rows_kernel(const double* __restrict__ A, long long lda, const double* __restrict__ rs,
+                                    int N, double* __restrict__ cs, float* __restrict__ B, long long ldb,
+                                    const int* __restrict__ perm) {
+  __shared__ double red[32];
+  const int j = blockIdx.x;
+  const double* col = A + static_cast<long long>(j) * lda;
+  double c = 1.0;
+  if (rs) {
+    double m = 0.0;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) m = fmax(m, fabs(rs[i] * col[i]));
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      m = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+      if (threadIdx.x == 0) red[0] = m;
+    }
+    __syncthreads();
+    c = pow2_inverse(red[0]);
+    if (threadIdx.x == 0) cs[j] = c;
+  }
+  float* out = B + static_cast<long long>(j) * ldb;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const int p = perm[i];
+    out[i] = static_cast<float>((rs ? rs[p] : 1.0) * col[p] * c);
+  }
 }
 
 __global__ void scale_vec_kernel(double* __restrict__ x, const double* __restrict__ s, int N) {
@@ -376,6 +552,7 @@ double now_ms() {
 }  // namespace
 
 DenseLU::DenseLU(Context* ctx) : ctx_(ctx) {
+  if (const char* e = std::getenv("KD_SWEEP")) pull_sweeps = std::string(e) != "barrier";
   if (cublasCreate(&blas_) != CUBLAS_STATUS_SUCCESS) throw KdError(KD_ERR_CUDA, "cublasCreate failed");
   cublasSetStream(blas_, ctx_->stream());
   cuda_check(cudaMalloc(&d_info_, sizeof(int)), "cudaMalloc(info)");
@@ -412,6 +589,7 @@ DenseLU::~DenseLU() {
   cudaFree(dinv2_u_);
   cudaFree(perm_);
   cudaFree(tri_work_);
+  cudaFree(bsave_);
 }
 
 void DenseLU::ensure_work(size_t n) {
@@ -892,6 +1070,154 @@ __global__ void __launch_bounds__(256) trsv_sweep(const T* __restrict__ A, long 
     }
     if (step + 1 < nblk) sweep_prefetch(A, ld, Dinv, Dinv2, sweep_step(step + 1, nblk, N, lower, ntiles), pf);
     if (!grid_barrier(bar, gridDim.x * static_cast<unsigned>(step + 1) + stall, err, &s_ok, wait_ns)) return;
+  }
+}
+
+// ---- triangular sweeps that pull finished blocks (no grid barrier) --------
+// Block k of the solution, x_k = Dinv_k (b_k - sum_i T_ki x_i) over the
+// blocks i before k in sweep order (T = L forward, U backward).  CTA c owns
+// the blocks at sweep positions c, c + G, ... (G = gridDim.x, every CTA
+// resident: cooperative launch).  A CTA accumulates the products of its
+// block's rows with every finished x_i as soon as that block is done, so
+// only the last product and the Dinv_k product remain on the critical path
+// once x_{k-1} appears.  Finished blocks are announced through one progress
+// counter (release max by the producer, acquire loads by the consumers),
+// the number of sweep positions whose x is in y.  Thread (warp w, lane):
+// row h*32 + lane of the block (h = w >> 2), columns 16 q .. 16 q + 15
+// (q = w & 3) of each contributing block; products in the factors'
+// precision T, 16 at a time, summed in FP64.  Every wait is bounded by
+// wait_ns: on timeout the CTA sets *err and leaves.
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Waits until *progress >= target; returns the value seen, or 0 on timeout.
+__device__ __forceinline__ unsigned wait_progress(const unsigned* progress, unsigned target,
+                                                  unsigned long long wait_ns) {
+  unsigned v = ld_acquire_u32(progress);
+  if (v >= target) return v;
+  const unsigned long long t0 = globaltimer_ns();
+  for (unsigned it = 0;; it++) {
+    __nanosleep(32);
+    v = ld_acquire_u32(progress);
+    if (v >= target) return v;
+    if ((it & 15) == 15 && globaltimer_ns() - t0 > wait_ns) return 0;
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) trsv_pull(const T* __restrict__ A, long long ld, int N,
+                                                 const double* __restrict__ b, double* __restrict__ y,
+                                                 const double* __restrict__ Dinv, const float2* __restrict__ Dinv2,
+                                                 int lower, unsigned* progress, int* err,
+                                                 unsigned long long wait_ns, unsigned stall) {
+  __shared__ double part[4][TB];
+  __shared__ float vh[TB], vl[TB];
+  __shared__ double vd[TB];
+  __shared__ int s_abort;
+  const int nblk = (N + TB - 1) / TB;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int q = warp & 3, h = warp >> 2;
+  const int rr = h * 32 + lane;  // row within the block
+  const int c0 = q * 16;
+  if (tid == 0) s_abort = 0;
+  __syncthreads();
+  unsigned avail = 0;  // sweep positions known finished
+  for (int p = blockIdx.x; p < nblk; p += gridDim.x) {
+    const int k = lower ? p : nblk - 1 - p;
+    const int r0 = k * TB;
+    const int n = (N - r0 < TB) ? N - r0 : TB;
+    const int row = r0 + rr;
+    // this warp's 8 rows of Dinv_k, loaded before any wait
+    float2 dlo[8], dhi[8];
+    double lo[8], hi[8];
+    const size_t dofs = static_cast<size_t>(k) * TB * TB + static_cast<size_t>(warp) * 8 * TB;
+    if constexpr (std::is_same<T, float>::value) {
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        dlo[j] = Dinv2[dofs + j * TB + lane];
+        dhi[j] = Dinv2[dofs + j * TB + lane + 32];
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        lo[j] = Dinv[dofs + j * TB + lane];
+        hi[j] = Dinv[dofs + j * TB + lane + 32];
+      }
+    }
+    double acc = 0.0;
+    bool ok = true;
+    for (int pi = 0; pi < p; pi++) {
+      const int i = lower ? pi : nblk - 1 - pi;
+      const int cb = i * TB + c0;  // first column of this thread's quarter
+      T a[16];
+#pragma unroll
+      for (int j = 0; j < 16; j++)
+        a[j] = (row < N && cb + j < N) ? A[static_cast<long long>(cb + j) * ld + row] : T(0);
+      if (static_cast<unsigned>(pi) >= avail) {
+        avail = wait_progress(progress, static_cast<unsigned>(pi) + 1 + stall, wait_ns);
+        if (avail == 0) {
+          ok = false;
+          break;
+        }
+      }
+      T sum = T(0);
+#pragma unroll
+      for (int j = 0; j < 16; j++) {
+        const double xj = (cb + j < N) ? __ldcg(y + cb + j) : 0.0;
+        sum = fma(a[j], static_cast<T>(xj), sum);
+      }
+      acc += static_cast<double>(sum);
+    }
+    if (!ok) s_abort = 1;
+    part[q][rr] = acc;
+    __syncthreads();
+    if (s_abort) {
+      if (tid == 0) atomicExch(err, 1);
+      return;
+    }
+    if (tid < TB) {
+      const double v = (tid < n) ? b[r0 + tid] - ((part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]))
+                                 : 0.0;
+      vd[tid] = v;
+      const float hv = static_cast<float>(v);
+      vh[tid] = hv;
+      vl[tid] = static_cast<float>(v - static_cast<double>(hv));
+    }
+    __syncthreads();
+    // x_k = Dinv_k v: warp w computes rows 8 w .. 8 w + 7
+    if constexpr (std::is_same<T, float>::value) {
+      const float b0h = vh[lane], b0l = vl[lane], b1h = vh[lane + 32], b1l = vl[lane + 32];
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        DF pr = df_add(df_mul(dlo[j].x, dlo[j].y, b0h, b0l), df_mul(dhi[j].x, dhi[j].y, b1h, b1l));
+        for (int o = 16; o > 0; o >>= 1) {
+          DF r;
+          r.h = __shfl_xor_sync(0xffffffffu, pr.h, o);
+          r.l = __shfl_xor_sync(0xffffffffu, pr.l, o);
+          pr = df_add(pr, r);
+        }
+        const int xr = warp * 8 + j;
+        if (lane == 0 && xr < n) y[r0 + xr] = static_cast<double>(pr.h) + static_cast<double>(pr.l);
+      }
+    } else {
+      const double b0 = vd[lane], b1 = vd[lane + 32];
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        double pr = lo[j] * b0 + hi[j] * b1;
+        for (int o = 16; o > 0; o >>= 1) pr += __shfl_xor_sync(0xffffffffu, pr, o);
+        const int xr = warp * 8 + j;
+        if (lane == 0 && xr < n) y[r0 + xr] = pr;
+      }
+    }
+    __syncthreads();
+    if (tid == 0) {
+      __threadfence();
+      asm volatile("red.release.gpu.global.max.u32 [%0], %1;" ::"l"(progress), "r"(static_cast<unsigned>(p) + 1)
+                   : "memory");
+    }
   }
 }
 
@@ -1700,6 +2026,90 @@ void DenseLU::factor_f32(float* A, long long ld, int N, bool tf32) {
   if (side_pending) ctx_->join();
 }
 
+// Static-pivot factorisation of the FP32 working copy, whose rows are
+// already in the pivot order of an earlier factorisation: per panel of up to
+// 96 columns one launch factors the diagonal block and solves L21, the
+// U12 = L11^-1 A12 triangular solve follows, then the tensor-core trailing
+// update on the whole GPU.  No row exchanges, no grid-wide synchronisation.
+void DenseLU::factor_f32_nopiv(float* A, long long ld, int N, bool tf32) {
+  cudaStream_t s = ctx_->stream();
+  cuda_check(cudaMemsetAsync(d_info_, 0, sizeof(int), s), "memset info");
+  const int NB = NP_NB;
+  for (int j0 = 0; j0 < N; j0 += NB) {
+    const int jb = (N - j0 < NB) ? N - j0 : NB;
+    const int m = N - j0 - jb;
+    {
+      double fl = 0;
+      for (int j = j0; j < j0 + jb; j++) fl += 2.0 * (N - j - 1) * (j0 + jb - j - 1) + (N - j);
+      ProfScope ps(ctx_, Context::PROF_LU_PANEL, fl);
+      const int grid = m > 0 ? blocks(m, NP_THREADS) : 1;
+      panel_nopiv_kernel<<<grid, NP_THREADS, 0, s>>>(A, ld, N, j0, jb, d_info_);
+      ctx_->launches++;
+    }
+    if (m <= 0) break;
+    {
+      ProfScope ps(ctx_, Context::PROF_LU_SWAP_TRSM, double(jb) * jb * m);
+      trsm_unit_lower_f32<<<blocks(m, TRSM32_THREADS), TRSM32_THREADS, 0, s>>>(A, ld, j0, jb, j0 + jb, N);
+      ctx_->launches++;
+    }
+    float* A21 = A + static_cast<long long>(j0) * ld + j0 + jb;
+    float* A12 = A + static_cast<long long>(j0 + jb) * ld + j0;
+    float* A22 = A + static_cast<long long>(j0 + jb) * ld + j0 + jb;
+    const int writable = static_cast<int>(ld - j0 - jb);
+    gemm_update_f32(ctx_, blas_, m, m, jb, A21, ld, A12, ld, A22, ld, tf32, writable, tf32_terms);
+  }
+  cuda_check(cudaGetLastError(), "static-pivot factorisation");
+}
+
+// FP32 working copy of the FP64 matrix (equilibrated, rows in the order
+// `perm` when it is given) and its factorisation: with perm, the
+// static-pivot path; without, partial pivoting.
+void DenseLU::factor_mixed(double* A, long long ld, int N, int mode, const int* perm) {
+  double* rs = eq_buf_;
+  double* cs = eq_buf_ + N;
+  unsigned long long* rmax = reinterpret_cast<unsigned long long*>(eq_buf_ + 2 * static_cast<size_t>(N));
+  cudaStream_t st = ctx_->stream();
+  if (equilibrate) {
+    cuda_check(cudaMemsetAsync(rmax, 0, sizeof(unsigned long long) * N, st), "memset row max");
+    const int rb = blocks(N, 256);
+    int nch = (4 * nsm_ + rb - 1) / rb;
+    if (nch < 1) nch = 1;
+    const int chunk = (N + nch - 1) / nch;
+    nch = (N + chunk - 1) / chunk;
+    row_absmax_kernel<<<dim3(rb, nch), 256, 0, st>>>(A, ld, N, chunk, rmax);
+    row_scale_kernel<<<rb, 256, 0, st>>>(rmax, N, rs);
+    if (perm)
+      convert_rows_kernel<<<N, 256, 0, st>>>(A, ld, rs, N, cs, A32_, ld32_, perm);
+    else
+      col_scale_convert_kernel<<<N, 256, 0, st>>>(A, ld, rs, N, cs, A32_, ld32_);
+    ctx_->launches += 3;
+  } else if (perm) {
+    convert_rows_kernel<<<N, 256, 0, st>>>(A, ld, nullptr, N, nullptr, A32_, ld32_, perm);
+    ctx_->launches++;
+  } else {
+    d2s<<<152 * 8, 256, 0, st>>>(A, ld, A32_, ld32_, N);
+    ctx_->launches++;
+  }
+  scaled_ = equilibrate;
+  iota_kernel<<<blocks(N, 256), 256, 0, st>>>(ipiv_, N);
+  ctx_->launches++;
+  if (perm) {
+    factor_f32_nopiv(A32_, ld32_, N, mode == LU_TF32_IR);
+    prepare_solves<float>(A32_, ld32_, N, true);
+  } else {
+    factor_f32(A32_, ld32_, N, mode == LU_TF32_IR);
+    prepare_solves<float>(A32_, ld32_, N, false);
+  }
+  nopiv_ = perm != nullptr;
+}
+
+int DenseLU::read_info() {
+  int info = 0;
+  cuda_check(cudaMemcpyAsync(&info, d_info_, sizeof(int), cudaMemcpyDeviceToHost, ctx_->stream()), "D2H info");
+  cuda_check(cudaStreamSynchronize(ctx_->stream()), "sync after LU");
+  return info;
+}
+
 void DenseLU::factor(double* A, long long ld, int N, int mode) {
   if (N <= 0) throw KdError(KD_ERR_ARG, "empty matrix");
   double t0 = now_ms();
@@ -1718,7 +2128,8 @@ void DenseLU::factor(double* A, long long ld, int N, int mode) {
   ctx_->launches++;
   if (mode == LU_FP64) {
     factor_fp64(A, ld, N);
-    prepare_solves<double>(A, ld, N);
+    prepare_solves<double>(A, ld, N, false);
+    nopiv_ = false;
   } else {
     ld32_ = ((static_cast<long long>(N) + 31) / 32) * 32;  // 128-byte aligned columns
     const size_t need = static_cast<size_t>(ld32_) * N;
@@ -1732,32 +2143,18 @@ void DenseLU::factor(double* A, long long ld, int N, int mode) {
       cuda_check(cudaMalloc(&eq_buf_, sizeof(double) * 3 * static_cast<size_t>(N)), "cudaMalloc(equilibration)");
       eq_cap_ = N;
     }
-    double* rs = eq_buf_;
-    double* cs = eq_buf_ + N;
-    unsigned long long* rmax = reinterpret_cast<unsigned long long*>(eq_buf_ + 2 * static_cast<size_t>(N));
-    cudaStream_t st = ctx_->stream();
-    if (equilibrate) {
-      cuda_check(cudaMemsetAsync(rmax, 0, sizeof(unsigned long long) * N, st), "memset row max");
-      const int rb = blocks(N, 256);
-      int nch = (4 * nsm_ + rb - 1) / rb;
-      if (nch < 1) nch = 1;
-      const int chunk = (N + nch - 1) / nch;
-      nch = (N + chunk - 1) / chunk;
-      row_absmax_kernel<<<dim3(rb, nch), 256, 0, st>>>(A, ld, N, chunk, rmax);
-      row_scale_kernel<<<rb, 256, 0, st>>>(rmax, N, rs);
-      col_scale_convert_kernel<<<N, 256, 0, st>>>(A, ld, rs, N, cs, A32_, ld32_);
-      ctx_->launches += 3;
-    } else {
-      d2s<<<152 * 8, 256, 0, st>>>(A, ld, A32_, ld32_, N);
-      ctx_->launches++;
+    // later factorisations of a matrix of the same size reuse the pivot
+    // order of the last partial-pivoting factorisation (static pivoting)
+    const bool reuse = reuse_pivots && perm_n_ == N;
+    factor_mixed(A, ld, N, mode, reuse ? perm_ : nullptr);
+    if (reuse && read_info() != 0) {
+      // a zero or non-finite pivot in that order: factor with partial pivoting
+      stats.static_pivot_fallback = 1;
+      perm_n_ = 0;
+      factor_mixed(A, ld, N, mode, nullptr);
     }
-    scaled_ = equilibrate;
-    factor_f32(A32_, ld32_, N, mode == LU_TF32_IR);
-    prepare_solves<float>(A32_, ld32_, N);
   }
-  int info = 0;
-  cuda_check(cudaMemcpyAsync(&info, d_info_, sizeof(int), cudaMemcpyDeviceToHost, ctx_->stream()), "D2H info");
-  cuda_check(cudaStreamSynchronize(ctx_->stream()), "sync after LU");
+  int info = read_info();
   stats.t_factor_ms = now_ms() - t0;
   int perr = 0;
   cuda_check(cudaMemcpyAsync(&perr, panel_err_, sizeof(int), cudaMemcpyDeviceToHost, ctx_->stream()),
@@ -1770,6 +2167,8 @@ void DenseLU::factor(double* A, long long ld, int N, int mode) {
   if (mode == LU_TF32_IR && tf32_gemm_error_flag(ctx_))
     throw KdError(KD_ERR_TIMEOUT, "tensor-core trailing update timed out waiting for its MMAs");
   if (info != 0) throw KdError(KD_ERR_SINGULAR, "Jacobian is singular (zero pivot at column " + std::to_string(info) + ")");
+  if (!nopiv_) perm_n_ = N;  // perm_ holds this factorisation's pivot order
+  stats.static_pivots = nopiv_ ? 1 : 0;
 }
 
 // Triangular solves by 64-row blocks with precomputed inverses of the
@@ -1804,12 +2203,25 @@ void DenseLU::tri_solve(const T* LU, long long ld, int N, double* b, int trans) 
     const float2* du2 = std::is_same<T, float>::value ? dinv2_u_ : nullptr;
     const unsigned long long wait = ctx_->grid_wait_ns;
     const unsigned stall = ctx_->stall_waits ? 1u : 0u;
-    cuda_check(cudaLaunchKernelEx(&cfg, trsv_sweep<T>, LU, ld, N, w1, w2, dl, dl2, 1, tri_bar_, panel_err_, wait,
-                                  stall),
-               "forward sweep");
-    cuda_check(cudaLaunchKernelEx(&cfg, trsv_sweep<T>, LU, ld, N, w2, b, du, du2, 0, tri_bar_ + 1, panel_err_, wait,
-                                  stall),
-               "backward sweep");
+    if (pull_sweeps) {
+      int gp = nblk < ctx_->sms() ? nblk : ctx_->sms();
+      cfg.gridDim = dim3(gp, 1, 1);
+      const double* w1c = w1;
+      const double* w2c = w2;
+      cuda_check(cudaLaunchKernelEx(&cfg, trsv_pull<T>, LU, ld, N, w1c, w2, dl, dl2, 1, tri_bar_, panel_err_, wait,
+                                    stall),
+                 "forward sweep");
+      cuda_check(cudaLaunchKernelEx(&cfg, trsv_pull<T>, LU, ld, N, w2c, b, du, du2, 0, tri_bar_ + 1, panel_err_,
+                                    wait, stall),
+                 "backward sweep");
+    } else {
+      cuda_check(cudaLaunchKernelEx(&cfg, trsv_sweep<T>, LU, ld, N, w1, w2, dl, dl2, 1, tri_bar_, panel_err_, wait,
+                                    stall),
+                 "forward sweep");
+      cuda_check(cudaLaunchKernelEx(&cfg, trsv_sweep<T>, LU, ld, N, w2, b, du, du2, 0, tri_bar_ + 1, panel_err_,
+                                    wait, stall),
+                 "backward sweep");
+    }
     ctx_->launches += 3;
     cuda_check(cudaGetLastError(), "triangular solve");
     return;
@@ -1851,10 +2263,34 @@ void DenseLU::solve_f32(double* b) {
   }
 }
 
+// A sweep that gave up is reported first (its garbage also stops the
+// refinement), and its flag is cleared so the context stays usable.
+void DenseLU::check_sweeps() {
+  cuda_check(cudaStreamSynchronize(ctx_->stream()), "sync after solve");
+  int perr = 0;
+  cuda_check(cudaMemcpyAsync(&perr, panel_err_, sizeof(int), cudaMemcpyDeviceToHost, ctx_->stream()),
+             "D2H sweep flag");
+  cuda_check(cudaStreamSynchronize(ctx_->stream()), "sync sweep flag");
+  if (perr) {
+    cuda_check(cudaMemsetAsync(panel_err_, 0, sizeof(int), ctx_->stream()), "reset sweep flag");
+    cuda_check(cudaStreamSynchronize(ctx_->stream()), "sync sweep flag reset");
+    throw KdError(KD_ERR_TIMEOUT, "triangular solve: a grid barrier wait ran out");
+  }
+}
+
+void DenseLU::ensure_bsave() {
+  if (static_cast<size_t>(N_) > bsave_cap_) {
+    cudaFree(bsave_);
+    bsave_ = nullptr;
+    cuda_check(cudaMalloc(&bsave_, sizeof(double) * N_), "cudaMalloc(rhs copy)");
+    bsave_cap_ = N_;
+  }
+}
+
 // After factorisation: pivots as one permutation, inverses of the 64 x 64
 // diagonal blocks of L (unit lower) and U.
 template <class T>
-void DenseLU::prepare_solves(const T* LU, long long ld, int N) {
+void DenseLU::prepare_solves(const T* LU, long long ld, int N, bool keep_perm) {
   cudaStream_t s = ctx_->stream();
   const int nblk = (N + TB - 1) / TB;
   size_t need = static_cast<size_t>(nblk) * TB * TB;
@@ -1877,7 +2313,7 @@ void DenseLU::prepare_solves(const T* LU, long long ld, int N) {
     cuda_check(cudaMalloc(&tri_work_, sizeof(double) * 2 * N), "cudaMalloc(tri work)");
     perm_cap_ = N;
   }
-  build_perm<<<1, 1, 0, s>>>(ipiv_, N, perm_);
+  if (!keep_perm) build_perm<<<1, 1, 0, s>>>(ipiv_, N, perm_);
   size_t smem = sizeof(double) * 3 * TB * TB;
   static std::once_flag attr_set;
   std::call_once(attr_set, [smem] {
@@ -2046,20 +2482,35 @@ void DenseLU::solve(double* b, int trans) {
     solve_fp64(A_, ld_, N_, b, trans);
   } else {
     if (trans) throw KdError(KD_ERR_UNSUPPORTED, "transposed solve needs the FP64 factors");
+    if (nopiv_) {
+      ensure_bsave();
+      cuda_check(cudaMemcpyAsync(bsave_, b, sizeof(double) * N_, cudaMemcpyDeviceToDevice, ctx_->stream()),
+                 "keep right-hand side");
+    }
     gmres_ir(b);
+    check_sweeps();
+    if (nopiv_) {
+      if (!(stats.final_rel_residual < 1e-10)) {
+        // the reused pivot order does not precondition this matrix: factor
+        // it with partial pivoting and solve again
+        stats.static_pivot_fallback = 1;
+        perm_n_ = 0;
+        factor_mixed(A_, ld_, N_, mode_, nullptr);
+        const int info = read_info();
+        if (info != 0)
+          throw KdError(KD_ERR_SINGULAR, "Jacobian is singular (zero pivot at column " + std::to_string(info) + ")");
+        perm_n_ = N_;
+        cuda_check(cudaMemcpyAsync(b, bsave_, sizeof(double) * N_, cudaMemcpyDeviceToDevice, ctx_->stream()),
+                   "restore right-hand side");
+        gmres_ir(b);
+        check_sweeps();
+      } else if (stats.refine_iters > pivoted_iters_ + 4) {
+        perm_n_ = 0;  // the order has drifted: the next factorisation pivots again
+      }
+    }
+    if (!nopiv_) pivoted_iters_ = stats.refine_iters;
   }
-  // a sweep that gave up is reported first (its garbage also stops the
-  // refinement), and its flag is cleared so the context stays usable
-  cuda_check(cudaStreamSynchronize(ctx_->stream()), "sync after solve");
-  int perr = 0;
-  cuda_check(cudaMemcpyAsync(&perr, panel_err_, sizeof(int), cudaMemcpyDeviceToHost, ctx_->stream()),
-             "D2H sweep flag");
-  cuda_check(cudaStreamSynchronize(ctx_->stream()), "sync sweep flag");
-  if (perr) {
-    cuda_check(cudaMemsetAsync(panel_err_, 0, sizeof(int), ctx_->stream()), "reset sweep flag");
-    cuda_check(cudaStreamSynchronize(ctx_->stream()), "sync sweep flag reset");
-    throw KdError(KD_ERR_TIMEOUT, "triangular solve: a grid barrier wait ran out");
-  }
+  check_sweeps();
   if (mode_ != LU_FP64 && !(stats.final_rel_residual < 1e-10))
     throw KdError(KD_ERR_NOCONV, "GMRES-IR did not converge (relative residual " +
                                      std::to_string(stats.final_rel_residual) + ")");

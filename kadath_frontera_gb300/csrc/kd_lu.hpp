@@ -21,6 +21,8 @@ struct LuStats {
   int refine_iters = 0;
   double final_rel_residual = 0;
   long long flops = 0;
+  int static_pivots = 0;          // the factors used a reused pivot order
+  int static_pivot_fallback = 0;  // that order failed and partial pivoting was redone
 };
 
 class DenseLU {
@@ -50,6 +52,19 @@ class DenseLU {
   // Mixed modes: factor D_r A D_c (power-of-two row and column scales), the
   // refinement works on A itself.
   bool equilibrate = true;
+  // Mixed modes: a factorisation of a matrix of the size of the last
+  // partial-pivoting one reuses its pivot order (static pivoting: the rows
+  // are gathered in that order and factored without row search; GMRES-IR
+  // against the FP64 matrix restores the accuracy).  When the refinement
+  // does not converge with those factors, the matrix is factored again with
+  // partial pivoting; when it needs more than 4 iterations beyond the
+  // pivoted factors' count, the next factorisation pivots again.
+  bool reuse_pivots = false;
+  // Triangular sweeps that pull finished blocks through a progress counter
+  // (true) or step with one grid barrier per 64-row block (false).
+  bool pull_sweeps = true;
+  // Forgets the pivot order: the next factorisation pivots.
+  void forget_pivots() { perm_n_ = 0; }
 
  private:
   Context* ctx_;
@@ -89,7 +104,17 @@ class DenseLU {
   template <class T>
   void tri_solve(const T* LU, long long ld, int N, double* b, int trans);
   template <class T>
-  void prepare_solves(const T* LU, long long ld, int N);
+  void prepare_solves(const T* LU, long long ld, int N, bool keep_perm);
+  void factor_f32_nopiv(float* A, long long ld, int N, bool tf32);
+  void factor_mixed(double* A, long long ld, int N, int mode, const int* perm);
+  int read_info();
+  void check_sweeps();
+  void ensure_bsave();
+  bool nopiv_ = false;        // the current factors are static-pivot ones
+  int perm_n_ = 0;            // N of the pivot order in perm_ (0: none)
+  int pivoted_iters_ = 1000;  // refinement iterations with the last pivoted factors
+  double* bsave_ = nullptr;   // right-hand side kept for a re-solve
+  size_t bsave_cap_ = 0;
   double* dinv_l_ = nullptr;  // inverses of the 64 x 64 diagonal blocks
   double* dinv_u_ = nullptr;
   float2* dinv2_l_ = nullptr;  // the same as (hi, lo) FP32 pairs (sweeps with FP32 factors)

@@ -79,6 +79,7 @@ bool Newton::step(const NewtonOpts& o, NewtonReport& rep) {
   lu_->gmres_tol = o.gmres_tol;
   lu_->gmres_max_iter = o.max_refine;
   lu_->gmres_restarts = o.gmres_restarts;
+  lu_->reuse_pivots = o.pivot_every_step == 0;
   const bool mixed = o.lu_mode != LU_FP64;
   if (mixed)
     cuda_check(cudaMemcpyAsync(d_F0, d_F, sizeof(double) * N, cudaMemcpyDeviceToDevice, s), "keep F");
@@ -98,6 +99,7 @@ bool Newton::step(const NewtonOpts& o, NewtonReport& rep) {
     lu_->solve(d_F, 0);
   }
   rep.t_solve_ms = lu_->stats.t_solve_ms;
+  rep.static_pivots = lu_->stats.static_pivots && !lu_->stats.static_pivot_fallback;
   rep.refine_iters = lu_->stats.refine_iters;
   rep.refine_rel_residual = lu_->stats.final_rel_residual;
   auto t3 = std::chrono::steady_clock::now();
@@ -170,6 +172,7 @@ bool Newton::step_gauss_newton(const NewtonOpts& o, NewtonReport& rep) {
   lu_->gmres_tol = o.gmres_tol;
   lu_->gmres_max_iter = o.max_refine;
   lu_->gmres_restarts = o.gmres_restarts;
+  lu_->reuse_pivots = o.pivot_every_step == 0;
   lu_->factor(d_JtJ_, n, n, o.lu_mode);
   rep.t_factor_ms = lu_->stats.t_factor_ms;
   lu_->solve(d_JtF_, 0);
@@ -238,6 +241,7 @@ bool Newton::step_linesearch(const NewtonOpts& o, int ntrymax, double stepmax, N
   lu_->gmres_tol = o.gmres_tol;
   lu_->gmres_max_iter = o.max_refine;
   lu_->gmres_restarts = o.gmres_restarts;
+  lu_->reuse_pivots = o.pivot_every_step == 0;
   lu_->factor(d_J, ld, N, o.lu_mode);
   rep.t_factor_ms = lu_->stats.t_factor_ms;
   lu_->solve(d_F, 0);

@@ -17,6 +17,7 @@ struct NewtonOpts {
   int max_refine = 50;
   int gmres_restarts = 4;
   int graph_capture = 0;
+  int pivot_every_step = 0;
 };
 
 struct NewtonReport {
@@ -28,6 +29,7 @@ struct NewtonReport {
   double refine_rel_residual = 0;
   long long kernel_launches = 0;
   int fp64_fallback = 0;
+  int static_pivots = 0;
 };
 
 class Newton {

@@ -32,14 +32,14 @@ KD_EOS_EPSILON, KD_EOS_PRESSURE, KD_EOS_DENSITY, KD_EOS_DHDRHO = 0, 1, 2, 3
 
 class NewtonOpts(C.Structure):
     _fields_ = [("precision", C.c_double), ("lu_mode", C.c_int), ("gmres_tol", C.c_double), ("max_refine", C.c_int),
-                ("graph_capture", C.c_int), ("gmres_restarts", C.c_int)]
+                ("graph_capture", C.c_int), ("gmres_restarts", C.c_int), ("pivot_every_step", C.c_int)]
 
 
 class NewtonReport(C.Structure):
     _fields_ = [("error", C.c_double), ("converged", C.c_int), ("n", C.c_int), ("t_residual_ms", C.c_double),
                 ("t_assembly_ms", C.c_double), ("t_factor_ms", C.c_double), ("t_solve_ms", C.c_double),
                 ("t_update_ms", C.c_double), ("refine_iters", C.c_int), ("refine_rel_residual", C.c_double),
-                ("kernel_launches", C.c_longlong), ("fp64_fallback", C.c_int)]
+                ("kernel_launches", C.c_longlong), ("fp64_fallback", C.c_int), ("static_pivots", C.c_int)]
 
     def as_dict(self):
         return {f[0]: getattr(self, f[0]) for f in self._fields_}
@@ -108,6 +108,7 @@ def _declare_system(lib):
         "kd_system_jacobian_device": (I, [P, P, C.c_longlong]),
         "kd_system_update": (I, [P, DP]),
         "kd_newton_step": (I, [P, C.POINTER(NewtonOpts), C.POINTER(NewtonReport)]),
+        "kd_system_reset_pivot_order": (I, [P]),
         "kd_newton_step_gauss_newton": (I, [P, C.POINTER(NewtonOpts), C.POINTER(NewtonReport)]),
         "kd_newton_step_linesearch": (I, [P, C.POINTER(NewtonOpts), I, D, C.POINTER(NewtonReport), DP]),
         "kd_system_set_cst": (I, [P, C.c_char_p, D]),
@@ -124,6 +125,8 @@ def _declare_system(lib):
         "kd_lu_solve": (I, [P, P, I]),
         "kd_lu_stats": (I, [P, DP, DP, IP, DP]),
         "kd_lu_set_refinement": (I, [P, D, I, I]),
+        "kd_lu_set_pivot_reuse": (I, [P, I]),
+        "kd_lu_pivot_info": (I, [P, IP, IP]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -635,22 +638,28 @@ class System_of_eqs:
         self._J = None
 
     def do_newton(self, precision, lu_mode=None, gmres_tol=1e-14, max_refine=50, solver=None, graph=None,
-                  gmres_restarts=4):
+                  gmres_restarts=4, pivot_every_step=False):
         """System_of_eqs::do_newton(precision, error, solver): returns
         (converged, error); solver NEWTON_RAPHSON (default) or GAUSS_NEWTON.
         graph: replay the residual's value pass from a CUDA graph (default:
         the system's graph_capture attribute).  A mixed-precision solve that
         ends above a relative residual of 1e-10 is redone with the FP64 LU
-        (last_report["fp64_fallback"])."""
+        (last_report["fp64_fallback"]).  Later mixed-precision steps reuse the
+        pivot order of the last pivoted factorisation unless pivot_every_step
+        (last_report["static_pivots"])."""
         g = self.graph_capture if graph is None else graph
         opts = NewtonOpts(precision, self.lu_mode if lu_mode is None else lu_mode, gmres_tol, max_refine,
-                          1 if g else 0, gmres_restarts)
+                          1 if g else 0, gmres_restarts, 1 if pivot_every_step else 0)
         rep = NewtonReport()
         fn = _L().kd_newton_step_gauss_newton if solver == GAUSS_NEWTON else _L().kd_newton_step
         self.ctx.check(fn(self.h, C.byref(opts), C.byref(rep)))
         self.last_report = rep.as_dict()
         self._J = None
         return bool(rep.converged), rep.error
+
+    def reset_pivot_order(self):
+        """The next mixed-precision step factors with partial pivoting."""
+        self.ctx.check(_L().kd_system_reset_pivot_order(self.h))
 
     def graph_stats(self):
         """(captures, replays) of the residual's value pass."""
@@ -662,7 +671,7 @@ class System_of_eqs:
                                   max_refine=50):
         """System_of_eqs::do_newton_with_linesearch: returns (converged, error,
         last lambda)."""
-        opts = NewtonOpts(precision, self.lu_mode if lu_mode is None else lu_mode, gmres_tol, max_refine, 0, 4)
+        opts = NewtonOpts(precision, self.lu_mode if lu_mode is None else lu_mode, gmres_tol, max_refine, 0, 4, 0)
         rep = NewtonReport()
         lam = C.c_double()
         self.ctx.check(_L().kd_newton_step_linesearch(self.h, C.byref(opts), ntrymax, stepmax, C.byref(rep),
@@ -693,6 +702,16 @@ class DenseLU:
 
     def solve(self, db_ptr, trans=0):
         self.ctx.check(_L().kd_lu_solve(self.h, C.c_void_p(db_ptr), trans))
+
+    def set_pivot_reuse(self, on=True):
+        """Static pivoting: later factorisations reuse the last pivot order."""
+        self.ctx.check(_L().kd_lu_set_pivot_reuse(self.h, 1 if on else 0))
+
+    def pivot_info(self):
+        """(static pivots used, fallback to partial pivoting) of the last call."""
+        a, b = C.c_int(), C.c_int()
+        self.ctx.check(_L().kd_lu_pivot_info(self.h, C.byref(a), C.byref(b)))
+        return bool(a.value), bool(b.value)
 
     def set_refinement(self, tol=1e-14, iters=50, restarts=4):
         """GMRES(iters) with at most `restarts` cycles down to tol (mixed modes)."""

@@ -72,12 +72,18 @@ def build():
 
 
 def run_spec(spec: str, workdir: Path):
+    """Runs the driver; returns the reference's own printed timings of each
+    Newton step (do_newton_seq's "Loading the matrix" and "Inverting the
+    matrix" lines, seconds) as an array of (assembly, LU) pairs."""
     (workdir / "case.spec").write_text(spec)
     t = time.time()
     r = subprocess.run([str(REF_BIN / "ref_newton"), "case.spec"], cwd=workdir, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"ref_newton failed ({r.returncode}):\n{r.stdout[-2000:]}\n{r.stderr[-2000:]}")
     print(f"  ref_newton: {time.time() - t:.1f} s", flush=True)
+    load = [float(ln.split(":")[1].split()[0]) for ln in r.stdout.splitlines() if ln.startswith("Loading the matrix")]
+    inv = [float(ln.split(":")[1].split()[0]) for ln in r.stdout.splitlines() if ln.startswith("Inverting the matrix")]
+    return np.array(list(zip(load, inv)))
 
 
 def load(workdir: Path, name: str) -> np.ndarray:
@@ -210,8 +216,12 @@ def system_dumps(spec_body, w: Path, n_unknowns, cols, seed, newton=True):
         spec += "dump_jx x.bin jx.bin\n"
     if newton:
         spec += "newton 1e-10 12 it\n"
-    run_spec(spec, w)
+    timings = run_spec(spec, w)
     out = {"F0": load(w, "F0.bin")}
+    if newton:
+        # seconds per step as the reference prints them, on the machine that
+        # made the fixture (assembly on one core; LU through the stand-in)
+        out["ref_step_seconds"] = timings
     if cols is not None:
         out["cols"] = np.array(cols)
         out["J_cols"] = load(w, "cols.bin").reshape(len(cols), -1)

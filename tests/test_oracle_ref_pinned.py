@@ -125,3 +125,19 @@ def test_vector_star_matches_the_reference(name):
 def _star_vector(res):
     doms, sysm, fields, matter = CF.star_vector(res)
     return doms, sysm, fields, matter
+
+
+def test_star_residual_at_the_timed_size_matches_the_reference():
+    """The isolated star at (13, 9, 4), N = 12,331: the oracle's residual at
+    the initial guess against the reference's sec_member (the iterates at this
+    size are compared on the GPU, tests/test_gpu_ref_pinned.py)."""
+    z = np.load(GOLD / "ref_star_1394.npz")
+    doms, sysm, _, (E, E2S) = _star_vector(tuple(z["res"]))
+    got_E = np.concatenate([np.asarray(E[d.num].c).ravel() for d in doms])
+    assert np.array_equal(got_E, z["E"])
+    F = sysm.residual()
+    assert len(F) == len(z["F0"]) == 12331
+    # absolute round-off of the residual (about 1e-14 here, amplified by the
+    # spectral second derivatives); the other tests compare at 1e-13 max|J|
+    # and max|J| is far above 1 at this resolution
+    assert np.abs(F - z["F0"]).max() < 1e-13
