@@ -161,12 +161,14 @@ __global__ void col_scale_convert_kernel(const double* __restrict__ A, long long
 // *info (the caller then factors with partial pivoting instead).
 constexpr int NP_NB = 96;
 constexpr int NP_LD = NP_NB + 1;  // odd row stride: row-wise access without bank conflicts
-constexpr int NP_THREADS = 128;
+constexpr int NP_THREADS = 256;
+static_assert(NP_THREADS == 256 && NP_NB == 96, "the register tiling is 8 warps x 12 rows by 32 lanes x 3 columns");
 __global__ void __launch_bounds__(NP_THREADS) panel_nopiv_kernel(float* __restrict__ A, long long ld, int N, int j0,
                                                                  int jb, int* __restrict__ info) {
   __shared__ float U[NP_NB * NP_LD];
   __shared__ float rdiag[NP_NB];
-  const int tid = threadIdx.x;
+  __shared__ float pbuf[2][NP_NB], cbuf[2][NP_NB];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int e = tid; e < NP_NB * NP_NB; e += NP_THREADS) {
     const int i = e % NP_NB, k = e / NP_NB;  // down the columns: coalesced reads
     float v;
@@ -177,71 +179,63 @@ __global__ void __launch_bounds__(NP_THREADS) panel_nopiv_kernel(float* __restri
     U[i * NP_LD + k] = v;
   }
   __syncthreads();
-  // Elimination by 32-column chunks.  Inside a chunk, thread i owns row i
-  // and step k updates only the chunk's columns, with the row segment and
-  // the pivot row's segment held in registers (no store-to-load chains in
-  // shared memory).  At the end of a chunk the columns right of it get the
-  // chunk's contributions: U12 = L11^-1 A12 for the chunk's rows (a thread
-  // per column), then A22 -= L21 U12 for the rows below (independent dot
-  // products of length 32).
-#pragma unroll 1
-  for (int c0 = 0; c0 < jb; c0 += 32) {
-    const int c1 = (c0 + 32 < jb) ? c0 + 32 : jb;
-#pragma unroll 1
-    for (int k = c0; k < c1; k++) {
-      if (tid > k && tid < jb) {
-        float* ri = U + tid * NP_LD + c0;
-        const float* rk = U + k * NP_LD + c0;
-        float a[32], p[32];
+  // Right-looking elimination with the block in registers: thread (warp w,
+  // lane l) holds rows w + 8 ii (ii < 12) and columns l + 32 jj (jj < 3).
+  // Step k publishes the pivot row (by warp k mod 8) and the pivot column
+  // (by lane k mod 32 of every warp) through double-buffered shared memory,
+  // one barrier per step; every thread then forms its rows' multipliers and
+  // updates its 36 elements in registers.
+  float a[12][3];
 #pragma unroll
-        for (int j = 0; j < 32; j++) {
-          a[j] = ri[j];
-          p[j] = rk[j];
+  for (int ii = 0; ii < 12; ii++)
+#pragma unroll
+    for (int jj = 0; jj < 3; jj++) a[ii][jj] = U[(warp + 8 * ii) * NP_LD + lane + 32 * jj];
+  for (int k = 0; k < jb - 1; k++) {
+    float* prow = pbuf[k & 1];
+    float* pcol = cbuf[k & 1];
+    if (warp == (k & 7)) {
+      const int ik = k >> 3;
+#pragma unroll
+      for (int ii = 0; ii < 12; ii++)
+        if (ii == ik) {
+#pragma unroll
+          for (int jj = 0; jj < 3; jj++) prow[lane + 32 * jj] = a[ii][jj];
         }
-        const int kk = k - c0;
-        float l = 0.0f;
+    }
+    if (lane == (k & 31)) {
+      const int jk = k >> 5;
 #pragma unroll
-        for (int j = 0; j < 32; j++)
-          if (j == kk) l = a[j] / p[j];
+      for (int jj = 0; jj < 3; jj++)
+        if (jj == jk) {
 #pragma unroll
-        for (int j = 0; j < 32; j++) {
-          if (j == kk) a[j] = l;
-          else if (j > kk && c0 + j < c1) a[j] = fmaf(-l, p[j], a[j]);
+          for (int ii = 0; ii < 12; ii++) pcol[warp + 8 * ii] = a[ii][jj];
         }
+    }
+    __syncthreads();
+    const float rp = 1.0f / prow[k];
+    float pr[3];
 #pragma unroll
-        for (int j = 0; j < 32; j++)
-          if (c0 + j < c1) ri[j] = a[j];
+    for (int jj = 0; jj < 3; jj++) pr[jj] = prow[lane + 32 * jj];
+#pragma unroll
+    for (int ii = 0; ii < 12; ii++) {
+      const int i = warp + 8 * ii;
+      if (i > k) {
+        const float l = pcol[i] * rp;
+#pragma unroll
+        for (int jj = 0; jj < 3; jj++) {
+          const int j = lane + 32 * jj;
+          if (j == k) a[ii][jj] = l;
+          else if (j > k) a[ii][jj] = fmaf(-l, pr[jj], a[ii][jj]);
+        }
       }
-      __syncthreads();
     }
-    if (c1 >= jb) break;
-    // U12 of the chunk's rows: thread t takes column c1 + t
-    if (tid < jb - c1) {
-      const int col = c1 + tid;
-      float u[32];
-#pragma unroll
-      for (int r = 0; r < 32; r++) u[r] = U[(c0 + r) * NP_LD + col];
-#pragma unroll
-      for (int r = 0; r < 32; r++)
-#pragma unroll
-        for (int k = 0; k < 32; k++)
-          if (k < r) u[r] = fmaf(-U[(c0 + r) * NP_LD + c0 + k], u[k], u[r]);
-#pragma unroll
-      for (int r = 0; r < 32; r++) U[(c0 + r) * NP_LD + col] = u[r];
-    }
-    __syncthreads();
-    // A22 -= L21 U12 over the rows and columns past the chunk
-    const int w = jb - c1;
-    for (int e = tid; e < w * w; e += NP_THREADS) {
-      const int i = c1 + e / w, j = c1 + e % w;
-      const float* li = U + i * NP_LD + c0;
-      float acc = U[i * NP_LD + j];
-#pragma unroll
-      for (int k = 0; k < 32; k++) acc = fmaf(-li[k], U[(c0 + k) * NP_LD + j], acc);
-      U[i * NP_LD + j] = acc;
-    }
-    __syncthreads();
   }
+  __syncthreads();
+#pragma unroll
+  for (int ii = 0; ii < 12; ii++)
+#pragma unroll
+    for (int jj = 0; jj < 3; jj++) U[(warp + 8 * ii) * NP_LD + lane + 32 * jj] = a[ii][jj];
+  __syncthreads();
   if (tid < NP_NB) {
     const float d = U[tid * NP_LD + tid];
     if (tid < jb && !(fabsf(d) > 0.0f && isfinite(d)) && blockIdx.x == 0) atomicExch(info, j0 + tid + 1);
@@ -552,7 +546,10 @@ double now_ms() {
 }  // namespace
 
 DenseLU::DenseLU(Context* ctx) : ctx_(ctx) {
-  if (const char* e = std::getenv("KD_SWEEP")) pull_sweeps = std::string(e) != "barrier";
+  if (const char* e = std::getenv("KD_SWEEP")) {
+    const std::string v(e);
+    sweep_kind = v == "barrier" ? 0 : v == "pull" ? 1 : 2;
+  }
   if (cublasCreate(&blas_) != CUBLAS_STATUS_SUCCESS) throw KdError(KD_ERR_CUDA, "cublasCreate failed");
   cublasSetStream(blas_, ctx_->stream());
   cuda_check(cudaMalloc(&d_info_, sizeof(int)), "cudaMalloc(info)");
@@ -1157,11 +1154,12 @@ __global__ void __launch_bounds__(256) trsv_pull(const T* __restrict__ A, long l
       for (int j = 0; j < 16; j++)
         a[j] = (row < N && cb + j < N) ? A[static_cast<long long>(cb + j) * ld + row] : T(0);
       if (static_cast<unsigned>(pi) >= avail) {
-        avail = wait_progress(progress, static_cast<unsigned>(pi) + 1 + stall, wait_ns);
-        if (avail == 0) {
+        const unsigned v = wait_progress(progress, static_cast<unsigned>(pi) + 1 + stall, wait_ns);
+        if (v == 0) {
           ok = false;
           break;
         }
+        avail = v - stall;  // positions known finished
       }
       T sum = T(0);
 #pragma unroll
@@ -1217,6 +1215,182 @@ __global__ void __launch_bounds__(256) trsv_pull(const T* __restrict__ A, long l
       __threadfence();
       asm volatile("red.release.gpu.global.max.u32 [%0], %1;" ::"l"(progress), "r"(static_cast<unsigned>(p) + 1)
                    : "memory");
+    }
+  }
+}
+
+// The same sweep with CH_R consecutive blocks per CTA: CTA c owns sweep
+// positions c R .. c R + R - 1.  While earlier CTAs work it accumulates, for
+// all its blocks at once, the products with every finished x (phase A, one
+// progress wait per finished block).  Its own blocks then chain inside the
+// CTA (phase B): x_p from the accumulated rows and Dinv, published, and its
+// products with the CTA's later blocks from the internal L blocks, which
+// were staged in shared memory before phase A.  Only ceil(nblk / R)
+// hand-offs between CTAs remain on the critical path.
+constexpr int CH_R = 4;
+
+template <class T>
+__global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long long ld, int N,
+                                                  const double* __restrict__ b, double* __restrict__ y,
+                                                  const double* __restrict__ Dinv, const float2* __restrict__ Dinv2,
+                                                  int lower, unsigned* progress, int* err,
+                                                  unsigned long long wait_ns, unsigned stall) {
+  extern __shared__ __align__(16) unsigned char ch_raw[];
+  T* Lin = reinterpret_cast<T*>(ch_raw);  // internal blocks (r2, r1), r1 < r2: column-major 64 x 64
+  __shared__ double part[4][TB];
+  __shared__ float vh[TB], vl[TB];
+  __shared__ double vd[TB];
+  __shared__ double xs[TB];
+  __shared__ int s_abort;
+  const int nblk = (N + TB - 1) / TB;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int q = warp & 3, h = warp >> 2;
+  const int rr = h * 32 + lane;
+  const int c0 = q * 16;
+  const int p0 = blockIdx.x * CH_R;
+  const int np = (nblk - p0 < CH_R) ? nblk - p0 : CH_R;
+  auto blk = [&](int pos) { return lower ? pos : nblk - 1 - pos; };
+  auto tri = [](int r2, int r1) { return r2 * (r2 - 1) / 2 + r1; };  // index of block (r2, r1), r1 < r2
+  if (tid == 0) s_abort = 0;
+  // stage the internal blocks: rows of position p0 + r2, columns of p0 + r1
+  for (int r2 = 1; r2 < np; r2++)
+    for (int r1 = 0; r1 < r2; r1++) {
+      const int kr = blk(p0 + r2), kc = blk(p0 + r1);
+      T* dst = Lin + static_cast<size_t>(tri(r2, r1)) * TB * TB;
+      for (int e = tid; e < TB * TB; e += 256) {
+        const int i = e % TB, j = e / TB;
+        const int row = kr * TB + i, col = kc * TB + j;
+        dst[j * TB + i] = (row < N && col < N) ? A[static_cast<long long>(col) * ld + row] : T(0);
+      }
+    }
+  __syncthreads();
+  double acc[CH_R];
+#pragma unroll
+  for (int r = 0; r < CH_R; r++) acc[r] = 0.0;
+  // phase A: the finished blocks of earlier CTAs.  With FP32 factors the L
+  // tile of the next block is loaded while the current one is used (it
+  // does not depend on x), so the factor's HBM latency overlaps the
+  // progress waits and the x loads.
+  unsigned avail = 0;
+  bool ok = true;
+  constexpr bool kAhead = sizeof(T) == 4;  // FP64 tiles would not fit twice in registers
+  T a[CH_R][16], an[kAhead ? CH_R : 1][16];
+  auto load_tile = [&](int pi, T(&dst)[CH_R][16]) {
+    const int cb = blk(pi) * TB + c0;
+#pragma unroll
+    for (int r = 0; r < CH_R; r++) {
+      const int row = blk(p0 + r) * TB + rr;
+      const bool live = r < np && row < N;
+#pragma unroll
+      for (int j = 0; j < 16; j++)
+        dst[r][j] = (live && cb + j < N) ? A[static_cast<long long>(cb + j) * ld + row] : T(0);
+    }
+  };
+  if constexpr (kAhead) {
+    if (p0 > 0) load_tile(0, an);
+  }
+  for (int pi = 0; pi < p0; pi++) {
+    const int cb = blk(pi) * TB + c0;
+    if constexpr (kAhead) {
+#pragma unroll
+      for (int r = 0; r < CH_R; r++)
+#pragma unroll
+        for (int j = 0; j < 16; j++) a[r][j] = an[r][j];
+      if (pi + 1 < p0) load_tile(pi + 1, an);
+    } else {
+      load_tile(pi, a);
+    }
+    if (static_cast<unsigned>(pi) >= avail) {
+      const unsigned v = wait_progress(progress, static_cast<unsigned>(pi) + 1 + stall, wait_ns);
+      if (v == 0) {
+        ok = false;
+        break;
+      }
+      avail = v - stall;  // positions known finished
+    }
+    T xq[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) xq[j] = static_cast<T>((cb + j < N) ? __ldcg(y + cb + j) : 0.0);
+#pragma unroll
+    for (int r = 0; r < CH_R; r++) {
+      T sum = T(0);
+#pragma unroll
+      for (int j = 0; j < 16; j++) sum = fma(a[r][j], xq[j], sum);
+      acc[r] += static_cast<double>(sum);
+    }
+  }
+  if (!ok) s_abort = 1;
+  // phase B: this CTA's own blocks, chained in shared memory
+#pragma unroll
+  for (int r = 0; r < CH_R; r++) {
+    if (r >= np) break;
+    const int k = blk(p0 + r);
+    const int r0 = k * TB;
+    const int n = (N - r0 < TB) ? N - r0 : TB;
+    part[q][rr] = acc[r];
+    __syncthreads();
+    if (s_abort) {
+      if (tid == 0) atomicExch(err, 1);
+      return;
+    }
+    if (tid < TB) {
+      const double v = (tid < n) ? b[r0 + tid] - ((part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]))
+                                 : 0.0;
+      vd[tid] = v;
+      const float hv = static_cast<float>(v);
+      vh[tid] = hv;
+      vl[tid] = static_cast<float>(v - static_cast<double>(hv));
+    }
+    __syncthreads();
+    const size_t dofs = static_cast<size_t>(k) * TB * TB + static_cast<size_t>(warp) * 8 * TB;
+    if constexpr (std::is_same<T, float>::value) {
+      const float b0h = vh[lane], b0l = vl[lane], b1h = vh[lane + 32], b1l = vl[lane + 32];
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        const float2 dl = Dinv2[dofs + j * TB + lane], dh = Dinv2[dofs + j * TB + lane + 32];
+        DF pr = df_add(df_mul(dl.x, dl.y, b0h, b0l), df_mul(dh.x, dh.y, b1h, b1l));
+        for (int o = 16; o > 0; o >>= 1) {
+          DF t;
+          t.h = __shfl_xor_sync(0xffffffffu, pr.h, o);
+          t.l = __shfl_xor_sync(0xffffffffu, pr.l, o);
+          pr = df_add(pr, t);
+        }
+        const int xr = warp * 8 + j;
+        if (lane == 0) {
+          const double x = (xr < n) ? static_cast<double>(pr.h) + static_cast<double>(pr.l) : 0.0;
+          xs[xr] = x;
+          if (xr < n) y[r0 + xr] = x;
+        }
+      }
+    } else {
+      const double b0 = vd[lane], b1 = vd[lane + 32];
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        double pr = Dinv[dofs + j * TB + lane] * b0 + Dinv[dofs + j * TB + lane + 32] * b1;
+        for (int o = 16; o > 0; o >>= 1) pr += __shfl_xor_sync(0xffffffffu, pr, o);
+        const int xr = warp * 8 + j;
+        if (lane == 0) {
+          const double x = (xr < n) ? pr : 0.0;
+          xs[xr] = x;
+          if (xr < n) y[r0 + xr] = x;
+        }
+      }
+    }
+    __syncthreads();
+    if (tid == 0) {
+      __threadfence();
+      asm volatile("red.release.gpu.global.max.u32 [%0], %1;" ::"l"(progress), "r"(static_cast<unsigned>(p0 + r) + 1)
+                   : "memory");
+    }
+    // products of the later own blocks with x_p
+#pragma unroll
+    for (int r2 = r + 1; r2 < CH_R; r2++) {
+      if (r2 >= np) break;
+      const T* L = Lin + static_cast<size_t>(tri(r2, r)) * TB * TB;
+      T sum = T(0);
+#pragma unroll
+      for (int j = 0; j < 16; j++) sum = fma(L[(c0 + j) * TB + rr], static_cast<T>(xs[c0 + j]), sum);
+      acc[r2] += static_cast<double>(sum);
     }
   }
 }
@@ -2203,7 +2377,28 @@ void DenseLU::tri_solve(const T* LU, long long ld, int N, double* b, int trans) 
     const float2* du2 = std::is_same<T, float>::value ? dinv2_u_ : nullptr;
     const unsigned long long wait = ctx_->grid_wait_ns;
     const unsigned stall = ctx_->stall_waits ? 1u : 0u;
-    if (pull_sweeps) {
+    const int gch = (nblk + CH_R - 1) / CH_R;
+    if (sweep_kind == 2 && gch <= ctx_->sms()) {
+      static std::once_flag ch_attr;
+      std::call_once(ch_attr, [] {
+        cuda_check(cudaFuncSetAttribute(trsv_chain<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        static_cast<int>(CH_R * (CH_R - 1) / 2 * TB * TB * sizeof(float))),
+                   "cudaFuncSetAttribute(chain sweep)");
+        cuda_check(cudaFuncSetAttribute(trsv_chain<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        static_cast<int>(CH_R * (CH_R - 1) / 2 * TB * TB * sizeof(double))),
+                   "cudaFuncSetAttribute(chain sweep)");
+      });
+      cfg.gridDim = dim3(gch, 1, 1);
+      cfg.dynamicSmemBytes = static_cast<size_t>(CH_R * (CH_R - 1) / 2) * TB * TB * sizeof(T);
+      const double* w1c = w1;
+      const double* w2c = w2;
+      cuda_check(cudaLaunchKernelEx(&cfg, trsv_chain<T>, LU, ld, N, w1c, w2, dl, dl2, 1, tri_bar_, panel_err_, wait,
+                                    stall),
+                 "forward sweep");
+      cuda_check(cudaLaunchKernelEx(&cfg, trsv_chain<T>, LU, ld, N, w2c, b, du, du2, 0, tri_bar_ + 1, panel_err_,
+                                    wait, stall),
+                 "backward sweep");
+    } else if (sweep_kind == 1) {
       int gp = nblk < ctx_->sms() ? nblk : ctx_->sms();
       cfg.gridDim = dim3(gp, 1, 1);
       const double* w1c = w1;

@@ -60,9 +60,10 @@ class DenseLU {
   // partial pivoting; when it needs more than 4 iterations beyond the
   // pivoted factors' count, the next factorisation pivots again.
   bool reuse_pivots = false;
-  // Triangular sweeps that pull finished blocks through a progress counter
-  // (true) or step with one grid barrier per 64-row block (false).
-  bool pull_sweeps = true;
+  // Triangular sweeps: 2 = four consecutive 64-row blocks per CTA chained
+  // in shared memory, finished blocks pulled through a progress counter;
+  // 1 = one block per CTA, pulled; 0 = one grid barrier per block.
+  int sweep_kind = 2;
   // Forgets the pivot order: the next factorisation pivots.
   void forget_pivots() { perm_n_ = 0; }
 
