@@ -149,6 +149,10 @@ int kd_coef_host_noalloc(kd_ctx* ctx, const kd_transform_desc* desc);
 #define KD_OP_DIV_XM1 10   /* src/Ope_1d/div_xm1_1d.cpp */
 #define KD_OP_DIV_XP1 11   /* src/Ope_1d/div_xp1_1d.cpp */
 #define KD_OP_DIV_1MX2 12  /* src/Ope_1d/div_1mx2.cpp */
+/* Coefficients -> values at the n_out collocation points of the basis's own
+ * grid (Base_spectral::summation, src/Ope_1d/summation_1d.cpp, at those
+ * points); the 1-D step of kd_field_regrid.  kd_matrix_1d only. */
+#define KD_OP_RESAMPLE 14
 int kd_ope_1d(kd_ctx* ctx, int op, int dim, const kd_transform_desc* desc, int* base_out_r,
               int* base_out_t, int* base_out_p);
 
@@ -356,6 +360,25 @@ typedef struct kd_newton_report {
  * include/system_of_eqs.hpp:871).  Returns KD_OK and fills rep; the fields
  * registered with add_var are updated in place on the device. */
 int kd_newton_step(kd_system* s, const kd_newton_opts* opts, kd_newton_report* rep);
+/* One stage of a FUKA solver (the stage loops of
+ * include/Solvers/ns_3d_xcts/ns_3d_xcts_stages.cpp, e.g. norot_stage :141-165,
+ * and check_max_iter_exceeded in include/Solvers/solvers.hpp): Newton steps
+ * (kd_newton_step with opts) until the pre-step error is below
+ * opts->precision.  After every update, and once more at the end, the
+ * space and the nfields scalars are written to `checkpoint` (NULL: no file)
+ * in Kadath's save format (Space::save, then Scalar::save each).  More than
+ * max_iter updates: accepted when the last error is below 10 precision,
+ * else KD_ERR_NOCONV.  iterations/error (nullable): updates made and the
+ * last pre-step error. */
+int kd_stage_solve(kd_system* s, const kd_newton_opts* opts, int max_iter, const char* checkpoint, int nfields,
+                   kd_field* const* fields, int* iterations, double* error);
+/* The regrid of the FUKA solvers (include/Solvers/ns_3d_xcts/ns_3d_xcts_regrid.hpp):
+ * dst = src evaluated at the collocation points of dst's space, which must
+ * have the same domains as src's (kinds and radii) at any resolution; on the
+ * GPU, as three separable passes from src's coefficients (the summation of
+ * Base_spectral::summation at the new points).  dst gets the standard or
+ * anti-symmetric basis, as src has. */
+int kd_field_regrid(kd_field* dst, kd_field* src);
 /* Forgets the pivot order kept for static pivoting: the next mixed-precision
  * step factors with partial pivoting (no reference counterpart). */
 int kd_system_reset_pivot_order(kd_system* s);

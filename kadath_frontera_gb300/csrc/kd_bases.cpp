@@ -1024,8 +1024,41 @@ const char* basis_name(int b) {
 const char* op_name(int op) {
   static const char* names[] = {"coef",   "coef_i", "der",      "mult_sin", "div_sin",
                                 "mult_cos", "div_cos", "mult_x", "div_x",    "mult_xm1",
-                                "div_xm1", "div_xp1", "div_1mx2", "identity"};
+                                "div_xm1", "div_xp1", "div_1mx2", "identity", "resample"};
   return (op >= 0 && op < OP_COUNT) ? names[op] : "?";
+}
+
+// The n collocation points of a line of the given basis in the spherical
+// domains (Domain_*::do_coloc): Chebyshev x = -cos(pi i/(n-1)), the
+// nucleus's half grid x = sin(pi/2 i/(n-1)), theta on the half sphere
+// pi/2 j/(n-1) (on the full range pi j/(n-1) for COS/SIN) and phi 2 pi k/n.
+static double grid_point(int basis, int i, int n) {
+  const double pi = 3.14159265358979323846;
+  switch (basis) {
+    case CHEB: return n > 1 ? -std::cos(pi * i / (n - 1)) : 0.0;
+    case CHEB_EVEN:
+    case CHEB_ODD: return n > 1 ? std::sin(pi / 2. * i / (n - 1)) : 0.0;
+    case COS_EVEN:
+    case COS_ODD:
+    case SIN_EVEN:
+    case SIN_ODD: return n > 1 ? pi / 2. * i / (n - 1) : 0.0;
+    case COS:
+    case SIN: return n > 1 ? pi * i / (n - 1) : 0.0;
+    default: return 2. * pi * i / n;  // COSSIN, COSSIN_EVEN, COSSIN_ODD
+  }
+}
+
+static int resample_line(int basis, std::vector<double>& tab, int n_in, int n_out) {
+  std::vector<double> w(n_in), out(n_out, 0.0);
+  for (int r = 0; r < n_out; r++) {
+    if (!summation_weights_1d(basis, n_in, grid_point(basis, r, n_out), w.data())) return -1;
+    double v = 0.0;
+    for (int c = 0; c < n_in; c++) v += w[c] * tab[c];
+    out[r] = v;
+  }
+  for (int r = 0; r < n_out; r++) tab[r] = out[r];
+  for (size_t r = n_out; r < tab.size(); r++) tab[r] = 0.0;
+  return basis;
 }
 
 int apply_1d(int op, int basis, std::vector<double>& tab, int n_in, int n_out) {
@@ -1046,6 +1079,7 @@ int apply_1d(int op, int basis, std::vector<double>& tab, int n_in, int n_out) {
     case OP_DIV_XP1: return div_xp1_line(basis, tab, n);
     case OP_DIV_1MX2: return div_1mx2_line(basis, tab, n);
     case OP_IDENTITY: return basis;
+    case OP_RESAMPLE: return resample_line(basis, tab, n_in, n_out);
     default: return -1;
   }
 }

@@ -52,7 +52,11 @@ enum Op1d : int {
   OP_DIV_XP1 = 11,
   OP_DIV_1MX2 = 12,
   OP_IDENTITY = 13,
-  OP_COUNT = 14,
+  // Coefficients of n_in terms -> values at the n_out standard collocation
+  // points of the basis's grid (Scalar::val_point at those points, as the
+  // FUKA regrid does it): the rows are summation_weights_1d there.
+  OP_RESAMPLE = 14,
+  OP_COUNT = 15,
 };
 
 const char* basis_name(int b);

@@ -11,6 +11,7 @@
 #include "kd_context.hpp"
 #include "kd_noalloc.hpp"
 #include "kd_spectral.hpp"
+#include "kd_stages.hpp"
 
 struct kd_ctx {
   std::unique_ptr<kd::Context> c;
@@ -762,6 +763,30 @@ int kd_newton_step(kd_system* s, const kd_newton_opts* opts, kd_newton_report* r
     s->newton->step(to_opts(opts), r);
     to_report(r, rep);
   });
+}
+
+int kd_stage_solve(kd_system* s, const kd_newton_opts* opts, int max_iter, const char* checkpoint, int nfields,
+                   kd_field* const* fields, int* iterations, double* error) {
+  SYS_GUARD(s) {
+    if (!opts || max_iter < 1 || nfields < 0 || (nfields > 0 && !fields))
+      throw kd::KdError(KD_ERR_ARG, "bad stage arguments");
+    std::vector<kd::Field*> fl;
+    for (int i = 0; i < nfields; i++) {
+      if (!fields[i] || fields[i]->sp != s->sp)
+        throw kd::KdError(KD_ERR_ARG, "checkpoint fields must be on the system's space");
+      fl.push_back(fields[i]->f.get());
+    }
+    int it = 0;
+    double err = 0.0;
+    kd::stage_solve(*s->sys, *s->newton, to_opts(opts), max_iter, checkpoint, fl, it, err);
+    if (iterations) *iterations = it;
+    if (error) *error = err;
+  });
+}
+
+int kd_field_regrid(kd_field* dst, kd_field* src) {
+  if (!dst || !src) return KD_ERR_ARG;
+  return guarded(dst->sp->ctx, [&] { kd::regrid(*dst->f, *src->f); });
 }
 
 int kd_system_reset_pivot_order(kd_system* s) {

@@ -102,6 +102,32 @@ std::vector<LinePassSpec> coef_i_specs(Context& ctx, const Base& base, const int
   return v;
 }
 
+std::vector<LinePassSpec> resample_specs(Context& ctx, const Base& base, const int nc_old[3], const int np_new[3]) {
+  if (!base.def) throw KdError(KD_ERR_STATE, "Base not defined in the resampling");
+  std::vector<LinePassSpec> v(3);
+  v[0].dim = 0;
+  v[0].n_in = nc_old[0];
+  v[0].n_out = np_new[0];
+  v[0].mat_ld = nc_old[2];
+  v[0].offsets.resize(static_cast<size_t>(nc_old[1]) * nc_old[2]);
+  for (int j = 0; j < nc_old[1]; j++)
+    for (int k = 0; k < nc_old[2]; k++)
+      v[0].offsets[j * nc_old[2] + k] = mat_offset(ctx, OP_RESAMPLE, base.rb(j, k), nc_old[0], np_new[0], nullptr);
+  v[1].dim = 1;
+  v[1].n_in = nc_old[1];
+  v[1].n_out = np_new[1];
+  v[1].mat_ld = 0;
+  v[1].offsets.resize(nc_old[2]);
+  for (int k = 0; k < nc_old[2]; k++)
+    v[1].offsets[k] = mat_offset(ctx, OP_RESAMPLE, base.t[k], nc_old[1], np_new[1], nullptr);
+  v[2].dim = 2;
+  v[2].n_in = nc_old[2];
+  v[2].n_out = np_new[2];
+  v[2].mat_ld = 0;
+  v[2].offsets = {mat_offset(ctx, OP_RESAMPLE, base.p, nc_old[2], np_new[2], nullptr)};
+  return v;
+}
+
 KdItem make_item(Context& ctx, const std::vector<LinePassSpec>& specs, const double* in, double* out,
                  const int dims_in[3], long long in_stride, long long out_stride, double scale) {
   KdItem it{};

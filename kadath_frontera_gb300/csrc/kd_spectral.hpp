@@ -45,6 +45,11 @@ LinePassSpec ope_1d_spec(Context& ctx, int op, int dim, const Base& base, const 
 std::vector<LinePassSpec> coef_specs(Context& ctx, const Base& base, const int np[3], const int nc[3]);
 std::vector<LinePassSpec> coef_i_specs(Context& ctx, const Base& base, const int np[3], const int nc[3]);
 
+// Pass list of the evaluation of a field given by coefficients (dims
+// nc_old) at the collocation points of another resolution (np_new) of the
+// same domain: r, theta, then phi, each line through OP_RESAMPLE.
+std::vector<LinePassSpec> resample_specs(Context& ctx, const Base& base, const int nc_old[3], const int np_new[3]);
+
 // Turns pass specs into a kernel item (device tables resolved through ctx).
 KdItem make_item(Context& ctx, const std::vector<LinePassSpec>& specs, const double* in, double* out,
                  const int dims_in[3], long long in_stride, long long out_stride, double scale);

@@ -109,6 +109,8 @@ def _declare_system(lib):
         "kd_system_update": (I, [P, DP]),
         "kd_newton_step": (I, [P, C.POINTER(NewtonOpts), C.POINTER(NewtonReport)]),
         "kd_system_reset_pivot_order": (I, [P]),
+        "kd_stage_solve": (I, [P, C.POINTER(NewtonOpts), I, C.c_char_p, I, C.POINTER(P), IP, DP]),
+        "kd_field_regrid": (I, [P, P]),
         "kd_newton_step_gauss_newton": (I, [P, C.POINTER(NewtonOpts), C.POINTER(NewtonReport)]),
         "kd_newton_step_linesearch": (I, [P, C.POINTER(NewtonOpts), I, D, C.POINTER(NewtonReport), DP]),
         "kd_system_set_cst": (I, [P, C.c_char_p, D]),
@@ -350,6 +352,14 @@ class Scalar:
     def save(self, f: "KadathFile"):
         """Scalar::save."""
         self.space.ctx.check(_L().kd_field_save(self.h, f.h))
+
+    def regrid_from(self, src: "Scalar"):
+        """This field = src evaluated at the collocation points of this
+        field's space (same domains, other resolution): the FUKA regrid,
+        on the GPU.  The basis follows src's kind (standard or
+        anti-symmetric)."""
+        self.space.ctx.check(_L().kd_field_regrid(self.h, src.h))
+        return self
 
     def std_base_cart(self, c):
         """Basis of the Cartesian component c = 1, 2, 3 (x, y, z) of a vector."""
@@ -656,6 +666,23 @@ class System_of_eqs:
         self.last_report = rep.as_dict()
         self._J = None
         return bool(rep.converged), rep.error
+
+    def stage_solve(self, precision, max_iter=20, checkpoint=None, fields=(), lu_mode=None, gmres_tol=1e-14,
+                    max_refine=50):
+        """One stage of a FUKA solver: do_newton until converged, the space
+        and `fields` (Scalars) written to `checkpoint` after every update and
+        at the end.  Returns (updates made, last pre-step error)."""
+        opts = NewtonOpts(precision, self.lu_mode if lu_mode is None else lu_mode, gmres_tol, max_refine,
+                          1 if self.graph_capture else 0, 4, 0)
+        handles = [f.h.value if isinstance(f.h, C.c_void_p) else f.h for f in fields]
+        arr = (C.c_void_p * max(len(handles), 1))(*handles)
+        it = C.c_int()
+        err = C.c_double()
+        path = str(checkpoint).encode() if checkpoint else None
+        self.ctx.check(_L().kd_stage_solve(self.h, C.byref(opts), int(max_iter), path, len(handles),
+                                           C.cast(arr, C.POINTER(C.c_void_p)), C.byref(it), C.byref(err)))
+        self._J = None
+        return it.value, err.value
 
     def reset_pivot_order(self):
         """The next mixed-precision step factors with partial pivoting."""

@@ -119,3 +119,48 @@ def test_product_matrices_match_the_reference():
         checked += 1
     print(f"{checked} of {len(cases)} reference matrices checked")
     assert checked >= 0.8 * len(cases)
+
+
+def _grid(base, n):
+    if base == S.CHEB:
+        return [-np.cos(np.pi * i / (n - 1)) for i in range(n)]
+    if base in (S.CHEB_EVEN, S.CHEB_ODD):
+        return [np.sin(np.pi / 2 * i / (n - 1)) for i in range(n)]
+    if base in (S.COS_EVEN, S.COS_ODD, S.SIN_EVEN, S.SIN_ODD):
+        return [np.pi / 2 * i / (n - 1) for i in range(n)]
+    return [2 * np.pi * k / n for k in range(n)]
+
+
+RESAMPLE_OP = 14  # KD_OP_RESAMPLE
+
+
+@pytest.mark.parametrize("base", RADIAL + THETA + [S.COSSIN])
+@pytest.mark.parametrize("n_in,n_out", [(9, 13), (13, 9), (7, 7), (5, 17)])
+def test_resample_matrix_is_the_reference_summation_at_the_new_grid(base, n_in, n_out):
+    """kd_field_regrid's 1-D step: row r is the oracle's summation_1d (the
+    restatement of src/Ope_1d/summation_1d.cpp) at the r-th point of the
+    n_out-point grid of the basis."""
+    if base == S.COSSIN:
+        n_in, n_out = n_in + 1 - n_in % 2 + 2, n_out + 1 - n_out % 2  # phi: even point counts, 2 more coefs
+    ob, mp = product_matrix(RESAMPLE_OP, base, n_in, n_out)
+    assert ob == base
+    pts = _grid(base, n_out)
+    for c in range(n_in):
+        e = np.zeros(n_in)
+        e[c] = 1.0
+        col = np.array([S.summation_1d(base, x, e) for x in pts])
+        assert np.abs(mp[:, c] - col).max() <= 1e-13 * max(1.0, np.abs(col).max())
+
+
+@pytest.mark.parametrize("base", RADIAL + THETA)
+@pytest.mark.parametrize("n", [5, 9, 13])
+def test_resample_onto_the_same_grid_is_the_inverse_transform(base, n):
+    """On the field's own grid the resampling is coef_i, whose matrices are
+    pinned to the reference (ref_spectral_1d.npz), on every coefficient slot
+    that carries information on that grid (the reference's coef_i ignores
+    the last slot of the odd bases)."""
+    from tests.test_oracle_spectral import active_slots
+    _, mr = product_matrix(RESAMPLE_OP, base, n, n)
+    _, mi = product_matrix(S.OP_COEF_I, base, n, n)
+    act = active_slots(base, n)  # the slots that carry information on the grid
+    assert np.abs(mr[:, act] - mi[:, act]).max() <= 1e-13 * max(1.0, np.abs(mi).max())
