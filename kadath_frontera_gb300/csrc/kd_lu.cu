@@ -63,38 +63,63 @@ __global__ void trsm_unit_lower(T* __restrict__ A, long long ld, int j0, int nbk
   }
 }
 
-// FP32 version for the mixed modes, one thread per column with the column
-// (x, NB values) in registers: L11 (jb x jb, zero-padded to NB) sits
-// row-major in shared memory and every thread reads the same L entry at the
-// same time (broadcast).  Rows past jb hold zeros and stay zero.
-constexpr int TRSM32_NB = 96;
-constexpr int TRSM32_THREADS = 128;
-__global__ void __launch_bounds__(TRSM32_THREADS) trsm_unit_lower_f32(float* __restrict__ A, long long ld, int j0,
-                                                                      int jb, int c0, int c1) {
-  __shared__ __align__(16) float L[TRSM32_NB * TRSM32_NB];
-  for (int e = threadIdx.x; e < TRSM32_NB * TRSM32_NB; e += blockDim.x) {
-    const int i = e % TRSM32_NB, k = e / TRSM32_NB;  // column-major walk: coalesced reads of L11
-    L[i * TRSM32_NB + k] = (i < jb && k < jb && k < i) ? A[static_cast<long long>(j0 + k) * ld + j0 + i] : 0.0f;
+// U12 = L11^-1 A12 (L11 unit lower, jb <= 96) for FP32 factors, 128 columns
+// per CTA.  The CTA's 96 x 128 tile goes through shared memory with
+// coalesced loads and stores; each thread then solves its column in three
+// 32-row chunks held in registers: a chunk first takes off the products with
+// the finished chunks (read back from shared memory), then its own 32 x 32
+// triangle.  The loops over finished rows stay rolled, so the code fits the
+// instruction cache (a fully unrolled 96 x 96 substitution does not).
+constexpr int TC_THREADS = 128;
+constexpr int TC_LDL = 97;   // row stride of L11 in shared memory
+constexpr int TC_LDX = 129;  // row stride of the column tile
+constexpr size_t TC_SMEM = sizeof(float) * (96 * TC_LDL + 96 * TC_LDX);
+__global__ void __launch_bounds__(TC_THREADS) trsm_chunk_f32(float* __restrict__ A, long long ld, int j0, int jb,
+                                                             int c0, int c1) {
+  extern __shared__ __align__(16) float tc_sm[];
+  float* L = tc_sm;                // L[i * TC_LDL + k], strictly lower part, zero elsewhere
+  float* X = tc_sm + 96 * TC_LDL;  // X[i * TC_LDX + c]
+  const int tid = threadIdx.x;
+  const int cb = c0 + blockIdx.x * TC_THREADS;
+  for (int e = tid; e < 96 * 96; e += TC_THREADS) {
+    const int i = e % 96, k = e / 96;
+    L[i * TC_LDL + k] = (i < jb && k < i) ? A[static_cast<long long>(j0 + k) * ld + j0 + i] : 0.0f;
+  }
+  for (int e = tid; e < 96 * TC_THREADS; e += TC_THREADS) {
+    const int i = e % 96, c = e / 96;
+    const int col = cb + c;
+    X[i * TC_LDX + c] = (i < jb && col < c1) ? A[static_cast<long long>(col) * ld + j0 + i] : 0.0f;
   }
   __syncthreads();
-  const int col = c0 + blockIdx.x * TRSM32_THREADS + threadIdx.x;
-  if (col >= c1) return;
-  float* xc = A + static_cast<long long>(col) * ld + j0;
-  float x[TRSM32_NB];
 #pragma unroll
-  for (int i = 0; i < TRSM32_NB; i++) x[i] = (i < jb) ? xc[i] : 0.0f;
-  // forward substitution, column by column (right-looking): every index
-  // into x is a compile-time constant, so x stays in registers
+  for (int ch = 0; ch < 3; ch++) {
+    if (ch * 32 >= jb) break;
+    float x[32];
 #pragma unroll
-  for (int k = 0; k < TRSM32_NB - 1; k++) {
-    const float xk = x[k];
+    for (int j = 0; j < 32; j++) x[j] = X[(ch * 32 + j) * TC_LDX + tid];
+    for (int k = 0; k < ch * 32; k++) {
+      const float y = X[k * TC_LDX + tid];
+      const float* lrow = L + ch * 32 * TC_LDL + k;
 #pragma unroll
-    for (int i = 0; i < TRSM32_NB; i++)
-      if (i > k) x[i] = fmaf(-L[i * TRSM32_NB + k], xk, x[i]);
+      for (int j = 0; j < 32; j++) x[j] = fmaf(-lrow[j * TC_LDL], y, x[j]);
+    }
+#pragma unroll
+    for (int kk = 0; kk < 32; kk++) {
+      const float y = x[kk];
+      const float* lrow = L + ch * 32 * TC_LDL + ch * 32 + kk;
+#pragma unroll
+      for (int j = 0; j < 32; j++)
+        if (j > kk) x[j] = fmaf(-lrow[j * TC_LDL], y, x[j]);
+    }
+#pragma unroll
+    for (int j = 0; j < 32; j++) X[(ch * 32 + j) * TC_LDX + tid] = x[j];
   }
-#pragma unroll
-  for (int i = 0; i < TRSM32_NB; i++)
-    if (i < jb) xc[i] = x[i];
+  __syncthreads();
+  for (int e = tid; e < 96 * TC_THREADS; e += TC_THREADS) {
+    const int i = e % 96, c = e / 96;
+    const int col = cb + c;
+    if (i < jb && col < c1) A[static_cast<long long>(col) * ld + j0 + i] = X[i * TC_LDX + c];
+  }
 }
 
 // ---- equilibration of the FP32 working copy (mixed modes) --------------
@@ -1275,15 +1300,40 @@ __global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long 
   bool ok = true;
   constexpr bool kAhead = sizeof(T) == 4;  // FP64 tiles would not fit twice in registers
   T a[CH_R][16], an[kAhead ? CH_R : 1][16];
+  // 16-byte vector loads of x only from an aligned y (callers pass offset
+  // vectors, e.g. a work vector at an odd offset N)
+  const bool y_aligned = (reinterpret_cast<unsigned long long>(y) & 15ull) == 0;
+  // rows of this thread in its CTA's blocks (N when past the matrix)
+  int rowof[CH_R];
+#pragma unroll
+  for (int r = 0; r < CH_R; r++) {
+    const int row = blk(p0 + r) * TB + rr;
+    rowof[r] = (r < np && row < N) ? row : N;
+  }
   auto load_tile = [&](int pi, T(&dst)[CH_R][16]) {
     const int cb = blk(pi) * TB + c0;
+    const T* colp = A + static_cast<long long>(cb) * ld;
+    if (cb + 16 <= N) {  // whole column quarter inside the matrix: no column predicates
 #pragma unroll
-    for (int r = 0; r < CH_R; r++) {
-      const int row = blk(p0 + r) * TB + rr;
-      const bool live = r < np && row < N;
+      for (int r = 0; r < CH_R; r++) {
+        if (rowof[r] < N) {
+          const T* q = colp + rowof[r];
 #pragma unroll
-      for (int j = 0; j < 16; j++)
-        dst[r][j] = (live && cb + j < N) ? A[static_cast<long long>(cb + j) * ld + row] : T(0);
+          for (int j = 0; j < 16; j++) {
+            dst[r][j] = *q;
+            q += ld;
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < 16; j++) dst[r][j] = T(0);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int r = 0; r < CH_R; r++)
+#pragma unroll
+        for (int j = 0; j < 16; j++)
+          dst[r][j] = (rowof[r] < N && cb + j < N) ? colp[static_cast<long long>(j) * ld + rowof[r]] : T(0);
     }
   };
   if constexpr (kAhead) {
@@ -1309,8 +1359,18 @@ __global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long 
       avail = v - stall;  // positions known finished
     }
     T xq[16];
+    if (y_aligned && cb + 16 <= N) {  // y + cb is then 16-byte aligned (cb is a multiple of 16)
+      const double2* y2 = reinterpret_cast<const double2*>(y + cb);
 #pragma unroll
-    for (int j = 0; j < 16; j++) xq[j] = static_cast<T>((cb + j < N) ? __ldcg(y + cb + j) : 0.0);
+      for (int j = 0; j < 8; j++) {
+        const double2 v = __ldcg(y2 + j);
+        xq[2 * j] = static_cast<T>(v.x);
+        xq[2 * j + 1] = static_cast<T>(v.y);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 16; j++) xq[j] = static_cast<T>((cb + j < N) ? __ldcg(y + cb + j) : 0.0);
+    }
 #pragma unroll
     for (int r = 0; r < CH_R; r++) {
       T sum = T(0);
@@ -2080,6 +2140,18 @@ static bool panel_factor(Context* ctx, T* A, long long ld, int N, int j0, int jb
   return false;
 }
 
+static void launch_trsm_chunk(Context* ctx, float* A, long long ld, int j0, int jb, int c0, int c1) {
+  static std::once_flag attr;
+  std::call_once(attr, [] {
+    cuda_check(cudaFuncSetAttribute(trsm_chunk_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(TC_SMEM)),
+               "cudaFuncSetAttribute(trsm)");
+  });
+  trsm_chunk_f32<<<blocks(c1 - c0, TC_THREADS), TC_THREADS, TC_SMEM, ctx->stream()>>>(A, ld, j0, jb, c0, c1);
+  ctx->launches += 1;
+  cuda_check(cudaGetLastError(), "trsm kernel");
+}
+
 template <class T>
 static void trsm_and_swaps(Context* ctx, T* A, long long ld, int N, int j0, int jb, const int* ipiv, int* map,
                            bool map_ready) {
@@ -2099,10 +2171,8 @@ static void trsm_and_swaps(Context* ctx, T* A, long long ld, int N, int j0, int 
     std::call_once(attr_set,
                    [] { cudaFuncSetAttribute(trsm_unit_lower<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); });
     if constexpr (std::is_same<T, float>::value) {
-      if (jb <= TRSM32_NB) {
-        trsm_unit_lower_f32<<<blocks(N - j0 - jb, TRSM32_THREADS), TRSM32_THREADS, 0, s>>>(A, ld, j0, jb, j0 + jb, N);
-        ctx->launches += 1;
-        cuda_check(cudaGetLastError(), "trsm kernel");
+      if (jb <= 96) {
+        launch_trsm_chunk(ctx, A, ld, j0, jb, j0 + jb, N);
         return;
       }
     }
@@ -2209,29 +2279,55 @@ void DenseLU::factor_f32_nopiv(float* A, long long ld, int N, bool tf32) {
   cudaStream_t s = ctx_->stream();
   cuda_check(cudaMemsetAsync(d_info_, 0, sizeof(int), s), "memset info");
   const int NB = NP_NB;
-  for (int j0 = 0; j0 < N; j0 += NB) {
-    const int jb = (N - j0 < NB) ? N - j0 : NB;
+  auto panel = [&](int j0, int jb) {
     const int m = N - j0 - jb;
-    {
-      double fl = 0;
-      for (int j = j0; j < j0 + jb; j++) fl += 2.0 * (N - j - 1) * (j0 + jb - j - 1) + (N - j);
-      ProfScope ps(ctx_, Context::PROF_LU_PANEL, fl);
-      const int grid = m > 0 ? blocks(m, NP_THREADS) : 1;
-      panel_nopiv_kernel<<<grid, NP_THREADS, 0, s>>>(A, ld, N, j0, jb, d_info_);
-      ctx_->launches++;
+    double fl = 0;
+    for (int j = j0; j < j0 + jb; j++) fl += 2.0 * (N - j - 1) * (j0 + jb - j - 1) + (N - j);
+    ProfScope ps(ctx_, Context::PROF_LU_PANEL, fl);
+    const int grid = m > 0 ? blocks(m, NP_THREADS) : 1;
+    panel_nopiv_kernel<<<grid, NP_THREADS, 0, ctx_->stream()>>>(A, ld, N, j0, jb, d_info_);
+    ctx_->launches++;
+  };
+  // Look-ahead (tensor-core update): the next panel's columns are updated
+  // first, then the rest of the trailing update runs on a side stream as
+  // 16-CTA clusters that leave one GPC free, while the next panel is
+  // factored on the main stream; its U12 solve waits for both.
+  const bool lookahead = tf32 && tf32_update_max_clusters16() >= 2;
+  int j0 = 0, jb = (N < NB) ? N : NB;
+  panel(j0, jb);
+  bool side_pending = false;
+  for (;;) {
+    if (side_pending) {
+      ctx_->join();
+      side_pending = false;
     }
+    const int m = N - j0 - jb;
     if (m <= 0) break;
     {
       ProfScope ps(ctx_, Context::PROF_LU_SWAP_TRSM, double(jb) * jb * m);
-      trsm_unit_lower_f32<<<blocks(m, TRSM32_THREADS), TRSM32_THREADS, 0, s>>>(A, ld, j0, jb, j0 + jb, N);
-      ctx_->launches++;
+      launch_trsm_chunk(ctx_, A, ld, j0, jb, j0 + jb, N);
     }
+    const int j0n = j0 + jb, jbn = (N - j0n < NB) ? N - j0n : NB;
     float* A21 = A + static_cast<long long>(j0) * ld + j0 + jb;
     float* A12 = A + static_cast<long long>(j0 + jb) * ld + j0;
     float* A22 = A + static_cast<long long>(j0 + jb) * ld + j0 + jb;
     const int writable = static_cast<int>(ld - j0 - jb);
-    gemm_update_f32(ctx_, blas_, m, m, jb, A21, ld, A12, ld, A22, ld, tf32, writable, tf32_terms);
+    if (lookahead && m > jbn) {
+      gemm_update_f32(ctx_, blas_, m, jbn, jb, A21, ld, A12, ld, A22, ld, tf32, writable, tf32_terms);
+      ctx_->fork(1);
+      ctx_->use(0);
+      gemm_update_f32(ctx_, blas_, m, m - jbn, jb, A21, ld, A12 + static_cast<long long>(jbn) * ld, ld,
+                      A22 + static_cast<long long>(jbn) * ld, ld, tf32, writable, tf32_terms, true);
+      ctx_->use(-1);
+      side_pending = true;
+    } else {
+      gemm_update_f32(ctx_, blas_, m, m, jb, A21, ld, A12, ld, A22, ld, tf32, writable, tf32_terms);
+    }
+    panel(j0n, jbn);
+    j0 = j0n;
+    jb = jbn;
   }
+  if (side_pending) ctx_->join();
   cuda_check(cudaGetLastError(), "static-pivot factorisation");
 }
 
@@ -2354,7 +2450,7 @@ void DenseLU::tri_solve(const T* LU, long long ld, int N, double* b, int trans) 
   ProfScope ps(ctx_, Context::PROF_LU_SOLVE, 2.0 * N * N);
   const int nblk = (N + TB - 1) / TB;
   double* w1 = tri_work_;
-  double* w2 = tri_work_ + N;
+  double* w2 = tri_work_ + ((static_cast<size_t>(N) + 31) / 32) * 32;  // 256-byte aligned second vector
   const size_t bs = static_cast<size_t>(TB) * TB;
   if (!trans) {
     gather_perm<<<blocks(N, 256), 256, 0, s>>>(b, perm_, N, w1);
@@ -2378,7 +2474,9 @@ void DenseLU::tri_solve(const T* LU, long long ld, int N, double* b, int trans) 
     const unsigned long long wait = ctx_->grid_wait_ns;
     const unsigned stall = ctx_->stall_waits ? 1u : 0u;
     const int gch = (nblk + CH_R - 1) / CH_R;
-    if (sweep_kind == 2 && gch <= ctx_->sms()) {
+    // the choice depends on the device only (not on a context's SM budget),
+    // so that concurrent and serial solves sum in the same order
+    if (sweep_kind == 2 && gch <= nsm_) {
       static std::once_flag ch_attr;
       std::call_once(ch_attr, [] {
         cuda_check(cudaFuncSetAttribute(trsv_chain<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -2505,7 +2603,8 @@ void DenseLU::prepare_solves(const T* LU, long long ld, int N, bool keep_perm) {
     cudaFree(perm_);
     cudaFree(tri_work_);
     cuda_check(cudaMalloc(&perm_, sizeof(int) * N), "cudaMalloc(perm)");
-    cuda_check(cudaMalloc(&tri_work_, sizeof(double) * 2 * N), "cudaMalloc(tri work)");
+    cuda_check(cudaMalloc(&tri_work_, sizeof(double) * 2 * (((static_cast<size_t>(N) + 31) / 32) * 32)),
+               "cudaMalloc(tri work)");
     perm_cap_ = N;
   }
   if (!keep_perm) build_perm<<<1, 1, 0, s>>>(ipiv_, N, perm_);
