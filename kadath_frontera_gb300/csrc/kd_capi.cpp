@@ -3,6 +3,7 @@
 #include <cmath>
 #include <cstring>
 #include <algorithm>
+#include <atomic>
 #include <memory>
 #include <string>
 
@@ -13,12 +14,21 @@
 #include "kd_spectral.hpp"
 #include "kd_stages.hpp"
 
+// Handles are reference counted: a space keeps its context alive, and a
+// field or system keeps its space alive, so a caller (or a garbage
+// collector) may destroy them in any order.
 struct kd_ctx {
   std::unique_ptr<kd::Context> c;
   std::string err;
+  std::atomic<int> refs{1};
 };
 
 namespace {
+
+void ctx_retain(kd_ctx* c) { c->refs.fetch_add(1); }
+void ctx_release(kd_ctx* c) {
+  if (c->refs.fetch_sub(1) == 1) delete c;
+}
 
 template <class F>
 int guarded(kd_ctx* ctx, F&& f) {
@@ -137,7 +147,7 @@ int kd_ctx_stall_waits(kd_ctx* ctx, int on) {
 
 int kd_ctx_destroy(kd_ctx* ctx) {
   if (!ctx) return KD_ERR_ARG;
-  delete ctx;
+  ctx_release(ctx);
   return KD_OK;
 }
 
@@ -226,7 +236,19 @@ int kd_matrix_1d(kd_ctx* ctx, int op, int basis, int n_in, int n_out, double* ma
 struct kd_space {
   kd_ctx* ctx;
   std::unique_ptr<kd::Space> sp;
+  std::atomic<int> refs{1};
 };
+
+namespace {
+void space_retain(kd_space* s) { s->refs.fetch_add(1); }
+void space_release(kd_space* s) {
+  if (s->refs.fetch_sub(1) == 1) {
+    kd_ctx* c = s->ctx;
+    delete s;
+    ctx_release(c);
+  }
+}
+}  // namespace
 struct kd_field {
   kd_space* sp;
   std::unique_ptr<kd::Field> f;
@@ -268,6 +290,7 @@ int kd_space_spheric_create(kd_ctx* ctx, const double center[3], const int res[3
     if (res[0] < 3 || res[1] < 2) throw kd::KdError(KD_ERR_ARG, "need nr >= 3 and ntheta >= 2");
     std::vector<double> b(bounds, bounds + nbounds);
     auto* s = new kd_space{ctx, std::make_unique<kd::Space>(center, res, b, withzec != 0)};
+    ctx_retain(ctx);
     *out = s;
   });
 }
@@ -296,7 +319,10 @@ int kd_space_save(const kd_space* sp, kd_file* f) {
 
 int kd_space_load(kd_ctx* ctx, kd_file* f, int withzec, kd_space** out) {
   if (!ctx || !f || f->writing || !out) return KD_ERR_ARG;
-  return guarded(ctx, [&] { *out = new kd_space{ctx, kd::load_space(f->f, withzec != 0)}; });
+  return guarded(ctx, [&] {
+    *out = new kd_space{ctx, kd::load_space(f->f, withzec != 0)};
+    ctx_retain(ctx);
+  });
 }
 
 int kd_field_save(kd_field* fld, kd_file* f) {
@@ -327,7 +353,7 @@ int kd_vector_load(kd_field* fx, kd_field* fy, kd_field* fz, int* type_index, kd
 
 int kd_space_destroy(kd_space* sp) {
   if (!sp) return KD_ERR_ARG;
-  delete sp;
+  space_release(sp);
   return KD_OK;
 }
 
@@ -386,12 +412,15 @@ int kd_field_create(kd_space* sp, kd_field** out) {
   if (!sp || !out) return KD_ERR_ARG;
   return guarded(sp->ctx, [&] {
     *out = new kd_field{sp, std::make_unique<kd::Field>(sp->ctx->c.get(), sp->sp.get())};
+    space_retain(sp);
   });
 }
 
 int kd_field_destroy(kd_field* f) {
   if (!f) return KD_ERR_ARG;
+  kd_space* sp = f->sp;
   delete f;
+  space_release(sp);
   return KD_OK;
 }
 
@@ -453,13 +482,16 @@ int kd_system_create(kd_space* sp, int dom_min, int dom_max, kd_system** out) {
   return guarded(sp->ctx, [&] {
     auto* s = new kd_system{sp, std::make_unique<kd::System>(sp->ctx->c.get(), sp->sp.get(), dom_min, dom_max), nullptr};
     s->newton = std::make_unique<kd::Newton>(s->sys.get());
+    space_retain(sp);
     *out = s;
   });
 }
 
 int kd_system_destroy(kd_system* s) {
   if (!s) return KD_ERR_ARG;
+  kd_space* sp = s->sp;
   delete s;
+  space_release(sp);
   return KD_OK;
 }
 
@@ -953,12 +985,17 @@ int kd_newton_step_linesearch(kd_system* s, const kd_newton_opts* opts, int ntry
 
 int kd_lu_create(kd_ctx* ctx, kd_lu** out) {
   if (!ctx || !ctx->c || !out) return KD_ERR_ARG;
-  return guarded(ctx, [&] { *out = new kd_lu{ctx, std::make_unique<kd::DenseLU>(ctx->c.get())}; });
+  return guarded(ctx, [&] {
+    *out = new kd_lu{ctx, std::make_unique<kd::DenseLU>(ctx->c.get())};
+    ctx_retain(ctx);
+  });
 }
 
 int kd_lu_destroy(kd_lu* lu) {
   if (!lu) return KD_ERR_ARG;
+  kd_ctx* c = lu->ctx;
   delete lu;
+  ctx_release(c);
   return KD_OK;
 }
 

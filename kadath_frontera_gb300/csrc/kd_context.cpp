@@ -80,6 +80,9 @@ Context::~Context() {
   cudaFree(d_pool_);
   for (void* w : ws_) cudaFree(w);
   cudaStreamDestroy(stream_);
+  // teardown reports nothing; its status must not surface as the "last
+  // error" of this thread's next, unrelated launch check
+  cudaGetLastError();
 }
 
 void* Context::workspace(int slot, size_t bytes, bool* fresh) {

@@ -81,14 +81,35 @@ __global__ void __launch_bounds__(TC_THREADS) trsm_chunk_f32(float* __restrict__
   float* X = tc_sm + 96 * TC_LDL;  // X[i * TC_LDX + c]
   const int tid = threadIdx.x;
   const int cb = c0 + blockIdx.x * TC_THREADS;
-  for (int e = tid; e < 96 * 96; e += TC_THREADS) {
-    const int i = e % 96, k = e / 96;
-    L[i * TC_LDL + k] = (i < jb && k < i) ? A[static_cast<long long>(j0 + k) * ld + j0 + i] : 0.0f;
+  // staging: 24 independent loads in flight per thread, then their stores
+  for (int e0 = 0; e0 < 96 * 96; e0 += 24 * TC_THREADS) {
+    float v[24];
+#pragma unroll
+    for (int u = 0; u < 24; u++) {
+      const int e = e0 + u * TC_THREADS + tid;
+      const int i = e % 96, k = e / 96;
+      v[u] = (e < 96 * 96 && i < jb && k < i) ? A[static_cast<long long>(j0 + k) * ld + j0 + i] : 0.0f;
+    }
+#pragma unroll
+    for (int u = 0; u < 24; u++) {
+      const int e = e0 + u * TC_THREADS + tid;
+      if (e < 96 * 96) L[(e % 96) * TC_LDL + e / 96] = v[u];
+    }
   }
-  for (int e = tid; e < 96 * TC_THREADS; e += TC_THREADS) {
-    const int i = e % 96, c = e / 96;
-    const int col = cb + c;
-    X[i * TC_LDX + c] = (i < jb && col < c1) ? A[static_cast<long long>(col) * ld + j0 + i] : 0.0f;
+  for (int e0 = 0; e0 < 96 * TC_THREADS; e0 += 24 * TC_THREADS) {
+    float v[24];
+#pragma unroll
+    for (int u = 0; u < 24; u++) {
+      const int e = e0 + u * TC_THREADS + tid;
+      const int i = e % 96, c = e / 96;
+      const int col = cb + c;
+      v[u] = (i < jb && col < c1) ? A[static_cast<long long>(col) * ld + j0 + i] : 0.0f;
+    }
+#pragma unroll
+    for (int u = 0; u < 24; u++) {
+      const int e = e0 + u * TC_THREADS + tid;
+      X[(e % 96) * TC_LDX + e / 96] = v[u];
+    }
   }
   __syncthreads();
 #pragma unroll
@@ -1252,7 +1273,13 @@ __global__ void __launch_bounds__(256) trsv_pull(const T* __restrict__ A, long l
 // products with the CTA's later blocks from the internal L blocks, which
 // were staged in shared memory before phase A.  Only ceil(nblk / R)
 // hand-offs between CTAs remain on the critical path.
-constexpr int CH_R = 4;
+constexpr int CH_R = 3;
+// dynamic shared memory: the internal L blocks, then Dinv of the own blocks
+// (8 bytes an entry: a (hi, lo) float pair or a double)
+template <class T>
+constexpr size_t chain_smem() {
+  return static_cast<size_t>(CH_R * (CH_R - 1) / 2) * TB * TB * sizeof(T) + static_cast<size_t>(CH_R) * TB * TB * 8;
+}
 
 template <class T>
 __global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long long ld, int N,
@@ -1262,6 +1289,11 @@ __global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long 
                                                   unsigned long long wait_ns, unsigned stall) {
   extern __shared__ __align__(16) unsigned char ch_raw[];
   T* Lin = reinterpret_cast<T*>(ch_raw);  // internal blocks (r2, r1), r1 < r2: column-major 64 x 64
+  // Dinv of the own blocks, row-major 64 x 64 each
+  unsigned char* dsm = ch_raw + static_cast<size_t>(CH_R * (CH_R - 1) / 2) * TB * TB * sizeof(T);
+  float2* D2s = reinterpret_cast<float2*>(dsm);
+  double* Dds = reinterpret_cast<double*>(dsm);
+  __shared__ double bsm[CH_R][TB];
   __shared__ double part[4][TB];
   __shared__ float vh[TB], vl[TB];
   __shared__ double vd[TB];
@@ -1277,17 +1309,48 @@ __global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long 
   auto blk = [&](int pos) { return lower ? pos : nblk - 1 - pos; };
   auto tri = [](int r2, int r1) { return r2 * (r2 - 1) / 2 + r1; };  // index of block (r2, r1), r1 < r2
   if (tid == 0) s_abort = 0;
-  // stage the internal blocks: rows of position p0 + r2, columns of p0 + r1
+  // Stage what the own blocks need besides the x of earlier blocks: the
+  // internal L blocks (rows of position p0 + r2, columns of p0 + r1), the
+  // Dinv blocks and the right-hand side, 16 independent loads in flight
+  // per thread.
   for (int r2 = 1; r2 < np; r2++)
     for (int r1 = 0; r1 < r2; r1++) {
       const int kr = blk(p0 + r2), kc = blk(p0 + r1);
       T* dst = Lin + static_cast<size_t>(tri(r2, r1)) * TB * TB;
-      for (int e = tid; e < TB * TB; e += 256) {
-        const int i = e % TB, j = e / TB;
-        const int row = kr * TB + i, col = kc * TB + j;
-        dst[j * TB + i] = (row < N && col < N) ? A[static_cast<long long>(col) * ld + row] : T(0);
+      for (int e0 = 0; e0 < TB * TB; e0 += 16 * 256) {
+        T v[16];
+#pragma unroll
+        for (int u = 0; u < 16; u++) {
+          const int e = e0 + u * 256 + tid;
+          const int row = kr * TB + e % TB, col = kc * TB + e / TB;
+          v[u] = (row < N && col < N) ? A[static_cast<long long>(col) * ld + row] : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < 16; u++) dst[e0 + u * 256 + tid] = v[u];  // dst[j * TB + i], e = j * TB + i
       }
     }
+  for (int r = 0; r < np; r++) {
+    const size_t src = static_cast<size_t>(blk(p0 + r)) * TB * TB;
+    for (int e0 = 0; e0 < TB * TB; e0 += 16 * 256) {
+      if constexpr (std::is_same<T, float>::value) {
+        float2 v[16];
+#pragma unroll
+        for (int u = 0; u < 16; u++) v[u] = Dinv2[src + e0 + u * 256 + tid];
+#pragma unroll
+        for (int u = 0; u < 16; u++) D2s[static_cast<size_t>(r) * TB * TB + e0 + u * 256 + tid] = v[u];
+      } else {
+        double v[16];
+#pragma unroll
+        for (int u = 0; u < 16; u++) v[u] = Dinv[src + e0 + u * 256 + tid];
+#pragma unroll
+        for (int u = 0; u < 16; u++) Dds[static_cast<size_t>(r) * TB * TB + e0 + u * 256 + tid] = v[u];
+      }
+    }
+    if (tid < TB) {
+      const int row = blk(p0 + r) * TB + tid;
+      bsm[r][tid] = (row < N) ? b[row] : 0.0;
+    }
+  }
   __syncthreads();
   double acc[CH_R];
 #pragma unroll
@@ -1394,7 +1457,7 @@ __global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long 
       return;
     }
     if (tid < TB) {
-      const double v = (tid < n) ? b[r0 + tid] - ((part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]))
+      const double v = (tid < n) ? bsm[r][tid] - ((part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]))
                                  : 0.0;
       vd[tid] = v;
       const float hv = static_cast<float>(v);
@@ -1402,12 +1465,12 @@ __global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long 
       vl[tid] = static_cast<float>(v - static_cast<double>(hv));
     }
     __syncthreads();
-    const size_t dofs = static_cast<size_t>(k) * TB * TB + static_cast<size_t>(warp) * 8 * TB;
+    const size_t dofs = static_cast<size_t>(r) * TB * TB + static_cast<size_t>(warp) * 8 * TB;
     if constexpr (std::is_same<T, float>::value) {
       const float b0h = vh[lane], b0l = vl[lane], b1h = vh[lane + 32], b1l = vl[lane + 32];
 #pragma unroll
       for (int j = 0; j < 8; j++) {
-        const float2 dl = Dinv2[dofs + j * TB + lane], dh = Dinv2[dofs + j * TB + lane + 32];
+        const float2 dl = D2s[dofs + j * TB + lane], dh = D2s[dofs + j * TB + lane + 32];
         DF pr = df_add(df_mul(dl.x, dl.y, b0h, b0l), df_mul(dh.x, dh.y, b1h, b1l));
         for (int o = 16; o > 0; o >>= 1) {
           DF t;
@@ -1426,7 +1489,7 @@ __global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long 
       const double b0 = vd[lane], b1 = vd[lane + 32];
 #pragma unroll
       for (int j = 0; j < 8; j++) {
-        double pr = Dinv[dofs + j * TB + lane] * b0 + Dinv[dofs + j * TB + lane + 32] * b1;
+        double pr = Dds[dofs + j * TB + lane] * b0 + Dds[dofs + j * TB + lane + 32] * b1;
         for (int o = 16; o > 0; o >>= 1) pr += __shfl_xor_sync(0xffffffffu, pr, o);
         const int xr = warp * 8 + j;
         if (lane == 0) {
@@ -2480,14 +2543,14 @@ void DenseLU::tri_solve(const T* LU, long long ld, int N, double* b, int trans) 
       static std::once_flag ch_attr;
       std::call_once(ch_attr, [] {
         cuda_check(cudaFuncSetAttribute(trsv_chain<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        static_cast<int>(CH_R * (CH_R - 1) / 2 * TB * TB * sizeof(float))),
+                                        static_cast<int>(chain_smem<float>())),
                    "cudaFuncSetAttribute(chain sweep)");
         cuda_check(cudaFuncSetAttribute(trsv_chain<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        static_cast<int>(CH_R * (CH_R - 1) / 2 * TB * TB * sizeof(double))),
+                                        static_cast<int>(chain_smem<double>())),
                    "cudaFuncSetAttribute(chain sweep)");
       });
       cfg.gridDim = dim3(gch, 1, 1);
-      cfg.dynamicSmemBytes = static_cast<size_t>(CH_R * (CH_R - 1) / 2) * TB * TB * sizeof(T);
+      cfg.dynamicSmemBytes = chain_smem<T>();
       const double* w1c = w1;
       const double* w2c = w2;
       cuda_check(cudaLaunchKernelEx(&cfg, trsv_chain<T>, LU, ld, N, w1c, w2, dl, dl2, 1, tri_bar_, panel_err_, wait,

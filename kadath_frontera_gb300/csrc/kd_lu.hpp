@@ -60,7 +60,7 @@ class DenseLU {
   // partial pivoting; when it needs more than 4 iterations beyond the
   // pivoted factors' count, the next factorisation pivots again.
   bool reuse_pivots = false;
-  // Triangular sweeps: 2 = four consecutive 64-row blocks per CTA chained
+  // Triangular sweeps: 2 = three consecutive 64-row blocks per CTA chained
   // in shared memory, finished blocks pulled through a progress counter;
   // 1 = one block per CTA, pulled; 0 = one grid barrier per block.
   int sweep_kind = 2;

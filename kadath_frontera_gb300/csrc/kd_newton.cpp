@@ -21,7 +21,7 @@ Newton::~Newton() {
   cudaFree(d_J);
   cudaFree(d_JtJ_);
   cudaFree(d_JtF_);
-  if (blas_) cublasDestroy(blas_);
+  if (blas_) cublasDestroy(blas_);  cudaGetLastError();  // teardown status is not the next launch's error
 }
 
 void Newton::ensure(int N) {

@@ -19,7 +19,7 @@ Field::~Field() {
   for (auto& p : d) {
     cudaFree(p.c);
     cudaFree(p.cf);
-  }
+  }  cudaGetLastError();  // teardown status is not the next launch's error
 }
 
 DVal Field::val(int dom) const {

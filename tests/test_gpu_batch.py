@@ -2,11 +2,13 @@
 nr in {9, ..., 17}) solved concurrently, one context (its own streams and
 workspaces) per instance from a pool of host threads.
 
-The mixed-precision path runs only this library's kernels, whose reductions
-have a fixed order, so concurrent solves give bitwise the fields of
-one-at-a-time solves.  The FP64 path's trailing update is cuBLAS DGEMM,
-which may pick another implementation while several streams are active:
-there the fields agree to rounding (1e-12 of their magnitude)."""
+Concurrent solves reach the fields of one-at-a-time solves to rounding (1e-12
+of their magnitude).  They are not bitwise equal: a context limited to a
+share of the SMs picks its LU panel shape (width, cluster or grid panel)
+from that share, so its first-step factors, and the pivot order the later
+steps reuse, round differently; the FP64 path's trailing update is cuBLAS
+DGEMM, which may pick another implementation while several streams are
+active.  Both paths refine to the FP64 solution of each step."""
 import numpy as np
 import pytest
 
@@ -18,7 +20,7 @@ def _fields(wl):
     return {(nm, d): f.get_coef(d) for nm, f in wl.unknowns for d in range(nd)}
 
 
-def test_concurrent_mixed_solves_match_serial_bitwise(ctx):
+def test_concurrent_mixed_solves_match_serial(ctx):
     from kadath_frontera_gb300 import workloads
     from kadath_frontera_gb300.kadath import KD_LU_TF32_IR
     cfgs = workloads.star_batch_configs(4, seed=3)
@@ -28,7 +30,7 @@ def test_concurrent_mixed_solves_match_serial_bitwise(ctx):
     for a, b in zip(serial, conc):
         fa, fb = _fields(a), _fields(b)
         for key in fa:
-            assert np.array_equal(fa[key], fb[key]), key
+            assert np.linalg.norm(fa[key] - fb[key]) <= 1e-12 * max(np.linalg.norm(fa[key]), 1.0), key
         assert np.abs(b.syst.sec_member()).max() < 1e-10
 
 
