@@ -341,12 +341,15 @@ def run_gpu(args, ws, rank, local):
         return 0
     peaks, peak_kind = load_peaks()
     fp64_tflops = measure_fp64_peak(f"cuda:{local}")
-    top = max(prof["mixed"].items(), key=lambda kv: kv[1]["ms"])
-    cat, st = top
-    roof = roofline_for(cat, st, peaks, peak_kind, N, fp64_tflops)
-    # the tensor-core trailing update, for reference next to the dominant kernel
-    gemm = prof["mixed"].get("lu_gemm")
-    roof_gemm = roofline_for("lu_gemm", gemm, peaks, peak_kind, N) if gemm and gemm["launches"] else None
+    # the dominant kernel: the largest device time of one instrumented solve
+    pm = prof["mixed"]
+    ranked = sorted(((k, v["ms"]) for k, v in pm.items() if v["launches"]), key=lambda kv: -kv[1])
+    dev_total = sum(ms for _, ms in ranked)
+    roof = roofline_for(ranked[0][0], pm[ranked[0][0]], peaks, peak_kind, fp64_tflops)
+    roof["share_of_device_time"] = ranked[0][1] / dev_total if dev_total else None
+    rooflines = {ROOF_KERNELS[k][0]: roofline_for(k, pm[k], peaks, peak_kind, fp64_tflops)
+                 for k in ("lu_solve", "lu_gemm", "lu_panel", "lu_panel_static", "lu_swap_trsm", "transform")
+                 if pm.get(k, {}).get("launches")}
     rep0 = results["mixed"][-1][2][0]
     rep64 = results["fp64"][-1][2][0]
     first_m, later_m = step_split(results["mixed"])
@@ -380,8 +383,9 @@ def run_gpu(args, ws, rank, local):
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches_mixed),
         "kernel_profile_ms": {name: {k: round(v["ms"], 3) for k, v in p.items()} for name, p in prof.items()},
+        "device_time_share": {k: round(ms / dev_total, 4) for k, ms in ranked} if dev_total else None,
         "roofline": roof,
-        "roofline_lu_gemm": roof_gemm,
+        "rooflines": rooflines,
         "fp64_peak_tflops_measured": fp64_tflops,
         "clocks": clk.summary(),
         "batch": batch,
@@ -512,39 +516,62 @@ def measure_fp64_peak(device):
     return 2.0 * n ** 3 / (best * 1e-3) / 1e12
 
 
-def roofline_for(cat, st, peaks, peak_kind, N, fp64_tflops=None):
-    """Roofline of the dominant kernel category of the mixed step, against
-    the resource that bounds it: FP64 arithmetic for the spectral line
-    passes, the tensor pipe for the trailing update, HBM for the rest."""
-    per_launch_ms = st["ms"] / max(st["launches"], 1)
-    work_per_launch = st["work"] / max(st["launches"], 1)
+# The kernel behind each profile category of the mixed-precision step, and
+# the resource that bounds it.  `work` of every category but the transforms
+# is algorithmic bytes (include/kadath_gb300.h, kd_ctx_profile_read).
+ROOF_KERNELS = {
+    "lu_solve": ("trsv_chain<float>", "one triangular sweep over the FP32 factors (forward L or backward U)"),
+    "lu_gemm": ("tf32_update_persistent", "3xTF32 tcgen05 trailing update"),
+    "lu_panel": ("panel_cluster16_kernel", "partial-pivoting panel, one 16-CTA cluster"),
+    "lu_panel_static": ("panel_nopiv_kernel", "static-pivot panel"),
+    "lu_swap_trsm": ("trsm_chunk_f32", "U12 triangular solve (and row swaps after a pivoting panel)"),
+    "refine_matvec": ("gemv_partial", "FP64 refinement matvec b - J x and GMRES vector work"),
+    "elementwise": ("ew_kernel", "pointwise algebra at collocation points"),
+    "tau_gather": ("gather_csr_kernel", "tau / Galerkin row gathers"),
+    "transform": ("line_passes_kernel", "separable spectral transforms and 1-D operators (FP64)"),
+}
+
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) over the
+# algorithmic bytes of one ncu-captured launch of each kernel on the star
+# workload (N = 12,331); the summaries under profiles/ give the launches and
+# the commands.  traffic per launch = ratio x algorithmic bytes per launch.
+NCU_TRAFFIC_RATIO = {
+    "lu_solve": (1.032, "profiles/trsv_chain_star_N12331.md"),
+    "lu_gemm": (0.955, "profiles/tf32_update_persistent_star_N12331.md"),
+    "lu_panel": (0.51, "profiles/panel_cluster16_kernel_star_N12331.md"),
+    "lu_panel_static": (0.51, "profiles/panel_nopiv_kernel_star_N12331.md"),
+}
+
+
+def roofline_for(cat, st, peaks, peak_kind, fp64_tflops=None):
+    """Roofline of one profile category of the mixed step: algorithmic work
+    per launch over the mean launch duration (CUDA events on the launching
+    stream, profile mode), against HBM (measured copy bandwidth) for the
+    byte-bound kernels and against the in-run DGEMM rate for the FP64
+    transforms."""
+    if not st or not st["launches"]:
+        return None
+    kernel, what = ROOF_KERNELS[cat]
+    per_launch_ms = st["ms"] / st["launches"]
+    work_per_launch = st["work"] / st["launches"]
+    out = {"kernel": kernel, "what": what, "launches": st["launches"], "avg_launch_ms": per_launch_ms,
+           "device_ms_per_solve": st["ms"]}
     if cat == "transform":
         achieved = work_per_launch / (per_launch_ms * 1e-3) / 1e12
-        return {"kernel": "line_passes_kernel (transform)", "bound": "fp64", "achieved": achieved,
-                "peak": fp64_tflops, "unit": "TFLOP/s",
-                "frac": (achieved / fp64_tflops) if fp64_tflops else None, "traffic": None,
-                "peak_note": "FP64 DGEMM throughput measured in this run (the transforms are FP64-arithmetic bound "
-                             "on GB300; work = algorithmic FP64 flops of the small-matrix contractions)",
-                "launches": st["launches"], "avg_launch_ms": per_launch_ms}
-    if cat in ("lu_gemm",):
-        # the 3xTF32 trailing update streams C through HBM once per panel:
-        # work = algorithmic bytes (8 m n for C plus 4 (m + n) k operands)
-        achieved = work_per_launch / (per_launch_ms * 1e-3) / 1e9
-        peak = peaks.get("hbm_gbs", PEAKS_FALLBACK["hbm_gbs"])
-        return {"kernel": "tf32_update_persistent (lu_gemm)", "bound": "hbm", "achieved": achieved, "peak": peak,
-                "unit": "GB/s", "frac": achieved / peak, "traffic": None,
-                "peak_note": f"{peak_kind} copy bandwidth; the update is bound by the C stream, its tensor pipe "
-                             "is 16-35% busy (profiles/)",
-                "launches": st["launches"], "avg_launch_ms": per_launch_ms}
-    if cat in ("lu_panel", "lu_swap_trsm", "lu_solve"):
-        achieved = work_per_launch / (per_launch_ms * 1e-3) / 1e12
-        return {"kernel": cat, "bound": "latency", "achieved": achieved, "peak": None, "unit": "TFLOP/s",
-                "frac": None, "traffic": None, "launches": st["launches"], "avg_launch_ms": per_launch_ms}
+        out.update({"bound": "fp64", "achieved": achieved, "peak": fp64_tflops, "unit": "TFLOP/s",
+                    "frac": (achieved / fp64_tflops) if fp64_tflops else None, "traffic": None,
+                    "work_per_launch": work_per_launch,
+                    "peak_note": "FP64 DGEMM throughput measured in this run; work = algorithmic FP64 flops"})
+        return out
     achieved = work_per_launch / (per_launch_ms * 1e-3) / 1e9
     peak = peaks.get("hbm_gbs", PEAKS_FALLBACK["hbm_gbs"])
-    return {"kernel": cat, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "traffic": None, "peak_note": f"{peak_kind} copy bandwidth",
-            "launches": st["launches"], "avg_launch_ms": per_launch_ms}
+    ratio = NCU_TRAFFIC_RATIO.get(cat)
+    out.update({"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "algorithmic_bytes_per_launch": work_per_launch,
+                "traffic": ratio[0] * work_per_launch if ratio else None,
+                "traffic_source": ratio[1] if ratio else None,
+                "peak_note": f"{peak_kind} copy bandwidth (of {peak_kind})"})
+    return out
 
 
 def run_large(args, local):

@@ -69,11 +69,17 @@ int kd_ctx_synchronize(kd_ctx* ctx);
 long long kd_ctx_launch_count(const kd_ctx* ctx);
 /* Kernel timing by category with CUDA events on the context's stream
  * (no reference counterpart: the reference prints wall-clock phase times,
- * src_par/do_newton.cpp:257,333).  Categories: 0 separable transforms and
- * 1-D operators, 1 elementwise, 2 tau gathers, 3 LU panel, 4 LU swaps+TRSM,
- * 5 LU trailing GEMM, 6 triangular solves, 7 refinement matvecs.  `work` is
- * algorithmic bytes (0-2, 7) or flops (3-6). */
-#define KD_PROF_NCAT 8
+ * src_par/do_newton.cpp:257,333).  Categories, with the unit of `work`:
+ * 0 separable transforms and 1-D operators (FP64 flops), 1 elementwise
+ * (bytes), 2 tau gathers (bytes), 3 partial-pivoting LU panels (bytes: the
+ * panel read and written once), 4 LU row swaps + U12 solve (bytes of A12
+ * read and written), 5 LU trailing update (bytes of the tensor-core update;
+ * flops of the FP64 GEMM), 6 one triangular sweep (bytes of the triangle
+ * read), 7 refinement matvecs and vector operations (bytes), 8 static-pivot
+ * LU panels (bytes).  While profiling is on, a short idle kernel is queued
+ * ahead of a timed launch whenever the stream has drained, so each event
+ * pair holds device time only; the residual is then not graph-captured. */
+#define KD_PROF_NCAT 9
 /* The CUDA stream (cudaStream_t) all of this context's work runs on, so a
  * caller can order its own work or record timing events on it. */
 void* kd_ctx_stream(const kd_ctx* ctx);

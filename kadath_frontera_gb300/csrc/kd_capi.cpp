@@ -1087,6 +1087,8 @@ int kd_ctx_profile_enable(kd_ctx* ctx, int on) {
   return guarded(ctx, [&] { ctx->c->prof_enable(on != 0); });
 }
 
+static_assert(KD_PROF_NCAT == kd::Context::PROF_NCAT, "profile categories of the C ABI and the context differ");
+
 int kd_ctx_profile_read(kd_ctx* ctx, double* ms, long long* launches, double* work) {
   if (!ctx || !ctx->c || !ms || !launches || !work) return KD_ERR_ARG;
   return guarded(ctx, [&] { ctx->c->prof_read(ms, launches, work); });

@@ -239,14 +239,36 @@ cudaEvent_t Context::next_event() {
 void Context::prof_enable(bool on) {
   prof_on_ = on;
   prof_.clear();
+  prof_last_.clear();
   ev_next_ = 0;
 }
 
+// An event pair around a launch measures the time between the stream
+// reaching the two events.  When the host issues launches more slowly than
+// the GPU runs them, the stream drains and the pair would also count the
+// wait for the host.  So whenever the last timed launch has already
+// finished, a 200 us hold kernel (outside every pair) goes in first and the
+// following launches queue behind it: the pairs then hold device time only.
 void Context::prof_begin(int cat) {
   (void)cat;
   if (!prof_on_) return;
+  cudaStream_t s = stream();
+  cudaEvent_t last = nullptr;  // end event of the last timed launch on s
+  for (auto& pe : prof_last_)
+    if (pe.first == s) last = pe.second;
+  bool drained = last == nullptr;
+  if (!drained) {
+    const cudaError_t q = cudaEventQuery(last);
+    if (q == cudaErrorNotReady) {
+      (void)cudaGetLastError();  // "not ready" is a status, not an error to keep
+    } else {
+      cuda_check(q, "cudaEventQuery (profile)");
+      drained = true;
+    }
+  }
+  if (drained) cuda_check(launch_hold(200000ull, s), "hold kernel (profile)");
   pending_begin_ = next_event();
-  cuda_check(cudaEventRecord(pending_begin_, stream()), "cudaEventRecord");
+  cuda_check(cudaEventRecord(pending_begin_, s), "cudaEventRecord");
 }
 
 void Context::prof_end(int cat, double work) {
@@ -254,6 +276,13 @@ void Context::prof_end(int cat, double work) {
   cudaEvent_t e = next_event();
   cuda_check(cudaEventRecord(e, stream()), "cudaEventRecord");
   prof_.push_back({cat, pending_begin_, e, work});
+  bool found = false;
+  for (auto& pe : prof_last_)
+    if (pe.first == stream()) {
+      pe.second = e;
+      found = true;
+    }
+  if (!found) prof_last_.push_back({stream(), e});
   pending_begin_ = nullptr;
 }
 

@@ -121,12 +121,13 @@ class Context {
     PROF_LINE_PASS = 0,  // separable transforms / 1-D coefficient operators (work: FP64 flops)
     PROF_EW = 1,         // elementwise algebra at collocation points
     PROF_GATHER = 2,     // tau export / affecte_tau gathers
-    PROF_LU_PANEL = 3,
-    PROF_LU_SWAP_TRSM = 4,
-    PROF_LU_GEMM = 5,    // trailing update (work: HBM bytes of the tensor-core update, flops of the FP64 GEMM)
-    PROF_LU_SOLVE = 6,   // triangular solves
-    PROF_GMRES = 7,      // refinement matvecs and vector ops
-    PROF_NCAT = 8,
+    PROF_LU_PANEL = 3,         // partial-pivoting panels (work: bytes, the panel read and written once)
+    PROF_LU_SWAP_TRSM = 4,     // row exchanges and the U12 solve (work: bytes of A12 read and written)
+    PROF_LU_GEMM = 5,          // trailing update (work: HBM bytes of the tensor-core update, flops of the FP64 GEMM)
+    PROF_LU_SOLVE = 6,         // one triangular sweep (work: bytes of the triangle read)
+    PROF_GMRES = 7,            // refinement matvecs and vector ops
+    PROF_LU_PANEL_STATIC = 8,  // static-pivot panels (work: bytes, the panel read and written once)
+    PROF_NCAT = 9,
   };
   void prof_enable(bool on);
   bool prof_on() const { return prof_on_; }
@@ -146,6 +147,7 @@ class Context {
   };
   std::vector<ProfRec> prof_;
   cudaEvent_t pending_begin_ = nullptr;
+  std::vector<std::pair<cudaStream_t, cudaEvent_t>> prof_last_;
   cudaEvent_t next_event();
 
  public:

@@ -482,6 +482,22 @@ cudaError_t launch_eos(const KdEos& eos, int var, long long npts, const double* 
   return cudaGetLastError();
 }
 
+// One thread that idles for ns nanoseconds (at most 4096 sleeps of ~1 us).
+__global__ void hold_kernel(unsigned long long ns) {
+  unsigned long long t0, t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+  for (int it = 0; it < 4096; it++) {
+    __nanosleep(1000);
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    if (t - t0 >= ns) break;
+  }
+}
+
+cudaError_t launch_hold(unsigned long long ns, cudaStream_t s) {
+  hold_kernel<<<1, 1, 0, s>>>(ns);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_absmax(const double* x, long long n, double* out_scalar, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(out_scalar, 0, sizeof(double), s);
   if (e != cudaSuccess) return e;

@@ -86,6 +86,9 @@ cudaError_t launch_gather_csr(const double* in, long long in_stride, int batch, 
 
 // Sum over the last axis reduction helpers used by residual norms.
 cudaError_t launch_absmax(const double* x, long long n, double* out_scalar, cudaStream_t s);
+// Occupies the stream for about ns nanoseconds (profile mode queues the
+// launches it times behind it, so that their event pairs see no host gaps).
+cudaError_t launch_hold(unsigned long long ns, cudaStream_t s);
 // Cold piecewise polytrope (Margherita Cold_PWPoly, include/EOS/standalone/
 // cold_pwpoly_implementation.hh), geometrised units, tables derived as in
 // Margherita_setup_polytrope (setup_polytrope.cc).

@@ -1267,13 +1267,38 @@ __global__ void __launch_bounds__(256) trsv_pull(const T* __restrict__ A, long l
 
 // The same sweep with CH_R consecutive blocks per CTA: CTA c owns sweep
 // positions c R .. c R + R - 1.  While earlier CTAs work it accumulates, for
-// all its blocks at once, the products with every finished x (phase A, one
-// progress wait per finished block).  Its own blocks then chain inside the
-// CTA (phase B): x_p from the accumulated rows and Dinv, published, and its
-// products with the CTA's later blocks from the internal L blocks, which
-// were staged in shared memory before phase A.  Only ceil(nblk / R)
-// hand-offs between CTAs remain on the critical path.
+// all its blocks at once, the products with every finished x (phase A).  Its
+// own blocks then chain inside the CTA (phase B): x_p from the accumulated
+// rows and Dinv, stored, and its products with the CTA's later blocks from
+// the internal L blocks, which were staged in shared memory before phase A.
+// Only ceil(nblk / R) hand-offs between CTAs remain on the critical path.
+//
+// The x values are their own flags: y is filled with the bit pattern
+// CHAIN_EMPTY (all ones, a NaN that arithmetic does not produce: a NaN
+// result is stored as the positive quiet NaN) before the launch, producers
+// store x with relaxed gpu-scope stores, and consumers poll the 16 entries
+// they need until none is CHAIN_EMPTY.  No fence, counter or second load is
+// on the hand-off; each entry is read as a whole (8-byte single-copy
+// atomicity), and nothing else is exchanged between the CTAs.
 constexpr int CH_R = 3;
+constexpr unsigned long long CHAIN_EMPTY = ~0ull;
+
+__device__ __forceinline__ double ld_relaxed_f64(const double* p) {
+  double v;
+  asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ double2 ld_relaxed_f64x2(const double* p) {
+  double2 v;
+  asm volatile("ld.relaxed.gpu.global.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed_f64(double* p, double v) {
+  asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
+}
+__device__ __forceinline__ bool chain_empty(double v) {
+  return static_cast<unsigned long long>(__double_as_longlong(v)) == CHAIN_EMPTY;
+}
 // dynamic shared memory: the internal L blocks, then Dinv of the own blocks
 // (8 bytes an entry: a (hi, lo) float pair or a double)
 template <class T>
@@ -1285,8 +1310,8 @@ template <class T>
 __global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long long ld, int N,
                                                   const double* __restrict__ b, double* __restrict__ y,
                                                   const double* __restrict__ Dinv, const float2* __restrict__ Dinv2,
-                                                  int lower, unsigned* progress, int* err,
-                                                  unsigned long long wait_ns, unsigned stall) {
+                                                  int lower, int* err, unsigned long long wait_ns,
+                                                  unsigned stall) {
   extern __shared__ __align__(16) unsigned char ch_raw[];
   T* Lin = reinterpret_cast<T*>(ch_raw);  // internal blocks (r2, r1), r1 < r2: column-major 64 x 64
   // Dinv of the own blocks, row-major 64 x 64 each
@@ -1358,8 +1383,7 @@ __global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long 
   // phase A: the finished blocks of earlier CTAs.  With FP32 factors the L
   // tile of the next block is loaded while the current one is used (it
   // does not depend on x), so the factor's HBM latency overlaps the
-  // progress waits and the x loads.
-  unsigned avail = 0;
+  // waits for x.
   bool ok = true;
   constexpr bool kAhead = sizeof(T) == 4;  // FP64 tiles would not fit twice in registers
   T a[CH_R][16], an[kAhead ? CH_R : 1][16];
@@ -1413,27 +1437,40 @@ __global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long 
     } else {
       load_tile(pi, a);
     }
-    if (static_cast<unsigned>(pi) >= avail) {
-      const unsigned v = wait_progress(progress, static_cast<unsigned>(pi) + 1 + stall, wait_ns);
-      if (v == 0) {
-        ok = false;
+    // x of block pi, this thread's 16 columns, polled until all are stored
+    // (a stall request makes every poll fail, for the timeout tests)
+    double xv[16];
+    bool ready = false;
+    unsigned long long t0 = 0;
+    for (unsigned it = 0;; it++) {
+      if (y_aligned && cb + 16 <= N) {  // y + cb is then 16-byte aligned (cb is a multiple of 16)
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          const double2 v = ld_relaxed_f64x2(y + cb + 2 * j);
+          xv[2 * j] = v.x;
+          xv[2 * j + 1] = v.y;
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 16; j++) xv[j] = (cb + j < N) ? ld_relaxed_f64(y + cb + j) : 0.0;
+      }
+      ready = stall == 0;
+#pragma unroll
+      for (int j = 0; j < 16; j++) ready = ready && !chain_empty(xv[j]);
+      if (ready) break;
+      if (it == 0) {
+        t0 = globaltimer_ns();
+      } else if ((it & 15) == 15 && globaltimer_ns() - t0 > wait_ns) {
         break;
       }
-      avail = v - stall;  // positions known finished
+    }
+    if (!ready) {
+      ok = false;
+      break;
     }
     T xq[16];
-    if (y_aligned && cb + 16 <= N) {  // y + cb is then 16-byte aligned (cb is a multiple of 16)
-      const double2* y2 = reinterpret_cast<const double2*>(y + cb);
 #pragma unroll
-      for (int j = 0; j < 8; j++) {
-        const double2 v = __ldcg(y2 + j);
-        xq[2 * j] = static_cast<T>(v.x);
-        xq[2 * j + 1] = static_cast<T>(v.y);
-      }
-    } else {
-#pragma unroll
-      for (int j = 0; j < 16; j++) xq[j] = static_cast<T>((cb + j < N) ? __ldcg(y + cb + j) : 0.0);
-    }
+    for (int j = 0; j < 16; j++) xq[j] = static_cast<T>(xv[j]);
 #pragma unroll
     for (int r = 0; r < CH_R; r++) {
       T sum = T(0);
@@ -1480,9 +1517,10 @@ __global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long 
         }
         const int xr = warp * 8 + j;
         if (lane == 0) {
-          const double x = (xr < n) ? static_cast<double>(pr.h) + static_cast<double>(pr.l) : 0.0;
+          double x = (xr < n) ? static_cast<double>(pr.h) + static_cast<double>(pr.l) : 0.0;
+          if (x != x) x = __longlong_as_double(0x7ff8000000000000ll);  // never CHAIN_EMPTY
           xs[xr] = x;
-          if (xr < n) y[r0 + xr] = x;
+          if (xr < n) st_relaxed_f64(y + r0 + xr, x);
         }
       }
     } else {
@@ -1493,18 +1531,14 @@ __global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long 
         for (int o = 16; o > 0; o >>= 1) pr += __shfl_xor_sync(0xffffffffu, pr, o);
         const int xr = warp * 8 + j;
         if (lane == 0) {
-          const double x = (xr < n) ? pr : 0.0;
+          double x = (xr < n) ? pr : 0.0;
+          if (x != x) x = __longlong_as_double(0x7ff8000000000000ll);
           xs[xr] = x;
-          if (xr < n) y[r0 + xr] = x;
+          if (xr < n) st_relaxed_f64(y + r0 + xr, x);
         }
       }
     }
     __syncthreads();
-    if (tid == 0) {
-      __threadfence();
-      asm volatile("red.release.gpu.global.max.u32 [%0], %1;" ::"l"(progress), "r"(static_cast<unsigned>(p0 + r) + 1)
-                   : "memory");
-    }
     // products of the later own blocks with x_p
 #pragma unroll
     for (int r2 = r + 1; r2 < CH_R; r2++) {
@@ -2160,9 +2194,7 @@ template <class T>
 static bool panel_factor(Context* ctx, T* A, long long ld, int N, int j0, int jb, int* ipiv, int* info, int nsm,
                          void* slot_mem, int* swap_map) {
   cudaStream_t s = ctx->stream();
-  double fl = 0;
-  for (int j = j0; j < j0 + jb; j++) fl += 2.0 * (N - j - 1) * (j0 + jb - j - 1) + (N - j);
-  ProfScope ps(ctx, Context::PROF_LU_PANEL, fl);
+  ProfScope ps(ctx, Context::PROF_LU_PANEL, 2.0 * sizeof(T) * jb * (N - j0));
   if (jb > 128) throw KdError(KD_ERR_ARG, "panel width above 128");
   PanelSlots<T> slots;
   {
@@ -2219,7 +2251,7 @@ template <class T>
 static void trsm_and_swaps(Context* ctx, T* A, long long ld, int N, int j0, int jb, const int* ipiv, int* map,
                            bool map_ready) {
   cudaStream_t s = ctx->stream();
-  ProfScope ps(ctx, Context::PROF_LU_SWAP_TRSM, double(jb) * jb * (N - j0 - jb));
+  ProfScope ps(ctx, Context::PROF_LU_SWAP_TRSM, 2.0 * sizeof(T) * jb * (N - j0 - jb));
   if (N > jb) {
     if (!map_ready) {
       build_swap_map<<<1, 32, 0, s>>>(ipiv, j0, jb, map);
@@ -2344,9 +2376,7 @@ void DenseLU::factor_f32_nopiv(float* A, long long ld, int N, bool tf32) {
   const int NB = NP_NB;
   auto panel = [&](int j0, int jb) {
     const int m = N - j0 - jb;
-    double fl = 0;
-    for (int j = j0; j < j0 + jb; j++) fl += 2.0 * (N - j - 1) * (j0 + jb - j - 1) + (N - j);
-    ProfScope ps(ctx_, Context::PROF_LU_PANEL, fl);
+    ProfScope ps(ctx_, Context::PROF_LU_PANEL_STATIC, 2.0 * sizeof(float) * jb * (N - j0));
     const int grid = m > 0 ? blocks(m, NP_THREADS) : 1;
     panel_nopiv_kernel<<<grid, NP_THREADS, 0, ctx_->stream()>>>(A, ld, N, j0, jb, d_info_);
     ctx_->launches++;
@@ -2367,7 +2397,7 @@ void DenseLU::factor_f32_nopiv(float* A, long long ld, int N, bool tf32) {
     const int m = N - j0 - jb;
     if (m <= 0) break;
     {
-      ProfScope ps(ctx_, Context::PROF_LU_SWAP_TRSM, double(jb) * jb * m);
+      ProfScope ps(ctx_, Context::PROF_LU_SWAP_TRSM, 2.0 * sizeof(float) * jb * m);
       launch_trsm_chunk(ctx_, A, ld, j0, jb, j0 + jb, N);
     }
     const int j0n = j0 + jb, jbn = (N - j0n < NB) ? N - j0n : NB;
@@ -2510,7 +2540,8 @@ void DenseLU::factor(double* A, long long ld, int N, int mode) {
 template <class T>
 void DenseLU::tri_solve(const T* LU, long long ld, int N, double* b, int trans) {
   cudaStream_t s = ctx_->stream();
-  ProfScope ps(ctx_, Context::PROF_LU_SOLVE, 2.0 * N * N);
+  // work of one sweep: the triangle of the factors it reads
+  const double sweep_bytes = 0.5 * sizeof(T) * N * static_cast<double>(N);
   const int nblk = (N + TB - 1) / TB;
   double* w1 = tri_work_;
   double* w2 = tri_work_ + ((static_cast<size_t>(N) + 31) / 32) * 32;  // 256-byte aligned second vector
@@ -2553,17 +2584,25 @@ void DenseLU::tri_solve(const T* LU, long long ld, int N, double* b, int trans) 
       cfg.dynamicSmemBytes = chain_smem<T>();
       const double* w1c = w1;
       const double* w2c = w2;
-      cuda_check(cudaLaunchKernelEx(&cfg, trsv_chain<T>, LU, ld, N, w1c, w2, dl, dl2, 1, tri_bar_, panel_err_, wait,
-                                    stall),
-                 "forward sweep");
-      cuda_check(cudaLaunchKernelEx(&cfg, trsv_chain<T>, LU, ld, N, w2c, b, du, du2, 0, tri_bar_ + 1, panel_err_,
-                                    wait, stall),
-                 "backward sweep");
+      // both outputs start as CHAIN_EMPTY (b was read by the gather above)
+      cuda_check(cudaMemsetAsync(w2, 0xff, sizeof(double) * N, s), "memset forward sweep output");
+      cuda_check(cudaMemsetAsync(b, 0xff, sizeof(double) * N, s), "memset backward sweep output");
+      {
+        ProfScope ps(ctx_, Context::PROF_LU_SOLVE, sweep_bytes);
+        cuda_check(cudaLaunchKernelEx(&cfg, trsv_chain<T>, LU, ld, N, w1c, w2, dl, dl2, 1, panel_err_, wait, stall),
+                   "forward sweep");
+      }
+      {
+        ProfScope ps(ctx_, Context::PROF_LU_SOLVE, sweep_bytes);
+        cuda_check(cudaLaunchKernelEx(&cfg, trsv_chain<T>, LU, ld, N, w2c, b, du, du2, 0, panel_err_, wait, stall),
+                   "backward sweep");
+      }
     } else if (sweep_kind == 1) {
       int gp = nblk < ctx_->sms() ? nblk : ctx_->sms();
       cfg.gridDim = dim3(gp, 1, 1);
       const double* w1c = w1;
       const double* w2c = w2;
+      ProfScope ps(ctx_, Context::PROF_LU_SOLVE, 2 * sweep_bytes);
       cuda_check(cudaLaunchKernelEx(&cfg, trsv_pull<T>, LU, ld, N, w1c, w2, dl, dl2, 1, tri_bar_, panel_err_, wait,
                                     stall),
                  "forward sweep");
@@ -2571,6 +2610,7 @@ void DenseLU::tri_solve(const T* LU, long long ld, int N, double* b, int trans) 
                                     wait, stall),
                  "backward sweep");
     } else {
+      ProfScope ps(ctx_, Context::PROF_LU_SOLVE, 2 * sweep_bytes);
       cuda_check(cudaLaunchKernelEx(&cfg, trsv_sweep<T>, LU, ld, N, w1, w2, dl, dl2, 1, tri_bar_, panel_err_, wait,
                                     stall),
                  "forward sweep");
@@ -2583,6 +2623,7 @@ void DenseLU::tri_solve(const T* LU, long long ld, int N, double* b, int trans) 
     return;
   } else {
     // A^T = U^T L^T P: U^T y = b (forward, lower), L^T z = y (backward), x = P^T z
+    ProfScope ps(ctx_, Context::PROF_LU_SOLVE, 2 * sweep_bytes);
     for (int k = 0; k < nblk; k++) {
       int r0 = k * TB, n = (N - r0 < TB) ? N - r0 : TB;
       int q0 = r0 + n, q1 = N;

@@ -759,7 +759,7 @@ class DenseLU:
 
 
 PROFILE_CATEGORIES = ("transform", "elementwise", "tau_gather", "lu_panel", "lu_swap_trsm", "lu_gemm", "lu_solve",
-                      "refine_matvec")
+                      "refine_matvec", "lu_panel_static")
 
 
 def profile_enable(ctx, on=True):
@@ -768,9 +768,10 @@ def profile_enable(ctx, on=True):
 
 def profile_read(ctx):
     """Per-category (ms, launches, work) of the launches since profile_enable."""
-    ms = np.zeros(8)
-    cnt = np.zeros(8, dtype=np.int64)
-    work = np.zeros(8)
+    n = len(PROFILE_CATEGORIES)
+    ms = np.zeros(n)
+    cnt = np.zeros(n, dtype=np.int64)
+    work = np.zeros(n)
     ctx.check(_L().kd_ctx_profile_read(ctx.h, _dp(ms), cnt.ctypes.data_as(C.POINTER(C.c_longlong)), _dp(work)))
     return {name: {"ms": float(ms[i]), "launches": int(cnt[i]), "work": float(work[i])}
             for i, name in enumerate(PROFILE_CATEGORIES)}

@@ -350,7 +350,11 @@ def solve_batch(configs, threads, precision=1e-10, lu_mode=None, device=0, keep=
 
 def main(argv=None) -> int:
     """Runs Newton steps of a workload from its initial guess: the command a
-    profiler wraps (`python -m kadath_frontera_gb300.workloads --steps 1`)."""
+    profiler wraps (`python -m kadath_frontera_gb300.workloads --steps 1`).
+    With --solves K it runs K complete solves instead (initial guess to
+    |F| <= precision, as the benchmark times them, residual graph-captured),
+    each inside an NVTX range "solve<i>", so that a profiler can select one
+    (`ncu --nvtx --nvtx-include "solve1/" ...`)."""
     import argparse
 
     from . import kadath as KD
@@ -359,10 +363,31 @@ def main(argv=None) -> int:
     ap.add_argument("--mode", default="mixed", choices=["mixed", "fp64", "fp32"])
     ap.add_argument("--warmup", type=int, default=1)
     ap.add_argument("--steps", type=int, default=1)
+    ap.add_argument("--solves", type=int, default=0)
     ap.add_argument("--precision", type=float, default=1e-10)
     args = ap.parse_args(argv)
     mode = {"mixed": KD.KD_LU_TF32_IR, "fp64": KD.KD_LU_FP64, "fp32": KD.KD_LU_FP32_IR}[args.mode]
     wl = WORKLOADS[args.workload]()
+    if args.solves > 0:
+        import torch
+        wl.syst.graph_capture = True
+        for i in range(args.solves):
+            wl.restore()
+            wl.syst.cache_tangents(False)
+            wl.syst.cache_tangents(True)
+            wl.syst.reset_pivot_order()
+            torch.cuda.nvtx.range_push(f"solve{i}")
+            steps = []
+            for _ in range(20):
+                done, err = wl.syst.do_newton(args.precision, lu_mode=mode)
+                steps.append(wl.syst.last_report)
+                if done:
+                    break
+            torch.cuda.synchronize()
+            torch.cuda.nvtx.range_pop()
+            print(f"solve {i}: {len(steps) - 1} updates, |F| = {err:.3e}, factor "
+                  + ", ".join(f"{r['t_factor_ms']:.1f}" for r in steps[:-1]) + " ms", flush=True)
+        return 0
     for i in range(args.warmup + args.steps):
         wl.restore()
         done, err = wl.syst.do_newton(args.precision, lu_mode=mode)
