@@ -55,12 +55,13 @@ int kd_ctx_destroy(kd_ctx* ctx);
 int kd_ctx_set_sm_budget(kd_ctx* ctx, int sms);
 /* Failure detection (no reference counterpart: MPI ranks of the reference
  * block forever on a lost peer).  Every grid-barrier wait of the solver's
- * cooperative kernels (LU panel, triangular sweeps) gives up after
- * `seconds` (default 2); the kernel then sets an error flag and returns, the
- * call reports KD_ERR_TIMEOUT, and the context stays usable.
+ * cooperative kernels (LU panel, triangular sweeps; in the chained sweep,
+ * the wait for an earlier block's unknowns) gives up after `seconds`
+ * (default 2); the kernel then sets an error flag and returns, the call
+ * reports KD_ERR_TIMEOUT, and the context stays usable.
  * kd_ctx_stall_waits(ctx, 1) injects the failure for tests: every barrier
- * target is raised by one, so no barrier completes and every wait runs out;
- * kd_ctx_stall_waits(ctx, 0) restores normal operation. */
+ * target is raised by one and every chained-sweep wait is refused, so the
+ * waits run out; kd_ctx_stall_waits(ctx, 0) restores normal operation. */
 int kd_ctx_set_wait_limit(kd_ctx* ctx, double seconds);
 int kd_ctx_stall_waits(kd_ctx* ctx, int on);
 const char* kd_last_error(const kd_ctx* ctx);
@@ -425,15 +426,46 @@ int kd_fields_val_points_device(int nfields, kd_field* const* fields, long long 
  *                          g = dQ/dy for Q = var's value at a point, y the
  *                          unknown vector (nbr_unknowns doubles, host);
  *  kd_system_dres_dcst     dF/dp for a double constant p (host vector);
+ *  kd_system_integral_gradient
+ *                          Q and g = dQ/dy for Q an integral observable:
+ *                          kind 0, the sum over domains dmin..dmax of
+ *                          `expr` (the left side of add_eq_int_volume,
+ *                          e.g. "integvolume(psi^5)");
+ *                          kind 1, the integral at infinity (the left side
+ *                          of add_eq_int_inf, e.g. "integ(dn(P))" or
+ *                          "integ(intMadm)" with intMadm = -dr(P)/2/PI
+ *                          defined in the last domain, as FUKA's ADM mass,
+ *                          include/Solvers/fuka_syst/fuka_syst_setup.hpp:62);
+ *                          g is the row such an equation would add to J;
+ *  kd_system_dres_dcst     dF/dp for a double constant p (host vector);
  *  kd_adjoint              dQ/dp = dq_explicit - lambda . dF/dp with
  *                          J^T lambda = g, J assembled at the current
  *                          (converged) fields and factored in FP64; lambda
- *                          (nullable) receives the adjoint vector. */
+ *                          (nullable) receives the adjoint vector;
+ *  kd_adjoint_ex           the same; with reuse_factors = 1 and the
+ *                          mixed-precision factors of the system's last
+ *                          Newton step at hand, J^T lambda = g is solved by
+ *                          FP64 GMRES on J^T (J at the current fields)
+ *                          preconditioned by those factors transposed, with
+ *                          no new factorisation; when that refinement does
+ *                          not converge, or without such factors, J is
+ *                          factored in FP64 as in kd_adjoint.  rep
+ *                          (nullable) tells which ran. */
+typedef struct {
+  int reused_factors;  /* 1: the Newton step's mixed factors preconditioned the solve */
+  int refine_iters;    /* GMRES iterations on J^T (reused factors only) */
+  double rel_residual; /* final |g - J^T lambda| / |g| (reused factors only) */
+  double t_assembly_ms, t_solve_ms;
+} kd_adjoint_report;
 int kd_system_set_cst(kd_system* s, const char* name, double v);
 int kd_field_val_point(kd_field* f, const double point[3], double* value);
 int kd_system_val_point_gradient(kd_system* s, const char* var, const double point[3], double* g);
+int kd_system_integral_gradient(kd_system* s, int kind, int dmin, int dmax, const char* expr, double* q,
+                                double* g);
 int kd_system_dres_dcst(kd_system* s, const char* cst, double* fp);
 int kd_adjoint(kd_system* s, const double* g, const char* cst, double dq_explicit, double* dqdp, double* lambda);
+int kd_adjoint_ex(kd_system* s, const double* g, const char* cst, double dq_explicit, int reuse_factors,
+                  double* dqdp, double* lambda, kd_adjoint_report* rep);
 
 /* ---- dense LU (Matrice::set_lu / solve, src/Matrice/matrice.cpp:192-249) */
 typedef struct kd_lu kd_lu;
@@ -443,7 +475,8 @@ int kd_lu_destroy(kd_lu* lu);
  * dA with its factors; mixed modes keep dA as the refinement operator. */
 int kd_lu_factor(kd_lu* lu, double* dA, long long ld, int n, int mode);
 /* Solves in place on the device vector db; trans = 1 solves A^T x = b
- * with the same factors (FP64 mode). */
+ * with the same factors (FP64 mode: transposed triangular solves; mixed
+ * modes: GMRES on A^T preconditioned by the transposed FP32 factors). */
 int kd_lu_solve(kd_lu* lu, double* db, int trans);
 /* Refinement of the mixed modes: GMRES(iters) restarted up to `restarts`
  * times until the relative residual is below tol (defaults 1e-14, 50, 4);

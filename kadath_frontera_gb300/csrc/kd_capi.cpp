@@ -972,6 +972,42 @@ int kd_adjoint(kd_system* s, const double* g, const char* cst, double dq_explici
   });
 }
 
+int kd_adjoint_ex(kd_system* s, const double* g, const char* cst, double dq_explicit, int reuse_factors,
+                  double* dqdp, double* lambda, kd_adjoint_report* rep) {
+  SYS_GUARD(s) {
+    if (!g || !cst || !dqdp) throw kd::KdError(KD_ERR_ARG, "null argument");
+    const int i = s->sys->find_cst(cst);
+    if (i < 0) throw kd::KdError(KD_ERR_ARG, std::string("unknown constant ") + cst);
+    kd::Newton::AdjointReport r;
+    *dqdp = s->newton->adjoint(g, i, dq_explicit, lambda, reuse_factors != 0, &r);
+    if (rep) {
+      rep->reused_factors = r.reused_factors;
+      rep->refine_iters = r.refine_iters;
+      rep->rel_residual = r.rel_residual;
+      rep->t_assembly_ms = r.t_assembly_ms;
+      rep->t_solve_ms = r.t_solve_ms;
+    }
+  });
+}
+
+int kd_system_integral_gradient(kd_system* s, int kind, int dmin, int dmax, const char* expr, double* q,
+                                double* g) {
+  SYS_GUARD(s) {
+    if (!expr || !q || !g) throw kd::KdError(KD_ERR_ARG, "null argument");
+    kd::Context* c = s->sp->ctx->c.get();
+    const int n = s->sys->nbr_unknowns();
+    double* d = nullptr;
+    kd::cuda_check(cudaMalloc(&d, sizeof(double) * (n > 0 ? n : 1)), "cudaMalloc(gradient)");
+    struct Free {
+      double* p;
+      ~Free() { cudaFree(p); }
+    } guard{d};
+    *q = s->sys->integral_gradient(kind, dmin, dmax, expr, d);
+    kd::cuda_check(cudaMemcpyAsync(g, d, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream()), "D2H");
+    kd::cuda_check(cudaStreamSynchronize(c->stream()), "sync");
+  });
+}
+
 int kd_newton_step_linesearch(kd_system* s, const kd_newton_opts* opts, int ntrymax, double stepmax,
                               kd_newton_report* rep, double* lambda) {
   SYS_GUARD(s) {

@@ -530,6 +530,30 @@ __global__ void gemv_finish(const double* __restrict__ part, int nchunk, int N, 
   y[row] = alpha * s + (b ? beta * b[row] : 0.0);
 }
 
+// y = alpha A^T x + beta b: one warp per column of A (a row of A^T), the
+// column read coalesced, lane partial sums reduced by xor shuffles (fixed
+// order).
+constexpr int GEMVT_WARPS = 8;
+__global__ void __launch_bounds__(GEMVT_WARPS * 32) gemv_t_kernel(const double* __restrict__ A, long long ld, int N,
+                                                                 const double* __restrict__ x, double alpha,
+                                                                 double beta, const double* __restrict__ b,
+                                                                 double* __restrict__ y) {
+  const int lane = threadIdx.x & 31;
+  const int col = blockIdx.x * GEMVT_WARPS + (threadIdx.x >> 5);
+  if (col >= N) return;
+  const double* a = A + static_cast<long long>(col) * ld;
+  double s0 = 0.0, s1 = 0.0;
+  int k = lane;
+  for (; k + 32 < N; k += 64) {
+    s0 = fma(a[k], x[k], s0);
+    s1 = fma(a[k + 32], x[k + 32], s1);
+  }
+  if (k < N) s0 = fma(a[k], x[k], s0);
+  double sum = s0 + s1;
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if (lane == 0) y[col] = alpha * sum + (b ? beta * b[col] : 0.0);
+}
+
 // ---- vector algebra of GMRES (fixed reduction order: bitwise reproducible) --
 constexpr int VA_THREADS = 256;
 
@@ -2646,16 +2670,19 @@ void DenseLU::solve_fp64(const double* LU, long long ld, int N, double* b, int t
   tri_solve<double>(LU, ld, N, b, trans);
 }
 
-void DenseLU::solve_f32(double* b) {
-  // M^-1 b = D_c (LU)^-1 (D_r b) with the equilibrated factors
+void DenseLU::solve_f32(double* b, int trans) {
+  // M^-1 b = D_c (LU)^-1 (D_r b) with the equilibrated factors LU of
+  // P D_r A D_c; transposed, M^-T b = D_r (LU)^-T (D_c b)
   cudaStream_t st = ctx_->stream();
+  const double* first = trans ? eq_buf_ + N_ : eq_buf_;
+  const double* last = trans ? eq_buf_ : eq_buf_ + N_;
   if (scaled_) {
-    scale_vec_kernel<<<blocks(N_, 256), 256, 0, st>>>(b, eq_buf_, N_);
+    scale_vec_kernel<<<blocks(N_, 256), 256, 0, st>>>(b, first, N_);
     ctx_->launches++;
   }
-  tri_solve<float>(A32_, ld32_, N_, b, 0);
+  tri_solve<float>(A32_, ld32_, N_, b, trans);
   if (scaled_) {
-    scale_vec_kernel<<<blocks(N_, 256), 256, 0, st>>>(b, eq_buf_ + N_, N_);
+    scale_vec_kernel<<<blocks(N_, 256), 256, 0, st>>>(b, last, N_);
     ctx_->launches++;
   }
 }
@@ -2732,9 +2759,14 @@ void DenseLU::prepare_solves(const T* LU, long long ld, int N, bool keep_perm) {
 // Right-preconditioned GMRES(m) in FP64 with the FP32 LU as preconditioner:
 // solves A x = b to a relative residual below gmres_tol.  Small dense
 // Hessenberg algebra runs on the host (m <= 50), vectors stay on the device.
-void DenseLU::gemv(const double* x, double* y, double alpha, double beta, const double* b) {
+void DenseLU::gemv(const double* x, double* y, double alpha, double beta, const double* b, int trans) {
   const int N = N_;
   cudaStream_t s = ctx_->stream();
+  if (trans) {
+    gemv_t_kernel<<<blocks(N, GEMVT_WARPS), GEMVT_WARPS * 32, 0, s>>>(A_, ld_, N, x, alpha, beta, b, y);
+    ctx_->launches++;
+    return;
+  }
   const int rb = blocks(N, GEMV_ROWS);
   int nchunk = (4 * nsm_ + rb - 1) / rb;  // the device's SMs: the split of the sums stays fixed
   if (nchunk > 32) nchunk = 32;
@@ -2752,12 +2784,13 @@ void DenseLU::gemv(const double* x, double* y, double alpha, double beta, const 
   ctx_->launches += 2;
 }
 
-void DenseLU::gmres_ir(double* b) {
+void DenseLU::gmres_ir(double* b, int trans) {
   // Right-preconditioned GMRES(m), M^-1 = the FP32 factors.  The basis is
   // orthogonalised by classical Gram-Schmidt run twice (CGS2): per
   // iteration two rounds of dot products and one norm on the device, one
   // copy of the results to the host; the small Hessenberg least-squares
-  // problem is solved on the host.  At most gmres_restarts cycles.
+  // problem is solved on the host.  At most gmres_restarts cycles.  With
+  // trans the operator is A^T and the preconditioner M^-T.
   const int N = N_;
   const int m = gmres_max_iter;
   cudaStream_t s = ctx_->stream();
@@ -2800,7 +2833,7 @@ void DenseLU::gmres_ir(double* b) {
     // r = b - A x
     {
       ProfScope ps(ctx_, Context::PROF_GMRES, 8.0 * double(N) * N);
-      gemv(x, r, -1.0, 1.0, b);
+      gemv(x, r, -1.0, 1.0, b, trans);
     }
     const double beta = norm(r);
     stats.final_rel_residual = beta / bnorm;
@@ -2812,10 +2845,10 @@ void DenseLU::gmres_ir(double* b) {
     for (; k < m; k++) {
       // w = A M^-1 v_k
       copy_scaled(V + static_cast<size_t>(k) * N, 1.0, r);
-      solve_f32(r);
+      solve_f32(r, trans);
       {
         ProfScope ps(ctx_, Context::PROF_GMRES, 8.0 * double(N) * N);
-        gemv(r, w, 1.0, 0.0, nullptr);
+        gemv(r, w, 1.0, 0.0, nullptr, trans);
       }
       // two rounds of w -= V (V^T w) over v_0 .. v_k, then |w|^2
       const int kk = k + 1;
@@ -2862,12 +2895,12 @@ void DenseLU::gmres_ir(double* b) {
     }
     cuda_check(cudaMemsetAsync(r, 0, sizeof(double) * N, s), "memset r");
     for (int i = 0; i < k; i++) add_scaled(V + static_cast<size_t>(i) * N, y[i], r);
-    solve_f32(r);
+    solve_f32(r, trans);
     add_scaled(r, 1.0, x);
   }
   {
     ProfScope ps(ctx_, Context::PROF_GMRES, 8.0 * double(N) * N);
-    gemv(x, r, -1.0, 1.0, b);
+    gemv(x, r, -1.0, 1.0, b, trans);
   }
   stats.final_rel_residual = norm(r) / bnorm;
   stats.refine_iters = total_it;
@@ -2878,8 +2911,12 @@ void DenseLU::solve(double* b, int trans) {
   double t0 = now_ms();
   if (mode_ == LU_FP64) {
     solve_fp64(A_, ld_, N_, b, trans);
+  } else if (trans) {
+    // A^T x = b: GMRES on A^T preconditioned by the transposed factors
+    // (no fallback to new factors: the caller decides)
+    gmres_ir(b, 1);
+    check_sweeps();
   } else {
-    if (trans) throw KdError(KD_ERR_UNSUPPORTED, "transposed solve needs the FP64 factors");
     if (nopiv_) {
       ensure_bsave();
       cuda_check(cudaMemcpyAsync(bsave_, b, sizeof(double) * N_, cudaMemcpyDeviceToDevice, ctx_->stream()),

@@ -41,6 +41,7 @@ class DenseLU {
 
   int mode() const { return mode_; }
   int n() const { return N_; }
+  const double* op() const { return A_; }  // the FP64 matrix of the last factor() call
   LuStats stats;
   double gmres_tol = 1e-14;
   int gmres_max_iter = 50;   // GMRES iterations per cycle
@@ -89,7 +90,7 @@ class DenseLU {
   bool scaled_ = false;
   double* part_ = nullptr;     // split-K partial sums of the FP64 matvec
   size_t part_cap_ = 0;
-  void gemv(const double* x, double* y, double alpha, double beta, const double* b);
+  void gemv(const double* x, double* y, double alpha, double beta, const double* b, int trans = 0);
   double* work_ = nullptr;     // solver workspace
   size_t work_cap_ = 0;
   double* hproj_ = nullptr;    // pinned host copy of one GMRES step's projections and norm
@@ -101,7 +102,7 @@ class DenseLU {
   void factor_fp64(double* A, long long ld, int N);
   void factor_f32(float* A, long long ld, int N, bool tf32);
   void solve_fp64(const double* LU, long long ld, int N, double* b, int trans);
-  void solve_f32(double* b);  // applies the FP32 factors to an FP64 vector
+  void solve_f32(double* b, int trans = 0);  // applies the FP32 factors to an FP64 vector
   template <class T>
   void tri_solve(const T* LU, long long ld, int N, double* b, int trans);
   template <class T>
@@ -124,7 +125,7 @@ class DenseLU {
   int* perm_ = nullptr;       // pivots as one permutation
   double* tri_work_ = nullptr;
   size_t perm_cap_ = 0;
-  void gmres_ir(double* b);
+  void gmres_ir(double* b, int trans = 0);
 };
 
 }  // namespace kd

@@ -330,16 +330,25 @@ bool Newton::step_linesearch(const NewtonOpts& o, int ntrymax, double stepmax, N
   return false;
 }
 
-double Newton::adjoint(const double* g, int cst, double dq_explicit, double* lambda_out) {
+double Newton::adjoint(const double* g, int cst, double dq_explicit, double* lambda_out, bool reuse_factors,
+                       AdjointReport* rep) {
   Context* ctx = sys_->ctx;
   cudaStream_t s = ctx->stream();
   if (sys_->nbr_conditions() < 0) sys_->residual(nullptr);
   const int N = sys_->nbr_conditions();
   if (sys_->nbr_unknowns() != N) throw KdError(KD_ERR_STATE, "Number of unknowns is different from the number of equations");
+  // mixed factors of the last Newton step of this size, whose refinement
+  // operator is d_J (the buffer the assembly below overwrites with J at the
+  // current fields)
+  const bool have_mixed = lu_->mode() != LU_FP64 && lu_->n() == N && d_J != nullptr && lu_->op() == d_J &&
+                          static_cast<size_t>(N) * static_cast<size_t>(ld) <= capJ_;
   ensure(N);
+  AdjointReport r;
+  auto t0 = std::chrono::steady_clock::now();
   sys_->residual(d_F, true);
   sys_->jacobian(d_J, ld, true);
-  lu_->factor(d_J, ld, N, LU_FP64);
+  cuda_check(cudaStreamSynchronize(s), "sync adjoint assembly");
+  r.t_assembly_ms = ms_since(t0);
   double* d = nullptr;
   cuda_check(cudaMalloc(&d, sizeof(double) * 2 * N), "cudaMalloc(adjoint)");
   struct Free {
@@ -348,8 +357,26 @@ double Newton::adjoint(const double* g, int cst, double dq_explicit, double* lam
   } guard{d};
   double* d_lambda = d;
   double* d_fp = d + N;
-  cuda_check(cudaMemcpyAsync(d_lambda, g, sizeof(double) * N, cudaMemcpyHostToDevice, s), "H2D g");
-  lu_->solve(d_lambda, 1);  // J^T lambda = g
+  t0 = std::chrono::steady_clock::now();
+  if (reuse_factors && have_mixed) {
+    cuda_check(cudaMemcpyAsync(d_lambda, g, sizeof(double) * N, cudaMemcpyHostToDevice, s), "H2D g");
+    try {
+      lu_->solve(d_lambda, 1);  // GMRES on J^T, preconditioned by the step's factors transposed
+      r.reused_factors = 1;
+    } catch (const KdError& e) {
+      if (e.code != KD_ERR_NOCONV) throw;
+    }
+  }
+  if (!r.reused_factors) {
+    lu_->factor(d_J, ld, N, LU_FP64);
+    cuda_check(cudaMemcpyAsync(d_lambda, g, sizeof(double) * N, cudaMemcpyHostToDevice, s), "H2D g");
+    lu_->solve(d_lambda, 1);  // J^T lambda = g with the FP64 factors
+  }
+  cuda_check(cudaStreamSynchronize(s), "sync adjoint solve");
+  r.t_solve_ms = ms_since(t0);
+  r.refine_iters = r.reused_factors ? lu_->stats.refine_iters : 0;
+  r.rel_residual = r.reused_factors ? lu_->stats.final_rel_residual : 0.0;
+  if (rep) *rep = r;
   sys_->dres_dcst(cst, d_fp);
   std::vector<double> lam(N), fp(N);
   cuda_check(cudaMemcpyAsync(lam.data(), d_lambda, sizeof(double) * N, cudaMemcpyDeviceToHost, s), "D2H lambda");

@@ -52,9 +52,20 @@ class Newton {
   // Adjoint sensitivity at a converged state (implicit-function theorem):
   // F(u0 + A y, p) = 0 with A the unknown coefficient patterns, so
   // dQ/dp = dQ_explicit - lambda . dF/dp with J^T lambda = g, g = dQ/dy.
-  // J is assembled and factored in FP64 here; the transposed solve reuses
-  // those factors.  g and lambda_out (nullable) are host vectors of N.
-  double adjoint(const double* g, int cst, double dq_explicit, double* lambda_out);
+  // J is assembled at the current fields.  With reuse_factors and
+  // mixed-precision factors from the last Newton step in hand, J^T lambda = g
+  // is solved by GMRES on that J^T preconditioned by those factors
+  // transposed (no new factorisation); otherwise, or when that refinement
+  // does not converge, J is factored in FP64 and solved with the transposed
+  // factors.  g and lambda_out (nullable) are host vectors of N.
+  struct AdjointReport {
+    int reused_factors = 0;
+    int refine_iters = 0;
+    double rel_residual = 0;
+    double t_assembly_ms = 0, t_solve_ms = 0;
+  };
+  double adjoint(const double* g, int cst, double dq_explicit, double* lambda_out, bool reuse_factors = false,
+                 AdjointReport* rep = nullptr);
   // Device buffers of the last step (valid until the next call).
   double* d_F = nullptr;
   double* d_J = nullptr;

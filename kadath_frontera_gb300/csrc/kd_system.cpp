@@ -1304,6 +1304,92 @@ void System::val_point_gradient(int var, const double point[3], double* g) {
   }
 }
 
+double System::integral_gradient(int kind, int dmin, int dmax, const std::string& expr, double* d_g) {
+  const int N = nbr_unknowns();
+  residual(nullptr, true);  // the unknown layout at the current fields
+  std::vector<OpePtr> parts;
+  if (kind == 0) {
+    if (dmin < 0 || dmax >= sp->ndom() || dmin > dmax) throw KdError(KD_ERR_ARG, "bad domain range for the integral");
+    for (int d = dmin; d <= dmax; d++) parts.push_back(parse_ope(*this, d, expr, -1));
+  } else if (kind == 1) {
+    const int last = sp->ndom() - 1;
+    if (sp->dom(last).type != DOM_COMPACT) throw KdError(KD_ERR_ARG, "integral at infinity needs a compactified domain");
+    parts.push_back(parse_ope(*this, last, expr, OUTER_BC));
+  } else {
+    throw KdError(KD_ERR_ARG, "integral kind must be 0 (volume) or 1 (at infinity)");
+  }
+  static const std::vector<int> rp = {0, 1}, one_idx = {0};
+  static const std::vector<double> one_w = {1.0};
+  // out[b] += tangent of part b (B numbers, or one constant)
+  auto add_tangent = [&](const Term& t, double* out, int B) {
+    if (!t.is_double) throw KdError(KD_ERR_STATE, "the integrand does not integrate to a number: " + expr);
+    if (!t.has_dd) return;
+    const double* v = t.ddv;
+    if (!v) {
+      if (t.dd == 0.0) return;
+      double* tmp = ctx->scratch().alloc_doubles(B);
+      cuda_check(launch_lincomb2(B, 1.0, nullptr, t.dd, 0.0, nullptr, 0.0, tmp, ctx->stream()), "constant tangent");
+      ctx->launches++;
+      v = tmp;
+    } else if (t.ddb != B) {
+      throw KdError(KD_ERR_STATE, "integral tangent of another batch size");
+    }
+    cuda_check(launch_gather_csr(v, 1, B, 1, ctx->table(rp), ctx->table(one_idx), ctx->dtable(one_w), out, 1, 0, 1.0,
+                                 1, ctx->stream()),
+               "integral gradient");
+    ctx->launches++;
+  };
+  ctx->scratch().reset();
+  double q = 0.0;
+  {
+    EvalState st;
+    st.sys = this;
+    st.with_der = false;
+    for (auto& p : parts) {
+      Term t = p->eval(st);
+      if (!t.is_double) throw KdError(KD_ERR_STATE, "the integrand does not integrate to a number: " + expr);
+      q += t.vd;
+    }
+  }
+  cuda_check(cudaMemsetAsync(d_g, 0, sizeof(double) * N, ctx->stream()), "memset gradient");
+  // double unknowns: one pass each (their columns come first)
+  const std::map<std::pair<int, int>, DVal> none;
+  for (size_t i = 0; i < vdoubles_.size(); i++) {
+    ctx->scratch().reset();
+    std::vector<double> e(vdoubles_.size(), 0.0);
+    e[i] = 1.0;
+    EvalState st;
+    st.sys = this;
+    st.with_der = true;
+    st.B = 1;
+    st.jx_seeds = &none;
+    st.jx_doubles = &e;
+    st.seed_var_double = static_cast<int>(i);
+    for (auto& p : parts) add_tangent(p->eval(st), d_g + i, 1);
+  }
+  // field unknowns: the seed blocks of the integrand's domains
+  for (size_t v = 0; v < vars_.size(); v++)
+    for (auto& p : parts) {
+      const int dd = p->dom;
+      if (dd < dom_min || dd > dom_max) continue;
+      ctx->scratch().reset();
+      int B;
+      Base base;
+      const double* seeds = seed_block(static_cast<int>(v), dd, B, base);
+      if (B == 0) continue;
+      EvalState st;
+      st.sys = this;
+      st.with_der = true;
+      st.B = B;
+      st.seed_var = static_cast<int>(v);
+      st.seed_dom = dd;
+      st.seed = DVal::from_coef(ctx, &sp->dom(dd), B, seeds, base);
+      add_tangent(p->eval(st), d_g + col0_[{static_cast<int>(v), dd}], B);
+    }
+  cuda_check(cudaStreamSynchronize(ctx->stream()), "sync integral gradient");
+  return q;
+}
+
 DVal System::x_to_field(int var, int dd, const double* d_x) {
   nbr_unknowns();
   const Domain& d = sp->dom(dd);

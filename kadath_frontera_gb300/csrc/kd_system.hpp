@@ -286,6 +286,12 @@ class System {
   // unknown vector (host, nbr_unknowns doubles): the point's summation
   // weights mapped through the unknown coefficient patterns.
   void val_point_gradient(int var, const double point[3], double* g);
+  // Q and dQ/dy (device vector of nbr_unknowns) for an integral observable:
+  // kind 0, `expr` (the left side of an add_eq_int_volume equation, e.g.
+  // "integvolume(psi^5)") summed over domains dmin..dmax; kind 1, the left
+  // side of add_eq_int_inf (e.g. "integ(dn(P))") in the last domain.  The gradient is the
+  // Jacobian row that equation would have (Eq_int::get_der, eq_int.cpp:45).
+  double integral_gradient(int kind, int dmin, int dmax, const std::string& expr, double* d_g);
   // Fields changed outside update_from_x: drop the recorded node values.
   void invalidate_values() { vcache_.clear(); }
   // Replays the value pass of residual(d_F, true) from a CUDA graph when the

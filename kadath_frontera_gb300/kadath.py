@@ -35,6 +35,11 @@ class NewtonOpts(C.Structure):
                 ("graph_capture", C.c_int), ("gmres_restarts", C.c_int), ("pivot_every_step", C.c_int)]
 
 
+class AdjointReport(C.Structure):
+    _fields_ = [("reused_factors", C.c_int), ("refine_iters", C.c_int), ("rel_residual", C.c_double),
+                ("t_assembly_ms", C.c_double), ("t_solve_ms", C.c_double)]
+
+
 class NewtonReport(C.Structure):
     _fields_ = [("error", C.c_double), ("converged", C.c_int), ("n", C.c_int), ("t_residual_ms", C.c_double),
                 ("t_assembly_ms", C.c_double), ("t_factor_ms", C.c_double), ("t_solve_ms", C.c_double),
@@ -121,6 +126,8 @@ def _declare_system(lib):
         "kd_system_val_point_gradient": (I, [P, C.c_char_p, DP, DP]),
         "kd_system_dres_dcst": (I, [P, C.c_char_p, DP]),
         "kd_adjoint": (I, [P, DP, C.c_char_p, D, DP, DP]),
+        "kd_adjoint_ex": (I, [P, DP, C.c_char_p, D, I, DP, DP, P]),
+        "kd_system_integral_gradient": (I, [P, I, I, I, C.c_char_p, DP, DP]),
         "kd_lu_create": (I, [P, C.POINTER(P)]),
         "kd_lu_destroy": (I, [P]),
         "kd_lu_factor": (I, [P, P, C.c_longlong, I, I]),
@@ -622,13 +629,33 @@ class System_of_eqs:
         self.ctx.check(_L().kd_system_dres_dcst(self.h, name.encode(), _dp(fp)))
         return fp
 
-    def adjoint(self, g, cst, dq_explicit=0.0):
+    def integral_gradient(self, expr, kind="inf", domains=None):
+        """(Q, dQ/dy) for an integral observable: kind "inf", the integral at
+        infinity of expr (the left side of add_eq_int_inf, e.g.
+        "integ(dn(P))"); kind "volume", expr summed over domains
+        (dmin, dmax) (the left side of add_eq_int_volume, e.g.
+        "integvolume(psi^5)")."""
+        k = {"volume": 0, "inf": 1}[kind]
+        dmin, dmax = domains if domains is not None else (0, 0)
+        g = np.zeros(self.get_nbr_unknowns())
+        q = C.c_double()
+        self.ctx.check(_L().kd_system_integral_gradient(self.h, k, int(dmin), int(dmax), expr.encode(), C.byref(q),
+                                                        _dp(g)))
+        return q.value, g
+
+    def adjoint(self, g, cst, dq_explicit=0.0, reuse_factors=False):
         """dQ/dp at the current (converged) fields: dq_explicit - lambda.dF/dp
-        with J^T lambda = g.  Returns (dQ/dp, lambda)."""
+        with J^T lambda = g.  Returns (dQ/dp, lambda).  With reuse_factors,
+        the mixed-precision factors of the last Newton step precondition
+        GMRES on J^T instead of a new FP64 factorisation (last_adjoint_report
+        says which ran)."""
         g = np.ascontiguousarray(g, dtype=np.float64)
         lam = np.zeros(self.get_nbr_unknowns())
         out = C.c_double()
-        self.ctx.check(_L().kd_adjoint(self.h, _dp(g), cst.encode(), float(dq_explicit), C.byref(out), _dp(lam)))
+        rep = AdjointReport()
+        self.ctx.check(_L().kd_adjoint_ex(self.h, _dp(g), cst.encode(), float(dq_explicit), 1 if reuse_factors else 0,
+                                          C.byref(out), _dp(lam), C.byref(rep)))
+        self.last_adjoint_report = {f: getattr(rep, f) for f, _ in AdjointReport._fields_}
         return out.value, lam
 
     def cache_tangents(self, on=True):

@@ -1,7 +1,13 @@
 """Adjoint sensitivities dQ/dp of a converged solution (implicit-function
-theorem, transposed solve with the FP64 factors), checked against central
-finite differences of full Newton re-solves on the GPU and with the CPU
-oracle, and through the torch.autograd.Function."""
+theorem), checked against central finite differences of full Newton re-solves
+on the GPU and with the CPU oracle, and through the torch.autograd.Function.
+
+Q is a field's value at a point, or an integral observable: the ADM-mass
+form M = -1/(2 pi) * integral at infinity of dn(psi) (FUKA's intMadm,
+include/Solvers/fuka_syst/fuka_syst_setup.hpp:62) and a volume integral.
+J^T lambda = g is solved either with a new FP64 factorisation or by GMRES on
+J^T preconditioned by the mixed-precision factors of the last Newton step,
+transposed (no new factorisation)."""
 import math
 
 import numpy as np
@@ -48,8 +54,9 @@ def solve(syst, prec=1e-12):
     raise AssertionError("no convergence")
 
 
-def oracle_q(amp, point):
-    """Q(amp) with the oracle's own Newton solver (the CPU reference path)."""
+def oracle_solve(amp):
+    """The oracle's own Newton solve of the same problem (the CPU reference
+    path); returns (domains, psi)."""
     doms = K.space_spheric(RES, [1.0, 2.0])
     psi = K.scalar_field(doms, lambda d: np.ones(d.np))
     nd = len(doms)
@@ -74,7 +81,20 @@ def oracle_q(amp, point):
         done, *_ = sysm.newton_step(1e-12)
         if done:
             break
+    return doms, psi
+
+
+def oracle_q(amp, point):
+    doms, psi = oracle_solve(amp)
     return K.val_point(doms, psi, point)
+
+
+def oracle_madm(amp):
+    """-1/(2 pi) * the integral at infinity of dn(psi) (Domain_compact::integ)."""
+    doms, psi = oracle_solve(amp)
+    d = doms[-1]
+    dn = K.OTerm(d, psi[d.num]).dn(K.OUTER_BC).val
+    return float(-K.integ_surface(dn, K.OUTER_BC)[0] / (2 * math.pi))
 
 
 def test_val_point_matches_oracle(ctx):
@@ -128,5 +148,124 @@ def test_autograd_function(ctx):
     h = 1e-4
     qp = converged_observable(torch.tensor(1.0 + h, dtype=torch.float64), syst, psi, "psi", "amp", POINTS[0])
     qm = converged_observable(torch.tensor(1.0 - h, dtype=torch.float64), syst, psi, "psi", "amp", POINTS[0])
+    fd = float(qp - qm) / (2 * h)
+    assert abs(float(p.grad) - fd) <= 1e-6 * abs(fd)
+
+
+MADM = "integ(dn(psi))"  # Q = -integ(dn(psi)) / (2 pi)
+
+
+def test_integral_gradient_matches_central_differences(ctx):
+    """dQ/dy of the ADM-mass integral (linear in the fields: exact to
+    roundoff) and of a volume integral of psi^5 (second-order differences),
+    along a random direction of the unknown vector."""
+    space, syst, psi, rho = build(1.0)
+    syst.do_newton(1e-12)  # a non-trivial iterate
+    n = syst.get_nbr_unknowns()
+    dy = np.random.default_rng(3).standard_normal(n)
+    for expr, kind, doms, h, tol in ((MADM, "inf", None, 1e-3, 1e-10), ("integvolume(psi^5)", "volume", (0, 1), 1e-5, 1e-7)):
+        q0, g = syst.integral_gradient(expr, kind, doms)
+        syst.xx_to_vars_update(-h * dy)  # u + h dy
+        qp, _ = syst.integral_gradient(expr, kind, doms)
+        syst.xx_to_vars_update(2 * h * dy)  # u - h dy
+        qm, _ = syst.integral_gradient(expr, kind, doms)
+        syst.xx_to_vars_update(-h * dy)
+        q1, _ = syst.integral_gradient(expr, kind, doms)
+        assert abs(q1 - q0) <= 1e-12 * max(1.0, abs(q0))
+        fd = (qp - qm) / (2 * h)
+        assert abs(g @ dy - fd) <= tol * max(abs(fd), 1e-300), (expr, g @ dy, fd)
+
+
+def test_integral_value_matches_oracle(ctx):
+    space, syst, psi, rho = build(1.0)
+    solve(syst)
+    q, _ = syst.integral_gradient(MADM, "inf")
+    doms = K.space_spheric(RES, [1.0, 2.0])
+    d = doms[-1]
+    v = K.VD(d, 1, cf=psi.get_coef(d.num)[None], base=d.std_base())
+    ref = K.integ_surface(K.OTerm(d, v).dn(K.OUTER_BC).val, K.OUTER_BC)[0]
+    assert abs(q - ref) <= 1e-12 * abs(ref)
+
+
+def test_transposed_mixed_solve_matches_lapack(ctx):
+    from kadath_frontera_gb300.kadath import DenseLU, KD_LU_TF32_IR
+    n = 1500
+    rng = np.random.default_rng(11)
+    u, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    v, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    A = (u * np.logspace(0, -4, n)) @ v.T
+    b = rng.standard_normal(n)
+    lu = DenseLU(ctx)
+    dA = torch.tensor(A.T.copy(), device="cuda")  # column-major A
+    lu.factor(dA.data_ptr(), n, n, KD_LU_TF32_IR)
+    db = torch.tensor(b, device="cuda")
+    lu.solve(db.data_ptr(), trans=1)
+    x = db.cpu().numpy()
+    ref = np.linalg.solve(A.T, b)
+    assert np.linalg.norm(x - ref) <= 1e-10 * np.linalg.norm(ref)
+    assert np.linalg.norm(A.T @ x - b) <= 1e-12 * np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("reuse", [False, True])
+def test_adm_mass_adjoint_matches_finite_differences(ctx, reuse):
+    """dM/damp for the ADM-mass integral, by the adjoint with a new FP64
+    factorisation or with the mixed factors of the last Newton step reused,
+    against central differences of full re-solves on the GPU and with the
+    oracle."""
+    from kadath_frontera_gb300.kadath import KD_LU_FP64, KD_LU_TF32_IR
+    space, syst, psi, rho = build(1.0)
+    mode = KD_LU_TF32_IR if reuse else KD_LU_FP64
+    for _ in range(30):
+        done, _ = syst.do_newton(1e-12, lu_mode=mode)
+        if done:
+            break
+    q, g = syst.integral_gradient(MADM, "inf")
+    dqdp, lam = syst.adjoint(-g / (2 * math.pi), "amp", reuse_factors=reuse)
+    assert syst.last_adjoint_report["reused_factors"] == int(reuse)
+    if reuse:
+        assert syst.last_adjoint_report["rel_residual"] < 1e-12
+    h = 1e-4
+    qs = []
+    for a in (1.0 + h, 1.0 - h):
+        syst.set_cst("amp", a)
+        solve(syst)
+        qs.append(-syst.integral_gradient(MADM, "inf")[0] / (2 * math.pi))
+    syst.set_cst("amp", 1.0)
+    fd = (qs[0] - qs[1]) / (2 * h)
+    assert abs(dqdp - fd) <= 1e-6 * abs(fd), (dqdp, fd)
+    ofd = (oracle_madm(1.0 + h) - oracle_madm(1.0 - h)) / (2 * h)
+    assert abs(dqdp - ofd) <= 1e-6 * abs(ofd), (dqdp, ofd)
+
+
+def test_reused_factors_give_the_fp64_adjoint(ctx):
+    """lambda from GMRES on J^T with the mixed factors of the last step equals
+    lambda from the FP64 factors of J at the converged fields."""
+    from kadath_frontera_gb300.kadath import KD_LU_TF32_IR
+    space, syst, psi, rho = build(1.0)
+    for _ in range(30):
+        done, _ = syst.do_newton(1e-12, lu_mode=KD_LU_TF32_IR)
+        if done:
+            break
+    g = syst.val_point_gradient("psi", POINTS[1])
+    d1, lam1 = syst.adjoint(g, "amp", reuse_factors=True)
+    assert syst.last_adjoint_report["reused_factors"] == 1
+    d0, lam0 = syst.adjoint(g, "amp", reuse_factors=False)
+    assert syst.last_adjoint_report["reused_factors"] == 0
+    assert np.linalg.norm(lam1 - lam0) <= 1e-10 * np.linalg.norm(lam0)
+    assert abs(d1 - d0) <= 1e-10 * abs(d0)
+
+
+def test_autograd_integral_with_reused_factors(ctx):
+    from kadath_frontera_gb300.adjoint import converged_integral
+    from kadath_frontera_gb300.kadath import KD_LU_TF32_IR
+    space, syst, psi, rho = build(1.0)
+    sc = -1.0 / (2 * math.pi)
+    p = torch.tensor(1.0, dtype=torch.float64, requires_grad=True)
+    q = converged_integral(p, syst, MADM, "amp", scale=sc, lu_mode=KD_LU_TF32_IR, reuse_factors=True)
+    q.backward()
+    assert syst.last_adjoint_report["reused_factors"] == 1
+    h = 1e-4
+    qp = converged_integral(torch.tensor(1.0 + h, dtype=torch.float64), syst, MADM, "amp", scale=sc)
+    qm = converged_integral(torch.tensor(1.0 - h, dtype=torch.float64), syst, MADM, "amp", scale=sc)
     fd = float(qp - qm) / (2 * h)
     assert abs(float(p.grad) - fd) <= 1e-6 * abs(fd)
