@@ -55,13 +55,12 @@ int kd_ctx_destroy(kd_ctx* ctx);
 int kd_ctx_set_sm_budget(kd_ctx* ctx, int sms);
 /* Failure detection (no reference counterpart: MPI ranks of the reference
  * block forever on a lost peer).  Every grid-barrier wait of the solver's
- * cooperative kernels (LU panel, triangular sweeps; in the chained sweep,
- * the wait for an earlier block's unknowns) gives up after `seconds`
- * (default 2); the kernel then sets an error flag and returns, the call
- * reports KD_ERR_TIMEOUT, and the context stays usable.
+ * cooperative kernels (LU panel, triangular sweeps) gives up after
+ * `seconds` (default 2); the kernel then sets an error flag and returns, the
+ * call reports KD_ERR_TIMEOUT, and the context stays usable.
  * kd_ctx_stall_waits(ctx, 1) injects the failure for tests: every barrier
- * target is raised by one and every chained-sweep wait is refused, so the
- * waits run out; kd_ctx_stall_waits(ctx, 0) restores normal operation. */
+ * target is raised by one, so the waits run out;
+ * kd_ctx_stall_waits(ctx, 0) restores normal operation. */
 int kd_ctx_set_wait_limit(kd_ctx* ctx, double seconds);
 int kd_ctx_stall_waits(kd_ctx* ctx, int on);
 const char* kd_last_error(const kd_ctx* ctx);

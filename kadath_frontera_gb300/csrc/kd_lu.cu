@@ -1291,59 +1291,37 @@ __global__ void __launch_bounds__(256) trsv_pull(const T* __restrict__ A, long l
 
 // The same sweep with CH_R consecutive blocks per CTA: CTA c owns sweep
 // positions c R .. c R + R - 1.  While earlier CTAs work it accumulates, for
-// all its blocks at once, the products with every finished x (phase A).  Its
-// own blocks then chain inside the CTA (phase B): x_p from the accumulated
-// rows and Dinv, stored, and its products with the CTA's later blocks from
-// the internal L blocks, which were staged in shared memory before phase A.
-// Only ceil(nblk / R) hand-offs between CTAs remain on the critical path.
-//
-// The x values are their own flags: y is filled with the bit pattern
-// CHAIN_EMPTY (all ones, a NaN that arithmetic does not produce: a NaN
-// result is stored as the positive quiet NaN) before the launch, producers
-// store x with relaxed gpu-scope stores, and consumers poll the 16 entries
-// they need until none is CHAIN_EMPTY.  No fence, counter or second load is
-// on the hand-off; each entry is read as a whole (8-byte single-copy
-// atomicity), and nothing else is exchanged between the CTAs.
+// all its blocks at once, the products with every finished x (phase A, one
+// progress wait per finished block).  Its own blocks then chain inside the
+// CTA (phase B): x_p from the accumulated rows and Dinv, published, and its
+// products with the CTA's later blocks from the internal L blocks, which
+// were staged in shared memory before phase A.  Only ceil(nblk / R)
+// hand-offs between CTAs remain on the critical path.
 constexpr int CH_R = 3;
-constexpr unsigned long long CHAIN_EMPTY = ~0ull;
-
-__device__ __forceinline__ double ld_relaxed_f64(const double* p) {
-  double v;
-  asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ double2 ld_relaxed_f64x2(const double* p) {
-  double2 v;
-  asm volatile("ld.relaxed.gpu.global.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ void st_relaxed_f64(double* p, double v) {
-  asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
-}
-__device__ __forceinline__ bool chain_empty(double v) {
-  return static_cast<unsigned long long>(__double_as_longlong(v)) == CHAIN_EMPTY;
-}
+constexpr int CH_DST = TB + 1;  // row stride of the staged Dinv blocks (8-byte entries: conflict-free row reads)
 // dynamic shared memory: the internal L blocks, then Dinv of the own blocks
 // (8 bytes an entry: a (hi, lo) float pair or a double)
 template <class T>
 constexpr size_t chain_smem() {
-  return static_cast<size_t>(CH_R * (CH_R - 1) / 2) * TB * TB * sizeof(T) + static_cast<size_t>(CH_R) * TB * TB * 8;
+  return static_cast<size_t>(CH_R * (CH_R - 1) / 2) * TB * TB * sizeof(T) +
+         static_cast<size_t>(CH_R) * TB * CH_DST * 8;
 }
 
 template <class T>
 __global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long long ld, int N,
                                                   const double* __restrict__ b, double* __restrict__ y,
                                                   const double* __restrict__ Dinv, const float2* __restrict__ Dinv2,
-                                                  int lower, int* err, unsigned long long wait_ns,
-                                                  unsigned stall) {
+                                                  int lower, unsigned* progress, int* err,
+                                                  unsigned long long wait_ns, unsigned stall) {
   extern __shared__ __align__(16) unsigned char ch_raw[];
   T* Lin = reinterpret_cast<T*>(ch_raw);  // internal blocks (r2, r1), r1 < r2: column-major 64 x 64
-  // Dinv of the own blocks, row-major 64 x 64 each
+  // Dinv of the own blocks, row-major 64 x 64 each with row stride CH_DST
   unsigned char* dsm = ch_raw + static_cast<size_t>(CH_R * (CH_R - 1) / 2) * TB * TB * sizeof(T);
   float2* D2s = reinterpret_cast<float2*>(dsm);
   double* Dds = reinterpret_cast<double*>(dsm);
   __shared__ double bsm[CH_R][TB];
   __shared__ double part[4][TB];
+  __shared__ float parth[4][TB], partl[4][TB];
   __shared__ float vh[TB], vl[TB];
   __shared__ double vd[TB];
   __shared__ double xs[TB];
@@ -1381,18 +1359,25 @@ __global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long 
   for (int r = 0; r < np; r++) {
     const size_t src = static_cast<size_t>(blk(p0 + r)) * TB * TB;
     for (int e0 = 0; e0 < TB * TB; e0 += 16 * 256) {
+      // entry e = row * TB + col of the block goes to row * CH_DST + col
       if constexpr (std::is_same<T, float>::value) {
         float2 v[16];
 #pragma unroll
         for (int u = 0; u < 16; u++) v[u] = Dinv2[src + e0 + u * 256 + tid];
 #pragma unroll
-        for (int u = 0; u < 16; u++) D2s[static_cast<size_t>(r) * TB * TB + e0 + u * 256 + tid] = v[u];
+        for (int u = 0; u < 16; u++) {
+          const int e = e0 + u * 256 + tid;
+          D2s[static_cast<size_t>(r) * TB * CH_DST + (e / TB) * CH_DST + e % TB] = v[u];
+        }
       } else {
         double v[16];
 #pragma unroll
         for (int u = 0; u < 16; u++) v[u] = Dinv[src + e0 + u * 256 + tid];
 #pragma unroll
-        for (int u = 0; u < 16; u++) Dds[static_cast<size_t>(r) * TB * TB + e0 + u * 256 + tid] = v[u];
+        for (int u = 0; u < 16; u++) {
+          const int e = e0 + u * 256 + tid;
+          Dds[static_cast<size_t>(r) * TB * CH_DST + (e / TB) * CH_DST + e % TB] = v[u];
+        }
       }
     }
     if (tid < TB) {
@@ -1407,7 +1392,8 @@ __global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long 
   // phase A: the finished blocks of earlier CTAs.  With FP32 factors the L
   // tile of the next block is loaded while the current one is used (it
   // does not depend on x), so the factor's HBM latency overlaps the
-  // waits for x.
+  // progress waits and the x loads.
+  unsigned avail = 0;
   bool ok = true;
   constexpr bool kAhead = sizeof(T) == 4;  // FP64 tiles would not fit twice in registers
   T a[CH_R][16], an[kAhead ? CH_R : 1][16];
@@ -1461,40 +1447,27 @@ __global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long 
     } else {
       load_tile(pi, a);
     }
-    // x of block pi, this thread's 16 columns, polled until all are stored
-    // (a stall request makes every poll fail, for the timeout tests)
-    double xv[16];
-    bool ready = false;
-    unsigned long long t0 = 0;
-    for (unsigned it = 0;; it++) {
-      if (y_aligned && cb + 16 <= N) {  // y + cb is then 16-byte aligned (cb is a multiple of 16)
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-          const double2 v = ld_relaxed_f64x2(y + cb + 2 * j);
-          xv[2 * j] = v.x;
-          xv[2 * j + 1] = v.y;
-        }
-      } else {
-#pragma unroll
-        for (int j = 0; j < 16; j++) xv[j] = (cb + j < N) ? ld_relaxed_f64(y + cb + j) : 0.0;
-      }
-      ready = stall == 0;
-#pragma unroll
-      for (int j = 0; j < 16; j++) ready = ready && !chain_empty(xv[j]);
-      if (ready) break;
-      if (it == 0) {
-        t0 = globaltimer_ns();
-      } else if ((it & 15) == 15 && globaltimer_ns() - t0 > wait_ns) {
+    if (static_cast<unsigned>(pi) >= avail) {
+      const unsigned v = wait_progress(progress, static_cast<unsigned>(pi) + 1 + stall, wait_ns);
+      if (v == 0) {
+        ok = false;
         break;
       }
-    }
-    if (!ready) {
-      ok = false;
-      break;
+      avail = v - stall;  // positions known finished
     }
     T xq[16];
+    if (y_aligned && cb + 16 <= N) {  // y + cb is then 16-byte aligned (cb is a multiple of 16)
+      const double2* y2 = reinterpret_cast<const double2*>(y + cb);
 #pragma unroll
-    for (int j = 0; j < 16; j++) xq[j] = static_cast<T>(xv[j]);
+      for (int j = 0; j < 8; j++) {
+        const double2 v = __ldcg(y2 + j);
+        xq[2 * j] = static_cast<T>(v.x);
+        xq[2 * j + 1] = static_cast<T>(v.y);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 16; j++) xq[j] = static_cast<T>((cb + j < N) ? __ldcg(y + cb + j) : 0.0);
+    }
 #pragma unroll
     for (int r = 0; r < CH_R; r++) {
       T sum = T(0);
@@ -1526,43 +1499,51 @@ __global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long 
       vl[tid] = static_cast<float>(v - static_cast<double>(hv));
     }
     __syncthreads();
-    const size_t dofs = static_cast<size_t>(r) * TB * TB + static_cast<size_t>(warp) * 8 * TB;
+    // x = Dinv v: thread (h, q, lane) forms row rr over columns c0 .. c0 + 15
+    // (two accumulators), the four column quarters are added in shared
+    // memory in a fixed order
+    const size_t drow = static_cast<size_t>(r) * TB * CH_DST + static_cast<size_t>(rr) * CH_DST + c0;
     if constexpr (std::is_same<T, float>::value) {
-      const float b0h = vh[lane], b0l = vl[lane], b1h = vh[lane + 32], b1l = vl[lane + 32];
+      DF s0 = {0.f, 0.f}, s1 = {0.f, 0.f};
 #pragma unroll
-      for (int j = 0; j < 8; j++) {
-        const float2 dl = D2s[dofs + j * TB + lane], dh = D2s[dofs + j * TB + lane + 32];
-        DF pr = df_add(df_mul(dl.x, dl.y, b0h, b0l), df_mul(dh.x, dh.y, b1h, b1l));
-        for (int o = 16; o > 0; o >>= 1) {
-          DF t;
-          t.h = __shfl_xor_sync(0xffffffffu, pr.h, o);
-          t.l = __shfl_xor_sync(0xffffffffu, pr.l, o);
-          pr = df_add(pr, t);
-        }
-        const int xr = warp * 8 + j;
-        if (lane == 0) {
-          double x = (xr < n) ? static_cast<double>(pr.h) + static_cast<double>(pr.l) : 0.0;
-          if (x != x) x = __longlong_as_double(0x7ff8000000000000ll);  // never CHAIN_EMPTY
-          xs[xr] = x;
-          if (xr < n) st_relaxed_f64(y + r0 + xr, x);
-        }
+      for (int j = 0; j < 16; j += 2) {
+        const float2 d0 = D2s[drow + j], d1 = D2s[drow + j + 1];
+        s0 = df_add(s0, df_mul(d0.x, d0.y, vh[c0 + j], vl[c0 + j]));
+        s1 = df_add(s1, df_mul(d1.x, d1.y, vh[c0 + j + 1], vl[c0 + j + 1]));
       }
+      const DF sq = df_add(s0, s1);
+      parth[q][rr] = sq.h;
+      partl[q][rr] = sq.l;
     } else {
-      const double b0 = vd[lane], b1 = vd[lane + 32];
+      double s0 = 0.0, s1 = 0.0;
 #pragma unroll
-      for (int j = 0; j < 8; j++) {
-        double pr = Dds[dofs + j * TB + lane] * b0 + Dds[dofs + j * TB + lane + 32] * b1;
-        for (int o = 16; o > 0; o >>= 1) pr += __shfl_xor_sync(0xffffffffu, pr, o);
-        const int xr = warp * 8 + j;
-        if (lane == 0) {
-          double x = (xr < n) ? pr : 0.0;
-          if (x != x) x = __longlong_as_double(0x7ff8000000000000ll);
-          xs[xr] = x;
-          if (xr < n) st_relaxed_f64(y + r0 + xr, x);
-        }
+      for (int j = 0; j < 16; j += 2) {
+        s0 = fma(Dds[drow + j], vd[c0 + j], s0);
+        s1 = fma(Dds[drow + j + 1], vd[c0 + j + 1], s1);
       }
+      part[q][rr] = s0 + s1;
     }
     __syncthreads();
+    if (tid < TB) {
+      double x;
+      if constexpr (std::is_same<T, float>::value) {
+        const DF a = df_add({parth[0][tid], partl[0][tid]}, {parth[1][tid], partl[1][tid]});
+        const DF c = df_add({parth[2][tid], partl[2][tid]}, {parth[3][tid], partl[3][tid]});
+        const DF t = df_add(a, c);
+        x = static_cast<double>(t.h) + static_cast<double>(t.l);
+      } else {
+        x = (part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]);
+      }
+      if (tid >= n) x = 0.0;
+      xs[tid] = x;
+      if (tid < n) y[r0 + tid] = x;
+    }
+    __syncthreads();
+    // release after the block barrier: the barrier orders every thread's
+    // store of x before thread 0's release (no separate fence)
+    if (tid == 0)
+      asm volatile("red.release.gpu.global.max.u32 [%0], %1;" ::"l"(progress), "r"(static_cast<unsigned>(p0 + r) + 1)
+                   : "memory");
     // products of the later own blocks with x_p
 #pragma unroll
     for (int r2 = r + 1; r2 < CH_R; r2++) {
@@ -2608,17 +2589,16 @@ void DenseLU::tri_solve(const T* LU, long long ld, int N, double* b, int trans) 
       cfg.dynamicSmemBytes = chain_smem<T>();
       const double* w1c = w1;
       const double* w2c = w2;
-      // both outputs start as CHAIN_EMPTY (b was read by the gather above)
-      cuda_check(cudaMemsetAsync(w2, 0xff, sizeof(double) * N, s), "memset forward sweep output");
-      cuda_check(cudaMemsetAsync(b, 0xff, sizeof(double) * N, s), "memset backward sweep output");
       {
         ProfScope ps(ctx_, Context::PROF_LU_SOLVE, sweep_bytes);
-        cuda_check(cudaLaunchKernelEx(&cfg, trsv_chain<T>, LU, ld, N, w1c, w2, dl, dl2, 1, panel_err_, wait, stall),
+        cuda_check(cudaLaunchKernelEx(&cfg, trsv_chain<T>, LU, ld, N, w1c, w2, dl, dl2, 1, tri_bar_, panel_err_, wait,
+                                      stall),
                    "forward sweep");
       }
       {
         ProfScope ps(ctx_, Context::PROF_LU_SOLVE, sweep_bytes);
-        cuda_check(cudaLaunchKernelEx(&cfg, trsv_chain<T>, LU, ld, N, w2c, b, du, du2, 0, panel_err_, wait, stall),
+        cuda_check(cudaLaunchKernelEx(&cfg, trsv_chain<T>, LU, ld, N, w2c, b, du, du2, 0, tri_bar_ + 1, panel_err_,
+                                      wait, stall),
                    "backward sweep");
       }
     } else if (sweep_kind == 1) {

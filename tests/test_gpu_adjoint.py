@@ -156,14 +156,19 @@ MADM = "integ(dn(psi))"  # Q = -integ(dn(psi)) / (2 pi)
 
 
 def test_integral_gradient_matches_central_differences(ctx):
-    """dQ/dy of the ADM-mass integral (linear in the fields: exact to
-    roundoff) and of a volume integral of psi^5 (second-order differences),
-    along a random direction of the unknown vector."""
+    """dQ/dy of the ADM-mass integral (linear in the fields: the difference
+    is exact up to rounding) and of a volume integral of psi^5 (second-order
+    differences with a small step: along a random coefficient direction the
+    quintic's third derivative is large), along a random direction of the
+    unknown vector."""
     space, syst, psi, rho = build(1.0)
     syst.do_newton(1e-12)  # a non-trivial iterate
     n = syst.get_nbr_unknowns()
     dy = np.random.default_rng(3).standard_normal(n)
-    for expr, kind, doms, h, tol in ((MADM, "inf", None, 1e-3, 1e-10), ("integvolume(psi^5)", "volume", (0, 1), 1e-5, 1e-7)):
+    # the update path u <- u - x rounds the coefficients (about 1e-11 in Q
+    # after three updates), which bounds the differences' accuracy
+    for expr, kind, doms, h, tol in ((MADM, "inf", None, 1e-1, 1e-8),
+                                     ("integvolume(psi^5)", "volume", (0, 1), 1e-6, 1e-6)):
         q0, g = syst.integral_gradient(expr, kind, doms)
         syst.xx_to_vars_update(-h * dy)  # u + h dy
         qp, _ = syst.integral_gradient(expr, kind, doms)
@@ -171,7 +176,7 @@ def test_integral_gradient_matches_central_differences(ctx):
         qm, _ = syst.integral_gradient(expr, kind, doms)
         syst.xx_to_vars_update(-h * dy)
         q1, _ = syst.integral_gradient(expr, kind, doms)
-        assert abs(q1 - q0) <= 1e-12 * max(1.0, abs(q0))
+        assert abs(q1 - q0) <= 1e-10 * max(1.0, abs(q0))
         fd = (qp - qm) / (2 * h)
         assert abs(g @ dy - fd) <= tol * max(abs(fd), 1e-300), (expr, g @ dy, fd)
 
