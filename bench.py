@@ -402,7 +402,10 @@ def run_gpu(args, ws, rank, local):
             "mixed": {k: results["mixed"][-1][2][1][k] for k in ("t_residual_ms", "t_assembly_ms", "t_factor_ms",
                                                                  "t_solve_ms", "t_update_ms")}}
         if len(results["mixed"][-1][2]) > 2 else None,
-        "refine": {"iters": rep0["refine_iters"], "rel_residual": rep0["refine_rel_residual"]},
+        "refine": {"iters": rep0["refine_iters"], "rel_residual": rep0["refine_rel_residual"],
+                   "iters_later_steps": [r["refine_iters"] for r in results["mixed"][-1][2][1:] if not r["converged"]],
+                   "static_pivots_later_steps": [r["static_pivots"] for r in results["mixed"][-1][2][1:]
+                                                 if not r["converged"]]},
         "mixed_vs_fp64_solution_max_rel_diff": mixed_vs_fp64,
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches_mixed),

@@ -1307,12 +1307,19 @@ constexpr size_t chain_smem() {
          static_cast<size_t>(CH_R) * TB * CH_DST * 8;
 }
 
+// With FP32 factors every value a thread multiplies is a float: the
+// producer stores x twice (y in FP64, yf in FP32), phase A and the internal
+// products read the FP32 copy, and the sums go in double-float.  (On this
+// GPU FP64 adds and FP64 <-> FP32 conversions run at the FP64 rate, a few
+// per clock per SM: one conversion per product would cost more than the
+// products.)
 template <class T>
 __global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long long ld, int N,
                                                   const double* __restrict__ b, double* __restrict__ y,
-                                                  const double* __restrict__ Dinv, const float2* __restrict__ Dinv2,
-                                                  int lower, unsigned* progress, int* err,
-                                                  unsigned long long wait_ns, unsigned stall) {
+                                                  float* __restrict__ yf, const double* __restrict__ Dinv,
+                                                  const float2* __restrict__ Dinv2, int lower, unsigned* progress,
+                                                  int* err, unsigned long long wait_ns, unsigned stall) {
+  constexpr bool kF = std::is_same<T, float>::value;
   extern __shared__ __align__(16) unsigned char ch_raw[];
   T* Lin = reinterpret_cast<T*>(ch_raw);  // internal blocks (r2, r1), r1 < r2: column-major 64 x 64
   // Dinv of the own blocks, row-major 64 x 64 each with row stride CH_DST
@@ -1325,6 +1332,7 @@ __global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long 
   __shared__ float vh[TB], vl[TB];
   __shared__ double vd[TB];
   __shared__ double xs[TB];
+  __shared__ float xsf[TB];
   __shared__ int s_abort;
   const int nblk = (N + TB - 1) / TB;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -1386,9 +1394,13 @@ __global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long 
     }
   }
   __syncthreads();
-  double acc[CH_R];
+  double acc[CH_R];  // FP64 factors
+  DF accf[CH_R];     // FP32 factors
 #pragma unroll
-  for (int r = 0; r < CH_R; r++) acc[r] = 0.0;
+  for (int r = 0; r < CH_R; r++) {
+    acc[r] = 0.0;
+    accf[r] = {0.f, 0.f};
+  }
   // phase A: the finished blocks of earlier CTAs.  With FP32 factors the L
   // tile of the next block is loaded while the current one is used (it
   // does not depend on x), so the factor's HBM latency overlaps the
@@ -1400,6 +1412,7 @@ __global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long 
   // 16-byte vector loads of x only from an aligned y (callers pass offset
   // vectors, e.g. a work vector at an odd offset N)
   const bool y_aligned = (reinterpret_cast<unsigned long long>(y) & 15ull) == 0;
+  const bool yf_aligned = kF && (reinterpret_cast<unsigned long long>(yf) & 15ull) == 0;
   // rows of this thread in its CTA's blocks (N when past the matrix)
   int rowof[CH_R];
 #pragma unroll
@@ -1456,7 +1469,22 @@ __global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long 
       avail = v - stall;  // positions known finished
     }
     T xq[16];
-    if (y_aligned && cb + 16 <= N) {  // y + cb is then 16-byte aligned (cb is a multiple of 16)
+    if constexpr (kF) {
+      if (yf_aligned && cb + 16 <= N) {  // yf + cb is then 16-byte aligned (cb is a multiple of 16)
+        const float4* y4 = reinterpret_cast<const float4*>(yf + cb);
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const float4 v = __ldcg(y4 + j);
+          xq[4 * j] = v.x;
+          xq[4 * j + 1] = v.y;
+          xq[4 * j + 2] = v.z;
+          xq[4 * j + 3] = v.w;
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 16; j++) xq[j] = (cb + j < N) ? __ldcg(yf + cb + j) : 0.f;
+      }
+    } else if (y_aligned && cb + 16 <= N) {  // y + cb is then 16-byte aligned (cb is a multiple of 16)
       const double2* y2 = reinterpret_cast<const double2*>(y + cb);
 #pragma unroll
       for (int j = 0; j < 8; j++) {
@@ -1473,7 +1501,11 @@ __global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long 
       T sum = T(0);
 #pragma unroll
       for (int j = 0; j < 16; j++) sum = fma(a[r][j], xq[j], sum);
-      acc[r] += static_cast<double>(sum);
+      if constexpr (kF) {
+        accf[r] = df_add(accf[r], {static_cast<float>(sum), 0.f});
+      } else {
+        acc[r] += static_cast<double>(sum);
+      }
     }
   }
   if (!ok) s_abort = 1;
@@ -1484,15 +1516,28 @@ __global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long 
     const int k = blk(p0 + r);
     const int r0 = k * TB;
     const int n = (N - r0 < TB) ? N - r0 : TB;
-    part[q][rr] = acc[r];
+    if constexpr (kF) {
+      parth[q][rr] = accf[r].h;
+      partl[q][rr] = accf[r].l;
+    } else {
+      part[q][rr] = acc[r];
+    }
     __syncthreads();
     if (s_abort) {
       if (tid == 0) atomicExch(err, 1);
       return;
     }
     if (tid < TB) {
-      const double v = (tid < n) ? bsm[r][tid] - ((part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]))
-                                 : 0.0;
+      double sacc;
+      if constexpr (kF) {
+        const DF a = df_add({parth[0][tid], partl[0][tid]}, {parth[1][tid], partl[1][tid]});
+        const DF c = df_add({parth[2][tid], partl[2][tid]}, {parth[3][tid], partl[3][tid]});
+        const DF t = df_add(a, c);
+        sacc = static_cast<double>(t.h) + static_cast<double>(t.l);
+      } else {
+        sacc = (part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]);
+      }
+      const double v = (tid < n) ? bsm[r][tid] - sacc : 0.0;
       vd[tid] = v;
       const float hv = static_cast<float>(v);
       vh[tid] = hv;
@@ -1537,6 +1582,11 @@ __global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long 
       if (tid >= n) x = 0.0;
       xs[tid] = x;
       if (tid < n) y[r0 + tid] = x;
+      if constexpr (kF) {
+        const float xf = static_cast<float>(x);
+        xsf[tid] = xf;
+        if (tid < n) yf[r0 + tid] = xf;
+      }
     }
     __syncthreads();
     // release after the block barrier: the barrier orders every thread's
@@ -1550,9 +1600,15 @@ __global__ void __launch_bounds__(256) trsv_chain(const T* __restrict__ A, long 
       if (r2 >= np) break;
       const T* L = Lin + static_cast<size_t>(tri(r2, r)) * TB * TB;
       T sum = T(0);
+      if constexpr (kF) {
 #pragma unroll
-      for (int j = 0; j < 16; j++) sum = fma(L[(c0 + j) * TB + rr], static_cast<T>(xs[c0 + j]), sum);
-      acc[r2] += static_cast<double>(sum);
+        for (int j = 0; j < 16; j++) sum = fmaf(L[(c0 + j) * TB + rr], xsf[c0 + j], sum);
+        accf[r2] = df_add(accf[r2], {sum, 0.f});
+      } else {
+#pragma unroll
+        for (int j = 0; j < 16; j++) sum = fma(L[(c0 + j) * TB + rr], static_cast<T>(xs[c0 + j]), sum);
+        acc[r2] += static_cast<double>(sum);
+      }
     }
   }
 }
@@ -2548,8 +2604,9 @@ void DenseLU::tri_solve(const T* LU, long long ld, int N, double* b, int trans) 
   // work of one sweep: the triangle of the factors it reads
   const double sweep_bytes = 0.5 * sizeof(T) * N * static_cast<double>(N);
   const int nblk = (N + TB - 1) / TB;
+  const size_t rnd = ((static_cast<size_t>(N) + 31) / 32) * 32;
   double* w1 = tri_work_;
-  double* w2 = tri_work_ + ((static_cast<size_t>(N) + 31) / 32) * 32;  // 256-byte aligned second vector
+  double* w2 = tri_work_ + rnd;  // 256-byte aligned second vector
   const size_t bs = static_cast<size_t>(TB) * TB;
   if (!trans) {
     gather_perm<<<blocks(N, 256), 256, 0, s>>>(b, perm_, N, w1);
@@ -2589,16 +2646,19 @@ void DenseLU::tri_solve(const T* LU, long long ld, int N, double* b, int trans) 
       cfg.dynamicSmemBytes = chain_smem<T>();
       const double* w1c = w1;
       const double* w2c = w2;
+      // FP32 copies of the two sweeps' outputs (FP32 factors only)
+      float* yf1 = std::is_same<T, float>::value ? reinterpret_cast<float*>(tri_work_ + 2 * rnd) : nullptr;
+      float* yf2 = std::is_same<T, float>::value ? yf1 + rnd : nullptr;
       {
         ProfScope ps(ctx_, Context::PROF_LU_SOLVE, sweep_bytes);
-        cuda_check(cudaLaunchKernelEx(&cfg, trsv_chain<T>, LU, ld, N, w1c, w2, dl, dl2, 1, tri_bar_, panel_err_, wait,
-                                      stall),
+        cuda_check(cudaLaunchKernelEx(&cfg, trsv_chain<T>, LU, ld, N, w1c, w2, yf1, dl, dl2, 1, tri_bar_, panel_err_,
+                                      wait, stall),
                    "forward sweep");
       }
       {
         ProfScope ps(ctx_, Context::PROF_LU_SOLVE, sweep_bytes);
-        cuda_check(cudaLaunchKernelEx(&cfg, trsv_chain<T>, LU, ld, N, w2c, b, du, du2, 0, tri_bar_ + 1, panel_err_,
-                                      wait, stall),
+        cuda_check(cudaLaunchKernelEx(&cfg, trsv_chain<T>, LU, ld, N, w2c, b, yf2, du, du2, 0, tri_bar_ + 1,
+                                      panel_err_, wait, stall),
                    "backward sweep");
       }
     } else if (sweep_kind == 1) {
@@ -2714,7 +2774,8 @@ void DenseLU::prepare_solves(const T* LU, long long ld, int N, bool keep_perm) {
     cudaFree(perm_);
     cudaFree(tri_work_);
     cuda_check(cudaMalloc(&perm_, sizeof(int) * N), "cudaMalloc(perm)");
-    cuda_check(cudaMalloc(&tri_work_, sizeof(double) * 2 * (((static_cast<size_t>(N) + 31) / 32) * 32)),
+    // two FP64 vectors, then two FP32 vectors (the chained sweeps' copies)
+    cuda_check(cudaMalloc(&tri_work_, sizeof(double) * 3 * (((static_cast<size_t>(N) + 31) / 32) * 32)),
                "cudaMalloc(tri work)");
     perm_cap_ = N;
   }
