@@ -740,7 +740,7 @@ def main():
     ap.add_argument("--precision", type=float, default=1e-10)
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--batch", type=int, default=16, help="instances of the batched-solve measurement (0: skip)")
+    ap.add_argument("--batch", type=int, default=64, help="instances of the batched-solve measurement (0: skip)")
     ap.add_argument("--export-points", type=int, default=1 << 20,
                     help="points of the exporter measurement (0: skip)")
     ap.add_argument("--batch-threads", type=int, default=8)
