@@ -389,6 +389,8 @@ def run_gpu(args, ws, rank, local):
                    "l2": "flushed between solves (256 MB write); the 1.2 GB Jacobian exceeds L2 within a solve",
                    "residual_graph": {"on": not args.no_graph,
                                       "captures_replays": list(syst.graph_stats())},
+                   "jacobian_graph": {"on": not args.no_graph,
+                                      "captures_replays": list(syst.jacobian_graph_stats())},
                    "parallelism": "replicas" if ws > 1 else "single"},
         "fp64_ms_per_step": fp64_ms, "mixed_speedup_vs_fp64": fp64_ms / mixed_ms if mixed_ms > 0 else None,
         "first_step_ms": {"mixed": first_m, "fp64": first_f},

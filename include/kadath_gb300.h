@@ -308,6 +308,13 @@ int kd_system_jacobian(kd_system* s, double* J);
  * Jacobian at every step (do_col_J, src/System_of_eqs/solver.cpp:120). */
 /* Captures and replays of the residual's value pass (kd_newton_opts.graph_capture). */
 int kd_system_graph_stats(kd_system* s, long long* captures, long long* replays);
+/* The same for the Jacobian's seed passes, which kd_newton_opts.graph_capture
+ * also replays from CUDA graphs: a pass is captured the second time the
+ * system is in the same state (the residual's state, the node values'
+ * addresses, the output buffer, the tangent cache's contents), with the
+ * tangent cache as the pass leaves it; systems with integral-type
+ * equations or double unknowns are never captured. */
+int kd_system_jacobian_graph_stats(kd_system* s, long long* captures, long long* replays);
 int kd_system_cache_tangents(kd_system* s, int enable);
 int kd_system_jacobian_device(kd_system* s, double* dJ, long long ld);
 /* do_JX (src/System_of_eqs/solver.cpp:87-118): y = J x without forming J,

@@ -686,6 +686,13 @@ int kd_system_check_equations(kd_system* s, double* errors) {
   });
 }
 
+int kd_system_jacobian_graph_stats(kd_system* s, long long* captures, long long* replays) {
+  if (!s || !s->sys || !captures || !replays) return KD_ERR_ARG;
+  *captures = s->sys->jacobian_graph_captures;
+  *replays = s->sys->jacobian_graph_replays;
+  return KD_OK;
+}
+
 int kd_system_graph_stats(kd_system* s, long long* captures, long long* replays) {
   if (!s || !s->sys || !captures || !replays) return KD_ERR_ARG;
   *captures = s->sys->residual_graph_captures;

@@ -370,6 +370,10 @@ void System::drop_graph() {
     if (g.exec) cudaGraphExecDestroy(g.exec);
   graphs_.clear();
   seen_sigs_.clear();
+  for (auto& g : jgraphs_)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+  jgraphs_.clear();
+  jseen_.clear();
 }
 
 void System::set_residual_graph(bool on) {
@@ -1155,6 +1159,45 @@ const double* System::seed_block(int var, int dom, int& B, Base& base) {
   return p;
 }
 
+// What a Jacobian pass's launches depend on besides the fields' data: the
+// state of the value pass (which representations, bases and numbers; the
+// node values' device addresses), the output, and the tangent cache's
+// contents (which subtrees are skipped) and arena position.
+std::vector<long long> System::jacobian_signature(const double* d_J, long long ld, bool rectangular) const {
+  std::vector<long long> g = state_signature();
+  g.push_back(reinterpret_cast<long long>(d_J));
+  g.push_back(ld);
+  g.push_back(rectangular ? 1 : 0);
+  g.push_back(cache_tangents_ ? 1 : 0);
+  g.push_back(static_cast<long long>(tcache_.ders.size()));
+  g.push_back(static_cast<long long>(tcache_.arena.mark()));
+  g.push_back(static_cast<long long>(vcache_.arena.mark()));
+  g.push_back(static_cast<long long>(vcache_.vals.size()));
+  // node values: an order-independent sum of per-node hashes
+  auto mix = [](unsigned long long x) {
+    x ^= x >> 33;
+    x *= 0xff51afd7ed558ccdull;
+    x ^= x >> 33;
+    x *= 0xc4ceb9fe1a85ec53ull;
+    x ^= x >> 33;
+    return x;
+  };
+  unsigned long long h = 0;
+  for (const auto& kv : vcache_.vals) {
+    unsigned long long e = mix(reinterpret_cast<unsigned long long>(kv.first));
+    unsigned long long vb;
+    std::memcpy(&vb, &kv.second.vd, sizeof vb);
+    e = mix(e ^ vb);
+    for (const auto& d : kv.second.vt) {
+      e = mix(e ^ reinterpret_cast<unsigned long long>(d.c));
+      e = mix(e ^ reinterpret_cast<unsigned long long>(d.cf));
+    }
+    h += e;
+  }
+  g.push_back(static_cast<long long>(h));
+  return g;
+}
+
 void System::jacobian(double* d_J, long long ld, bool reuse, bool rectangular) {
   int N = nbr_unknowns();
   if (!reuse || !vcache_.valid) residual(nullptr, true);
@@ -1163,6 +1206,90 @@ void System::jacobian(double* d_J, long long ld, bool reuse, bool rectangular) {
     os << "Number of unknowns (" << N << ") is different from the number of equations (" << nbr_conditions_ << ")";
     throw KdError(KD_ERR_STATE, os.str());
   }
+  const bool graphable = graph_on_ && !jgraph_failed_ && ieqs_.empty() && vdoubles_.empty() && !ctx->prof_on() &&
+                         !ctx->capturing;
+  if (!graphable) {
+    jacobian_pass(d_J, ld);
+    return;
+  }
+  std::vector<long long> sig = jacobian_signature(d_J, ld, rectangular);
+  cudaStream_t main = ctx->main_stream();
+  graph_clock_++;
+  for (auto& g : jgraphs_)
+    if (g.sig == sig) {
+      tcache_.ders = g.tders;
+      tcache_.arena.release_to(g.tmark);
+      ctx->scratch().reset();
+      cuda_check(cudaGraphLaunch(g.exec, main), "replay Jacobian pass");
+      ctx->launches += g.launches;
+      g.last_use = graph_clock_;
+      jacobian_graph_replays++;
+      return;
+    }
+  // first time: as it is (it also sizes the arenas and uploads the seeds
+  // and tables); second time: captured
+  if (std::find(jseen_.begin(), jseen_.end(), sig) == jseen_.end()) {
+    if (jseen_.size() >= 16) jseen_.erase(jseen_.begin());
+    jseen_.push_back(sig);
+    jacobian_pass(d_J, ld);
+    return;
+  }
+  const auto tders0 = tcache_.ders;
+  const size_t tmark0 = tcache_.arena.mark();
+  auto fall_back = [&] {
+    cudaGetLastError();
+    jgraph_failed_ = true;  // something in the pass cannot be captured
+    tcache_.ders = tders0;
+    tcache_.arena.release_to(tmark0);
+    jacobian_pass(d_J, ld);
+  };
+  cudaGraph_t graph = nullptr;
+  cuda_check(cudaStreamBeginCapture(main, cudaStreamCaptureModeThreadLocal), "begin capture");
+  ctx->capturing = true;
+  const long long l0 = ctx->launches;
+  try {
+    jacobian_pass(d_J, ld);
+  } catch (...) {
+    ctx->capturing = false;
+    cudaStreamEndCapture(main, &graph);
+    if (graph) cudaGraphDestroy(graph);
+    fall_back();
+    return;
+  }
+  ctx->capturing = false;
+  if (cudaStreamEndCapture(main, &graph) != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    fall_back();
+    return;
+  }
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t st = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (st != cudaSuccess) {
+    fall_back();
+    return;
+  }
+  if (jgraphs_.size() >= 4) {
+    auto lru = std::min_element(jgraphs_.begin(), jgraphs_.end(),
+                                [](const JacGraph& a, const JacGraph& b) { return a.last_use < b.last_use; });
+    cudaGraphExecDestroy(lru->exec);
+    jgraphs_.erase(lru);
+  }
+  JacGraph g;
+  g.sig = std::move(sig);
+  g.exec = exec;
+  g.launches = ctx->launches - l0;
+  g.tders = tcache_.ders;
+  g.tmark = tcache_.arena.mark();
+  g.last_use = graph_clock_;
+  jacobian_graph_captures++;
+  // the capture ran nothing: the pass itself is the first replay
+  cuda_check(cudaGraphLaunch(g.exec, main), "replay Jacobian pass");
+  jgraphs_.push_back(std::move(g));
+}
+
+void System::jacobian_pass(double* d_J, long long ld) {
+  const int N = nbr_unknowns();
   cuda_check(cudaMemsetAsync(d_J, 0, sizeof(double) * ld * N, ctx->stream()), "memset J");
   // Columns of the double unknowns (do_col_J with is_var_double): one pass
   // each with that unknown's tangent 1, every field's 0, all equations.

@@ -301,6 +301,7 @@ class System {
   // come back to the host in the pass).
   void set_residual_graph(bool on);
   long long residual_graph_replays = 0, residual_graph_captures = 0;
+  long long jacobian_graph_replays = 0, jacobian_graph_captures = 0;
 
   struct VarInfo {
     std::string name;
@@ -372,6 +373,22 @@ class System {
   long long graph_clock_ = 0;
   std::vector<long long> state_signature() const;
   void residual_pass(double* d_F, bool record);
+  // The Jacobian's seed passes as a CUDA graph: captured the second time a
+  // signature is met, with the tangent cache as the pass left it (its host
+  // side; the replay refills the device side at the same addresses).
+  struct JacGraph {
+    std::vector<long long> sig;
+    cudaGraphExec_t exec = nullptr;
+    long long launches = 0;
+    std::map<std::tuple<const Ope*, int, int>, TangentCache::Entry> tders;
+    size_t tmark = 0;
+    long long last_use = 0;
+  };
+  bool jgraph_failed_ = false;
+  std::vector<JacGraph> jgraphs_;
+  std::vector<std::vector<long long>> jseen_;
+  std::vector<long long> jacobian_signature(const double* d_J, long long ld, bool rectangular) const;
+  void jacobian_pass(double* d_J, long long ld);
   void drop_graph();
 
   void compute_unknowns();

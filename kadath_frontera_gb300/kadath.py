@@ -109,6 +109,7 @@ def _declare_system(lib):
         "kd_system_jacobian": (I, [P, DP]),
         "kd_system_cache_tangents": (I, [P, I]),
         "kd_system_graph_stats": (I, [P, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
+        "kd_system_jacobian_graph_stats": (I, [P, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
         "kd_system_jx": (I, [P, DP, DP]),
         "kd_system_jacobian_device": (I, [P, P, C.c_longlong]),
         "kd_system_update": (I, [P, DP]),
@@ -719,6 +720,12 @@ class System_of_eqs:
         """(captures, replays) of the residual's value pass."""
         c, r = C.c_longlong(), C.c_longlong()
         self.ctx.check(_L().kd_system_graph_stats(self.h, C.byref(c), C.byref(r)))
+        return c.value, r.value
+
+    def jacobian_graph_stats(self):
+        """(captures, replays) of the Jacobian's seed passes."""
+        c, r = C.c_longlong(), C.c_longlong()
+        self.ctx.check(_L().kd_system_jacobian_graph_stats(self.h, C.byref(c), C.byref(r)))
         return c.value, r.value
 
     def do_newton_with_linesearch(self, precision, ntrymax=10, stepmax=1.0, lu_mode=None, gmres_tol=1e-14,
