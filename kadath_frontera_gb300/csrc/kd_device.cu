@@ -223,6 +223,9 @@ __global__ void ew_kernel(int op, long long npts, long long total, int ba, const
       case EW_ATAN: r = atan(x); break;
       case EW_MULC_ADD: r = x * y * alpha; break;
       case EW_DIVC: r = x / alpha; break;
+      case EW_COSH: r = cosh(x); break;
+      case EW_SINH: r = sinh(x); break;
+      case EW_ATANH: r = atanh(x); break;
       default: r = 0.0; break;
     }
     out[i] = r;

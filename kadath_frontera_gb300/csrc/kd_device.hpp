@@ -72,6 +72,9 @@ enum EwOp : int {
   EW_ATAN = 19,
   EW_MULC_ADD = 20,  // out = a*b*alpha (product with constant)
   EW_DIVC = 21,      // a / alpha (Val_domain / double divides, it does not scale by 1/alpha)
+  EW_COSH = 22,
+  EW_SINH = 23,
+  EW_ATANH = 24,
 };
 
 cudaError_t launch_ew(int op, long long npts, int ba, const double* a, int bb, const double* b,

@@ -426,6 +426,31 @@ DVal vd_atan(const DVal& a) {
   return r;
 }
 
+DVal vd_cosh(const DVal& a) {
+  if (a.zero) {
+    DVal r = filled(a.ctx, a.dom, a.batch, 1.0);
+    r.base = a.base;
+    return r;
+  }
+  return conf_unary(EW_COSH, a);
+}
+
+DVal vd_sinh(const DVal& a) {
+  if (a.zero) {
+    DVal r = filled(a.ctx, a.dom, a.batch, 1.0);
+    r.base = a.base;
+    return r;
+  }
+  return conf_unary(EW_SINH, a);
+}
+
+DVal vd_atanh(const DVal& a) {
+  if (a.zero) return a;
+  DVal r = conf_unary(EW_ATANH, a);
+  r.base = a.base;
+  return r;
+}
+
 // ------------------------------------------------------- domain operators --
 DVal ope_coef(const DVal& so, int op, int dim) {
   so.coef();

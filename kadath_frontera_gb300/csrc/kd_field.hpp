@@ -78,6 +78,13 @@ DVal vd_log(const DVal& a);
 DVal vd_sin(const DVal& a);
 DVal vd_cos(const DVal& a);
 DVal vd_atan(const DVal& a);
+// cosh / sinh / atanh of Val_domain (src/Val_domain/val_domain_math.cpp):
+// at the collocation points.  cosh and sinh of a zero field give 1 with the
+// operand's basis (sinh too, as the reference does); otherwise no basis, as
+// for sin and cos.  atanh keeps the operand's basis.
+DVal vd_cosh(const DVal& a);
+DVal vd_sinh(const DVal& a);
+DVal vd_atanh(const DVal& a);
 
 // Domain operators (src/Domain/Spheric/domain_*_ope.cpp and do_der_abs_from_der_var).
 DVal ope_coef(const DVal& so, int op, int dim);  // generic ope_1d on the coefficients

@@ -625,7 +625,7 @@ class OpeFunctional : public Ope {
 // Unary operators acting component by component on value and tangent.
 class OpeUnary : public Ope {
  public:
-  enum Kind { LAP, DN, DR, MULTR, DIVR, DIVSINT, MULTSINT, DIVCOST };
+  enum Kind { LAP, DN, DR, MULTR, DIVR, DIVSINT, MULTSINT, DIVCOST, DDR };
   OpeUnary(int dom, Kind k, int bound, OpePtr a_) : Ope(dom), kind(k), bound(bound), a(std::move(a_)) {
     vc = a->vc;  // linear operators: the tangent is the operator of the tangent
     dc = a->dc;
@@ -641,6 +641,8 @@ class OpeUnary : public Ope {
         return comp_by_comp(t, [b](const DVal& v) { return der_normal(v, b); }, cv);
       }
       case DR: return comp_by_comp(t, [](const DVal& v) { return der_r(v); }, cv);
+      // Domain::ddr (src/Domain/domain.cpp:1522): der_r twice (Ope_ddr keeps zero as zero)
+      case DDR: return comp_by_comp(t, [](const DVal& v) { return v.zero ? v : der_r(der_r(v)); }, cv);
       case MULTR: return comp_by_comp(t, [](const DVal& v) { return mult_r(v); }, cv);
       case DIVR: return comp_by_comp(t, [](const DVal& v) { return div_r(v); }, cv);
       case DIVSINT: return comp_by_comp(t, [](const DVal& v) { return div_sin_theta(v); }, cv);
@@ -653,10 +655,14 @@ class OpeUnary : public Ope {
   OpePtr a;
 };
 
-// exp / sqrt / log of a scalar (src/Ope_eq/ope_exp.cpp, ope_sqrt.cpp, ope_log.cpp)
+// exp / sqrt / log / cos / sin / cosh / sinh / atanh of a scalar
+// (src/Ope_eq/ope_exp.cpp, ope_sqrt.cpp, ope_log.cpp, ope_cos.cpp,
+// ope_sin.cpp, ope_cosh.cpp, ope_sinh.cpp, ope_atanh.cpp), with their
+// tangents in the reference's operand order: -u' sin(u), u' cos(u),
+// u' sinh(u), u' cosh(u), u' / (1 - u u).
 class OpeFunc : public Ope {
  public:
-  enum Kind { EXP, SQRT, LOG };
+  enum Kind { EXP, SQRT, LOG, COS, SIN, COSH, SINH, ATANH };
   OpeFunc(int dom, Kind k, OpePtr a_) : Ope(dom), kind(k), a(std::move(a_)) {
     vc = a->vc;
     dz = a->dz;
@@ -666,32 +672,80 @@ class OpeFunc : public Ope {
   Term action(EvalState& st, const Term* cv) const override {
     Term t = a->eval(st);
     if (t.is_double) {
-      double v = kind == EXP ? std::exp(t.vd) : kind == SQRT ? std::sqrt(t.vd) : std::log(t.vd);
+      const double u = t.vd;
+      double v = 0.0;
+      switch (kind) {
+        case EXP: v = std::exp(u); break;
+        case SQRT: v = std::sqrt(u); break;
+        case LOG: v = std::log(u); break;
+        case COS: v = std::cos(u); break;
+        case SIN: v = std::sin(u); break;
+        case COSH: v = std::cosh(u); break;
+        case SINH: v = std::sinh(u); break;
+        case ATANH: v = std::atanh(u); break;
+      }
       Term r = Term::dbl(t.dom, v);
       if (t.has_dd && t.ddv) {
-        const double f1 = kind == EXP ? std::exp(t.vd) : kind == SQRT ? 0.5 / std::sqrt(t.vd) : 1.0 / t.vd;
+        double f1 = 0.0;
+        switch (kind) {
+          case EXP: f1 = std::exp(u); break;
+          case SQRT: f1 = 0.5 / std::sqrt(u); break;
+          case LOG: f1 = 1.0 / u; break;
+          case COS: f1 = -std::sin(u); break;
+          case SIN: f1 = std::cos(u); break;
+          case COSH: f1 = std::sinh(u); break;
+          case SINH: f1 = std::cosh(u); break;
+          case ATANH: f1 = 1.0 / (1 - u * u); break;
+        }
         dbl_tangent_lincomb(r, f1, t, 0.0, nullptr);
       } else if (t.has_dd) {
         r.has_dd = true;
-        r.dd = kind == EXP ? t.dd * std::exp(t.vd) : kind == SQRT ? t.dd / 2. / std::sqrt(t.vd) : t.dd / t.vd;
+        const double d = t.dd;
+        switch (kind) {
+          case EXP: r.dd = d * std::exp(u); break;
+          case SQRT: r.dd = d / 2. / std::sqrt(u); break;
+          case LOG: r.dd = d / u; break;
+          case COS: r.dd = -d * std::sin(u); break;
+          case SIN: r.dd = d * std::cos(u); break;
+          case COSH: r.dd = d * std::sinh(u); break;
+          case SINH: r.dd = d * std::cosh(u); break;
+          case ATANH: r.dd = d / (1 - u * u); break;
+        }
       }
       return r;
     }
-    if (t.vt.size() != 1) throw KdError(KD_ERR_UNSUPPORTED, "exp/sqrt/log only defined for a scalar");
+    if (t.vt.size() != 1) throw KdError(KD_ERR_UNSUPPORTED, "exp/sqrt/log/cos/sin/cosh/sinh/atanh only defined for a scalar");
     Term r = tensor_like(t);
     const DVal& v = t.vt[0];
-    if (cv) r.vt = cv->vt;
-    else if (kind == EXP) r.vt.push_back(vd_exp(v));
-    else if (kind == SQRT) r.vt.push_back(v.zero ? v : vd_sqrt(v));
-    else r.vt.push_back(vd_log(v));
+    if (cv) {
+      r.vt = cv->vt;
+    } else {
+      switch (kind) {
+        case EXP: r.vt.push_back(vd_exp(v)); break;
+        case SQRT: r.vt.push_back(v.zero ? v : vd_sqrt(v)); break;
+        case LOG: r.vt.push_back(vd_log(v)); break;
+        case COS: r.vt.push_back(vd_cos(v)); break;
+        case SIN: r.vt.push_back(vd_sin(v)); break;
+        case COSH: r.vt.push_back(vd_cosh(v)); break;
+        case SINH: r.vt.push_back(vd_sinh(v)); break;
+        case ATANH: r.vt.push_back(vd_atanh(v)); break;
+      }
+    }
     if (t.has_dt) {
       // der exp(u) = u' exp(u), der sqrt(u) = u' / 2 / sqrt(u): the result's
       // value is exp(u) / sqrt(u) itself
       r.has_dt = true;
       const DVal& d = t.dt[0];
-      if (kind == EXP) r.dt.push_back(d * r.vt[0]);
-      else if (kind == SQRT) r.dt.push_back(d.zero ? d : d / 2. / r.vt[0]);
-      else r.dt.push_back(d / v);
+      switch (kind) {
+        case EXP: r.dt.push_back(d * r.vt[0]); break;
+        case SQRT: r.dt.push_back(d.zero ? d : d / 2. / r.vt[0]); break;
+        case LOG: r.dt.push_back(d / v); break;
+        case COS: r.dt.push_back(d.zero ? d : -d * vd_sin(v)); break;
+        case SIN: r.dt.push_back(d.zero ? d : d * vd_cos(v)); break;
+        case COSH: r.dt.push_back(d.zero ? d : d * vd_sinh(v)); break;
+        case SINH: r.dt.push_back(d.zero ? d : d * vd_cosh(v)); break;
+        case ATANH: r.dt.push_back(d.zero ? d : d / (1.0 - v * v)); break;
+      }
     }
     return r;
   }
@@ -1070,7 +1124,7 @@ OpePtr parse_ope(const System& sys, int dd, const std::string& expr, int bound) 
   static const U unis[] = {{"Lap", OpeUnary::LAP},       {"lap", OpeUnary::LAP},        {"dn", OpeUnary::DN},
                            {"multr", OpeUnary::MULTR},   {"dr", OpeUnary::DR},          {"divr", OpeUnary::DIVR},
                            {"divsint", OpeUnary::DIVSINT}, {"multsint", OpeUnary::MULTSINT},
-                           {"divcost", OpeUnary::DIVCOST}};
+                           {"divcost", OpeUnary::DIVCOST}, {"ddr", OpeUnary::DDR}};
   for (const auto& u : unis)
     if (is_ope_uni(name, p1, u.n)) {
       if (u.k == OpeUnary::DN && bound < 0) throw KdError(KD_ERR_ARG, "dn() needs a boundary");
@@ -1087,6 +1141,12 @@ OpePtr parse_ope(const System& sys, int dd, const std::string& expr, int bound) 
     return std::make_shared<OpeFunc>(dd, OpeFunc::SQRT, parse_ope(sys, dd, p1, bound));
   if (is_ope_uni(name, p1, "exp")) return std::make_shared<OpeFunc>(dd, OpeFunc::EXP, parse_ope(sys, dd, p1, bound));
   if (is_ope_uni(name, p1, "log")) return std::make_shared<OpeFunc>(dd, OpeFunc::LOG, parse_ope(sys, dd, p1, bound));
+  // the order of give_ope.cpp:834-867
+  static const std::pair<const char*, OpeFunc::Kind> funcs[] = {
+      {"atanh", OpeFunc::ATANH}, {"cos", OpeFunc::COS}, {"sin", OpeFunc::SIN}, {"cosh", OpeFunc::COSH},
+      {"sinh", OpeFunc::SINH}};
+  for (const auto& f : funcs)
+    if (is_ope_uni(name, p1, f.first)) return std::make_shared<OpeFunc>(dd, f.second, parse_ope(sys, dd, p1, bound));
   if (is_ope_uni2(name, p1, p2, "scal"))
     return std::make_shared<OpeScal>(dd, parse_ope(sys, dd, p1, bound), parse_ope(sys, dd, p2, bound));
   // partial_x(f) etc.

@@ -617,6 +617,14 @@ class VD:
         self.coef_i()
         return VD(self.dom, self.B, c=np.log(self.c), base=self.base)
 
+    def atanh(self):
+        """atanh(Val_domain) (val_domain_math.cpp:506): at the collocation
+        points, the basis kept."""
+        if self.zero:
+            return self
+        self.coef_i()
+        return VD(self.dom, self.B, c=np.arctanh(self.c), base=self.base)
+
 
 def radius_vd(dom):
     return VD(dom, 1, c=dom.radius()[None])
@@ -694,6 +702,16 @@ def der_normal(so, bound):
         r = opc(opc(so.der_var(1), S.OP_MULT_XM1, 0), S.OP_MULT_XM1, 0)
         return r * (-d.alpha)
     return so.der_var(1) / d.alpha
+
+
+def der_r(so):
+    """Domain_nucleus::der_r and Domain_shell::der_r (domain_nucleus_ope.cpp:238,
+    domain_shell_ope.cpp:218): der_var(1) / alpha; Domain_compact::der_r
+    (domain_compact_ope.cpp:187): -alpha (x - 1)^2 der_var(1).  In these
+    domains that is der_normal at either boundary."""
+    if so.zero:
+        return so
+    return der_normal(so, OUTER_BC)
 
 
 def mult_r(so):
@@ -947,6 +965,16 @@ class OTerm:
         """Ope_log: der = u' / u."""
         v = self.val.log()
         return OTerm(self.dom, v, None if self.der is None else self.der / self.val)
+
+    def atanh(self):
+        """Ope_atanh (src/Ope_eq/ope_atanh.cpp): der = u' / (1 - u u)."""
+        v = self.val.atanh()
+        return OTerm(self.dom, v, None if self.der is None else self.der / (self.val * self.val).rsub(1.0))
+
+    def ddr(self):
+        """Ope_ddr (src/Ope_eq/ope_ddr.cpp, Domain::ddr in domain.cpp:1522):
+        der_r twice, value and tangent."""
+        return OTerm(self.dom, der_r(der_r(self.val)), None if self.der is None else der_r(der_r(self.der)))
 
     def dn(self, bound):
         return OTerm(self.dom, der_normal(self.val, bound), None if self.der is None else

@@ -17,6 +17,8 @@ small .npz fixtures next to it:
   (13, 7, 4); Lap(psi) + 2 pi rho psi^5 = 0): sec_member at the initial
   guess, Jacobian columns from do_col_J, do_JX of a seeded vector, and every
   do_newton_seq iterate with its pre-step error;
+* ref_funcs.npz -- the same system at (9, 5, 4) with cos, sin, cosh, sinh of
+  a double constant, atanh of the field and ddr (FUNCS_EQUATION);
 * ref_star_<nr><nt><np>.npz -- the isolated star with the shift as a
   Cartesian vector in index notation (the equations of
   kadath_frontera_gb300.workloads.STAR_VECTOR_EQUATIONS), at (9, 5, 4) with
@@ -234,7 +236,7 @@ def system_dumps(spec_body, w: Path, n_unknowns, cols, seed, newton=True):
     return out
 
 
-def make_toy(dest: Path, res=(13, 7, 4)):
+def make_toy(dest: Path, res=(13, 7, 4), equation=TOY_EQUATION, extra_csts=()):
     doms = K.space_spheric(res, [1.0, 2.0])
     rho = toy_rho(doms)
     nd = len(doms)
@@ -245,8 +247,10 @@ def make_toy(dest: Path, res=(13, 7, 4)):
         body = f"space {res[0]} {res[1]} {res[2]} 2 1.0 2.0\nsystem 0 {nd - 1}\n"
         body += "scalar psi std 1\nscalar rho std rho.bin\nvar psi\ncst rho\n"
         body += f"cstd pi {math.pi!r}\n"
+        for name, value in extra_csts:
+            body += f"cstd {name} {value!r}\n"
         for d in range(nd):
-            body += f"inside {d} | {TOY_EQUATION}\n"
+            body += f"inside {d} | {equation}\n"
         for d in range(nd - 1):
             body += f"matching {d} 1 | psi\nmatching {d} 1 | dn(psi)\n"
         body += f"bc {nd - 1} 1 | psi = 1\n"
@@ -258,8 +262,19 @@ def make_toy(dest: Path, res=(13, 7, 4)):
         out = system_dumps(body, w, N, cols, seed=7)
     out["res"] = np.array(res)
     out["rho"] = np.concatenate(rho)
+    out["equation"] = np.array(equation)
+    for name, value in extra_csts:
+        out["cst_" + name] = np.array(value)
     np.savez_compressed(dest, **out)
     print(f"  N = {N}, errors {out['errors']}")
+
+
+# cos, sin, cosh, sinh of a double constant, atanh of a field and ddr
+# (src/Ope_eq/ope_cos.cpp, ope_sin.cpp, ope_cosh.cpp, ope_sinh.cpp,
+# ope_atanh.cpp, ope_ddr.cpp).  With a field argument the reference's cos,
+# sin, cosh and sinh give a value without a basis, which its equations
+# cannot use, so those appear here on numbers only.
+FUNCS_EQUATION = "Lap(psi) + 2*pi*rho*psi^5*cos(amp) + rho*atanh(psi/4)*sinh(amp) + 0.01*sin(amp)*cosh(amp)*ddr(psi) = 0"
 
 
 def make_star(dest: Path, res, with_cols):
@@ -297,6 +312,7 @@ CASES = {
     "spectral": lambda: make_spectral(HERE / "ref_spectral_1d.npz"),
     "coef3d": lambda: make_coef3d(HERE / "ref_coef3d.npz"),
     "toy": lambda: make_toy(HERE / "ref_toy.npz"),
+    "funcs": lambda: make_toy(HERE / "ref_funcs.npz", (9, 5, 4), FUNCS_EQUATION, (("amp", 0.3),)),
     "star954": lambda: make_star(HERE / "ref_star_954.npz", (9, 5, 4), True),
     "star1394": lambda: make_star(HERE / "ref_star_1394.npz", (13, 9, 4), False),
 }

@@ -178,3 +178,56 @@ def test_timed_star_1394_matches_the_reference(ctx, form):
     diff = rel(fmx, f64)
     print(f"{form}: worst iterate vs reference fp64 {w64:.2e} mixed {wmx:.2e}; mixed vs fp64 {diff:.2e}")
     assert diff < FIELD
+
+
+def _funcs_system(z):
+    """The toy system with cos, sin, cosh, sinh of a double constant, atanh of
+    the field and ddr, as tests/golden/make_ref_vectors.py gives it to the
+    reference."""
+    import math
+    from types import SimpleNamespace
+    from kadath_frontera_gb300.kadath import CHEB_TYPE, OUTER_BC, Scalar, Space_spheric, System_of_eqs
+    res = tuple(int(v) for v in z["res"])
+    space = Space_spheric(CHEB_TYPE, (0, 0, 0), res, (1.0, 2.0))
+    pts, _, _ = _shapes(space)
+    nd = space.get_nbr_domains()
+    psi = Scalar(space, 1.0).std_base()
+    rho = Scalar(space)
+    for d, v in enumerate(split(z["rho"], pts)):
+        rho.set_domain(d, v)
+    rho.std_base()
+    syst = System_of_eqs(space, 0, nd - 1)
+    syst.add_var("psi", psi)
+    syst.add_cst("rho", rho)
+    syst.add_cst("pi", math.pi)
+    syst.add_cst("amp", float(z["cst_amp"]))
+    for d in range(nd):
+        syst.add_eq_inside(d, str(z["equation"]))
+    for d in range(nd - 1):
+        syst.add_eq_matching(d, OUTER_BC, "psi")
+        syst.add_eq_matching(d, OUTER_BC, "dn(psi)")
+    syst.add_eq_bc(nd - 1, OUTER_BC, "psi = 1")
+    return SimpleNamespace(space=space, syst=syst, unknowns=[("psi", psi)])
+
+
+@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+def test_trig_atanh_ddr_match_the_reference(ctx, mode):
+    """cos/sin/cosh/sinh of a number, atanh of a field and ddr (Ope_cos,
+    Ope_sin, Ope_cosh, Ope_sinh, Ope_atanh, Ope_ddr): F, Jacobian columns,
+    J x and every Newton iterate against the reference's own."""
+    z = np.load(GOLD / "ref_funcs.npz")
+    check_system(_funcs_system(z), z, _lu(mode))
+
+
+def test_trig_of_a_field_has_no_basis(ctx):
+    """cos of a field gives values without a basis (Val_domain cos,
+    src/Val_domain/val_domain_math.cpp:75): an equation that needs their
+    coefficients is refused with KD_ERR_STATE, where the reference stops."""
+    from kadath_frontera_gb300 import KadathError
+    from kadath_frontera_gb300._lib import KD_ERR_STATE
+    z = dict(np.load(GOLD / "ref_funcs.npz"))
+    z["equation"] = np.array("Lap(psi) + rho*cos(psi) = 0")
+    wl = _funcs_system(z)
+    with pytest.raises(KadathError) as e:
+        wl.syst.do_newton(1e-10)
+    assert e.value.status == KD_ERR_STATE

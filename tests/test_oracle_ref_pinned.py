@@ -141,3 +141,41 @@ def test_star_residual_at_the_timed_size_matches_the_reference():
     # spectral second derivatives); the other tests compare at 1e-13 max|J|
     # and max|J| is far above 1 at this resolution
     assert np.abs(F - z["F0"]).max() < 1e-13
+
+
+def test_trig_atanh_ddr_match_the_reference():
+    """cos/sin/cosh/sinh of a number, atanh of the field and ddr in the toy
+    system (tests/golden/ref_funcs.npz, made by the reference): F, Jacobian
+    columns, J x and every Newton iterate."""
+    import math
+    z = np.load(GOLD / "ref_funcs.npz")
+    res = tuple(int(v) for v in z["res"])
+    amp = float(z["cst_amp"])
+    doms = K.space_spheric(res, [1.0, 2.0])
+    nd = len(doms)
+    psi = K.scalar_field(doms, lambda d: np.ones(d.np))
+    rho = K.scalar_field(doms, CF.toy_rho)
+    got_rho = np.concatenate([np.asarray(rho[d.num].c).ravel() for d in doms])
+    assert np.array_equal(got_rho, z["rho"])
+    sysm = K.OSystem(doms, 0, nd - 1)
+    sysm.add_var("psi", psi)
+    for d in range(nd):
+        rh = rho[d]
+
+        # Lap(psi) + 2*pi*rho*psi^5*cos(amp) + rho*atanh(psi/4)*sinh(amp)
+        #   + 0.01*sin(amp)*cosh(amp)*ddr(psi), in the parser's order
+        def eq(T, b, rh=rh):
+            p = T["psi"]
+            zero = None if p.der is None else K.VD.zeros(rh.dom, p.der.B)
+            rho_t = K.OTerm(p.dom, rh, zero)
+            c = K.OTerm(p.dom, 2 * math.pi, None if p.der is None else 0.0)
+            t1 = ((c * rho_t) * p ** 5) * math.cos(amp)
+            t2 = (rho_t * (p / 4.0).atanh()) * math.sinh(amp)
+            t3 = ((0.01 * math.sin(amp)) * math.cosh(amp)) * p.ddr()
+            return ((p.lap() + t1) + t2) + t3
+        sysm.add_eq_inside(d, eq)
+    for d in range(nd - 1):
+        sysm.add_eq_matching(d, K.OUTER_BC, lambda T, b: T["psi"])
+        sysm.add_eq_matching(d, K.OUTER_BC, lambda T, b: T["psi"].dn(b))
+    sysm.add_eq_bc(nd - 1, K.OUTER_BC, lambda T, b: T["psi"] - 1.0)
+    _check_system(sysm, [psi], doms, z)
