@@ -556,6 +556,21 @@ DVal der_normal(const DVal& so, int bound) {
   return so.der_var(1) / d->alpha;
 }
 
+// Domain_nucleus::laplacian2 (domain_nucleus_ope.cpp:250), Domain_shell
+// (domain_shell_ope.cpp:271), Domain_compact (domain_compact_ope.cpp:217),
+// for m = 0 (no m quantum number is set by the equations here).
+DVal laplacian2(const DVal& so) {
+  const Domain* d = so.dom;
+  const DVal dert = so.der_var(2);
+  if (d->type == DOM_COMPACT) {
+    const DVal derr = mult_xm1(mult_xm1(so.der_var(1))) * (-d->alpha);
+    const DVal dderr = mult_xm1(mult_xm1(derr.der_var(1))) * (-d->alpha);
+    return dderr + div_r(derr + div_r(dert.der_var(2)));
+  }
+  const DVal derr = so.der_var(1) / d->alpha;
+  return derr.der_var(1) / d->alpha + div_r(derr + div_r(dert.der_var(2)));
+}
+
 DVal laplacian(const DVal& so) {
   DVal res = so.der_abs(1).der_abs(1);
   for (int j = 2; j <= 3; j++) res = res + so.der_abs(j).der_abs(j);

@@ -100,6 +100,8 @@ DVal div_xm1(const DVal& so);
 DVal mult_r(const DVal& so);
 DVal div_r(const DVal& so);
 DVal der_r(const DVal& so);
+// Domain_*::laplacian2 with m = 0 (Ope_lap2): d2/dr2 + (d/dr + d2/dtheta2 / r) / r.
+DVal laplacian2(const DVal& so);
 DVal der_normal(const DVal& so, int bound);
 DVal laplacian(const DVal& so);  // Domain::laplacian (domain.cpp:155)
 DVal radius_field(Context* ctx, const Domain* d);

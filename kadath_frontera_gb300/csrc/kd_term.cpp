@@ -625,7 +625,7 @@ class OpeFunctional : public Ope {
 // Unary operators acting component by component on value and tangent.
 class OpeUnary : public Ope {
  public:
-  enum Kind { LAP, DN, DR, MULTR, DIVR, DIVSINT, MULTSINT, DIVCOST, DDR };
+  enum Kind { LAP, DN, DR, MULTR, DIVR, DIVSINT, MULTSINT, DIVCOST, DDR, LAP2 };
   OpeUnary(int dom, Kind k, int bound, OpePtr a_) : Ope(dom), kind(k), bound(bound), a(std::move(a_)) {
     vc = a->vc;  // linear operators: the tangent is the operator of the tangent
     dc = a->dc;
@@ -643,6 +643,7 @@ class OpeUnary : public Ope {
       case DR: return comp_by_comp(t, [](const DVal& v) { return der_r(v); }, cv);
       // Domain::ddr (src/Domain/domain.cpp:1522): der_r twice (Ope_ddr keeps zero as zero)
       case DDR: return comp_by_comp(t, [](const DVal& v) { return v.zero ? v : der_r(der_r(v)); }, cv);
+      case LAP2: return comp_by_comp(t, [](const DVal& v) { return v.zero ? v : laplacian2(v); }, cv);
       case MULTR: return comp_by_comp(t, [](const DVal& v) { return mult_r(v); }, cv);
       case DIVR: return comp_by_comp(t, [](const DVal& v) { return div_r(v); }, cv);
       case DIVSINT: return comp_by_comp(t, [](const DVal& v) { return div_sin_theta(v); }, cv);
@@ -1124,12 +1125,21 @@ OpePtr parse_ope(const System& sys, int dd, const std::string& expr, int bound) 
   static const U unis[] = {{"Lap", OpeUnary::LAP},       {"lap", OpeUnary::LAP},        {"dn", OpeUnary::DN},
                            {"multr", OpeUnary::MULTR},   {"dr", OpeUnary::DR},          {"divr", OpeUnary::DIVR},
                            {"divsint", OpeUnary::DIVSINT}, {"multsint", OpeUnary::MULTSINT},
-                           {"divcost", OpeUnary::DIVCOST}, {"ddr", OpeUnary::DDR}};
+                           {"divcost", OpeUnary::DIVCOST}, {"ddr", OpeUnary::DDR},
+                           {"Lap2", OpeUnary::LAP2},     {"lap2", OpeUnary::LAP2}};
   for (const auto& u : unis)
     if (is_ope_uni(name, p1, u.n)) {
       if (u.k == OpeUnary::DN && bound < 0) throw KdError(KD_ERR_ARG, "dn() needs a boundary");
       return std::make_shared<OpeUnary>(dd, u.k, bound, parse_ope(sys, dd, p1, bound));
     }
+  // multrsint / divrsint (Ope_mult_rsint, Ope_div_rsint): mult_r then
+  // mult_sin_theta, div_r then div_sin_theta, component by component
+  if (is_ope_uni(name, p1, "multrsint"))
+    return std::make_shared<OpeUnary>(dd, OpeUnary::MULTSINT, bound,
+                                      std::make_shared<OpeUnary>(dd, OpeUnary::MULTR, bound, parse_ope(sys, dd, p1, bound)));
+  if (is_ope_uni(name, p1, "divrsint"))
+    return std::make_shared<OpeUnary>(dd, OpeUnary::DIVSINT, bound,
+                                      std::make_shared<OpeUnary>(dd, OpeUnary::DIVR, bound, parse_ope(sys, dd, p1, bound)));
   if (is_ope_uni(name, p1, "grad")) return std::make_shared<OpeGrad>(dd, parse_ope(sys, dd, p1, bound));
   if (is_ope_uni(name, p1, "integ"))
     return std::make_shared<OpeFunctional>(dd, OpeFunctional::INTEG, parse_ope(sys, dd, p1, bound), bound, nullptr,

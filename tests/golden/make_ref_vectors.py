@@ -17,8 +17,9 @@ small .npz fixtures next to it:
   (13, 7, 4); Lap(psi) + 2 pi rho psi^5 = 0): sec_member at the initial
   guess, Jacobian columns from do_col_J, do_JX of a seeded vector, and every
   do_newton_seq iterate with its pre-step error;
-* ref_funcs.npz -- the same system at (9, 5, 4) with cos, sin, cosh, sinh of
-  a double constant, atanh of the field and ddr (FUNCS_EQUATION);
+* ref_funcs.npz, ref_funcs2.npz -- the same system at (9, 5, 4) with cos,
+  sin, cosh, sinh of a double constant, atanh of the field and ddr
+  (FUNCS_EQUATION), and with lap2, multrsint and divrsint (FUNCS2_EQUATION);
 * ref_star_<nr><nt><np>.npz -- the isolated star with the shift as a
   Cartesian vector in index notation (the equations of
   kadath_frontera_gb300.workloads.STAR_VECTOR_EQUATIONS), at (9, 5, 4) with
@@ -275,6 +276,8 @@ def make_toy(dest: Path, res=(13, 7, 4), equation=TOY_EQUATION, extra_csts=()):
 # sin, cosh and sinh give a value without a basis, which its equations
 # cannot use, so those appear here on numbers only.
 FUNCS_EQUATION = "Lap(psi) + 2*pi*rho*psi^5*cos(amp) + rho*atanh(psi/4)*sinh(amp) + 0.01*sin(amp)*cosh(amp)*ddr(psi) = 0"
+# lap2 (Ope_lap2, Domain_*::laplacian2 with m = 0), multrsint, divrsint
+FUNCS2_EQUATION = "Lap(psi) + 2*pi*rho*psi^5 + 0.01*lap2(psi)*cos(amp) + 0.01*divrsint(multrsint(psi)) = 0"
 
 
 def make_star(dest: Path, res, with_cols):
@@ -313,6 +316,7 @@ CASES = {
     "coef3d": lambda: make_coef3d(HERE / "ref_coef3d.npz"),
     "toy": lambda: make_toy(HERE / "ref_toy.npz"),
     "funcs": lambda: make_toy(HERE / "ref_funcs.npz", (9, 5, 4), FUNCS_EQUATION, (("amp", 0.3),)),
+    "funcs2": lambda: make_toy(HERE / "ref_funcs2.npz", (9, 5, 4), FUNCS2_EQUATION, (("amp", 0.3),)),
     "star954": lambda: make_star(HERE / "ref_star_954.npz", (9, 5, 4), True),
     "star1394": lambda: make_star(HERE / "ref_star_1394.npz", (13, 9, 4), False),
 }

@@ -210,12 +210,14 @@ def _funcs_system(z):
     return SimpleNamespace(space=space, syst=syst, unknowns=[("psi", psi)])
 
 
+@pytest.mark.parametrize("fixture", ["ref_funcs.npz", "ref_funcs2.npz"])
 @pytest.mark.parametrize("mode", ["fp64", "mixed"])
-def test_trig_atanh_ddr_match_the_reference(ctx, mode):
+def test_more_operators_match_the_reference(ctx, mode, fixture):
     """cos/sin/cosh/sinh of a number, atanh of a field and ddr (Ope_cos,
-    Ope_sin, Ope_cosh, Ope_sinh, Ope_atanh, Ope_ddr): F, Jacobian columns,
+    Ope_sin, Ope_cosh, Ope_sinh, Ope_atanh, Ope_ddr); lap2, multrsint and
+    divrsint (Ope_lap2, Ope_mult_rsint, Ope_div_rsint): F, Jacobian columns,
     J x and every Newton iterate against the reference's own."""
-    z = np.load(GOLD / "ref_funcs.npz")
+    z = np.load(GOLD / fixture)
     check_system(_funcs_system(z), z, _lu(mode))
 
 
