@@ -36,6 +36,7 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "Newton-step time (assemble+LU+solve) at 1e-10 residual: FP64 vs mixed-prec"
+TUNING_TABLE = ROOT / "kadath_frontera_gb300" / "tuning" / "line_passes_gb300.json"
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 
 
@@ -219,6 +220,11 @@ def run_gpu(args, ws, rank, local):
     import numpy as np
     import torch
 
+    # the autotuner's table of line-pass launch shapes for this GPU, for
+    # every context this process makes (shapes change no result bit)
+    if TUNING_TABLE.exists() and not args.no_tuning:
+        os.environ["KD_TUNING_FILE"] = str(TUNING_TABLE)
+
     from kadath_frontera_gb300 import Context
     from kadath_frontera_gb300 import kadath as KD
     from kadath_frontera_gb300 import workloads
@@ -391,6 +397,9 @@ def run_gpu(args, ws, rank, local):
                                       "captures_replays": list(syst.graph_stats())},
                    "jacobian_graph": {"on": not args.no_graph,
                                       "captures_replays": list(syst.jacobian_graph_stats())},
+                   "autotuner": dict(ctx.autotune_stats(),
+                                     table=str(TUNING_TABLE.relative_to(ROOT)) if TUNING_TABLE.exists()
+                                     and not args.no_tuning else None),
                    "parallelism": "replicas" if ws > 1 else "single"},
         "fp64_ms_per_step": fp64_ms, "mixed_speedup_vs_fp64": fp64_ms / mixed_ms if mixed_ms > 0 else None,
         "first_step_ms": {"mixed": first_m, "fp64": first_f},
@@ -748,6 +757,8 @@ def main():
     ap.add_argument("--batch-threads", type=int, default=8)
     ap.add_argument("--gemm", default=None, metavar="M,N,K",
                     help="only the tensor-core trailing update at this shape")
+    ap.add_argument("--no-tuning", action="store_true",
+                    help="line passes with the fixed launch-shape rule instead of the autotuner's table")
     ap.add_argument("--no-graph", action="store_true",
                     help="run the residual's value pass without CUDA-graph replay")
     ap.add_argument("--large", action="store_true",

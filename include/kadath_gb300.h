@@ -63,6 +63,19 @@ int kd_ctx_set_sm_budget(kd_ctx* ctx, int sms);
  * kd_ctx_stall_waits(ctx, 0) restores normal operation. */
 int kd_ctx_set_wait_limit(kd_ctx* ctx, double seconds);
 int kd_ctx_stall_waits(kd_ctx* ctx, int on);
+/* The project's autotuner (no reference counterpart): launch shapes of the
+ * spectral line passes (one CTA of 64, 128 or 256 threads per field, or a
+ * cluster of 2, 4 or 8 CTAs per field) per shape class of a launch (number
+ * of fields, largest stage, passes).  mode 0: a fixed rule; 1: the shapes of
+ * the JSON table at `path` (the fixed rule for classes it lacks); 2: as 1,
+ * and a class met for the first time outside a graph capture is timed
+ * (every candidate, CUDA events, outputs to a scratch buffer), its fastest
+ * shape added and the table written back to `path`.  Shapes change no
+ * result bit.  Stats: table entries, classes timed by this context, launches
+ * that used a table entry.  A context starts in mode 1 with the table named
+ * by the environment variable KD_TUNING_FILE when it is set. */
+int kd_ctx_autotune(kd_ctx* ctx, const char* path, int mode);
+int kd_ctx_autotune_stats(const kd_ctx* ctx, long long* entries, long long* tuned, long long* hits);
 const char* kd_last_error(const kd_ctx* ctx);
 int kd_ctx_synchronize(kd_ctx* ctx);
 /* Number of kernels this context has launched so far. */

@@ -59,6 +59,8 @@ def _declare(lib: C.CDLL) -> None:
         "kd_ctx_set_sm_budget": (I, [P, I]),
         "kd_ctx_set_wait_limit": (I, [P, C.c_double]),
         "kd_ctx_stall_waits": (I, [P, I]),
+        "kd_ctx_autotune": (I, [P, C.c_char_p, I]),
+        "kd_ctx_autotune_stats": (I, [P, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
         "kd_last_error": (C.c_char_p, [P]),
         "kd_ctx_synchronize": (I, [P]),
         "kd_ctx_launch_count": (C.c_longlong, [P]),
@@ -127,6 +129,18 @@ class Context:
     def stall_waits(self, on: bool) -> None:
         """Failure injection for tests: no grid barrier completes while on."""
         self.check(self.lib.kd_ctx_stall_waits(self.h, 1 if on else 0))
+
+    def autotune(self, path=None, mode: int = 1) -> None:
+        """Launch shapes of the spectral line passes from the JSON table at
+        `path` (mode 1), also timing the shape classes it lacks and saving it
+        (mode 2), or the fixed rule (mode 0)."""
+        p = None if path is None else str(path).encode()
+        self.check(self.lib.kd_ctx_autotune(self.h, p, int(mode)))
+
+    def autotune_stats(self) -> dict:
+        e, t, h = C.c_longlong(), C.c_longlong(), C.c_longlong()
+        self.check(self.lib.kd_ctx_autotune_stats(self.h, C.byref(e), C.byref(t), C.byref(h)))
+        return {"entries": e.value, "tuned": t.value, "hits": h.value}
 
     @property
     def launches(self) -> int:

@@ -139,6 +139,19 @@ int kd_ctx_set_wait_limit(kd_ctx* ctx, double seconds) {
   return KD_OK;
 }
 
+int kd_ctx_autotune(kd_ctx* ctx, const char* path, int mode) {
+  if (!ctx || !ctx->c) return KD_ERR_ARG;
+  return guarded(ctx, [&] { ctx->c->set_autotune(path ? std::string(path) : std::string(), mode); });
+}
+
+int kd_ctx_autotune_stats(const kd_ctx* ctx, long long* entries, long long* tuned, long long* hits) {
+  if (!ctx || !ctx->c || !entries || !tuned || !hits) return KD_ERR_ARG;
+  *entries = static_cast<long long>(ctx->c->tuner.table.size());
+  *tuned = ctx->c->tuner.tuned;
+  *hits = ctx->c->tuner.hits;
+  return KD_OK;
+}
+
 int kd_ctx_stall_waits(kd_ctx* ctx, int on) {
   if (!ctx || !ctx->c) return KD_ERR_ARG;
   ctx->c->stall_waits = on ? 1 : 0;

@@ -1,6 +1,9 @@
 #include "kd_context.hpp"
 
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <sstream>
 
 namespace kd {
@@ -67,6 +70,9 @@ Context::Context(int device) : device_(device) {
   cur_ = stream_;
   pool_cap_ = size_t(4) << 20;  // 4 Mi doubles = 32 MB of operator matrices
   cuda_check(cudaMalloc(&d_pool_, pool_cap_ * sizeof(double)), "cudaMalloc(matrix pool)");
+  // a table of the autotuner for every context of the process (mode 1)
+  if (const char* p = std::getenv("KD_TUNING_FILE"))
+    if (*p) set_autotune(p, 1);
 }
 
 Context::~Context() {
@@ -217,8 +223,9 @@ void Context::run_items(const std::vector<KdItem>& items, const std::vector<int>
       }
       flops += f * (list.prefix[q + 1] - list.prefix[q]);
     }
+    const LpShape sh = line_shape(list, smem, dp);
     ProfScope ps(this, PROF_LINE_PASS, flops);
-    cuda_check(launch_line_passes(list, smem, dp, stream()), "line_passes kernel");
+    cuda_check(launch_line_passes(list, smem, dp, stream(), sh), "line_passes kernel");
     launches++;
   }
 }
@@ -300,6 +307,161 @@ void Context::prof_read(double* ms, long long* count, double* work) {
     count[r.cat] += 1;
     work[r.cat] += r.work;
   }
+}
+
+}  // namespace kd
+
+namespace kd {
+
+// ------------------------------------------------------------ autotuner --
+std::string LineTuner::key(const KdItemList& list, int smem_doubles) {
+  const int nf = list.prefix[list.nitems];
+  static const int fb[] = {1, 2, 4, 8, 16, 32, 64, 152, 512, 2048};
+  int fhi = 0;
+  for (int b : fb)
+    if (nf <= b) {
+      fhi = b;
+      break;
+    }
+  int e = 64;
+  while (e < smem_doubles) e *= 2;
+  int np = 0;
+  for (int i = 0; i < list.nitems; i++)
+    if (list.items[i].npass > np) np = list.items[i].npass;
+  std::ostringstream os;
+  os << "f" << (fhi ? std::to_string(fhi) : std::string("big")) << "/e" << e << "/p" << np;
+  return os.str();
+}
+
+// The table as written by save(): {"line_passes": {"<class>": {"cluster": c,
+// "threads": t, "us": x}, ...}}.
+void LineTuner::load(const std::string& p) {
+  std::ifstream f(p);
+  if (!f) return;
+  std::stringstream ss;
+  ss << f.rdbuf();
+  const std::string s = ss.str();
+  size_t at = s.find("\"line_passes\"");
+  if (at == std::string::npos) return;
+  at = s.find('{', at);
+  while (at != std::string::npos) {
+    const size_t k0 = s.find('"', at + 1);
+    if (k0 == std::string::npos) break;
+    const size_t k1 = s.find('"', k0 + 1);
+    const size_t b0 = s.find('{', k1);
+    const size_t b1 = s.find('}', b0);
+    if (k1 == std::string::npos || b0 == std::string::npos || b1 == std::string::npos) break;
+    const std::string k = s.substr(k0 + 1, k1 - k0 - 1);
+    const std::string body = s.substr(b0, b1 - b0 + 1);
+    Entry en;
+    auto num = [&](const char* name, double& out) {
+      const size_t q = body.find(std::string("\"") + name + "\"");
+      if (q == std::string::npos) return false;
+      const size_t c = body.find(':', q);
+      out = std::atof(body.c_str() + c + 1);
+      return true;
+    };
+    double cl = 1, th = 128, us = 0;
+    if (num("cluster", cl) && num("threads", th)) {
+      num("us", us);
+      en.shape.cluster = static_cast<int>(cl);
+      en.shape.threads = static_cast<int>(th);
+      en.us = us;
+      table[k] = en;
+    }
+    at = s.find(',', b1);
+    if (at == std::string::npos || s.find('"', at) == std::string::npos) break;
+  }
+}
+
+void LineTuner::save() const {
+  if (path.empty()) return;
+  std::ofstream f(path);
+  if (!f) return;
+  f << "{\n  \"line_passes\": {";
+  bool first = true;
+  for (const auto& kv : table) {
+    f << (first ? "\n" : ",\n") << "    \"" << kv.first << "\": {\"cluster\": " << kv.second.shape.cluster
+      << ", \"threads\": " << kv.second.shape.threads << ", \"us\": " << kv.second.us << "}";
+    first = false;
+  }
+  f << "\n  }\n}\n";
+}
+
+void Context::set_autotune(const std::string& path, int mode) {
+  if (mode < 0 || mode > 2) throw KdError(KD_ERR_ARG, "autotune mode must be 0, 1 or 2");
+  tuner.mode = mode;
+  tuner.path = path;
+  tuner.table.clear();
+  if (mode > 0 && !path.empty()) tuner.load(path);
+}
+
+LpShape Context::line_shape(const KdItemList& list, int smem_doubles, const double* pool) {
+  const int nf = list.prefix[list.nitems];
+  if (tuner.mode == 0 || nf <= 0) return lp_default_shape(nf);
+  const std::string k = LineTuner::key(list, smem_doubles);
+  auto it = tuner.table.find(k);
+  if (it != tuner.table.end()) {
+    tuner.hits++;
+    return it->second.shape;
+  }
+  if (tuner.mode < 2 || capturing || prof_on_) return lp_default_shape(nf);
+  // Time every candidate shape on copies of the launch whose outputs go to
+  // a scratch buffer (the real outputs may alias the inputs).
+  KdItemList probe = list;
+  size_t total = 0;
+  std::vector<size_t> need(list.nitems);
+  for (int i = 0; i < list.nitems; i++) {
+    const KdItem& itm = list.items[i];
+    int d0 = itm.n0, d1 = itm.n1, d2 = itm.n2;
+    for (int q = 0; q < itm.npass; q++) {
+      if (itm.pass[q].dim == 0) d0 = itm.pass[q].n_out;
+      if (itm.pass[q].dim == 1) d1 = itm.pass[q].n_out;
+      if (itm.pass[q].dim == 2) d2 = itm.pass[q].n_out;
+    }
+    const long long per = std::max<long long>(itm.out_stride, static_cast<long long>(d0) * d1 * d2);
+    need[i] = static_cast<size_t>(list.prefix[i + 1] - list.prefix[i]) * static_cast<size_t>(per);
+    total += need[i];
+  }
+  double* scratch = nullptr;
+  cuda_check(cudaMalloc(&scratch, sizeof(double) * (total ? total : 1)), "cudaMalloc(autotune scratch)");
+  size_t off = 0;
+  for (int i = 0; i < list.nitems; i++) {
+    probe.items[i].out = scratch + off;
+    off += need[i];
+  }
+  std::vector<LpShape> cands;
+  if (nf <= 64)
+    for (int cl : {8, 4, 2}) cands.push_back({cl, 128});
+  for (int th : {64, 128, 256}) cands.push_back({1, th});
+  cudaStream_t s = stream();
+  cudaEvent_t e0, e1;
+  cuda_check(cudaEventCreate(&e0), "cudaEventCreate");
+  cuda_check(cudaEventCreate(&e1), "cudaEventCreate");
+  LpShape best = lp_default_shape(nf);
+  double best_us = 1e30;
+  constexpr int reps = 5;
+  for (const LpShape& c : cands) {
+    cuda_check(launch_line_passes(probe, smem_doubles, pool, s, c), "autotune warm-up");
+    cuda_check(cudaEventRecord(e0, s), "cudaEventRecord");
+    for (int r = 0; r < reps; r++) cuda_check(launch_line_passes(probe, smem_doubles, pool, s, c), "autotune run");
+    cuda_check(cudaEventRecord(e1, s), "cudaEventRecord");
+    cuda_check(cudaEventSynchronize(e1), "autotune sync");
+    float ms = 0;
+    cuda_check(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+    const double us = 1e3 * ms / reps;
+    if (us < best_us) {
+      best_us = us;
+      best = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(scratch);
+  tuner.table[k] = {best, best_us};
+  tuner.tuned++;
+  tuner.save();
+  return best;
 }
 
 }  // namespace kd

@@ -45,6 +45,24 @@ class DeviceArena {
   size_t cur_chunk_ = 0, off_ = 0, chunk_;
 };
 
+// Launch shapes of the line passes picked by timing (the project's
+// autotuner): per shape class of a launch (fields, largest stage, passes)
+// the fastest candidate shape, kept in a JSON table.
+class LineTuner {
+ public:
+  int mode = 0;  // 0: default rule; 1: the table (default rule for classes it lacks); 2: also time the classes it lacks and save
+  std::string path;
+  struct Entry {
+    LpShape shape;
+    double us = 0;
+  };
+  std::map<std::string, Entry> table;
+  long long tuned = 0, hits = 0;
+  void load(const std::string& p);
+  void save() const;
+  static std::string key(const KdItemList& list, int smem_doubles);
+};
+
 class Context {
  public:
   explicit Context(int device);
@@ -129,6 +147,13 @@ class Context {
     PROF_LU_PANEL_STATIC = 8,  // static-pivot panels (work: bytes, the panel read and written once)
     PROF_NCAT = 9,
   };
+  // The autotuner of the line passes (see LineTuner); path "" keeps the
+  // table in memory only.
+  void set_autotune(const std::string& path, int mode);
+  LineTuner tuner;
+  // The shape for one line-pass launch: the table's, or the default rule; in
+  // mode 2 an unknown class is timed first (never during a capture).
+  LpShape line_shape(const KdItemList& list, int smem_doubles, const double* pool);
   void prof_enable(bool on);
   bool prof_on() const { return prof_on_; }
   void prof_begin(int cat);

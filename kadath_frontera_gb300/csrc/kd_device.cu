@@ -120,13 +120,13 @@ __global__ void line_passes_kernel(const __grid_constant__ KdItemList list, cons
   }
 }
 
-// Small batches: one 8-CTA cluster per field.  Each CTA computes every
-// 8th block of a pass's outputs and stores them into all eight CTAs' shared
-// buffers (distributed shared memory), then one cluster barrier; the last
-// pass writes straight to global memory.  A field's FP64 work is spread over
-// eight SMs instead of one.
-constexpr int LP_CL = 8;
+// Small batches: one LP_CL-CTA cluster per field.  Each CTA computes every
+// LP_CL-th block of a pass's outputs and stores them into all the cluster's
+// shared buffers (distributed shared memory), then one cluster barrier; the
+// last pass writes straight to global memory.  A field's FP64 work is spread
+// over LP_CL SMs instead of one.
 constexpr int LP_CLUSTER_MAX_FIELDS = 32;
+template <int LP_CL>
 __global__ void line_passes_cluster_kernel(const __grid_constant__ KdItemList list, const double* __restrict__ pool) {
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
@@ -276,6 +276,31 @@ __global__ void absmax_kernel(const double* __restrict__ x, long long n, double*
   }
 }
 
+template <int CL>
+cudaError_t launch_lp_cluster(const KdItemList& list, int total_fields, size_t smem, const double* d_pool,
+                              cudaStream_t s) {
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(line_passes_cluster_kernel<CL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(total_fields * CL, 1, 1);
+  cfg.blockDim = dim3(128, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = CL;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaError_t e = cudaLaunchKernelEx(&cfg, line_passes_cluster_kernel<CL>, list, d_pool);
+  if (e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
 int grid_for(long long n, int threads) {
   long long g = (n + threads - 1) / threads;
   if (g < 1) g = 1;
@@ -285,42 +310,37 @@ int grid_for(long long n, int threads) {
 
 }  // namespace
 
-cudaError_t launch_line_passes(const KdItemList& list, int smem_doubles, const double* d_pool,
-                               cudaStream_t s) {
+LpShape lp_default_shape(int total_fields) {
+  LpShape sh;
+  if (total_fields <= LP_CLUSTER_MAX_FIELDS) sh.cluster = 8;
+  return sh;
+}
+
+cudaError_t launch_line_passes(const KdItemList& list, int smem_doubles, const double* d_pool, cudaStream_t s,
+                               LpShape shape) {
   const int total_fields = list.prefix[list.nitems];
   if (total_fields <= 0) return cudaSuccess;
   size_t smem = static_cast<size_t>(smem_doubles) * 2 * sizeof(double);
+  switch (shape.cluster) {
+    case 2: return launch_lp_cluster<2>(list, total_fields, smem, d_pool, s);
+    case 4: return launch_lp_cluster<4>(list, total_fields, smem, d_pool, s);
+    case 8: return launch_lp_cluster<8>(list, total_fields, smem, d_pool, s);
+    default: break;
+  }
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(line_passes_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
   }
-  if (total_fields <= LP_CLUSTER_MAX_FIELDS) {
-    // few fields: eight SMs per field
-    if (smem > 48 * 1024) {
-      cudaError_t e = cudaFuncSetAttribute(line_passes_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           static_cast<int>(smem));
-      if (e != cudaSuccess) return e;
-    }
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(total_fields * LP_CL, 1, 1);
-    cfg.blockDim = dim3(128, 1, 1);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = s;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = LP_CL;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    cudaError_t e = cudaLaunchKernelEx(&cfg, line_passes_cluster_kernel, list, d_pool);
-    if (e != cudaSuccess) return e;
-    return cudaGetLastError();
-  }
+  const int threads = (shape.threads == 64 || shape.threads == 256) ? shape.threads : 128;
   int grid = total_fields < 152 * 8 ? total_fields : 152 * 8;
-  line_passes_kernel<<<grid, 128, smem, s>>>(list, d_pool);
+  line_passes_kernel<<<grid, threads, smem, s>>>(list, d_pool);
   return cudaGetLastError();
+}
+
+cudaError_t launch_line_passes(const KdItemList& list, int smem_doubles, const double* d_pool,
+                               cudaStream_t s) {
+  return launch_line_passes(list, smem_doubles, d_pool, s, lp_default_shape(list.prefix[list.nitems]));
 }
 
 cudaError_t launch_ew(int op, long long npts, int ba, const double* a, int bb, const double* b, double* out,

@@ -43,7 +43,23 @@ struct KdItemList {
   KdItem items[KD_MAX_ITEMS];
 };
 
-// Runs the pass lists of all items; one CTA per field.
+// Launch shape of a line-pass launch: one CTA of `threads` threads per field
+// (cluster = 1), or a cluster of `cluster` CTAs (2, 4 or 8) of 128 threads
+// per field, each CTA computing every cluster-th block of a pass's outputs.
+// Every output value is summed in the same order whatever the shape, so the
+// shape changes no result bit.
+struct LpShape {
+  int cluster = 1;
+  int threads = 128;
+};
+// The rule without a tuning table: 8-CTA clusters up to 32 fields, else one
+// 128-thread CTA per field.
+LpShape lp_default_shape(int total_fields);
+
+// Runs the pass lists of all items with the given shape (default rule: the
+// overload without one).
+cudaError_t launch_line_passes(const KdItemList& list, int smem_doubles, const double* d_pool,
+                               cudaStream_t s, LpShape shape);
 cudaError_t launch_line_passes(const KdItemList& list, int smem_doubles, const double* d_pool,
                                cudaStream_t s);
 
