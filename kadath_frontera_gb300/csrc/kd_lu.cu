@@ -507,6 +507,21 @@ __global__ void __launch_bounds__(GEMV_ROWS) gemv_partial(const double* __restri
   const double* a = A + static_cast<long long>(c0) * ld + row;
   double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
   int k = c0;
+  // eight column loads in flight per thread, then the multiply-adds
+  for (; k + 7 < c1; k += 8) {
+    double v[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) v[u] = __ldcs(a + u * ld);
+    s0 = fma(v[0], x[k], s0);
+    s1 = fma(v[1], x[k + 1], s1);
+    s2 = fma(v[2], x[k + 2], s2);
+    s3 = fma(v[3], x[k + 3], s3);
+    s0 = fma(v[4], x[k + 4], s0);
+    s1 = fma(v[5], x[k + 5], s1);
+    s2 = fma(v[6], x[k + 6], s2);
+    s3 = fma(v[7], x[k + 7], s3);
+    a += 8 * ld;
+  }
   for (; k + 3 < c1; k += 4) {
     s0 = fma(a[0], x[k], s0);
     s1 = fma(a[ld], x[k + 1], s1);
@@ -2871,8 +2886,10 @@ void DenseLU::gmres_ir(double* b, int trans) {
   if (bnorm == 0) return;
   int total_it = 0;
   for (int restart = 0; restart < gmres_restarts; restart++) {
-    // r = b - A x
-    {
+    // r = b - A x (x = 0 on the first cycle: r = b, no matvec)
+    if (restart == 0) {
+      cuda_check(cudaMemcpyAsync(r, b, sizeof(double) * N, cudaMemcpyDeviceToDevice, s), "copy b");
+    } else {
       ProfScope ps(ctx_, Context::PROF_GMRES, 8.0 * double(N) * N);
       gemv(x, r, -1.0, 1.0, b, trans);
     }

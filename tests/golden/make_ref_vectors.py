@@ -13,6 +13,10 @@ small .npz fixtures next to it:
 * ref_coef3d.npz -- Base_spectral::coef / coef_i (src/Coef/coef.cpp:96,
   coef_i.cpp:96) of seeded fields in the nucleus, shell and compactified
   domain, for the standard, anti-symmetric and Cartesian-component bases;
+* ref_coef3_bases.npz -- Base_spectral::coef / coef_i with the bispheric
+  domains' bases (COS / SIN in phi, CHEB_EVEN / CHEB_ODD in chi, CHEB in eta)
+  and with the COSSIN_EVEN / COSSIN_ODD phi bases (oracle/ref_drivers/
+  ref_coef3.cpp);
 * ref_toy.npz -- the CPU-runnable configuration (nucleus, shell, compact,
   (13, 7, 4); Lap(psi) + 2 pi rho psi^5 = 0): sec_member at the initial
   guess, Jacobian columns from do_col_J, do_JX of a seeded vector, and every
@@ -311,9 +315,59 @@ def make_star(dest: Path, res, with_cols):
     print(f"  N = {N}, errors {out['errors']}")
 
 
+# Base_spectral::coef / coef_i with the bases of the bispheric domains
+# (domain_bispheric_rect.cpp:466-500: COS or SIN in phi, CHEB_EVEN / CHEB_ODD
+# in chi by the parity of the phi index, CHEB in eta; points = coefficients)
+# and with the COSSIN_EVEN / COSSIN_ODD phi bases, through oracle/ref_drivers/
+# ref_coef3.cpp.
+def coef3_cases():
+    cases = []
+    n = 9
+    for name, bp in (("bispheric_std", S.COS), ("bispheric_anti", S.SIN)):
+        bt = [S.CHEB_EVEN if k % 2 == 0 else S.CHEB_ODD for k in range(n)]
+        br = [[S.CHEB] * n for _ in range(n)]
+        cases.append((name, (n, n, n), (n, n, n), bp, bt, br))
+    for name, bp in (("cossin_even", S.COSSIN_EVEN), ("cossin_odd", S.COSSIN_ODD)):
+        np_, nc = (9, 7, 8), (9, 7, 10)
+        bt = [S.COS_EVEN if k % 2 == 0 else S.SIN_EVEN for k in range(nc[2])]
+        br = [[S.CHEB] * nc[2] for _ in range(nc[1])]
+        cases.append((name, np_, nc, bp, bt, br))
+    return cases
+
+
+def make_coef3(dest: Path):
+    rng = np.random.default_rng(31)
+    out = {}
+    for name, np_, nc, bp, bt, br in coef3_cases():
+        vals = rng.standard_normal(int(np.prod(np_)))
+        cfs = rng.standard_normal(int(np.prod(nc)))
+        lines = [" ".join(map(str, np_ + nc)), str(bp), " ".join(map(str, bt))]
+        lines.append(" ".join(str(br[j][k]) for k in range(nc[2]) for j in range(nc[1])))
+        lines.append(" ".join(repr(float(v)) for v in vals))
+        lines.append(" ".join(repr(float(v)) for v in cfs))
+        r = subprocess.run([str(REF_BIN / "ref_coef3")], input="\n".join(lines) + "\n", capture_output=True,
+                           text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"ref_coef3 failed ({r.returncode}) on {name}: {r.stderr[-500:]}")
+        nums = [float(t) for t in r.stdout.split()[1:]]
+        ncf = int(np.prod(nc))
+        out[f"{name}_np"] = np.array(np_)
+        out[f"{name}_nc"] = np.array(nc)
+        out[f"{name}_bp"] = np.array(bp)
+        out[f"{name}_bt"] = np.array(bt)
+        out[f"{name}_br"] = np.array(br)
+        out[f"{name}_values"] = vals
+        out[f"{name}_coefs_in"] = cfs
+        out[f"{name}_coef"] = np.array(nums[:ncf])
+        out[f"{name}_coef_i"] = np.array(nums[ncf:])
+    np.savez_compressed(dest, **out)
+    print(f"  {len(out) // 9} cases")
+
+
 CASES = {
     "spectral": lambda: make_spectral(HERE / "ref_spectral_1d.npz"),
     "coef3d": lambda: make_coef3d(HERE / "ref_coef3d.npz"),
+    "coef3bases": lambda: make_coef3(HERE / "ref_coef3_bases.npz"),
     "toy": lambda: make_toy(HERE / "ref_toy.npz"),
     "funcs": lambda: make_toy(HERE / "ref_funcs.npz", (9, 5, 4), FUNCS_EQUATION, (("amp", 0.3),)),
     "funcs2": lambda: make_toy(HERE / "ref_funcs2.npz", (9, 5, 4), FUNCS2_EQUATION, (("amp", 0.3),)),

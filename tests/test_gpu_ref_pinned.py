@@ -233,3 +233,32 @@ def test_trig_of_a_field_has_no_basis(ctx):
     with pytest.raises(KadathError) as e:
         wl.syst.do_newton(1e-10)
     assert e.value.status == KD_ERR_STATE
+
+
+@pytest.mark.parametrize("case", ["bispheric_std", "bispheric_anti", "cossin_even", "cossin_odd"])
+def test_transforms_with_bispheric_and_cossin_parity_bases_match_the_reference(ctx, case):
+    """The GPU line passes with the bispheric domains' bases (COS / SIN in
+    phi, CHEB_EVEN / CHEB_ODD in chi, CHEB in eta) and with the COSSIN_EVEN /
+    COSSIN_ODD phi bases, against Base_spectral::coef / coef_i of the
+    reference (tests/golden/ref_coef3_bases.npz)."""
+    from kadath_frontera_gb300._lib import TransformDesc
+    z = np.load(GOLD / "ref_coef3_bases.npz")
+    np_, nc = [int(v) for v in z[f"{case}_np"]], [int(v) for v in z[f"{case}_nc"]]
+    br, bt, bp = np.asarray(z[f"{case}_br"]), [int(v) for v in z[f"{case}_bt"]], int(z[f"{case}_bp"])
+    r = (C.c_int * (nc[1] * nc[2]))(*[int(br[j][k]) for j in range(nc[1]) for k in range(nc[2])])
+    t = (C.c_int * nc[2])(*bt)
+    for fn, src, n_out, ref in ((ctx.lib.kd_coef_host, z[f"{case}_values"], nc, z[f"{case}_coef"]),
+                                (ctx.lib.kd_coef_i_host, z[f"{case}_coefs_in"], np_, z[f"{case}_coef_i"])):
+        x = np.ascontiguousarray(src, dtype=np.float64)
+        y = np.zeros(int(np.prod(n_out)))
+        desc = TransformDesc()
+        desc.nbr_points[:] = np_
+        desc.nbr_coefs[:] = nc
+        desc.base_r = C.cast(r, C.POINTER(C.c_int))
+        desc.base_t = C.cast(t, C.POINTER(C.c_int))
+        desc.base_p = bp
+        desc.batch = 1
+        desc.in_ = x.ctypes.data
+        desc.out = y.ctypes.data
+        ctx.check(fn(ctx.h, C.byref(desc)))
+        assert rel(y, ref) < TOL_T, (case, fn.__name__, rel(y, ref))

@@ -179,3 +179,16 @@ def test_trig_atanh_ddr_match_the_reference():
         sysm.add_eq_matching(d, K.OUTER_BC, lambda T, b: T["psi"].dn(b))
     sysm.add_eq_bc(nd - 1, K.OUTER_BC, lambda T, b: T["psi"] - 1.0)
     _check_system(sysm, [psi], doms, z)
+
+
+@pytest.mark.parametrize("case", ["bispheric_std", "bispheric_anti", "cossin_even", "cossin_odd"])
+def test_coef_3d_with_bispheric_and_cossin_parity_bases_matches_the_reference(case):
+    """Base_spectral::coef / coef_i with the bispheric domains' bases and the
+    COSSIN_EVEN / COSSIN_ODD phi bases (tests/golden/ref_coef3_bases.npz)."""
+    z = np.load(GOLD / "ref_coef3_bases.npz")
+    np_, nc = tuple(int(v) for v in z[f"{case}_np"]), tuple(int(v) for v in z[f"{case}_nc"])
+    br, bt, bp = np.asarray(z[f"{case}_br"]), np.asarray(z[f"{case}_bt"]), int(z[f"{case}_bp"])
+    got = S.coef_3d(z[f"{case}_values"].reshape(np_), br, bt, bp, nc)
+    assert _rel(got, z[f"{case}_coef"]) < 1e-13
+    back = S.coef_i_3d(z[f"{case}_coefs_in"].reshape(nc), br, bt, bp, np_)
+    assert _rel(back, z[f"{case}_coef_i"]) < 1e-13
