@@ -595,7 +595,7 @@ int tf32_update_max_clusters16() {
 }
 
 void tf32_gemm_update(Context* ctx, int m, int n, int k, const float* A, long long lda, const float* B, long long ldb,
-                      float* C, long long ldc, int c_rows_writable, int terms, bool spare_gpc) {
+                      float* C, long long ldc, int c_rows_writable, int terms, int clusters) {
   if (m <= 0 || n <= 0 || k <= 0) return;
   if (k > TC_MAXK) throw KdError(KD_ERR_ARG, "tcgen05 trailing update: panel width above 128");
   const bool split3 = (terms == 3);
@@ -651,11 +651,12 @@ void tf32_gemm_update(Context* ctx, int m, int n, int k, const float* A, long lo
     const size_t psmem = 1024 + ops + static_cast<size_t>(ncs) * P_CHUNK_BYTES;
     if (psmem > P_MAX_SMEM) throw KdError(KD_ERR_UNSUPPORTED, "tcgen05 update: operands do not fit in shared memory");
     const int ntm = mpad / TC_M, ntiles = ntm * (npad / TC_N);
-    const int maxc = spare_gpc ? tf32_update_max_clusters16() : 0;
+    const int maxc = clusters ? tf32_update_max_clusters16() : 0;
     if (maxc >= 2) {
-      // 16-CTA clusters (the CTAs share nothing), one fewer than fit
+      // 16-CTA clusters (the CTAs share nothing): one fewer than fit, or all
       int ncl = (ntiles + 15) / 16;
-      if (ncl > maxc - 1) ncl = maxc - 1;
+      const int cap = clusters == 2 ? maxc : maxc - 1;
+      if (ncl > cap) ncl = cap;
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(16 * ncl, 1, 1);
       cfg.blockDim = dim3(P_THREADS, 1, 1);
@@ -715,13 +716,13 @@ int tf32_gemm_error_flag(Context* ctx) {
 
 void gemm_update_f32(Context* ctx, cublasHandle_t blas, int m, int n, int k, const float* A, long long lda,
                      const float* B, long long ldb, float* C, long long ldc, bool tf32, int c_rows_writable,
-                     int terms, bool spare_gpc) {
+                     int terms, int clusters) {
   // work: the algorithmic HBM bytes (C read and written once, A and B read
   // once); the update is bound by the C stream
   ProfScope ps(ctx, Context::PROF_LU_GEMM, 8.0 * m * n + 4.0 * (static_cast<double>(m) + n) * k);
   if (tf32 && tf32_gemm_supported(k)) {
     if (terms == 3 && !tf32x3_gemm_possible(k, C, ldc, m, c_rows_writable)) terms = 1;
-    tf32_gemm_update(ctx, m, n, k, A, lda, B, ldb, C, ldc, c_rows_writable, terms, spare_gpc);
+    tf32_gemm_update(ctx, m, n, k, A, lda, B, ldb, C, ldc, c_rows_writable, terms, clusters);
     return;
   }
   // plain FP32 product (the FP32-IR mode): library SGEMM

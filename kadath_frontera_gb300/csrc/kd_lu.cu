@@ -208,9 +208,10 @@ __global__ void col_scale_convert_kernel(const double* __restrict__ A, long long
 constexpr int NP_NB = 96;
 constexpr int NP_LD = NP_NB + 1;  // odd row stride: row-wise access without bank conflicts
 constexpr int NP_THREADS = 256;
+constexpr int NP_MAX_CTAS = 38;  // SMs outside the seven 16-CTA clusters of a GB300's trailing update: 152 - 112 = 40
 static_assert(NP_THREADS == 256 && NP_NB == 96, "the register tiling is 8 warps x 12 rows by 32 lanes x 3 columns");
 __global__ void __launch_bounds__(NP_THREADS) panel_nopiv_kernel(float* __restrict__ A, long long ld, int N, int j0,
-                                                                 int jb, int* __restrict__ info) {
+                                                                 int jb, int rpt, int* __restrict__ info) {
   __shared__ float U[NP_NB * NP_LD];
   __shared__ float rdiag[NP_NB];
   __shared__ float pbuf[2][NP_NB], cbuf[2][NP_NB];
@@ -293,11 +294,13 @@ __global__ void __launch_bounds__(NP_THREADS) panel_nopiv_kernel(float* __restri
       const int i = e % jb, k = e / jb;
       A[static_cast<long long>(j0 + k) * ld + j0 + i] = U[i * NP_LD + k];
     }
-  // L21: x U11 = a for this thread's row, by 32-column chunks with the
-  // chunk in registers: a chunk first takes off the products with the
-  // finished chunks (re-read from memory), then is solved against its
-  // 32 x 32 diagonal block of U11, then written back.
-  const int row = j0 + jb + blockIdx.x * NP_THREADS + tid;
+  // L21: x U11 = a for each of this thread's rpt rows (CTA b owns rows
+  // j0 + jb + [b rpt NP_THREADS, (b + 1) rpt NP_THREADS)), by 32-column
+  // chunks with the chunk in registers: a chunk first takes off the products
+  // with the finished chunks (re-read from memory), then is solved against
+  // its 32 x 32 diagonal block of U11, then written back.
+  for (int rr = 0; rr < rpt; rr++) {
+  const int row = j0 + jb + (blockIdx.x * rpt + rr) * NP_THREADS + tid;
   if (row >= N) return;
   float* arow = A + static_cast<long long>(j0) * ld + row;  // element k at arow[k * ld]
 #pragma unroll
@@ -328,6 +331,7 @@ __global__ void __launch_bounds__(NP_THREADS) panel_nopiv_kernel(float* __restri
 #pragma unroll
     for (int j = 0; j < 32; j++)
       if (c * 32 + j < jb) arow[static_cast<long long>(c * 32 + j) * ld] = x[j];
+  }
   }
 }
 
@@ -2453,8 +2457,12 @@ void DenseLU::factor_f32_nopiv(float* A, long long ld, int N, bool tf32) {
   auto panel = [&](int j0, int jb) {
     const int m = N - j0 - jb;
     ProfScope ps(ctx_, Context::PROF_LU_PANEL_STATIC, 2.0 * sizeof(float) * jb * (N - j0));
-    const int grid = m > 0 ? blocks(m, NP_THREADS) : 1;
-    panel_nopiv_kernel<<<grid, NP_THREADS, 0, ctx_->stream()>>>(A, ld, N, j0, jb, d_info_);
+    // at most NP_MAX_CTAS CTAs (several 256-row groups each): the SMs left
+    // beside the trailing update's 16-CTA clusters
+    const int groups = m > 0 ? blocks(m, NP_THREADS) : 1;
+    const int rpt = (groups + NP_MAX_CTAS - 1) / NP_MAX_CTAS;
+    const int grid = (groups + rpt - 1) / rpt;
+    panel_nopiv_kernel<<<grid, NP_THREADS, 0, ctx_->stream()>>>(A, ld, N, j0, jb, rpt, d_info_);
     ctx_->launches++;
   };
   // Look-ahead (tensor-core update): the next panel's columns are updated
@@ -2486,7 +2494,7 @@ void DenseLU::factor_f32_nopiv(float* A, long long ld, int N, bool tf32) {
       ctx_->fork(1);
       ctx_->use(0);
       gemm_update_f32(ctx_, blas_, m, m - jbn, jb, A21, ld, A12 + static_cast<long long>(jbn) * ld, ld,
-                      A22 + static_cast<long long>(jbn) * ld, ld, tf32, writable, tf32_terms, true);
+                      A22 + static_cast<long long>(jbn) * ld, ld, tf32, writable, tf32_terms, 2);
       ctx_->use(-1);
       side_pending = true;
     } else {
