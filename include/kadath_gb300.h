@@ -520,7 +520,7 @@ int kd_tf32_gemm_update(kd_ctx* ctx, int m, int n, int k, const float* A, long l
                         long long ldb, float* C, long long ldc);
 /* The same update with 3xTF32 products (A = Ah + Al, B = Bh + Bl in TF32,
  * C -= Al Bh + Ah Bl + Ah Bh), about FP32 accurate; the update the mixed LU
- * uses.  Needs k <= 96, C 16-byte aligned, ldc a multiple of 4 and m a
+ * uses.  Needs k <= 192, C 16-byte aligned, ldc a multiple of 4 and m a
  * multiple of 4 (else KD_ERR_UNSUPPORTED). */
 int kd_tf32x3_gemm_update(kd_ctx* ctx, int m, int n, int k, const float* A, long long lda, const float* B,
                           long long ldb, float* C, long long ldc);

@@ -1125,7 +1125,7 @@ int kd_tf32x3_gemm_update(kd_ctx* ctx, int m, int n, int k, const float* A, long
                           long long ldb, float* C, long long ldc) {
   if (!ctx || !ctx->c) return KD_ERR_ARG;
   return guarded(ctx, [&] {
-    if (m < 0 || n < 0 || k < 1 || k > 96) throw kd::KdError(KD_ERR_ARG, "need m, n >= 0 and 1 <= k <= 96");
+    if (m < 0 || n < 0 || k < 1 || k > 192) throw kd::KdError(KD_ERR_ARG, "need m, n >= 0 and 1 <= k <= 192");
     if ((m > 0 && lda < m) || ldb < k || (m > 0 && ldc < m)) throw kd::KdError(KD_ERR_ARG, "leading dimension too small");
     if (!A || !B || !C) throw kd::KdError(KD_ERR_ARG, "null matrix");
     kd::tf32_gemm_update(ctx->c.get(), m, n, k, A, lda, B, ldb, C, ldc, m, 3);

@@ -33,7 +33,8 @@ namespace {
 constexpr int TC_M = 128;
 constexpr int TC_N = 128;
 constexpr int TC_KBLK = 32;        // TF32 elements per 128-byte row
-constexpr int TC_MAXK = 128;       // largest panel width supported
+constexpr int TC_MAXK = 128;       // largest panel width of the one-tile kernel (all of k in shared memory)
+constexpr int TC_MAXK_P = 192;     // largest panel width of the persistent kernel (k streamed by 32-wide blocks)
 constexpr int TC_THREADS = 128;
 constexpr unsigned TC_TMEM_COLS = 128;
 constexpr size_t TC_MIN_SMEM = 56 * 1024;
@@ -562,7 +563,8 @@ bool tf32_gemm_supported(int k) { return k > 0 && k <= TC_MAXK; }
 
 bool tf32x3_gemm_possible(int k, const float* C, long long ldc, int m, int c_rows_writable) {
   const int kpad = ((k + TC_KBLK - 1) / TC_KBLK) * TC_KBLK;
-  return k > 0 && kpad <= 96 && reinterpret_cast<uintptr_t>(C) % 16 == 0 && ldc % 4 == 0 &&
+  // the persistent pipeline's conditions (it streams k, so k may reach TC_MAXK_P)
+  return k > 0 && kpad <= TC_MAXK_P && reinterpret_cast<uintptr_t>(C) % 16 == 0 && ldc % 4 == 0 &&
          (m + 3) / 4 * 4 <= c_rows_writable && encode_fn() != nullptr;
 }
 
@@ -595,12 +597,12 @@ int tf32_update_max_clusters16() {
 }
 
 void tf32_gemm_update(Context* ctx, int m, int n, int k, const float* A, long long lda, const float* B, long long ldb,
-                      float* C, long long ldc, int c_rows_writable, int terms, int clusters) {
+                      float* C, long long ldc, int c_rows_writable, int terms, int clusters, int max_ctas) {
   if (m <= 0 || n <= 0 || k <= 0) return;
-  if (k > TC_MAXK) throw KdError(KD_ERR_ARG, "tcgen05 trailing update: panel width above 128");
   const bool split3 = (terms == 3);
   if (split3 && !tf32x3_gemm_possible(k, C, ldc, m, c_rows_writable))
-    throw KdError(KD_ERR_UNSUPPORTED, "3xTF32 update needs k <= 96 and a 16-byte aligned C with ldc % 4 == 0");
+    throw KdError(KD_ERR_UNSUPPORTED, "3xTF32 update needs k <= 192 and a 16-byte aligned C with ldc % 4 == 0");
+  if (k > TC_MAXK && !split3) throw KdError(KD_ERR_ARG, "tcgen05 trailing update: panel width above 128");
   cudaStream_t s = ctx->stream();
   const int kpad = ((k + TC_KBLK - 1) / TC_KBLK) * TC_KBLK;
   const int mpad = ((m + TC_M - 1) / TC_M) * TC_M;
@@ -675,7 +677,8 @@ void tf32_gemm_update(Context* ctx, int m, int n, int k, const float* A, long lo
       ctx->launches += 1;
       return;
     }
-    const int cap = ctx->sms() < nsm ? ctx->sms() : nsm;
+    int cap = ctx->sms() < nsm ? ctx->sms() : nsm;
+    if (max_ctas > 0 && max_ctas < cap) cap = max_ctas;
     const int grid = ntiles < cap ? ntiles : cap;
     tf32_update_persistent<<<grid, P_THREADS, psmem, s>>>(mA, mB, mAl, mBl, mC, nkb, ntm, ntiles, split3 ? 1 : 0, ncs,
                                                           err);
@@ -716,13 +719,13 @@ int tf32_gemm_error_flag(Context* ctx) {
 
 void gemm_update_f32(Context* ctx, cublasHandle_t blas, int m, int n, int k, const float* A, long long lda,
                      const float* B, long long ldb, float* C, long long ldc, bool tf32, int c_rows_writable,
-                     int terms, int clusters) {
+                     int terms, int clusters, int max_ctas) {
   // work: the algorithmic HBM bytes (C read and written once, A and B read
   // once); the update is bound by the C stream
   ProfScope ps(ctx, Context::PROF_LU_GEMM, 8.0 * m * n + 4.0 * (static_cast<double>(m) + n) * k);
-  if (tf32 && tf32_gemm_supported(k)) {
+  if (tf32 && (tf32_gemm_supported(k) || (terms == 3 && tf32x3_gemm_possible(k, C, ldc, m, c_rows_writable)))) {
     if (terms == 3 && !tf32x3_gemm_possible(k, C, ldc, m, c_rows_writable)) terms = 1;
-    tf32_gemm_update(ctx, m, n, k, A, lda, B, ldb, C, ldc, c_rows_writable, terms, clusters);
+    tf32_gemm_update(ctx, m, n, k, A, lda, B, ldb, C, ldc, c_rows_writable, terms, clusters, max_ctas);
     return;
   }
   // plain FP32 product (the FP32-IR mode): library SGEMM

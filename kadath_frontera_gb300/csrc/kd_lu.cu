@@ -2446,14 +2446,20 @@ void DenseLU::factor_f32(float* A, long long ld, int N, bool tf32) {
 }
 
 // Static-pivot factorisation of the FP32 working copy, whose rows are
-// already in the pivot order of an earlier factorisation: per panel of up to
-// 96 columns one launch factors the diagonal block and solves L21, the
-// U12 = L11^-1 A12 triangular solve follows, then the tensor-core trailing
-// update on the whole GPU.  No row exchanges, no grid-wide synchronisation.
+// already in the pivot order of an earlier factorisation.  Panels are 192
+// columns wide, each made of two 96-column halves: the left half is factored
+// (panel_nopiv_kernel: the diagonal block and L21 in one launch), its U12
+// over the right half solved, the right half updated below it, then
+// factored.  The U12 solve of a wide panel goes the same way by halves, and
+// the trailing update runs with k = 192 on the tensor cores, which streams
+// the trailing matrix through HBM half as often as 96-column panels would.
+// Columns that do not fill a wide panel take 96-column panels.  No row
+// exchanges, no grid-wide synchronisation.
 void DenseLU::factor_f32_nopiv(float* A, long long ld, int N, bool tf32) {
   cudaStream_t s = ctx_->stream();
   cuda_check(cudaMemsetAsync(d_info_, 0, sizeof(int), s), "memset info");
-  const int NB = NP_NB;
+  const int NB = NP_NB, NW = 2 * NP_NB;
+  auto at = [&](int row, int col) { return A + static_cast<long long>(col) * ld + row; };
   auto panel = [&](int j0, int jb) {
     const int m = N - j0 - jb;
     ProfScope ps(ctx_, Context::PROF_LU_PANEL_STATIC, 2.0 * sizeof(float) * jb * (N - j0));
@@ -2465,13 +2471,42 @@ void DenseLU::factor_f32_nopiv(float* A, long long ld, int N, bool tf32) {
     panel_nopiv_kernel<<<grid, NP_THREADS, 0, ctx_->stream()>>>(A, ld, N, j0, jb, rpt, d_info_);
     ctx_->launches++;
   };
+  auto trsm = [&](int j0, int jb, int c0, int c1) {
+    ProfScope ps(ctx_, Context::PROF_LU_SWAP_TRSM, 2.0 * sizeof(float) * jb * (c1 - c0));
+    launch_trsm_chunk(ctx_, A, ld, j0, jb, c0, c1);
+  };
+  // a panel of jb <= 96 columns, or a wide one of 192 as two halves
+  auto wide_panel = [&](int j0, int jb) {
+    if (jb <= NB) {
+      panel(j0, jb);
+      return;
+    }
+    panel(j0, NB);
+    trsm(j0, NB, j0 + NB, j0 + jb);
+    const int mr = N - j0 - NB;
+    gemm_update_f32(ctx_, blas_, mr, jb - NB, NB, at(j0 + NB, j0), ld, at(j0, j0 + NB), ld, at(j0 + NB, j0 + NB), ld,
+                    tf32, static_cast<int>(ld - j0 - NB), tf32_terms, 0, NP_MAX_CTAS);
+    panel(j0 + NB, jb - NB);
+  };
+  // U12 = L11^-1 A12 for the panel's rows over columns [c0, c1)
+  auto wide_trsm = [&](int j0, int jb, int c0, int c1) {
+    if (jb <= NB) {
+      trsm(j0, jb, c0, c1);
+      return;
+    }
+    trsm(j0, NB, c0, c1);
+    gemm_update_f32(ctx_, blas_, jb - NB, c1 - c0, NB, at(j0 + NB, j0), ld, at(j0, c0), ld, at(j0 + NB, c0), ld, tf32,
+                    jb - NB, tf32_terms);
+    trsm(j0 + NB, jb - NB, c0, c1);
+  };
+  auto width = [&](int j0) { return N - j0 >= NW ? NW : (N - j0 < NB ? N - j0 : NB); };
   // Look-ahead (tensor-core update): the next panel's columns are updated
   // first, then the rest of the trailing update runs on a side stream as
-  // 16-CTA clusters that leave one GPC free, while the next panel is
-  // factored on the main stream; its U12 solve waits for both.
+  // every 16-CTA cluster the GPU holds, while the next panel is factored on
+  // the main stream on the SMs left; the next U12 solve waits for both.
   const bool lookahead = tf32 && tf32_update_max_clusters16() >= 2;
-  int j0 = 0, jb = (N < NB) ? N : NB;
-  panel(j0, jb);
+  int j0 = 0, jb = width(0);
+  wide_panel(j0, jb);
   bool side_pending = false;
   for (;;) {
     if (side_pending) {
@@ -2480,14 +2515,11 @@ void DenseLU::factor_f32_nopiv(float* A, long long ld, int N, bool tf32) {
     }
     const int m = N - j0 - jb;
     if (m <= 0) break;
-    {
-      ProfScope ps(ctx_, Context::PROF_LU_SWAP_TRSM, 2.0 * sizeof(float) * jb * m);
-      launch_trsm_chunk(ctx_, A, ld, j0, jb, j0 + jb, N);
-    }
-    const int j0n = j0 + jb, jbn = (N - j0n < NB) ? N - j0n : NB;
-    float* A21 = A + static_cast<long long>(j0) * ld + j0 + jb;
-    float* A12 = A + static_cast<long long>(j0 + jb) * ld + j0;
-    float* A22 = A + static_cast<long long>(j0 + jb) * ld + j0 + jb;
+    wide_trsm(j0, jb, j0 + jb, N);
+    const int j0n = j0 + jb, jbn = width(j0n);
+    float* A21 = at(j0 + jb, j0);
+    float* A12 = at(j0, j0 + jb);
+    float* A22 = at(j0 + jb, j0 + jb);
     const int writable = static_cast<int>(ld - j0 - jb);
     if (lookahead && m > jbn) {
       gemm_update_f32(ctx_, blas_, m, jbn, jb, A21, ld, A12, ld, A22, ld, tf32, writable, tf32_terms);
@@ -2500,7 +2532,7 @@ void DenseLU::factor_f32_nopiv(float* A, long long ld, int N, bool tf32) {
     } else {
       gemm_update_f32(ctx_, blas_, m, m, jb, A21, ld, A12, ld, A22, ld, tf32, writable, tf32_terms);
     }
-    panel(j0n, jbn);
+    wide_panel(j0n, jbn);
     j0 = j0n;
     jb = jbn;
   }

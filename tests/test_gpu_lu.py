@@ -105,7 +105,8 @@ def test_tcgen05_tf32_update_matches_fp64_product(ctx, m, n, k, aligned):
     assert np.array_equal(got[:, m:], Cm[:, m:])
 
 
-@pytest.mark.parametrize("m,n,k", [(128, 128, 32), (256, 384, 96), (200, 130, 96), (1000, 777, 64), (2000, 1500, 96)])
+@pytest.mark.parametrize("m,n,k", [(128, 128, 32), (256, 384, 96), (200, 130, 96), (1000, 777, 64), (2000, 1500, 96),
+                                   (1000, 777, 128), (300, 200, 160), (2000, 1500, 192)])
 def test_tcgen05_3xtf32_update_is_fp32_accurate(ctx, m, n, k):
     """3xTF32 (hi/lo split of both operands, three tensor-core products) is
     about FP32 accurate: error bound 2^-17 * max|A| max|B| k, 256 times
