@@ -118,7 +118,9 @@ class Context {
   // (contents are not kept across growth; *fresh tells the caller the
   // buffer is new).  Work of one context is ordered on its streams, so
   // contexts driven from different host threads never share a workspace.
-  enum WorkSlot : int { WS_TC_A = 0, WS_TC_B = 1, WS_TC_FLAG = 2, WS_NSLOT = 3 };
+  // WS_TC_A2 / WS_TC_B2: the packed operands of the update that runs as
+  // 16-CTA clusters on a side stream, beside updates on the main stream
+  enum WorkSlot : int { WS_TC_A = 0, WS_TC_B = 1, WS_TC_FLAG = 2, WS_TC_A2 = 3, WS_TC_B2 = 4, WS_NSLOT = 5 };
   void* workspace(int slot, size_t bytes, bool* fresh = nullptr);
 
   // While a CUDA graph is being captured no host->device upload may happen;

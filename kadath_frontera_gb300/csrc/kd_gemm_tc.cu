@@ -609,9 +609,12 @@ void tf32_gemm_update(Context* ctx, int m, int n, int k, const float* A, long lo
   const int npad = ((n + TC_N - 1) / TC_N) * TC_N;
   // hi parts first, lo parts (3xTF32) right after them
   size_t need_a = static_cast<size_t>(mpad) * kpad, need_b = static_cast<size_t>(npad) * kpad;
-  // packed operands and the timeout flag live in the context's workspaces
-  float* at = static_cast<float*>(ctx->workspace(Context::WS_TC_A, 2 * need_a * sizeof(float)));
-  float* bt = static_cast<float*>(ctx->workspace(Context::WS_TC_B, 2 * need_b * sizeof(float)));
+  // packed operands and the timeout flag live in the context's workspaces;
+  // an update as clusters (the side stream's, beside the main stream's
+  // updates of the next panel) packs into workspaces of its own
+  const bool side = clusters != 0;
+  float* at = static_cast<float*>(ctx->workspace(side ? Context::WS_TC_A2 : Context::WS_TC_A, 2 * need_a * sizeof(float)));
+  float* bt = static_cast<float*>(ctx->workspace(side ? Context::WS_TC_B2 : Context::WS_TC_B, 2 * need_b * sizeof(float)));
   bool fresh = false;
   int* err = static_cast<int*>(ctx->workspace(Context::WS_TC_FLAG, sizeof(int), &fresh));
   if (fresh) cuda_check(cudaMemsetAsync(err, 0, sizeof(int), s), "memset err");

@@ -237,7 +237,14 @@ __global__ void __launch_bounds__(NP_THREADS) panel_nopiv_kernel(float* __restri
   for (int ii = 0; ii < 12; ii++)
 #pragma unroll
     for (int jj = 0; jj < 3; jj++) a[ii][jj] = U[(warp + 8 * ii) * NP_LD + lane + 32 * jj];
-  for (int k = 0; k < jb - 1; k++) {
+  // The step is branch-free: the published pivot row holds zeros up to
+  // column k and rows up to k get a zero multiplier, so every thread does
+  // its 36 multiply-adds unconditionally (the same results: those elements
+  // get -0 * pr + a = a); then the lane owning column k stores the
+  // multipliers there.  (Two columns per barrier gave the same factors but
+  // took longer: the step is bound by its instructions, not the barrier.)
+  int k = 0;
+  for (; k < jb - 1; k++) {
     float* prow = pbuf[k & 1];
     float* pcol = cbuf[k & 1];
     if (warp == (k & 7)) {
@@ -246,7 +253,7 @@ __global__ void __launch_bounds__(NP_THREADS) panel_nopiv_kernel(float* __restri
       for (int ii = 0; ii < 12; ii++)
         if (ii == ik) {
 #pragma unroll
-          for (int jj = 0; jj < 3; jj++) prow[lane + 32 * jj] = a[ii][jj];
+          for (int jj = 0; jj < 3; jj++) prow[lane + 32 * jj] = (lane + 32 * jj > k) ? a[ii][jj] : 0.0f;
         }
     }
     if (lane == (k & 31)) {
@@ -259,22 +266,27 @@ __global__ void __launch_bounds__(NP_THREADS) panel_nopiv_kernel(float* __restri
         }
     }
     __syncthreads();
-    const float rp = 1.0f / prow[k];
+    const float rp = __frcp_rn(pcol[k]);  // the correctly rounded 1 / pivot
     float pr[3];
 #pragma unroll
     for (int jj = 0; jj < 3; jj++) pr[jj] = prow[lane + 32 * jj];
+    float lm[12];
 #pragma unroll
     for (int ii = 0; ii < 12; ii++) {
       const int i = warp + 8 * ii;
-      if (i > k) {
-        const float l = pcol[i] * rp;
+      lm[ii] = (i > k) ? pcol[i] * rp : 0.0f;
 #pragma unroll
-        for (int jj = 0; jj < 3; jj++) {
-          const int j = lane + 32 * jj;
-          if (j == k) a[ii][jj] = l;
-          else if (j > k) a[ii][jj] = fmaf(-l, pr[jj], a[ii][jj]);
+      for (int jj = 0; jj < 3; jj++) a[ii][jj] = fmaf(-lm[ii], pr[jj], a[ii][jj]);
+    }
+    if (lane == (k & 31)) {
+      const int jk = k >> 5;
+#pragma unroll
+      for (int jj = 0; jj < 3; jj++)
+        if (jj == jk) {
+#pragma unroll
+          for (int ii = 0; ii < 12; ii++)
+            if (warp + 8 * ii > k) a[ii][jj] = lm[ii];
         }
-      }
     }
   }
   __syncthreads();

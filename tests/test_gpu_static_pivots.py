@@ -102,3 +102,30 @@ def test_newton_with_static_pivots_matches_fp64_iterates(ctx):
                 assert np.linalg.norm(a - b) <= 1e-10 * max(np.linalg.norm(b), 1e-300)
     assert d_ref
     assert used[0] == 0 and all(used[1:]) and len(used) >= 2
+
+
+def test_static_factors_precondition_as_well_as_pivoted_ones_at_the_timed_size(ctx):
+    """The star at (13, 9, 4), N = 12,331, solved three times: every later
+    step factors with the kept pivot order (192-column panels, the trailing
+    update on a side stream beside the next panel) and its refinement needs
+    at most 4 iterations more than the pivoted first step's; factors spoilt
+    by a race between the two streams' updates would need many more (and
+    the step would then drop the order)."""
+    from kadath_frontera_gb300 import workloads
+    from kadath_frontera_gb300.kadath import KD_LU_TF32_IR
+    wl = workloads.star(ctx=ctx)
+    for _ in range(3):
+        wl.restore()
+        wl.syst.reset_pivot_order()
+        reps = []
+        for _ in range(10):
+            done, _ = wl.syst.do_newton(1e-10, lu_mode=KD_LU_TF32_IR)
+            if done:
+                break
+            reps.append(dict(wl.syst.last_report))
+        assert done and len(reps) >= 2
+        first = reps[0]["refine_iters"]
+        assert reps[0]["static_pivots"] == 0
+        for r in reps[1:]:
+            assert r["static_pivots"] == 1
+            assert r["refine_iters"] <= first + 4, (first, [x["refine_iters"] for x in reps])
