@@ -206,95 +206,160 @@ __global__ void col_scale_convert_kernel(const double* __restrict__ A, long long
 // registers.  CTA 0 writes L11 \ U11 back.  A zero or non-finite pivot sets
 // *info (the caller then factors with partial pivoting instead).
 constexpr int NP_NB = 96;
-constexpr int NP_LD = NP_NB + 1;  // odd row stride: row-wise access without bank conflicts
+constexpr int NP_LD = NP_NB + 4;  // row stride: 16-byte aligned rows, read four elements at a time by L21
 constexpr int NP_THREADS = 256;
+constexpr int NP_XS_BYTES = (NP_NB - 32) * NP_THREADS * 4;  // the solved chunks 0 and 1 of every thread's row
 constexpr int NP_MAX_CTAS = 38;  // SMs outside the seven 16-CTA clusters of a GB300's trailing update: 152 - 112 = 40
-static_assert(NP_THREADS == 256 && NP_NB == 96, "the register tiling is 8 warps x 12 rows by 32 lanes x 3 columns");
+static_assert(NP_THREADS == 256 && NP_NB == 96, "three 32-column blocks; 16 x 16 threads tile the trailing blocks");
+
+// Rank-32 update of the trailing block of the diagonal block after its
+// 32-column block o: a_ij -= l_ik u_kj for k = o .. o+31 in order, rows and
+// columns o+32 .. 95; thread (ty, tx) holds rows ty + 16 a and columns
+// tx + 16 c (a, c < R) in registers.
+template <int R>
+__device__ __forceinline__ void np_trailing(float* __restrict__ U, int o, int tid) {
+  const int ty = tid >> 4, tx = tid & 15, b = o + 32;
+  float acc[R][R];
+#pragma unroll
+  for (int a = 0; a < R; a++)
+#pragma unroll
+    for (int c = 0; c < R; c++) acc[a][c] = U[(b + ty + 16 * a) * NP_LD + b + tx + 16 * c];
+#pragma unroll 4
+  for (int k = 0; k < 32; k++) {
+    float l[R], u[R];
+#pragma unroll
+    for (int a = 0; a < R; a++) l[a] = U[(b + ty + 16 * a) * NP_LD + o + k];
+#pragma unroll
+    for (int c = 0; c < R; c++) u[c] = U[(o + k) * NP_LD + b + tx + 16 * c];
+#pragma unroll
+    for (int a = 0; a < R; a++)
+#pragma unroll
+      for (int c = 0; c < R; c++) acc[a][c] = fmaf(-l[a], u[c], acc[a][c]);
+  }
+#pragma unroll
+  for (int a = 0; a < R; a++)
+#pragma unroll
+    for (int c = 0; c < R; c++) U[(b + ty + 16 * a) * NP_LD + b + tx + 16 * c] = acc[a][c];
+}
+
+// Eight elimination steps k0 .. k0+7 of a 32 x 32 diagonal block held by
+// one warp, lane l holding row l with its values shifted so that d[0] is
+// column k (see panel_nopiv_kernel).  From step k0 on at most W = 32 - k0
+// columns are live, so only W - 1 values of the pivot row are broadcast.
+// rp enters as __frcp_rn of step k0's pivot and leaves as the next one's;
+// each step stores the element of column k that became final.
+template <int W>
+__device__ __forceinline__ void np_diag_steps(float (&d)[32], float& rp, float* __restrict__ urow,
+                                              float* __restrict__ rpv, int lane, int k0) {
+#pragma unroll 1
+  for (int k = k0; k < k0 + 8; k++) {
+    float pr[W];  // the pivot row (lane k's values)
+#pragma unroll
+    for (int j = 1; j < W; j++) pr[j] = __shfl_sync(0xffffffffu, d[j], k);
+    // rows up to k (the finished ones and the pivot row) take a zero
+    // multiplier: their multiply-adds leave them as they are
+    const float lm = (lane > k) ? d[0] * rp : 0.0f;
+    if (lane == 0) rpv[k] = rp;
+    urow[k] = (lane > k) ? lm : d[0];
+    // the next pivot first, so that its reciprocal overlaps this step
+    d[0] = fmaf(-lm, pr[1], d[1]);
+    const float rpn = __frcp_rn(__shfl_sync(0xffffffffu, d[0], (k + 1) & 31));
+#pragma unroll
+    for (int j = 2; j < W; j++) d[j - 1] = fmaf(-lm, pr[j], d[j]);
+    d[W - 1] = 0.0f;
+    rp = rpn;
+  }
+}
+
 __global__ void __launch_bounds__(NP_THREADS) panel_nopiv_kernel(float* __restrict__ A, long long ld, int N, int j0,
                                                                  int jb, int rpt, int* __restrict__ info) {
-  __shared__ float U[NP_NB * NP_LD];
+  __shared__ __align__(16) float U[NP_NB * NP_LD];
   __shared__ float rdiag[NP_NB];
-  __shared__ float pbuf[2][NP_NB], cbuf[2][NP_NB];
+  __shared__ float rpv[NP_NB];  // __frcp_rn of the pivots
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int e = tid; e < NP_NB * NP_NB; e += NP_THREADS) {
-    const int i = e % NP_NB, k = e / NP_NB;  // down the columns: coalesced reads
-    float v;
-    if (i < jb && k < jb)
-      v = A[static_cast<long long>(j0 + k) * ld + j0 + i];
-    else
-      v = (i == k) ? 1.0f : 0.0f;  // identity padding past jb
-    U[i * NP_LD + k] = v;
+  {
+    // all 36 loads of the thread in flight before the shared stores
+    constexpr int NV = NP_NB * NP_NB / NP_THREADS;
+    static_assert(NV * NP_THREADS == NP_NB * NP_NB, "the diagonal block splits evenly over the threads");
+    float v[NV];
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+      const int e = tid + q * NP_THREADS;
+      const int i = e % NP_NB, k = e / NP_NB;  // down the columns: coalesced reads
+      v[q] = (i < jb && k < jb) ? A[static_cast<long long>(j0 + k) * ld + j0 + i]
+                                : ((i == k) ? 1.0f : 0.0f);  // identity padding past jb
+    }
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+      const int e = tid + q * NP_THREADS;
+      U[(e % NP_NB) * NP_LD + e / NP_NB] = v[q];
+    }
   }
   __syncthreads();
-  // Right-looking elimination with the block in registers: thread (warp w,
-  // lane l) holds rows w + 8 ii (ii < 12) and columns l + 32 jj (jj < 3).
-  // Step k publishes the pivot row (by warp k mod 8) and the pivot column
-  // (by lane k mod 32 of every warp) through double-buffered shared memory,
-  // one barrier per step; every thread then forms its rows' multipliers and
-  // updates its 36 elements in registers.
-  float a[12][3];
+  // Blocked right-looking elimination in shared memory, by 32-column
+  // blocks o = 0, 32, 64 (identity padding past jb stays identity):
+  //  (a) warp 0 factors the diagonal block in registers, lane l holding row
+  //      o + l; step k broadcasts the pivot row by shuffles, no barrier;
+  //  (b) threads 0..rest-1 solve the block row U12 by columns and threads
+  //      128..128+rest-1 the block column L21 by rows;
+  //  (c) all threads apply the rank-32 update to the trailing block, a
+  //      register tile each.
+  // Every element receives its multiply-adds in increasing k and every
+  // multiplier is (value) * __frcp_rn(pivot), the unblocked right-looking
+  // elimination's own operations in its own order: the factors are the same.
+  // The loop over k of (a) stays rolled: one warp running unrolled
+  // straight-line code once per launch waits on instruction fetch most of
+  // the time.  So that registers are never indexed by k, each step shifts
+  // the lane's values down by one (column o + k is always d[0]) and stores
+  // the element that became final.
 #pragma unroll
-  for (int ii = 0; ii < 12; ii++)
+  for (int o = 0; o < NP_NB; o += 32) {
+    if (warp == 0) {
+      float d[32];  // row o + lane, columns o + k + j
 #pragma unroll
-    for (int jj = 0; jj < 3; jj++) a[ii][jj] = U[(warp + 8 * ii) * NP_LD + lane + 32 * jj];
-  // The step is branch-free: the published pivot row holds zeros up to
-  // column k and rows up to k get a zero multiplier, so every thread does
-  // its 36 multiply-adds unconditionally (the same results: those elements
-  // get -0 * pr + a = a); then the lane owning column k stores the
-  // multipliers there.  (Two columns per barrier gave the same factors but
-  // took longer: the step is bound by its instructions, not the barrier.)
-  int k = 0;
-  for (; k < jb - 1; k++) {
-    float* prow = pbuf[k & 1];
-    float* pcol = cbuf[k & 1];
-    if (warp == (k & 7)) {
-      const int ik = k >> 3;
-#pragma unroll
-      for (int ii = 0; ii < 12; ii++)
-        if (ii == ik) {
-#pragma unroll
-          for (int jj = 0; jj < 3; jj++) prow[lane + 32 * jj] = (lane + 32 * jj > k) ? a[ii][jj] : 0.0f;
-        }
-    }
-    if (lane == (k & 31)) {
-      const int jk = k >> 5;
-#pragma unroll
-      for (int jj = 0; jj < 3; jj++)
-        if (jj == jk) {
-#pragma unroll
-          for (int ii = 0; ii < 12; ii++) pcol[warp + 8 * ii] = a[ii][jj];
-        }
+      for (int j = 0; j < 32; j++) d[j] = U[(o + lane) * NP_LD + o + j];
+      float* urow = U + (o + lane) * NP_LD + o;
+      float rp = __frcp_rn(__shfl_sync(0xffffffffu, d[0], 0));  // the correctly rounded 1 / pivot
+      np_diag_steps<32>(d, rp, urow, rpv + o, lane, 0);
+      np_diag_steps<24>(d, rp, urow, rpv + o, lane, 8);
+      np_diag_steps<16>(d, rp, urow, rpv + o, lane, 16);
+      np_diag_steps<8>(d, rp, urow, rpv + o, lane, 24);
     }
     __syncthreads();
-    const float rp = __frcp_rn(pcol[k]);  // the correctly rounded 1 / pivot
-    float pr[3];
+    const int rest = NP_NB - o - 32;
+    if (rest == 0) break;
+    if (tid < rest) {  // column j of U12: u_tj -= l_tk u_kj, k < t
+      const int j = o + 32 + tid;
+      float c[32];
 #pragma unroll
-    for (int jj = 0; jj < 3; jj++) pr[jj] = prow[lane + 32 * jj];
-    float lm[12];
+      for (int t = 0; t < 32; t++) c[t] = U[(o + t) * NP_LD + j];
 #pragma unroll
-    for (int ii = 0; ii < 12; ii++) {
-      const int i = warp + 8 * ii;
-      lm[ii] = (i > k) ? pcol[i] * rp : 0.0f;
+      for (int k = 0; k < 31; k++)
 #pragma unroll
-      for (int jj = 0; jj < 3; jj++) a[ii][jj] = fmaf(-lm[ii], pr[jj], a[ii][jj]);
+        for (int t = k + 1; t < 32; t++) c[t] = fmaf(-U[(o + t) * NP_LD + o + k], c[k], c[t]);
+#pragma unroll
+      for (int t = 1; t < 32; t++) U[(o + t) * NP_LD + j] = c[t];
+    } else if (tid >= 128 && tid < 128 + rest) {  // row i of L21: l_ik = (a_ik - l_it u_tk, t < k) / u_kk
+      const int i = o + 32 + tid - 128;
+      float r[32];
+#pragma unroll
+      for (int k = 0; k < 32; k++) r[k] = U[i * NP_LD + o + k];
+#pragma unroll
+      for (int k = 0; k < 32; k++) {
+        r[k] *= rpv[o + k];
+#pragma unroll
+        for (int t = k + 1; t < 32; t++) r[t] = fmaf(-r[k], U[(o + k) * NP_LD + o + t], r[t]);
+      }
+#pragma unroll
+      for (int k = 0; k < 32; k++) U[i * NP_LD + o + k] = r[k];
     }
-    if (lane == (k & 31)) {
-      const int jk = k >> 5;
-#pragma unroll
-      for (int jj = 0; jj < 3; jj++)
-        if (jj == jk) {
-#pragma unroll
-          for (int ii = 0; ii < 12; ii++)
-            if (warp + 8 * ii > k) a[ii][jj] = lm[ii];
-        }
-    }
+    __syncthreads();
+    if (rest == 64)
+      np_trailing<4>(U, o, tid);
+    else
+      np_trailing<2>(U, o, tid);
+    __syncthreads();
   }
-  __syncthreads();
-#pragma unroll
-  for (int ii = 0; ii < 12; ii++)
-#pragma unroll
-    for (int jj = 0; jj < 3; jj++) U[(warp + 8 * ii) * NP_LD + lane + 32 * jj] = a[ii][jj];
-  __syncthreads();
   if (tid < NP_NB) {
     const float d = U[tid * NP_LD + tid];
     if (tid < jb && !(fabsf(d) > 0.0f && isfinite(d)) && blockIdx.x == 0) atomicExch(info, j0 + tid + 1);
@@ -309,8 +374,10 @@ __global__ void __launch_bounds__(NP_THREADS) panel_nopiv_kernel(float* __restri
   // L21: x U11 = a for each of this thread's rpt rows (CTA b owns rows
   // j0 + jb + [b rpt NP_THREADS, (b + 1) rpt NP_THREADS)), by 32-column
   // chunks with the chunk in registers: a chunk first takes off the products
-  // with the finished chunks (re-read from memory), then is solved against
-  // its 32 x 32 diagonal block of U11, then written back.
+  // with the finished chunks (kept in the thread's column of np_xs, dynamic
+  // shared memory, rather than re-read from global memory), then is solved
+  // against its 32 x 32 diagonal block of U11, then written back.
+  extern __shared__ float np_xs[];  // [64][NP_THREADS]
   for (int rr = 0; rr < rpt; rr++) {
   const int row = j0 + jb + (blockIdx.x * rpt + rr) * NP_THREADS + tid;
   if (row >= N) return;
@@ -323,26 +390,41 @@ __global__ void __launch_bounds__(NP_THREADS) panel_nopiv_kernel(float* __restri
     for (int j = 0; j < 32; j++) x[j] = (c * 32 + j < jb) ? arow[static_cast<long long>(c * 32 + j) * ld] : 0.0f;
 #pragma unroll
     for (int cp = 0; cp < c; cp++) {
-#pragma unroll 2
+#pragma unroll 8
       for (int kk = 0; kk < 32; kk++) {
-        const float yk = arow[static_cast<long long>(cp * 32 + kk) * ld];
-        const float* urow = U + (cp * 32 + kk) * NP_LD + c * 32;
+        const float yk = np_xs[(cp * 32 + kk) * NP_THREADS + tid];
+        const float4* urow = reinterpret_cast<const float4*>(U + (cp * 32 + kk) * NP_LD + c * 32);
 #pragma unroll
-        for (int j = 0; j < 32; j++) x[j] = fmaf(-yk, urow[j], x[j]);
+        for (int j4 = 0; j4 < 8; j4++) {
+          const float4 u = urow[j4];
+          x[4 * j4] = fmaf(-yk, u.x, x[4 * j4]);
+          x[4 * j4 + 1] = fmaf(-yk, u.y, x[4 * j4 + 1]);
+          x[4 * j4 + 2] = fmaf(-yk, u.z, x[4 * j4 + 2]);
+          x[4 * j4 + 3] = fmaf(-yk, u.w, x[4 * j4 + 3]);
+        }
       }
     }
 #pragma unroll
     for (int kk = 0; kk < 32; kk++) {
       x[kk] *= rdiag[c * 32 + kk];
       const float xk = x[kk];
-      const float* urow = U + (c * 32 + kk) * NP_LD + c * 32;
+      const float4* urow = reinterpret_cast<const float4*>(U + (c * 32 + kk) * NP_LD + c * 32);
 #pragma unroll
-      for (int j = 0; j < 32; j++)
-        if (j > kk) x[j] = fmaf(-xk, urow[j], x[j]);
+      for (int j4 = (kk + 1) / 4; j4 < 8; j4++) {
+        const float4 u = urow[j4];
+        if (4 * j4 > kk) x[4 * j4] = fmaf(-xk, u.x, x[4 * j4]);
+        if (4 * j4 + 1 > kk) x[4 * j4 + 1] = fmaf(-xk, u.y, x[4 * j4 + 1]);
+        if (4 * j4 + 2 > kk) x[4 * j4 + 2] = fmaf(-xk, u.z, x[4 * j4 + 2]);
+        if (4 * j4 + 3 > kk) x[4 * j4 + 3] = fmaf(-xk, u.w, x[4 * j4 + 3]);
+      }
     }
 #pragma unroll
     for (int j = 0; j < 32; j++)
       if (c * 32 + j < jb) arow[static_cast<long long>(c * 32 + j) * ld] = x[j];
+    if (c < NP_NB / 32 - 1) {
+#pragma unroll
+      for (int j = 0; j < 32; j++) np_xs[(c * 32 + j) * NP_THREADS + tid] = x[j];
+    }
   }
   }
 }
@@ -2480,7 +2562,12 @@ void DenseLU::factor_f32_nopiv(float* A, long long ld, int N, bool tf32) {
     const int groups = m > 0 ? blocks(m, NP_THREADS) : 1;
     const int rpt = (groups + NP_MAX_CTAS - 1) / NP_MAX_CTAS;
     const int grid = (groups + rpt - 1) / rpt;
-    panel_nopiv_kernel<<<grid, NP_THREADS, 0, ctx_->stream()>>>(A, ld, N, j0, jb, rpt, d_info_);
+    static std::once_flag attr;
+    std::call_once(attr, [] {
+      cuda_check(cudaFuncSetAttribute(panel_nopiv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, NP_XS_BYTES),
+                 "panel_nopiv smem");
+    });
+    panel_nopiv_kernel<<<grid, NP_THREADS, NP_XS_BYTES, ctx_->stream()>>>(A, ld, N, j0, jb, rpt, d_info_);
     ctx_->launches++;
   };
   auto trsm = [&](int j0, int jb, int c0, int c1) {
