@@ -64,82 +64,145 @@ __global__ void trsm_unit_lower(T* __restrict__ A, long long ld, int j0, int nbk
 }
 
 // U12 = L11^-1 A12 (L11 unit lower, jb <= 96) for FP32 factors, 128 columns
-// per CTA.  The CTA's 96 x 128 tile goes through shared memory with
-// coalesced loads and stores; each thread then solves its column in three
-// 32-row chunks held in registers: a chunk first takes off the products with
-// the finished chunks (read back from shared memory), then its own 32 x 32
-// triangle.  The loops over finished rows stay rolled, so the code fits the
-// instruction cache (a fully unrolled 96 x 96 substitution does not).
-constexpr int TC_THREADS = 128;
-constexpr int TC_LDL = 97;   // row stride of L11 in shared memory
-constexpr int TC_LDX = 129;  // row stride of the column tile
-constexpr size_t TC_SMEM = sizeof(float) * (96 * TC_LDL + 96 * TC_LDX);
-__global__ void __launch_bounds__(TC_THREADS) trsm_chunk_f32(float* __restrict__ A, long long ld, int j0, int jb,
-                                                             int c0, int c1) {
-  extern __shared__ __align__(16) float tc_sm[];
-  float* L = tc_sm;                // L[i * TC_LDL + k], strictly lower part, zero elsewhere
-  float* X = tc_sm + 96 * TC_LDL;  // X[i * TC_LDX + c]
-  const int tid = threadIdx.x;
-  const int cb = c0 + blockIdx.x * TC_THREADS;
-  // staging: 24 independent loads in flight per thread, then their stores
-  for (int e0 = 0; e0 < 96 * 96; e0 += 24 * TC_THREADS) {
-    float v[24];
+// per CTA of 512 threads.  L11, transposed (LT[k][i] = l_ik), and the CTA's
+// 96 x 128 column tile X go through shared memory.  The solve runs by 32-row
+// chunks: a chunk's own triangle by columns (one thread per column, threads
+// 0..127), and its products with the finished chunks as a register-tiled
+// product (8 rows x 4 columns per thread, 128 threads).  Those products are
+// split by k: right after chunk 0's triangle, chunks 1 and 2 take off their
+// products with chunk 0 at the same time (threads 0..127 and 128..255).
+// Every element still receives its multiply-adds in increasing k: the
+// operations of a column-by-column forward substitution, in its order.  All
+// 512 threads stage the tile (every load of a thread in flight before its
+// stores) and write it back.
+constexpr int TS_THREADS = 512;
+constexpr int TS_COLS = 128;
+constexpr int TS_LDL = 100;  // row stride of LT: 16-byte aligned rows
+constexpr int TS_LDX = 132;  // row stride of X: 16-byte aligned rows
+constexpr size_t TS_SMEM = sizeof(float) * (96 * TS_LDL + 96 * TS_LDX);
+
+// X[r][c] -= sum_{k0 <= k < k1} l_rk X[k][c] (k in order) for the rows
+// r = R0 + 8 tr + a and columns c = 4 tc + b of thread t = 32 tr + tc < 128.
+__device__ __forceinline__ void ts_cross(const float* __restrict__ LT, float* __restrict__ X, int R0, int k0, int k1,
+                                         int t) {
+  const int tr = t >> 5, tc = t & 31;
+  const int r0 = R0 + 8 * tr;
+  float acc[8][4];
 #pragma unroll
-    for (int u = 0; u < 24; u++) {
-      const int e = e0 + u * TC_THREADS + tid;
-      const int i = e % 96, k = e / 96;
+  for (int a = 0; a < 8; a++) {
+    const float4 q = *reinterpret_cast<const float4*>(X + (r0 + a) * TS_LDX + 4 * tc);
+    acc[a][0] = q.x;
+    acc[a][1] = q.y;
+    acc[a][2] = q.z;
+    acc[a][3] = q.w;
+  }
+#pragma unroll 4
+  for (int k = k0; k < k1; k++) {
+    const float4 la = *reinterpret_cast<const float4*>(LT + k * TS_LDL + r0);  // the same for the whole warp
+    const float4 lb = *reinterpret_cast<const float4*>(LT + k * TS_LDL + r0 + 4);
+    const float4 y = *reinterpret_cast<const float4*>(X + k * TS_LDX + 4 * tc);
+    const float l[8] = {la.x, la.y, la.z, la.w, lb.x, lb.y, lb.z, lb.w};
+    const float yy[4] = {y.x, y.y, y.z, y.w};
+#pragma unroll
+    for (int a = 0; a < 8; a++)
+#pragma unroll
+      for (int b = 0; b < 4; b++) acc[a][b] = fmaf(-l[a], yy[b], acc[a][b]);
+  }
+#pragma unroll
+  for (int a = 0; a < 8; a++)
+    *reinterpret_cast<float4*>(X + (r0 + a) * TS_LDX + 4 * tc) = make_float4(acc[a][0], acc[a][1], acc[a][2], acc[a][3]);
+}
+
+// The 32 x 32 unit lower triangle of chunk R0 for column t (< 128).
+__device__ __forceinline__ void ts_diag(const float* __restrict__ LT, float* __restrict__ X, int R0, int t) {
+  float x[32];
+#pragma unroll
+  for (int j = 0; j < 32; j++) x[j] = X[(R0 + j) * TS_LDX + t];
+#pragma unroll
+  for (int kk = 0; kk < 32; kk++) {
+    const float y = x[kk];
+    const float* lrow = LT + (R0 + kk) * TS_LDL + R0;
+#pragma unroll
+    for (int j = 0; j < 32; j++)
+      if (j > kk) x[j] = fmaf(-lrow[j], y, x[j]);
+  }
+#pragma unroll
+  for (int j = 0; j < 32; j++) X[(R0 + j) * TS_LDX + t] = x[j];
+}
+
+__global__ void __launch_bounds__(TS_THREADS) trsm_chunk_f32(float* __restrict__ A, long long ld, int j0, int jb,
+                                                             int c0, int c1) {
+  extern __shared__ __align__(16) float ts_sm[];
+  float* LT = ts_sm;                // LT[k * TS_LDL + i] = l_ik (i > k, i < jb), zero elsewhere
+  float* X = ts_sm + 96 * TS_LDL;  // X[i * TS_LDX + c]
+  const int tid = threadIdx.x;
+  const int cb = c0 + blockIdx.x * TS_COLS;
+  {
+    constexpr int NL = (96 * 96 + TS_THREADS - 1) / TS_THREADS, NX = 96 * TS_COLS / TS_THREADS;
+    float v[NL], w[NX];
+#pragma unroll
+    for (int u = 0; u < NL; u++) {
+      const int e = u * TS_THREADS + tid;
+      const int i = e % 96, k = e / 96;  // down the columns: coalesced reads
       v[u] = (e < 96 * 96 && i < jb && k < i) ? A[static_cast<long long>(j0 + k) * ld + j0 + i] : 0.0f;
     }
 #pragma unroll
-    for (int u = 0; u < 24; u++) {
-      const int e = e0 + u * TC_THREADS + tid;
-      if (e < 96 * 96) L[(e % 96) * TC_LDL + e / 96] = v[u];
-    }
-  }
-  for (int e0 = 0; e0 < 96 * TC_THREADS; e0 += 24 * TC_THREADS) {
-    float v[24];
-#pragma unroll
-    for (int u = 0; u < 24; u++) {
-      const int e = e0 + u * TC_THREADS + tid;
-      const int i = e % 96, c = e / 96;
-      const int col = cb + c;
-      v[u] = (i < jb && col < c1) ? A[static_cast<long long>(col) * ld + j0 + i] : 0.0f;
+    for (int u = 0; u < NX; u++) {
+      const int e = u * TS_THREADS + tid;
+      const int i = e % 96, col = cb + e / 96;
+      w[u] = (i < jb && col < c1) ? A[static_cast<long long>(col) * ld + j0 + i] : 0.0f;
     }
 #pragma unroll
-    for (int u = 0; u < 24; u++) {
-      const int e = e0 + u * TC_THREADS + tid;
-      X[(e % 96) * TC_LDX + e / 96] = v[u];
+    for (int u = 0; u < NL; u++) {
+      const int e = u * TS_THREADS + tid;
+      if (e < 96 * 96) LT[(e / 96) * TS_LDL + e % 96] = v[u];
+    }
+#pragma unroll
+    for (int u = 0; u < NX; u++) {
+      const int e = u * TS_THREADS + tid;
+      X[(e % 96) * TS_LDX + e / 96] = w[u];
     }
   }
   __syncthreads();
-#pragma unroll
-  for (int ch = 0; ch < 3; ch++) {
-    if (ch * 32 >= jb) break;
-    float x[32];
-#pragma unroll
-    for (int j = 0; j < 32; j++) x[j] = X[(ch * 32 + j) * TC_LDX + tid];
-    for (int k = 0; k < ch * 32; k++) {
-      const float y = X[k * TC_LDX + tid];
-      const float* lrow = L + ch * 32 * TC_LDL + k;
-#pragma unroll
-      for (int j = 0; j < 32; j++) x[j] = fmaf(-lrow[j * TC_LDL], y, x[j]);
-    }
-#pragma unroll
-    for (int kk = 0; kk < 32; kk++) {
-      const float y = x[kk];
-      const float* lrow = L + ch * 32 * TC_LDL + ch * 32 + kk;
-#pragma unroll
-      for (int j = 0; j < 32; j++)
-        if (j > kk) x[j] = fmaf(-lrow[j * TC_LDL], y, x[j]);
-    }
-#pragma unroll
-    for (int j = 0; j < 32; j++) X[(ch * 32 + j) * TC_LDX + tid] = x[j];
-  }
+  const int nch = (jb + 31) / 32;
+  if (tid < 128) ts_diag(LT, X, 0, tid);
   __syncthreads();
-  for (int e = tid; e < 96 * TC_THREADS; e += TC_THREADS) {
-    const int i = e % 96, c = e / 96;
+  if (nch > 1) {
+    if (tid < 128)
+      ts_cross(LT, X, 32, 0, 32, tid);
+    else if (tid < 256 && nch > 2)
+      ts_cross(LT, X, 64, 0, 32, tid - 128);
+    __syncthreads();
+    if (tid < 128) ts_diag(LT, X, 32, tid);
+    __syncthreads();
+  }
+  if (nch > 2) {
+    if (tid < 128) ts_cross(LT, X, 64, 32, 64, tid);
+    __syncthreads();
+    if (tid < 128) ts_diag(LT, X, 64, tid);
+    __syncthreads();
+  }
+  // write-back: four consecutive rows of one column per thread and step, as
+  // one 16-byte store where the rows start 16-byte aligned
+  const bool vec = (reinterpret_cast<unsigned long long>(A) & 15) == 0 && (ld & 3) == 0 && (j0 & 3) == 0;
+#pragma unroll
+  for (int q = 0; q < 96 * TS_COLS / 4 / TS_THREADS; q++) {
+    const int e = tid + q * TS_THREADS;
+    const int i = 4 * (e % 24), c = e / 24;
     const int col = cb + c;
-    if (i < jb && col < c1) A[static_cast<long long>(col) * ld + j0 + i] = X[i * TC_LDX + c];
+    if (col < c1 && i < jb) {
+      float* dst = A + static_cast<long long>(col) * ld + j0 + i;
+      const float4 r = make_float4(X[i * TS_LDX + c], X[(i + 1) * TS_LDX + c], X[(i + 2) * TS_LDX + c],
+                                   X[(i + 3) * TS_LDX + c]);
+      if (vec && i + 3 < jb) {
+        *reinterpret_cast<float4*>(dst) = r;
+      } else {
+        dst[0] = r.x;
+        if (i + 1 < jb) dst[1] = r.y;
+        if (i + 2 < jb) dst[2] = r.z;
+        if (i + 3 < jb) dst[3] = r.w;
+      }
+    }
   }
 }
 
@@ -2413,10 +2476,10 @@ static void launch_trsm_chunk(Context* ctx, float* A, long long ld, int j0, int 
   static std::once_flag attr;
   std::call_once(attr, [] {
     cuda_check(cudaFuncSetAttribute(trsm_chunk_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    static_cast<int>(TC_SMEM)),
+                                    static_cast<int>(TS_SMEM)),
                "cudaFuncSetAttribute(trsm)");
   });
-  trsm_chunk_f32<<<blocks(c1 - c0, TC_THREADS), TC_THREADS, TC_SMEM, ctx->stream()>>>(A, ld, j0, jb, c0, c1);
+  trsm_chunk_f32<<<blocks(c1 - c0, TS_COLS), TS_THREADS, TS_SMEM, ctx->stream()>>>(A, ld, j0, jb, c0, c1);
   ctx->launches += 1;
   cuda_check(cudaGetLastError(), "trsm kernel");
 }
