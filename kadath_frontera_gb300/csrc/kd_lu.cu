@@ -1979,7 +1979,7 @@ __global__ void build_swap_map(const int* __restrict__ ipiv, int j0, int jb, int
 // parity: a CTA can only overwrite a slot after every CTA has passed the
 // next cluster barrier, i.e. has finished reading it.
 constexpr int CP_CL = 16;
-constexpr int CP_THREADS = 512;
+constexpr int CP_THREADS = 384;  // 251 rows per CTA and warp-level reductions over 12 warps (512 and 768 were slower)
 constexpr int CP_WARPS = CP_THREADS / 32;
 constexpr size_t CP_MAX_SMEM = 212 * 1024;
 constexpr int CP_IB = 16;  // inner block: columns updated per column step
@@ -2047,11 +2047,59 @@ __device__ __forceinline__ void cp_column_step(float* __restrict__ tile, int S, 
   }
 }
 
+// The per-column exchange of the cluster panel: each CTA's candidate (and the
+// owner's row j) go to every CTA's receive slot by st.async, which completes
+// on that CTA's mbarrier for the slot (its complete-tx has release semantics
+// at cluster scope); a CTA waits on its own mbarrier (acquire at cluster
+// scope), bounded by wait_ns.  False (and *err set) when the wait ran out.
+__device__ __forceinline__ unsigned cp_smem(const void* p) { return static_cast<unsigned>(__cvta_generic_to_shared(p)); }
+__device__ __forceinline__ unsigned cp_mapa(unsigned a, unsigned rank) {
+  unsigned d;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(rank));
+  return d;
+}
+__device__ __forceinline__ void cp_push4(unsigned dst, float4 v, unsigned bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.b32 [%0], {%1, %2, %3, %4}, [%5];" ::"r"(dst),
+               "r"(__float_as_uint(v.x)), "r"(__float_as_uint(v.y)), "r"(__float_as_uint(v.z)),
+               "r"(__float_as_uint(v.w)), "r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void cp_push1(unsigned dst, unsigned v, unsigned bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];" ::"r"(dst), "r"(v), "r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void cp_arm(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(cp_smem(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool cp_wait(unsigned long long* bar, unsigned parity, unsigned long long wait_ns,
+                                        int* err) {
+  const unsigned a = cp_smem(bar);
+  unsigned long long t0 = 0;
+  for (int spin = 0;; spin++) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\tselp.u32 "
+        "%0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (spin == 0) {
+      t0 = globaltimer_ns();
+    } else if ((spin & 15) == 0 && globaltimer_ns() - t0 > wait_ns) {
+      atomicExch(err, 1);
+      return false;
+    }
+  }
+}
+
 __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __restrict__ A, long long ld, int N,
                                                                      int j0, int jb, int per,
                                                                      int* __restrict__ ipiv,
                                                                      int* __restrict__ info,
-                                                                     int* __restrict__ swap_map) {
+                                                                     int* __restrict__ swap_map,
+                                                                     int* __restrict__ err,
+                                                                     unsigned long long wait_ns, unsigned stall) {
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   extern __shared__ __align__(16) unsigned char cp_raw[];
@@ -2063,6 +2111,7 @@ __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __re
   __shared__ __align__(16) float ublk[CP_IB][128];  // rows of the current inner block (L11 | A12 -> U12)
   __shared__ float wv[CP_WARPS];
   __shared__ int wi[CP_WARPS];
+  __shared__ __align__(8) unsigned long long xmb[2];  // the exchange's mbarriers, one per receive slot
   const int S = cp_row_stride(jb);
   const int rank = static_cast<int>(cluster.block_rank());
   const int ncl = static_cast<int>(cluster.num_blocks());  // 2, 4, 8 or 16 CTAs
@@ -2075,7 +2124,19 @@ __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __re
     int k = e / nr, r = e % nr;
     tile[r * S + k] = A[static_cast<long long>(j0 + k) * ld + r0 + r];
   }
-  __syncthreads();
+  // bytes one column's exchange brings to each CTA: every CTA's candidate
+  // (its 16-column segment, value and row) and the owner's segment of row j;
+  // stall_waits asks for bytes that never come
+  const unsigned xbytes = static_cast<unsigned>(ncl) * (4 * 16 + 8) + 4 * 16 + (stall ? 16u : 0u);
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(cp_smem(&xmb[0])) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(cp_smem(&xmb[1])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    cp_arm(&xmb[0], xbytes);
+    cp_arm(&xmb[1], xbytes);
+  }
+  bool dead = false;  // this thread's exchange wait ran out: no more waits
+  cluster.sync();     // every CTA's mbarriers exist before the first push
   for (int b0 = 0; b0 < jb; b0 += CP_IB) {
     const int be = (b0 + CP_IB < jb) ? b0 + CP_IB : jb;
     const int nb = be - b0;
@@ -2122,28 +2183,35 @@ __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __re
         const int crow = (ci < N) ? ci - r0 : 0;  // row 0's words stand in when there is no candidate
         if (ci < N)
           for (int k = lane; k < jb; k += 32) cand_row[slot][k] = tile[crow * S + k];
+        __syncwarp();  // the whole row copy before any lane's (releasing) push
         const float4* src = reinterpret_cast<const float4*>(tile + static_cast<size_t>(crow) * S + b0);
         for (int e = lane; e < 2 * ncl; e += 32) {  // (destination CTA, half of the inner block)
-          CpSlot* R = cluster.map_shared_rank(&recv[slot], e >> 1);
+          const unsigned d = static_cast<unsigned>(e >> 1);
           const int c0 = (e & 1) * 2;
-          R->seg[rank][c0] = src[c0];
-          R->seg[rank][c0 + 1] = src[c0 + 1];
+          const unsigned bar = cp_mapa(cp_smem(&xmb[slot]), d);
+          cp_push4(cp_mapa(cp_smem(&recv[slot].seg[rank][c0]), d), src[c0], bar);
+          cp_push4(cp_mapa(cp_smem(&recv[slot].seg[rank][c0 + 1]), d), src[c0 + 1], bar);
           if ((e & 1) == 0) {
-            R->v[rank] = cv;
-            R->i[rank] = ci;
+            cp_push1(cp_mapa(cp_smem(&recv[slot].v[rank]), d), __float_as_uint(cv), bar);
+            cp_push1(cp_mapa(cp_smem(&recv[slot].i[rank]), d), static_cast<unsigned>(ci), bar);
           }
         }
       } else if (warp == 1 && j >= r0 && j < r1) {
         for (int k = lane; k < jb; k += 32) jrow[slot][k] = tile[(j - r0) * S + k];
+        __syncwarp();
         const float4* src = reinterpret_cast<const float4*>(tile + static_cast<size_t>(j - r0) * S + b0);
         for (int e = lane; e < 2 * ncl; e += 32) {
-          CpSlot* R = cluster.map_shared_rank(&recv[slot], e >> 1);
+          const unsigned d = static_cast<unsigned>(e >> 1);
           const int c0 = (e & 1) * 2;
-          R->jseg[c0] = src[c0];
-          R->jseg[c0 + 1] = src[c0 + 1];
+          const unsigned bar = cp_mapa(cp_smem(&xmb[slot]), d);
+          cp_push4(cp_mapa(cp_smem(&recv[slot].jseg[c0]), d), src[c0], bar);
+          cp_push4(cp_mapa(cp_smem(&recv[slot].jseg[c0 + 1]), d), src[c0 + 1], bar);
         }
       }
-      cluster.sync();
+      // every CTA's push of this column; the slot's next phase is column jj + 2
+      // (its pushes come only after this CTA's own push of column jj + 1)
+      if (!dead) dead = !cp_wait(&xmb[slot], static_cast<unsigned>(jj >> 1) & 1u, wait_ns, err);
+      if (tid == 0 && !dead) cp_arm(&xmb[slot], xbytes);
       // the winner, from this CTA's own receive slot: every warp reduces the
       // candidates across its lanes (same result everywhere)
       float gv = -1.0f;
@@ -2311,7 +2379,7 @@ static bool grid_panel_fits(int rows, int jb, int nsm, size_t elem) {
 // cannot host a 16-CTA cluster (the caller then uses the cooperative grid
 // kernel).
 static bool panel_cluster16(Context* ctx, float* A, long long ld, int N, int j0, int jb, int* ipiv, int* info,
-                            int* swap_map) {
+                            int* swap_map, int* err, unsigned long long wait_ns, unsigned stall) {
   const int rows = N - j0;
   int ncl = 2;
   while (ncl < CP_CL &&
@@ -2357,7 +2425,8 @@ static bool panel_cluster16(Context* ctx, float* A, long long ld, int N, int j0,
   at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  cuda_check(cudaLaunchKernelEx(&cfg, panel_cluster16_kernel, A, ld, N, j0, jb, per, ipiv, info, swap_map),
+  cuda_check(cudaLaunchKernelEx(&cfg, panel_cluster16_kernel, A, ld, N, j0, jb, per, ipiv, info, swap_map, err, wait_ns,
+                                stall),
              "panel cluster kernel");
   ctx->launches += 1;
   return true;
@@ -2450,7 +2519,7 @@ static bool panel_factor(Context* ctx, T* A, long long ld, int N, int j0, int jb
     slots.stall = ctx->stall_waits ? 1u : 0u;
   }
   if constexpr (std::is_same<T, float>::value) {
-    if (panel_cluster16(ctx, A, ld, N, j0, jb, ipiv, info, swap_map)) return true;
+    if (panel_cluster16(ctx, A, ld, N, j0, jb, ipiv, info, swap_map, slots.err, slots.wait_ns, slots.stall)) return true;
   }
   if (panel_grid<T>(ctx, A, ld, N, j0, jb, ipiv, info, nsm < ctx->sms() ? nsm : ctx->sms(), slots)) return false;
   // Panels too tall for the shared memory of the GPU: one 8-CTA cluster
@@ -2803,7 +2872,7 @@ void DenseLU::factor(double* A, long long ld, int N, int mode) {
   cuda_check(cudaStreamSynchronize(ctx_->stream()), "sync panel flag");
   if (perr) {
     cuda_check(cudaMemsetAsync(panel_err_, 0, sizeof(int), ctx_->stream()), "reset panel flag");
-    throw KdError(KD_ERR_TIMEOUT, "panel factorisation: a grid barrier wait ran out");
+    throw KdError(KD_ERR_TIMEOUT, "panel factorisation: a grid barrier wait ran out (or a cluster panel's exchange wait)");
   }
   if (mode == LU_TF32_IR && tf32_gemm_error_flag(ctx_))
     throw KdError(KD_ERR_TIMEOUT, "tensor-core trailing update timed out waiting for its MMAs");

@@ -87,6 +87,38 @@ def test_sweep_barrier_wait_runs_out_and_context_recovers(ctx):
     assert np.linalg.norm(A @ x - b) / np.linalg.norm(b) < 1e-12
 
 
+def test_cluster_panel_exchange_wait_runs_out_and_context_recovers(ctx):
+    """The partial-pivoting panel of the mixed modes runs on a thread-block
+    cluster and exchanges each column's candidates by asynchronous stores
+    that complete on the receivers' mbarriers.  With stall_waits every
+    exchange expects bytes that never come: each wait runs out after the
+    context's limit, the factorisation reports KD_ERR_TIMEOUT, and the same
+    context then factors and solves correctly."""
+    from kadath_frontera_gb300 import KadathError
+    from kadath_frontera_gb300._lib import KD_ERR_TIMEOUT
+    from kadath_frontera_gb300.kadath import DenseLU, KD_LU_TF32_IR
+    n = 900
+    A = make(n, 1e4, 7)
+    b = np.random.default_rng(8).standard_normal(n)
+    lu = DenseLU(ctx)
+    dA = torch.tensor(A.T.copy(), device="cuda")
+    ctx.set_wait_limit(1e-3)
+    ctx.stall_waits(True)
+    try:
+        with pytest.raises(KadathError) as e:
+            lu.factor(dA.data_ptr(), n, n, KD_LU_TF32_IR)
+        assert _status(e) == KD_ERR_TIMEOUT
+    finally:
+        ctx.stall_waits(False)
+        ctx.set_wait_limit(2.0)
+    dA = torch.tensor(A.T.copy(), device="cuda")
+    db = torch.tensor(b, device="cuda")
+    lu.factor(dA.data_ptr(), n, n, KD_LU_TF32_IR)
+    lu.solve(db.data_ptr())
+    x = db.cpu().numpy()
+    assert np.linalg.norm(A @ x - b) / np.linalg.norm(b) < 1e-12
+
+
 def test_refinement_that_cannot_converge_reports_noconv(ctx):
     from kadath_frontera_gb300 import KadathError
     from kadath_frontera_gb300._lib import KD_ERR_NOCONV
