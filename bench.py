@@ -580,7 +580,8 @@ NCU_TRAFFIC_RATIO = {
     "lu_solve": (1.032, "profiles/trsv_chain_star_N12331.md"),
     "lu_gemm": (0.955, "profiles/tf32_update_persistent_star_N12331.md"),
     "lu_panel": (0.51, "profiles/panel_cluster16_kernel_star_N12331.md"),
-    "lu_panel_static": (0.51, "profiles/panel_nopiv_kernel_star_N12331.md"),
+    "lu_panel_static": (0.52, "profiles/panel_nopiv_kernel_star_N12331.md"),
+    "lu_swap_trsm": (0.51, "profiles/trsm_chunk_f32_star_N12331.md"),
 }
 
 
