@@ -266,7 +266,7 @@ __global__ void col_scale_convert_kernel(const double* __restrict__ A, long long
 // the (at most 96 x 96) diagonal block itself in shared memory -- redundant,
 // but it removes every grid-wide synchronisation -- and then solves
 // x U11 = a for NP_THREADS rows of A21, one row per thread with the row in
-// registers.  CTA 0 writes L11 \ U11 back.  A zero or non-finite pivot sets
+// registers.  The last CTA to finish writes L11 \ U11 back.  A zero or non-finite pivot sets
 // *info (the caller then factors with partial pivoting instead).
 constexpr int NP_NB = 96;
 constexpr int NP_LD = NP_NB + 4;  // row stride: 16-byte aligned rows, read four elements at a time by L21
@@ -335,7 +335,8 @@ __device__ __forceinline__ void np_diag_steps(float (&d)[32], float& rp, float* 
 }
 
 __global__ void __launch_bounds__(NP_THREADS) panel_nopiv_kernel(float* __restrict__ A, long long ld, int N, int j0,
-                                                                 int jb, int rpt, int* __restrict__ info) {
+                                                                 int jb, int rpt, int* __restrict__ info,
+                                                                 unsigned* __restrict__ done) {
   __shared__ __align__(16) float U[NP_NB * NP_LD];
   __shared__ float rdiag[NP_NB];
   __shared__ float rpv[NP_NB];  // __frcp_rn of the pivots
@@ -429,11 +430,6 @@ __global__ void __launch_bounds__(NP_THREADS) panel_nopiv_kernel(float* __restri
     rdiag[tid] = 1.0f / d;
   }
   __syncthreads();
-  if (blockIdx.x == 0)
-    for (int e = tid; e < jb * jb; e += NP_THREADS) {
-      const int i = e % jb, k = e / jb;
-      A[static_cast<long long>(j0 + k) * ld + j0 + i] = U[i * NP_LD + k];
-    }
   // L21: x U11 = a for each of this thread's rpt rows (CTA b owns rows
   // j0 + jb + [b rpt NP_THREADS, (b + 1) rpt NP_THREADS)), by 32-column
   // chunks with the chunk in registers: a chunk first takes off the products
@@ -443,7 +439,7 @@ __global__ void __launch_bounds__(NP_THREADS) panel_nopiv_kernel(float* __restri
   extern __shared__ float np_xs[];  // [64][NP_THREADS]
   for (int rr = 0; rr < rpt; rr++) {
   const int row = j0 + jb + (blockIdx.x * rpt + rr) * NP_THREADS + tid;
-  if (row >= N) return;
+  if (row >= N) break;
   float* arow = A + static_cast<long long>(j0) * ld + row;  // element k at arow[k * ld]
 #pragma unroll
   for (int c = 0; c < NP_NB / 32; c++) {
@@ -489,6 +485,25 @@ __global__ void __launch_bounds__(NP_THREADS) panel_nopiv_kernel(float* __restri
       for (int j = 0; j < 32; j++) np_xs[(c * 32 + j) * NP_THREADS + tid] = x[j];
     }
   }
+  }
+  // L11 \ U11 goes back to A only when every CTA has read the diagonal
+  // block: the last CTA to finish writes it (each holds the same factors)
+  // and resets the counter for the next panel.  CTAs need not be resident
+  // together, as they are beside the trailing update on a side stream.
+  __shared__ int np_last;
+  __syncthreads();
+  if (tid == 0) {
+    __threadfence();
+    np_last = (atomicAdd(done, 1u) == gridDim.x - 1) ? 1 : 0;
+    __threadfence();
+  }
+  __syncthreads();
+  if (np_last) {
+    for (int e = tid; e < jb * jb; e += NP_THREADS) {
+      const int i = e % jb, k = e / jb;
+      A[static_cast<long long>(j0 + k) * ld + j0 + i] = U[i * NP_LD + k];
+    }
+    if (tid == 0) *done = 0u;
   }
 }
 
@@ -807,11 +822,12 @@ DenseLU::DenseLU(Context* ctx) : ctx_(ctx) {
   const size_t slot_bytes = sizeof(double) * (2 * 128 * static_cast<size_t>(nsm_) + 2 * nsm_ + 2 * 128) +
                             sizeof(int) * 2 * static_cast<size_t>(nsm_) + 32;
   const size_t map_bytes = sizeof(int) * (1 + 4 * 128) + 60;  // + padding to 16 bytes
-  cuda_check(cudaMalloc(&slot_mem_, slot_bytes + map_bytes + 16), "cudaMalloc(panel slots)");
-  cuda_check(cudaMemsetAsync(slot_mem_, 0, slot_bytes + map_bytes + 16, ctx_->stream()), "memset panel slots");
+  cuda_check(cudaMalloc(&slot_mem_, slot_bytes + map_bytes + 32), "cudaMalloc(panel slots)");
+  cuda_check(cudaMemsetAsync(slot_mem_, 0, slot_bytes + map_bytes + 32, ctx_->stream()), "memset panel slots");
   swap_map_ = reinterpret_cast<int*>(static_cast<char*>(slot_mem_) + slot_bytes);
   tri_bar_ = reinterpret_cast<unsigned*>(static_cast<char*>(slot_mem_) + slot_bytes + map_bytes);
   panel_err_ = reinterpret_cast<int*>(static_cast<char*>(slot_mem_) + slot_bytes - 16);
+  np_done_ = tri_bar_ + 4;
 }
 
 DenseLU::~DenseLU() {
@@ -2699,7 +2715,7 @@ void DenseLU::factor_f32_nopiv(float* A, long long ld, int N, bool tf32) {
       cuda_check(cudaFuncSetAttribute(panel_nopiv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, NP_XS_BYTES),
                  "panel_nopiv smem");
     });
-    panel_nopiv_kernel<<<grid, NP_THREADS, NP_XS_BYTES, ctx_->stream()>>>(A, ld, N, j0, jb, rpt, d_info_);
+    panel_nopiv_kernel<<<grid, NP_THREADS, NP_XS_BYTES, ctx_->stream()>>>(A, ld, N, j0, jb, rpt, d_info_, np_done_);
     ctx_->launches++;
   };
   auto trsm = [&](int j0, int jb, int c0, int c1) {

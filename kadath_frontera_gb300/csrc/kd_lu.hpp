@@ -85,6 +85,7 @@ class DenseLU {
   int* swap_map_ = nullptr;
   int* panel_err_ = nullptr;   // set when a grid barrier wait runs out (panel or sweep)
   unsigned* tri_bar_ = nullptr;  // barrier counters of the two triangular sweeps
+  unsigned* np_done_ = nullptr;  // CTAs of a static panel that have finished (the last one resets it)
   double* eq_buf_ = nullptr;   // row scales, column scales, row maxima (mixed modes)
   size_t eq_cap_ = 0;
   bool scaled_ = false;
