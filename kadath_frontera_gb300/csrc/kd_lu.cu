@@ -3150,7 +3150,7 @@ void DenseLU::gmres_ir(double* b, int trans) {
   double* w = work_ + static_cast<size_t>(N) * (m + 1);
   double* x = w + N;
   double* r = x + N;
-  double* dproj = r + N;  // [0, m+1): round 1, [m+1, 2m+2): round 2, [2m+2]: |w|^2
+  double* dproj = r + N;  // [0, m+1): first pass, [m+1, 2m+2): second pass, [2m+2]: |w|^2
   const int nb = blocks(N, VA_THREADS);
   auto copy_scaled = [&](const double* src, double alpha, double* dst) {
     scaled_copy<<<nb, VA_THREADS, 0, s>>>(N, alpha, src, dst, 0);
