@@ -3130,7 +3130,7 @@ void DenseLU::gemv(const double* x, double* y, double alpha, double beta, const 
 void DenseLU::gmres_ir(double* b, int trans) {
   // Right-preconditioned GMRES(m), M^-1 = the FP32 factors.  The basis is
   // orthogonalised by classical Gram-Schmidt run twice (CGS2): per
-  // iteration two rounds of dot products and one norm on the device, one
+  // iteration two passes of dot products and one norm on the device, one
   // copy of the results to the host; the small Hessenberg least-squares
   // problem is solved on the host.  At most gmres_restarts cycles.  With
   // trans the operator is A^T and the preconditioner M^-T.
@@ -3195,10 +3195,10 @@ void DenseLU::gmres_ir(double* b, int trans) {
         ProfScope ps(ctx_, Context::PROF_GMRES, 8.0 * double(N) * N);
         gemv(r, w, 1.0, 0.0, nullptr, trans);
       }
-      // two rounds of w -= V (V^T w) over v_0 .. v_k, then |w|^2
+      // two passes of w -= V (V^T w) over v_0 .. v_k, then |w|^2
       const int kk = k + 1;
-      for (int round = 0; round < 2; round++) {
-        double* h = dproj + static_cast<size_t>(round) * (m + 1);
+      for (int pass = 0; pass < 2; pass++) {
+        double* h = dproj + static_cast<size_t>(pass) * (m + 1);
         basis_dots<<<kk, VA_THREADS, 0, s>>>(V, N, kk, w, h);
         basis_subtract<<<nb, VA_THREADS, 0, s>>>(V, N, kk, h, w);
         ctx_->launches += 2;
