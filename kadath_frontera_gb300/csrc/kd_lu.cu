@@ -3137,7 +3137,7 @@ void DenseLU::gmres_ir(double* b, int trans) {
   const int N = N_;
   const int m = gmres_max_iter;
   cudaStream_t s = ctx_->stream();
-  const size_t hn_at = 2 * static_cast<size_t>(m + 1);  // projections of both rounds, then |w|^2
+  const size_t hn_at = 2 * static_cast<size_t>(m + 1);  // projections of both passes, then |w|^2
   ensure_work(static_cast<size_t>(N) * (m + 4) + hn_at + 1);
   if (hproj_cap_ < hn_at + 1) {
     if (hproj_) cudaFreeHost(hproj_);
