@@ -2247,7 +2247,10 @@ __global__ void __launch_bounds__(CP_THREADS) panel_cluster16_kernel(float* __re
           tag = ot;
         }
       }
-      if (gi >= N) {  // nothing usable below the diagonal: no swap
+      // nothing usable below the diagonal: no swap.  (A winner is always a
+      // row at or below j; a thread whose exchange wait ran out may read a
+      // stale slot, and the row-move list must still hold rows of the panel.)
+      if (gi < j || gi >= N) {
         gi = j;
         tag = -1;
       }
